@@ -1,0 +1,404 @@
+"""Benchmark of the RPY grand-mobility product (one GB300).
+
+A step is one application of the whole grand mobility -- all four blocks,
+v_segs = Mss f_segs + Msb f_blobs and v_blobs = Mbs f_segs + Mbb f_blobs --
+to the medium swimmer (R = 60a sphere of 2562 blobs carrying 640 filaments x
+20 segments = 12 800 segments; seeded synthetic geometry, N(0,1) forces), in
+the mixed-precision form (FP32 pairs with compensated accumulation, FP64
+inputs/outputs). Printed: one JSON line (rank 0).
+
+  value    matvecs/s with inputs resident in HBM, CUDA events around each step,
+           L2 flushed between steps (outside the events)
+  e2e      matvecs/s through the C-ABI hooks with pinned host buffers: the H2D
+           copies of positions and forces and the D2H copies of velocities are
+           inside the timed region
+  roofline the dominant kernel (the segment-target tile kernel) against the
+           measured FP32 FMA peak
+  fp64     the same product in plain FP64 (the parity drop-in) for comparison
+
+`--impl reference` times the reference's RPY sums on the host cores instead
+(the CPU restatement in oracle/, all threads), on a bounded sample of the
+same workload.
+
+With torchrun (N > 1) every rank runs an independent replica on its own GPU
+(the product of one swimmer is not split across GPUs); value is the total
+over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOPS_66, FLOPS_63, FLOPS_36, FLOPS_33 = 93, 56, 56, 40  # canonical flops per pair
+
+
+def grand_flops(ns, nb):
+    return ns * ns * FLOPS_66 + ns * nb * FLOPS_63 + nb * ns * FLOPS_36 + nb * nb * FLOPS_33
+
+
+def grand_pairs(ns, nb):
+    return (ns + nb) ** 2
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        busy = [s for s in sm if s >= 0.5 * max(sm)] or sm
+        return {"sm_mhz": float(np.median(busy)), "sm_max_mhz": float(max(smax)),
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": float(max(power)) if power else None}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def bench_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from timfilsimmod_gb300 import _native
+    from timfilsimmod_gb300.geometry import make_config
+    from timfilsimmod_gb300.mobility import (RpyMobilitySolver, kernel_launch_count,
+                                             measure_fma_peak)
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    _native.load()  # fails loudly without the library
+
+    sw = make_config(args.config, seed=1234 + rank)
+    ns, nb = sw.num_segs, sw.num_blobs
+    stream = torch.cuda.current_stream()
+
+    def make(precision):
+        s = RpyMobilitySolver(1, sw.nfil, sw.nseg, nb, precision=precision)
+        s.set_stream(stream.cuda_stream)
+        s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
+        return s
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def timed_steps(solver, steps, warmup, timing=False):
+        for _ in range(warmup):
+            solver.apply_grand_mobility()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        if timing:
+            solver.enable_kernel_timing(True)
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        launches0 = kernel_launch_count()
+        for k in range(steps):
+            flush.zero_()  # L2 flush, outside the timed events
+            starts[k].record(stream)
+            solver.apply_grand_mobility()
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        launches = kernel_launch_count() - launches0
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+        ktimes = solver.kernel_timing() if timing else []
+        if timing:
+            solver.enable_kernel_timing(False)
+        return ms, launches, ktimes
+
+    peak32 = measure_fma_peak("fp32c")
+    peak64 = measure_fma_peak("fp64")
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+
+    # --- mixed precision, device resident (value) ---------------------------
+    s32 = make("fp32c")
+    ms32, launches, ktimes = timed_steps(s32, args.steps, args.warmup, timing=True)
+    seg_launches = ktimes[0::2]  # per step: segment-target launch, then blob-target launch
+
+    # --- end to end through the C-ABI hooks, pinned host buffers ----------------
+    s32.f_segs_host[:] = sw.f_segs.ravel()
+    s32.f_blobs_host[:] = sw.f_blobs.ravel()
+    e2e_steps = max(1, args.steps)
+    for _ in range(args.warmup):
+        s32.copy_segment_positions_to_device()
+        s32.copy_segment_forces_to_device()
+        s32.copy_blob_positions_to_device()
+        s32.copy_blob_forces_to_device()
+        s32.apply_grand_mobility()
+        s32.copy_segment_velocities_to_host()
+        s32.copy_blob_velocities_to_host()
+        s32.wait_for_device()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t_e2e = 0.0
+    for _ in range(e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        s32.copy_segment_positions_to_device()
+        s32.copy_segment_forces_to_device()
+        s32.copy_blob_positions_to_device()
+        s32.copy_blob_forces_to_device()
+        s32.apply_grand_mobility()
+        s32.copy_segment_velocities_to_host()
+        s32.copy_blob_velocities_to_host()
+        b.record(stream)
+        s32.wait_for_device()
+        t_e2e += a.elapsed_time(b)
+    v32 = np.concatenate([s32.v_segs_host, s32.v_blobs_host]).copy()
+
+    # --- plain FP64 drop-in, same product ------------------------------------
+    s64 = make("fp64")
+    steps64 = max(3, min(args.steps, 10))
+    ms64, _, ktimes64 = timed_steps(s64, steps64, 1, timing=True)
+    s64.copy_segment_velocities_to_host()
+    s64.copy_blob_velocities_to_host()
+    s64.wait_for_device()
+    v64 = np.concatenate([s64.v_segs_host, s64.v_blobs_host]).copy()
+    clocks = sampler.stop()
+
+    # max over ranks
+    t = torch.tensor([ms32, t_e2e, ms64], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms32, t_e2e, ms64 = t.tolist()
+
+    per_step_ms = ms32 / args.steps
+    value = world * args.steps / (ms32 * 1e-3)
+    e2e_value = world * e2e_steps / (t_e2e * 1e-3)
+    value64 = world * steps64 / (ms64 * 1e-3)
+    seg_flops = ns * ns * FLOPS_66 + ns * nb * FLOPS_63
+    seg_ms = float(np.mean(seg_launches)) if seg_launches else float("nan")
+    achieved = seg_flops / (seg_ms * 1e-3) / 1e12
+    seg64 = ktimes64[0::2]
+    seg64_ms = float(np.mean(seg64)) if seg64 else float("nan")
+    achieved64 = seg_flops / (seg64_ms * 1e-3) / 1e12
+    err = float(np.linalg.norm(v32 - v64) / np.linalg.norm(v64))
+
+    result = None
+    if rank == 0:
+        cpu = cpu_baseline(sw, args.cpu_sample) if not args.no_cpu else None
+        h2d = 8 * (3 * ns + 6 * ns + 3 * nb + 3 * nb)
+        d2h = 8 * (6 * ns + 3 * nb)
+        result = {
+            "metric": "RPY grand-mobility matvecs/s (4 blocks, medium swimmer)",
+            "value": value,
+            "unit": "matvecs/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": per_step_ms,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "fp32 pairs, compensated accumulation; fp64 in/out",
+            "data": "synthetic (seeded icosphere + Fibonacci filaments, N(0,1) forces)",
+            "config": {"workload": f"grand mobility, {args.config} swimmer", "segments": ns,
+                       "blobs": nb, "pairs_per_matvec": grand_pairs(ns, nb),
+                       "l2": "flushed between steps (256 MB write, outside the timed events)",
+                       "parallelism": f"replicas x{world}"},
+            "pair_interactions_per_s": value * grand_pairs(ns, nb),
+            "e2e": {"value": e2e_value, "unit": "matvecs/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "fp32-fma", "kernel": "rpy_tile_kernel<float,6,6,3>",
+                         "achieved": achieved, "peak": peak32 / 1e12, "unit": "TFLOP/s",
+                         "frac": achieved / (peak32 / 1e12),
+                         "peak_source": "measured live (FMA-chain microbenchmark, this run)",
+                         "flops_per_launch": seg_flops, "avg_launch_ms": seg_ms,
+                         "traffic": None},
+            "fp64": {"value": value64, "unit": "matvecs/s", "steps": steps64,
+                     "roofline": {"bound": "fp64-fma", "achieved": achieved64,
+                                  "peak": peak64 / 1e12, "unit": "TFLOP/s",
+                                  "frac": achieved64 / (peak64 / 1e12),
+                                  "avg_launch_ms": seg64_ms}},
+            "speedup_vs_fp64": value / value64,
+            "rel_l2_error_vs_fp64": err,
+            "clocks": clocks,
+            "gpu_launches": launches,
+        }
+        if cpu is not None:
+            result["cpu_baseline"] = cpu
+    for sv in (s32, s64):
+        sv.finalise()
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return result
+
+
+def cpu_baseline(sw, stride: int):
+    """The reference's RPY sums on the host cores (oracle port, all threads):
+    every `stride`-th segment and blob target against all sources, four
+    blocks, extrapolated to a full grand matvec by the pair count."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+
+    threads = os.cpu_count() or 1
+    o = Oracle(threads=threads)
+    xs_t, xb_t = sw.x_segs[::stride], sw.x_blobs[::stride]
+    t0 = time.perf_counter()
+    o.block(6, 6, xs_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
+    o.block(6, 3, xs_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
+    o.block(3, 6, xb_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
+    o.block(3, 3, xb_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
+    dt = time.perf_counter() - t0
+    ns, nb = sw.num_segs, sw.num_blobs
+    pairs = (xs_t.shape[0] + xb_t.shape[0]) * (ns + nb)
+    rate = pairs / dt / grand_pairs(ns, nb)
+    return {"value": rate, "unit": "matvecs/s", "cores": threads, "kind": "port",
+            "sample": f"every {stride}th target of the full grand matvec ({pairs} pairs, "
+                      f"{dt:.2f} s), extrapolated by pair count"}
+
+
+def bench_reference(args):
+    """Reference arm: the reference's RPY sums on the host cores."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return None
+    from timfilsimmod_gb300.geometry import make_config
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+
+    sw = make_config(args.config, seed=1234)
+    threads = os.cpu_count() or 1
+    o = Oracle(threads=threads)
+    stride = args.cpu_sample
+    xs_t, xb_t = sw.x_segs[::stride], sw.x_blobs[::stride]
+    ns, nb = sw.num_segs, sw.num_blobs
+    pairs = (xs_t.shape[0] + xb_t.shape[0]) * (ns + nb)
+
+    def step():
+        o.block(6, 6, xs_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
+        o.block(6, 3, xs_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
+        o.block(3, 6, xb_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
+        o.block(3, 3, xb_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    value = args.steps * pairs / dt / grand_pairs(ns, nb)
+    sample = (f"every {stride}th target of the full grand matvec per step ({pairs} pairs), "
+              f"extrapolated by pair count")
+    return {
+        "impl": "reference",
+        "metric": "RPY grand-mobility matvecs/s (4 blocks, medium swimmer)",
+        "value": value,
+        "unit": "matvecs/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp64",
+        "data": "synthetic (seeded icosphere + Fibonacci filaments, N(0,1) forces)",
+        "config": {"workload": f"grand mobility, {args.config} swimmer", "segments": ns,
+                   "blobs": nb, "pairs_per_matvec": grand_pairs(ns, nb)},
+        "cpu_baseline": {"value": value, "unit": "matvecs/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "matvecs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "the reference's RPY sums (cuda_functions.cu:205-757) restated in C "
+                "(oracle/tfs_oracle.c, pinned bit-close to the reference's own kernels), "
+                "OpenMP over targets on the host cores",
+    }
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--config", default="medium")
+    p.add_argument("--cpu-sample", type=int, default=16,
+                   help="CPU legs use every n-th target of the workload")
+    p.add_argument("--no-cpu", action="store_true")
+    args = p.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    res = bench_reference(args) if args.impl == "reference" else bench_ours(args)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

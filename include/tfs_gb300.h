@@ -1,0 +1,148 @@
+/* tfs_gb300.h -- C ABI of libtfs_gb300.so, the GB300 (sm_103a) implementation
+ * of the reference's RPY mobility path.
+ *
+ * The reference exposes this path as the C++ class `rpy_mobility_solver`
+ * (src/cilia/mobility/rpy_mobility_solver.hpp:15-64), which implements the 17
+ * pure-virtual device hooks of `mobility_solver`
+ * (src/cilia/mobility/mobility_solver.hpp:26-46). Each hook has one entry
+ * point here, taking an opaque solver handle; a replacement
+ * rpy_mobility_solver.cu calls them one to one (INTEGRATION.md shows it).
+ * Host arrays keep the reference's AoS float64 layouts
+ * (rpy_mobility_solver.cu:65-71):
+ *   x_segs[3*Ns]  f_segs[6*Ns] (fx,fy,fz,tx,ty,tz)  v_segs[6*Ns] (vx,vy,vz,wx,wy,wz)
+ *   x_blobs[3*Nb] f_blobs[3*Nb]                      v_blobs[3*Nb]
+ *   f_blobs_repulsion[3*Nb]
+ * with Ns = NSWIM*NFIL*NSEG and Nb = NSWIM*NBLOB.
+ *
+ * Every call returns 0 (TFS_OK) or a negative TFS_E* status; no exception or
+ * abort crosses the ABI. tfs_last_error() gives a message for the calling
+ * thread's most recent failure. Copies and kernels are asynchronous on the
+ * solver's stream; tfs_wait_for_device() is the synchronisation point, as
+ * `wait_for_device` is in the reference (rpy_mobility_solver.cu:247-256).
+ * Host buffers passed to the copy calls must stay valid until then (pinned
+ * memory gives asynchronous copies; pageable memory also works).
+ */
+#ifndef TFS_GB300_H
+#define TFS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TFS_OK 0
+#define TFS_EINVAL (-1)   /* bad argument or size */
+#define TFS_ENOMEM (-2)   /* device allocation failed */
+#define TFS_ECUDA (-3)    /* CUDA runtime error (message has the CUDA text) */
+#define TFS_ENOTCONV (-4) /* iterative solve hit its iteration cap */
+#define TFS_ENAN (-5)     /* non-finite value in a solve */
+#define TFS_ETIMEOUT (-6) /* bounded wait expired */
+#define TFS_ESTATE (-7)   /* call out of order (e.g. data not set) */
+
+/* Arithmetic of the pairwise sums. */
+#define TFS_FP64 0        /* plain FP64 (the parity drop-in) */
+#define TFS_FP32C 1       /* FP32 pairs, compensated (two-sum) accumulation */
+
+typedef struct tfs_solver tfs_solver; /* opaque */
+
+/* Sizes and physical constants. The reference takes these from config.hpp
+ * macros and globals.ini (config.hpp:254-257, cilia_sim_main.cu:56-87);
+ * here they are run-time values. */
+typedef struct tfs_config {
+  int nswim;                 /* swimmers (NSWIM) */
+  int nfil;                  /* filaments per swimmer (NFIL) */
+  int nseg;                  /* segments per filament (NSEG) */
+  int nblob;                 /* blobs per swimmer (NBLOB) */
+  double mu;                 /* viscosity (MU) */
+  double a_seg;              /* segment radius (RSEG) */
+  double a_blob;             /* blob radius (RBLOB) */
+  int end_force_magnitude;   /* device copy of END_FORCE_MAGNITUDE: an int in the
+                                reference (globals.hpp:14, sync_var) */
+  double repulsive_force_factor; /* REPULSIVE_FORCE_FACTOR (config.hpp:404) */
+  int free_body;             /* !PRESCRIBED_BODY_VELOCITIES: barrier forces on blobs */
+  int precision;             /* TFS_FP64 or TFS_FP32C */
+} tfs_config;
+
+/* Fill *cfg with the reference's defaults for the elastic-filament, free-body
+ * RPY configuration (MU = RSEG = RBLOB = 1, REPULSIVE_FORCE_FACTOR = 2,
+ * free body, FP64) and the given sizes. */
+int tfs_config_default(tfs_config *cfg, int nswim, int nfil, int nseg, int nblob);
+
+/* allocate_host_memory + allocate_device_memory
+ * (rpy_mobility_solver.cu:54-117). Uses the current CUDA device. Host arrays
+ * stay owned by the caller. */
+int tfs_solver_create(const tfs_config *cfg, tfs_solver **out);
+/* free_host_memory + free_device_memory (rpy_mobility_solver.cu:14-52). */
+int tfs_solver_destroy(tfs_solver *s);
+
+/* Run the solver's work on `stream` (a cudaStream_t; NULL = the solver's own
+ * non-blocking stream). */
+int tfs_solver_set_stream(tfs_solver *s, void *stream);
+/* Change the pairwise-sum arithmetic (TFS_FP64 / TFS_FP32C). */
+int tfs_solver_set_precision(tfs_solver *s, int precision);
+
+/* Device buffers of the solver (AoS float64), for callers that keep data
+ * resident in HBM instead of going through the host copy hooks. */
+typedef struct tfs_device_buffers {
+  double *x_segs, *f_segs, *v_segs;
+  double *x_blobs, *f_blobs, *v_blobs, *f_blobs_repulsion;
+} tfs_device_buffers;
+int tfs_solver_device_buffers(tfs_solver *s, tfs_device_buffers *out);
+/* Tell the solver that positions in its device buffers were written directly
+ * (the copy hooks do this themselves). */
+int tfs_solver_positions_updated(tfs_solver *s);
+
+/* --- the 17 hooks of mobility_solver.hpp:26-46 ------------------------- */
+int tfs_copy_segment_positions_to_device(tfs_solver *s, const double *x_segs_host);   /* rpy_mobility_solver.cu:119-128 */
+int tfs_copy_segment_forces_to_device(tfs_solver *s, const double *f_segs_host);      /* :130-139 */
+int tfs_copy_blob_positions_to_device(tfs_solver *s, const double *x_blobs_host);     /* :141-150 */
+int tfs_copy_blob_forces_to_device(tfs_solver *s, const double *f_blobs_host);        /* :152-161 */
+int tfs_copy_interparticle_blob_forces_to_host(tfs_solver *s, double *f_blobs_repulsion_host); /* :163-175 */
+int tfs_copy_blob_velocities_to_host(tfs_solver *s, double *v_blobs_host);           /* :177-189 */
+int tfs_copy_segment_velocities_to_host(tfs_solver *s, double *v_segs_host);         /* :191-205 */
+/* barrier_forces: adds segment repulsion into the device f_segs and writes
+ * the blob repulsion (free body) (rpy_mobility_solver.cu:207-245,
+ * cuda_functions.cu:1240-1436). */
+int tfs_apply_interparticle_forces(tfs_solver *s);
+int tfs_wait_for_device(tfs_solver *s);                                              /* :247-256 */
+int tfs_evaluate_segment_segment_mobility(tfs_solver *s); /* v_segs  = Mss f_segs  (:258-274, cuda_functions.cu:362-474) */
+int tfs_evaluate_segment_blob_mobility(tfs_solver *s);    /* v_segs += Msb f_blobs (:276-292, :551-636) */
+int tfs_evaluate_blob_blob_mobility(tfs_solver *s);       /* v_blobs = Mbb f_blobs (:294-310, :476-549) */
+int tfs_evaluate_blob_segment_mobility(tfs_solver *s);    /* v_blobs = Mbs f_segs  (:312-328, :638-757) */
+/* evaluate_full_mobility (rpy_mobility_solver.cu:330-337): Mss + Msb into
+ * v_segs and Mbb, then Mbs into v_blobs -- the reference's sequence assigns
+ * v_blobs twice, so v_blobs ends as Mbs f_segs; this entry reproduces that.
+ * Segment and blob velocities are copied to the given host arrays when they
+ * are non-NULL. */
+int tfs_evaluate_full_mobility(tfs_solver *s, double *v_segs_host, double *v_blobs_host);
+
+/* --- fused forms (no reference counterpart; same arithmetic) ------------ */
+/* One launch per target kind: v_segs = Mss f_segs + Msb f_blobs and
+ * v_blobs = Mbs f_segs + Mbb f_blobs, i.e. the whole grand mobility applied
+ * to [f_segs; f_blobs]. */
+int tfs_apply_grand_mobility(tfs_solver *s);
+
+/* --- diagnostics ------------------------------------------------------- */
+/* CUDA-event timing of the solver's RPY tile kernels (the dominant kernels;
+ * pack and reduce kernels excluded), on the solver's stream. Enabling resets
+ * the record. tfs_solver_kernel_timing synchronises the stream, writes the
+ * duration in ms of each timed launch since the last query, in launch order,
+ * into ms[0..capacity), sets *launches to the number recorded, and resets.
+ * At most 4096 launches are recorded between two queries. */
+int tfs_solver_enable_kernel_timing(tfs_solver *s, int enable);
+int tfs_solver_kernel_timing(tfs_solver *s, double *ms, int capacity, int *launches);
+/* Message of the calling thread's last failed call ("" if none). */
+const char *tfs_last_error(void);
+/* Number of this library's kernels launched since load (all solvers). */
+long long tfs_kernel_launch_count(void);
+/* Measured FMA throughput of the current device in FLOP/s (2 per FMA),
+ * precision TFS_FP64 or TFS_FP32C (plain FP32 FMAs), from a dependent-chain
+ * microbenchmark over every SM. */
+int tfs_measure_fma_peak(int precision, double *flops_per_second);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TFS_GB300_H */

@@ -1,0 +1,217 @@
+"""ctypes bindings for the CPU oracle (test infrastructure only).
+
+`Oracle` wraps liboracle.so, the C restatement of the reference's RPY path
+(tfs_oracle.c). `ReferenceKernels` wraps oracle/_ref/libref_kernels_*.so, the
+reference's own cuda_functions.cu compiled unchanged for the CPU, which exists
+only where the reference tree was present at build time.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module; the product package never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+
+_P = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_P)
+
+
+def build_oracle(quiet: bool = True) -> str:
+    """Compile liboracle.so with make (gcc; seconds)."""
+    out = subprocess.run(["make", "-C", HERE, "liboracle.so"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    return os.path.join(HERE, "liboracle.so")
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("mu", ctypes.c_double), ("a_seg", ctypes.c_double), ("a_blob", ctypes.c_double)]
+
+
+class Oracle:
+    """FP64 CPU restatement of the reference's mobility blocks, barrier forces
+    and flow field. Inputs/outputs are the reference's AoS float64 arrays."""
+
+    def __init__(self, mu: float = 1.0, a_seg: float = 1.0, a_blob: float = 1.0, threads: int = 1):
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build_oracle()
+        self.lib = ctypes.CDLL(path)
+        self.p = _Params(mu, a_seg, a_blob)
+        self.set_threads(threads)
+
+    def set_threads(self, n: int) -> None:
+        self.lib.orc_set_threads(int(n))
+        self.threads = self.lib.orc_get_threads()
+
+    def mss(self, x_segs, f_segs):
+        x, f = _c(x_segs), _c(f_segs)
+        ns = x.size // 3
+        v = np.zeros(6 * ns)
+        self.lib.orc_mss(ctypes.byref(self.p), _ptr(v), _ptr(f), _ptr(x), ns)
+        return v
+
+    def msb(self, x_segs, x_blobs, f_blobs, v_segs=None):
+        xs, xb, fb = _c(x_segs), _c(x_blobs), _c(f_blobs)
+        ns, nb = xs.size // 3, xb.size // 3
+        v = np.zeros(6 * ns) if v_segs is None else np.array(v_segs, dtype=np.float64).ravel()
+        self.lib.orc_msb(ctypes.byref(self.p), _ptr(v), _ptr(fb), _ptr(xs), _ptr(xb), ns, nb)
+        return v
+
+    def mbb(self, x_blobs, f_blobs):
+        x, f = _c(x_blobs), _c(f_blobs)
+        nb = x.size // 3
+        v = np.zeros(3 * nb)
+        self.lib.orc_mbb(ctypes.byref(self.p), _ptr(v), _ptr(f), _ptr(x), nb)
+        return v
+
+    def mbs(self, x_blobs, x_segs, f_segs):
+        xb, xs, fs = _c(x_blobs), _c(x_segs), _c(f_segs)
+        nb, ns = xb.size // 3, xs.size // 3
+        v = np.zeros(3 * nb)
+        self.lib.orc_mbs(ctypes.byref(self.p), _ptr(v), _ptr(fs), _ptr(xb), _ptr(xs), nb, ns)
+        return v
+
+    def full(self, x_segs, f_segs, x_blobs, f_blobs):
+        """All four blocks, in the order of rpy_mobility_solver.cu:330-337."""
+        v_segs = self.mss(x_segs, f_segs)
+        v_segs = self.msb(x_segs, x_blobs, f_blobs, v_segs)
+        v_blobs = self.mbb(x_blobs, f_blobs)
+        v_bs = self.mbs(x_blobs, x_segs, f_segs)
+        return v_segs, v_blobs, v_bs
+
+    def block(self, vd, fd, x_tgt, a_tgt, x_src, f_src, a_src, v=None):
+        """General block (orc_rpy_block); v given = accumulate into it."""
+        xt, xs, fs = _c(x_tgt), _c(x_src), _c(f_src)
+        nt, ns = xt.size // 3, xs.size // 3
+        acc = v is not None
+        out = np.array(v, dtype=np.float64).ravel() if acc else np.zeros(vd * nt)
+        self.lib.orc_rpy_block(ctypes.byref(self.p), int(vd), int(fd), _ptr(out), _ptr(xt), nt,
+                               ctypes.c_double(a_tgt), _ptr(xs), _ptr(fs), ns,
+                               ctypes.c_double(a_src), int(acc))
+        return out
+
+    def barrier_forces(self, x_segs, x_blobs, f_segs, nseg, end_force_magnitude: int,
+                       repulsive_force_factor=2.0, free_body=True):
+        xs, xb = _c(x_segs), _c(x_blobs)
+        fs = np.array(f_segs, dtype=np.float64).ravel().copy()
+        ns, nb = xs.size // 3, xb.size // 3
+        frep = np.zeros(3 * nb)
+        self.lib.orc_barrier_forces(ctypes.byref(self.p), _ptr(fs), _ptr(frep), _ptr(xs),
+                                    _ptr(xb), ns, nb, int(nseg), int(end_force_magnitude),
+                                    ctypes.c_double(repulsive_force_factor), int(bool(free_body)))
+        return fs, frep
+
+    def flow_velocities(self, x_flow, x_segs, f_segs, segs_per_body, x_blobs, f_blobs,
+                        blobs_per_body, x_bodies, prefac, remove_net_force=False):
+        xf, xs, fs = _c(x_flow), _c(x_segs), _c(f_segs)
+        xb = _c(x_blobs) if blobs_per_body else np.zeros(3)
+        fb = _c(f_blobs) if blobs_per_body else np.zeros(3)
+        xbod = _c(x_bodies)
+        nf = xf.size // 3
+        nbod = xbod.size // 3
+        v = np.zeros(3 * nf)
+        self.lib.orc_flow_velocities(_ptr(v), _ptr(xf), nf, _ptr(fs), _ptr(xs), int(segs_per_body),
+                                     _ptr(fb), _ptr(xb), int(blobs_per_body), _ptr(xbod), nbod,
+                                     ctypes.c_double(prefac), int(bool(remove_net_force)))
+        return v
+
+
+def _c(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).ravel())
+
+
+class ReferenceKernels:
+    """The reference's own kernels (cuda_functions.cu), compiled unchanged for
+    the CPU by `make -C oracle ref`. `variant` is "a1" (RSEG = RBLOB = 1) or
+    "a16" (RSEG = 1, RBLOB = 1.6)."""
+
+    def __init__(self, variant: str = "a1"):
+        path = os.path.join(REF_DIR, f"libref_kernels_{variant}.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+        for name in ("ref_rseg", "ref_rblob", "ref_mu"):
+            getattr(self.lib, name).restype = ctypes.c_double
+        self.a_seg = self.lib.ref_rseg()
+        self.a_blob = self.lib.ref_rblob()
+        self.mu = self.lib.ref_mu()
+
+    @staticmethod
+    def available(variant: str = "a1") -> bool:
+        return os.path.exists(os.path.join(REF_DIR, f"libref_kernels_{variant}.so"))
+
+    def sync(self, nswim, nseg, nfil, nblob, end_force_magnitude=0, seg_sep=2.2):
+        self.lib.ref_sync_var(int(nswim), int(nseg), int(nfil), int(nblob),
+                              int(end_force_magnitude), ctypes.c_double(seg_sep))
+
+    def mss(self, x_segs, f_segs):
+        x, f = _c(x_segs), _c(f_segs)
+        v = np.zeros(f.size)
+        self.lib.ref_mss(_ptr(v), _ptr(f), _ptr(x), x.size // 3)
+        return v
+
+    def msb(self, x_segs, x_blobs, f_blobs, v_segs=None):
+        xs, xb, fb = _c(x_segs), _c(x_blobs), _c(f_blobs)
+        v = np.zeros(2 * xs.size) if v_segs is None else np.array(v_segs, dtype=np.float64).ravel()
+        self.lib.ref_msb(_ptr(v), _ptr(fb), _ptr(xs), _ptr(xb), xs.size // 3)
+        return v
+
+    def mbb(self, x_blobs, f_blobs):
+        x, f = _c(x_blobs), _c(f_blobs)
+        v = np.zeros(x.size)
+        self.lib.ref_mbb(_ptr(v), _ptr(f), _ptr(x), x.size // 3)
+        return v
+
+    def mbs(self, x_blobs, x_segs, f_segs):
+        xb, xs, fs = _c(x_blobs), _c(x_segs), _c(f_segs)
+        v = np.zeros(xb.size)
+        self.lib.ref_mbs(_ptr(v), _ptr(fs), _ptr(xb), _ptr(xs), xb.size // 3)
+        return v
+
+    def barrier_forces(self, x_segs, x_blobs, f_segs):
+        xs, xb = _c(x_segs), _c(x_blobs)
+        fs = np.array(f_segs, dtype=np.float64).ravel().copy()
+        frep = np.zeros(xb.size)
+        self.lib.ref_barrier_forces(_ptr(fs), _ptr(frep), _ptr(xs), _ptr(xb), xs.size // 3,
+                                    xb.size // 3)
+        return fs, frep
+
+
+class ReferenceFlow:
+    """The reference's flow_velocities kernel (flow_field_evaluator.cu:13-228),
+    compiled unchanged for the CPU by `make -C oracle ref`."""
+
+    def __init__(self):
+        path = os.path.join(REF_DIR, "libref_flow.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(os.path.join(REF_DIR, "libref_flow.so"))
+
+    def flow_velocities(self, x_flow, x_segs, f_segs, segs_per_body, x_blobs, f_blobs,
+                        blobs_per_body, x_bodies, prefac, remove_net_force=False):
+        xf, xs, fs = _c(x_flow), _c(x_segs), _c(f_segs)
+        xb = _c(x_blobs) if blobs_per_body else np.zeros(3)
+        fb = _c(f_blobs) if blobs_per_body else np.zeros(3)
+        xbod = _c(x_bodies)
+        v = np.zeros(xf.size)
+        self.lib.ref_flow_velocities(_ptr(v), _ptr(xf), _ptr(fs), _ptr(fb), _ptr(xs), _ptr(xbod),
+                                     _ptr(xb), xf.size // 3, int(segs_per_body), xbod.size // 3,
+                                     int(blobs_per_body), ctypes.c_double(prefac),
+                                     int(bool(remove_net_force)))
+        return v

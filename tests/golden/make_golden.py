@@ -1,0 +1,133 @@
+"""Generate the golden vectors in tests/golden/ from the reference itself.
+
+The outputs come from the reference's own kernels (src/cilia/cuda_functions.cu
+and the flow_velocities kernel of src/flow_field/flow_field_evaluator.cu),
+compiled unchanged for the CPU by `make -C oracle ref` (see oracle/Makefile).
+That needs the reference tree, so this script runs only where it is present;
+the .npz files it writes are committed and travel with the tests.
+
+    make -C oracle ref && python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from oracle import ReferenceFlow, ReferenceKernels  # noqa: E402
+
+from timfilsimmod_gb300.geometry import make_config  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+END_FORCE = 100      # integer device copy of END_FORCE_MAGNITUDE (globals.hpp:14)
+REPULSIVE = 2.0      # REPULSIVE_FORCE_FACTOR for elastic cilia (config.hpp:404)
+
+
+def run_blocks(ref: ReferenceKernels, xs, fs, xb, fb, nseg, nfil):
+    ref.sync(1, nseg, nfil, xb.shape[0], END_FORCE, 2.2)
+    out = dict(
+        v_mss=ref.mss(xs, fs),
+        v_msb=ref.msb(xs, xb, fb),             # accumulates onto zeros
+        v_mbb=ref.mbb(xb, fb),
+        v_mbs=ref.mbs(xb, xs, fs),
+    )
+    fsb, frep = ref.barrier_forces(xs, xb, fs)
+    out.update(f_segs_barrier=fsb, f_blobs_repulsion=frep)
+    return out
+
+
+def case_small():
+    """The small swimmer (R = 20, 642 blobs, 32 x 20 segments), seed 1, with
+    three segments pushed into the barrier range of others."""
+    sw = make_config("small", seed=1)
+    xs = sw.x_segs.copy()
+    xs[45] = xs[230] + np.array([0.9, 1.2, 0.3])     # inter-filament contact
+    xs[101] = xs[103] + np.array([0.0, 0.5, 1.5])    # same filament, two apart
+    xb = sw.x_blobs.copy()
+    xb[17] = xs[0] + np.array([1.1, -0.9, 0.4])      # segment-blob contact
+    ref = ReferenceKernels("a1")
+    out = run_blocks(ref, xs, sw.f_segs, xb, sw.f_blobs, sw.nseg, sw.nfil)
+    return dict(x_segs=xs, f_segs=sw.f_segs, x_blobs=xb, f_blobs=sw.f_blobs, nseg=sw.nseg,
+                nfil=sw.nfil, a_seg=ref.a_seg, a_blob=ref.a_blob, mu=ref.mu,
+                end_force_magnitude=END_FORCE, repulsive_force_factor=REPULSIVE, **out)
+
+
+def case_overlap():
+    """Ragged sizes (77 segments of 7 per filament, 45 blobs), unequal radii
+    (RSEG 1, RBLOB 1.6), particles packed so that every branch of the RPY pair
+    function is taken: far, overlapping, nested, and self (r = 0)."""
+    rng = np.random.default_rng(7)
+    xs = rng.uniform(-4.0, 4.0, size=(77, 3))
+    xb = rng.uniform(-4.0, 4.0, size=(45, 3))
+    xb[:10] = xs[:10] + rng.normal(0.0, 0.25, size=(10, 3))  # nested (r < 0.6)
+    xb[10:20] = xs[10:20] + rng.normal(0.0, 1.2, size=(10, 3))  # overlapping
+    xs[30] = xs[31] + np.array([0.3, 0.2, -0.1])
+    fs = rng.normal(size=(77, 6))
+    fb = rng.normal(size=(45, 3))
+    ref = ReferenceKernels("a16")
+    out = run_blocks(ref, xs, fs, xb, fb, 7, 11)
+    return dict(x_segs=xs, f_segs=fs, x_blobs=xb, f_blobs=fb, nseg=7, nfil=11,
+                a_seg=ref.a_seg, a_blob=ref.a_blob, mu=ref.mu, end_force_magnitude=END_FORCE,
+                repulsive_force_factor=REPULSIVE, **out)
+
+
+def case_tiny():
+    """One segment, one blob; and 65 segments (one past a 64-thread tile)
+    with 3 blobs."""
+    rng = np.random.default_rng(11)
+    ref = ReferenceKernels("a1")
+    res = {}
+    for tag, ns, nb, nseg in (("one", 1, 1, 1), ("tile", 65, 3, 5)):
+        xs = rng.uniform(-10, 10, size=(ns, 3))
+        xb = rng.uniform(-10, 10, size=(nb, 3))
+        fs = rng.normal(size=(ns, 6))
+        fb = rng.normal(size=(nb, 3))
+        out = run_blocks(ref, xs, fs, xb, fb, nseg, ns // nseg)
+        res.update({f"{tag}_{k}": v for k, v in
+                    dict(x_segs=xs, f_segs=fs, x_blobs=xb, f_blobs=fb, nseg=nseg, **out).items()})
+    res.update(a_seg=ref.a_seg, a_blob=ref.a_blob, mu=ref.mu, end_force_magnitude=END_FORCE,
+               repulsive_force_factor=REPULSIVE)
+    return res
+
+
+def case_flow():
+    """Flow field of the small swimmer at 333 points, with blobs (free space)
+    with and without the net-force Stokeslet removed, and with no blobs (the
+    Blakelet wall form)."""
+    sw = make_config("small", seed=2)
+    rng = np.random.default_rng(13)
+    xf = rng.uniform(-70.0, 70.0, size=(333, 3))
+    xf[:, 2] = np.abs(xf[:, 2]) + 1.0   # above the z = 0 wall for the Blakelet case
+    xbod = np.zeros((1, 3))
+    prefac = 1.0 / (8.0 * np.pi * 1.0)
+    flow = ReferenceFlow()
+    res = dict(x_flow=xf, x_segs=sw.x_segs, f_segs=sw.f_segs, x_blobs=sw.x_blobs,
+               f_blobs=sw.f_blobs, x_bodies=xbod, prefac=prefac)
+    # the wall case lifts the swimmer above z = 0
+    lift = np.array([0.0, 0.0, 90.0])
+    res["x_segs_wall"] = sw.x_segs + lift
+    res["v_blobs"] = flow.flow_velocities(xf, sw.x_segs, sw.f_segs, sw.num_segs, sw.x_blobs,
+                                          sw.f_blobs, sw.num_blobs, xbod, prefac, False)
+    res["v_blobs_rnf"] = flow.flow_velocities(xf, sw.x_segs, sw.f_segs, sw.num_segs, sw.x_blobs,
+                                              sw.f_blobs, sw.num_blobs, xbod, prefac, True)
+    res["v_wall"] = flow.flow_velocities(xf, res["x_segs_wall"], sw.f_segs, sw.num_segs,
+                                         sw.x_blobs, sw.f_blobs, 0, xbod + lift, prefac, False)
+    return res
+
+
+def main():
+    for name, fn in (("small_matvec", case_small), ("overlap_a16", case_overlap),
+                     ("tiny", case_tiny), ("flow_small", case_flow)):
+        data = fn()
+        path = os.path.join(OUT, f"{name}.npz")
+        np.savez_compressed(path, **{k: np.asarray(v) for k, v in data.items()})
+        print(f"wrote {path} ({os.path.getsize(path)} bytes)")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+"""GPU parity of libtfs_gb300.so, called through its C ABI (ctypes), against
+the reference's own outputs (golden vectors) and the CPU oracle.
+
+Tolerances:
+  FP64 (TFS_FP64):   max-abs error <= 1e-12 x max-abs reference value
+  FP32C (TFS_FP32C): ||v - v_ref||_2 <= 2e-5 ||v_ref||_2
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import Oracle
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+TOL64 = 1e-12
+TOL32 = 2e-5
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_max(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def rel_l2(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, f"{name}.npz"))
+
+
+def make_solver(ns, nb, nseg, precision="fp64", **kw):
+    from timfilsimmod_gb300.mobility import RpyMobilitySolver
+
+    assert ns % nseg == 0
+    return RpyMobilitySolver(1, ns // nseg, nseg, nb, precision=precision, **kw)
+
+
+def run_blocks(solver, xs, fs, xb, fb):
+    """Each hook on its own, in the reference's order, returning host copies."""
+    out = {}
+    solver.set_state(xs, fs, xb, fb)
+    solver.evaluate_segment_segment_mobility()
+    solver.copy_segment_velocities_to_host()
+    solver.wait_for_device()
+    out["v_mss"] = solver.v_segs_host.copy()
+    solver.evaluate_blob_blob_mobility()
+    solver.copy_blob_velocities_to_host()
+    solver.wait_for_device()
+    out["v_mbb"] = solver.v_blobs_host.copy()
+    solver.evaluate_blob_segment_mobility()
+    solver.copy_blob_velocities_to_host()
+    solver.wait_for_device()
+    out["v_mbs"] = solver.v_blobs_host.copy()
+    # Msb accumulates (cuda_functions.cu:625-630): start from Mss, subtract
+    solver.evaluate_segment_segment_mobility()
+    solver.evaluate_segment_blob_mobility()
+    solver.copy_segment_velocities_to_host()
+    solver.wait_for_device()
+    out["v_mss_plus_msb"] = solver.v_segs_host.copy()
+    return out
+
+
+@pytest.mark.parametrize("case", ["small_matvec", "overlap_a16"])
+def test_blocks_fp64_match_reference(case):
+    d = load(case)
+    xs, fs, xb, fb = d["x_segs"], d["f_segs"], d["x_blobs"], d["f_blobs"]
+    s = make_solver(xs.shape[0], xb.shape[0], int(d["nseg"]), a_seg=float(d["a_seg"]),
+                    a_blob=float(d["a_blob"]), mu=float(d["mu"]))
+    out = run_blocks(s, xs, fs, xb, fb)
+    s.finalise()
+    assert rel_max(out["v_mss"], d["v_mss"]) < TOL64
+    assert rel_max(out["v_mbb"], d["v_mbb"]) < TOL64
+    assert rel_max(out["v_mbs"], d["v_mbs"]) < TOL64
+    assert rel_max(out["v_mss_plus_msb"], d["v_mss"] + d["v_msb"]) < TOL64
+
+
+@pytest.mark.parametrize("tag", ["one", "tile"])
+def test_tiny_and_ragged_fp64(tag):
+    d = load("tiny")
+    g = {k[len(tag) + 1:]: d[k] for k in d.files if k.startswith(tag + "_")}
+    xs, fs, xb, fb = g["x_segs"], g["f_segs"], g["x_blobs"], g["f_blobs"]
+    s = make_solver(xs.shape[0], xb.shape[0], int(g["nseg"]))
+    out = run_blocks(s, xs, fs, xb, fb)
+    s.apply_interparticle_forces()
+    s.wait_for_device()
+    s.finalise()
+    assert rel_max(out["v_mss"], g["v_mss"]) < TOL64
+    assert rel_max(out["v_mbb"], g["v_mbb"]) < TOL64
+    assert rel_max(out["v_mbs"], g["v_mbs"]) < TOL64
+    assert rel_max(out["v_mss_plus_msb"], g["v_mss"] + g["v_msb"]) < TOL64
+
+
+@pytest.mark.parametrize("case", ["small_matvec", "overlap_a16"])
+def test_barrier_forces_match_reference(case):
+    import torch
+
+    d = load(case)
+    xs, fs, xb, fb = d["x_segs"], d["f_segs"], d["x_blobs"], d["f_blobs"]
+    s = make_solver(xs.shape[0], xb.shape[0], int(d["nseg"]), a_seg=float(d["a_seg"]),
+                    a_blob=float(d["a_blob"]), end_force_magnitude=int(d["end_force_magnitude"]),
+                    repulsive_force_factor=float(d["repulsive_force_factor"]))
+    s.set_state(xs, fs, xb, fb)
+    s.apply_interparticle_forces()
+    s.copy_interparticle_blob_forces_to_host()
+    s.wait_for_device()
+    f_dev = torch.as_tensor(s.device_arrays()["f_segs"], device="cuda").cpu().numpy()
+    frep = s.f_blobs_repulsion_host.copy()
+    s.finalise()
+    assert rel_max(f_dev, d["f_segs_barrier"]) < TOL64
+    assert rel_max(frep, d["f_blobs_repulsion"]) < TOL64
+
+
+def test_full_mobility_hook_semantics():
+    """evaluate_full_mobility leaves v_blobs = Mbs f_segs (rpy_mobility_solver.cu:330-337)."""
+    d = load("small_matvec")
+    xs, fs, xb, fb = d["x_segs"], d["f_segs"], d["x_blobs"], d["f_blobs"]
+    s = make_solver(xs.shape[0], xb.shape[0], int(d["nseg"]))
+    s.set_state(xs, fs, xb, fb)
+    s.evaluate_full_mobility()
+    s.wait_for_device()
+    vs, vb = s.v_segs_host.copy(), s.v_blobs_host.copy()
+    s.finalise()
+    assert rel_max(vs, d["v_mss"] + d["v_msb"]) < TOL64
+    assert rel_max(vb, d["v_mbs"]) < TOL64
+
+
+@pytest.mark.parametrize("case", ["small_matvec", "overlap_a16"])
+def test_blocks_fp32c_error_bound(case):
+    d = load(case)
+    xs, fs, xb, fb = d["x_segs"], d["f_segs"], d["x_blobs"], d["f_blobs"]
+    s = make_solver(xs.shape[0], xb.shape[0], int(d["nseg"]), precision="fp32c",
+                    a_seg=float(d["a_seg"]), a_blob=float(d["a_blob"]))
+    out = run_blocks(s, xs, fs, xb, fb)
+    s.finalise()
+    errs = {k: rel_l2(out[k], d[k]) for k in ("v_mss", "v_mbb", "v_mbs")}
+    errs["v_mss_plus_msb"] = rel_l2(out["v_mss_plus_msb"], d["v_mss"] + d["v_msb"])
+    print("fp32c relative L2 errors", errs)
+    assert max(errs.values()) < TOL32, errs
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_grand_mobility_medium_vs_oracle(precision):
+    """The whole grand mobility of the medium swimmer (12 800 segments, 2562
+    blobs) against the oracle."""
+    from timfilsimmod_gb300.geometry import make_config
+
+    sw = make_config("medium", seed=5)
+    s = make_solver(sw.num_segs, sw.num_blobs, sw.nseg, precision=precision)
+    s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
+    s.apply_grand_mobility()
+    s.copy_segment_velocities_to_host()
+    s.copy_blob_velocities_to_host()
+    s.wait_for_device()
+    vs, vb = s.v_segs_host.copy(), s.v_blobs_host.copy()
+    s.finalise()
+    o = Oracle(threads=os.cpu_count() or 1)
+    ref_s = o.msb(sw.x_segs, sw.x_blobs, sw.f_blobs, o.mss(sw.x_segs, sw.f_segs))
+    ref_b = o.mbs(sw.x_blobs, sw.x_segs, sw.f_segs) + o.mbb(sw.x_blobs, sw.f_blobs)
+    if precision == "fp64":
+        assert rel_max(vs, ref_s) < TOL64 and rel_max(vb, ref_b) < TOL64
+    else:
+        es, eb = rel_l2(vs, ref_s), rel_l2(vb, ref_b)
+        print("fp32c medium errors", es, eb)
+        assert es < TOL32 and eb < TOL32
+
+
+def _grand(s, fs, fb):
+    s.f_segs_host[:] = fs
+    s.f_blobs_host[:] = fb
+    s.copy_segment_forces_to_device()
+    s.copy_blob_forces_to_device()
+    s.apply_grand_mobility()
+    s.copy_segment_velocities_to_host()
+    s.copy_blob_velocities_to_host()
+    s.wait_for_device()
+    return np.concatenate([s.v_segs_host, s.v_blobs_host])
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("fp32c", 2e-5)])
+def test_large_swimmer_symmetry_and_linearity(precision, tol):
+    """Size-independent properties at the full large size (80 000 segments,
+    10 242 blobs): the grand mobility is symmetric (u.Mw = w.Mu) and linear."""
+    from timfilsimmod_gb300.geometry import make_config
+
+    sw = make_config("large", seed=6)
+    rng = np.random.default_rng(8)
+    s = make_solver(sw.num_segs, sw.num_blobs, sw.nseg, precision=precision)
+    s.x_segs_host[:] = sw.x_segs.ravel()
+    s.x_blobs_host[:] = sw.x_blobs.ravel()
+    s.copy_segment_positions_to_device()
+    s.copy_blob_positions_to_device()
+    ns, nb = 6 * sw.num_segs, 3 * sw.num_blobs
+    u = rng.normal(size=ns + nb)
+    w = rng.normal(size=ns + nb)
+    Mu = _grand(s, u[:ns], u[ns:])
+    Mw = _grand(s, w[:ns], w[ns:])
+    M2u = _grand(s, 2.5 * u[:ns], 2.5 * u[ns:])
+    s.finalise()
+    a, b = np.dot(w, Mu), np.dot(u, Mw)
+    assert abs(a - b) <= tol * np.linalg.norm(w) * np.linalg.norm(Mu)
+    assert rel_l2(M2u, 2.5 * Mu) < tol
+
+
+def test_native_library_is_loaded_and_counts_launches():
+    from timfilsimmod_gb300 import _native
+    from timfilsimmod_gb300.mobility import kernel_launch_count
+
+    before = kernel_launch_count()
+    d = load("tiny")
+    s = make_solver(65, 3, 5)
+    s.set_state(d["tile_x_segs"], d["tile_f_segs"], d["tile_x_blobs"], d["tile_f_blobs"])
+    s.evaluate_segment_segment_mobility()
+    s.wait_for_device()
+    s.finalise()
+    assert kernel_launch_count() > before
+    maps = open("/proc/self/maps").read()
+    assert os.path.basename(_native.lib_path()) in maps

@@ -1,0 +1,121 @@
+"""ctypes binding of libtfs_gb300.so (the C ABI in include/tfs_gb300.h).
+
+There is no CPU fallback: if the library is missing or does not load, every
+entry point raises. Build it with `python -m timfilsimmod_gb300.build` or
+`__graft_entry__.build()`.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+TFS_OK = 0
+TFS_EINVAL = -1
+TFS_ENOMEM = -2
+TFS_ECUDA = -3
+TFS_ENOTCONV = -4
+TFS_ENAN = -5
+TFS_ETIMEOUT = -6
+TFS_ESTATE = -7
+
+TFS_FP64 = 0
+TFS_FP32C = 1
+
+_STATUS = {TFS_EINVAL: "EINVAL", TFS_ENOMEM: "ENOMEM", TFS_ECUDA: "ECUDA",
+           TFS_ENOTCONV: "ENOTCONV", TFS_ENAN: "ENAN", TFS_ETIMEOUT: "ETIMEOUT",
+           TFS_ESTATE: "ESTATE"}
+
+
+class TfsError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{_STATUS.get(code, code)}: {message}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("nswim", ctypes.c_int), ("nfil", ctypes.c_int), ("nseg", ctypes.c_int),
+                ("nblob", ctypes.c_int), ("mu", ctypes.c_double), ("a_seg", ctypes.c_double),
+                ("a_blob", ctypes.c_double), ("end_force_magnitude", ctypes.c_int),
+                ("repulsive_force_factor", ctypes.c_double), ("free_body", ctypes.c_int),
+                ("precision", ctypes.c_int)]
+
+
+class DeviceBuffers(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("x_segs", "f_segs", "v_segs", "x_blobs",
+                                                "f_blobs", "v_blobs", "f_blobs_repulsion")]
+
+
+_P = ctypes.c_void_p
+_H = ctypes.c_void_p  # opaque handle
+
+# name -> argument types (all return int unless listed in _RESTYPES)
+_SIGNATURES = {
+    "tfs_config_default": [ctypes.POINTER(Config), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                           ctypes.c_int],
+    "tfs_solver_create": [ctypes.POINTER(Config), ctypes.POINTER(_H)],
+    "tfs_solver_destroy": [_H],
+    "tfs_solver_set_stream": [_H, _P],
+    "tfs_solver_set_precision": [_H, ctypes.c_int],
+    "tfs_solver_device_buffers": [_H, ctypes.POINTER(DeviceBuffers)],
+    "tfs_solver_positions_updated": [_H],
+    "tfs_copy_segment_positions_to_device": [_H, _P],
+    "tfs_copy_segment_forces_to_device": [_H, _P],
+    "tfs_copy_blob_positions_to_device": [_H, _P],
+    "tfs_copy_blob_forces_to_device": [_H, _P],
+    "tfs_copy_interparticle_blob_forces_to_host": [_H, _P],
+    "tfs_copy_blob_velocities_to_host": [_H, _P],
+    "tfs_copy_segment_velocities_to_host": [_H, _P],
+    "tfs_apply_interparticle_forces": [_H],
+    "tfs_wait_for_device": [_H],
+    "tfs_evaluate_segment_segment_mobility": [_H],
+    "tfs_evaluate_segment_blob_mobility": [_H],
+    "tfs_evaluate_blob_blob_mobility": [_H],
+    "tfs_evaluate_blob_segment_mobility": [_H],
+    "tfs_evaluate_full_mobility": [_H, _P, _P],
+    "tfs_apply_grand_mobility": [_H],
+    "tfs_solver_enable_kernel_timing": [_H, ctypes.c_int],
+    "tfs_solver_kernel_timing": [_H, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                 ctypes.POINTER(ctypes.c_int)],
+    "tfs_last_error": [],
+    "tfs_kernel_launch_count": [],
+    "tfs_measure_fma_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
+}
+_RESTYPES = {"tfs_last_error": ctypes.c_char_p, "tfs_kernel_launch_count": ctypes.c_longlong}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False) -> ctypes.CDLL:
+    """Load libtfs_gb300.so (building it first if asked). Raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise ImportError(f"{path} is missing: build it with __graft_entry__.build() "
+                              "(the RPY path has no CPU fallback)")
+        _build.build()
+    lib = ctypes.CDLL(path)
+    for name, args in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _RESTYPES.get(name, ctypes.c_int)
+    _lib = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != TFS_OK:
+        msg = load().tfs_last_error().decode(errors="replace")
+        raise TfsError(rc, msg)
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGNATURES)

@@ -1,0 +1,518 @@
+// rpy_kernels.cu -- all-pairs RPY mobility, barrier-force and support
+// kernels for sm_103a.
+//
+// Layout. User arrays stay in the reference's AoS float64 layouts. Before a
+// product, the sources are packed once into fixed-size records
+// (pack_sources): FP64 segments {x,y,z,fx,fy,fz,tx,ty,tz,0} (80 B), FP64 blobs
+// {x,y,z,fx,fy,fz} (48 B), FP32 segments {x,y,z,fx,fy,fz,tx,ty,tz,0,0,0}
+// (48 B), FP32 blobs {x,y,z,fx,fy,fz,0,0} (32 B). Records are multiples of
+// 16 B so a tile of consecutive sources is one contiguous, 16-B aligned block
+// that the CTA stages into shared memory with 16-B vector loads; every thread
+// then reads each record by broadcast.
+// FP32 positions are stored relative to an origin (the mean particle
+// position, computed on the device), which keeps FP32 rounding of
+// differences relative to the swimmer's size rather than to absolute
+// coordinates.
+//
+// Work decomposition. A CTA owns BLOCK*TPT targets (TPT per thread, strided
+// by BLOCK) and one contiguous chunk of the sources; grid.y is the number of
+// source splits. With one split the CTA writes (or adds) the final velocities
+// (assign/accumulate semantics of cuda_functions.cu:463-468 and :625-630);
+// with several, each CTA writes its partial sums to a scratch buffer and
+// reduce_partials adds them in split order. Either way every target sums its
+// sources in a fixed order, so results are deterministic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "tfs_device.cuh"
+#include "tfs_kernels.h"
+
+namespace tfs {
+
+template <typename T, int FD>
+struct Rec;
+template <>
+struct Rec<double, 6> {
+  static constexpr int len = 10;
+};
+template <>
+struct Rec<double, 3> {
+  static constexpr int len = 6;
+};
+template <>
+struct Rec<float, 6> {
+  static constexpr int len = 12;
+};
+template <>
+struct Rec<float, 3> {
+  static constexpr int len = 8;
+};
+
+// ---------------------------------------------------------------------------
+// Origin/extent of a particle set: origin = mean position, extent = max over
+// particles of max |x_k - origin_k|. One CTA; used for FP32 centring and for
+// the FP32 candidate test of the barrier kernel.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) origin_kernel(const double *__restrict__ xa, int na,
+                                                     const double *__restrict__ xb, int nb,
+                                                     double *__restrict__ out /* [4] */) {
+  __shared__ double red[512][3];
+  const int tid = threadIdx.x;
+  double s[3] = {0, 0, 0};
+  for (int i = tid; i < na; i += blockDim.x)
+    for (int k = 0; k < 3; ++k) s[k] += xa[3 * (size_t)i + k];
+  for (int i = tid; i < nb; i += blockDim.x)
+    for (int k = 0; k < 3; ++k) s[k] += xb[3 * (size_t)i + k];
+  for (int k = 0; k < 3; ++k) red[tid][k] = s[k];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (tid < w)
+      for (int k = 0; k < 3; ++k) red[tid][k] += red[tid + w][k];
+    __syncthreads();
+  }
+  const int n = na + nb;
+  double o[3];
+  for (int k = 0; k < 3; ++k) o[k] = n > 0 ? red[0][k] / n : 0.0;
+  __syncthreads();
+  double m = 0.0;
+  for (int i = tid; i < na; i += blockDim.x)
+    for (int k = 0; k < 3; ++k) m = fmax(m, fabs(xa[3 * (size_t)i + k] - o[k]));
+  for (int i = tid; i < nb; i += blockDim.x)
+    for (int k = 0; k < 3; ++k) m = fmax(m, fabs(xb[3 * (size_t)i + k] - o[k]));
+  red[tid][0] = m;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (tid < w) red[tid][0] = fmax(red[tid][0], red[tid + w][0]);
+    __syncthreads();
+  }
+  if (tid == 0) {
+    out[0] = o[0];
+    out[1] = o[1];
+    out[2] = o[2];
+    out[3] = red[0][0];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Source packing: AoS float64 positions/forces -> records.
+// ---------------------------------------------------------------------------
+template <typename T, int FD>
+__global__ void pack_sources_kernel(T *__restrict__ rec, const double *__restrict__ x,
+                                    const double *__restrict__ f, int n,
+                                    const double *__restrict__ origin) {
+  constexpr int L = Rec<T, FD>::len;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double o0 = 0.0, o1 = 0.0, o2 = 0.0;
+  if (origin != nullptr) {
+    o0 = origin[0];
+    o1 = origin[1];
+    o2 = origin[2];
+  }
+  T *r = rec + (size_t)i * L;
+  r[0] = T(x[3 * (size_t)i] - o0);
+  r[1] = T(x[3 * (size_t)i + 1] - o1);
+  r[2] = T(x[3 * (size_t)i + 2] - o2);
+#pragma unroll
+  for (int k = 0; k < FD; ++k) r[3 + k] = T(f[(size_t)FD * i + k]);
+#pragma unroll
+  for (int k = 3 + FD; k < L; ++k) r[k] = T(0);
+}
+
+// ---------------------------------------------------------------------------
+// Accumulator: plain sum for FP64; FP32 tile sums folded into a (hi, lo)
+// pair by TwoSum after every tile (compensated accumulation).
+// ---------------------------------------------------------------------------
+template <typename T, int VD>
+struct Acc;
+
+template <int VD>
+struct Acc<double, VD> {
+  double v[VD];
+  __device__ void zero() {
+#pragma unroll
+    for (int k = 0; k < VD; ++k) v[k] = 0.0;
+  }
+  __device__ double *tile() { return v; }
+  __device__ void fold() {}
+  __device__ double get(int k) const { return v[k]; }
+};
+
+template <int VD>
+struct Acc<float, VD> {
+  float v[VD], hi[VD], lo[VD];
+  __device__ void zero() {
+#pragma unroll
+    for (int k = 0; k < VD; ++k) v[k] = hi[k] = lo[k] = 0.f;
+  }
+  __device__ float *tile() { return v; }
+  __device__ void fold() {
+#pragma unroll
+    for (int k = 0; k < VD; ++k) {
+      two_sum(hi[k], lo[k], v[k]);
+      v[k] = 0.f;
+    }
+  }
+  __device__ double get(int k) const { return (double)hi[k] + (double)lo[k]; }
+};
+
+template <typename T>
+__device__ __forceinline__ T load_target(const double *x, int i, int k, const double *origin) {
+  return T(x[3 * (size_t)i + k] - (origin ? origin[k] : 0.0));
+}
+
+// Sum the sources [lo, hi) of one record array into the accumulators.
+template <typename T, int VD, int FD, int BLOCK, int TPT, int TS>
+__device__ __forceinline__ void sum_source_range(Acc<T, VD> (&acc)[TPT], const T (&xt)[TPT],
+                                                 const T (&yt)[TPT], const T (&zt)[TPT],
+                                                 const T *__restrict__ rec, int lo, int hi,
+                                                 const PairConst<T> &pc, T *smem) {
+  constexpr int L = Rec<T, FD>::len;
+  constexpr int VEC_PER_REC = L * (int)sizeof(T) / 16;
+  for (int base = lo; base < hi; base += TS) {
+    const int cnt = min(TS, hi - base);
+    __syncthreads();  // previous tile fully consumed
+    const int4 *src = reinterpret_cast<const int4 *>(rec + (size_t)base * L);
+    int4 *dst = reinterpret_cast<int4 *>(smem);
+    const int nvec = cnt * VEC_PER_REC;
+    for (int q = threadIdx.x; q < nvec; q += BLOCK) dst[q] = __ldg(src + q);
+    __syncthreads();
+#pragma unroll 2
+    for (int j = 0; j < cnt; ++j) {
+      T f[FD];
+      const T *r = smem + j * L;
+      const T sx = r[0], sy = r[1], sz = r[2];
+#pragma unroll
+      for (int k = 0; k < FD; ++k) f[k] = r[3 + k];
+#pragma unroll
+      for (int t = 0; t < TPT; ++t) {
+        rpy_pair<T, VD, FD>(acc[t].tile(), xt[t] - sx, yt[t] - sy, zt[t] - sz, f, pc);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < TPT; ++t) acc[t].fold();
+  }
+}
+
+template <typename T, int VD, int FDA, int FDB, int BLOCK, int TPT, int TS>
+__global__ void __launch_bounds__(BLOCK) rpy_tile_kernel(const TileArgs args) {
+  constexpr int LA = Rec<T, FDA>::len;
+  constexpr int LB = FDB > 0 ? Rec<T, (FDB > 0 ? FDB : 3)>::len : 0;
+  constexpr int LMAX = LA > LB ? LA : LB;
+  __shared__ __align__(16) T smem[TS * LMAX];
+
+  const int n_tgt = args.n_tgt;
+  const double *origin = args.fp32 ? args.origin : nullptr;
+  const int tile0 = blockIdx.x * BLOCK * TPT;
+
+  T xt[TPT], yt[TPT], zt[TPT];
+  Acc<T, VD> acc[TPT];
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    int i = tile0 + t * BLOCK + threadIdx.x;
+    i = i < n_tgt ? i : n_tgt - 1;  // duplicate the last target; not written
+    xt[t] = load_target<T>(args.x_tgt, i, 0, origin);
+    yt[t] = load_target<T>(args.x_tgt, i, 1, origin);
+    zt[t] = load_target<T>(args.x_tgt, i, 2, origin);
+    acc[t].zero();
+  }
+
+  const int n_src = args.n_a + args.n_b;
+  const int s0 = blockIdx.y * args.chunk;
+  const int s1 = min(s0 + args.chunk, n_src);
+
+  {
+    PairConst<T> pc;
+    pc.ai = T(args.a_tgt);
+    pc.aj = T(args.a_a);
+    pc.asum2 = T((args.a_tgt + args.a_a) * (args.a_tgt + args.a_a));
+    pc.s = T((args.a_tgt * args.a_tgt + args.a_a * args.a_a) / 3.0);
+    pc.s3 = T(-(args.a_tgt * args.a_tgt + args.a_a * args.a_a));
+    const int lo = min(s0, args.n_a), hi = min(s1, args.n_a);
+    if (lo < hi)
+      sum_source_range<T, VD, FDA, BLOCK, TPT, TS>(acc, xt, yt, zt,
+                                                   reinterpret_cast<const T *>(args.src_a), lo,
+                                                   hi, pc, smem);
+  }
+  if constexpr (FDB > 0) {
+    PairConst<T> pc;
+    pc.ai = T(args.a_tgt);
+    pc.aj = T(args.a_b);
+    pc.asum2 = T((args.a_tgt + args.a_b) * (args.a_tgt + args.a_b));
+    pc.s = T((args.a_tgt * args.a_tgt + args.a_b * args.a_b) / 3.0);
+    pc.s3 = T(-(args.a_tgt * args.a_tgt + args.a_b * args.a_b));
+    const int lo = max(s0 - args.n_a, 0), hi = max(s1 - args.n_a, 0);
+    if (lo < hi)
+      sum_source_range<T, VD, FDB, BLOCK, TPT, TS>(acc, xt, yt, zt,
+                                                   reinterpret_cast<const T *>(args.src_b), lo,
+                                                   hi, pc, smem);
+  }
+
+  const double c = args.scale;
+#pragma unroll
+  for (int t = 0; t < TPT; ++t) {
+    const int i = tile0 + t * BLOCK + threadIdx.x;
+    if (i >= n_tgt) continue;
+    if (args.mode == OUT_PARTIAL) {
+      double *o = args.out + ((size_t)blockIdx.y * n_tgt + i) * VD;
+#pragma unroll
+      for (int k = 0; k < VD; ++k) o[k] = c * acc[t].get(k);
+    } else if (args.mode == OUT_ACCUMULATE) {
+      double *o = args.out + (size_t)i * VD;
+#pragma unroll
+      for (int k = 0; k < VD; ++k) o[k] += c * acc[t].get(k);
+    } else {
+      double *o = args.out + (size_t)i * VD;
+#pragma unroll
+      for (int k = 0; k < VD; ++k) o[k] = c * acc[t].get(k);
+    }
+  }
+}
+
+// out[i] (= or +=) sum over splits of partial[s][i], s in order.
+__global__ void reduce_partials_kernel(double *__restrict__ out,
+                                       const double *__restrict__ partial, int n_elems,
+                                       int splits, int accumulate) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_elems) return;
+  double s = 0.0;
+  for (int p = 0; p < splits; ++p) s += partial[(size_t)p * n_elems + i];
+  out[i] = accumulate ? out[i] + s : s;
+}
+
+// ---------------------------------------------------------------------------
+// Barrier (steric) forces, cuda_functions.cu:1240-1436 without a plane wall.
+// A candidate test on FP32 positions (relative to the origin, with a margin
+// that bounds their rounding) discards the vast majority of pairs on the FP32
+// pipe; candidates are then tested and evaluated in FP64 exactly as the
+// reference does. Targets are segments (kind 0: skip self and the nearest
+// neighbours on the same filament; adds into f_segs) or blobs (kind 1: skip
+// self; assigns f_blobs_repulsion).
+// ---------------------------------------------------------------------------
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
+  __shared__ double sxd[BLOCK][3];
+  __shared__ float sxf[BLOCK][3];
+  const int i = blockIdx.x * BLOCK + threadIdx.x;
+  const int n_tgt = a.target_blobs ? a.num_blobs : a.num_segs;
+  const bool active = i < n_tgt;
+  const double *xt = a.target_blobs ? a.x_blobs : a.x_segs;
+  const int ii = active ? i : 0;
+  const double o0 = a.origin[0], o1 = a.origin[1], o2 = a.origin[2];
+  const double extent = a.origin[3];
+  const double xi = n_tgt > 0 ? xt[3 * (size_t)ii] : 0.0;
+  const double yi = n_tgt > 0 ? xt[3 * (size_t)ii + 1] : 0.0;
+  const double zi = n_tgt > 0 ? xt[3 * (size_t)ii + 2] : 0.0;
+  const float xif = float(xi - o0), yif = float(yi - o1), zif = float(zi - o2);
+  // |d_fp32 - d| <= 2 sqrt(3) extent 2^-24 =: delta (each coordinate is
+  // rounded once to FP32, relative 2^-24), plus FP32 arithmetic in d^2.
+  const float delta = float(4.0 * extent * 5.9604644775390625e-08 + 1e-30);
+  const int fil_i = active && !a.target_blobs ? i / a.nseg : -1;
+  const double emag = a.repulsive_force_factor * (double)a.end_force_magnitude;
+  const int n_src = a.num_segs + a.num_blobs;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  for (int base = 0; base < n_src; base += BLOCK) {
+    const int j = base + threadIdx.x;
+    __syncthreads();
+    if (j < n_src) {
+      const double *xs = j < a.num_segs ? a.x_segs + 3 * (size_t)j
+                                        : a.x_blobs + 3 * (size_t)(j - a.num_segs);
+      sxd[threadIdx.x][0] = xs[0];
+      sxd[threadIdx.x][1] = xs[1];
+      sxd[threadIdx.x][2] = xs[2];
+      sxf[threadIdx.x][0] = float(xs[0] - o0);
+      sxf[threadIdx.x][1] = float(xs[1] - o1);
+      sxf[threadIdx.x][2] = float(xs[2] - o2);
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int cnt = min(BLOCK, n_src - base);
+    for (int q = 0; q < cnt; ++q) {
+      const int jj = base + q;
+      const bool src_is_seg = jj < a.num_segs;
+      double asum;
+      if (a.target_blobs)
+        asum = src_is_seg ? a.a_blob + a.a_seg : 2.0 * a.a_blob;
+      else
+        asum = src_is_seg ? 2.0 * a.a_seg : a.a_seg + a.a_blob;
+      const float dxf = xif - sxf[q][0], dyf = yif - sxf[q][1], dzf = zif - sxf[q][2];
+      const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      const float thr = float(1.1 * asum) + 2.f * delta;
+      if (d2f >= thr * thr * 1.0001f) continue;
+      // exclusions, :1319 and :1410
+      if (a.target_blobs) {
+        if (i + a.num_segs == jj) continue;
+      } else if (src_is_seg) {
+        const int fil_j = jj / a.nseg;
+        if (fil_i == fil_j && (i - jj <= 1 && jj - i <= 1)) continue;
+      }
+      const double dx = xi - sxd[q][0], dy = yi - sxd[q][1], dz = zi - sxd[q][2];
+      const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+      if (dist < 1.1 * asum) {
+        const double chi = 10.0 / asum;
+        double fac = fmin(1.0, 1.0 - chi * (dist - asum));
+        fac *= emag * fac * fac * fac;
+        const double dm1 = 1.0 / dist;
+        fx += fac * dx * dm1;
+        fy += fac * dy * dm1;
+        fz += fac * dz * dm1;
+      }
+    }
+  }
+  if (!active) return;
+  if (a.target_blobs) {
+    a.f_blobs_repulsion[3 * (size_t)i] = fx;
+    a.f_blobs_repulsion[3 * (size_t)i + 1] = fy;
+    a.f_blobs_repulsion[3 * (size_t)i + 2] = fz;
+  } else {
+    a.f_segs[6 * (size_t)i] += fx;
+    a.f_segs[6 * (size_t)i + 1] += fy;
+    a.f_segs[6 * (size_t)i + 2] += fz;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers
+// ---------------------------------------------------------------------------
+static int g_num_sms = 0;
+
+int num_sms() {
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 1;
+  }
+  return g_num_sms;
+}
+
+cudaError_t launch_origin(const double *xa, int na, const double *xb, int nb, double *out,
+                          cudaStream_t st) {
+  origin_kernel<<<1, 512, 0, st>>>(xa, na, xb, nb, out);
+  count_launch();
+  return cudaGetLastError();
+}
+
+template <typename T, int FD>
+static cudaError_t pack_t(void *rec, const double *x, const double *f, int n,
+                          const double *origin, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  pack_sources_kernel<T, FD><<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<T *>(rec), x, f,
+                                                               n, origin);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack(int fp32, int fd, void *rec, const double *x, const double *f, int n,
+                        const double *origin, cudaStream_t st) {
+  if (fp32) return fd == 6 ? pack_t<float, 6>(rec, x, f, n, origin, st)
+                           : pack_t<float, 3>(rec, x, f, n, origin, st);
+  return fd == 6 ? pack_t<double, 6>(rec, x, f, n, nullptr, st)
+                 : pack_t<double, 3>(rec, x, f, n, nullptr, st);
+}
+
+size_t record_bytes(int fp32, int fd) {
+  if (fp32) return fd == 6 ? 48 : 32;
+  return fd == 6 ? 80 : 48;
+}
+
+// Launch geometry per precision: FP64 is bound by the FP64 pipe, so one
+// target per thread and enough source splits to give every SM several
+// warps; FP32 register-blocks two targets per thread.
+template <typename T>
+struct Geom;
+template <>
+struct Geom<double> {
+  static constexpr int BLOCK = 128, TPT = 1, TS = 128;
+};
+template <>
+struct Geom<float> {
+  static constexpr int BLOCK = 128, TPT = 2, TS = 256;
+};
+
+// Choose the number of source splits: aim for ~`waves` CTAs per SM with at
+// least `min_chunk` sources per split.
+static int choose_splits(int target_ctas, int n_src, int max_splits, int min_chunk) {
+  const int want = std::max(1, (4 * num_sms() + target_ctas - 1) / target_ctas);
+  int s = std::min(want, max_splits);
+  s = std::min(s, std::max(1, n_src / std::max(1, min_chunk)));
+  return std::max(1, s);
+}
+
+template <typename T, int VD, int FDA, int FDB>
+static cudaError_t tile_t(TileArgs a, double *scratch, size_t scratch_elems, int mode,
+                          cudaStream_t st, cudaEvent_t *ev) {
+  using G = Geom<T>;
+  constexpr int per_cta = G::BLOCK * G::TPT;
+  const int ctas = (a.n_tgt + per_cta - 1) / per_cta;
+  const int n_src = a.n_a + a.n_b;
+  if (a.n_tgt <= 0) return cudaSuccess;
+  int splits = a.splits > 0 ? a.splits : choose_splits(ctas, n_src, kMaxSplits, 2 * G::TS);
+  if ((size_t)splits * a.n_tgt * VD > scratch_elems) splits = 1;
+  if (n_src == 0) splits = 1;
+  int chunk = (n_src + splits - 1) / splits;
+  chunk = ((chunk + G::TS - 1) / G::TS) * G::TS;
+  if (chunk == 0) chunk = G::TS;
+  splits = std::max(1, (n_src + chunk - 1) / chunk);
+  a.chunk = chunk;
+  dim3 grid(ctas, splits);
+  if (ev) cudaEventRecord(ev[0], st);
+  if (splits == 1) {
+    a.mode = mode;
+    rpy_tile_kernel<T, VD, FDA, FDB, G::BLOCK, G::TPT, G::TS><<<grid, G::BLOCK, 0, st>>>(a);
+    count_launch();
+    if (ev) cudaEventRecord(ev[1], st);
+    return cudaGetLastError();
+  }
+  double *final_out = a.out;
+  a.mode = OUT_PARTIAL;
+  a.out = scratch;
+  rpy_tile_kernel<T, VD, FDA, FDB, G::BLOCK, G::TPT, G::TS><<<grid, G::BLOCK, 0, st>>>(a);
+  count_launch();
+  if (ev) cudaEventRecord(ev[1], st);
+  const int n_elems = a.n_tgt * VD;
+  reduce_partials_kernel<<<(n_elems + 255) / 256, 256, 0, st>>>(
+      final_out, scratch, n_elems, splits, mode == OUT_ACCUMULATE ? 1 : 0);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile(const TileArgs &a, int vd, int fda, int fdb, double *scratch,
+                        size_t scratch_elems, int mode, cudaStream_t st, cudaEvent_t *ev) {
+  if (a.fp32) {
+    if (vd == 6 && fda == 6 && fdb == 0) return tile_t<float, 6, 6, 0>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 6 && fda == 3 && fdb == 0) return tile_t<float, 6, 3, 0>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 3 && fda == 3 && fdb == 0) return tile_t<float, 3, 3, 0>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 3 && fda == 6 && fdb == 0) return tile_t<float, 3, 6, 0>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 6 && fda == 6 && fdb == 3) return tile_t<float, 6, 6, 3>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 3 && fda == 6 && fdb == 3) return tile_t<float, 3, 6, 3>(a, scratch, scratch_elems, mode, st, ev);
+  } else {
+    if (vd == 6 && fda == 6 && fdb == 0) return tile_t<double, 6, 6, 0>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 6 && fda == 3 && fdb == 0) return tile_t<double, 6, 3, 0>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 3 && fda == 3 && fdb == 0) return tile_t<double, 3, 3, 0>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 3 && fda == 6 && fdb == 0) return tile_t<double, 3, 6, 0>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 6 && fda == 6 && fdb == 3) return tile_t<double, 6, 6, 3>(a, scratch, scratch_elems, mode, st, ev);
+    if (vd == 3 && fda == 6 && fdb == 3) return tile_t<double, 3, 6, 3>(a, scratch, scratch_elems, mode, st, ev);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st) {
+  constexpr int B = 128;
+  if (a.num_segs > 0) {
+    BarrierArgs s = a;
+    s.target_blobs = 0;
+    barrier_kernel<B><<<(a.num_segs + B - 1) / B, B, 0, st>>>(s);
+    count_launch();
+  }
+  if (a.free_body && a.num_blobs > 0) {
+    BarrierArgs b = a;
+    b.target_blobs = 1;
+    barrier_kernel<B><<<(a.num_blobs + B - 1) / B, B, 0, st>>>(b);
+    count_launch();
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tfs

@@ -1,0 +1,477 @@
+// tfs_api.cu -- the C ABI of libtfs_gb300.so (include/tfs_gb300.h): the
+// solver object that stands in for the reference's rpy_mobility_solver
+// (src/cilia/mobility/rpy_mobility_solver.{hpp,cu}).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/tfs_gb300.h"
+#include "tfs_kernels.h"
+
+namespace tfs {
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+static thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(TFS_ECUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+}  // namespace tfs
+
+using namespace tfs;
+
+struct tfs_solver {
+  tfs_config cfg;
+  int ns = 0, nb = 0;
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  double *x_segs = nullptr, *f_segs = nullptr, *v_segs = nullptr;
+  double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
+  double *origin = nullptr;  // [4]: mean position and extent
+  void *rec_segs = nullptr, *rec_blobs = nullptr;
+  double *scratch = nullptr;
+  size_t scratch_elems = 0;
+  bool origin_dirty = true;
+  // dominant-kernel timing (tfs_solver_enable_kernel_timing)
+  bool timing = false;
+  std::vector<cudaEvent_t> events;  // pairs, in launch order
+  size_t events_used = 0;
+};
+
+#define TFS_CHECK_SOLVER(s)                                          \
+  do {                                                               \
+    if ((s) == nullptr) return fail(TFS_EINVAL, "null solver handle"); \
+  } while (0)
+
+#define TFS_CUDA(call, what)                  \
+  do {                                        \
+    cudaError_t e_ = (call);                  \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+// Next free event pair for the timing hook (nullptr when timing is off).
+static cudaEvent_t *next_events(tfs_solver *s) {
+  if (!s->timing) return nullptr;
+  if (s->events_used + 2 > s->events.size()) {
+    if (s->events.size() >= 2 * 4096) return nullptr;  // bounded
+    for (int k = 0; k < 2; ++k) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      s->events.push_back(e);
+    }
+  }
+  cudaEvent_t *p = &s->events[s->events_used];
+  s->events_used += 2;
+  return p;
+}
+
+static void free_all(tfs_solver *s) {
+  for (cudaEvent_t e : s->events) cudaEventDestroy(e);
+  s->events.clear();
+  cudaFree(s->x_segs);
+  cudaFree(s->f_segs);
+  cudaFree(s->v_segs);
+  cudaFree(s->x_blobs);
+  cudaFree(s->f_blobs);
+  cudaFree(s->v_blobs);
+  cudaFree(s->f_rep);
+  cudaFree(s->origin);
+  cudaFree(s->rec_segs);
+  cudaFree(s->rec_blobs);
+  cudaFree(s->scratch);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+}
+
+static int alloc_dev(void **p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(TFS_ENOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  }
+  return TFS_OK;
+}
+
+static int ensure_origin(tfs_solver *s) {
+  if (!s->origin_dirty) return TFS_OK;
+  cudaError_t e = launch_origin(s->x_segs, s->ns, s->x_blobs, s->nb, s->origin, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "origin kernel");
+  s->origin_dirty = false;
+  return TFS_OK;
+}
+
+static int pack(tfs_solver *s, int segs) {
+  const int fp32 = s->cfg.precision == TFS_FP32C;
+  cudaError_t e = segs ? launch_pack(fp32, 6, s->rec_segs, s->x_segs, s->f_segs, s->ns,
+                                     s->origin, s->stream)
+                       : launch_pack(fp32, 3, s->rec_blobs, s->x_blobs, s->f_blobs, s->nb,
+                                     s->origin, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "pack kernel");
+  return TFS_OK;
+}
+
+static TileArgs base_args(tfs_solver *s) {
+  TileArgs a{};
+  a.origin = s->origin;
+  a.fp32 = s->cfg.precision == TFS_FP32C;
+  a.scale = 1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu);
+  a.splits = 0;
+  return a;
+}
+
+// Product of one block or fused pair of blocks into `out`.
+static int product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mode) {
+  int rc;
+  if (s->cfg.precision == TFS_FP32C && (rc = ensure_origin(s)) != TFS_OK) return rc;
+  if (src_segs && (rc = pack(s, 1)) != TFS_OK) return rc;
+  if (src_blobs && (rc = pack(s, 0)) != TFS_OK) return rc;
+  TileArgs a = base_args(s);
+  a.x_tgt = tgt_segs ? s->x_segs : s->x_blobs;
+  a.n_tgt = tgt_segs ? s->ns : s->nb;
+  a.a_tgt = tgt_segs ? s->cfg.a_seg : s->cfg.a_blob;
+  a.out = tgt_segs ? s->v_segs : s->v_blobs;
+  int fda, fdb = 0;
+  if (src_segs) {
+    a.src_a = s->rec_segs;
+    a.n_a = s->ns;
+    a.a_a = s->cfg.a_seg;
+    fda = 6;
+    if (src_blobs) {
+      a.src_b = s->rec_blobs;
+      a.n_b = s->nb;
+      a.a_b = s->cfg.a_blob;
+      fdb = 3;
+    }
+  } else {
+    a.src_a = s->rec_blobs;
+    a.n_a = s->nb;
+    a.a_a = s->cfg.a_blob;
+    fda = 3;
+  }
+  if (a.n_tgt == 0) return TFS_OK;
+  if (a.n_a + a.n_b == 0) {
+    if (mode == OUT_ASSIGN)
+      TFS_CUDA(cudaMemsetAsync(a.out, 0, sizeof(double) * (tgt_segs ? 6 : 3) * a.n_tgt, s->stream),
+               "cudaMemsetAsync");
+    return TFS_OK;
+  }
+  cudaError_t e = launch_tile(a, tgt_segs ? 6 : 3, fda, fdb, s->scratch, s->scratch_elems, mode,
+                              s->stream, next_events(s));
+  if (e != cudaSuccess) return cuda_fail(e, "RPY tile kernel");
+  return TFS_OK;
+}
+
+extern "C" {
+
+int tfs_config_default(tfs_config *cfg, int nswim, int nfil, int nseg, int nblob) {
+  if (cfg == nullptr) return fail(TFS_EINVAL, "null config");
+  std::memset(cfg, 0, sizeof *cfg);
+  cfg->nswim = nswim;
+  cfg->nfil = nfil;
+  cfg->nseg = nseg;
+  cfg->nblob = nblob;
+  cfg->mu = 1.0;
+  cfg->a_seg = 1.0;
+  cfg->a_blob = 1.0;
+  // END_FORCE_MAGNITUDE = DIMENSIONLESS_FORCE*KB/(DL*DL*NSEG*NSEG) with the
+  // default DL = 2.6 (globals.cu:14-18, config.hpp:261,275), truncated to int.
+  cfg->end_force_magnitude =
+      nseg > 0 ? (int)(220.0 * 1800.0 / (2.6 * 2.6 * (double)nseg * (double)nseg)) : 0;
+  cfg->repulsive_force_factor = 2.0;
+  cfg->free_body = 1;
+  cfg->precision = TFS_FP64;
+  return TFS_OK;
+}
+
+int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
+  if (cfg == nullptr || out == nullptr) return fail(TFS_EINVAL, "null argument");
+  *out = nullptr;
+  if (cfg->nswim < 0 || cfg->nfil < 0 || cfg->nseg < 0 || cfg->nblob < 0)
+    return fail(TFS_EINVAL, "negative size");
+  const long long ns = (long long)cfg->nswim * cfg->nfil * cfg->nseg;
+  const long long nb = (long long)cfg->nswim * cfg->nblob;
+  if (ns > (1LL << 26) || nb > (1LL << 26))
+    return fail(TFS_EINVAL, "too many particles (%lld segments, %lld blobs; max 2^26 each)", ns, nb);
+  if (!(cfg->mu > 0) || !(cfg->a_seg > 0) || !(cfg->a_blob > 0))
+    return fail(TFS_EINVAL, "mu and radii must be positive");
+  if (cfg->precision != TFS_FP64 && cfg->precision != TFS_FP32C)
+    return fail(TFS_EINVAL, "unknown precision %d", cfg->precision);
+  if (ns > 0 && cfg->nseg <= 0) return fail(TFS_EINVAL, "nseg must be positive");
+
+  tfs_solver *s = new (std::nothrow) tfs_solver;
+  if (s == nullptr) return fail(TFS_ENOMEM, "host allocation failed");
+  s->cfg = *cfg;
+  s->ns = (int)ns;
+  s->nb = (int)nb;
+  cudaGetDevice(&s->device);
+  int rc = TFS_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete s;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  s->stream = s->own_stream;
+  const size_t dsz = sizeof(double);
+  s->scratch_elems = (size_t)kMaxSplits * (size_t)std::max(6 * ns, 3 * nb);
+  if ((rc = alloc_dev((void **)&s->x_segs, dsz * 3 * ns)) ||
+      (rc = alloc_dev((void **)&s->f_segs, dsz * 6 * ns)) ||
+      (rc = alloc_dev((void **)&s->v_segs, dsz * 6 * ns)) ||
+      (rc = alloc_dev((void **)&s->x_blobs, dsz * 3 * nb)) ||
+      (rc = alloc_dev((void **)&s->f_blobs, dsz * 3 * nb)) ||
+      (rc = alloc_dev((void **)&s->v_blobs, dsz * 3 * nb)) ||
+      (rc = alloc_dev((void **)&s->f_rep, dsz * 3 * nb)) ||
+      (rc = alloc_dev((void **)&s->origin, dsz * 4)) ||
+      (rc = alloc_dev(&s->rec_segs, record_bytes(0, 6) * ns)) ||
+      (rc = alloc_dev(&s->rec_blobs, record_bytes(0, 3) * nb)) ||
+      (rc = alloc_dev((void **)&s->scratch, dsz * s->scratch_elems))) {
+    free_all(s);
+    delete s;
+    return rc;
+  }
+  // GMRES warm starts read f_blobs before any force is written
+  // (mobility_solver.cpp:35-39 zeroes the host copy); zero everything.
+  cudaMemsetAsync(s->f_blobs, 0, dsz * 3 * nb, s->stream);
+  cudaMemsetAsync(s->f_rep, 0, dsz * 3 * nb, s->stream);
+  cudaMemsetAsync(s->origin, 0, dsz * 4, s->stream);
+  e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) {
+    free_all(s);
+    delete s;
+    return cuda_fail(e, "solver initialisation");
+  }
+  *out = s;
+  return TFS_OK;
+}
+
+int tfs_solver_destroy(tfs_solver *s) {
+  if (s == nullptr) return TFS_OK;
+  cudaStreamSynchronize(s->stream);
+  free_all(s);
+  delete s;
+  return TFS_OK;
+}
+
+int tfs_solver_set_stream(tfs_solver *s, void *stream) {
+  TFS_CHECK_SOLVER(s);
+  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+  return TFS_OK;
+}
+
+int tfs_solver_set_precision(tfs_solver *s, int precision) {
+  TFS_CHECK_SOLVER(s);
+  if (precision != TFS_FP64 && precision != TFS_FP32C)
+    return fail(TFS_EINVAL, "unknown precision %d", precision);
+  s->cfg.precision = precision;
+  return TFS_OK;
+}
+
+int tfs_solver_device_buffers(tfs_solver *s, tfs_device_buffers *out) {
+  TFS_CHECK_SOLVER(s);
+  if (out == nullptr) return fail(TFS_EINVAL, "null output");
+  out->x_segs = s->x_segs;
+  out->f_segs = s->f_segs;
+  out->v_segs = s->v_segs;
+  out->x_blobs = s->x_blobs;
+  out->f_blobs = s->f_blobs;
+  out->v_blobs = s->v_blobs;
+  out->f_blobs_repulsion = s->f_rep;
+  // the caller may write positions directly
+  s->origin_dirty = true;
+  return TFS_OK;
+}
+
+int tfs_solver_positions_updated(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  s->origin_dirty = true;
+  return TFS_OK;
+}
+
+static int h2d(tfs_solver *s, double *dst, const double *src, size_t n, const char *what) {
+  TFS_CHECK_SOLVER(s);
+  if (n == 0) return TFS_OK;
+  if (src == nullptr) return fail(TFS_EINVAL, "%s: null host pointer", what);
+  TFS_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, s->stream), what);
+  return TFS_OK;
+}
+
+static int d2h(tfs_solver *s, double *dst, const double *src, size_t n, const char *what) {
+  TFS_CHECK_SOLVER(s);
+  if (n == 0) return TFS_OK;
+  if (dst == nullptr) return fail(TFS_EINVAL, "%s: null host pointer", what);
+  TFS_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream), what);
+  return TFS_OK;
+}
+
+int tfs_copy_segment_positions_to_device(tfs_solver *s, const double *x) {
+  TFS_CHECK_SOLVER(s);
+  s->origin_dirty = true;
+  return h2d(s, s->x_segs, x, 3 * (size_t)s->ns, "copy_segment_positions_to_device");
+}
+int tfs_copy_segment_forces_to_device(tfs_solver *s, const double *f) {
+  TFS_CHECK_SOLVER(s);
+  return h2d(s, s->f_segs, f, 6 * (size_t)s->ns, "copy_segment_forces_to_device");
+}
+int tfs_copy_blob_positions_to_device(tfs_solver *s, const double *x) {
+  TFS_CHECK_SOLVER(s);
+  s->origin_dirty = true;
+  return h2d(s, s->x_blobs, x, 3 * (size_t)s->nb, "copy_blob_positions_to_device");
+}
+int tfs_copy_blob_forces_to_device(tfs_solver *s, const double *f) {
+  TFS_CHECK_SOLVER(s);
+  return h2d(s, s->f_blobs, f, 3 * (size_t)s->nb, "copy_blob_forces_to_device");
+}
+int tfs_copy_interparticle_blob_forces_to_host(tfs_solver *s, double *f) {
+  TFS_CHECK_SOLVER(s);
+  return d2h(s, f, s->f_rep, 3 * (size_t)s->nb, "copy_interparticle_blob_forces_to_host");
+}
+int tfs_copy_blob_velocities_to_host(tfs_solver *s, double *v) {
+  TFS_CHECK_SOLVER(s);
+  return d2h(s, v, s->v_blobs, 3 * (size_t)s->nb, "copy_blob_velocities_to_host");
+}
+int tfs_copy_segment_velocities_to_host(tfs_solver *s, double *v) {
+  TFS_CHECK_SOLVER(s);
+  return d2h(s, v, s->v_segs, 6 * (size_t)s->ns, "copy_segment_velocities_to_host");
+}
+
+int tfs_apply_interparticle_forces(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  int rc = ensure_origin(s);
+  if (rc != TFS_OK) return rc;
+  BarrierArgs a{};
+  a.f_segs = s->f_segs;
+  a.f_blobs_repulsion = s->f_rep;
+  a.x_segs = s->x_segs;
+  a.x_blobs = s->x_blobs;
+  a.origin = s->origin;
+  a.num_segs = s->ns;
+  a.num_blobs = s->nb;
+  a.nseg = s->cfg.nseg > 0 ? s->cfg.nseg : 1;
+  a.a_seg = s->cfg.a_seg;
+  a.a_blob = s->cfg.a_blob;
+  a.end_force_magnitude = s->cfg.end_force_magnitude;
+  a.repulsive_force_factor = s->cfg.repulsive_force_factor;
+  a.free_body = s->cfg.free_body;
+  cudaError_t e = launch_barrier(a, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "barrier kernel");
+  return TFS_OK;
+}
+
+int tfs_wait_for_device(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "wait_for_device");
+  TFS_CUDA(cudaGetLastError(), "wait_for_device");
+  return TFS_OK;
+}
+
+int tfs_evaluate_segment_segment_mobility(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  return product(s, true, true, false, OUT_ASSIGN);
+}
+int tfs_evaluate_segment_blob_mobility(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  return product(s, true, false, true, OUT_ACCUMULATE);
+}
+int tfs_evaluate_blob_blob_mobility(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  return product(s, false, false, true, OUT_ASSIGN);
+}
+int tfs_evaluate_blob_segment_mobility(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  return product(s, false, true, false, OUT_ASSIGN);
+}
+
+int tfs_evaluate_full_mobility(tfs_solver *s, double *v_segs_host, double *v_blobs_host) {
+  TFS_CHECK_SOLVER(s);
+  int rc;
+  if ((rc = tfs_evaluate_segment_segment_mobility(s)) != TFS_OK) return rc;
+  if ((rc = tfs_evaluate_segment_blob_mobility(s)) != TFS_OK) return rc;
+  if (v_segs_host && (rc = tfs_copy_segment_velocities_to_host(s, v_segs_host)) != TFS_OK)
+    return rc;
+  if ((rc = tfs_evaluate_blob_blob_mobility(s)) != TFS_OK) return rc;
+  if ((rc = tfs_evaluate_blob_segment_mobility(s)) != TFS_OK) return rc;
+  if (v_blobs_host && (rc = tfs_copy_blob_velocities_to_host(s, v_blobs_host)) != TFS_OK)
+    return rc;
+  return TFS_OK;
+}
+
+int tfs_apply_grand_mobility(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  int rc;
+  if (s->ns > 0 && (rc = product(s, true, true, s->nb > 0, OUT_ASSIGN)) != TFS_OK) return rc;
+  if (s->nb > 0) {
+    if (s->ns > 0) {
+      // blob targets: segment sources (set A) then blob sources (set B);
+      // both record arrays are already packed.
+      int r2;
+      if (s->cfg.precision == TFS_FP32C && (r2 = ensure_origin(s)) != TFS_OK) return r2;
+      TileArgs a = base_args(s);
+      a.x_tgt = s->x_blobs;
+      a.n_tgt = s->nb;
+      a.a_tgt = s->cfg.a_blob;
+      a.out = s->v_blobs;
+      a.src_a = s->rec_segs;
+      a.n_a = s->ns;
+      a.a_a = s->cfg.a_seg;
+      a.src_b = s->rec_blobs;
+      a.n_b = s->nb;
+      a.a_b = s->cfg.a_blob;
+      cudaError_t e = launch_tile(a, 3, 6, 3, s->scratch, s->scratch_elems, OUT_ASSIGN, s->stream,
+                                  next_events(s));
+      if (e != cudaSuccess) return cuda_fail(e, "RPY tile kernel");
+    } else if ((rc = product(s, false, false, true, OUT_ASSIGN)) != TFS_OK) {
+      return rc;
+    }
+  }
+  return TFS_OK;
+}
+
+int tfs_solver_enable_kernel_timing(tfs_solver *s, int enable) {
+  TFS_CHECK_SOLVER(s);
+  s->timing = enable != 0;
+  s->events_used = 0;
+  return TFS_OK;
+}
+
+int tfs_solver_kernel_timing(tfs_solver *s, double *ms, int capacity, int *launches) {
+  TFS_CHECK_SOLVER(s);
+  if (launches == nullptr || (ms == nullptr && capacity > 0)) return fail(TFS_EINVAL, "null output");
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "kernel timing");
+  const int n = (int)(s->events_used / 2);
+  for (int k = 0; k < n && k < capacity; ++k) {
+    float t = 0.f;
+    TFS_CUDA(cudaEventElapsedTime(&t, s->events[2 * k], s->events[2 * k + 1]),
+             "cudaEventElapsedTime");
+    ms[k] = t;
+  }
+  *launches = n;
+  s->events_used = 0;
+  return TFS_OK;
+}
+
+const char *tfs_last_error(void) { return g_last_error.c_str(); }
+
+long long tfs_kernel_launch_count(void) { return g_launches.load(); }
+
+}  // extern "C"

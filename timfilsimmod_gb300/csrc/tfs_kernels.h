@@ -1,0 +1,67 @@
+// tfs_kernels.h -- host-side declarations of the kernel launchers
+// (internal to libtfs_gb300.so).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace tfs {
+
+enum OutMode { OUT_ASSIGN = 0, OUT_ACCUMULATE = 1, OUT_PARTIAL = 2 };
+
+// Upper bound on source splits of one product (sizes the scratch buffer).
+constexpr int kMaxSplits = 32;
+
+struct TileArgs {
+  const double *x_tgt;  // target positions, AoS float64 [3*n_tgt]
+  int n_tgt;
+  double a_tgt;         // target radius
+  const void *src_a;    // packed source records, set A
+  int n_a;
+  double a_a;
+  const void *src_b;    // packed source records, set B (or null)
+  int n_b;
+  double a_b;
+  const double *origin; // device [4]: FP32 centring origin (+ extent)
+  int fp32;             // 1: FP32 compensated, 0: FP64
+  double scale;         // 1 / (8 pi mu)
+  double *out;          // velocities, AoS float64 [VD*n_tgt]
+  int splits;           // 0: automatic
+  int chunk;            // set by the launcher
+  int mode;             // set by the launcher
+};
+
+struct BarrierArgs {
+  double *f_segs;             // += on segment targets
+  double *f_blobs_repulsion;  // = on blob targets
+  const double *x_segs;
+  const double *x_blobs;
+  const double *origin;       // device [4] origin + extent
+  int num_segs, num_blobs, nseg;
+  double a_seg, a_blob;
+  int end_force_magnitude;
+  double repulsive_force_factor;
+  int free_body;
+  int target_blobs;           // set by the launcher
+};
+
+int num_sms();
+void count_launch();
+size_t record_bytes(int fp32, int fd);
+
+cudaError_t launch_origin(const double *xa, int na, const double *xb, int nb, double *out,
+                          cudaStream_t st);
+cudaError_t launch_pack(int fp32, int fd, void *rec, const double *x, const double *f, int n,
+                        const double *origin, cudaStream_t st);
+// vd: 6 (segment targets) or 3 (blob targets); fda/fdb: 6 (segment sources),
+// 3 (blob sources), fdb = 0 for a single source set. mode: OUT_ASSIGN or
+// OUT_ACCUMULATE. scratch must hold kMaxSplits * n_tgt * vd doubles for
+// split launches (the launcher falls back to one split when it is smaller).
+// ev (optional): a pair of events recorded around the tile kernel itself
+// (not the pack or reduce kernels), for the dominant-kernel timing hook.
+cudaError_t launch_tile(const TileArgs &a, int vd, int fda, int fdb, double *scratch,
+                        size_t scratch_elems, int mode, cudaStream_t st,
+                        cudaEvent_t *ev = nullptr);
+cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st);
+
+}  // namespace tfs

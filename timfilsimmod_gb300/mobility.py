@@ -1,0 +1,222 @@
+"""Python mirror of the reference's `rpy_mobility_solver`
+(src/cilia/mobility/rpy_mobility_solver.{hpp,cu}) over the C ABI.
+
+Method names, argument meaning and call order are the reference's: the host
+arrays `x_segs_host`, `f_segs_host`, `f_blobs_host`, `v_segs_host`,
+`v_blobs_host`, `f_blobs_repulsion_host` are owned by the solver (pinned when
+PyTorch is available, mobility_solver.hpp:57-63), callers write positions and
+forces into them in place, and the hooks move them to and from the device.
+Everything computes on the GPU through libtfs_gb300.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+
+class _DeviceArray:
+    """A view of one solver device buffer with __cuda_array_interface__, so
+    torch.as_tensor(view, device="cuda") aliases it without copying."""
+
+    def __init__(self, ptr: int, n: int, owner):
+        self._owner = owner
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8",
+                                         "data": (int(ptr), False), "version": 3,
+                                         "strides": None}
+
+
+def _host_array(n: int, pinned: bool) -> np.ndarray:
+    if pinned:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                t = torch.zeros(n, dtype=torch.float64, pin_memory=True)
+                arr = t.numpy()
+                arr._tfs_keepalive = t  # type: ignore[attr-defined]
+                return arr
+        except Exception:  # pragma: no cover - pinned memory is an optimisation only
+            pass
+    return np.zeros(n, dtype=np.float64)
+
+
+def _ptr(a: np.ndarray) -> int:
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+PRECISIONS = {"fp64": N.TFS_FP64, "fp32c": N.TFS_FP32C}
+
+
+class RpyMobilitySolver:
+    """RPY mobility solver on one GB300.
+
+    nswim, nfil, nseg, nblob: NSWIM, NFIL, NSEG, NBLOB of the reference.
+    precision: "fp64" (plain FP64, the parity form) or "fp32c" (FP32 pairwise
+    sums with compensated accumulation).
+    """
+
+    def __init__(self, nswim: int, nfil: int, nseg: int, nblob: int, precision: str = "fp64",
+                 mu: float = 1.0, a_seg: float = 1.0, a_blob: float = 1.0,
+                 end_force_magnitude: int | None = None, repulsive_force_factor: float = 2.0,
+                 free_body: bool = True, pinned: bool = True):
+        self.lib = N.load()
+        cfg = N.Config()
+        N.check(self.lib.tfs_config_default(ctypes.byref(cfg), nswim, nfil, nseg, nblob))
+        cfg.mu, cfg.a_seg, cfg.a_blob = mu, a_seg, a_blob
+        if end_force_magnitude is not None:
+            cfg.end_force_magnitude = int(end_force_magnitude)
+        cfg.repulsive_force_factor = repulsive_force_factor
+        cfg.free_body = int(bool(free_body))
+        cfg.precision = PRECISIONS[precision]
+        self.cfg = cfg
+        self.precision = precision
+        self.num_segs = nswim * nfil * nseg
+        self.num_blobs = nswim * nblob
+        self._pinned = pinned
+        self._h = None
+        self.initialise()
+
+    # -- allocate_host_memory / allocate_device_memory (rpy_mobility_solver.cu:54-117)
+    def initialise(self) -> None:
+        if self._h is not None:
+            return
+        h = ctypes.c_void_p()
+        N.check(self.lib.tfs_solver_create(ctypes.byref(self.cfg), ctypes.byref(h)))
+        self._h = h
+        ns, nb, pin = self.num_segs, self.num_blobs, self._pinned
+        self.x_segs_host = _host_array(3 * ns, pin)
+        self.f_segs_host = _host_array(6 * ns, pin)
+        self.v_segs_host = _host_array(6 * ns, pin)
+        self.x_blobs_host = _host_array(3 * nb, pin)
+        self.f_blobs_host = _host_array(3 * nb, pin)
+        self.v_blobs_host = _host_array(3 * nb, pin)
+        self.f_blobs_repulsion_host = _host_array(3 * nb, pin)
+
+    # -- free_host_memory / free_device_memory
+    def finalise(self) -> None:
+        if self._h is not None:
+            self.lib.tfs_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.finalise()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.finalise()
+
+    def _call(self, name: str, *args) -> None:
+        if self._h is None:
+            raise N.TfsError(N.TFS_ESTATE, "solver has been finalised")
+        N.check(getattr(self.lib, name)(self._h, *args))
+
+    # -- configuration
+    def set_stream(self, stream: int | None) -> None:
+        """Run on a cudaStream_t handle (e.g. torch.cuda.current_stream().cuda_stream)."""
+        self._call("tfs_solver_set_stream", ctypes.c_void_p(stream or 0))
+
+    def set_precision(self, precision: str) -> None:
+        self._call("tfs_solver_set_precision", PRECISIONS[precision])
+        self.precision = precision
+
+    def device_arrays(self) -> dict:
+        """Device buffers as __cuda_array_interface__ views (float64, AoS)."""
+        b = N.DeviceBuffers()
+        self._call("tfs_solver_device_buffers", ctypes.byref(b))
+        ns, nb = self.num_segs, self.num_blobs
+        sizes = dict(x_segs=3 * ns, f_segs=6 * ns, v_segs=6 * ns, x_blobs=3 * nb,
+                     f_blobs=3 * nb, v_blobs=3 * nb, f_blobs_repulsion=3 * nb)
+        return {k: _DeviceArray(getattr(b, k), n, self) for k, n in sizes.items()}
+
+    def enable_kernel_timing(self, enable: bool = True) -> None:
+        self._call("tfs_solver_enable_kernel_timing", int(bool(enable)))
+
+    def kernel_timing(self) -> list[float]:
+        """Durations (ms) of the RPY tile-kernel launches since the last call,
+        in launch order."""
+        buf = (ctypes.c_double * 4096)()
+        n = ctypes.c_int()
+        self._call("tfs_solver_kernel_timing", buf, 4096, ctypes.byref(n))
+        return list(buf[:min(n.value, 4096)])
+
+    def positions_updated(self) -> None:
+        self._call("tfs_solver_positions_updated")
+
+    # -- the hooks (mobility_solver.hpp:26-46)
+    def copy_segment_positions_to_device(self):
+        self._call("tfs_copy_segment_positions_to_device", _ptr(self.x_segs_host))
+
+    def copy_segment_forces_to_device(self):
+        self._call("tfs_copy_segment_forces_to_device", _ptr(self.f_segs_host))
+
+    def copy_blob_positions_to_device(self):
+        self._call("tfs_copy_blob_positions_to_device", _ptr(self.x_blobs_host))
+
+    def copy_blob_forces_to_device(self):
+        self._call("tfs_copy_blob_forces_to_device", _ptr(self.f_blobs_host))
+
+    def copy_interparticle_blob_forces_to_host(self):
+        self._call("tfs_copy_interparticle_blob_forces_to_host", _ptr(self.f_blobs_repulsion_host))
+
+    def copy_blob_velocities_to_host(self):
+        self._call("tfs_copy_blob_velocities_to_host", _ptr(self.v_blobs_host))
+
+    def copy_segment_velocities_to_host(self):
+        self._call("tfs_copy_segment_velocities_to_host", _ptr(self.v_segs_host))
+
+    def apply_interparticle_forces(self):
+        self._call("tfs_apply_interparticle_forces")
+
+    def wait_for_device(self):
+        self._call("tfs_wait_for_device")
+
+    def evaluate_segment_segment_mobility(self):
+        self._call("tfs_evaluate_segment_segment_mobility")
+
+    def evaluate_segment_blob_mobility(self):
+        self._call("tfs_evaluate_segment_blob_mobility")
+
+    def evaluate_blob_blob_mobility(self):
+        self._call("tfs_evaluate_blob_blob_mobility")
+
+    def evaluate_blob_segment_mobility(self):
+        self._call("tfs_evaluate_blob_segment_mobility")
+
+    def evaluate_full_mobility(self):
+        """rpy_mobility_solver.cu:330-337, including its D2H copies."""
+        self._call("tfs_evaluate_full_mobility", _ptr(self.v_segs_host), _ptr(self.v_blobs_host))
+
+    def apply_grand_mobility(self):
+        """v_segs = Mss f_segs + Msb f_blobs; v_blobs = Mbs f_segs + Mbb f_blobs."""
+        self._call("tfs_apply_grand_mobility")
+
+    # -- convenience: set all inputs from arrays (AoS float64)
+    def set_state(self, x_segs, f_segs, x_blobs, f_blobs) -> None:
+        self.x_segs_host[:] = np.asarray(x_segs, dtype=np.float64).ravel()
+        self.f_segs_host[:] = np.asarray(f_segs, dtype=np.float64).ravel()
+        self.x_blobs_host[:] = np.asarray(x_blobs, dtype=np.float64).ravel()
+        self.f_blobs_host[:] = np.asarray(f_blobs, dtype=np.float64).ravel()
+        self.copy_segment_positions_to_device()
+        self.copy_segment_forces_to_device()
+        self.copy_blob_positions_to_device()
+        self.copy_blob_forces_to_device()
+
+
+def measure_fma_peak(precision: str = "fp64") -> float:
+    """FMA throughput of the current device, FLOP/s (2 per FMA)."""
+    lib = N.load()
+    out = ctypes.c_double()
+    N.check(lib.tfs_measure_fma_peak(PRECISIONS[precision], ctypes.byref(out)))
+    return out.value
+
+
+def kernel_launch_count() -> int:
+    return int(N.load().tfs_kernel_launch_count())
