@@ -136,7 +136,9 @@ def bench_ours(args):
 
     sw = make_config(args.config, seed=1234 + rank)
     ns, nb = sw.num_segs, sw.num_blobs
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the solver and every timing event run on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
 
     def make(precision):
         s = RpyMobilitySolver(1, sw.nfil, sw.nseg, nb, precision=precision)
