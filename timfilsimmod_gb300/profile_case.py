@@ -1,0 +1,44 @@
+"""Run a few grand-mobility products of one synthetic swimmer, for profiling.
+
+    python -m timfilsimmod_gb300.profile_case --config medium --precision fp32c --reps 2
+
+Each repetition is one tfs_apply_grand_mobility call (pack, tile and reduce
+kernels). Meant to be run under `ncu -k regex:rpy_tile_kernel -c N`.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+from .geometry import make_config
+from .mobility import RpyMobilitySolver
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--config", default="medium")
+    p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
+    p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier"])
+    args = p.parse_args()
+    sw = make_config(args.config, seed=1)
+    s = RpyMobilitySolver(1, sw.nfil, sw.nseg, sw.num_blobs, precision=args.precision)
+    s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
+    t0 = time.perf_counter()
+    for _ in range(args.reps):
+        if args.op == "grand":
+            s.apply_grand_mobility()
+        elif args.op == "mss":
+            s.evaluate_segment_segment_mobility()
+        elif args.op == "mbb":
+            s.evaluate_blob_blob_mobility()
+        else:
+            s.apply_interparticle_forces()
+    s.wait_for_device()
+    dt = time.perf_counter() - t0
+    print(f"{args.reps} x {args.op} ({args.precision}, {args.config}): {dt * 1e3:.2f} ms")
+    s.finalise()
+
+
+if __name__ == "__main__":
+    main()
