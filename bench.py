@@ -140,10 +140,17 @@ def bench_ours(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
 
+    tuning = {}
+
     def make(precision):
         s = RpyMobilitySolver(1, sw.nfil, sw.nseg, nb, precision=precision)
         s.set_stream(stream.cuda_stream)
         s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
+        if not args.no_tune:
+            # pick the tile-kernel launch variant per block for these sizes
+            table = s.autotune((precision,), reps=2 if precision == "fp32c" else 1)[precision]
+            tuning[precision] = {k: [v["block"], v["tpt"], v["ts"], v["ctas_per_sm"]]
+                                 for k, v in table.items()}
         return s
 
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
@@ -290,6 +297,8 @@ def bench_ours(args):
             "rel_l2_error_vs_fp64": err,
             "clocks": clocks,
             "gpu_launches": launches,
+            "tuning": {"columns": ["threads/CTA", "targets/thread", "sources/tile",
+                                   "CTAs/SM target"], **tuning},
         }
         if cpu is not None:
             result["cpu_baseline"] = cpu
@@ -394,6 +403,7 @@ def main():
     p.add_argument("--cpu-sample", type=int, default=16,
                    help="CPU legs use every n-th target of the workload")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-tune", action="store_true", help="skip the launch autotuner")
     args = p.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

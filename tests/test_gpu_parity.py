@@ -220,3 +220,49 @@ def test_native_library_is_loaded_and_counts_launches():
     assert kernel_launch_count() > before
     maps = open("/proc/self/maps").read()
     assert os.path.basename(_native.lib_path()) in maps
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_every_launch_variant_matches_reference(precision):
+    """Every compiled tile-kernel variant, at two split targets, on the ragged
+    unequal-radius case (all branches) and on the small swimmer."""
+    from timfilsimmod_gb300.mobility import num_tile_variants
+
+    for case in ("overlap_a16", "small_matvec"):
+        d = load(case)
+        xs, fs, xb, fb = d["x_segs"], d["f_segs"], d["x_blobs"], d["f_blobs"]
+        s = make_solver(xs.shape[0], xb.shape[0], int(d["nseg"]), precision=precision,
+                        a_seg=float(d["a_seg"]), a_blob=float(d["a_blob"]))
+        for var in range(num_tile_variants(precision)):
+            for cps in (1, 8):
+                for combo in range(6):
+                    s.set_tuning(combo, var, cps)
+                out = run_blocks(s, xs, fs, xb, fb)
+                s.apply_grand_mobility()
+                s.copy_segment_velocities_to_host()
+                s.copy_blob_velocities_to_host()
+                s.wait_for_device()
+                gs, gb = s.v_segs_host.copy(), s.v_blobs_host.copy()
+                ref = {"v_mss": d["v_mss"], "v_mbb": d["v_mbb"], "v_mbs": d["v_mbs"],
+                       "v_mss_plus_msb": d["v_mss"] + d["v_msb"]}
+                for k, r in ref.items():
+                    e = rel_max(out[k], r) if precision == "fp64" else rel_l2(out[k], r)
+                    assert e < (TOL64 if precision == "fp64" else TOL32), (case, var, cps, k, e)
+                eg = (rel_max if precision == "fp64" else rel_l2)(
+                    np.concatenate([gs, gb]),
+                    np.concatenate([d["v_mss"] + d["v_msb"], d["v_mbs"] + d["v_mbb"]]))
+                assert eg < (TOL64 if precision == "fp64" else TOL32), (case, var, cps, "grand", eg)
+        s.finalise()
+
+
+def test_autotune_table_and_parity():
+    d = load("small_matvec")
+    xs, fs, xb, fb = d["x_segs"], d["f_segs"], d["x_blobs"], d["f_blobs"]
+    s = make_solver(xs.shape[0], xb.shape[0], int(d["nseg"]))
+    s.set_state(xs, fs, xb, fb)
+    table = s.autotune(reps=1)
+    assert set(table) == {"fp64", "fp32c"}
+    assert "seg<-seg" in table["fp64"] and table["fp64"]["seg<-seg"]["ms"] > 0
+    out = run_blocks(s, xs, fs, xb, fb)
+    s.finalise()
+    assert rel_max(out["v_mss"], d["v_mss"]) < TOL64

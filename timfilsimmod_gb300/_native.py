@@ -78,6 +78,11 @@ _SIGNATURES = {
     "tfs_solver_enable_kernel_timing": [_H, ctypes.c_int],
     "tfs_solver_kernel_timing": [_H, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
                                  ctypes.POINTER(ctypes.c_int)],
+    "tfs_solver_autotune": [_H, ctypes.c_int, ctypes.c_int],
+    "tfs_solver_tuning_report": [_H, ctypes.c_char_p, ctypes.c_size_t,
+                                 ctypes.POINTER(ctypes.c_size_t)],
+    "tfs_solver_set_tuning": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+    "tfs_num_tile_variants": [ctypes.c_int],
     "tfs_last_error": [],
     "tfs_kernel_launch_count": [],
     "tfs_measure_fma_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],

@@ -25,29 +25,11 @@
 
 #include <algorithm>
 
+#include "rpy_tile.cuh"
 #include "tfs_device.cuh"
 #include "tfs_kernels.h"
 
 namespace tfs {
-
-template <typename T, int FD>
-struct Rec;
-template <>
-struct Rec<double, 6> {
-  static constexpr int len = 10;
-};
-template <>
-struct Rec<double, 3> {
-  static constexpr int len = 6;
-};
-template <>
-struct Rec<float, 6> {
-  static constexpr int len = 12;
-};
-template <>
-struct Rec<float, 3> {
-  static constexpr int len = 8;
-};
 
 // ---------------------------------------------------------------------------
 // Origin/extent of a particle set: origin = mean position, extent = max over
@@ -118,156 +100,6 @@ __global__ void pack_sources_kernel(T *__restrict__ rec, const double *__restric
   for (int k = 0; k < FD; ++k) r[3 + k] = T(f[(size_t)FD * i + k]);
 #pragma unroll
   for (int k = 3 + FD; k < L; ++k) r[k] = T(0);
-}
-
-// ---------------------------------------------------------------------------
-// Accumulator: plain sum for FP64; FP32 tile sums folded into a (hi, lo)
-// pair by TwoSum after every tile (compensated accumulation).
-// ---------------------------------------------------------------------------
-template <typename T, int VD>
-struct Acc;
-
-template <int VD>
-struct Acc<double, VD> {
-  double v[VD];
-  __device__ void zero() {
-#pragma unroll
-    for (int k = 0; k < VD; ++k) v[k] = 0.0;
-  }
-  __device__ double *tile() { return v; }
-  __device__ void fold() {}
-  __device__ double get(int k) const { return v[k]; }
-};
-
-template <int VD>
-struct Acc<float, VD> {
-  float v[VD], hi[VD], lo[VD];
-  __device__ void zero() {
-#pragma unroll
-    for (int k = 0; k < VD; ++k) v[k] = hi[k] = lo[k] = 0.f;
-  }
-  __device__ float *tile() { return v; }
-  __device__ void fold() {
-#pragma unroll
-    for (int k = 0; k < VD; ++k) {
-      two_sum(hi[k], lo[k], v[k]);
-      v[k] = 0.f;
-    }
-  }
-  __device__ double get(int k) const { return (double)hi[k] + (double)lo[k]; }
-};
-
-template <typename T>
-__device__ __forceinline__ T load_target(const double *x, int i, int k, const double *origin) {
-  return T(x[3 * (size_t)i + k] - (origin ? origin[k] : 0.0));
-}
-
-// Sum the sources [lo, hi) of one record array into the accumulators.
-template <typename T, int VD, int FD, int BLOCK, int TPT, int TS>
-__device__ __forceinline__ void sum_source_range(Acc<T, VD> (&acc)[TPT], const T (&xt)[TPT],
-                                                 const T (&yt)[TPT], const T (&zt)[TPT],
-                                                 const T *__restrict__ rec, int lo, int hi,
-                                                 const PairConst<T> &pc, T *smem) {
-  constexpr int L = Rec<T, FD>::len;
-  constexpr int VEC_PER_REC = L * (int)sizeof(T) / 16;
-  for (int base = lo; base < hi; base += TS) {
-    const int cnt = min(TS, hi - base);
-    __syncthreads();  // previous tile fully consumed
-    const int4 *src = reinterpret_cast<const int4 *>(rec + (size_t)base * L);
-    int4 *dst = reinterpret_cast<int4 *>(smem);
-    const int nvec = cnt * VEC_PER_REC;
-    for (int q = threadIdx.x; q < nvec; q += BLOCK) dst[q] = __ldg(src + q);
-    __syncthreads();
-#pragma unroll 2
-    for (int j = 0; j < cnt; ++j) {
-      T f[FD];
-      const T *r = smem + j * L;
-      const T sx = r[0], sy = r[1], sz = r[2];
-#pragma unroll
-      for (int k = 0; k < FD; ++k) f[k] = r[3 + k];
-#pragma unroll
-      for (int t = 0; t < TPT; ++t) {
-        rpy_pair<T, VD, FD>(acc[t].tile(), xt[t] - sx, yt[t] - sy, zt[t] - sz, f, pc);
-      }
-    }
-#pragma unroll
-    for (int t = 0; t < TPT; ++t) acc[t].fold();
-  }
-}
-
-template <typename T, int VD, int FDA, int FDB, int BLOCK, int TPT, int TS>
-__global__ void __launch_bounds__(BLOCK) rpy_tile_kernel(const TileArgs args) {
-  constexpr int LA = Rec<T, FDA>::len;
-  constexpr int LB = FDB > 0 ? Rec<T, (FDB > 0 ? FDB : 3)>::len : 0;
-  constexpr int LMAX = LA > LB ? LA : LB;
-  __shared__ __align__(16) T smem[TS * LMAX];
-
-  const int n_tgt = args.n_tgt;
-  const double *origin = args.fp32 ? args.origin : nullptr;
-  const int tile0 = blockIdx.x * BLOCK * TPT;
-
-  T xt[TPT], yt[TPT], zt[TPT];
-  Acc<T, VD> acc[TPT];
-#pragma unroll
-  for (int t = 0; t < TPT; ++t) {
-    int i = tile0 + t * BLOCK + threadIdx.x;
-    i = i < n_tgt ? i : n_tgt - 1;  // duplicate the last target; not written
-    xt[t] = load_target<T>(args.x_tgt, i, 0, origin);
-    yt[t] = load_target<T>(args.x_tgt, i, 1, origin);
-    zt[t] = load_target<T>(args.x_tgt, i, 2, origin);
-    acc[t].zero();
-  }
-
-  const int n_src = args.n_a + args.n_b;
-  const int s0 = blockIdx.y * args.chunk;
-  const int s1 = min(s0 + args.chunk, n_src);
-
-  {
-    PairConst<T> pc;
-    pc.ai = T(args.a_tgt);
-    pc.aj = T(args.a_a);
-    pc.asum2 = T((args.a_tgt + args.a_a) * (args.a_tgt + args.a_a));
-    pc.s = T((args.a_tgt * args.a_tgt + args.a_a * args.a_a) / 3.0);
-    pc.s3 = T(-(args.a_tgt * args.a_tgt + args.a_a * args.a_a));
-    const int lo = min(s0, args.n_a), hi = min(s1, args.n_a);
-    if (lo < hi)
-      sum_source_range<T, VD, FDA, BLOCK, TPT, TS>(acc, xt, yt, zt,
-                                                   reinterpret_cast<const T *>(args.src_a), lo,
-                                                   hi, pc, smem);
-  }
-  if constexpr (FDB > 0) {
-    PairConst<T> pc;
-    pc.ai = T(args.a_tgt);
-    pc.aj = T(args.a_b);
-    pc.asum2 = T((args.a_tgt + args.a_b) * (args.a_tgt + args.a_b));
-    pc.s = T((args.a_tgt * args.a_tgt + args.a_b * args.a_b) / 3.0);
-    pc.s3 = T(-(args.a_tgt * args.a_tgt + args.a_b * args.a_b));
-    const int lo = max(s0 - args.n_a, 0), hi = max(s1 - args.n_a, 0);
-    if (lo < hi)
-      sum_source_range<T, VD, FDB, BLOCK, TPT, TS>(acc, xt, yt, zt,
-                                                   reinterpret_cast<const T *>(args.src_b), lo,
-                                                   hi, pc, smem);
-  }
-
-  const double c = args.scale;
-#pragma unroll
-  for (int t = 0; t < TPT; ++t) {
-    const int i = tile0 + t * BLOCK + threadIdx.x;
-    if (i >= n_tgt) continue;
-    if (args.mode == OUT_PARTIAL) {
-      double *o = args.out + ((size_t)blockIdx.y * n_tgt + i) * VD;
-#pragma unroll
-      for (int k = 0; k < VD; ++k) o[k] = c * acc[t].get(k);
-    } else if (args.mode == OUT_ACCUMULATE) {
-      double *o = args.out + (size_t)i * VD;
-#pragma unroll
-      for (int k = 0; k < VD; ++k) o[k] += c * acc[t].get(k);
-    } else {
-      double *o = args.out + (size_t)i * VD;
-#pragma unroll
-      for (int k = 0; k < VD; ++k) o[k] = c * acc[t].get(k);
-    }
-  }
 }
 
 // out[i] (= or +=) sum over splits of partial[s][i], s in order.
@@ -417,85 +249,71 @@ size_t record_bytes(int fp32, int fd) {
   return fd == 6 ? 80 : 48;
 }
 
-// Launch geometry per precision: FP64 is bound by the FP64 pipe, so one
-// target per thread and enough source splits to give every SM several
-// warps; FP32 register-blocks two targets per thread.
-template <typename T>
-struct Geom;
-template <>
-struct Geom<double> {
-  static constexpr int BLOCK = 128, TPT = 1, TS = 128;
-};
-template <>
-struct Geom<float> {
-  static constexpr int BLOCK = 128, TPT = 2, TS = 256;
-};
+int combo_of(int vd, int fda, int fdb) {
+  if (vd == 6 && fda == 6 && fdb == 0) return C_SS;
+  if (vd == 6 && fda == 3 && fdb == 0) return C_SB;
+  if (vd == 3 && fda == 3 && fdb == 0) return C_BB;
+  if (vd == 3 && fda == 6 && fdb == 0) return C_BS;
+  if (vd == 6 && fda == 6 && fdb == 3) return C_SX;
+  if (vd == 3 && fda == 6 && fdb == 3) return C_BX;
+  return -1;
+}
 
-// Choose the number of source splits: aim for ~`waves` CTAs per SM with at
-// least `min_chunk` sources per split.
-static int choose_splits(int target_ctas, int n_src, int max_splits, int min_chunk) {
-  const int want = std::max(1, (4 * num_sms() + target_ctas - 1) / target_ctas);
-  int s = std::min(want, max_splits);
-  s = std::min(s, std::max(1, n_src / std::max(1, min_chunk)));
+// Source splits for a launch of `ctas` target CTAs over n_src sources: aim
+// for ctas_per_sm CTAs on every SM, with at least two tiles per split.
+static int choose_splits(int ctas, int n_src, int ctas_per_sm, int ts) {
+  const int want = std::max(1, (ctas_per_sm * num_sms() + ctas - 1) / ctas);
+  int s = std::min(want, kMaxSplits);
+  s = std::min(s, std::max(1, n_src / std::max(1, 2 * ts)));
   return std::max(1, s);
 }
 
-template <typename T, int VD, int FDA, int FDB>
-static cudaError_t tile_t(TileArgs a, double *scratch, size_t scratch_elems, int mode,
-                          cudaStream_t st, cudaEvent_t *ev) {
-  using G = Geom<T>;
-  constexpr int per_cta = G::BLOCK * G::TPT;
+cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuning tune,
+                        double *scratch, size_t scratch_elems, int mode, cudaStream_t st,
+                        cudaEvent_t *ev) {
+  TileArgs a = a_in;
+  const int combo = combo_of(vd, fda, fdb);
+  if (combo < 0) return cudaErrorInvalidValue;
+  const int nvar = a.fp32 ? kNumVariantsF32 : kNumVariantsF64;
+  if (tune.variant < 0 || tune.variant >= nvar) tune.variant = 0;
+  if (tune.ctas_per_sm <= 0) tune.ctas_per_sm = 4;
+  const TileVariant var = a.fp32 ? g_variants_f32[tune.variant] : g_variants_f64[tune.variant];
+  const TileFn fn = a.fp32 ? g_tile_f32[tune.variant][combo] : g_tile_f64[tune.variant][combo];
+  if (a.n_tgt <= 0) return cudaSuccess;
+  const int per_cta = var.block * var.tpt;
   const int ctas = (a.n_tgt + per_cta - 1) / per_cta;
   const int n_src = a.n_a + a.n_b;
-  if (a.n_tgt <= 0) return cudaSuccess;
-  int splits = a.splits > 0 ? a.splits : choose_splits(ctas, n_src, kMaxSplits, 2 * G::TS);
-  if ((size_t)splits * a.n_tgt * VD > scratch_elems) splits = 1;
+  int splits = a.splits > 0 ? std::min(a.splits, kMaxSplits)
+                            : choose_splits(ctas, n_src, tune.ctas_per_sm, var.ts);
+  if ((size_t)splits * a.n_tgt * vd > scratch_elems) splits = 1;
   if (n_src == 0) splits = 1;
   int chunk = (n_src + splits - 1) / splits;
-  chunk = ((chunk + G::TS - 1) / G::TS) * G::TS;
-  if (chunk == 0) chunk = G::TS;
+  chunk = ((chunk + var.ts - 1) / var.ts) * var.ts;
+  if (chunk == 0) chunk = var.ts;
   splits = std::max(1, (n_src + chunk - 1) / chunk);
   a.chunk = chunk;
-  dim3 grid(ctas, splits);
+  const dim3 grid(ctas, splits);
+  cudaError_t e;
   if (ev) cudaEventRecord(ev[0], st);
   if (splits == 1) {
     a.mode = mode;
-    rpy_tile_kernel<T, VD, FDA, FDB, G::BLOCK, G::TPT, G::TS><<<grid, G::BLOCK, 0, st>>>(a);
+    e = fn(a, grid, st);
     count_launch();
     if (ev) cudaEventRecord(ev[1], st);
-    return cudaGetLastError();
+    return e;
   }
   double *final_out = a.out;
   a.mode = OUT_PARTIAL;
   a.out = scratch;
-  rpy_tile_kernel<T, VD, FDA, FDB, G::BLOCK, G::TPT, G::TS><<<grid, G::BLOCK, 0, st>>>(a);
+  e = fn(a, grid, st);
   count_launch();
   if (ev) cudaEventRecord(ev[1], st);
-  const int n_elems = a.n_tgt * VD;
+  if (e != cudaSuccess) return e;
+  const int n_elems = a.n_tgt * vd;
   reduce_partials_kernel<<<(n_elems + 255) / 256, 256, 0, st>>>(
       final_out, scratch, n_elems, splits, mode == OUT_ACCUMULATE ? 1 : 0);
   count_launch();
   return cudaGetLastError();
-}
-
-cudaError_t launch_tile(const TileArgs &a, int vd, int fda, int fdb, double *scratch,
-                        size_t scratch_elems, int mode, cudaStream_t st, cudaEvent_t *ev) {
-  if (a.fp32) {
-    if (vd == 6 && fda == 6 && fdb == 0) return tile_t<float, 6, 6, 0>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 6 && fda == 3 && fdb == 0) return tile_t<float, 6, 3, 0>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 3 && fda == 3 && fdb == 0) return tile_t<float, 3, 3, 0>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 3 && fda == 6 && fdb == 0) return tile_t<float, 3, 6, 0>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 6 && fda == 6 && fdb == 3) return tile_t<float, 6, 6, 3>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 3 && fda == 6 && fdb == 3) return tile_t<float, 3, 6, 3>(a, scratch, scratch_elems, mode, st, ev);
-  } else {
-    if (vd == 6 && fda == 6 && fdb == 0) return tile_t<double, 6, 6, 0>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 6 && fda == 3 && fdb == 0) return tile_t<double, 6, 3, 0>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 3 && fda == 3 && fdb == 0) return tile_t<double, 3, 3, 0>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 3 && fda == 6 && fdb == 0) return tile_t<double, 3, 6, 0>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 6 && fda == 6 && fdb == 3) return tile_t<double, 6, 6, 3>(a, scratch, scratch_elems, mode, st, ev);
-    if (vd == 3 && fda == 6 && fdb == 3) return tile_t<double, 3, 6, 3>(a, scratch, scratch_elems, mode, st, ev);
-  }
-  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st) {

@@ -1,0 +1,14 @@
+// rpy_tile_f64.cu -- FP64 instantiations of the tile kernel.
+#include "rpy_tile.cuh"
+
+namespace tfs {
+
+// (threads per CTA, targets per thread, sources per tile); index = variant.
+const TileVariant g_variants_f64[kNumVariantsF64] = {
+    {128, 1, 128}, {64, 1, 128}, {128, 2, 128}, {256, 1, 128}};
+
+const TileFn g_tile_f64[kNumVariantsF64][kNumCombos] = {
+    TFS_TILE_ROW(double, 128, 1, 128), TFS_TILE_ROW(double, 64, 1, 128),
+    TFS_TILE_ROW(double, 128, 2, 128), TFS_TILE_ROW(double, 256, 1, 128)};
+
+}  // namespace tfs

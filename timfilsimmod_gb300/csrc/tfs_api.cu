@@ -54,6 +54,9 @@ struct tfs_solver {
   double *scratch = nullptr;
   size_t scratch_elems = 0;
   bool origin_dirty = true;
+  // launch tuning per precision and (target, source-set) combination
+  TileTuning tune[2][kNumCombos];
+  std::string tuning_report = "{}";
   // dominant-kernel timing (tfs_solver_enable_kernel_timing)
   bool timing = false;
   std::vector<cudaEvent_t> events;  // pairs, in launch order
@@ -177,8 +180,10 @@ static int product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, 
                "cudaMemsetAsync");
     return TFS_OK;
   }
-  cudaError_t e = launch_tile(a, tgt_segs ? 6 : 3, fda, fdb, s->scratch, s->scratch_elems, mode,
-                              s->stream, next_events(s));
+  const int combo = combo_of(tgt_segs ? 6 : 3, fda, fdb);
+  const TileTuning tune = s->tune[s->cfg.precision == TFS_FP32C][combo];
+  cudaError_t e = launch_tile(a, tgt_segs ? 6 : 3, fda, fdb, tune, s->scratch, s->scratch_elems,
+                              mode, s->stream, next_events(s));
   if (e != cudaSuccess) return cuda_fail(e, "RPY tile kernel");
   return TFS_OK;
 }
@@ -223,6 +228,8 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
   tfs_solver *s = new (std::nothrow) tfs_solver;
   if (s == nullptr) return fail(TFS_ENOMEM, "host allocation failed");
   s->cfg = *cfg;
+  for (int p = 0; p < 2; ++p)
+    for (int c = 0; c < kNumCombos; ++c) s->tune[p][c] = TileTuning{0, 4};
   s->ns = (int)ns;
   s->nb = (int)nb;
   cudaGetDevice(&s->device);
@@ -437,8 +444,9 @@ int tfs_apply_grand_mobility(tfs_solver *s) {
       a.src_b = s->rec_blobs;
       a.n_b = s->nb;
       a.a_b = s->cfg.a_blob;
-      cudaError_t e = launch_tile(a, 3, 6, 3, s->scratch, s->scratch_elems, OUT_ASSIGN, s->stream,
-                                  next_events(s));
+      const TileTuning tune = s->tune[s->cfg.precision == TFS_FP32C][C_BX];
+      cudaError_t e = launch_tile(a, 3, 6, 3, tune, s->scratch, s->scratch_elems, OUT_ASSIGN,
+                                  s->stream, next_events(s));
       if (e != cudaSuccess) return cuda_fail(e, "RPY tile kernel");
     } else if ((rc = product(s, false, false, true, OUT_ASSIGN)) != TFS_OK) {
       return rc;
@@ -467,6 +475,140 @@ int tfs_solver_kernel_timing(tfs_solver *s, double *ms, int capacity, int *launc
   }
   *launches = n;
   s->events_used = 0;
+  return TFS_OK;
+}
+
+static const char *combo_name(int c) {
+  static const char *names[kNumCombos] = {"seg<-seg", "seg<-blob", "blob<-blob", "blob<-seg",
+                                          "seg<-seg+blob", "blob<-seg+blob"};
+  return names[c];
+}
+
+// Time every (variant, CTAs-per-SM) candidate of every combination the
+// solver uses, on its current positions and forces, and keep the fastest.
+int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
+  TFS_CHECK_SOLVER(s);
+  if (reps <= 0) reps = 2;
+  const int saved_precision = s->cfg.precision;
+  const bool saved_timing = s->timing;
+  s->timing = false;
+  static const int kCps[] = {1, 2, 4, 8};
+  cudaEvent_t e0, e1;
+  TFS_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
+  TFS_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
+  std::string report = "{";
+  int rc = TFS_OK;
+  for (int p = 0; p < 2 && rc == TFS_OK; ++p) {
+    if (!(precision_mask & (1 << p))) continue;
+    s->cfg.precision = p;  // TFS_FP64 = 0, TFS_FP32C = 1
+    if (p == TFS_FP32C && (rc = ensure_origin(s)) != TFS_OK) break;
+    if (s->ns > 0 && (rc = pack(s, 1)) != TFS_OK) break;
+    if (s->nb > 0 && (rc = pack(s, 0)) != TFS_OK) break;
+    if (report.size() > 1) report += ",";
+    report += std::string("\"") + (p ? "fp32c" : "fp64") + "\":{";
+    bool first_combo = true;
+    for (int c = 0; c < kNumCombos && rc == TFS_OK; ++c) {
+      const bool tgt_segs = (c == C_SS || c == C_SB || c == C_SX);
+      const bool src_segs = (c != C_SB && c != C_BB);
+      const bool src_blobs = (c == C_SB || c == C_BB || c == C_SX || c == C_BX);
+      if ((tgt_segs ? s->ns : s->nb) == 0 || (src_segs && s->ns == 0) ||
+          (src_blobs && s->nb == 0))
+        continue;
+      TileArgs a = base_args(s);
+      a.x_tgt = tgt_segs ? s->x_segs : s->x_blobs;
+      a.n_tgt = tgt_segs ? s->ns : s->nb;
+      a.a_tgt = tgt_segs ? s->cfg.a_seg : s->cfg.a_blob;
+      a.out = tgt_segs ? s->v_segs : s->v_blobs;
+      int fda, fdb = 0;
+      if (src_segs) {
+        a.src_a = s->rec_segs; a.n_a = s->ns; a.a_a = s->cfg.a_seg; fda = 6;
+        if (src_blobs) { a.src_b = s->rec_blobs; a.n_b = s->nb; a.a_b = s->cfg.a_blob; fdb = 3; }
+      } else {
+        a.src_a = s->rec_blobs; a.n_a = s->nb; a.a_a = s->cfg.a_blob; fda = 3;
+      }
+      const int vd = tgt_segs ? 6 : 3;
+      const int nvar = p ? kNumVariantsF32 : kNumVariantsF64;
+      float best_ms = 1e30f;
+      TileTuning best{0, 4};
+      std::string cands;
+      for (int v = 0; v < nvar && rc == TFS_OK; ++v) {
+        for (int cps : kCps) {
+          TileTuning t{v, cps};
+          cudaError_t e = launch_tile(a, vd, fda, fdb, t, s->scratch, s->scratch_elems, OUT_ASSIGN,
+                                      s->stream);  // warm-up
+          cudaEventRecord(e0, s->stream);
+          for (int r = 0; r < reps && e == cudaSuccess; ++r)
+            e = launch_tile(a, vd, fda, fdb, t, s->scratch, s->scratch_elems, OUT_ASSIGN,
+                            s->stream);
+          cudaEventRecord(e1, s->stream);
+          if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+          if (e != cudaSuccess) {
+            rc = cuda_fail(e, "autotune launch");
+            break;
+          }
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          ms /= reps;
+          const TileVariant tv = p ? g_variants_f32[v] : g_variants_f64[v];
+          char buf[96];
+          snprintf(buf, sizeof buf, "%s[%d,%d,%d,%d,%.4f]", cands.empty() ? "" : ",", tv.block,
+                   tv.tpt, tv.ts, cps, ms);
+          cands += buf;
+          if (ms < best_ms) {
+            best_ms = ms;
+            best = t;
+          }
+        }
+      }
+      if (rc != TFS_OK) break;
+      s->tune[p][c] = best;
+      const TileVariant bv = p ? g_variants_f32[best.variant] : g_variants_f64[best.variant];
+      char buf[256];
+      snprintf(buf, sizeof buf,
+               "%s\"%s\":{\"block\":%d,\"tpt\":%d,\"ts\":%d,\"ctas_per_sm\":%d,\"ms\":%.4f,"
+               "\"candidates\":[",
+               first_combo ? "" : ",", combo_name(c), bv.block, bv.tpt, bv.ts, best.ctas_per_sm,
+               best_ms);
+      report += buf;
+      report += cands + "]}";
+      first_combo = false;
+    }
+    report += "}";
+  }
+  report += "}";
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  s->cfg.precision = saved_precision;
+  s->timing = saved_timing;
+  if (rc == TFS_OK) s->tuning_report = report;
+  return rc;
+}
+
+int tfs_solver_set_tuning(tfs_solver *s, int precision, int combo, int variant, int ctas_per_sm) {
+  TFS_CHECK_SOLVER(s);
+  if (precision != TFS_FP64 && precision != TFS_FP32C)
+    return fail(TFS_EINVAL, "unknown precision %d", precision);
+  if (combo < 0 || combo >= kNumCombos) return fail(TFS_EINVAL, "combination %d out of range", combo);
+  const int nvar = precision == TFS_FP32C ? kNumVariantsF32 : kNumVariantsF64;
+  if (variant < 0 || variant >= nvar) return fail(TFS_EINVAL, "variant %d out of range", variant);
+  if (ctas_per_sm < 1 || ctas_per_sm > 64) return fail(TFS_EINVAL, "ctas_per_sm out of range");
+  s->tune[precision][combo] = TileTuning{variant, ctas_per_sm};
+  return TFS_OK;
+}
+
+int tfs_num_tile_variants(int precision) {
+  return precision == TFS_FP32C ? kNumVariantsF32 : kNumVariantsF64;
+}
+
+int tfs_solver_tuning_report(tfs_solver *s, char *buf, size_t len, size_t *needed) {
+  TFS_CHECK_SOLVER(s);
+  const size_t n = s->tuning_report.size() + 1;
+  if (needed) *needed = n;
+  if (buf != nullptr && len > 0) {
+    const size_t k = std::min(len - 1, s->tuning_report.size());
+    std::memcpy(buf, s->tuning_report.data(), k);
+    buf[k] = 0;
+  }
   return TFS_OK;
 }
 

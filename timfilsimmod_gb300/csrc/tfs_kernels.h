@@ -45,6 +45,31 @@ struct BarrierArgs {
   int target_blobs;           // set by the launcher
 };
 
+// Launch variants of the tile kernel and their dispatch tables
+// (rpy_tile_f32.cu, rpy_tile_f64.cu).
+struct TileVariant {
+  int block, tpt, ts;  // threads per CTA, targets per thread, sources per tile
+};
+// (target kind, source sets): 0 = seg<-seg, 1 = seg<-blob, 2 = blob<-blob,
+// 3 = blob<-seg, 4 = seg<-(seg,blob), 5 = blob<-(seg,blob)
+enum TileCombo { C_SS = 0, C_SB = 1, C_BB = 2, C_BS = 3, C_SX = 4, C_BX = 5 };
+constexpr int kNumCombos = 6;
+constexpr int kNumVariantsF32 = 6;
+constexpr int kNumVariantsF64 = 4;
+typedef cudaError_t (*TileFn)(const TileArgs &, dim3, cudaStream_t);
+extern const TileVariant g_variants_f32[kNumVariantsF32];
+extern const TileVariant g_variants_f64[kNumVariantsF64];
+extern const TileFn g_tile_f32[kNumVariantsF32][kNumCombos];
+extern const TileFn g_tile_f64[kNumVariantsF64][kNumCombos];
+
+// Tuning of one launch: variant and the number of CTAs per SM the source
+// splitting aims for.
+struct TileTuning {
+  int variant;
+  int ctas_per_sm;
+};
+int combo_of(int vd, int fda, int fdb);
+
 int num_sms();
 void count_launch();
 size_t record_bytes(int fp32, int fd);
@@ -59,8 +84,8 @@ cudaError_t launch_pack(int fp32, int fd, void *rec, const double *x, const doub
 // split launches (the launcher falls back to one split when it is smaller).
 // ev (optional): a pair of events recorded around the tile kernel itself
 // (not the pack or reduce kernels), for the dominant-kernel timing hook.
-cudaError_t launch_tile(const TileArgs &a, int vd, int fda, int fdb, double *scratch,
-                        size_t scratch_elems, int mode, cudaStream_t st,
+cudaError_t launch_tile(const TileArgs &a, int vd, int fda, int fdb, TileTuning tune,
+                        double *scratch, size_t scratch_elems, int mode, cudaStream_t st,
                         cudaEvent_t *ev = nullptr);
 cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st);
 

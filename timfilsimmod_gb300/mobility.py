@@ -147,6 +147,28 @@ class RpyMobilitySolver:
         self._call("tfs_solver_kernel_timing", buf, 4096, ctypes.byref(n))
         return list(buf[:min(n.value, 4096)])
 
+    def autotune(self, precisions=("fp64", "fp32c"), reps: int = 2) -> dict:
+        """Pick the fastest tile-kernel launch variant per block for this
+        solver's sizes (on its current data); returns the tuning table."""
+        import json
+
+        mask = sum(1 << PRECISIONS[p] for p in precisions)
+        self._call("tfs_solver_autotune", mask, int(reps))
+        return json.loads(self.tuning_report())
+
+    def set_tuning(self, combo: int, variant: int, ctas_per_sm: int = 4,
+                   precision: str | None = None) -> None:
+        """Pin the tile-kernel launch of one (target, source-set) combination."""
+        prec = PRECISIONS[precision or self.precision]
+        self._call("tfs_solver_set_tuning", prec, int(combo), int(variant), int(ctas_per_sm))
+
+    def tuning_report(self) -> str:
+        need = ctypes.c_size_t()
+        self._call("tfs_solver_tuning_report", None, 0, ctypes.byref(need))
+        buf = ctypes.create_string_buffer(need.value)
+        self._call("tfs_solver_tuning_report", buf, need.value, None)
+        return buf.value.decode()
+
     def positions_updated(self) -> None:
         self._call("tfs_solver_positions_updated")
 
@@ -216,6 +238,10 @@ def measure_fma_peak(precision: str = "fp64") -> float:
     out = ctypes.c_double()
     N.check(lib.tfs_measure_fma_peak(PRECISIONS[precision], ctypes.byref(out)))
     return out.value
+
+
+def num_tile_variants(precision: str) -> int:
+    return int(N.load().tfs_num_tile_variants(PRECISIONS[precision]))
 
 
 def kernel_launch_count() -> int:
