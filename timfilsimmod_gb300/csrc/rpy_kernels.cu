@@ -244,6 +244,44 @@ cudaError_t launch_pack(int fp32, int fd, void *rec, const double *x, const doub
                  : pack_t<double, 3>(rec, x, f, n, nullptr, st);
 }
 
+// FP32x2 records: {-x,-x,-y,-y,-z,-z,f0,f0,...} (see rpy_tile_x2.cuh).
+template <int FD>
+__global__ void pack_sources_x2_kernel(float *__restrict__ rec, const double *__restrict__ x,
+                                       const double *__restrict__ f, int n,
+                                       const double *__restrict__ origin) {
+  constexpr int L = FD == 6 ? 20 : 12;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float *r = rec + (size_t)i * L;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float m = float(origin[k] - x[3 * (size_t)i + k]);
+    r[2 * k] = m;
+    r[2 * k + 1] = m;
+  }
+#pragma unroll
+  for (int k = 0; k < FD; ++k) {
+    const float q = float(f[(size_t)FD * i + k]);
+    r[6 + 2 * k] = q;
+    r[6 + 2 * k + 1] = q;
+  }
+#pragma unroll
+  for (int k = 6 + 2 * FD; k < L; ++k) r[k] = 0.f;
+}
+
+cudaError_t launch_pack_x2(int fd, void *rec, const double *x, const double *f, int n,
+                           const double *origin, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (fd == 6)
+    pack_sources_x2_kernel<6><<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<float *>(rec), x,
+                                                                f, n, origin);
+  else
+    pack_sources_x2_kernel<3><<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<float *>(rec), x,
+                                                                f, n, origin);
+  count_launch();
+  return cudaGetLastError();
+}
+
 size_t record_bytes(int fp32, int fd) {
   if (fp32) return fd == 6 ? 48 : 32;
   return fd == 6 ? 80 : 48;
@@ -278,7 +316,11 @@ cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuni
   if (tune.variant < 0 || tune.variant >= nvar) tune.variant = 0;
   if (tune.ctas_per_sm <= 0) tune.ctas_per_sm = 4;
   const TileVariant var = a.fp32 ? g_variants_f32[tune.variant] : g_variants_f64[tune.variant];
-  const TileFn fn = a.fp32 ? g_tile_f32[tune.variant][combo] : g_tile_f64[tune.variant][combo];
+  const TileFn fn = !a.fp32 ? g_tile_f64[tune.variant][combo]
+                    : var.x2 ? g_tile_f32x2[tune.variant - kNumVariantsF32Scalar][combo]
+                             : g_tile_f32[tune.variant][combo];
+  if (var.x2 && (a.src_a2 == nullptr || (a.n_b > 0 && a.src_b2 == nullptr)))
+    return cudaErrorInvalidValue;
   if (a.n_tgt <= 0) return cudaSuccess;
   const int per_cta = var.block * var.tpt;
   const int ctas = (a.n_tgt + per_cta - 1) / per_cta;

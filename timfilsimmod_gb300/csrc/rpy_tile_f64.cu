@@ -5,7 +5,7 @@ namespace tfs {
 
 // (threads per CTA, targets per thread, sources per tile); index = variant.
 const TileVariant g_variants_f64[kNumVariantsF64] = {
-    {128, 1, 128}, {64, 1, 128}, {128, 2, 128}, {256, 1, 128}};
+    {128, 1, 128, 0}, {64, 1, 128, 0}, {128, 2, 128, 0}, {256, 1, 128, 0}};
 
 const TileFn g_tile_f64[kNumVariantsF64][kNumCombos] = {
     TFS_TILE_ROW(double, 128, 1, 128), TFS_TILE_ROW(double, 64, 1, 128),

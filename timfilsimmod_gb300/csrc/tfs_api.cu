@@ -51,6 +51,7 @@ struct tfs_solver {
   double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
   double *origin = nullptr;  // [4]: mean position and extent
   void *rec_segs = nullptr, *rec_blobs = nullptr;
+  void *rec_segs_x2 = nullptr, *rec_blobs_x2 = nullptr;  // FP32x2 records
   double *scratch = nullptr;
   size_t scratch_elems = 0;
   bool origin_dirty = true;
@@ -103,6 +104,8 @@ static void free_all(tfs_solver *s) {
   cudaFree(s->origin);
   cudaFree(s->rec_segs);
   cudaFree(s->rec_blobs);
+  cudaFree(s->rec_segs_x2);
+  cudaFree(s->rec_blobs_x2);
   cudaFree(s->scratch);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
@@ -132,6 +135,12 @@ static int pack(tfs_solver *s, int segs) {
                        : launch_pack(fp32, 3, s->rec_blobs, s->x_blobs, s->f_blobs, s->nb,
                                      s->origin, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "pack kernel");
+  if (fp32) {
+    e = segs ? launch_pack_x2(6, s->rec_segs_x2, s->x_segs, s->f_segs, s->ns, s->origin, s->stream)
+             : launch_pack_x2(3, s->rec_blobs_x2, s->x_blobs, s->f_blobs, s->nb, s->origin,
+                              s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "pack kernel");
+  }
   return TFS_OK;
 }
 
@@ -158,17 +167,20 @@ static int product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, 
   int fda, fdb = 0;
   if (src_segs) {
     a.src_a = s->rec_segs;
+    a.src_a2 = s->rec_segs_x2;
     a.n_a = s->ns;
     a.a_a = s->cfg.a_seg;
     fda = 6;
     if (src_blobs) {
       a.src_b = s->rec_blobs;
+      a.src_b2 = s->rec_blobs_x2;
       a.n_b = s->nb;
       a.a_b = s->cfg.a_blob;
       fdb = 3;
     }
   } else {
     a.src_a = s->rec_blobs;
+    a.src_a2 = s->rec_blobs_x2;
     a.n_a = s->nb;
     a.a_a = s->cfg.a_blob;
     fda = 3;
@@ -252,6 +264,8 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
       (rc = alloc_dev((void **)&s->origin, dsz * 4)) ||
       (rc = alloc_dev(&s->rec_segs, record_bytes(0, 6) * ns)) ||
       (rc = alloc_dev(&s->rec_blobs, record_bytes(0, 3) * nb)) ||
+      (rc = alloc_dev(&s->rec_segs_x2, 80 * (size_t)ns)) ||
+      (rc = alloc_dev(&s->rec_blobs_x2, 48 * (size_t)nb)) ||
       (rc = alloc_dev((void **)&s->scratch, dsz * s->scratch_elems))) {
     free_all(s);
     delete s;
@@ -439,9 +453,11 @@ int tfs_apply_grand_mobility(tfs_solver *s) {
       a.a_tgt = s->cfg.a_blob;
       a.out = s->v_blobs;
       a.src_a = s->rec_segs;
+      a.src_a2 = s->rec_segs_x2;
       a.n_a = s->ns;
       a.a_a = s->cfg.a_seg;
       a.src_b = s->rec_blobs;
+      a.src_b2 = s->rec_blobs_x2;
       a.n_b = s->nb;
       a.a_b = s->cfg.a_blob;
       const TileTuning tune = s->tune[s->cfg.precision == TFS_FP32C][C_BX];
@@ -521,10 +537,15 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
       a.out = tgt_segs ? s->v_segs : s->v_blobs;
       int fda, fdb = 0;
       if (src_segs) {
-        a.src_a = s->rec_segs; a.n_a = s->ns; a.a_a = s->cfg.a_seg; fda = 6;
-        if (src_blobs) { a.src_b = s->rec_blobs; a.n_b = s->nb; a.a_b = s->cfg.a_blob; fdb = 3; }
+        a.src_a = s->rec_segs; a.src_a2 = s->rec_segs_x2; a.n_a = s->ns; a.a_a = s->cfg.a_seg;
+        fda = 6;
+        if (src_blobs) {
+          a.src_b = s->rec_blobs; a.src_b2 = s->rec_blobs_x2; a.n_b = s->nb;
+          a.a_b = s->cfg.a_blob; fdb = 3;
+        }
       } else {
-        a.src_a = s->rec_blobs; a.n_a = s->nb; a.a_a = s->cfg.a_blob; fda = 3;
+        a.src_a = s->rec_blobs; a.src_a2 = s->rec_blobs_x2; a.n_a = s->nb; a.a_a = s->cfg.a_blob;
+        fda = 3;
       }
       const int vd = tgt_segs ? 6 : 3;
       const int nvar = p ? kNumVariantsF32 : kNumVariantsF64;
@@ -551,8 +572,8 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
           ms /= reps;
           const TileVariant tv = p ? g_variants_f32[v] : g_variants_f64[v];
           char buf[96];
-          snprintf(buf, sizeof buf, "%s[%d,%d,%d,%d,%.4f]", cands.empty() ? "" : ",", tv.block,
-                   tv.tpt, tv.ts, cps, ms);
+          snprintf(buf, sizeof buf, "%s[%d,%d,%d,%d,%d,%.4f]", cands.empty() ? "" : ",",
+                   tv.block, tv.tpt, tv.ts, tv.x2, cps, ms);
           cands += buf;
           if (ms < best_ms) {
             best_ms = ms;
@@ -565,10 +586,10 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
       const TileVariant bv = p ? g_variants_f32[best.variant] : g_variants_f64[best.variant];
       char buf[256];
       snprintf(buf, sizeof buf,
-               "%s\"%s\":{\"block\":%d,\"tpt\":%d,\"ts\":%d,\"ctas_per_sm\":%d,\"ms\":%.4f,"
-               "\"candidates\":[",
-               first_combo ? "" : ",", combo_name(c), bv.block, bv.tpt, bv.ts, best.ctas_per_sm,
-               best_ms);
+               "%s\"%s\":{\"block\":%d,\"tpt\":%d,\"ts\":%d,\"x2\":%d,\"ctas_per_sm\":%d,"
+               "\"ms\":%.4f,\"candidates\":[",
+               first_combo ? "" : ",", combo_name(c), bv.block, bv.tpt, bv.ts, bv.x2,
+               best.ctas_per_sm, best_ms);
       report += buf;
       report += cands + "]}";
       first_combo = false;

@@ -22,6 +22,8 @@ struct TileArgs {
   const void *src_b;    // packed source records, set B (or null)
   int n_b;
   double a_b;
+  const void *src_a2;   // FP32x2 records (duplicated pairs) of set A, set B
+  const void *src_b2;
   const double *origin; // device [4]: FP32 centring origin (+ extent)
   int fp32;             // 1: FP32 compensated, 0: FP64
   double scale;         // 1 / (8 pi mu)
@@ -49,17 +51,21 @@ struct BarrierArgs {
 // (rpy_tile_f32.cu, rpy_tile_f64.cu).
 struct TileVariant {
   int block, tpt, ts;  // threads per CTA, targets per thread, sources per tile
+  int x2;              // 1: packed FP32x2 kernel (rpy_tile_x2.cuh)
 };
 // (target kind, source sets): 0 = seg<-seg, 1 = seg<-blob, 2 = blob<-blob,
 // 3 = blob<-seg, 4 = seg<-(seg,blob), 5 = blob<-(seg,blob)
 enum TileCombo { C_SS = 0, C_SB = 1, C_BB = 2, C_BS = 3, C_SX = 4, C_BX = 5 };
 constexpr int kNumCombos = 6;
-constexpr int kNumVariantsF32 = 6;
+constexpr int kNumVariantsF32Scalar = 6;
+constexpr int kNumVariantsF32X2 = 3;
+constexpr int kNumVariantsF32 = kNumVariantsF32Scalar + kNumVariantsF32X2;
 constexpr int kNumVariantsF64 = 4;
 typedef cudaError_t (*TileFn)(const TileArgs &, dim3, cudaStream_t);
 extern const TileVariant g_variants_f32[kNumVariantsF32];
 extern const TileVariant g_variants_f64[kNumVariantsF64];
-extern const TileFn g_tile_f32[kNumVariantsF32][kNumCombos];
+extern const TileFn g_tile_f32[kNumVariantsF32Scalar][kNumCombos];
+extern const TileFn g_tile_f32x2[kNumVariantsF32X2][kNumCombos];
 extern const TileFn g_tile_f64[kNumVariantsF64][kNumCombos];
 
 // Tuning of one launch: variant and the number of CTAs per SM the source
@@ -78,6 +84,10 @@ cudaError_t launch_origin(const double *xa, int na, const double *xb, int nb, do
                           cudaStream_t st);
 cudaError_t launch_pack(int fp32, int fd, void *rec, const double *x, const double *f, int n,
                         const double *origin, cudaStream_t st);
+// FP32x2 records (positions negated, every value duplicated), 80 B per
+// segment and 48 B per blob.
+cudaError_t launch_pack_x2(int fd, void *rec, const double *x, const double *f, int n,
+                           const double *origin, cudaStream_t st);
 // vd: 6 (segment targets) or 3 (blob targets); fda/fdb: 6 (segment sources),
 // 3 (blob sources), fdb = 0 for a single source set. mode: OUT_ASSIGN or
 // OUT_ACCUMULATE. scratch must hold kMaxSplits * n_tgt * vd doubles for
