@@ -20,10 +20,20 @@ def main():
     p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier"])
+    p.add_argument("--variant", type=int, default=None,
+                   help="pin every combination to this tile-kernel variant")
+    p.add_argument("--ctas-per-sm", type=int, default=4)
+    p.add_argument("--autotune", action="store_true", help="print the autotuner's table")
     args = p.parse_args()
     sw = make_config(args.config, seed=1)
     s = RpyMobilitySolver(1, sw.nfil, sw.nseg, sw.num_blobs, precision=args.precision)
     s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
+    if args.autotune:
+        import json
+        print(json.dumps(s.autotune((args.precision,), reps=3)))
+    if args.variant is not None:
+        for combo in range(6):
+            s.set_tuning(combo, args.variant, args.ctas_per_sm)
     t0 = time.perf_counter()
     for _ in range(args.reps):
         if args.op == "grand":
