@@ -149,7 +149,7 @@ def bench_ours(args):
         if not args.no_tune:
             # pick the tile-kernel launch variant per block for these sizes
             table = s.autotune((precision,), reps=2 if precision == "fp32c" else 1)[precision]
-            tuning[precision] = {k: [v["block"], v["tpt"], v["ts"], v["ctas_per_sm"]]
+            tuning[precision] = {k: [v["block"], v["tpt"], v["ts"], v["x2"], v["waves"]]
                                  for k, v in table.items()}
         return s
 
@@ -298,7 +298,7 @@ def bench_ours(args):
             "clocks": clocks,
             "gpu_launches": launches,
             "tuning": {"columns": ["threads/CTA", "targets/thread", "sources/tile",
-                                   "CTAs/SM target"], **tuning},
+                                   "packed fp32x2", "waves"], **tuning},
         }
         if cpu is not None:
             result["cpu_baseline"] = cpu

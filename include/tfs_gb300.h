@@ -125,8 +125,9 @@ int tfs_apply_grand_mobility(tfs_solver *s);
 
 /* --- autotuning ---------------------------------------------------------- */
 /* Time every launch variant of the tile kernel (threads per CTA, targets per
- * thread, sources per tile) and every source-split target (1, 2, 4 or 8
- * CTAs per SM) for each (target, source set) combination the solver uses,
+ * thread, sources per tile, scalar or packed FP32x2) and every source-split
+ * target (1, 2 or 4 full waves of resident CTAs) for each (target, source
+ * set) combination the solver uses,
  * on its current positions and forces, and keep the fastest per combination.
  * precision_mask: bit 0 = TFS_FP64, bit 1 = TFS_FP32C. reps: timed
  * launches per candidate. Overwrites the solver's velocity buffers.
@@ -134,8 +135,9 @@ int tfs_apply_grand_mobility(tfs_solver *s);
 int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps);
 /* Pin the launch of one combination: combo 0..5 = seg<-seg, seg<-blob,
  * blob<-blob, blob<-seg, seg<-(seg,blob), blob<-(seg,blob); variant in
- * [0, tfs_num_tile_variants(precision)); ctas_per_sm in [1, 64]. */
-int tfs_solver_set_tuning(tfs_solver *s, int precision, int combo, int variant, int ctas_per_sm);
+ * [0, tfs_num_tile_variants(precision)); waves in [1, 64] (the source split
+ * aims for this many full waves of resident CTAs). */
+int tfs_solver_set_tuning(tfs_solver *s, int precision, int combo, int variant, int waves);
 int tfs_num_tile_variants(int precision);
 /* The tuning table of the last autotune as JSON (NUL-terminated, truncated to
  * len); *needed (if non-NULL) gets the full size including the NUL. */

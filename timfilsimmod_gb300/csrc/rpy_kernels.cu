@@ -297,11 +297,13 @@ int combo_of(int vd, int fda, int fdb) {
   return -1;
 }
 
-// Source splits for a launch of `ctas` target CTAs over n_src sources: aim
-// for ctas_per_sm CTAs on every SM, with at least two tiles per split.
-static int choose_splits(int ctas, int n_src, int ctas_per_sm, int ts) {
-  const int want = std::max(1, (ctas_per_sm * num_sms() + ctas - 1) / ctas);
-  int s = std::min(want, kMaxSplits);
+// Source splits for a launch of `ctas` target CTAs over n_src sources: the
+// largest split count whose grid fits `waves` full waves (resident CTAs per
+// SM x SMs), so no wave runs part-empty; at least two tiles per split.
+static int choose_splits(int ctas, int n_src, int resident, int waves, int ts) {
+  const long slots = (long)resident * num_sms() * std::max(1, waves);
+  int s = (int)std::max(1L, slots / std::max(1, ctas));
+  s = std::min(s, kMaxSplits);
   s = std::min(s, std::max(1, n_src / std::max(1, 2 * ts)));
   return std::max(1, s);
 }
@@ -314,7 +316,7 @@ cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuni
   if (combo < 0) return cudaErrorInvalidValue;
   const int nvar = a.fp32 ? kNumVariantsF32 : kNumVariantsF64;
   if (tune.variant < 0 || tune.variant >= nvar) tune.variant = 0;
-  if (tune.ctas_per_sm <= 0) tune.ctas_per_sm = 4;
+  if (tune.waves <= 0) tune.waves = 1;
   const TileVariant var = a.fp32 ? g_variants_f32[tune.variant] : g_variants_f64[tune.variant];
   const TileFn fn = !a.fp32 ? g_tile_f64[tune.variant][combo]
                     : var.x2 ? g_tile_f32x2[tune.variant - kNumVariantsF32Scalar][combo]
@@ -325,8 +327,11 @@ cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuni
   const int per_cta = var.block * var.tpt;
   const int ctas = (a.n_tgt + per_cta - 1) / per_cta;
   const int n_src = a.n_a + a.n_b;
+  int resident = 1;
+  cudaError_t qe = fn(a, dim3(0), st, &resident);
+  if (qe != cudaSuccess) return qe;
   int splits = a.splits > 0 ? std::min(a.splits, kMaxSplits)
-                            : choose_splits(ctas, n_src, tune.ctas_per_sm, var.ts);
+                            : choose_splits(ctas, n_src, resident, tune.waves, var.ts);
   if ((size_t)splits * a.n_tgt * vd > scratch_elems) splits = 1;
   if (n_src == 0) splits = 1;
   int chunk = (n_src + splits - 1) / splits;
@@ -339,7 +344,7 @@ cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuni
   if (ev) cudaEventRecord(ev[0], st);
   if (splits == 1) {
     a.mode = mode;
-    e = fn(a, grid, st);
+    e = fn(a, grid, st, nullptr);
     count_launch();
     if (ev) cudaEventRecord(ev[1], st);
     return e;
@@ -347,7 +352,7 @@ cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuni
   double *final_out = a.out;
   a.mode = OUT_PARTIAL;
   a.out = scratch;
-  e = fn(a, grid, st);
+  e = fn(a, grid, st, nullptr);
   count_launch();
   if (ev) cudaEventRecord(ev[1], st);
   if (e != cudaSuccess) return e;

@@ -136,7 +136,7 @@ __device__ __forceinline__ void sum_source_range(T (&v)[TPT][VD], const T (&xt)[
     for (int q = threadIdx.x; q < nvec; q += BLOCK) dst[q] = __ldg(src + q);
     __syncthreads();
     bool near = false;
-#pragma unroll 1
+#pragma unroll 2
     for (int j = 0; j < cnt; ++j) {
       T sx, sy, sz, f[FD];
       RecLoad<T, FD>::get(smem + j * L, sx, sy, sz, f);
@@ -261,16 +261,22 @@ constexpr size_t tile_smem_bytes() {
   return sizeof(T) * TS * LMAX + (sizeof(T) == 4 ? sizeof(float) * 2 * TPT * VD * BLOCK : 0);
 }
 
+// Launch one instantiation. With grid.x == 0 it only reports (in *resident)
+// how many CTAs of it fit on one SM.
 template <typename T, int VD, int FDA, int FDB, int BLOCK, int TPT, int TS>
-cudaError_t tile_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st) {
+cudaError_t tile_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st, int *resident) {
   constexpr size_t smem = tile_smem_bytes<T, VD, FDA, FDB, BLOCK, TPT, TS>();
-  static bool configured = false;
+  static int occupancy = 0;
   auto kern = rpy_tile_kernel<T, VD, FDA, FDB, BLOCK, TPT, TS>;
-  if (!configured) {
+  if (occupancy == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    configured = true;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occupancy, kern, BLOCK, smem);
+    if (e != cudaSuccess) return e;
+    if (occupancy < 1) occupancy = 1;
   }
+  if (resident) *resident = occupancy;
+  if (grid.x == 0) return cudaSuccess;  // query only
   kern<<<grid, BLOCK, smem, st>>>(a);
   return cudaGetLastError();
 }

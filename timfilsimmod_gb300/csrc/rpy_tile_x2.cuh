@@ -63,16 +63,20 @@ __device__ __forceinline__ void far_pair_x2(float2 *__restrict__ v, float2 dx, f
   v[1] = fma2(A, f[1], fma2(Bd, dy, v[1]));
   v[2] = fma2(A, f[2], fma2(Bd, dz, v[2]));
   if (FD == 6 || VD == 6) {
+    // e = rm3 d and its negation: the packed FMA has no operand negation, so
+    // the cross products use -e instead of negated source components.
+    const float2 nrm3 = mul2(make_float2(-1.f, -1.f), rm3);
     const float2 ex = mul2(rm3, dx), ey = mul2(rm3, dy), ez = mul2(rm3, dz);
+    const float2 nx = mul2(nrm3, dx), ny = mul2(nrm3, dy), nz = mul2(nrm3, dz);
     if (FD == 6) {
-      v[0] = fma2(f[4], ez, fma2(neg2(f[5]), ey, v[0]));
-      v[1] = fma2(f[5], ex, fma2(neg2(f[3]), ez, v[1]));
-      v[2] = fma2(f[3], ey, fma2(neg2(f[4]), ex, v[2]));
+      v[0] = fma2(f[4], ez, fma2(f[5], ny, v[0]));
+      v[1] = fma2(f[5], ex, fma2(f[3], nz, v[1]));
+      v[2] = fma2(f[3], ey, fma2(f[4], nx, v[2]));
     }
     if (VD == 6) {
-      v[3] = fma2(f[1], ez, fma2(neg2(f[2]), ey, v[3]));
-      v[4] = fma2(f[2], ex, fma2(neg2(f[0]), ez, v[4]));
-      v[5] = fma2(f[0], ey, fma2(neg2(f[1]), ex, v[5]));
+      v[3] = fma2(f[1], ez, fma2(f[2], ny, v[3]));
+      v[4] = fma2(f[2], ex, fma2(f[0], nz, v[4]));
+      v[5] = fma2(f[0], ey, fma2(f[1], nx, v[5]));
       if (FD == 6) {
         const float2 h = mul2(make_float2(-0.5f, -0.5f), rm3);
         const float2 dT = fma2(dx, f[3], fma2(dy, f[4], mul2(dz, f[5])));
@@ -268,15 +272,19 @@ constexpr size_t tile_x2_smem_bytes() {
 }
 
 template <int VD, int FDA, int FDB, int BLOCK, int TPT, int TS>
-cudaError_t tile_x2_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st) {
+cudaError_t tile_x2_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st, int *resident) {
   constexpr size_t smem = tile_x2_smem_bytes<VD, FDA, FDB, BLOCK, TPT, TS>();
-  static bool configured = false;
+  static int occupancy = 0;
   auto kern = rpy_tile_x2_kernel<VD, FDA, FDB, BLOCK, TPT, TS>;
-  if (!configured) {
+  if (occupancy == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    configured = true;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occupancy, kern, BLOCK, smem);
+    if (e != cudaSuccess) return e;
+    if (occupancy < 1) occupancy = 1;
   }
+  if (resident) *resident = occupancy;
+  if (grid.x == 0) return cudaSuccess;  // query only
   kern<<<grid, BLOCK, smem, st>>>(a);
   return cudaGetLastError();
 }

@@ -241,7 +241,7 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
   if (s == nullptr) return fail(TFS_ENOMEM, "host allocation failed");
   s->cfg = *cfg;
   for (int p = 0; p < 2; ++p)
-    for (int c = 0; c < kNumCombos; ++c) s->tune[p][c] = TileTuning{0, 4};
+    for (int c = 0; c < kNumCombos; ++c) s->tune[p][c] = TileTuning{0, 1};
   s->ns = (int)ns;
   s->nb = (int)nb;
   cudaGetDevice(&s->device);
@@ -508,7 +508,7 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
   const int saved_precision = s->cfg.precision;
   const bool saved_timing = s->timing;
   s->timing = false;
-  static const int kCps[] = {1, 2, 4, 8};
+  static const int kWaves[] = {1, 2, 4};
   cudaEvent_t e0, e1;
   TFS_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
   TFS_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
@@ -550,10 +550,10 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
       const int vd = tgt_segs ? 6 : 3;
       const int nvar = p ? kNumVariantsF32 : kNumVariantsF64;
       float best_ms = 1e30f;
-      TileTuning best{0, 4};
+      TileTuning best{0, 1};
       std::string cands;
       for (int v = 0; v < nvar && rc == TFS_OK; ++v) {
-        for (int cps : kCps) {
+        for (int cps : kWaves) {
           TileTuning t{v, cps};
           cudaError_t e = launch_tile(a, vd, fda, fdb, t, s->scratch, s->scratch_elems, OUT_ASSIGN,
                                       s->stream);  // warm-up
@@ -586,10 +586,10 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
       const TileVariant bv = p ? g_variants_f32[best.variant] : g_variants_f64[best.variant];
       char buf[256];
       snprintf(buf, sizeof buf,
-               "%s\"%s\":{\"block\":%d,\"tpt\":%d,\"ts\":%d,\"x2\":%d,\"ctas_per_sm\":%d,"
+               "%s\"%s\":{\"block\":%d,\"tpt\":%d,\"ts\":%d,\"x2\":%d,\"waves\":%d,"
                "\"ms\":%.4f,\"candidates\":[",
                first_combo ? "" : ",", combo_name(c), bv.block, bv.tpt, bv.ts, bv.x2,
-               best.ctas_per_sm, best_ms);
+               best.waves, best_ms);
       report += buf;
       report += cands + "]}";
       first_combo = false;
@@ -605,15 +605,15 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
   return rc;
 }
 
-int tfs_solver_set_tuning(tfs_solver *s, int precision, int combo, int variant, int ctas_per_sm) {
+int tfs_solver_set_tuning(tfs_solver *s, int precision, int combo, int variant, int waves) {
   TFS_CHECK_SOLVER(s);
   if (precision != TFS_FP64 && precision != TFS_FP32C)
     return fail(TFS_EINVAL, "unknown precision %d", precision);
   if (combo < 0 || combo >= kNumCombos) return fail(TFS_EINVAL, "combination %d out of range", combo);
   const int nvar = precision == TFS_FP32C ? kNumVariantsF32 : kNumVariantsF64;
   if (variant < 0 || variant >= nvar) return fail(TFS_EINVAL, "variant %d out of range", variant);
-  if (ctas_per_sm < 1 || ctas_per_sm > 64) return fail(TFS_EINVAL, "ctas_per_sm out of range");
-  s->tune[precision][combo] = TileTuning{variant, ctas_per_sm};
+  if (waves < 1 || waves > 64) return fail(TFS_EINVAL, "waves out of range");
+  s->tune[precision][combo] = TileTuning{variant, waves};
   return TFS_OK;
 }
 

@@ -61,18 +61,19 @@ constexpr int kNumVariantsF32Scalar = 6;
 constexpr int kNumVariantsF32X2 = 3;
 constexpr int kNumVariantsF32 = kNumVariantsF32Scalar + kNumVariantsF32X2;
 constexpr int kNumVariantsF64 = 4;
-typedef cudaError_t (*TileFn)(const TileArgs &, dim3, cudaStream_t);
+// Launch (grid.x > 0) or, with grid.x == 0, report resident CTAs per SM.
+typedef cudaError_t (*TileFn)(const TileArgs &, dim3, cudaStream_t, int *resident);
 extern const TileVariant g_variants_f32[kNumVariantsF32];
 extern const TileVariant g_variants_f64[kNumVariantsF64];
 extern const TileFn g_tile_f32[kNumVariantsF32Scalar][kNumCombos];
 extern const TileFn g_tile_f32x2[kNumVariantsF32X2][kNumCombos];
 extern const TileFn g_tile_f64[kNumVariantsF64][kNumCombos];
 
-// Tuning of one launch: variant and the number of CTAs per SM the source
-// splitting aims for.
+// Tuning of one launch: variant and the number of full waves (resident CTAs
+// on every SM) the source splitting aims for.
 struct TileTuning {
   int variant;
-  int ctas_per_sm;
+  int waves;
 };
 int combo_of(int vd, int fda, int fdb);
 

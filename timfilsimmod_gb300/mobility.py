@@ -156,11 +156,11 @@ class RpyMobilitySolver:
         self._call("tfs_solver_autotune", mask, int(reps))
         return json.loads(self.tuning_report())
 
-    def set_tuning(self, combo: int, variant: int, ctas_per_sm: int = 4,
+    def set_tuning(self, combo: int, variant: int, waves: int = 1,
                    precision: str | None = None) -> None:
         """Pin the tile-kernel launch of one (target, source-set) combination."""
         prec = PRECISIONS[precision or self.precision]
-        self._call("tfs_solver_set_tuning", prec, int(combo), int(variant), int(ctas_per_sm))
+        self._call("tfs_solver_set_tuning", prec, int(combo), int(variant), int(waves))
 
     def tuning_report(self) -> str:
         need = ctypes.c_size_t()

@@ -22,7 +22,7 @@ def main():
     p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier"])
     p.add_argument("--variant", type=int, default=None,
                    help="pin every combination to this tile-kernel variant")
-    p.add_argument("--ctas-per-sm", type=int, default=4)
+    p.add_argument("--waves", type=int, default=1)
     p.add_argument("--autotune", action="store_true", help="print the autotuner's table")
     args = p.parse_args()
     sw = make_config(args.config, seed=1)
@@ -33,7 +33,7 @@ def main():
         print(json.dumps(s.autotune((args.precision,), reps=3)))
     if args.variant is not None:
         for combo in range(6):
-            s.set_tuning(combo, args.variant, args.ctas_per_sm)
+            s.set_tuning(combo, args.variant, args.waves)
     t0 = time.perf_counter()
     for _ in range(args.reps):
         if args.op == "grand":
