@@ -297,14 +297,18 @@ int combo_of(int vd, int fda, int fdb) {
   return -1;
 }
 
+// Sources per split are a multiple of this (also the smallest split).
+constexpr int kMinChunk = 64;
+
 // Source splits for a launch of `ctas` target CTAs over n_src sources: the
 // largest split count whose grid fits `waves` full waves (resident CTAs per
 // SM x SMs), so no wave runs part-empty; at least two tiles per split.
 static int choose_splits(int ctas, int n_src, int resident, int waves, int ts) {
+  (void)ts;
   const long slots = (long)resident * num_sms() * std::max(1, waves);
   int s = (int)std::max(1L, slots / std::max(1, ctas));
   s = std::min(s, kMaxSplits);
-  s = std::min(s, std::max(1, n_src / std::max(1, 2 * ts)));
+  s = std::min(s, std::max(1, n_src / kMinChunk));
   return std::max(1, s);
 }
 
@@ -335,8 +339,8 @@ cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuni
   if ((size_t)splits * a.n_tgt * vd > scratch_elems) splits = 1;
   if (n_src == 0) splits = 1;
   int chunk = (n_src + splits - 1) / splits;
-  chunk = ((chunk + var.ts - 1) / var.ts) * var.ts;
-  if (chunk == 0) chunk = var.ts;
+  chunk = ((chunk + kMinChunk - 1) / kMinChunk) * kMinChunk;
+  if (chunk == 0) chunk = kMinChunk;
   splits = std::max(1, (n_src + chunk - 1) / chunk);
   a.chunk = chunk;
   const dim3 grid(ctas, splits);

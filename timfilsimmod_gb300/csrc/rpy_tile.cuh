@@ -168,8 +168,8 @@ __device__ __forceinline__ void sum_source_range(T (&v)[TPT][VD], const T (&xt)[
   }
 }
 
-template <typename T, int VD, int FDA, int FDB, int BLOCK, int TPT, int TS>
-__global__ void __launch_bounds__(BLOCK) rpy_tile_kernel(const TileArgs args) {
+template <typename T, int VD, int FDA, int FDB, int BLOCK, int TPT, int TS, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) rpy_tile_kernel(const TileArgs args) {
   constexpr int LA = Rec<T, FDA>::len;
   constexpr int LB = FDB > 0 ? Rec<T, (FDB > 0 ? FDB : 3)>::len : 0;
   constexpr int LMAX = LA > LB ? LA : LB;
@@ -263,11 +263,11 @@ constexpr size_t tile_smem_bytes() {
 
 // Launch one instantiation. With grid.x == 0 it only reports (in *resident)
 // how many CTAs of it fit on one SM.
-template <typename T, int VD, int FDA, int FDB, int BLOCK, int TPT, int TS>
+template <typename T, int VD, int FDA, int FDB, int BLOCK, int TPT, int TS, int MINB>
 cudaError_t tile_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st, int *resident) {
   constexpr size_t smem = tile_smem_bytes<T, VD, FDA, FDB, BLOCK, TPT, TS>();
   static int occupancy = 0;
-  auto kern = rpy_tile_kernel<T, VD, FDA, FDB, BLOCK, TPT, TS>;
+  auto kern = rpy_tile_kernel<T, VD, FDA, FDB, BLOCK, TPT, TS, MINB>;
   if (occupancy == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -283,11 +283,11 @@ cudaError_t tile_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st, int *r
 
 // One row of the dispatch table: the six (target, source-set) combinations
 // in the order of TileCombo.
-#define TFS_TILE_ROW(T, B, P, S)                                                           \
+#define TFS_TILE_ROW(T, B, P, S, M)                                                        \
   {                                                                                        \
-    tile_launch_fn<T, 6, 6, 0, B, P, S>, tile_launch_fn<T, 6, 3, 0, B, P, S>,              \
-        tile_launch_fn<T, 3, 3, 0, B, P, S>, tile_launch_fn<T, 3, 6, 0, B, P, S>,          \
-        tile_launch_fn<T, 6, 6, 3, B, P, S>, tile_launch_fn<T, 3, 6, 3, B, P, S>           \
+    tile_launch_fn<T, 6, 6, 0, B, P, S, M>, tile_launch_fn<T, 6, 3, 0, B, P, S, M>,        \
+        tile_launch_fn<T, 3, 3, 0, B, P, S, M>, tile_launch_fn<T, 3, 6, 0, B, P, S, M>,    \
+        tile_launch_fn<T, 6, 6, 3, B, P, S, M>, tile_launch_fn<T, 3, 6, 3, B, P, S, M>     \
   }
 
 }  // namespace tfs

@@ -10,7 +10,7 @@ namespace tfs {
 enum OutMode { OUT_ASSIGN = 0, OUT_ACCUMULATE = 1, OUT_PARTIAL = 2 };
 
 // Upper bound on source splits of one product (sizes the scratch buffer).
-constexpr int kMaxSplits = 32;
+constexpr int kMaxSplits = 64;
 
 struct TileArgs {
   const double *x_tgt;  // target positions, AoS float64 [3*n_tgt]
@@ -52,15 +52,16 @@ struct BarrierArgs {
 struct TileVariant {
   int block, tpt, ts;  // threads per CTA, targets per thread, sources per tile
   int x2;              // 1: packed FP32x2 kernel (rpy_tile_x2.cuh)
+  int min_blocks;      // __launch_bounds__ minimum resident CTAs (register cap), 0 = none
 };
 // (target kind, source sets): 0 = seg<-seg, 1 = seg<-blob, 2 = blob<-blob,
 // 3 = blob<-seg, 4 = seg<-(seg,blob), 5 = blob<-(seg,blob)
 enum TileCombo { C_SS = 0, C_SB = 1, C_BB = 2, C_BS = 3, C_SX = 4, C_BX = 5 };
 constexpr int kNumCombos = 6;
-constexpr int kNumVariantsF32Scalar = 6;
+constexpr int kNumVariantsF32Scalar = 8;
 constexpr int kNumVariantsF32X2 = 3;
 constexpr int kNumVariantsF32 = kNumVariantsF32Scalar + kNumVariantsF32X2;
-constexpr int kNumVariantsF64 = 4;
+constexpr int kNumVariantsF64 = 5;
 // Launch (grid.x > 0) or, with grid.x == 0, report resident CTAs per SM.
 typedef cudaError_t (*TileFn)(const TileArgs &, dim3, cudaStream_t, int *resident);
 extern const TileVariant g_variants_f32[kNumVariantsF32];
