@@ -123,6 +123,53 @@ int tfs_evaluate_full_mobility(tfs_solver *s, double *v_segs_host, double *v_blo
  * to [f_segs; f_blobs]. */
 int tfs_apply_grand_mobility(tfs_solver *s);
 
+/* --- the free-body mobility solve (one swimmer per solver, nswim = 1) ---- */
+/* The body's blob references in the body frame (rigid_body::blob_references,
+ * rigid_body.cpp:325-365), 3*nblob values. Required before the calls below. */
+int tfs_set_blob_references(tfs_solver *s, const double *blob_refs_host);
+/* Body position x[3] and orientation quaternion q[4] = (q0, q1, q2, q3)
+ * (rigid_body::x, q; q may be NULL to keep the orientation). Computes the blob
+ * positions on the device (rigid_body::blob_positions, rigid_body.cpp:482-500). */
+int tfs_set_body_pose(tfs_solver *s, const double *x, const double *q);
+/* LINEAR_SYSTEM_TOL and MAX_LINEAR_SYSTEM_ITER (config.hpp:312-313); the
+ * defaults are the reference's 1e-4 and min(350, 3 nblob + 6). */
+int tfs_set_linear_solver(tfs_solver *s, double tol, int max_iter);
+/* TFS_FP32C only: the linear solve is iterative refinement -- FP64 residuals
+ * r = rhs - A x around inner GMRES solves with FP32 blob-blob products, each
+ * to inner_tol relative to |r|, at most max_cycles cycles. */
+int tfs_set_refinement(tfs_solver *s, double inner_tol, int max_cycles);
+/* make_body_reference_matrices (mobility_solver.cpp:2950-3047): (K^T K)^-1
+ * from the blob references and the 6x6 body mobility from six solves with
+ * rhs = -e_{n-1-j}, at the current pose. Leaves the last solution as the next
+ * warm start, as the reference does. */
+int tfs_make_body_reference_matrices(tfs_solver *s);
+/* The two 6x6 matrices (column-major, body frame); either pointer may be NULL. */
+int tfs_get_body_reference_matrices(tfs_solver *s, double *body_mobility, double *ktkinv);
+int tfs_set_body_reference_matrices(tfs_solver *s, const double *body_mobility,
+                                    const double *ktkinv);
+/* compute_velocities, free-body branch (mobility_solver.cpp:2574-2659) on the
+ * segment positions and forces already on the device: barrier forces, Mss and
+ * Mbs, the right-hand side [-v_blobs; -F] with F = swimmer_f[6] (the swimmer's
+ * total force and torque, swimmer::forces_and_torques) plus the blob
+ * repulsion, the GMRES solve for blob forces and body velocity (warm-started
+ * from the previous solution), and Msb with the solved blob forces. On return
+ * swimmer_f holds F with the blob repulsion added, as the reference leaves
+ * swimmer.f; segment velocities, blob forces and body velocity are on the
+ * device (tfs_copy_segment_velocities_to_host, tfs_copy_blob_forces_to_host,
+ * tfs_get_body_velocities). Synchronises the solver's stream. */
+int tfs_compute_velocities(tfs_solver *s, double *swimmer_f, int *gmres_iters);
+/* The linear solve alone (solve_linear_system, mobility_solver.cpp:2092-2570)
+ * for a right-hand side rhs_host[3 nblob + 6]. */
+int tfs_solve_linear_system(tfs_solver *s, const double *rhs_host, int *gmres_iters);
+int tfs_get_body_velocities(tfs_solver *s, double *v_bodies);
+/* Warm start of the next solve (the reference keeps v_bodies between solves). */
+int tfs_set_body_velocities(tfs_solver *s, const double *v_bodies);
+/* The solved blob forces (f_blobs_host after the reference's GMRES). */
+int tfs_copy_blob_forces_to_host(tfs_solver *s, double *f_blobs_host);
+/* Iterations (summed over refinement cycles), refinement cycles and final
+ * relative residual of the last solve. */
+int tfs_solve_info(tfs_solver *s, int *iters, int *cycles, double *rel_residual);
+
 /* --- autotuning ---------------------------------------------------------- */
 /* Time every launch variant of the tile kernel (threads per CTA, targets per
  * thread, sources per tile, scalar or packed FP32x2) and every source-split

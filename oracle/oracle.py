@@ -215,3 +215,112 @@ class ReferenceFlow:
                                      int(blobs_per_body), ctypes.c_double(prefac),
                                      int(bool(remove_net_force)))
         return v
+
+
+class OracleSolver:
+    """CPU restatement of the reference's free-body mobility solve
+    (tfs_oracle_solve.c): one swimmer, barrier forces, Mss/Mbs, the
+    right-preconditioned GMRES saddle-point solve for blob forces and body
+    velocity, then Msb."""
+
+    def __init__(self, nfil, nseg, blob_refs, end_force_magnitude: int, tol=1e-10,
+                 max_iter=350, mu=1.0, a_seg=1.0, a_blob=1.0, repulsive_force_factor=2.0,
+                 threads=1):
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build_oracle()
+        self.lib = ctypes.CDLL(path)
+        self.lib.orc_solver_create.restype = ctypes.c_void_p
+        self.lib.orc_solver_create.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, _P, ctypes.c_int, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_int]
+        for name in ("orc_solver_destroy", "orc_solver_set_body", "orc_solver_gmres",
+                     "orc_solver_make_body_reference_matrices", "orc_solver_compute_velocities",
+                     "orc_solver_state", "orc_solver_set_state"):
+            getattr(self.lib, name).argtypes = None
+        self.lib.orc_set_threads(int(threads))
+        self.p = _Params(mu, a_seg, a_blob)
+        self.refs = _c(blob_refs)
+        self.nblob = self.refs.size // 3
+        self.ns = nfil * nseg
+        self.h = self.lib.orc_solver_create(ctypes.byref(self.p), nfil, nseg, self.nblob,
+                                            _ptr(self.refs), int(end_force_magnitude),
+                                            repulsive_force_factor, tol, max_iter)
+
+    def __del__(self):
+        try:
+            self.lib.orc_solver_destroy(ctypes.c_void_p(self.h))
+        except Exception:
+            pass
+
+    def set_body(self, x, q):
+        x, q = _c(x), _c(q)
+        self.lib.orc_solver_set_body(ctypes.c_void_p(self.h), _ptr(x), _ptr(q))
+
+    def make_body_reference_matrices(self, x_segs, f_segs):
+        xs, fs = _c(x_segs), _c(f_segs)
+        self.lib.orc_solver_make_body_reference_matrices(ctypes.c_void_p(self.h), _ptr(xs), _ptr(fs))
+        return self.state()
+
+    def compute_velocities(self, x_segs, f_segs, swimmer_f):
+        xs, fs = _c(x_segs), _c(f_segs)
+        sf = np.array(swimmer_f, dtype=np.float64).ravel().copy()
+        vs = np.zeros(6 * self.ns)
+        vb = np.zeros(3 * self.nblob)
+        it = self.lib.orc_solver_compute_velocities(ctypes.c_void_p(self.h), _ptr(xs), _ptr(fs),
+                                                    _ptr(sf), _ptr(vs), _ptr(vb))
+        st = self.state()
+        return dict(iters=it, v_segs=vs, v_blobs_rhs=vb, swimmer_f=sf, **st)
+
+    def state(self):
+        fb, vb, bm, kt = np.zeros(3 * self.nblob), np.zeros(6), np.zeros(36), np.zeros(36)
+        self.lib.orc_solver_state(ctypes.c_void_p(self.h), _ptr(fb), _ptr(vb), _ptr(bm), _ptr(kt))
+        return dict(f_blobs=fb, v_bodies=vb, body_mobility=bm, ktkinv=kt)
+
+    def set_state(self, f_blobs=None, v_bodies=None, body_mobility=None, ktkinv=None):
+        args = [None if a is None else _c(a) for a in (f_blobs, v_bodies, body_mobility, ktkinv)]
+        self.lib.orc_solver_set_state(ctypes.c_void_p(self.h),
+                                      *[None if a is None else _ptr(a) for a in args])
+
+
+class ReferenceSolver:
+    """The reference's own mobility_solver.cpp (compute_velocities, GMRES,
+    make_body_reference_matrices) compiled for the CPU by `make -C oracle ref`
+    with LINEAR_SYSTEM_TOL = 1e-10; single instance per process."""
+
+    def __init__(self, nfil, nseg, blob_refs, end_force_magnitude_real, seg_sep=2.2,
+                 body_x=(0, 0, 0), body_q=(1, 0, 0, 0)):
+        path = os.path.join(REF_DIR, "libref_solver_s1.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+        self.lib.ref_linear_system_tol.restype = ctypes.c_double
+        self.refs = _c(blob_refs)
+        self.nblob = self.refs.size // 3
+        self.ns = nfil * nseg
+        bx, bq = _c(body_x), _c(body_q)
+        self.lib.ref_solver_setup(nfil, nseg, self.nblob, ctypes.c_double(end_force_magnitude_real),
+                                  ctypes.c_double(seg_sep), _ptr(self.refs), _ptr(bx), _ptr(bq))
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(os.path.join(REF_DIR, "libref_solver_s1.so"))
+
+    def make_body_reference_matrices(self, x_segs, f_segs):
+        xs, fs = _c(x_segs), _c(f_segs)
+        bm, kt = np.zeros(36), np.zeros(36)
+        self.lib.ref_make_body_reference_matrices(_ptr(xs), _ptr(fs), _ptr(bm), _ptr(kt))
+        return dict(body_mobility=bm, ktkinv=kt)
+
+    def set_body(self, x, q):
+        x, q = _c(x), _c(q)
+        self.lib.ref_set_body(_ptr(x), _ptr(q))
+
+    def compute_velocities(self, x_segs, f_segs, swimmer_f, nt=0):
+        xs, fs, sf = _c(x_segs), _c(f_segs), _c(swimmer_f)
+        vs, vb = np.zeros(6 * self.ns), np.zeros(3 * self.nblob)
+        fb, vbod, sfo = np.zeros(3 * self.nblob), np.zeros(6), np.zeros(6)
+        it = self.lib.ref_compute_velocities(_ptr(xs), _ptr(fs), _ptr(sf), int(nt), _ptr(vs),
+                                             _ptr(vb), _ptr(fb), _ptr(vbod), _ptr(sfo))
+        return dict(iters=it, v_segs=vs, v_blobs_rhs=vb, f_blobs=fb, v_bodies=vbod,
+                    swimmer_f=sfo)

@@ -82,6 +82,36 @@ void orc_flow_velocities(double *v_flow, const double *x_flow, int num_flow, con
                          const double *x_blobs, int blobs_per_body, const double *x_bodies,
                          int num_bodies, double prefac, int remove_net_force);
 
+/* --- free-body mobility solve (tfs_oracle_solve.c) --------------------- */
+typedef struct orc_solver orc_solver;
+/* One swimmer: nfil x nseg segments, nblob blobs with body-frame references
+ * blob_refs[3*nblob]; tol = LINEAR_SYSTEM_TOL, max_iter =
+ * MAX_LINEAR_SYSTEM_ITER (capped at the system size). Body at the origin
+ * with identity orientation until orc_solver_set_body. */
+orc_solver *orc_solver_create(const orc_params *p, int nfil, int nseg, int nblob,
+                              const double *blob_refs, int end_force_magnitude,
+                              double repulsive_force_factor, double tol, int max_iter);
+void orc_solver_destroy(orc_solver *s);
+/* body position x[3] and orientation quaternion q = (q0, q1, q2, q3) */
+void orc_solver_set_body(orc_solver *s, const double *x, const double *q);
+/* mobility_solver.cpp:2950-3047 (six solves; updates the warm start) */
+void orc_solver_make_body_reference_matrices(orc_solver *s, const double *x_segs,
+                                             const double *f_segs);
+/* compute_velocities, free-body branch (mobility_solver.cpp:2574-2659):
+ * swimmer_f[6] is the swimmer's total force/torque and gets the blob
+ * repulsion added, as in read_positions_and_forces. Writes v_segs[6 Ns],
+ * v_blobs[3 Nb] (= M_bs f_segs, the RHS source; may be NULL); returns the
+ * GMRES iteration count. The solution (blob forces, body velocity) is the
+ * solver state (orc_solver_state) and the next solve's warm start. */
+int orc_solver_compute_velocities(orc_solver *s, const double *x_segs, const double *f_segs,
+                                  double *swimmer_f, double *v_segs, double *v_blobs);
+/* GMRES on the current rhs/positions (solve_linear_system). */
+int orc_solver_gmres(orc_solver *s);
+void orc_solver_state(const orc_solver *s, double *f_blobs, double *v_bodies, double *body_mob,
+                      double *ktkinv);
+void orc_solver_set_state(orc_solver *s, const double *f_blobs, const double *v_bodies,
+                          const double *body_mob, const double *ktkinv);
+
 #ifdef __cplusplus
 }
 #endif

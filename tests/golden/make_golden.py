@@ -19,7 +19,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-from oracle import ReferenceFlow, ReferenceKernels  # noqa: E402
+from oracle import ReferenceFlow, ReferenceKernels, ReferenceSolver  # noqa: E402
 
 from timfilsimmod_gb300.geometry import make_config  # noqa: E402
 
@@ -120,9 +120,54 @@ def case_flow():
     return res
 
 
+def quat_rot(q):
+    s, a, b, c = q
+    return np.array([[1 - 2 * b * b - 2 * c * c, 2 * a * b - 2 * s * c, 2 * a * c + 2 * s * b],
+                     [2 * a * b + 2 * s * c, 1 - 2 * a * a - 2 * c * c, 2 * b * c - 2 * s * a],
+                     [2 * a * c - 2 * s * b, 2 * b * c + 2 * s * a, 1 - 2 * a * a - 2 * b * b]])
+
+
+def swimmer_force(x_segs, f_segs, body_x):
+    F = f_segs[:, :3].sum(0)
+    T = (np.cross(x_segs - body_x, f_segs[:, :3]) + f_segs[:, 3:]).sum(0)
+    return np.concatenate([F, T])
+
+
+def case_solve():
+    """The reference's own free-body mobility solve (mobility_solver.cpp,
+    LINEAR_SYSTEM_TOL = 1e-10) on the small swimmer: make_body_reference_
+    matrices, then compute_velocities twice -- at the start pose, then with
+    the body translated and rotated (segments moved with it) and new forces,
+    warm-started from the first solution as in a time step sequence."""
+    sw = make_config("small", seed=1)
+    efm = 220.0 * 1800.0 / (2.6 * 2.6 * sw.nseg ** 2)  # END_FORCE_MAGNITUDE, default DL
+    ref = ReferenceSolver(sw.nfil, sw.nseg, sw.blob_references, efm, seg_sep=2.2)
+    res = dict(x_segs=sw.x_segs, f_segs=sw.f_segs, blob_refs=sw.blob_references,
+               nfil=sw.nfil, nseg=sw.nseg, end_force_magnitude_real=efm,
+               end_force_magnitude=int(efm), tol=ref.lib.ref_linear_system_tol())
+    bref = ref.make_body_reference_matrices(sw.x_segs, sw.f_segs)
+    res.update({f"bodyref_{k}": v for k, v in bref.items()})
+    sf = swimmer_force(sw.x_segs, sw.f_segs, np.zeros(3))
+    r1 = ref.compute_velocities(sw.x_segs, sw.f_segs, sf, nt=0)
+    res.update({f"cv1_{k}": v for k, v in r1.items() if k != "v_blobs_rhs"})
+    res["cv1_swimmer_f_in"] = sf
+    q = np.array([0.9, 0.1, -0.3, 0.2])
+    q /= np.linalg.norm(q)
+    bx = np.array([1.5, -2.0, 0.7])
+    R = quat_rot(q)
+    xs2 = bx + sw.x_segs @ R.T
+    f2 = np.random.default_rng(17).normal(size=sw.f_segs.shape)
+    ref.set_body(bx, q)
+    sf2 = swimmer_force(xs2, f2, bx)
+    r2 = ref.compute_velocities(xs2, f2, sf2, nt=1)
+    res.update({f"cv2_{k}": v for k, v in r2.items() if k != "v_blobs_rhs"})
+    res.update(cv2_x_segs=xs2, cv2_f_segs=f2, cv2_body_x=bx, cv2_body_q=q, cv2_swimmer_f_in=sf2)
+    return res
+
+
 def main():
     for name, fn in (("small_matvec", case_small), ("overlap_a16", case_overlap),
-                     ("tiny", case_tiny), ("flow_small", case_flow)):
+                     ("tiny", case_tiny), ("flow_small", case_flow), ("solve_small", case_solve)):
         data = fn()
         path = os.path.join(OUT, f"{name}.npz")
         np.savez_compressed(path, **{k: np.asarray(v) for k, v in data.items()})

@@ -1,0 +1,134 @@
+"""GPU parity of the device-resident free-body solve (compute_velocities,
+GMRES, make_body_reference_matrices) against the reference's own
+mobility_solver.cpp (golden vectors, LINEAR_SYSTEM_TOL = 1e-10) and the CPU
+oracle.
+
+Tolerances (GMRES stops at a relative residual of 1e-10, so two correct
+implementations agree to about that level, not to rounding):
+  FP64:  max-abs error <= 1e-8 x max-abs reference value; GMRES iteration
+         counts within 1 of the reference's
+  FP32C (iterative refinement to the same 1e-10 residual): <= 1e-8 as well
+"""
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+TOL = 1e-8
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_max(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, f"{name}.npz"))
+
+
+def make_solver(d, precision):
+    from timfilsimmod_gb300.mobility import RpyMobilitySolver
+
+    s = RpyMobilitySolver(1, int(d["nfil"]), int(d["nseg"]), d["blob_refs"].shape[0],
+                          precision=precision, end_force_magnitude=int(d["end_force_magnitude"]))
+    s.set_blob_references(d["blob_refs"])
+    s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+    s.set_linear_solver(float(d["tol"]))
+    return s
+
+
+def set_segments(s, xs, fs):
+    s.x_segs_host[:] = np.asarray(xs).ravel()
+    s.f_segs_host[:] = np.asarray(fs).ravel()
+    s.copy_segment_positions_to_device()
+    s.copy_segment_forces_to_device()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_solve_sequence_matches_reference(precision):
+    d = load("solve_small")
+    s = make_solver(d, precision)
+    set_segments(s, d["x_segs"], d["f_segs"])
+    bm, kt = s.make_body_reference_matrices()
+    assert rel_max(kt, d["bodyref_ktkinv"]) < 1e-12
+    assert rel_max(bm, d["bodyref_body_mobility"]) < TOL
+    # first step: body at the origin
+    set_segments(s, d["x_segs"], d["f_segs"])
+    it1, sf1 = s.compute_velocities(d["cv1_swimmer_f_in"])
+    s.copy_segment_velocities_to_host()
+    s.wait_for_device()
+    out1 = dict(v_segs=s.v_segs_host.copy(), f_blobs=s.blob_forces(), v_bodies=s.body_velocities())
+    # second step: moved and rotated body, new forces, warm start from the first
+    s.set_body_pose(d["cv2_body_x"], d["cv2_body_q"])
+    set_segments(s, d["cv2_x_segs"], d["cv2_f_segs"])
+    it2, sf2 = s.compute_velocities(d["cv2_swimmer_f_in"])
+    s.copy_segment_velocities_to_host()
+    s.wait_for_device()
+    out2 = dict(v_segs=s.v_segs_host.copy(), f_blobs=s.blob_forces(), v_bodies=s.body_velocities())
+    info = s.solve_info()
+    s.finalise()
+    print(precision, "iters", it1, it2, "ref", int(d["cv1_iters"]), int(d["cv2_iters"]), info)
+    assert rel_max(sf1, d["cv1_swimmer_f"]) < 1e-12
+    assert rel_max(sf2, d["cv2_swimmer_f"]) < 1e-12
+    for k in ("v_segs", "f_blobs", "v_bodies"):
+        e1, e2 = rel_max(out1[k], d[f"cv1_{k}"]), rel_max(out2[k], d[f"cv2_{k}"])
+        print(precision, k, e1, e2)
+        assert e1 < TOL and e2 < TOL, (k, e1, e2)
+    if precision == "fp64":
+        assert abs(it1 - int(d["cv1_iters"])) <= 1 and abs(it2 - int(d["cv2_iters"])) <= 1
+    assert info["rel_residual"] <= float(d["tol"])
+
+
+def test_zero_rhs_and_warm_start_exit():
+    d = load("solve_small")
+    s = make_solver(d, "fp64")
+    n = 3 * d["blob_refs"].shape[0] + 6
+    assert s.solve_linear_system(np.zeros(n)) == 0
+    assert np.all(s.body_velocities() == 0) and np.all(s.blob_forces() == 0)
+    rhs = np.random.default_rng(3).normal(size=n)
+    it = s.solve_linear_system(rhs)
+    assert it > 0
+    # solving the same system again starts from its own solution: no iterations
+    assert s.solve_linear_system(rhs) == 0
+    s.finalise()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_medium_swimmer_solve_vs_oracle(precision):
+    """compute_velocities of the medium swimmer (12 800 segments, 2562 blobs)
+    against the oracle's restatement, at LINEAR_SYSTEM_TOL = 1e-10."""
+    from oracle import OracleSolver
+
+    from timfilsimmod_gb300.geometry import make_config
+    from timfilsimmod_gb300.mobility import RpyMobilitySolver
+
+    sw = make_config("medium", seed=3)
+    efm = int(220.0 * 1800.0 / (2.6 * 2.6 * sw.nseg ** 2))
+    F = sw.f_segs[:, :3].sum(0)
+    T = (np.cross(sw.x_segs, sw.f_segs[:, :3]) + sw.f_segs[:, 3:]).sum(0)
+    sf = np.concatenate([F, T])
+    bm_ref = np.eye(6).ravel()  # identity preconditioner matrices: no reference solves needed
+    s = RpyMobilitySolver(1, sw.nfil, sw.nseg, sw.num_blobs, precision=precision,
+                          end_force_magnitude=efm)
+    s.set_blob_references(sw.blob_references)
+    s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+    s.set_linear_solver(1e-10)
+    set_segments(s, sw.x_segs, sw.f_segs)
+    it, sf_out = s.compute_velocities(sf)
+    s.copy_segment_velocities_to_host()
+    s.wait_for_device()
+    vs, fb, vb = s.v_segs_host.copy(), s.blob_forces(), s.body_velocities()
+    s.finalise()
+    o = OracleSolver(sw.nfil, sw.nseg, sw.blob_references, efm, tol=1e-10,
+                     threads=os.cpu_count() or 1)
+    o.set_state(body_mobility=bm_ref, ktkinv=bm_ref)
+    r = o.compute_velocities(sw.x_segs, sw.f_segs, sf)
+    print(precision, "iters", it, r["iters"])
+    assert rel_max(sf_out, r["swimmer_f"]) < 1e-12
+    for k, v in (("v_segs", vs), ("f_blobs", fb), ("v_bodies", vb)):
+        e = rel_max(v, r[k])
+        print(precision, k, e)
+        assert e < TOL, (k, e)

@@ -75,6 +75,20 @@ _SIGNATURES = {
     "tfs_evaluate_blob_segment_mobility": [_H],
     "tfs_evaluate_full_mobility": [_H, _P, _P],
     "tfs_apply_grand_mobility": [_H],
+    "tfs_set_blob_references": [_H, _P],
+    "tfs_set_body_pose": [_H, _P, _P],
+    "tfs_set_linear_solver": [_H, ctypes.c_double, ctypes.c_int],
+    "tfs_set_refinement": [_H, ctypes.c_double, ctypes.c_int],
+    "tfs_make_body_reference_matrices": [_H],
+    "tfs_get_body_reference_matrices": [_H, _P, _P],
+    "tfs_set_body_reference_matrices": [_H, _P, _P],
+    "tfs_compute_velocities": [_H, _P, ctypes.POINTER(ctypes.c_int)],
+    "tfs_solve_linear_system": [_H, _P, ctypes.POINTER(ctypes.c_int)],
+    "tfs_get_body_velocities": [_H, _P],
+    "tfs_set_body_velocities": [_H, _P],
+    "tfs_copy_blob_forces_to_host": [_H, _P],
+    "tfs_solve_info": [_H, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                       ctypes.POINTER(ctypes.c_double)],
     "tfs_solver_enable_kernel_timing": [_H, ctypes.c_int],
     "tfs_solver_kernel_timing": [_H, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
                                  ctypes.POINTER(ctypes.c_int)],

@@ -105,7 +105,8 @@ __global__ void pack_sources_kernel(T *__restrict__ rec, const double *__restric
 // out[i] (= or +=) sum over splits of partial[s][i], s in order.
 __global__ void reduce_partials_kernel(double *__restrict__ out,
                                        const double *__restrict__ partial, int n_elems,
-                                       int splits, int accumulate) {
+                                       int splits, int accumulate, const int *skip) {
+  if (skip != nullptr && *skip) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_elems) return;
   double s = 0.0;
@@ -362,7 +363,7 @@ cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuni
   if (e != cudaSuccess) return e;
   const int n_elems = a.n_tgt * vd;
   reduce_partials_kernel<<<(n_elems + 255) / 256, 256, 0, st>>>(
-      final_out, scratch, n_elems, splits, mode == OUT_ACCUMULATE ? 1 : 0);
+      final_out, scratch, n_elems, splits, mode == OUT_ACCUMULATE ? 1 : 0, a.skip);
   count_launch();
   return cudaGetLastError();
 }

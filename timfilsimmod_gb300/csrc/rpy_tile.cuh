@@ -178,6 +178,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) rpy_tile_kernel(const TileArgs ar
   T *smem = reinterpret_cast<T *>(tile_smem);
   float *hl = reinterpret_cast<float *>(tile_smem + sizeof(T) * TS * LMAX);
 
+  if (args.skip != nullptr && *args.skip) return;
   const int n_tgt = args.n_tgt;
   const double *origin = args.fp32 ? args.origin : nullptr;
   const int tile0 = blockIdx.x * BLOCK * TPT;

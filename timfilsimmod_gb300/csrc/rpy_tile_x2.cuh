@@ -186,6 +186,7 @@ __global__ void __launch_bounds__(BLOCK) rpy_tile_x2_kernel(const TileArgs args)
   float *smem = reinterpret_cast<float *>(tile_smem);
   float *hl = smem + TS * LMAX;
 
+  if (args.skip != nullptr && *args.skip) return;
   const int n_tgt = args.n_tgt;
   const double *origin = args.origin;
   const int tile0 = blockIdx.x * BLOCK * TPT;

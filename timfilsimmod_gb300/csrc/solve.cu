@@ -1,0 +1,494 @@
+// solve.cu -- the free-body mobility solve behind the C ABI: body geometry
+// and pose, make_body_reference_matrices, and compute_velocities
+// (src/cilia/mobility/mobility_solver.cpp:2574-2659 and :2950-3047) on the
+// device, with the GMRES of gmres.cu. In FP32C mode the linear solve is
+// iterative refinement: FP64 residuals r = rhs - A x around inner GMRES
+// solves whose blob-blob products run in FP32 with compensated sums.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "tfs_solver.h"
+
+using namespace tfs;
+
+namespace {
+
+void rot_mat(double *R, const double *q) {
+  const double s = q[0], a = q[1], b = q[2], c = q[3];
+  R[0] = 1.0 - 2.0 * b * b - 2.0 * c * c;  // (0,0)
+  R[4] = 1.0 - 2.0 * a * a - 2.0 * c * c;  // (1,1)
+  R[8] = 1.0 - 2.0 * a * a - 2.0 * b * b;  // (2,2)
+  R[1] = 2.0 * a * b + 2.0 * s * c;        // (1,0)
+  R[3] = 2.0 * a * b - 2.0 * s * c;        // (0,1)
+  R[2] = 2.0 * a * c - 2.0 * s * b;        // (2,0)
+  R[6] = 2.0 * a * c + 2.0 * s * b;        // (0,2)
+  R[5] = 2.0 * b * c + 2.0 * s * a;        // (2,1)
+  R[7] = 2.0 * b * c - 2.0 * s * a;        // (1,2)
+}
+
+// Each 3x3 block B of the 6x6 `in` becomes R B R^T (mobility_solver.cpp:1455-1467).
+void rotate_blocks(double *out, const double *in, const double *R) {
+  for (int bi = 0; bi < 2; ++bi)
+    for (int bj = 0; bj < 2; ++bj) {
+      double RB[9];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double t = 0.0;
+          for (int k = 0; k < 3; ++k) t += R[i + 3 * k] * in[(3 * bi + k) + 6 * (3 * bj + j)];
+          RB[i + 3 * j] = t;
+        }
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double t = 0.0;
+          for (int k = 0; k < 3; ++k) t += RB[i + 3 * k] * R[j + 3 * k];
+          out[(3 * bi + i) + 6 * (3 * bj + j)] = t;
+        }
+    }
+}
+
+bool invert6(double *A) {
+  double M[6][12];
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) {
+      M[i][j] = A[i + 6 * j];
+      M[i][6 + j] = (i == j) ? 1.0 : 0.0;
+    }
+  for (int k = 0; k < 6; ++k) {
+    int p = k;
+    for (int i = k + 1; i < 6; ++i)
+      if (std::fabs(M[i][k]) > std::fabs(M[p][k])) p = i;
+    if (M[p][k] == 0.0) return false;
+    if (p != k)
+      for (int j = 0; j < 12; ++j) std::swap(M[k][j], M[p][j]);
+    const double piv = M[k][k];
+    for (int j = 0; j < 12; ++j) M[k][j] /= piv;
+    for (int i = 0; i < 6; ++i) {
+      if (i == k) continue;
+      const double f = M[i][k];
+      for (int j = 0; j < 12; ++j) M[i][j] -= f * M[k][j];
+    }
+  }
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) A[i + 6 * j] = M[i][6 + j];
+  return true;
+}
+
+int upload_mats(tfs_solver *s) {
+  rotate_blocks(s->mats_host, s->body_mob_ref, s->pose.R);
+  rotate_blocks(s->mats_host + 36, s->ktkinv_ref, s->pose.R);
+  TFS_CUDA(cudaMemcpyAsync(s->mats, s->mats_host, sizeof s->mats_host, cudaMemcpyHostToDevice,
+                           s->stream),
+           "upload body matrices");
+  // the staging buffer may change before an asynchronous copy runs
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "upload body matrices");
+  return TFS_OK;
+}
+
+GmresArgs gmres_args(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies,
+                     GmresScalars *st, double tol, int fp32) {
+  GmresArgs g{};
+  g.n = s->n;
+  g.nb = s->nb;
+  g.max_iter = s->max_iter;
+  g.tol = tol;
+  g.mu = s->cfg.mu;
+  g.a_blob = s->cfg.a_blob;
+  g.fp32 = fp32;
+  g.x_blobs = s->x_blobs;
+  g.diff = s->diff;
+  g.origin = s->origin;
+  g.rec64 = s->rec_blobs;
+  g.rec32 = s->rec_blobs;
+  g.rec32x2 = s->rec_blobs_x2;
+  g.mats = s->mats;
+  g.rhs = rhs;
+  g.soln = s->soln;
+  g.Q = s->Q;
+  g.H = s->H;
+  g.beta = s->beta;
+  g.cs = s->cs;
+  g.sn = s->sn;
+  g.y = s->y;
+  g.z = s->z;
+  g.tmp = s->tmp;
+  g.v = s->vtmp;
+  g.f_blobs = f_blobs;
+  g.v_bodies = v_bodies;
+  g.st = st;
+  return g;
+}
+
+// v = M_bb (the blob records just packed), in FP64 or FP32C; skipped when
+// *skip is set.
+int mbb_product(tfs_solver *s, int fp32, const int *skip) {
+  TileArgs a = base_args(s);
+  a.fp32 = fp32;
+  a.x_tgt = s->x_blobs;
+  a.n_tgt = s->nb;
+  a.a_tgt = s->cfg.a_blob;
+  a.src_a = s->rec_blobs;
+  a.src_a2 = s->rec_blobs_x2;
+  a.n_a = s->nb;
+  a.a_a = s->cfg.a_blob;
+  a.out = s->vtmp;
+  a.skip = skip;
+  cudaError_t e = launch_tile(a, 3, 3, 0, s->tune[fp32][C_BB], s->scratch, s->scratch_elems,
+                              OUT_ASSIGN, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "blob-blob product");
+  return TFS_OK;
+}
+
+int poll(tfs_solver *s, int which, GmresScalars *out) {
+  TFS_CUDA(cudaMemcpyAsync(s->gst_host + which, s->gst + which, sizeof(GmresScalars),
+                           cudaMemcpyDeviceToHost, s->stream),
+           "read solver state");
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "read solver state");
+  *out = s->gst_host[which];
+  return TFS_OK;
+}
+
+// GMRES on rhs with warm start / solution (f_blobs, v_bodies).
+int gmres_run(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies, double tol,
+              int fp32, int *iters) {
+  if (s->nb == 0) return fail(TFS_ESTATE, "the free-body solve needs blobs");
+  GmresScalars *st = s->gst;
+  const GmresArgs g = gmres_args(s, rhs, f_blobs, v_bodies, st, tol, fp32);
+  cudaError_t e;
+  if ((e = launch_gmres_start(g, s->stream)) != cudaSuccess) return cuda_fail(e, "gmres start");
+  int rc = mbb_product(s, fp32, &st->done);
+  if (rc) return rc;
+  if ((e = launch_gmres_residual(g, s->stream)) != cudaSuccess)
+    return cuda_fail(e, "gmres residual");
+  GmresScalars h{};
+  const int max_chunks = s->max_iter / std::max(1, s->chunk) + 2;
+  for (int c = 0; c < max_chunks; ++c) {
+    if ((rc = poll(s, 0, &h)) != TFS_OK) return rc;
+    if (h.done) break;
+    for (int k = 0; k < s->chunk; ++k) {
+      if ((e = launch_gmres_precond(g, s->stream)) != cudaSuccess)
+        return cuda_fail(e, "gmres preconditioner");
+      if ((rc = mbb_product(s, fp32, &st->done)) != TFS_OK) return rc;
+      if ((e = launch_gmres_arnoldi(g, s->stream)) != cudaSuccess)
+        return cuda_fail(e, "gmres arnoldi");
+    }
+  }
+  if ((rc = poll(s, 0, &h)) != TFS_OK) return rc;
+  if (!h.done) return fail(TFS_ENOTCONV, "GMRES did not finish within %d steps", s->max_iter);
+  if (h.status) return fail(TFS_ENAN, "GMRES residual is not finite");
+  *iters = h.iters;
+  s->last_rel = h.rel;
+  return TFS_OK;
+}
+
+// The linear solve of compute_velocities on s->rhs: plain FP64 GMRES, or
+// FP32C iterative refinement.
+int linear_solve(tfs_solver *s, int *iters) {
+  const int fp32 = s->cfg.precision == TFS_FP32C;
+  int rc;
+  if (!fp32) {
+    rc = gmres_run(s, s->rhs, s->f_blobs, s->v_bodies, s->tol, 0, iters);
+    s->last_outer = 1;
+    return rc;
+  }
+  if ((rc = ensure_origin(s)) != TFS_OK) return rc;
+  const int vel = 3 * s->nb;
+  TFS_CUDA(cudaMemcpyAsync(s->xr, s->f_blobs, sizeof(double) * vel, cudaMemcpyDeviceToDevice,
+                           s->stream),
+           "refinement start");
+  TFS_CUDA(cudaMemcpyAsync(s->xr + vel, s->v_bodies, sizeof(double) * 6,
+                           cudaMemcpyDeviceToDevice, s->stream),
+           "refinement start");
+  GmresScalars *outer = s->gst + 1;
+  const GmresArgs g64 = gmres_args(s, s->rhs, nullptr, nullptr, outer, s->tol, 0);
+  int total = 0, cycles = 0;
+  GmresScalars h{};
+  for (int it = 0; it <= s->max_outer; ++it) {
+    cudaError_t e = launch_pack(0, 3, s->rec_blobs, s->x_blobs, s->xr, s->nb, nullptr, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "pack");
+    if ((rc = mbb_product(s, 0, nullptr)) != TFS_OK) return rc;
+    if ((e = launch_refine_residual(g64, s->xr, s->r, s->dx, it, s->stream)) != cudaSuccess)
+      return cuda_fail(e, "refinement residual");
+    if ((rc = poll(s, 1, &h)) != TFS_OK) return rc;
+    if (h.status) return fail(TFS_ENAN, "refinement residual is not finite");
+    if (h.done || it == s->max_outer) break;
+    int inner = 0;
+    rc = gmres_run(s, s->r, s->dx, s->dx + vel, s->inner_tol, 1, &inner);
+    if (rc != TFS_OK && rc != TFS_ENOTCONV) return rc;
+    total += inner;
+    ++cycles;
+    if ((e = launch_axpy(s->xr, s->dx, s->n, s->stream)) != cudaSuccess)
+      return cuda_fail(e, "refinement update");
+  }
+  TFS_CUDA(cudaMemcpyAsync(s->f_blobs, s->xr, sizeof(double) * vel, cudaMemcpyDeviceToDevice,
+                           s->stream),
+           "refinement result");
+  TFS_CUDA(cudaMemcpyAsync(s->v_bodies, s->xr + vel, sizeof(double) * 6,
+                           cudaMemcpyDeviceToDevice, s->stream),
+           "refinement result");
+  *iters = total;
+  s->last_outer = cycles;
+  s->last_rel = h.rel;
+  if (!h.done)
+    return fail(TFS_ENOTCONV, "iterative refinement reached %d cycles at relative residual %.3e",
+                s->max_outer, h.rel);
+  return TFS_OK;
+}
+
+}  // namespace
+
+namespace tfs {
+
+int solve_alloc(tfs_solver *s) {
+  s->n = 3 * s->nb + 6;
+  s->max_iter = std::min(350, s->n);
+  const size_t n = s->n, m = s->max_iter, nb3 = 3 * (size_t)s->nb;
+  int rc;
+  if ((rc = alloc_dev((void **)&s->refs, 8 * nb3)) || (rc = alloc_dev((void **)&s->diff, 8 * nb3)) ||
+      (rc = alloc_dev((void **)&s->mats, 8 * 72)) ||
+      (rc = alloc_dev((void **)&s->Q, 8 * n * (m + 1))) ||
+      (rc = alloc_dev((void **)&s->H, 8 * (m + 1) * (m + 1))) ||
+      (rc = alloc_dev((void **)&s->beta, 8 * (m + 1))) ||
+      (rc = alloc_dev((void **)&s->cs, 8 * (m + 1))) ||
+      (rc = alloc_dev((void **)&s->sn, 8 * (m + 1))) ||
+      (rc = alloc_dev((void **)&s->y, 8 * (m + 1))) || (rc = alloc_dev((void **)&s->z, 8 * n)) ||
+      (rc = alloc_dev((void **)&s->tmp, 8 * n)) || (rc = alloc_dev((void **)&s->soln, 8 * n)) ||
+      (rc = alloc_dev((void **)&s->rhs, 8 * n)) || (rc = alloc_dev((void **)&s->vtmp, 8 * nb3)) ||
+      (rc = alloc_dev((void **)&s->v_bodies, 8 * 6)) ||
+      (rc = alloc_dev((void **)&s->swimmer_f, 8 * 6)) ||
+      (rc = alloc_dev((void **)&s->xr, 8 * n)) || (rc = alloc_dev((void **)&s->r, 8 * n)) ||
+      (rc = alloc_dev((void **)&s->dx, 8 * n)) ||
+      (rc = alloc_dev((void **)&s->gst, 2 * sizeof(GmresScalars))))
+    return rc;
+  if (cudaHostAlloc((void **)&s->gst_host, 2 * sizeof(GmresScalars), cudaHostAllocDefault) !=
+          cudaSuccess ||
+      cudaHostAlloc((void **)&s->f6_host, 8 * 6, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(TFS_ENOMEM, "pinned host allocation failed");
+  }
+  std::memset(s->body_mob_ref, 0, sizeof s->body_mob_ref);
+  std::memset(s->ktkinv_ref, 0, sizeof s->ktkinv_ref);
+  for (int i = 0; i < 6; ++i) {
+    // identity(6) until make_body_reference_matrices (mobility_solver.cpp:112-114)
+    s->body_mob_ref[i + 6 * i] = 1.0;
+    s->ktkinv_ref[i + 6 * i] = 1.0;
+  }
+  const double q[4] = {1, 0, 0, 0};
+  rot_mat(s->pose.R, q);
+  std::memset(s->pose.x, 0, sizeof s->pose.x);
+  cudaMemsetAsync(s->v_bodies, 0, 8 * 6, s->stream);
+  cudaMemsetAsync(s->gst, 0, 2 * sizeof(GmresScalars), s->stream);
+  cudaMemsetAsync(s->diff, 0, 8 * nb3, s->stream);
+  rotate_blocks(s->mats_host, s->body_mob_ref, s->pose.R);
+  rotate_blocks(s->mats_host + 36, s->ktkinv_ref, s->pose.R);
+  if (cudaMemcpy(s->mats, s->mats_host, sizeof s->mats_host, cudaMemcpyHostToDevice) !=
+      cudaSuccess)
+    return fail(TFS_ECUDA, "upload body matrices");
+  return TFS_OK;
+}
+
+void solve_free(tfs_solver *s) {
+  double *bufs[] = {s->refs, s->diff, s->mats, s->Q, s->H, s->beta, s->cs, s->sn, s->y, s->z,
+                    s->tmp, s->soln, s->rhs, s->vtmp, s->v_bodies, s->swimmer_f, s->xr, s->r,
+                    s->dx};
+  for (double *b : bufs) cudaFree(b);
+  cudaFree(s->gst);
+  if (s->gst_host) cudaFreeHost(s->gst_host);
+  if (s->f6_host) cudaFreeHost(s->f6_host);
+}
+
+}  // namespace tfs
+
+extern "C" {
+
+int tfs_set_blob_references(tfs_solver *s, const double *refs) {
+  TFS_CHECK_SOLVER(s);
+  if (refs == nullptr && s->nb > 0) return fail(TFS_EINVAL, "null blob references");
+  if (s->nb > 0)
+    TFS_CUDA(cudaMemcpyAsync(s->refs, refs, sizeof(double) * 3 * s->nb, cudaMemcpyHostToDevice,
+                             s->stream),
+             "copy blob references");
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "copy blob references");
+  s->have_refs = true;
+  return tfs_set_body_pose(s, s->pose.x, nullptr);
+}
+
+int tfs_set_body_pose(tfs_solver *s, const double *x, const double *q) {
+  TFS_CHECK_SOLVER(s);
+  if (x == nullptr) return fail(TFS_EINVAL, "null body position");
+  for (int k = 0; k < 3; ++k) s->pose.x[k] = x[k];
+  if (q != nullptr) {
+    const double nq = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    if (!(nq > 0.0)) return fail(TFS_EINVAL, "zero quaternion");
+    rot_mat(s->pose.R, q);
+  }
+  if (!s->have_refs) return fail(TFS_ESTATE, "set the blob references first");
+  cudaError_t e = launch_blob_positions(s->x_blobs, s->diff, s->refs, s->nb, s->pose, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "blob positions");
+  s->origin_dirty = true;
+  return upload_mats(s);
+}
+
+int tfs_set_linear_solver(tfs_solver *s, double tol, int max_iter) {
+  TFS_CHECK_SOLVER(s);
+  if (!(tol > 0.0) || max_iter < 1) return fail(TFS_EINVAL, "tol must be > 0, max_iter >= 1");
+  const int cap = std::min(350, s->n);
+  if (max_iter > cap)
+    return fail(TFS_EINVAL, "max_iter %d exceeds the Krylov storage of %d columns", max_iter, cap);
+  s->tol = tol;
+  s->max_iter = max_iter;
+  return TFS_OK;
+}
+
+int tfs_set_refinement(tfs_solver *s, double inner_tol, int max_cycles) {
+  TFS_CHECK_SOLVER(s);
+  if (!(inner_tol > 0.0 && inner_tol < 1.0) || max_cycles < 1)
+    return fail(TFS_EINVAL, "inner_tol in (0, 1), max_cycles >= 1");
+  s->inner_tol = inner_tol;
+  s->max_outer = max_cycles;
+  return TFS_OK;
+}
+
+int tfs_make_body_reference_matrices(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  if (!s->have_refs) return fail(TFS_ESTATE, "set the blob references first");
+  // (K^T K)^-1 from the body-frame references (mobility_solver.cpp:2954-2971);
+  // rcross(v) a = a x v.
+  std::vector<double> refs(3 * (size_t)s->nb);
+  TFS_CUDA(cudaMemcpyAsync(refs.data(), s->refs, sizeof(double) * refs.size(),
+                           cudaMemcpyDeviceToHost, s->stream),
+           "read blob references");
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "read blob references");
+  double KTK[36] = {0};
+  KTK[0] = KTK[7] = KTK[14] = (double)s->nb;
+  for (int m = 0; m < s->nb; ++m) {
+    const double *v = &refs[3 * (size_t)m];
+    const double rc[9] = {0, -v[2], v[1], v[2], 0, -v[0], -v[1], v[0], 0};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double rc2 = 0.0;
+        for (int k = 0; k < 3; ++k) rc2 += rc[i + 3 * k] * rc[k + 3 * j];
+        KTK[i + 6 * (3 + j)] += rc[i + 3 * j];
+        KTK[(3 + i) + 6 * j] -= rc[i + 3 * j];
+        KTK[(3 + i) + 6 * (3 + j)] -= rc2;
+      }
+  }
+  if (!invert6(KTK)) return fail(TFS_EINVAL, "K^T K is singular (fewer than 3 distinct blobs?)");
+  std::memcpy(s->ktkinv_ref, KTK, sizeof KTK);
+  int rc;
+  if ((rc = upload_mats(s)) != TFS_OK) return rc;
+  // six solves with rhs = -e_{n-1-j}; each warm-starts from the last
+  double cols[36];
+  for (int j = 0; j < 6; ++j) {
+    cudaError_t e = launch_unit_rhs(s->rhs, s->n, j, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "unit rhs");
+    int iters = 0;
+    if ((rc = linear_solve(s, &iters)) != TFS_OK) return rc;
+    TFS_CUDA(cudaMemcpyAsync(s->f6_host, s->v_bodies, 8 * 6, cudaMemcpyDeviceToHost, s->stream),
+             "read body velocity");
+    TFS_CUDA(cudaStreamSynchronize(s->stream), "read body velocity");
+    for (int i = 0; i < 6; ++i) cols[i + 6 * (5 - j)] = s->f6_host[i];
+  }
+  std::memcpy(s->body_mob_ref, cols, sizeof cols);
+  return upload_mats(s);
+}
+
+int tfs_get_body_reference_matrices(tfs_solver *s, double *body_mobility, double *ktkinv) {
+  TFS_CHECK_SOLVER(s);
+  if (body_mobility) std::memcpy(body_mobility, s->body_mob_ref, sizeof s->body_mob_ref);
+  if (ktkinv) std::memcpy(ktkinv, s->ktkinv_ref, sizeof s->ktkinv_ref);
+  return TFS_OK;
+}
+
+int tfs_set_body_reference_matrices(tfs_solver *s, const double *body_mobility,
+                                    const double *ktkinv) {
+  TFS_CHECK_SOLVER(s);
+  if (body_mobility) std::memcpy(s->body_mob_ref, body_mobility, sizeof s->body_mob_ref);
+  if (ktkinv) std::memcpy(s->ktkinv_ref, ktkinv, sizeof s->ktkinv_ref);
+  return upload_mats(s);
+}
+
+int tfs_compute_velocities(tfs_solver *s, double *swimmer_f, int *gmres_iters) {
+  TFS_CHECK_SOLVER(s);
+  if (swimmer_f == nullptr) return fail(TFS_EINVAL, "null swimmer force");
+  if (s->cfg.nswim != 1) return fail(TFS_EINVAL, "compute_velocities solves one swimmer per solver");
+  if (!s->have_refs) return fail(TFS_ESTATE, "set the blob references first");
+  int rc;
+  // read_positions_and_forces: barrier forces (device f_segs, blob repulsion)
+  if ((rc = tfs_apply_interparticle_forces(s)) != TFS_OK) return rc;
+  std::memcpy(s->f6_host, swimmer_f, 8 * 6);
+  TFS_CUDA(cudaMemcpyAsync(s->swimmer_f, s->f6_host, 8 * 6, cudaMemcpyHostToDevice, s->stream),
+           "copy swimmer force");
+  // v_segs = Mss f_segs, v_blobs = Mbs f_segs
+  if ((rc = tfs_evaluate_segment_segment_mobility(s)) != TFS_OK) return rc;
+  if ((rc = tfs_evaluate_blob_segment_mobility(s)) != TFS_OK) return rc;
+  cudaError_t e = launch_rhs(s->f_rep, s->diff, s->v_blobs, s->nb, s->swimmer_f, s->rhs, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "right-hand side");
+  int iters = 0;
+  if ((rc = linear_solve(s, &iters)) != TFS_OK) return rc;
+  // v_segs += Msb f_blobs (the solved blob forces)
+  if ((rc = tfs_evaluate_segment_blob_mobility(s)) != TFS_OK) return rc;
+  TFS_CUDA(cudaMemcpyAsync(s->f6_host, s->swimmer_f, 8 * 6, cudaMemcpyDeviceToHost, s->stream),
+           "read swimmer force");
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "compute_velocities");
+  std::memcpy(swimmer_f, s->f6_host, 8 * 6);
+  s->last_iters = iters;
+  if (gmres_iters) *gmres_iters = iters;
+  return TFS_OK;
+}
+
+int tfs_solve_linear_system(tfs_solver *s, const double *rhs_host, int *gmres_iters) {
+  TFS_CHECK_SOLVER(s);
+  if (rhs_host == nullptr) return fail(TFS_EINVAL, "null right-hand side");
+  if (!s->have_refs) return fail(TFS_ESTATE, "set the blob references first");
+  TFS_CUDA(cudaMemcpyAsync(s->rhs, rhs_host, sizeof(double) * s->n, cudaMemcpyHostToDevice,
+                           s->stream),
+           "copy right-hand side");
+  int iters = 0, rc;
+  if ((rc = linear_solve(s, &iters)) != TFS_OK) return rc;
+  s->last_iters = iters;
+  if (gmres_iters) *gmres_iters = iters;
+  return tfs_wait_for_device(s);
+}
+
+int tfs_get_body_velocities(tfs_solver *s, double *v_bodies) {
+  TFS_CHECK_SOLVER(s);
+  if (v_bodies == nullptr) return fail(TFS_EINVAL, "null output");
+  TFS_CUDA(cudaMemcpyAsync(s->f6_host, s->v_bodies, 8 * 6, cudaMemcpyDeviceToHost, s->stream),
+           "read body velocity");
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "read body velocity");
+  std::memcpy(v_bodies, s->f6_host, 8 * 6);
+  return TFS_OK;
+}
+
+int tfs_set_body_velocities(tfs_solver *s, const double *v_bodies) {
+  TFS_CHECK_SOLVER(s);
+  if (v_bodies == nullptr) return fail(TFS_EINVAL, "null input");
+  std::memcpy(s->f6_host, v_bodies, 8 * 6);
+  TFS_CUDA(cudaMemcpyAsync(s->v_bodies, s->f6_host, 8 * 6, cudaMemcpyHostToDevice, s->stream),
+           "write body velocity");
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "write body velocity");
+  return TFS_OK;
+}
+
+int tfs_copy_blob_forces_to_host(tfs_solver *s, double *f_blobs_host) {
+  TFS_CHECK_SOLVER(s);
+  if (f_blobs_host == nullptr && s->nb > 0) return fail(TFS_EINVAL, "null host pointer");
+  if (s->nb > 0)
+    TFS_CUDA(cudaMemcpyAsync(f_blobs_host, s->f_blobs, sizeof(double) * 3 * s->nb,
+                             cudaMemcpyDeviceToHost, s->stream),
+             "copy blob forces to host");
+  return TFS_OK;
+}
+
+int tfs_solve_info(tfs_solver *s, int *iters, int *cycles, double *rel_residual) {
+  TFS_CHECK_SOLVER(s);
+  if (iters) *iters = s->last_iters;
+  if (cycles) *cycles = s->last_outer;
+  if (rel_residual) *rel_residual = s->last_rel;
+  return TFS_OK;
+}
+
+}  // extern "C"

@@ -41,39 +41,7 @@ int cuda_fail(cudaError_t e, const char *what) {
 
 using namespace tfs;
 
-struct tfs_solver {
-  tfs_config cfg;
-  int ns = 0, nb = 0;
-  int device = 0;
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-  double *x_segs = nullptr, *f_segs = nullptr, *v_segs = nullptr;
-  double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
-  double *origin = nullptr;  // [4]: mean position and extent
-  void *rec_segs = nullptr, *rec_blobs = nullptr;
-  void *rec_segs_x2 = nullptr, *rec_blobs_x2 = nullptr;  // FP32x2 records
-  double *scratch = nullptr;
-  size_t scratch_elems = 0;
-  bool origin_dirty = true;
-  // launch tuning per precision and (target, source-set) combination
-  TileTuning tune[2][kNumCombos];
-  std::string tuning_report = "{}";
-  // dominant-kernel timing (tfs_solver_enable_kernel_timing)
-  bool timing = false;
-  std::vector<cudaEvent_t> events;  // pairs, in launch order
-  size_t events_used = 0;
-};
-
-#define TFS_CHECK_SOLVER(s)                                          \
-  do {                                                               \
-    if ((s) == nullptr) return fail(TFS_EINVAL, "null solver handle"); \
-  } while (0)
-
-#define TFS_CUDA(call, what)                  \
-  do {                                        \
-    cudaError_t e_ = (call);                  \
-    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-  } while (0)
+#include "tfs_solver.h"
 
 // Next free event pair for the timing hook (nullptr when timing is off).
 static cudaEvent_t *next_events(tfs_solver *s) {
@@ -94,6 +62,7 @@ static cudaEvent_t *next_events(tfs_solver *s) {
 static void free_all(tfs_solver *s) {
   for (cudaEvent_t e : s->events) cudaEventDestroy(e);
   s->events.clear();
+  solve_free(s);
   cudaFree(s->x_segs);
   cudaFree(s->f_segs);
   cudaFree(s->v_segs);
@@ -110,7 +79,7 @@ static void free_all(tfs_solver *s) {
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
-static int alloc_dev(void **p, size_t bytes) {
+int tfs::alloc_dev(void **p, size_t bytes) {
   if (bytes == 0) bytes = 16;
   cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) {
@@ -120,7 +89,7 @@ static int alloc_dev(void **p, size_t bytes) {
   return TFS_OK;
 }
 
-static int ensure_origin(tfs_solver *s) {
+int tfs::ensure_origin(tfs_solver *s) {
   if (!s->origin_dirty) return TFS_OK;
   cudaError_t e = launch_origin(s->x_segs, s->ns, s->x_blobs, s->nb, s->origin, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "origin kernel");
@@ -128,7 +97,7 @@ static int ensure_origin(tfs_solver *s) {
   return TFS_OK;
 }
 
-static int pack(tfs_solver *s, int segs) {
+int tfs::pack(tfs_solver *s, int segs) {
   const int fp32 = s->cfg.precision == TFS_FP32C;
   cudaError_t e = segs ? launch_pack(fp32, 6, s->rec_segs, s->x_segs, s->f_segs, s->ns,
                                      s->origin, s->stream)
@@ -144,7 +113,7 @@ static int pack(tfs_solver *s, int segs) {
   return TFS_OK;
 }
 
-static TileArgs base_args(tfs_solver *s) {
+TileArgs tfs::base_args(tfs_solver *s) {
   TileArgs a{};
   a.origin = s->origin;
   a.fp32 = s->cfg.precision == TFS_FP32C;
@@ -154,7 +123,7 @@ static TileArgs base_args(tfs_solver *s) {
 }
 
 // Product of one block or fused pair of blocks into `out`.
-static int product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mode) {
+int tfs::product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mode) {
   int rc;
   if (s->cfg.precision == TFS_FP32C && (rc = ensure_origin(s)) != TFS_OK) return rc;
   if (src_segs && (rc = pack(s, 1)) != TFS_OK) return rc;
@@ -266,7 +235,8 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
       (rc = alloc_dev(&s->rec_blobs, record_bytes(0, 3) * nb)) ||
       (rc = alloc_dev(&s->rec_segs_x2, 80 * (size_t)ns)) ||
       (rc = alloc_dev(&s->rec_blobs_x2, 48 * (size_t)nb)) ||
-      (rc = alloc_dev((void **)&s->scratch, dsz * s->scratch_elems))) {
+      (rc = alloc_dev((void **)&s->scratch, dsz * s->scratch_elems)) ||
+      (rc = solve_alloc(s))) {
     free_all(s);
     delete s;
     return rc;

@@ -28,6 +28,7 @@ struct TileArgs {
   int fp32;             // 1: FP32 compensated, 0: FP64
   double scale;         // 1 / (8 pi mu)
   double *out;          // velocities, AoS float64 [VD*n_tgt]
+  const int *skip;      // device flag: the launch does nothing when *skip != 0 (or null)
   int splits;           // 0: automatic
   int chunk;            // set by the launcher
   int mode;             // set by the launcher

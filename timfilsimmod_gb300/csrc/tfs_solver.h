@@ -1,0 +1,89 @@
+// tfs_solver.h -- the solver object behind the C ABI (internal to
+// libtfs_gb300.so): device buffers of one swimmer system, launch tuning,
+// and the state of the free-body solve.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/tfs_gb300.h"
+#include "gmres.h"
+#include "tfs_kernels.h"
+
+namespace tfs {
+int fail(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+}  // namespace tfs
+
+struct tfs_solver {
+  tfs_config cfg;
+  int ns = 0, nb = 0;
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  double *x_segs = nullptr, *f_segs = nullptr, *v_segs = nullptr;
+  double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
+  double *origin = nullptr;  // [4]: mean position and extent
+  void *rec_segs = nullptr, *rec_blobs = nullptr;
+  void *rec_segs_x2 = nullptr, *rec_blobs_x2 = nullptr;  // FP32x2 records
+  double *scratch = nullptr;
+  size_t scratch_elems = 0;
+  bool origin_dirty = true;
+
+  // --- free-body solve (solve.cu) ---
+  int n = 0;                 // 3 nb + 6
+  int max_iter = 350;        // MAX_LINEAR_SYSTEM_ITER, capped at n
+  double tol = 1e-4;         // LINEAR_SYSTEM_TOL
+  double inner_tol = 1e-4;   // FP32C: inner GMRES tolerance of each refinement cycle
+  int max_outer = 12;        // FP32C: refinement cycles
+  int chunk = 8;             // Arnoldi steps launched between polls of the done flag
+  bool have_refs = false;
+  double *refs = nullptr, *diff = nullptr;   // 3 nb: body-frame references, R ref
+  tfs::BodyPose pose{};
+  double body_mob_ref[36], ktkinv_ref[36];   // column-major, body frame
+  double mats_host[72];
+  double *mats = nullptr;    // device copy of the rotated matrices
+  double *Q = nullptr, *H = nullptr, *beta = nullptr, *cs = nullptr, *sn = nullptr,
+         *y = nullptr, *z = nullptr, *tmp = nullptr, *soln = nullptr, *rhs = nullptr,
+         *vtmp = nullptr;
+  double *v_bodies = nullptr;  // 6: warm start / solution
+  double *swimmer_f = nullptr; // 6
+  double *xr = nullptr, *r = nullptr, *dx = nullptr;  // FP32C refinement (n each)
+  tfs::GmresScalars *gst = nullptr;   // device scalars: [0] inner, [1] outer
+  tfs::GmresScalars *gst_host = nullptr;  // pinned copies
+  double *f6_host = nullptr;              // pinned 6
+  int last_iters = 0, last_outer = 0;
+  double last_rel = 0.0;
+  // launch tuning per precision and (target, source-set) combination
+  tfs::TileTuning tune[2][tfs::kNumCombos];
+  std::string tuning_report = "{}";
+  // dominant-kernel timing (tfs_solver_enable_kernel_timing)
+  bool timing = false;
+  std::vector<cudaEvent_t> events;  // pairs, in launch order
+  size_t events_used = 0;
+};
+
+
+#define TFS_CHECK_SOLVER(s)                                              \
+  do {                                                                   \
+    if ((s) == nullptr) return tfs::fail(TFS_EINVAL, "null solver handle"); \
+  } while (0)
+
+#define TFS_CUDA(call, what)                                 \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return tfs::cuda_fail(e_, what);  \
+  } while (0)
+
+namespace tfs {
+// helpers shared by tfs_api.cu and solve.cu
+int ensure_origin(tfs_solver *s);
+int pack(tfs_solver *s, int segs);
+TileArgs base_args(tfs_solver *s);
+int product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mode);
+int alloc_dev(void **p, size_t bytes);
+int solve_alloc(tfs_solver *s);
+void solve_free(tfs_solver *s);
+}  // namespace tfs

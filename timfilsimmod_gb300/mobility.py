@@ -220,6 +220,81 @@ class RpyMobilitySolver:
         """v_segs = Mss f_segs + Msb f_blobs; v_blobs = Mbs f_segs + Mbb f_blobs."""
         self._call("tfs_apply_grand_mobility")
 
+    # -- the free-body solve (mobility_solver.cpp: compute_velocities,
+    #    solve_linear_system, make_body_reference_matrices)
+    def set_blob_references(self, blob_refs) -> None:
+        """rigid_body::blob_references: blob offsets in the body frame."""
+        self._refs = np.ascontiguousarray(np.asarray(blob_refs, dtype=np.float64).ravel())
+        self._call("tfs_set_blob_references", _ptr(self._refs))
+
+    def set_body_pose(self, x, q=None) -> None:
+        """rigid_body::x and q (q0, q1, q2, q3); places the blobs on the device."""
+        xx = np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())
+        if q is None:
+            self._call("tfs_set_body_pose", _ptr(xx), None)
+        else:
+            qq = np.ascontiguousarray(np.asarray(q, dtype=np.float64).ravel())
+            self._call("tfs_set_body_pose", _ptr(xx), _ptr(qq))
+
+    def set_linear_solver(self, tol: float, max_iter: int | None = None) -> None:
+        """LINEAR_SYSTEM_TOL and MAX_LINEAR_SYSTEM_ITER."""
+        if max_iter is None:
+            max_iter = min(350, 3 * self.num_blobs + 6)
+        self._call("tfs_set_linear_solver", float(tol), int(max_iter))
+
+    def set_refinement(self, inner_tol: float = 1e-4, max_cycles: int = 12) -> None:
+        self._call("tfs_set_refinement", float(inner_tol), int(max_cycles))
+
+    def make_body_reference_matrices(self) -> tuple[np.ndarray, np.ndarray]:
+        """Returns (body_mobility_reference, KTKinv_reference), 6x6 column-major flat."""
+        self._call("tfs_make_body_reference_matrices")
+        return self.body_reference_matrices()
+
+    def body_reference_matrices(self) -> tuple[np.ndarray, np.ndarray]:
+        bm, kt = np.zeros(36), np.zeros(36)
+        self._call("tfs_get_body_reference_matrices", _ptr(bm), _ptr(kt))
+        return bm, kt
+
+    def set_body_reference_matrices(self, body_mobility=None, ktkinv=None) -> None:
+        a = None if body_mobility is None else np.ascontiguousarray(body_mobility, dtype=np.float64)
+        b = None if ktkinv is None else np.ascontiguousarray(ktkinv, dtype=np.float64)
+        self._call("tfs_set_body_reference_matrices", None if a is None else _ptr(a),
+                   None if b is None else _ptr(b))
+
+    def compute_velocities(self, swimmer_f) -> tuple[int, np.ndarray]:
+        """compute_velocities on the device-resident positions/forces; returns
+        (GMRES iterations, swimmer force with the blob repulsion added)."""
+        f = np.ascontiguousarray(np.array(swimmer_f, dtype=np.float64).ravel())
+        it = ctypes.c_int()
+        self._call("tfs_compute_velocities", _ptr(f), ctypes.byref(it))
+        return it.value, f
+
+    def solve_linear_system(self, rhs) -> int:
+        r = np.ascontiguousarray(np.asarray(rhs, dtype=np.float64).ravel())
+        it = ctypes.c_int()
+        self._call("tfs_solve_linear_system", _ptr(r), ctypes.byref(it))
+        return it.value
+
+    def body_velocities(self) -> np.ndarray:
+        v = np.zeros(6)
+        self._call("tfs_get_body_velocities", _ptr(v))
+        return v
+
+    def set_body_velocities(self, v) -> None:
+        vv = np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel())
+        self._call("tfs_set_body_velocities", _ptr(vv))
+
+    def blob_forces(self) -> np.ndarray:
+        """The solved blob forces (synchronises)."""
+        self._call("tfs_copy_blob_forces_to_host", _ptr(self.f_blobs_host))
+        self.wait_for_device()
+        return self.f_blobs_host.copy()
+
+    def solve_info(self) -> dict:
+        it, cyc, rel = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        self._call("tfs_solve_info", ctypes.byref(it), ctypes.byref(cyc), ctypes.byref(rel))
+        return {"iters": it.value, "cycles": cyc.value, "rel_residual": rel.value}
+
     # -- convenience: set all inputs from arrays (AoS float64)
     def set_state(self, x_segs, f_segs, x_blobs, f_blobs) -> None:
         self.x_segs_host[:] = np.asarray(x_segs, dtype=np.float64).ravel()
