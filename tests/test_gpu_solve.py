@@ -93,9 +93,13 @@ def test_zero_rhs_and_warm_start_exit():
     assert s.solve_linear_system(np.zeros(n)) == 0
     assert np.all(s.body_velocities() == 0) and np.all(s.blob_forces() == 0)
     rhs = np.random.default_rng(3).normal(size=n)
+    # at a tolerance well above rounding, the GMRES residual estimate and the
+    # true residual of the solution agree: a second solve of the same system
+    # starts from the first one's solution and exits before iterating
+    # (mobility_solver.cpp:2304-2307)
+    s.set_linear_solver(1e-6)
     it = s.solve_linear_system(rhs)
     assert it > 0
-    # solving the same system again starts from its own solution: no iterations
     assert s.solve_linear_system(rhs) == 0
     s.finalise()
 
