@@ -107,7 +107,9 @@ def test_zero_rhs_and_warm_start_exit():
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
 def test_medium_swimmer_solve_vs_oracle(precision):
     """compute_velocities of the medium swimmer (12 800 segments, 2562 blobs)
-    against the oracle's restatement, at LINEAR_SYSTEM_TOL = 1e-10."""
+    against the oracle's restatement, at LINEAR_SYSTEM_TOL = 1e-10, after
+    make_body_reference_matrices as the reference runs it; the oracle gets the
+    same body matrices and warm start."""
     from oracle import OracleSolver
 
     from timfilsimmod_gb300.geometry import make_config
@@ -118,21 +120,27 @@ def test_medium_swimmer_solve_vs_oracle(precision):
     F = sw.f_segs[:, :3].sum(0)
     T = (np.cross(sw.x_segs, sw.f_segs[:, :3]) + sw.f_segs[:, 3:]).sum(0)
     sf = np.concatenate([F, T])
-    bm_ref = np.eye(6).ravel()  # identity preconditioner matrices: no reference solves needed
     s = RpyMobilitySolver(1, sw.nfil, sw.nseg, sw.num_blobs, precision=precision,
                           end_force_magnitude=efm)
     s.set_blob_references(sw.blob_references)
     s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
     s.set_linear_solver(1e-10)
     set_segments(s, sw.x_segs, sw.f_segs)
+    bm, kt = s.make_body_reference_matrices()
+    warm_f, warm_v = s.blob_forces(), s.body_velocities()
     it, sf_out = s.compute_velocities(sf)
     s.copy_segment_velocities_to_host()
     s.wait_for_device()
     vs, fb, vb = s.v_segs_host.copy(), s.blob_forces(), s.body_velocities()
     s.finalise()
+    # Stokes drag of the blob sphere (R = 60): the reference's start-up check
+    # (mobility_solver.cpp:3017-3033); a discretised sphere is within a few %
+    R = 60.0
+    drag = np.array([1 / (6 * np.pi * R)] * 3 + [1 / (8 * np.pi * R ** 3)] * 3)
+    assert np.allclose(bm.reshape(6, 6).T.diagonal(), drag, rtol=0.05)
     o = OracleSolver(sw.nfil, sw.nseg, sw.blob_references, efm, tol=1e-10,
                      threads=os.cpu_count() or 1)
-    o.set_state(body_mobility=bm_ref, ktkinv=bm_ref)
+    o.set_state(f_blobs=warm_f, v_bodies=warm_v, body_mobility=bm, ktkinv=kt)
     r = o.compute_velocities(sw.x_segs, sw.f_segs, sf)
     print(precision, "iters", it, r["iters"])
     assert rel_max(sf_out, r["swimmer_f"]) < 1e-12
@@ -140,3 +148,5 @@ def test_medium_swimmer_solve_vs_oracle(precision):
         e = rel_max(v, r[k])
         print(precision, k, e)
         assert e < TOLS[precision], (k, e)
+    if precision == "fp64":
+        assert abs(it - r["iters"]) <= 1
