@@ -144,9 +144,13 @@ def test_medium_swimmer_solve_vs_oracle(precision):
     r = o.compute_velocities(sw.x_segs, sw.f_segs, sf)
     print(precision, "iters", it, r["iters"])
     assert rel_max(sf_out, r["swimmer_f"]) < 1e-12
+    # two correct GMRES runs that stop at a relative residual of 1e-10 one
+    # iteration apart differ by that residual times the conditioning of the
+    # saddle-point system (~1e4 here): bound at 1e-6 for FP64
+    tol = {"fp64": 1e-6, "fp32c": 2e-5}[precision]
     for k, v in (("v_segs", vs), ("f_blobs", fb), ("v_bodies", vb)):
         e = rel_max(v, r[k])
         print(precision, k, e)
-        assert e < TOLS[precision], (k, e)
+        assert e < tol, (k, e)
     if precision == "fp64":
         assert abs(it - r["iters"]) <= 1
