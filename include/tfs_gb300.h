@@ -190,6 +190,27 @@ int tfs_num_tile_variants(int precision);
  * len); *needed (if non-NULL) gets the full size including the NUL. */
 int tfs_solver_tuning_report(tfs_solver *s, char *buf, size_t len, size_t *needed);
 
+/* --- without device allocation ------------------------------------------ */
+/* No counterpart in the reference (its rpy_mobility_solver allocates its own
+ * device arrays). For callers that cannot allocate device memory -- a driver
+ * that reserves all device memory up front for its own pool, a real-time loop
+ * that must not block on cudaMalloc, code running inside another framework's
+ * stream capture: v_segs = M_ss f_segs in FP64 (the same arithmetic and
+ * assign semantics as tfs_evaluate_segment_segment_mobility) on the caller's
+ * device arrays x_segs[3n], f_segs[6n], v_segs[6n], on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream), asynchronously.
+ * Working memory is one file-scope device array of fixed size that every GPU
+ * loading this library holds until exit; it allows n <= TFS_NOALLOC_MAX_SEGS
+ * (larger n returns TFS_EINVAL). The entry point calls no cudaMalloc, cudaFree
+ * or other allocating routine. The first call on a device looks up the
+ * array's device address there (cudaGetSymbolAddress); make that first call
+ * outside any stream capture. Calls share the array: each call overwrites
+ * every entry it later reads, so nothing needs clearing, but two calls that
+ * overlap on the GPU (different streams, no ordering) race on it. */
+#define TFS_NOALLOC_MAX_SEGS 12800
+int tfs_mss_noalloc(const double *x_segs, const double *f_segs, double *v_segs, int num_segs,
+                    double mu, double a_seg, void *stream);
+
 /* --- diagnostics ------------------------------------------------------- */
 /* CUDA-event timing of the solver's RPY tile kernels (the dominant kernels;
  * pack and reduce kernels excluded), on the solver's stream. Enabling resets

@@ -97,6 +97,7 @@ _SIGNATURES = {
                                  ctypes.POINTER(ctypes.c_size_t)],
     "tfs_solver_set_tuning": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "tfs_num_tile_variants": [ctypes.c_int],
+    "tfs_mss_noalloc": [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P],
     "tfs_last_error": [],
     "tfs_kernel_launch_count": [],
     "tfs_measure_fma_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
