@@ -237,6 +237,8 @@ def bench_ours(args):
     s64.copy_blob_velocities_to_host()
     s64.wait_for_device()
     v64 = np.concatenate([s64.v_segs_host, s64.v_blobs_host]).copy()
+    # --- the mobility solve of one Broyden iteration (compute_velocities) -----
+    solve = None if args.no_solve else solve_bench(sw, stream, args, RpyMobilitySolver)
     clocks = sampler.stop()
 
     # max over ranks
@@ -302,12 +304,93 @@ def bench_ours(args):
         }
         if cpu is not None:
             result["cpu_baseline"] = cpu
+        if solve is not None:
+            result["solve"] = solve
     for sv in (s32, s64):
         sv.finalise()
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
     return result
+
+
+def solve_bench(sw, stream, args, RpyMobilitySolver):
+    """compute_velocities (barrier forces, Mss, Mbs, the free-body GMRES
+    solve for blob forces and body velocity, Msb) per Broyden iteration, FP64
+    vs FP32C (iterative refinement), at a 1e-8 relative linear residual. Each
+    step uploads positions and slightly perturbed forces (a Broyden sequence:
+    the warm start is close but not exact) and reads back the segment
+    velocities, all inside the timed region."""
+    import torch
+
+    ns, nb = sw.num_segs, sw.num_blobs
+    F = sw.f_segs[:, :3].sum(0)
+    T = (np.cross(sw.x_segs, sw.f_segs[:, :3]) + sw.f_segs[:, 3:]).sum(0)
+    rng = np.random.default_rng(99)
+    steps = {"fp64": max(3, min(args.steps, 5)), "fp32c": max(3, min(args.steps, 20))}
+    perturb = [1e-3 * rng.normal(size=sw.f_segs.shape) for _ in range(max(steps.values()) + 2)]
+    out, results = {}, {}
+    for precision in ("fp64", "fp32c"):
+        s = RpyMobilitySolver(1, sw.nfil, sw.nseg, nb, precision=precision)
+        s.set_stream(stream.cuda_stream)
+        s.set_blob_references(sw.blob_references)
+        s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+        s.set_linear_solver(1e-8)
+        s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
+        s.make_body_reference_matrices()
+
+        def step(k):
+            f = sw.f_segs + perturb[k]
+            s.f_segs_host[:] = f.ravel()
+            s.copy_segment_positions_to_device()
+            s.copy_segment_forces_to_device()
+            sf = np.concatenate([f[:, :3].sum(0),
+                                 (np.cross(sw.x_segs, f[:, :3]) + f[:, 3:]).sum(0)])
+            it, _ = s.compute_velocities(sf)
+            s.copy_segment_velocities_to_host()
+            s.wait_for_device()
+            return it
+
+        step(0)  # warm-up
+        iters, ms = [], 0.0
+        for k in range(1, steps[precision] + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            iters.append(step(k))
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+        info = s.solve_info()
+        results[precision] = s.v_segs_host.copy()
+        out[precision] = {"value": steps[precision] / (ms * 1e-3), "unit": "solves/s",
+                          "ms_per_solve": ms / steps[precision],
+                          "gmres_iters_mean": float(np.mean(iters)),
+                          "refinement_cycles_last": info["cycles"],
+                          "rel_residual_last": info["rel_residual"], "steps": steps[precision]}
+        s.finalise()
+    # both forms ended on the same step only if their step counts match; compare the
+    # FP32C result with an FP64 solve of its last step
+    s = RpyMobilitySolver(1, sw.nfil, sw.nseg, nb, precision="fp64")
+    s.set_stream(stream.cuda_stream)
+    s.set_blob_references(sw.blob_references)
+    s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+    s.set_linear_solver(1e-8)
+    s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
+    s.make_body_reference_matrices()
+    f = sw.f_segs + perturb[steps["fp32c"]]
+    s.f_segs_host[:] = f.ravel()
+    s.copy_segment_forces_to_device()
+    sf = np.concatenate([f[:, :3].sum(0), (np.cross(sw.x_segs, f[:, :3]) + f[:, 3:]).sum(0)])
+    s.compute_velocities(sf)
+    s.copy_segment_velocities_to_host()
+    s.wait_for_device()
+    ref = s.v_segs_host.copy()
+    s.finalise()
+    err = float(np.linalg.norm(results["fp32c"] - ref) / np.linalg.norm(ref))
+    return {"workload": "compute_velocities (one Broyden iteration's mobility solve), "
+                        "linear residual 1e-8", **out,
+            "speedup_fp32c_vs_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
+            "fp32c_rel_l2_error_v_segs_vs_fp64": err}
 
 
 def cpu_baseline(sw, stride: int):
@@ -404,6 +487,7 @@ def main():
                    help="CPU legs use every n-th target of the workload")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-tune", action="store_true", help="skip the launch autotuner")
+    p.add_argument("--no-solve", action="store_true", help="skip the solve timing")
     args = p.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
