@@ -19,7 +19,7 @@ def main():
     p.add_argument("--config", default="medium")
     p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     p.add_argument("--reps", type=int, default=2)
-    p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier"])
+    p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier", "solve"])
     p.add_argument("--variant", type=int, default=None,
                    help="pin every combination to this tile-kernel variant")
     p.add_argument("--waves", type=int, default=1)
@@ -34,6 +34,14 @@ def main():
     if args.variant is not None:
         for combo in range(6):
             s.set_tuning(combo, args.variant, args.waves)
+    if args.op == "solve":
+        import numpy as np
+
+        s.set_blob_references(sw.blob_references)
+        s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+        s.set_linear_solver(1e-8)
+        s.make_body_reference_matrices()
+        rng = np.random.default_rng(5)
     t0 = time.perf_counter()
     for _ in range(args.reps):
         if args.op == "grand":
@@ -42,6 +50,13 @@ def main():
             s.evaluate_segment_segment_mobility()
         elif args.op == "mbb":
             s.evaluate_blob_blob_mobility()
+        elif args.op == "solve":
+            f = sw.f_segs + 1e-3 * rng.normal(size=sw.f_segs.shape)
+            s.f_segs_host[:] = f.ravel()
+            s.copy_segment_forces_to_device()
+            sf = np.concatenate([f[:, :3].sum(0),
+                                 (np.cross(sw.x_segs, f[:, :3]) + f[:, 3:]).sum(0)])
+            s.compute_velocities(sf)
         else:
             s.apply_interparticle_forces()
     s.wait_for_device()
