@@ -49,9 +49,28 @@ __device__ double block_sum(double v, double *red) {
   return red[32];
 }
 
-// Six simultaneous block sums.
+// Six simultaneous block sums in one pass (red holds >= 33 * 6 doubles):
+// per-warp shuffle sums, then thread k adds the warps' partials of value k in
+// warp order (deterministic).
 __device__ void block_sum6(double (&v)[6], double *red) {
-  for (int k = 0; k < 6; ++k) v[k] = block_sum(v[k], red);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) red[6 * wid + k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double t = 0.0;
+    for (int w = 0; w < nw; ++w) t += red[6 * w + threadIdx.x];
+    red[6 * 32 + threadIdx.x] = t;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 6; ++k) v[k] = red[6 * 32 + k];
 }
 
 __device__ void matvec6(double *out, const double *M, const double *v) {
@@ -165,7 +184,7 @@ __device__ double block_dot(const double *x, const double *y, int n, double *red
 
 // Start: ||rhs||, zero-rhs exit, soln = warm start, pack soln_lambda for M_bb.
 __global__ void __launch_bounds__(kSolveThreads) gmres_start_kernel(GmresArgs a) {
-  __shared__ double red[33];
+  __shared__ double red[6 * 33];
   GmresScalars *st = a.st;
   const int n = a.n, vel = 3 * a.nb;
   double ss = 0.0;
@@ -194,7 +213,7 @@ __global__ void __launch_bounds__(kSolveThreads) gmres_start_kernel(GmresArgs a)
 
 // r0 = rhs - A soln, the warm-start tests, Q_0 = r0 / beta_0.
 __global__ void __launch_bounds__(kSolveThreads) gmres_residual_kernel(GmresArgs a) {
-  __shared__ double red[33];
+  __shared__ double red[6 * 33];
   GmresScalars *st = a.st;
   if (st->done) return;
   const int n = a.n;
@@ -231,7 +250,7 @@ __global__ void __launch_bounds__(kSolveThreads) gmres_residual_kernel(GmresArgs
 
 // z = P^-1 Q_{k-1}; pack z_lambda for M_bb.
 __global__ void __launch_bounds__(kSolveThreads) gmres_precond_kernel(GmresArgs a) {
-  __shared__ double red[33];
+  __shared__ double red[6 * 33];
   __shared__ double sh6[6];
   GmresScalars *st = a.st;
   if (st->done) return;
@@ -243,25 +262,50 @@ __global__ void __launch_bounds__(kSolveThreads) gmres_precond_kernel(GmresArgs 
 // Q_k = A z (from v = M_bb z_lambda), modified Gram-Schmidt, Givens
 // rotations, convergence; on exit the back solve, x = x0 + P^-1 Q y and the
 // solution written to (f_blobs, v_bodies).
+//
+// The new basis vector w is kept in shared memory when it fits (dynamic
+// shared memory of n doubles; otherwise it lives in its Q column) and every
+// thread owns the same entries throughout, so the Gram-Schmidt steps need no
+// barrier beyond their reductions. Each step fuses the previous step's update
+// w -= h_{i-1} q_{i-1} with the next dot product <w, q_i>: the operations on
+// w are those of modified Gram-Schmidt, in the same order.
 __global__ void __launch_bounds__(kSolveThreads) gmres_arnoldi_kernel(GmresArgs a) {
-  __shared__ double red[33];
+  __shared__ double red[6 * 33];
   __shared__ double sh6[6];
   __shared__ int finish;
+  extern __shared__ double wsm[];
   GmresScalars *st = a.st;
   if (st->done) return;
   const int n = a.n, k = st->iter, ld = a.max_iter + 1;
   double *qk = a.Q + (size_t)k * n;
   double *H = a.H;
-  finish_system_mult(a, qk, a.z, a.v, red);
+  double *w = a.w_in_smem ? wsm : qk;
+  finish_system_mult(a, w, a.z, a.v, red);
+  double hprev = 0.0;
+  const double *qprev = nullptr;
   for (int i = 0; i < k; ++i) {
     const double *qi = a.Q + (size_t)i * n;
-    const double h = block_dot(qk, qi, n, red);
-    for (int t = threadIdx.x; t < n; t += blockDim.x) qk[t] -= h * qi[t];
+    double part = 0.0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+      double wt = w[t];
+      if (qprev) wt -= hprev * qprev[t];
+      w[t] = wt;
+      part += wt * qi[t];
+    }
+    const double h = block_sum(part, red);
     if (threadIdx.x == 0) H[i + (size_t)(k - 1) * ld] = h;
-    __syncthreads();
+    hprev = h;
+    qprev = qi;
   }
-  const double qn = sqrt(block_dot(qk, qk, n, red));
-  for (int t = threadIdx.x; t < n; t += blockDim.x) qk[t] /= qn;
+  double part = 0.0;
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    double wt = w[t];
+    if (qprev) wt -= hprev * qprev[t];
+    w[t] = wt;
+    part += wt * wt;
+  }
+  const double qn = sqrt(block_sum(part, red));
+  for (int t = threadIdx.x; t < n; t += blockDim.x) qk[t] = w[t] / qn;
   if (threadIdx.x == 0) {
     double *cs = a.cs, *sn = a.sn, *beta = a.beta;
 #define HH(i, j) H[(i) + (size_t)(j) * ld]
@@ -342,7 +386,7 @@ __global__ void __launch_bounds__(kSolveThreads) refine_residual_kernel(GmresArg
                                                                         const double *x,
                                                                         double *r, double *dx,
                                                                         int outer) {
-  __shared__ double red[33];
+  __shared__ double red[6 * 33];
   GmresScalars *st = a.st;
   const int n = a.n;
   finish_system_mult(a, r, x, a.v, red);  // r = A x
@@ -413,7 +457,7 @@ __global__ void __launch_bounds__(kSolveThreads) rhs_kernel(const double *frep,
                                                              const double *diff,
                                                              const double *v_blobs, int nb,
                                                              double *swimmer_f, double *rhs) {
-  __shared__ double red[33];
+  __shared__ double red[6 * 33];
   double s[6] = {0, 0, 0, 0, 0, 0};
   for (int m = threadIdx.x; m < nb; m += blockDim.x) {
     const double *r = diff + 3 * (size_t)m, *f = frep + 3 * (size_t)m;
@@ -462,8 +506,22 @@ cudaError_t launch_gmres_precond(const GmresArgs &a, cudaStream_t st) {
   count_launch();
   return cudaGetLastError();
 }
+// Largest basis vector kept in shared memory by the Arnoldi kernel.
+constexpr int kMaxSmemVector = 24 * 1024;  // doubles (192 KB)
+
+bool gmres_w_fits_smem(int n) { return n <= kMaxSmemVector; }
+
 cudaError_t launch_gmres_arnoldi(const GmresArgs &a, cudaStream_t st) {
-  gmres_arnoldi_kernel<<<1, kSolveThreads, 0, st>>>(a);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(gmres_arnoldi_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(double) * kMaxSmemVector));
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const size_t smem = a.w_in_smem ? sizeof(double) * a.n : 0;
+  gmres_arnoldi_kernel<<<1, kSolveThreads, smem, st>>>(a);
   count_launch();
   return cudaGetLastError();
 }

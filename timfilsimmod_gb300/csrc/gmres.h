@@ -37,7 +37,10 @@ struct GmresArgs {
   double *v;                // 3 nb: M_bb output
   double *f_blobs, *v_bodies;  // warm start in, solution out
   GmresScalars *st;
+  int w_in_smem;            // Arnoldi keeps the new basis vector in shared memory
 };
+
+bool gmres_w_fits_smem(int n);
 
 cudaError_t launch_gmres_start(const GmresArgs &a, cudaStream_t st);
 cudaError_t launch_gmres_residual(const GmresArgs &a, cudaStream_t st);

@@ -144,11 +144,14 @@ __global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
   const int fil_i = active && !a.target_blobs ? i / a.nseg : -1;
   const double emag = a.repulsive_force_factor * (double)a.end_force_magnitude;
   const int n_src = a.num_segs + a.num_blobs;
+  // this CTA's share of the sources (grid.y splits them)
+  const int s0 = blockIdx.y * a.chunk;
+  const int s1 = min(s0 + a.chunk, n_src);
   double fx = 0.0, fy = 0.0, fz = 0.0;
-  for (int base = 0; base < n_src; base += BLOCK) {
+  for (int base = s0; base < s1; base += BLOCK) {
     const int j = base + threadIdx.x;
     __syncthreads();
-    if (j < n_src) {
+    if (j < s1) {
       const double *xs = j < a.num_segs ? a.x_segs + 3 * (size_t)j
                                         : a.x_blobs + 3 * (size_t)(j - a.num_segs);
       sxd[threadIdx.x][0] = xs[0];
@@ -160,7 +163,7 @@ __global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
     }
     __syncthreads();
     if (!active) continue;
-    const int cnt = min(BLOCK, n_src - base);
+    const int cnt = min(BLOCK, s1 - base);
     for (int q = 0; q < cnt; ++q) {
       const int jj = base + q;
       const bool src_is_seg = jj < a.num_segs;
@@ -194,6 +197,13 @@ __global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
     }
   }
   if (!active) return;
+  if (a.splits > 1) {
+    double *o = a.scratch + ((size_t)blockIdx.y * n_tgt + i) * 3;
+    o[0] = fx;
+    o[1] = fy;
+    o[2] = fz;
+    return;
+  }
   if (a.target_blobs) {
     a.f_blobs_repulsion[3 * (size_t)i] = fx;
     a.f_blobs_repulsion[3 * (size_t)i + 1] = fy;
@@ -368,21 +378,53 @@ cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuni
   return cudaGetLastError();
 }
 
-cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st) {
+// Split barrier forces: out[stride * i + k] (+= or =) sum over splits s in
+// order of partial[s][i][k], k < 3.
+__global__ void barrier_reduce_kernel(double *__restrict__ out, int stride, int accumulate,
+                                      const double *__restrict__ partial, int n_tgt,
+                                      int splits) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= 3 * n_tgt) return;
+  const int i = e / 3, k = e - 3 * i;
+  double s = 0.0;
+  for (int p = 0; p < splits; ++p) s += partial[(size_t)p * 3 * n_tgt + e];
+  double *o = out + (size_t)stride * i + k;
+  *o = accumulate ? *o + s : s;
+}
+
+// One target kind: grid = target CTAs x source splits, the split count chosen
+// for about eight CTAs per SM; partial forces summed in split order.
+static cudaError_t barrier_launch(BarrierArgs a, int target_blobs, cudaStream_t st) {
   constexpr int B = 128;
-  if (a.num_segs > 0) {
-    BarrierArgs s = a;
-    s.target_blobs = 0;
-    barrier_kernel<B><<<(a.num_segs + B - 1) / B, B, 0, st>>>(s);
-    count_launch();
-  }
-  if (a.free_body && a.num_blobs > 0) {
-    BarrierArgs b = a;
-    b.target_blobs = 1;
-    barrier_kernel<B><<<(a.num_blobs + B - 1) / B, B, 0, st>>>(b);
+  a.target_blobs = target_blobs;
+  const int n_tgt = target_blobs ? a.num_blobs : a.num_segs;
+  const int n_src = a.num_segs + a.num_blobs;
+  const int ctas = (n_tgt + B - 1) / B;
+  int splits = std::max(1, (8 * num_sms() + ctas - 1) / ctas);
+  splits = std::min(splits, kMaxSplits);
+  splits = std::min(splits, std::max(1, n_src / (2 * B)));
+  if (a.scratch == nullptr || (size_t)splits * 3 * n_tgt > a.scratch_elems) splits = 1;
+  int chunk = (n_src + splits - 1) / splits;
+  chunk = std::max(B, ((chunk + B - 1) / B) * B);
+  splits = std::max(1, (n_src + chunk - 1) / chunk);
+  a.chunk = chunk;
+  a.splits = splits;
+  barrier_kernel<B><<<dim3(ctas, splits), B, 0, st>>>(a);
+  count_launch();
+  if (splits > 1) {
+    barrier_reduce_kernel<<<(3 * n_tgt + 255) / 256, 256, 0, st>>>(
+        target_blobs ? a.f_blobs_repulsion : a.f_segs, target_blobs ? 3 : 6,
+        target_blobs ? 0 : 1, a.scratch, n_tgt, splits);
     count_launch();
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (a.num_segs > 0 && (e = barrier_launch(a, 0, st)) != cudaSuccess) return e;
+  if (a.free_body && a.num_blobs > 0) e = barrier_launch(a, 1, st);
+  return e;
 }
 
 }  // namespace tfs

@@ -118,6 +118,7 @@ GmresArgs gmres_args(tfs_solver *s, const double *rhs, double *f_blobs, double *
   g.f_blobs = f_blobs;
   g.v_bodies = v_bodies;
   g.st = st;
+  g.w_in_smem = gmres_w_fits_smem(s->n) ? 1 : 0;
   return g;
 }
 

@@ -23,6 +23,27 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static thread_local std::string g_last_error;
 
+// Process-wide tuning results: (precision, combination, Ns, Nb) -> tuning, so
+// solvers created after an autotune of the same sizes start tuned.
+#include <map>
+#include <mutex>
+#include <tuple>
+static std::mutex g_tune_mutex;
+static std::map<std::tuple<int, int, int, int>, TileTuning> g_tune_cache;
+
+void tune_cache_store(int precision, int combo, int ns, int nb, TileTuning t) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  g_tune_cache[std::make_tuple(precision, combo, ns, nb)] = t;
+}
+
+bool tune_cache_lookup(int precision, int combo, int ns, int nb, TileTuning *t) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  auto it = g_tune_cache.find(std::make_tuple(precision, combo, ns, nb));
+  if (it == g_tune_cache.end()) return false;
+  *t = it->second;
+  return true;
+}
+
 int fail(int code, const char *fmt, ...) {
   char buf[512];
   va_list ap;
@@ -210,7 +231,10 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
   if (s == nullptr) return fail(TFS_ENOMEM, "host allocation failed");
   s->cfg = *cfg;
   for (int p = 0; p < 2; ++p)
-    for (int c = 0; c < kNumCombos; ++c) s->tune[p][c] = TileTuning{0, 1};
+    for (int c = 0; c < kNumCombos; ++c) {
+      s->tune[p][c] = TileTuning{0, 1};
+      tune_cache_lookup(p, c, (int)ns, (int)nb, &s->tune[p][c]);
+    }
   s->ns = (int)ns;
   s->nb = (int)nb;
   cudaGetDevice(&s->device);
@@ -364,6 +388,8 @@ int tfs_apply_interparticle_forces(tfs_solver *s) {
   a.end_force_magnitude = s->cfg.end_force_magnitude;
   a.repulsive_force_factor = s->cfg.repulsive_force_factor;
   a.free_body = s->cfg.free_body;
+  a.scratch = s->scratch;
+  a.scratch_elems = s->scratch_elems;
   cudaError_t e = launch_barrier(a, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "barrier kernel");
   return TFS_OK;
@@ -553,6 +579,7 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
       }
       if (rc != TFS_OK) break;
       s->tune[p][c] = best;
+      tune_cache_store(p, c, s->ns, s->nb, best);
       const TileVariant bv = p ? g_variants_f32[best.variant] : g_variants_f64[best.variant];
       char buf[256];
       snprintf(buf, sizeof buf,

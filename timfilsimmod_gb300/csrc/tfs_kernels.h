@@ -45,7 +45,10 @@ struct BarrierArgs {
   int end_force_magnitude;
   double repulsive_force_factor;
   int free_body;
+  double *scratch;            // split partial forces (kMaxSplits * 6 * max(Ns, Nb) doubles)
+  size_t scratch_elems;
   int target_blobs;           // set by the launcher
+  int chunk, splits;          // set by the launcher
 };
 
 // Launch variants of the tile kernel and their dispatch tables
