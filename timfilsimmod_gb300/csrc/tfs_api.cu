@@ -5,6 +5,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -25,9 +28,6 @@ static thread_local std::string g_last_error;
 
 // Process-wide tuning results: (precision, combination, Ns, Nb) -> tuning, so
 // solvers created after an autotune of the same sizes start tuned.
-#include <map>
-#include <mutex>
-#include <tuple>
 static std::mutex g_tune_mutex;
 static std::map<std::tuple<int, int, int, int>, TileTuning> g_tune_cache;
 
