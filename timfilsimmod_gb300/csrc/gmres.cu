@@ -10,18 +10,29 @@
 //             N and KTKinv the body mobility and (K^T K)^-1 rotated to the body's
 //             current orientation,
 // where d_m = R ref_m. Right-preconditioned GMRES without restarts, warm
-// started from the previous (lambda, U, Omega), modified Gram-Schmidt Arnoldi
-// and the reference's Givens sign convention, stopping when
-// |beta_k| / ||rhs|| <= tol or after min(n, max_iter) steps.
+// started from the previous (lambda, U, Omega), the reference's Givens sign
+// convention, stopping when |beta_k| / ||rhs|| <= tol or after
+// min(n, max_iter) steps.
 //
-// Every vector and scalar of the iteration lives on the device. The small
-// per-instance work (preconditioner, K/K^T, Gram-Schmidt, Givens, back
-// solve) runs in single-CTA kernels; the blob-blob product M_bb runs on the
-// tile kernel (rpy_kernels.cu) between them. A `done` flag in device memory
-// makes every later kernel of the sequence return at once, so the host can
-// launch the iteration in chunks (or replay it as a CUDA graph) and only
-// poll the flag between chunks.
+// Work split. GB300 issues 2 FP64 FMAs per clock per SM, so the FP64 vector
+// work of an Arnoldi step (~4 k n FMAs at step k) is spread over the SMs: the
+// blobs are cut into G contiguous slices, one CTA each (the last CTA also owns
+// the 6 body rows). Every reduction (the preconditioner's and K^T's 6-vectors,
+// the Gram-Schmidt dot products, norms) is finished by the last CTA to
+// arrive: each CTA writes its partial sums, and the CTA that takes the last
+// ticket of the kernel's counter adds them in CTA order (deterministic),
+// does the scalar work (6x6 products, Givens rotations, convergence test) and
+// resets the counter. Orthogonalisation is classical Gram-Schmidt applied
+// twice (CGS2: the second pass re-orthogonalises against the same basis),
+// two reductions per step instead of one per basis vector.
+//
+// Every vector and scalar lives on the device; the blob-blob product M_bb
+// runs on the tile kernel (rpy_kernels.cu) between the phases. A `done` flag
+// in device memory makes the iteration kernels return at once, so the host
+// launches steps in chunks and polls the flag between chunks.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "gmres.h"
 #include "tfs_kernels.h"
@@ -29,48 +40,98 @@
 namespace tfs {
 
 constexpr double kPiD = 3.14159265358979323846264338327950288;
-constexpr int kSolveThreads = 1024;
+constexpr int kGT = 128;  // threads per CTA of the GMRES kernels
 
-// Deterministic block sum of one double per thread (all threads get it).
-__device__ double block_sum(double v, double *red) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if (lane == 0) red[wid] = v;
-  __syncthreads();
-  if (wid == 0) {
-    double t = lane < nw ? red[lane] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-    if (lane == 0) red[32] = t;
-  }
-  __syncthreads();
-  return red[32];
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+
+struct Slice {
+  int m0, m1;  // blobs [m0, m1)
+  bool body;   // this CTA owns the six body rows
+};
+
+__device__ __forceinline__ Slice my_slice(const GmresArgs &a) {
+  Slice s;
+  s.m0 = min(a.nb, (int)blockIdx.x * a.blobs_per_cta);
+  s.m1 = min(a.nb, s.m0 + a.blobs_per_cta);
+  s.body = blockIdx.x == gridDim.x - 1;
+  return s;
 }
 
-// Six simultaneous block sums in one pass (red holds >= 33 * 6 doubles):
-// per-warp shuffle sums, then thread k adds the warps' partials of value k in
-// warp order (deterministic).
-__device__ void block_sum6(double (&v)[6], double *red) {
+// Block sum of L values per thread into sh[0..L); all threads get them.
+// red holds >= 32 * L doubles.
+template <int L>
+__device__ void block_sum_vec(double (&v)[L], double *red, double *sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-  for (int k = 0; k < 6; ++k)
+  for (int k = 0; k < L; ++k)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
   __syncthreads();
   if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < 6; ++k) red[6 * wid + k] = v[k];
+    for (int k = 0; k < L; ++k) red[L * wid + k] = v[k];
   __syncthreads();
-  if (threadIdx.x < 6) {
+  if (threadIdx.x < L) {
     double t = 0.0;
-    for (int w = 0; w < nw; ++w) t += red[6 * w + threadIdx.x];
-    red[6 * 32 + threadIdx.x] = t;
+    for (int w = 0; w < nw; ++w) t += red[L * w + threadIdx.x];
+    sh[threadIdx.x] = t;
   }
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < 6; ++k) v[k] = red[6 * 32 + k];
+  for (int k = 0; k < L; ++k) v[k] = sh[k];
+}
+
+// The rows of a slice: its blobs' rows, then (last CTA) the six body rows.
+__device__ __forceinline__ int slice_rows(const Slice &sl) {
+  return 3 * (sl.m1 - sl.m0) + (sl.body ? 6 : 0);
+}
+__device__ __forceinline__ int slice_row(const GmresArgs &a, const Slice &sl, int r) {
+  const int nblob_rows = 3 * (sl.m1 - sl.m0);
+  return r < nblob_rows ? 3 * sl.m0 + r : 3 * a.nb + (r - nblob_rows);
+}
+
+// k dot products <w, Q_i> over this CTA's rows (blob rows only when
+// with_body is false) into part[blockIdx.x * stride + i]. red holds >= 32*64.
+__device__ void block_dots(const GmresArgs &a, const Slice &sl, bool with_body, const double *w,
+                           int k, double *part, int stride, double *red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int rows = 3 * (sl.m1 - sl.m0) + (with_body && sl.body ? 6 : 0);
+  for (int i = 0; i < k; ++i) {
+    const double *qi = a.Q + (size_t)i * a.n;
+    double v = 0.0;
+    for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+      const int t = slice_row(a, sl, r);
+      v += w[t] * qi[t];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wid * 64 + (i & 63)] = v;
+    if ((i & 63) == 63 || i == k - 1) {
+      __syncthreads();
+      const int base = i & ~63;
+      if ((int)threadIdx.x <= i - base) {
+        double t = 0.0;
+        for (int ww = 0; ww < nw; ++ww) t += red[ww * 64 + threadIdx.x];
+        part[(size_t)blockIdx.x * stride + base + threadIdx.x] = t;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Last-CTA election: every CTA calls this after writing its partials; it
+// returns true in exactly one CTA (the last to arrive), which then sees all
+// partials and must reset the counter.
+__device__ bool last_cta(unsigned *counter) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
 }
 
 __device__ void matvec6(double *out, const double *M, const double *v) {
@@ -81,9 +142,7 @@ __device__ void matvec6(double *out, const double *M, const double *v) {
   }
 }
 
-// Pack blob forces f[3 nb] (with blob positions x) into the source-record
-// formats the tile kernel reads: FP64 {x,y,z,fx,fy,fz}; FP32 (centred)
-// {x,y,z,fx,fy,fz,0,0}; FP32x2 {-x,-x,-y,-y,-z,-z,fx,fx,fy,fy,fz,fz}.
+// Blob force records for the M_bb product (FP64 / FP32 / FP32x2 formats).
 __device__ void pack_blob_records(const GmresArgs &a, const double *f, int m) {
   const double *x = a.x_blobs + 3 * (size_t)m;
   if (!a.fp32) {
@@ -107,226 +166,324 @@ __device__ void pack_blob_records(const GmresArgs &a, const double *f, int m) {
   }
 }
 
-// out = P^-1 in (all n entries); `in` and `out` may not alias.
-__device__ void precondition(const GmresArgs &a, double *out, const double *in, double *red,
-                             double *sh6) {
-  const int nb = a.nb, vel = 3 * nb;
-  double b[6] = {0, 0, 0, 0, 0, 0};
-  for (int m = threadIdx.x; m < nb; m += blockDim.x) {
-    const double *d = a.diff + 3 * (size_t)m;
-    const double *l = in + 3 * (size_t)m;
-    b[0] -= l[0];
-    b[1] -= l[1];
-    b[2] -= l[2];
-    b[3] -= d[1] * l[2] - d[2] * l[1];
-    b[4] -= d[2] * l[0] - d[0] * l[2];
-    b[5] -= d[0] * l[1] - d[1] * l[0];
-  }
-  block_sum6(b, red);
-  if (threadIdx.x == 0) {
-    double t1[6], t2[6];
-    matvec6(t1, a.mats + 36, b);     // rotated KTKinv
-    matvec6(t2, a.mats, in + vel);   // rotated body mobility
-    for (int k = 0; k < 6; ++k) sh6[k] = t1[k] - t2[k];
-  }
-  __syncthreads();
-  const double minv = 6.0 * kPiD * a.mu * a.a_blob;
-  for (int m = threadIdx.x; m < nb; m += blockDim.x) {
-    const double *d = a.diff + 3 * (size_t)m;
-    const double *l = in + 3 * (size_t)m;
-    double blk0 = l[0] + sh6[0], blk1 = l[1] + sh6[1], blk2 = l[2] + sh6[2];
-    blk0 += sh6[4] * d[2] - sh6[5] * d[1];
-    blk1 += sh6[5] * d[0] - sh6[3] * d[2];
-    blk2 += sh6[3] * d[1] - sh6[4] * d[0];
-    out[3 * (size_t)m] = minv * blk0;
-    out[3 * (size_t)m + 1] = minv * blk1;
-    out[3 * (size_t)m + 2] = minv * blk2;
-  }
-  if (threadIdx.x < 6) out[vel + threadIdx.x] = sh6[threadIdx.x];
-  __syncthreads();
-}
-
-// w = A x given v = M_bb x_lambda (all n entries of w).
-__device__ void finish_system_mult(const GmresArgs &a, double *w, const double *x,
-                                   const double *v, double *red) {
-  const int nb = a.nb, vel = 3 * nb;
-  const double U0 = x[vel], U1 = x[vel + 1], U2 = x[vel + 2];
-  const double W0 = x[vel + 3], W1 = x[vel + 4], W2 = x[vel + 5];
+// sum over this CTA's blobs of (l_m ; d_m x l_m) into part6[blockIdx.x]
+__device__ void kt_partial(const GmresArgs &a, const Slice &sl, const double *l, double *part6,
+                           double *red, double *sh) {
   double s[6] = {0, 0, 0, 0, 0, 0};
-  for (int m = threadIdx.x; m < nb; m += blockDim.x) {
+  for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += blockDim.x) {
     const double *d = a.diff + 3 * (size_t)m;
-    const double *l = x + 3 * (size_t)m;
-    s[0] -= l[0];
-    s[1] -= l[1];
-    s[2] -= l[2];
-    s[3] -= d[1] * l[2] - d[2] * l[1];
-    s[4] -= d[2] * l[0] - d[0] * l[2];
-    s[5] -= d[0] * l[1] - d[1] * l[0];
-    const double *vv = v + 3 * (size_t)m;
-    w[3 * (size_t)m] = -(U0 - d[1] * W2 + d[2] * W1) + vv[0];
-    w[3 * (size_t)m + 1] = -(U1 - d[2] * W0 + d[0] * W2) + vv[1];
-    w[3 * (size_t)m + 2] = -(U2 - d[0] * W1 + d[1] * W0) + vv[2];
+    const double *v = l + 3 * (size_t)m;
+    s[0] += v[0];
+    s[1] += v[1];
+    s[2] += v[2];
+    s[3] += d[1] * v[2] - d[2] * v[1];
+    s[4] += d[2] * v[0] - d[0] * v[2];
+    s[5] += d[0] * v[1] - d[1] * v[0];
   }
-  block_sum6(s, red);
-  if (threadIdx.x < 6) w[vel + threadIdx.x] = s[threadIdx.x];
+  block_sum_vec<6>(s, red, sh);
+  if (threadIdx.x < 6) part6[6 * blockIdx.x + threadIdx.x] = s[threadIdx.x];
+}
+
+// sum over CTAs (in order) of part6, by the last CTA; result in sh[0..6)
+__device__ void sum_part6(const double *part6, int G, double *sh) {
+  if (threadIdx.x < 6) {
+    double t = 0.0;
+    for (int c = 0; c < G; ++c) t += part6[6 * c + threadIdx.x];
+    sh[threadIdx.x] = t;
+  }
   __syncthreads();
 }
 
-__device__ double block_dot(const double *x, const double *y, int n, double *red) {
-  double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += x[i] * y[i];
-  return block_sum(s, red);
+// ---------------------------------------------------------------------------
+// preconditioner: out = P^-1 in, in two kernels
+// ---------------------------------------------------------------------------
+
+// (1) b = -sum_m (in_m ; d_m x in_m); the last CTA forms the body rows
+//     out_vel = KTKinv b - N in_vel. use_iter: in = Q_{k-1}.
+__global__ void __launch_bounds__(kGT) precond_reduce_kernel(GmresArgs a, const double *in_base,
+                                                             double *out, int use_iter) {
+  __shared__ double red[32 * 8], sh[8];
+  GmresScalars *st = a.st;
+  if (use_iter && st->done) return;
+  const double *in = use_iter ? in_base + (size_t)(st->iter - 1) * a.n : in_base;
+  const Slice sl = my_slice(a);
+  kt_partial(a, sl, in, a.part6, red, sh);
+  if (!last_cta(a.counters + 0)) return;
+  sum_part6(a.part6, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    double b[6], t1[6], t2[6];
+    for (int k = 0; k < 6; ++k) b[k] = -sh[k];
+    matvec6(t1, a.mats + 36, b);         // rotated KTKinv
+    matvec6(t2, a.mats, in + 3 * a.nb);  // rotated body mobility
+    for (int k = 0; k < 6; ++k) out[3 * a.nb + k] = t1[k] - t2[k];
+    a.counters[0] = 0;
+  }
+}
+
+// (2) out_m = 6 pi mu a (in_m + U' + Omega' x d_m); optionally pack out_lambda
+//     as blob records for M_bb.
+__global__ void __launch_bounds__(kGT) precond_apply_kernel(GmresArgs a, const double *in_base,
+                                                            double *out, int use_iter,
+                                                            int pack) {
+  GmresScalars *st = a.st;
+  if (use_iter && st->done) return;
+  const double *in = use_iter ? in_base + (size_t)(st->iter - 1) * a.n : in_base;
+  const Slice sl = my_slice(a);
+  const double *U = out + 3 * a.nb;
+  const double u0 = U[0], u1 = U[1], u2 = U[2], w0 = U[3], w1 = U[4], w2 = U[5];
+  const double minv = 6.0 * kPiD * a.mu * a.a_blob;
+  for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += blockDim.x) {
+    const double *d = a.diff + 3 * (size_t)m;
+    const double *l = in + 3 * (size_t)m;
+    double b0 = l[0] + u0, b1 = l[1] + u1, b2 = l[2] + u2;
+    b0 += w1 * d[2] - w2 * d[1];
+    b1 += w2 * d[0] - w0 * d[2];
+    b2 += w0 * d[1] - w1 * d[0];
+    double *o = out + 3 * (size_t)m;
+    o[0] = minv * b0;
+    o[1] = minv * b1;
+    o[2] = minv * b2;
+    if (pack) pack_blob_records(a, o, m);
+  }
 }
 
 // ---------------------------------------------------------------------------
-// Phase kernels (one CTA per solve).
+// start and residual
 // ---------------------------------------------------------------------------
 
-// Start: ||rhs||, zero-rhs exit, soln = warm start, pack soln_lambda for M_bb.
-__global__ void __launch_bounds__(kSolveThreads) gmres_start_kernel(GmresArgs a) {
-  __shared__ double red[6 * 33];
+// ||rhs|| (last CTA), soln = warm start, pack soln_lambda for M_bb.
+__global__ void __launch_bounds__(kGT) gmres_start_kernel(GmresArgs a) {
+  __shared__ double red[32 * 8], sh[8];
   GmresScalars *st = a.st;
-  const int n = a.n, vel = 3 * a.nb;
-  double ss = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) ss += a.rhs[i] * a.rhs[i];
-  const double nr = sqrt(block_sum(ss, red));
+  const Slice sl = my_slice(a);
+  const int vel = 3 * a.nb;
+  double ss[1] = {0.0};
+  for (int t = 3 * sl.m0 + threadIdx.x; t < 3 * sl.m1; t += blockDim.x) {
+    ss[0] += a.rhs[t] * a.rhs[t];
+    a.soln[t] = a.f_blobs[t];
+  }
+  for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += blockDim.x)
+    pack_blob_records(a, a.f_blobs + 3 * (size_t)m, m);
+  if (sl.body && threadIdx.x < 6) {
+    ss[0] += a.rhs[vel + threadIdx.x] * a.rhs[vel + threadIdx.x];
+    a.soln[vel + threadIdx.x] = a.v_bodies[threadIdx.x];
+  }
+  block_sum_vec<1>(ss, red, sh);
+  if (threadIdx.x == 0) a.part[blockIdx.x] = ss[0];
+  if (!last_cta(a.counters + 1)) return;
   if (threadIdx.x == 0) {
-    st->norm_rhs = nr;
+    double t = 0.0;
+    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[c];
+    st->norm_rhs = sqrt(t);
     st->iter = 0;
     st->done = 0;
     st->iters = 0;
     st->status = 0;
     st->rel = 0.0;
+    st->flag = 0;
+    a.counters[1] = 0;
   }
-  if (nr == 0.0) {
-    // the solution is zero (mobility_solver.cpp:2158-2170)
-    for (int i = threadIdx.x; i < vel; i += blockDim.x) a.f_blobs[i] = 0.0;
-    if (threadIdx.x < 6) a.v_bodies[threadIdx.x] = 0.0;
-    if (threadIdx.x == 0) st->done = 1;
-    return;
-  }
-  for (int i = threadIdx.x; i < vel; i += blockDim.x) a.soln[i] = a.f_blobs[i];
-  if (threadIdx.x < 6) a.soln[vel + threadIdx.x] = a.v_bodies[threadIdx.x];
-  __syncthreads();
-  for (int m = threadIdx.x; m < a.nb; m += blockDim.x) pack_blob_records(a, a.soln + 3 * m, m);
 }
 
-// r0 = rhs - A soln, the warm-start tests, Q_0 = r0 / beta_0.
-__global__ void __launch_bounds__(kSolveThreads) gmres_residual_kernel(GmresArgs a) {
-  __shared__ double red[6 * 33];
+// r0 = rhs - A soln into Q_0 (blob rows per CTA; body rows by the last CTA),
+// beta_0 = ||r0||, and the warm-start tests (mobility_solver.cpp:2279-2320):
+// flag 1 = the warm start already solves the system (done), 2 = discard it,
+// 3 = zero right-hand side (the solution is zero, :2158-2170).
+__global__ void __launch_bounds__(kGT) gmres_residual_kernel(GmresArgs a) {
+  __shared__ double red[32 * 8], sh[8];
   GmresScalars *st = a.st;
-  if (st->done) return;
-  const int n = a.n;
+  const Slice sl = my_slice(a);
+  const int vel = 3 * a.nb;
   double *q0 = a.Q;
-  finish_system_mult(a, q0, a.soln, a.v, red);  // q0 = A soln
-  double ss = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double r = a.rhs[i] - q0[i];
-    q0[i] = r;
-    ss += r * r;
+  const double *x = a.soln;
+  const double u0 = x[vel], u1 = x[vel + 1], u2 = x[vel + 2];
+  const double w0 = x[vel + 3], w1 = x[vel + 4], w2 = x[vel + 5];
+  double ss[1] = {0.0};
+  for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += blockDim.x) {
+    const double *d = a.diff + 3 * (size_t)m;
+    const double *v = a.v + 3 * (size_t)m;
+    const double *b = a.rhs + 3 * (size_t)m;
+    const double r0 = b[0] - (-(u0 - d[1] * w2 + d[2] * w1) + v[0]);
+    const double r1 = b[1] - (-(u1 - d[2] * w0 + d[0] * w2) + v[1]);
+    const double r2 = b[2] - (-(u2 - d[0] * w1 + d[1] * w0) + v[2]);
+    q0[3 * (size_t)m] = r0;
+    q0[3 * (size_t)m + 1] = r1;
+    q0[3 * (size_t)m + 2] = r2;
+    ss[0] += r0 * r0 + r1 * r1 + r2 * r2;
   }
-  double beta0 = sqrt(block_sum(ss, red));
-  const double nr = st->norm_rhs;
-  if (fabs(beta0) <= a.tol * nr) {
-    // the warm start already solves the system (mobility_solver.cpp:2304-2307)
-    if (threadIdx.x == 0) st->done = 1;
-    return;
-  }
-  if (fabs(beta0) > nr) {
-    // discard a poor warm start (:2313-2320)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      a.soln[i] = 0.0;
-      q0[i] = a.rhs[i];
+  kt_partial(a, sl, x, a.part6, red, sh);
+  block_sum_vec<1>(ss, red, sh);
+  if (threadIdx.x == 0) a.part[blockIdx.x] = ss[0];
+  if (!last_cta(a.counters + 2)) return;
+  sum_part6(a.part6, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[c];
+    for (int k = 0; k < 6; ++k) {
+      const double r = a.rhs[vel + k] - (-sh[k]);
+      q0[vel + k] = r;
+      t += r * r;
     }
-    beta0 = nr;
+    const double nr = st->norm_rhs;
+    double beta0 = sqrt(t);
+    int flag = 0;
+    if (nr == 0.0) {
+      flag = 3;
+    } else if (fabs(beta0) <= a.tol * nr) {
+      flag = 1;
+    } else if (fabs(beta0) > nr) {
+      flag = 2;
+      beta0 = nr;
+    }
+    a.beta[0] = beta0;
+    st->flag = flag;
+    if (flag == 1 || flag == 3) st->done = 1;
+    else st->iter = 1;
+    a.counters[2] = 0;
+  }
+}
+
+// Q_0 /= beta_0 (or Q_0 = rhs / ||rhs|| and soln = 0 for a discarded warm
+// start); for a zero right-hand side, f_blobs = v_bodies = 0.
+__global__ void __launch_bounds__(kGT) gmres_residual_scale_kernel(GmresArgs a) {
+  GmresScalars *st = a.st;
+  const Slice sl = my_slice(a);
+  const int flag = st->flag;
+  const double beta0 = a.beta[0];
+  if (flag == 1) return;
+  const int rows = slice_rows(sl);
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    const int t = slice_row(a, sl, r);
+    if (flag == 3) {
+      if (t < 3 * a.nb) a.f_blobs[t] = 0.0;
+      else a.v_bodies[t - 3 * a.nb] = 0.0;
+    } else if (flag == 2) {
+      a.soln[t] = 0.0;
+      a.Q[t] = a.rhs[t] / beta0;
+    } else {
+      a.Q[t] /= beta0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Arnoldi step k: w = A z into Q_k, CGS2 against Q_0..Q_{k-1}, norm, Givens.
+// ---------------------------------------------------------------------------
+
+// w_blob = M_bb z_lambda - (U + Omega x d_m) (v = M_bb z from the tile
+// kernel); first-pass dots over blob rows; the last CTA adds the body rows
+// w_vel = -sum (z_m ; d_m x z_m) and their dot terms: h1.
+__global__ void __launch_bounds__(kGT) arnoldi_dot1_kernel(GmresArgs a) {
+  __shared__ double red[32 * 64], sh[8];
+  GmresScalars *st = a.st;
+  if (st->done) return;
+  const int k = st->iter, n = a.n, vel = 3 * a.nb;
+  const Slice sl = my_slice(a);
+  double *w = a.Q + (size_t)k * n;
+  const double *z = a.z;
+  const double u0 = z[vel], u1 = z[vel + 1], u2 = z[vel + 2];
+  const double w0 = z[vel + 3], w1 = z[vel + 4], w2 = z[vel + 5];
+  for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += blockDim.x) {
+    const double *d = a.diff + 3 * (size_t)m;
+    const double *v = a.v + 3 * (size_t)m;
+    w[3 * (size_t)m] = -(u0 - d[1] * w2 + d[2] * w1) + v[0];
+    w[3 * (size_t)m + 1] = -(u1 - d[2] * w0 + d[0] * w2) + v[1];
+    w[3 * (size_t)m + 2] = -(u2 - d[0] * w1 + d[1] * w0) + v[2];
+  }
+  kt_partial(a, sl, z, a.part6, red, sh);
+  __syncthreads();
+  block_dots(a, sl, false, w, k, a.part, a.part_stride, red);
+  if (!last_cta(a.counters + 3)) return;
+  sum_part6(a.part6, gridDim.x, sh);
+  if (threadIdx.x < 6) w[vel + threadIdx.x] = -sh[threadIdx.x];
+  __syncthreads();
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    double t = 0.0;
+    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[(size_t)c * a.part_stride + i];
+    const double *qi = a.Q + (size_t)i * n;
+    for (int j = 0; j < 6; ++j) t += w[vel + j] * qi[vel + j];
+    a.h1[i] = t;
+  }
+  if (threadIdx.x == 0) a.counters[3] = 0;
+}
+
+// w -= sum_i h1_i Q_i (this CTA's rows), then second-pass dots: h2, and
+// H(:, k-1) = h1 + h2.
+__global__ void __launch_bounds__(kGT) arnoldi_dot2_kernel(GmresArgs a) {
+  __shared__ double red[32 * 64];
+  GmresScalars *st = a.st;
+  if (st->done) return;
+  const int k = st->iter, n = a.n;
+  const Slice sl = my_slice(a);
+  double *w = a.Q + (size_t)k * n;
+  const int rows = slice_rows(sl);
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    const int t = slice_row(a, sl, r);
+    double wt = w[t];
+    for (int i = 0; i < k; ++i) wt -= a.h1[i] * a.Q[(size_t)i * n + t];
+    w[t] = wt;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < n; i += blockDim.x) q0[i] /= beta0;
-  if (threadIdx.x == 0) {
-    a.beta[0] = beta0;
-    st->iter = 1;
+  block_dots(a, sl, true, w, k, a.part, a.part_stride, red);
+  if (!last_cta(a.counters + 4)) return;
+  const int ld = a.max_iter + 1;
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    double t = 0.0;
+    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[(size_t)c * a.part_stride + i];
+    a.h2[i] = t;
+    a.H[i + (size_t)(k - 1) * ld] = a.h1[i] + t;
   }
+  if (threadIdx.x == 0) a.counters[4] = 0;
 }
 
-// z = P^-1 Q_{k-1}; pack z_lambda for M_bb.
-__global__ void __launch_bounds__(kSolveThreads) gmres_precond_kernel(GmresArgs a) {
-  __shared__ double red[6 * 33];
-  __shared__ double sh6[6];
+// w -= sum_i h2_i Q_i, ||w||; the last CTA applies the Givens rotations
+// (mobility_solver.cpp:2370-2413), tests convergence and, when finishing,
+// back-solves for y (:2419-2438).
+__global__ void __launch_bounds__(kGT) arnoldi_norm_kernel(GmresArgs a) {
+  __shared__ double red[32 * 8], sh[8];
   GmresScalars *st = a.st;
   if (st->done) return;
-  const int k = st->iter;
-  precondition(a, a.z, a.Q + (size_t)(k - 1) * a.n, red, sh6);
-  for (int m = threadIdx.x; m < a.nb; m += blockDim.x) pack_blob_records(a, a.z + 3 * m, m);
-}
-
-// Q_k = A z (from v = M_bb z_lambda), modified Gram-Schmidt, Givens
-// rotations, convergence; on exit the back solve, x = x0 + P^-1 Q y and the
-// solution written to (f_blobs, v_bodies).
-//
-// The new basis vector w is kept in shared memory when it fits (dynamic
-// shared memory of n doubles; otherwise it lives in its Q column) and every
-// thread owns the same entries throughout, so the Gram-Schmidt steps need no
-// barrier beyond their reductions. Each step fuses the previous step's update
-// w -= h_{i-1} q_{i-1} with the next dot product <w, q_i>: the operations on
-// w are those of modified Gram-Schmidt, in the same order.
-__global__ void __launch_bounds__(kSolveThreads) gmres_arnoldi_kernel(GmresArgs a) {
-  __shared__ double red[6 * 33];
-  __shared__ double sh6[6];
-  __shared__ int finish;
-  extern __shared__ double wsm[];
-  GmresScalars *st = a.st;
-  if (st->done) return;
-  const int n = a.n, k = st->iter, ld = a.max_iter + 1;
-  double *qk = a.Q + (size_t)k * n;
-  double *H = a.H;
-  double *w = a.w_in_smem ? wsm : qk;
-  finish_system_mult(a, w, a.z, a.v, red);
-  double hprev = 0.0;
-  const double *qprev = nullptr;
-  for (int i = 0; i < k; ++i) {
-    const double *qi = a.Q + (size_t)i * n;
-    double part = 0.0;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-      double wt = w[t];
-      if (qprev) wt -= hprev * qprev[t];
-      w[t] = wt;
-      part += wt * qi[t];
-    }
-    const double h = block_sum(part, red);
-    if (threadIdx.x == 0) H[i + (size_t)(k - 1) * ld] = h;
-    hprev = h;
-    qprev = qi;
-  }
-  double part = 0.0;
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+  const int k = st->iter, n = a.n;
+  const Slice sl = my_slice(a);
+  double *w = a.Q + (size_t)k * n;
+  const int rows = slice_rows(sl);
+  double ss[1] = {0.0};
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    const int t = slice_row(a, sl, r);
     double wt = w[t];
-    if (qprev) wt -= hprev * qprev[t];
+    for (int i = 0; i < k; ++i) wt -= a.h2[i] * a.Q[(size_t)i * n + t];
     w[t] = wt;
-    part += wt * wt;
+    ss[0] += wt * wt;
   }
-  const double qn = sqrt(block_sum(part, red));
-  for (int t = threadIdx.x; t < n; t += blockDim.x) qk[t] = w[t] / qn;
+  block_sum_vec<1>(ss, red, sh);
+  if (threadIdx.x == 0) a.part[blockIdx.x] = ss[0];
+  if (!last_cta(a.counters + 5)) return;
   if (threadIdx.x == 0) {
-    double *cs = a.cs, *sn = a.sn, *beta = a.beta;
+    double t = 0.0;
+    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[c];
+    const double qn = sqrt(t);
+    st->qnorm = qn;
+    const int ld = a.max_iter + 1;
+    double *H = a.H, *cs = a.cs, *sn = a.sn, *beta = a.beta;
 #define HH(i, j) H[(i) + (size_t)(j) * ld]
     HH(k, k - 1) = qn;
     for (int i = 1; i < k; ++i) {
-      const double t = cs[i - 1] * HH(i - 1, k - 1) + sn[i - 1] * HH(i, k - 1);
+      const double tt = cs[i - 1] * HH(i - 1, k - 1) + sn[i - 1] * HH(i, k - 1);
       HH(i, k - 1) = cs[i - 1] * HH(i, k - 1) - sn[i - 1] * HH(i - 1, k - 1);
-      HH(i - 1, k - 1) = t;
+      HH(i - 1, k - 1) = tt;
     }
     const double hd = HH(k - 1, k - 1), hs = HH(k, k - 1);
     if (hs == 0.0) {
       cs[k - 1] = 1.0;
       sn[k - 1] = 0.0;
     } else if (fabs(hs) > fabs(hd)) {
-      const double t = hd / hs;
-      sn[k - 1] = (2.0 * (double)(hs > 0) - 1.0) / sqrt(1.0 + t * t);
-      cs[k - 1] = t * sn[k - 1];
+      const double tt = hd / hs;
+      sn[k - 1] = (2.0 * (double)(hs > 0) - 1.0) / sqrt(1.0 + tt * tt);
+      cs[k - 1] = tt * sn[k - 1];
     } else {
-      const double t = hs / hd;
-      cs[k - 1] = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + t * t);
-      sn[k - 1] = t * cs[k - 1];
+      const double tt = hs / hd;
+      cs[k - 1] = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + tt * tt);
+      sn[k - 1] = tt * cs[k - 1];
     }
     HH(k - 1, k - 1) = cs[k - 1] * hd + sn[k - 1] * hs;
     HH(k, k - 1) = 0.0;
@@ -334,9 +491,9 @@ __global__ void __launch_bounds__(kSolveThreads) gmres_arnoldi_kernel(GmresArgs 
     beta[k - 1] = cs[k - 1] * beta[k - 1];
     const double rel = fabs(beta[k]) / st->norm_rhs;
     st->rel = rel;
-    finish = (rel <= a.tol || k == a.max_iter) ? 1 : 0;
+    bool finish = rel <= a.tol || k == a.max_iter;
     if (!(rel == rel)) {  // NaN: stop and report
-      finish = 1;
+      finish = true;
       st->status = 1;
     }
     if (finish) {
@@ -347,32 +504,58 @@ __global__ void __launch_bounds__(kSolveThreads) gmres_arnoldi_kernel(GmresArgs 
         for (int j = k - 1; j > i; --j) yi -= HH(i, j) * y[j];
         y[i] = yi / HH(i, i);
       }
+      st->iters = k;
+      st->done = 1;
+    } else {
+      st->iter = k + 1;
     }
 #undef HH
+    a.counters[5] = 0;
   }
-  __syncthreads();
-  if (!finish) {
-    if (threadIdx.x == 0) st->iter = k + 1;
-    return;
+}
+
+// Q_k = w / ||w|| (the step was not the last one).
+__global__ void __launch_bounds__(kGT) arnoldi_scale_kernel(GmresArgs a) {
+  GmresScalars *st = a.st;
+  if (st->done) return;
+  const int k = st->iter - 1, n = a.n;
+  const Slice sl = my_slice(a);
+  double *w = a.Q + (size_t)k * n;
+  const double qn = st->qnorm;
+  const int rows = slice_rows(sl);
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    const int t = slice_row(a, sl, r);
+    w[t] = w[t] / qn;
   }
-  // tmp = Q_{0..k-1} y; soln += P^-1 tmp
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+}
+
+// ---------------------------------------------------------------------------
+// finish: tmp = Q y; z = P^-1 tmp; soln += z -> (f_blobs, v_bodies)
+// (mobility_solver.cpp:2440-2563)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kGT) finish_qy_kernel(GmresArgs a) {
+  const int k = a.st->iters, n = a.n;
+  const Slice sl = my_slice(a);
+  const int rows = slice_rows(sl);
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    const int t = slice_row(a, sl, r);
     double s = 0.0;
     for (int i = 0; i < k; ++i) s += a.y[i] * a.Q[(size_t)i * n + t];
     a.tmp[t] = s;
   }
-  __syncthreads();
-  precondition(a, a.z, a.tmp, red, sh6);
+}
+
+__global__ void __launch_bounds__(kGT) finish_update_kernel(GmresArgs a) {
   const int vel = 3 * a.nb;
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+  const Slice sl = my_slice(a);
+  const int rows = slice_rows(sl);
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    const int t = slice_row(a, sl, r);
     const double x = a.soln[t] + a.z[t];
     a.soln[t] = x;
     if (t < vel) a.f_blobs[t] = x;
     else a.v_bodies[t - vel] = x;
-  }
-  if (threadIdx.x == 0) {
-    st->iters = k;
-    st->done = 1;
   }
 }
 
@@ -382,26 +565,54 @@ __global__ void __launch_bounds__(kSolveThreads) gmres_arnoldi_kernel(GmresArgs 
 
 // r = rhs - A x (v = M_bb x_lambda in FP64), rel = ||r|| / ||rhs||; done when
 // rel <= tol (or rhs = 0, where x = 0). Zeroes the correction dx.
-__global__ void __launch_bounds__(kSolveThreads) refine_residual_kernel(GmresArgs a,
-                                                                        const double *x,
-                                                                        double *r, double *dx,
-                                                                        int outer) {
-  __shared__ double red[6 * 33];
+__global__ void __launch_bounds__(kGT) refine_residual_kernel(GmresArgs a, const double *x,
+                                                              double *r, double *dx,
+                                                              int outer) {
+  __shared__ double red[32 * 8], sh[8];
   GmresScalars *st = a.st;
-  const int n = a.n;
-  finish_system_mult(a, r, x, a.v, red);  // r = A x
-  double rr = 0.0, bb = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double b = a.rhs[i];
-    const double t = b - r[i];
-    r[i] = t;
-    rr += t * t;
-    bb += b * b;
-    dx[i] = 0.0;
+  const Slice sl = my_slice(a);
+  const int vel = 3 * a.nb;
+  const double u0 = x[vel], u1 = x[vel + 1], u2 = x[vel + 2];
+  const double w0 = x[vel + 3], w1 = x[vel + 4], w2 = x[vel + 5];
+  double ss[2] = {0.0, 0.0};
+  for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += blockDim.x) {
+    const double *d = a.diff + 3 * (size_t)m;
+    const double *v = a.v + 3 * (size_t)m;
+    const double *b = a.rhs + 3 * (size_t)m;
+    const double ax[3] = {-(u0 - d[1] * w2 + d[2] * w1) + v[0],
+                          -(u1 - d[2] * w0 + d[0] * w2) + v[1],
+                          -(u2 - d[0] * w1 + d[1] * w0) + v[2]};
+    for (int j = 0; j < 3; ++j) {
+      const double rr = b[j] - ax[j];
+      r[3 * (size_t)m + j] = rr;
+      dx[3 * (size_t)m + j] = 0.0;
+      ss[0] += rr * rr;
+      ss[1] += b[j] * b[j];
+    }
   }
-  const double nr = sqrt(block_sum(rr, red));
-  const double nb = sqrt(block_sum(bb, red));
+  kt_partial(a, sl, x, a.part6, red, sh);
+  block_sum_vec<2>(ss, red, sh);
   if (threadIdx.x == 0) {
+    a.part[2 * blockIdx.x] = ss[0];
+    a.part[2 * blockIdx.x + 1] = ss[1];
+  }
+  if (!last_cta(a.counters + 6)) return;
+  sum_part6(a.part6, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    double rr = 0.0, bb = 0.0;
+    for (int c = 0; c < (int)gridDim.x; ++c) {
+      rr += a.part[2 * c];
+      bb += a.part[2 * c + 1];
+    }
+    for (int k = 0; k < 6; ++k) {
+      const double b = a.rhs[vel + k];
+      const double t = b - (-sh[k]);
+      r[vel + k] = t;
+      dx[vel + k] = 0.0;
+      rr += t * t;
+      bb += b * b;
+    }
+    const double nr = sqrt(rr), nb = sqrt(bb);
     if (outer == 0) st->status = 0;
     st->norm_rhs = nb;
     st->rel = nb > 0.0 ? nr / nb : 0.0;
@@ -411,27 +622,13 @@ __global__ void __launch_bounds__(kSolveThreads) refine_residual_kernel(GmresArg
       st->done = 1;
       st->status = 1;
     }
+    a.counters[6] = 0;
   }
-  if (nb == 0.0)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) r[i] = 0.0;
 }
 
 __global__ void axpy_kernel(double *x, const double *d, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     x[i] += d[i];
-}
-
-cudaError_t launch_refine_residual(const GmresArgs &a, const double *x, double *r, double *dx,
-                                   int outer, cudaStream_t st) {
-  refine_residual_kernel<<<1, kSolveThreads, 0, st>>>(a, x, r, dx, outer);
-  count_launch();
-  return cudaGetLastError();
-}
-
-cudaError_t launch_axpy(double *x, const double *d, int n, cudaStream_t st) {
-  axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, d, n);
-  count_launch();
-  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -453,28 +650,22 @@ __global__ void blob_positions_kernel(double *x_blobs, double *diff, const doubl
 
 // swimmer_f += sum_m (frep_m ; d_m x frep_m) (mobility_solver.cpp:208-234),
 // then rhs = [-v_blobs ; -swimmer_f] (assemble_rhs :439-570).
-__global__ void __launch_bounds__(kSolveThreads) rhs_kernel(const double *frep,
-                                                             const double *diff,
-                                                             const double *v_blobs, int nb,
-                                                             double *swimmer_f, double *rhs) {
-  __shared__ double red[6 * 33];
-  double s[6] = {0, 0, 0, 0, 0, 0};
-  for (int m = threadIdx.x; m < nb; m += blockDim.x) {
-    const double *r = diff + 3 * (size_t)m, *f = frep + 3 * (size_t)m;
-    s[0] += f[0];
-    s[1] += f[1];
-    s[2] += f[2];
-    s[3] += r[1] * f[2] - r[2] * f[1];
-    s[4] += r[2] * f[0] - r[0] * f[2];
-    s[5] += r[0] * f[1] - r[1] * f[0];
-  }
-  block_sum6(s, red);
-  for (int i = threadIdx.x; i < 3 * nb; i += blockDim.x) rhs[i] = -v_blobs[i];
+__global__ void __launch_bounds__(kGT) rhs_kernel(GmresArgs a, const double *frep,
+                                                  const double *v_blobs, double *swimmer_f,
+                                                  double *rhs) {
+  __shared__ double red[32 * 8], sh[8];
+  const Slice sl = my_slice(a);
+  const int vel = 3 * a.nb;
+  for (int t = 3 * sl.m0 + threadIdx.x; t < 3 * sl.m1; t += blockDim.x) rhs[t] = -v_blobs[t];
+  kt_partial(a, sl, frep, a.part6, red, sh);
+  if (!last_cta(a.counters + 7)) return;
+  sum_part6(a.part6, gridDim.x, sh);
   if (threadIdx.x < 6) {
-    const double f = swimmer_f[threadIdx.x] + s[threadIdx.x];
+    const double f = swimmer_f[threadIdx.x] + sh[threadIdx.x];
     swimmer_f[threadIdx.x] = f;
-    rhs[3 * nb + threadIdx.x] = -f;
+    rhs[vel + threadIdx.x] = -f;
   }
+  if (threadIdx.x == 0) a.counters[7] = 0;
 }
 
 // rhs = -e_{n-1-j} (make_body_reference_matrices, mobility_solver.cpp:2996-3000)
@@ -483,45 +674,67 @@ __global__ void unit_rhs_kernel(double *rhs, int n, int j) {
     rhs[i] = (i == n - 1 - j) ? -1.0 : 0.0;
 }
 
-// column 5-j of the body mobility = v_bodies
-__global__ void store_body_column_kernel(double *body_mob, const double *v_bodies, int j) {
-  if (threadIdx.x < 6) body_mob[threadIdx.x + 6 * (5 - j)] = v_bodies[threadIdx.x];
-}
-
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+
+int gmres_grid(int nb, int sms, int *blobs_per_cta) {
+  int G = std::max(1, std::min(sms, (nb + 3) / 4));
+  int per = std::max(1, (nb + G - 1) / G);
+  G = std::max(1, (nb + per - 1) / per);
+  *blobs_per_cta = per;
+  return G;
+}
+
 cudaError_t launch_gmres_start(const GmresArgs &a, cudaStream_t st) {
-  gmres_start_kernel<<<1, kSolveThreads, 0, st>>>(a);
+  gmres_start_kernel<<<a.G, kGT, 0, st>>>(a);
   count_launch();
   return cudaGetLastError();
 }
 cudaError_t launch_gmres_residual(const GmresArgs &a, cudaStream_t st) {
-  gmres_residual_kernel<<<1, kSolveThreads, 0, st>>>(a);
+  gmres_residual_kernel<<<a.G, kGT, 0, st>>>(a);
+  count_launch();
+  gmres_residual_scale_kernel<<<a.G, kGT, 0, st>>>(a);
   count_launch();
   return cudaGetLastError();
 }
 cudaError_t launch_gmres_precond(const GmresArgs &a, cudaStream_t st) {
-  gmres_precond_kernel<<<1, kSolveThreads, 0, st>>>(a);
+  precond_reduce_kernel<<<a.G, kGT, 0, st>>>(a, a.Q, a.z, 1);
+  count_launch();
+  precond_apply_kernel<<<a.G, kGT, 0, st>>>(a, a.Q, a.z, 1, 1);
   count_launch();
   return cudaGetLastError();
 }
-// Largest basis vector kept in shared memory by the Arnoldi kernel.
-constexpr int kMaxSmemVector = 24 * 1024;  // doubles (192 KB)
-
-bool gmres_w_fits_smem(int n) { return n <= kMaxSmemVector; }
-
 cudaError_t launch_gmres_arnoldi(const GmresArgs &a, cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(gmres_arnoldi_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(sizeof(double) * kMaxSmemVector));
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
-  const size_t smem = a.w_in_smem ? sizeof(double) * a.n : 0;
-  gmres_arnoldi_kernel<<<1, kSolveThreads, smem, st>>>(a);
+  arnoldi_dot1_kernel<<<a.G, kGT, 0, st>>>(a);
+  count_launch();
+  arnoldi_dot2_kernel<<<a.G, kGT, 0, st>>>(a);
+  count_launch();
+  arnoldi_norm_kernel<<<a.G, kGT, 0, st>>>(a);
+  count_launch();
+  arnoldi_scale_kernel<<<a.G, kGT, 0, st>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+cudaError_t launch_gmres_finish(const GmresArgs &a, cudaStream_t st) {
+  finish_qy_kernel<<<a.G, kGT, 0, st>>>(a);
+  count_launch();
+  precond_reduce_kernel<<<a.G, kGT, 0, st>>>(a, a.tmp, a.z, 0);
+  count_launch();
+  precond_apply_kernel<<<a.G, kGT, 0, st>>>(a, a.tmp, a.z, 0, 0);
+  count_launch();
+  finish_update_kernel<<<a.G, kGT, 0, st>>>(a);
+  count_launch();
+  return cudaGetLastError();
+}
+cudaError_t launch_refine_residual(const GmresArgs &a, const double *x, double *r, double *dx,
+                                   int outer, cudaStream_t st) {
+  refine_residual_kernel<<<a.G, kGT, 0, st>>>(a, x, r, dx, outer);
+  count_launch();
+  return cudaGetLastError();
+}
+cudaError_t launch_axpy(double *x, const double *d, int n, cudaStream_t st) {
+  axpy_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, d, n);
   count_launch();
   return cudaGetLastError();
 }
@@ -532,20 +745,14 @@ cudaError_t launch_blob_positions(double *x_blobs, double *diff, const double *r
   count_launch();
   return cudaGetLastError();
 }
-cudaError_t launch_rhs(const double *frep, const double *diff, const double *v_blobs, int nb,
+cudaError_t launch_rhs(const GmresArgs &a, const double *frep, const double *v_blobs,
                        double *swimmer_f, double *rhs, cudaStream_t st) {
-  rhs_kernel<<<1, kSolveThreads, 0, st>>>(frep, diff, v_blobs, nb, swimmer_f, rhs);
+  rhs_kernel<<<a.G, kGT, 0, st>>>(a, frep, v_blobs, swimmer_f, rhs);
   count_launch();
   return cudaGetLastError();
 }
 cudaError_t launch_unit_rhs(double *rhs, int n, int j, cudaStream_t st) {
   unit_rhs_kernel<<<(n + 255) / 256, 256, 0, st>>>(rhs, n, j);
-  count_launch();
-  return cudaGetLastError();
-}
-cudaError_t launch_store_body_column(double *body_mob, const double *v_bodies, int j,
-                                     cudaStream_t st) {
-  store_body_column_kernel<<<1, 32, 0, st>>>(body_mob, v_bodies, j);
   count_launch();
   return cudaGetLastError();
 }

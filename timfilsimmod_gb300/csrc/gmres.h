@@ -10,10 +10,12 @@ namespace tfs {
 struct GmresScalars {
   double norm_rhs;
   double rel;    // |beta_k| / ||rhs|| of the last step
+  double qnorm;  // ||w|| of the last Arnoldi step
   int iter;      // Arnoldi step being built (k)
   int done;      // 1: finished; later kernels of the sequence return at once
   int iters;     // iterations taken (0: warm start or zero right-hand side)
   int status;    // 0 ok, 1 non-finite residual
+  int flag;      // warm-start test: 1 accepted, 2 discarded, 3 zero right-hand side
 };
 
 // Body pose: position and rotation matrix (column-major).
@@ -37,10 +39,19 @@ struct GmresArgs {
   double *v;                // 3 nb: M_bb output
   double *f_blobs, *v_bodies;  // warm start in, solution out
   GmresScalars *st;
-  int w_in_smem;            // Arnoldi keeps the new basis vector in shared memory
+  // multi-CTA work split: G CTAs of blobs_per_cta blobs (the last CTA also
+  // owns the six body rows); per-CTA partial sums and last-CTA counters
+  int G, blobs_per_cta;
+  double *part;             // G * part_stride
+  int part_stride;          // max_iter + 1
+  double *part6;            // 6 * G
+  unsigned *counters;       // 8, zero between kernels
+  double *h1, *h2;          // max_iter + 1 each: the two Gram-Schmidt passes
 };
 
-bool gmres_w_fits_smem(int n);
+// CTAs and blobs per CTA of the GMRES kernels for nb blobs on `sms` SMs.
+int gmres_grid(int nb, int sms, int *blobs_per_cta);
+cudaError_t launch_gmres_finish(const GmresArgs &a, cudaStream_t st);
 
 cudaError_t launch_gmres_start(const GmresArgs &a, cudaStream_t st);
 cudaError_t launch_gmres_residual(const GmresArgs &a, cudaStream_t st);
@@ -51,10 +62,8 @@ cudaError_t launch_refine_residual(const GmresArgs &a, const double *x, double *
 cudaError_t launch_axpy(double *x, const double *d, int n, cudaStream_t st);
 cudaError_t launch_blob_positions(double *x_blobs, double *diff, const double *refs, int nb,
                                   const BodyPose &pose, cudaStream_t st);
-cudaError_t launch_rhs(const double *frep, const double *diff, const double *v_blobs, int nb,
+cudaError_t launch_rhs(const GmresArgs &a, const double *frep, const double *v_blobs,
                        double *swimmer_f, double *rhs, cudaStream_t st);
 cudaError_t launch_unit_rhs(double *rhs, int n, int j, cudaStream_t st);
-cudaError_t launch_store_body_column(double *body_mob, const double *v_bodies, int j,
-                                     cudaStream_t st);
 
 }  // namespace tfs

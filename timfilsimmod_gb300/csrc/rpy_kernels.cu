@@ -143,6 +143,13 @@ __global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
   const float delta = float(4.0 * extent * 5.9604644775390625e-08 + 1e-30);
   const int fil_i = active && !a.target_blobs ? i / a.nseg : -1;
   const double emag = a.repulsive_force_factor * (double)a.end_force_magnitude;
+  // contact distances of the two source kinds and their FP32 candidate
+  // thresholds (squared, with the rounding margin), hoisted out of the loop
+  const double asum_seg = a.target_blobs ? a.a_blob + a.a_seg : 2.0 * a.a_seg;
+  const double asum_blob = a.target_blobs ? 2.0 * a.a_blob : a.a_seg + a.a_blob;
+  const float thr_seg = float(1.1 * asum_seg) + 2.f * delta;
+  const float thr_blob = float(1.1 * asum_blob) + 2.f * delta;
+  const float thr2_seg = thr_seg * thr_seg * 1.0001f, thr2_blob = thr_blob * thr_blob * 1.0001f;
   const int n_src = a.num_segs + a.num_blobs;
   // this CTA's share of the sources (grid.y splits them)
   const int s0 = blockIdx.y * a.chunk;
@@ -167,15 +174,10 @@ __global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
     for (int q = 0; q < cnt; ++q) {
       const int jj = base + q;
       const bool src_is_seg = jj < a.num_segs;
-      double asum;
-      if (a.target_blobs)
-        asum = src_is_seg ? a.a_blob + a.a_seg : 2.0 * a.a_blob;
-      else
-        asum = src_is_seg ? 2.0 * a.a_seg : a.a_seg + a.a_blob;
       const float dxf = xif - sxf[q][0], dyf = yif - sxf[q][1], dzf = zif - sxf[q][2];
       const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
-      const float thr = float(1.1 * asum) + 2.f * delta;
-      if (d2f >= thr * thr * 1.0001f) continue;
+      if (d2f >= (src_is_seg ? thr2_seg : thr2_blob)) continue;
+      const double asum = src_is_seg ? asum_seg : asum_blob;
       // exclusions, :1319 and :1410
       if (a.target_blobs) {
         if (i + a.num_segs == jj) continue;

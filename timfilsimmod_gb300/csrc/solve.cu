@@ -118,7 +118,14 @@ GmresArgs gmres_args(tfs_solver *s, const double *rhs, double *f_blobs, double *
   g.f_blobs = f_blobs;
   g.v_bodies = v_bodies;
   g.st = st;
-  g.w_in_smem = gmres_w_fits_smem(s->n) ? 1 : 0;
+  g.G = s->gG;
+  g.blobs_per_cta = s->g_blobs_per_cta;
+  g.part = s->gpart;
+  g.part_stride = s->max_iter + 1;
+  g.part6 = s->gpart6;
+  g.counters = s->gcounters;
+  g.h1 = s->gh1;
+  g.h2 = s->gh2;
   return g;
 }
 
@@ -179,6 +186,8 @@ int gmres_run(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodie
   if ((rc = poll(s, 0, &h)) != TFS_OK) return rc;
   if (!h.done) return fail(TFS_ENOTCONV, "GMRES did not finish within %d steps", s->max_iter);
   if (h.status) return fail(TFS_ENAN, "GMRES residual is not finite");
+  if (h.iters > 0 && (e = launch_gmres_finish(g, s->stream)) != cudaSuccess)
+    return cuda_fail(e, "gmres finish");
   *iters = h.iters;
   s->last_rel = h.rel;
   return TFS_OK;
@@ -263,6 +272,14 @@ int solve_alloc(tfs_solver *s) {
       (rc = alloc_dev((void **)&s->dx, 8 * n)) ||
       (rc = alloc_dev((void **)&s->gst, 2 * sizeof(GmresScalars))))
     return rc;
+  s->gG = gmres_grid(std::max(1, s->nb), num_sms(), &s->g_blobs_per_cta);
+  if ((rc = alloc_dev((void **)&s->gpart, 8 * (size_t)s->gG * (m + 1))) ||
+      (rc = alloc_dev((void **)&s->gpart6, 8 * 6 * (size_t)s->gG)) ||
+      (rc = alloc_dev((void **)&s->gh1, 8 * (m + 1))) ||
+      (rc = alloc_dev((void **)&s->gh2, 8 * (m + 1))) ||
+      (rc = alloc_dev((void **)&s->gcounters, 8 * sizeof(unsigned))))
+    return rc;
+  cudaMemsetAsync(s->gcounters, 0, 8 * sizeof(unsigned), s->stream);
   if (cudaHostAlloc((void **)&s->gst_host, 2 * sizeof(GmresScalars), cudaHostAllocDefault) !=
           cudaSuccess ||
       cudaHostAlloc((void **)&s->f6_host, 8 * 6, cudaHostAllocDefault) != cudaSuccess) {
@@ -293,8 +310,9 @@ int solve_alloc(tfs_solver *s) {
 void solve_free(tfs_solver *s) {
   double *bufs[] = {s->refs, s->diff, s->mats, s->Q, s->H, s->beta, s->cs, s->sn, s->y, s->z,
                     s->tmp, s->soln, s->rhs, s->vtmp, s->v_bodies, s->swimmer_f, s->xr, s->r,
-                    s->dx};
+                    s->dx, s->gpart, s->gpart6, s->gh1, s->gh2};
   for (double *b : bufs) cudaFree(b);
+  cudaFree(s->gcounters);
   cudaFree(s->gst);
   if (s->gst_host) cudaFreeHost(s->gst_host);
   if (s->f6_host) cudaFreeHost(s->f6_host);
@@ -425,7 +443,8 @@ int tfs_compute_velocities(tfs_solver *s, double *swimmer_f, int *gmres_iters) {
   // v_segs = Mss f_segs, v_blobs = Mbs f_segs
   if ((rc = tfs_evaluate_segment_segment_mobility(s)) != TFS_OK) return rc;
   if ((rc = tfs_evaluate_blob_segment_mobility(s)) != TFS_OK) return rc;
-  cudaError_t e = launch_rhs(s->f_rep, s->diff, s->v_blobs, s->nb, s->swimmer_f, s->rhs, s->stream);
+  const GmresArgs ga = gmres_args(s, s->rhs, s->f_blobs, s->v_bodies, s->gst, s->tol, 0);
+  cudaError_t e = launch_rhs(ga, s->f_rep, s->v_blobs, s->swimmer_f, s->rhs, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "right-hand side");
   int iters = 0;
   if ((rc = linear_solve(s, &iters)) != TFS_OK) return rc;

@@ -52,6 +52,9 @@ struct tfs_solver {
   double *swimmer_f = nullptr; // 6
   double *xr = nullptr, *r = nullptr, *dx = nullptr;  // FP32C refinement (n each)
   tfs::GmresScalars *gst = nullptr;   // device scalars: [0] inner, [1] outer
+  int gG = 1, g_blobs_per_cta = 1;    // GMRES kernel grid
+  double *gpart = nullptr, *gpart6 = nullptr, *gh1 = nullptr, *gh2 = nullptr;
+  unsigned *gcounters = nullptr;
   tfs::GmresScalars *gst_host = nullptr;  // pinned copies
   double *f6_host = nullptr;              // pinned 6
   int last_iters = 0, last_outer = 0;
