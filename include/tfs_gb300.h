@@ -190,6 +190,40 @@ int tfs_num_tile_variants(int precision);
  * len); *needed (if non-NULL) gets the full size including the NUL. */
 int tfs_solver_tuning_report(tfs_solver *s, char *buf, size_t len, size_t *needed);
 
+/* --- flow-field evaluator ---------------------------------------------- */
+/* Replaces the reference's flow_field_evaluator
+ * (src/flow_field/flow_field_evaluator.hpp:8-61): the fluid velocity at
+ * num_flow points due to the segment forces/torques and blob forces of a
+ * saved state of num_bodies swimmers,
+ *   v(x) = 1/(8 pi mu) [ sum_segs (Stokeslet + rotlet) + sum_blobs Stokeslet ]
+ * (flow_velocities, flow_field_evaluator.cu:13-228; velocities, :546-579).
+ * With blobs_per_body == 0 the segment Stokeslet becomes the Blakelet of a
+ * no-slip wall at z = 0, as in the reference. precision TFS_FP64 (the
+ * reference's arithmetic) or TFS_FP32C (FP32 pair terms about the mean body
+ * centre, compensated sums, FP64 output). Arrays are AoS float64:
+ * x_flow[3 num_flow] v_flow[3 num_flow], x_segs[3 Ns] f_segs[6 Ns],
+ * x_blobs[3 Nb] f_blobs[3 Nb] (NULL when Nb = 0), x_bodies[3 num_bodies],
+ * with Ns = num_bodies * segs_per_body and Nb = num_bodies * blobs_per_body.
+ * A point on top of a source gives inf/NaN there, as in the reference. */
+typedef struct tfs_flow tfs_flow;
+int tfs_flow_create(int num_flow, int num_bodies, int segs_per_body, int blobs_per_body,
+                    int precision, tfs_flow **out);
+int tfs_flow_destroy(tfs_flow *f);
+int tfs_flow_set_stream(tfs_flow *f, void *stream);
+/* read_positions_and_forces (flow_field_evaluator.cu:401-544), from host
+ * arrays; returns once they are on the device. */
+int tfs_flow_copy_inputs_to_device(tfs_flow *f, const double *x_flow, const double *x_segs,
+                                   const double *f_segs, const double *x_blobs,
+                                   const double *f_blobs, const double *x_bodies);
+/* velocities (flow_field_evaluator.cu:546-579); remove_net_force != 0
+ * subtracts, for every source force, its Stokeslet placed at its body's
+ * centre (REMOVE_NET_FORCE_STOKESLET). Asynchronous on the flow's stream. */
+int tfs_flow_velocities(tfs_flow *f, double mu, int remove_net_force);
+int tfs_flow_copy_velocities_to_host(tfs_flow *f, double *v_flow);
+/* Device arrays x_flow[3 num_flow] and v_flow[3 num_flow] (either may be NULL). */
+int tfs_flow_device_buffers(tfs_flow *f, double **x_flow, double **v_flow);
+int tfs_flow_wait(tfs_flow *f);
+
 /* --- without device allocation ------------------------------------------ */
 /* No counterpart in the reference (its rpy_mobility_solver allocates its own
  * device arrays). For callers that cannot allocate device memory -- a driver

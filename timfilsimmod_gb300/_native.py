@@ -97,6 +97,15 @@ _SIGNATURES = {
                                  ctypes.POINTER(ctypes.c_size_t)],
     "tfs_solver_set_tuning": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "tfs_num_tile_variants": [ctypes.c_int],
+    "tfs_flow_create": [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                        ctypes.POINTER(_H)],
+    "tfs_flow_destroy": [_H],
+    "tfs_flow_set_stream": [_H, _P],
+    "tfs_flow_copy_inputs_to_device": [_H, _P, _P, _P, _P, _P, _P],
+    "tfs_flow_velocities": [_H, ctypes.c_double, ctypes.c_int],
+    "tfs_flow_copy_velocities_to_host": [_H, _P],
+    "tfs_flow_device_buffers": [_H, ctypes.POINTER(_P), ctypes.POINTER(_P)],
+    "tfs_flow_wait": [_H],
     "tfs_mss_noalloc": [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P],
     "tfs_last_error": [],
     "tfs_kernel_launch_count": [],

@@ -232,6 +232,15 @@ int num_sms() {
   return g_num_sms;
 }
 
+cudaError_t launch_reduce_partials(double *out, const double *partial, int n_elems, int splits,
+                                   int accumulate, cudaStream_t st) {
+  if (n_elems <= 0) return cudaSuccess;
+  reduce_partials_kernel<<<(n_elems + 255) / 256, 256, 0, st>>>(out, partial, n_elems, splits,
+                                                                accumulate, nullptr);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_origin(const double *xa, int na, const double *xb, int nb, double *out,
                           cudaStream_t st) {
   origin_kernel<<<1, 512, 0, st>>>(xa, na, xb, nb, out);

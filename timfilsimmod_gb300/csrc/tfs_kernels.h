@@ -104,5 +104,9 @@ cudaError_t launch_tile(const TileArgs &a, int vd, int fda, int fdb, TileTuning 
                         double *scratch, size_t scratch_elems, int mode, cudaStream_t st,
                         cudaEvent_t *ev = nullptr);
 cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st);
+// out[i] (= or += with accumulate) sum over splits s, in order, of
+// partial[s * n_elems + i].
+cudaError_t launch_reduce_partials(double *out, const double *partial, int n_elems, int splits,
+                                   int accumulate, cudaStream_t st);
 
 }  // namespace tfs
