@@ -16,6 +16,11 @@ inputs/outputs). Printed: one JSON line (rank 0).
            measured FP32 FMA peak
   fp64     the same product in plain FP64 (the parity drop-in) for comparison
 
+  solve    compute_velocities (the free-body GMRES solve of one Broyden
+           iteration) at a 1e-8 linear residual, FP64 vs FP32C refinement
+  flow     the flow-field evaluator on a 128^3 grid around the large swimmer
+           (80 000 segments, 10 242 blobs), FP32C, with an FP64 subset
+
 `--impl reference` times the reference's RPY sums on the host cores instead
 (the CPU restatement in oracle/, all threads), on a bounded sample of the
 same workload.
@@ -239,6 +244,8 @@ def bench_ours(args):
     v64 = np.concatenate([s64.v_segs_host, s64.v_blobs_host]).copy()
     # --- the mobility solve of one Broyden iteration (compute_velocities) -----
     solve = None if args.no_solve else solve_bench(sw, stream, args, RpyMobilitySolver)
+    # --- the flow-field evaluator on a 128^3 grid around the large swimmer -----
+    flow = None if args.no_flow else flow_bench(stream, flush, args, peak32, peak64, rank)
     clocks = sampler.stop()
 
     # max over ranks
@@ -306,6 +313,8 @@ def bench_ours(args):
             result["cpu_baseline"] = cpu
         if solve is not None:
             result["solve"] = solve
+        if flow is not None:
+            result["flow"] = flow
     for sv in (s32, s64):
         sv.finalise()
     if world > 1:
@@ -391,6 +400,114 @@ def solve_bench(sw, stream, args, RpyMobilitySolver):
                         "linear residual 1e-8", **out,
             "speedup_fp32c_vs_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
             "fp32c_rel_l2_error_v_segs_vs_fp64": err}
+
+
+FLOW_SEG, FLOW_BLOB, FLOW_POINT = 44, 28, 3  # canonical flops per source, per point
+
+
+def flow_bench(stream, flush, args, peak32, peak64, rank):
+    """flow_velocities on a 128^3 grid (2 097 152 points) around the large
+    swimmer (80 000 segments, 10 242 blobs): FP32C on the whole grid (CUDA
+    events per evaluation on the flow's stream, L2 flushed between them), FP64
+    on every 256th grid point (its error against FP32C stated there), the
+    end-to-end call with host arrays, and the CPU oracle on a sample."""
+    import torch
+
+    from timfilsimmod_gb300.flow_field import FlowFieldEvaluator
+    from timfilsimmod_gb300.geometry import flow_grid, make_config
+
+    sw = make_config("large", seed=7 + rank)
+    ns, nb = sw.num_segs, sw.num_blobs
+    reach = float(np.max(np.linalg.norm(sw.x_segs, axis=1)))
+    n = args.flow_grid
+    xf = flow_grid(n, 1.25 * reach)
+    nf = xf.shape[0]
+    flops_per_point = ns * FLOW_SEG + nb * FLOW_BLOB + FLOW_POINT
+    flops = flops_per_point * nf
+
+    ev = FlowFieldEvaluator(1, sw.nfil, sw.nseg, nb, nf, precision="fp32c")
+    ev.set_stream(stream.cuda_stream)
+    ev.read_positions_and_forces(xf, sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs, sw.body_x)
+    variant, _ = ev.autotune(reps=1)
+    steps = max(3, min(args.steps, 5))
+    ev.velocities(copy_to_host=False)  # warm-up
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ev.velocities(copy_to_host=False)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    ms32 = float(np.mean(ms))
+    # end to end: points and sources from host arrays, velocities back to the host
+    e2e_ms = []
+    for _ in range(2):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ev.read_positions_and_forces()
+        v32 = ev.velocities().copy()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    ev.close()
+    # FP64 (the reference's arithmetic) on a subset of the grid
+    sub = slice(None, None, 256)
+    xs_ = np.ascontiguousarray(xf[sub])
+    ev64 = FlowFieldEvaluator(1, sw.nfil, sw.nseg, nb, xs_.shape[0], precision="fp64")
+    ev64.set_stream(stream.cuda_stream)
+    ev64.read_positions_and_forces(xs_, sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs,
+                                   sw.body_x)
+    ev64.velocities(copy_to_host=False)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    ev64.velocities(copy_to_host=False)
+    b.record(stream)
+    v64 = ev64.velocities().copy()
+    ms64 = a.elapsed_time(b)
+    ev64.close()
+    err = float(np.linalg.norm(v32[sub] - v64) / np.linalg.norm(v64))
+    achieved32 = flops / (ms32 * 1e-3) / 1e12
+    achieved64 = flops_per_point * xs_.shape[0] / (ms64 * 1e-3) / 1e12
+    out = {"workload": f"flow_velocities, {n}^3 grid around the large swimmer "
+                       f"(cube of half-width {1.25 * reach:.0f})",
+           "points": nf, "segments": ns, "blobs": nb, "pairs": nf * (ns + nb),
+           "value": nf / (ms32 * 1e-3), "unit": "points/s", "ms_per_grid": ms32,
+           "steps": steps, "launch_variant": variant,
+           "e2e": {"value": nf / (np.mean(e2e_ms) * 1e-3), "unit": "points/s",
+                   "ms_per_grid": float(np.mean(e2e_ms)), "h2d_bytes_per_step":
+                   8 * (3 * nf + 9 * ns + 6 * nb + 3), "d2h_bytes_per_step": 8 * 3 * nf},
+           "roofline": {"bound": "fp32-fma", "kernel": "flow_kernel<float>",
+                        "achieved": achieved32, "peak": peak32 / 1e12, "unit": "TFLOP/s",
+                        "frac": achieved32 / (peak32 / 1e12),
+                        "flops_per_launch": flops,
+                        "note": "event time of velocities(): the two pack kernels "
+                                "(90 242 records) inside it take microseconds"},
+           "fp64_subset": {"points": xs_.shape[0], "ms": ms64,
+                           "value": xs_.shape[0] / (ms64 * 1e-3), "unit": "points/s",
+                           "roofline": {"bound": "fp64-fma", "achieved": achieved64,
+                                        "peak": peak64 / 1e12, "unit": "TFLOP/s",
+                                        "frac": achieved64 / (peak64 / 1e12)}},
+           "fp32c_rel_l2_error_vs_fp64": err,
+           "l2": "flushed between evaluations (256 MB write, outside the events)"}
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from oracle import Oracle
+
+        threads = os.cpu_count() or 1
+        o = Oracle(threads=threads)
+        xc = np.ascontiguousarray(xf[::1024])
+        t0 = time.perf_counter()
+        o.flow_velocities(xc, sw.x_segs, sw.f_segs, ns, sw.x_blobs, sw.f_blobs, nb,
+                          sw.body_x.reshape(1, 3), 1.0 / (8.0 * np.pi), False)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": xc.shape[0] / dt, "unit": "points/s", "cores": threads,
+                               "kind": "port",
+                               "sample": f"every 1024th grid point ({xc.shape[0]} points, "
+                                         f"{dt:.2f} s)"}
+    return out
 
 
 def cpu_baseline(sw, stride: int):
@@ -488,6 +605,8 @@ def main():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-tune", action="store_true", help="skip the launch autotuner")
     p.add_argument("--no-solve", action="store_true", help="skip the solve timing")
+    p.add_argument("--no-flow", action="store_true", help="skip the flow-field timing")
+    p.add_argument("--flow-grid", type=int, default=128, help="flow points per grid axis")
     args = p.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

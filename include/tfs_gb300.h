@@ -220,6 +220,15 @@ int tfs_flow_copy_inputs_to_device(tfs_flow *f, const double *x_flow, const doub
  * centre (REMOVE_NET_FORCE_STOKESLET). Asynchronous on the flow's stream. */
 int tfs_flow_velocities(tfs_flow *f, double mu, int remove_net_force);
 int tfs_flow_copy_velocities_to_host(tfs_flow *f, double *v_flow);
+/* Launch variants of the flow kernel (threads per CTA x targets per thread)
+ * for a precision; tfs_flow_set_variant picks one for the flow's precision.
+ * tfs_flow_autotune times every variant on the inputs on the device (reps
+ * evaluations each, after one warm-up) and keeps the fastest: *best gets
+ * its index and *best_ms its time per evaluation (either may be NULL). */
+int tfs_flow_num_variants(int precision);
+int tfs_flow_set_variant(tfs_flow *f, int variant);
+int tfs_flow_autotune(tfs_flow *f, double mu, int remove_net_force, int reps, int *best,
+                      double *best_ms);
 /* Device arrays x_flow[3 num_flow] and v_flow[3 num_flow] (either may be NULL). */
 int tfs_flow_device_buffers(tfs_flow *f, double **x_flow, double **v_flow);
 int tfs_flow_wait(tfs_flow *f);

@@ -147,3 +147,30 @@ def test_flow_repeatable():
     b = evaluate(d["x_flow"], d["x_segs"], d["f_segs"], d["x_blobs"], d["f_blobs"],
                  d["x_bodies"], ns, nb, True, "fp32c")
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_flow_every_variant_and_autotune(precision):
+    """Every launch variant of the flow kernel, and the autotuner's pick, on
+    the wall case with the net-force Stokeslet removed (three bodies)."""
+    from timfilsimmod_gb300.flow_field import FlowFieldEvaluator
+
+    rng = np.random.default_rng(77)
+    centres, xs, fs, _, _ = random_bodies(rng, 3, 60, 1, True)
+    xf = rng.uniform(-80.0, 80.0, size=(700, 3))
+    xf[:, 2] = np.abs(xf[:, 2]) + 0.5
+    ref = Oracle().flow_velocities(xf, xs, fs, 60, np.zeros((0, 3)), np.zeros((0, 3)), 0,
+                                   centres, 1.0 / (8.0 * np.pi), True)
+    with FlowFieldEvaluator(3, 1, 60, 0, 700, remove_net_force=True, precision=precision) as ev:
+        ev.read_positions_and_forces(xf, xs, fs, None, None, centres)
+        for var in range(ev.num_variants()):
+            ev.set_variant(var)
+            v = ev.velocities().ravel().copy()
+            if precision == "fp64":
+                assert rel_max(v, ref) < TOL64, var
+            else:
+                assert rel_l2(v, ref) < TOL32_RNF, var
+        best, ms = ev.autotune(reps=1)
+        assert 0 <= best < ev.num_variants() and ms > 0
+        v = ev.velocities().ravel().copy()
+        assert rel_max(v, ref) < (TOL64 if precision == "fp64" else 1e-4)

@@ -106,6 +106,10 @@ _SIGNATURES = {
     "tfs_flow_copy_velocities_to_host": [_H, _P],
     "tfs_flow_device_buffers": [_H, ctypes.POINTER(_P), ctypes.POINTER(_P)],
     "tfs_flow_wait": [_H],
+    "tfs_flow_num_variants": [ctypes.c_int],
+    "tfs_flow_set_variant": [_H, ctypes.c_int],
+    "tfs_flow_autotune": [_H, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                          ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
     "tfs_mss_noalloc": [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P],
     "tfs_last_error": [],
     "tfs_kernel_launch_count": [],

@@ -1,26 +1,16 @@
 // flow.cu -- the flow-field evaluator: fluid velocity at arbitrary points due
 // to the segment forces/torques and blob forces of saved swimmer states
-// (the reference's flow_velocities kernel, src/flow_field/flow_field_evaluator.cu
-// :13-228, and flow_field_evaluator::velocities :546-579).
-//
-//   u(x) = prefac [ sum_segs ( F/r + (r.F) r / r^3 + (T x r) / r^3 )
-//                 + sum_blobs ( F/r + (r.F) r / r^3 ) ],      r = x - x_j,
-// point Stokeslets and rotlets without the RPY finite-size terms. With no
-// blobs the segment Stokeslet becomes the Blakelet of a no-slip wall at z = 0
-// (image Stokeslet plus the source-doublet/stresslet correction, :83-116);
-// optionally the Stokeslet of every source force placed at its body's centre
-// is subtracted (remove_net_force, :125-143, :189-203).
-//
-// Same tile machinery as the mobility product (rpy_tile.cuh): sources packed
-// into 16-byte records and staged through shared memory, targets register
-// blocked, FP32 sums compensated per tile, deterministic source splits.
+// (the reference's flow_field_evaluator, src/flow_field/flow_field_evaluator.cu;
+// kernel flow_velocities :13-228, velocities() :546-579). The tile kernel is
+// in flow_kernels.cuh; this file holds its launcher, the body-centre points
+// of the net-force Stokeslet, the launch-variant autotuner and the C ABI.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <new>
 
 #include "../../include/tfs_gb300.h"
-#include "rpy_tile.cuh"
+#include "flow_kernels.cuh"
 #include "tfs_kernels.h"
 
 namespace tfs {
@@ -28,189 +18,84 @@ int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 int alloc_dev(void **p, size_t bytes);
 
-struct FlowArgs {
-  const double *x_flow;
-  int n_flow;
-  const void *rec_segs;   // segment records (Rec<T,6>)
-  int n_segs, segs_per_body;
-  const void *rec_blobs;  // blob records (Rec<T,3>)
-  int n_blobs, blobs_per_body;
-  const double *x_bodies;  // body centres (remove_net_force)
-  int n_bodies;
-  const double *origin;    // FP32 centring origin (z = 0 when the wall is on)
-  double prefac;
-  double *out;             // 3 * n_flow, or partials
-  int mode;                // OUT_ASSIGN or OUT_PARTIAL
-  int chunk;               // sources per split
-};
-
-// Stokeslet of force f at separation d: v += rm1 f + rm3 (d.f) d
+// One record per body b, appended after the blob records: the body centre
+// (minus the FP32 origin) carrying minus the sum of the forces of the body's
+// segments and blobs. One CTA per body; each thread sums a fixed strided
+// subset, then a fixed-shape tree: the result does not depend on timing.
 template <typename T>
-__device__ __forceinline__ void stokeslet(T *v, T dx, T dy, T dz, T rm1, const T *f, T sgn) {
-  const T rm3 = rm1 * rm1 * rm1;
-  const T w = rm3 * fma(dx, f[0], fma(dy, f[1], dz * f[2]));
-  const T a = sgn * rm1, b = sgn * w;
-  v[0] = fma(a, f[0], fma(b, dx, v[0]));
-  v[1] = fma(a, f[1], fma(b, dy, v[1]));
-  v[2] = fma(a, f[2], fma(b, dz, v[2]));
-}
-
-template <typename T>
-__device__ __forceinline__ T rsq(T r2) {
-  return rsqrt_far(r2);
-}
-
-// One segment source: Stokeslet (or Blakelet, WALL) + rotlet (+ net-force removal).
-template <typename T, bool WALL, bool RNF>
-__device__ __forceinline__ void flow_seg_pair(T *v, T xi, T yi, T zi, T sx, T sy, T sz,
-                                              const T *f, T bx, T by, T bz) {
-  const T dx = xi - sx, dy = yi - sy, dz = zi - sz;
-  const T r2 = fma(dx, dx, fma(dy, dy, dz * dz));
-  const T rm1 = rsq(r2);
-  stokeslet(v, dx, dy, dz, rm1, f, T(1));
-  if (WALL) {
-    // minus the image Stokeslet at (sx, sy, -sz), then the higher-order
-    // correction (flow_field_evaluator.cu:83-116)
-    const T Rz = zi + sz;
-    const T R2 = fma(dx, dx, fma(dy, dy, Rz * Rz));
-    const T Rm1 = rsq(R2);
-    stokeslet(v, dx, dy, Rz, Rm1, f, T(-1));
-    const T Dxx = (T(3) * dx * dx - R2) * zi;
-    const T Dxy = T(3) * dx * dy * zi;
-    const T Dxz = (R2 - T(3) * Rz * zi) * dx;
-    const T Dyy = (T(3) * dy * dy - R2) * zi;
-    const T Dyz = (R2 - T(3) * Rz * zi) * dy;
-    const T Dzx = (T(3) * Rz * zi + R2) * dx;
-    const T Dzy = (T(3) * Rz * zi + R2) * dy;
-    const T Dzz = (R2 - T(3) * Rz * Rz) * zi;
-    const T Rm2 = Rm1 * Rm1;
-    const T Dfac = T(2) * sz * Rm2 * Rm2 * Rm1;
-    v[0] += Dfac * (Dxx * f[0] + Dxy * f[1] + Dxz * f[2]);
-    v[1] += Dfac * (Dxy * f[0] + Dyy * f[1] + Dyz * f[2]);
-    v[2] += Dfac * (Dzx * f[0] + Dzy * f[1] + Dzz * f[2]);
+__global__ void __launch_bounds__(256) body_points_kernel(
+    T *__restrict__ rec, const double *__restrict__ f_segs, int segs_per_body,
+    const double *__restrict__ f_blobs, int blobs_per_body, const double *__restrict__ x_bodies,
+    const double *__restrict__ origin) {
+  constexpr int L = Rec<T, 3>::len;
+  __shared__ double red[3][256];
+  const int b = blockIdx.x;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  const double *fs = f_segs + 6 * (size_t)b * segs_per_body;
+  for (int j = threadIdx.x; j < segs_per_body; j += 256) {
+    s0 += fs[6 * (size_t)j];
+    s1 += fs[6 * (size_t)j + 1];
+    s2 += fs[6 * (size_t)j + 2];
   }
-  // rotlet (:118-123)
-  const T rm3 = rm1 * rm1 * rm1;
-  v[0] = fma(rm3, f[4] * dz - f[5] * dy, v[0]);
-  v[1] = fma(rm3, f[5] * dx - f[3] * dz, v[1]);
-  v[2] = fma(rm3, f[3] * dy - f[4] * dx, v[2]);
-  if (RNF) {
-    const T ex = xi - bx, ey = yi - by, ez = zi - bz;
-    stokeslet(v, ex, ey, ez, rsq(fma(ex, ex, fma(ey, ey, ez * ez))), f, T(-1));
+  const double *fb = f_blobs + 3 * (size_t)b * blobs_per_body;
+  for (int j = threadIdx.x; j < blobs_per_body; j += 256) {
+    s0 += fb[3 * (size_t)j];
+    s1 += fb[3 * (size_t)j + 1];
+    s2 += fb[3 * (size_t)j + 2];
   }
-}
-
-template <typename T, bool RNF>
-__device__ __forceinline__ void flow_blob_pair(T *v, T xi, T yi, T zi, T sx, T sy, T sz,
-                                               const T *f, T bx, T by, T bz) {
-  const T dx = xi - sx, dy = yi - sy, dz = zi - sz;
-  stokeslet(v, dx, dy, dz, rsq(fma(dx, dx, fma(dy, dy, dz * dz))), f, T(1));
-  if (RNF) {
-    const T ex = xi - bx, ey = yi - by, ez = zi - bz;
-    stokeslet(v, ex, ey, ez, rsq(fma(ex, ex, fma(ey, ey, ez * ez))), f, T(-1));
-  }
-}
-
-template <typename T, int FD, bool WALL, bool RNF, int BLOCK, int TPT, int TS>
-__device__ __forceinline__ void flow_range(T (&v)[TPT][3], const T (&xt)[TPT], const T (&yt)[TPT],
-                                           const T (&zt)[TPT], const T *__restrict__ rec, int lo,
-                                           int hi, int per_body, const double *x_bodies,
-                                           const double *origin, T *smem, float *hl) {
-  constexpr int L = Rec<T, FD>::len;
-  constexpr int VEC_PER_REC = L * (int)sizeof(T) / 16;
-  for (int base = lo; base < hi; base += TS) {
-    const int cnt = min(TS, hi - base);
+  red[0][threadIdx.x] = s0;
+  red[1][threadIdx.x] = s1;
+  red[2][threadIdx.x] = s2;
+  for (int h = 128; h > 0; h >>= 1) {
     __syncthreads();
-    const int4 *src = reinterpret_cast<const int4 *>(rec + (size_t)base * L);
-    int4 *dst = reinterpret_cast<int4 *>(smem);
-    for (int q = threadIdx.x; q < cnt * VEC_PER_REC; q += BLOCK) dst[q] = __ldg(src + q);
-    __syncthreads();
-    int body = -1;
-    T bx = 0, by = 0, bz = 0;
-#pragma unroll 2
-    for (int j = 0; j < cnt; ++j) {
-      T sx, sy, sz, f[FD];
-      RecLoad<T, FD>::get(smem + j * L, sx, sy, sz, f);
-      if (RNF) {
-        const int b = (base + j) / per_body;  // warp-uniform
-        if (b != body) {
-          body = b;
-          const double *xb = x_bodies + 3 * (size_t)b;
-          bx = T(xb[0] - (origin ? origin[0] : 0.0));
-          by = T(xb[1] - (origin ? origin[1] : 0.0));
-          bz = T(xb[2] - (origin ? origin[2] : 0.0));
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < TPT; ++t) {
-        if (FD == 6)
-          flow_seg_pair<T, WALL, RNF>(v[t], xt[t], yt[t], zt[t], sx, sy, sz, f, bx, by, bz);
-        else
-          flow_blob_pair<T, RNF>(v[t], xt[t], yt[t], zt[t], sx, sy, sz, f, bx, by, bz);
-      }
+    if (threadIdx.x < h)
+      for (int k = 0; k < 3; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+  }
+  if (threadIdx.x == 0) {
+    T *r = rec + (size_t)b * L;
+    for (int k = 0; k < 3; ++k) {
+      r[k] = T(x_bodies[3 * (size_t)b + k] - (origin ? origin[k] : 0.0));
+      r[3 + k] = T(-red[k][0]);
     }
-    Comp<T, 3, BLOCK, TPT>::fold(v, hl);
+    for (int k = 6; k < L; ++k) r[k] = T(0);
   }
 }
 
-template <typename T, bool WALL, bool RNF, int BLOCK, int TPT, int TS>
-__global__ void __launch_bounds__(BLOCK) flow_kernel(const FlowArgs a) {
-  constexpr int LMAX = Rec<T, 6>::len;
-  constexpr bool kComp = sizeof(T) == 4;
-  __shared__ __align__(16) T smem[TS * LMAX];
-  __shared__ float hl[kComp ? 2 * TPT * 3 * BLOCK : 1];
-  const double *origin = kComp ? a.origin : nullptr;
-  const int tile0 = blockIdx.x * BLOCK * TPT;
-  T xt[TPT], yt[TPT], zt[TPT], v[TPT][3];
-#pragma unroll
-  for (int t = 0; t < TPT; ++t) {
-    int i = tile0 + t * BLOCK + threadIdx.x;
-    i = i < a.n_flow ? i : a.n_flow - 1;
-    xt[t] = load_target<T>(a.x_flow, i, 0, origin);
-    yt[t] = load_target<T>(a.x_flow, i, 1, origin);
-    zt[t] = load_target<T>(a.x_flow, i, 2, origin);
-    v[t][0] = v[t][1] = v[t][2] = T(0);
-  }
-  if (kComp)
-    for (int q = threadIdx.x; q < 2 * TPT * 3 * BLOCK; q += BLOCK) hl[q] = 0.f;
-  const int n_src = a.n_segs + a.n_blobs;
-  const int s0 = blockIdx.y * a.chunk, s1 = min(s0 + a.chunk, n_src);
-  {
-    const int lo = min(s0, a.n_segs), hi = min(s1, a.n_segs);
-    if (lo < hi)
-      flow_range<T, 6, WALL, RNF, BLOCK, TPT, TS>(v, xt, yt, zt,
-                                                  reinterpret_cast<const T *>(a.rec_segs), lo,
-                                                  hi, a.segs_per_body, a.x_bodies, origin, smem,
-                                                  hl);
-  }
-  {
-    const int lo = max(s0 - a.n_segs, 0), hi = max(s1 - a.n_segs, 0);
-    if (lo < hi)
-      flow_range<T, 3, false, RNF, BLOCK, TPT, TS>(v, xt, yt, zt,
-                                                   reinterpret_cast<const T *>(a.rec_blobs), lo,
-                                                   hi, a.blobs_per_body, a.x_bodies, origin,
-                                                   smem, hl);
-  }
-#pragma unroll
-  for (int t = 0; t < TPT; ++t) {
-    const int i = tile0 + t * BLOCK + threadIdx.x;
-    if (i >= a.n_flow) continue;
-    double *o = a.mode == OUT_PARTIAL ? a.out + ((size_t)blockIdx.y * a.n_flow + i) * 3
-                                      : a.out + (size_t)i * 3;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) o[k] = a.prefac * Comp<T, 3, BLOCK, TPT>::get(v, hl, t, k);
-  }
+static cudaError_t launch_body_points(int fp32, void *rec, const double *f_segs,
+                                      int segs_per_body, const double *f_blobs,
+                                      int blobs_per_body, const double *x_bodies, int nbod,
+                                      const double *origin, cudaStream_t st) {
+  if (fp32)
+    body_points_kernel<float><<<nbod, 256, 0, st>>>(static_cast<float *>(rec), f_segs,
+                                                    segs_per_body, f_blobs, blobs_per_body,
+                                                    x_bodies, origin);
+  else
+    body_points_kernel<double><<<nbod, 256, 0, st>>>(static_cast<double *>(rec), f_segs,
+                                                     segs_per_body, f_blobs, blobs_per_body,
+                                                     x_bodies, origin);
+  count_launch();
+  return cudaGetLastError();
 }
 
-template <typename T, bool WALL, bool RNF>
-static cudaError_t flow_launch_t(FlowArgs a, double *scratch, size_t scratch_elems,
-                                 cudaStream_t st) {
-  constexpr int BLOCK = 128, TPT = sizeof(T) == 4 ? 2 : 1, TS = sizeof(T) == 4 ? 256 : 128;
-  const int per_cta = BLOCK * TPT;
+// Source splits: while the point set fills less than one wave of resident
+// CTAs, split the sources so that the grid does (partials summed in split
+// order by launch_reduce_partials); sources per split a multiple of 64.
+static cudaError_t launch_flow(FlowArgs a, int fp32, int wall, int variant, double *scratch,
+                               size_t scratch_elems, cudaStream_t st) {
+  if (a.n_flow <= 0) return cudaSuccess;
+  const int nvar = fp32 ? kFlowVariantsF32 : kFlowVariantsF64;
+  if (variant < 0 || variant >= nvar) variant = 0;
+  const FlowVariant var = fp32 ? g_flow_variants_f32[variant] : g_flow_variants_f64[variant];
+  const FlowFn fn = fp32 ? g_flow_f32[variant][wall ? 1 : 0] : g_flow_f64[variant][wall ? 1 : 0];
+  const int per_cta = var.block * var.tpt;
   const int ctas = (a.n_flow + per_cta - 1) / per_cta;
-  const int n_src = a.n_segs + a.n_blobs;
-  int splits = std::max(1, (8 * num_sms() + ctas - 1) / ctas);
-  splits = std::min({splits, kMaxSplits, std::max(1, n_src / 128)});
+  const int n_src = a.n_segs + a.n_points;
+  int resident = 1;
+  cudaError_t e = fn(a, dim3(0), st, &resident);
+  if (e != cudaSuccess) return e;
+  const long slots = (long)resident * num_sms();
+  int splits = (int)std::max(1L, slots / std::max(1, ctas));
+  splits = std::min({splits, kMaxSplits, std::max(1, n_src / 64)});
   if ((size_t)splits * 3 * a.n_flow > scratch_elems) splits = 1;
   int chunk = (n_src + splits - 1) / splits;
   chunk = std::max(64, ((chunk + 63) / 64) * 64);
@@ -223,25 +108,11 @@ static cudaError_t flow_launch_t(FlowArgs a, double *scratch, size_t scratch_ele
   } else {
     a.mode = OUT_ASSIGN;
   }
-  flow_kernel<T, WALL, RNF, BLOCK, TPT, TS><<<dim3(ctas, splits), BLOCK, 0, st>>>(a);
+  e = fn(a, dim3(ctas, splits), st, nullptr);
   count_launch();
+  if (e != cudaSuccess) return e;
   if (splits > 1) return launch_reduce_partials(final_out, scratch, 3 * a.n_flow, splits, 0, st);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_flow(const FlowArgs &a, int fp32, int wall, int rnf, double *scratch,
-                        size_t scratch_elems, cudaStream_t st) {
-  if (a.n_flow <= 0) return cudaSuccess;
-  if (fp32) {
-    if (wall) return rnf ? flow_launch_t<float, true, true>(a, scratch, scratch_elems, st)
-                         : flow_launch_t<float, true, false>(a, scratch, scratch_elems, st);
-    return rnf ? flow_launch_t<float, false, true>(a, scratch, scratch_elems, st)
-               : flow_launch_t<float, false, false>(a, scratch, scratch_elems, st);
-  }
-  if (wall) return rnf ? flow_launch_t<double, true, true>(a, scratch, scratch_elems, st)
-                       : flow_launch_t<double, true, false>(a, scratch, scratch_elems, st);
-  return rnf ? flow_launch_t<double, false, true>(a, scratch, scratch_elems, st)
-             : flow_launch_t<double, false, false>(a, scratch, scratch_elems, st);
+  return cudaSuccess;
 }
 
 }  // namespace tfs
@@ -261,6 +132,7 @@ struct tfs_flow {
   double *scratch = nullptr;
   size_t scratch_elems = 0;
   double origin_host[4] = {0, 0, 0, 0};
+  int variant[2] = {0, 0};  // launch variant per precision (TFS_FP64, TFS_FP32C)
 };
 
 static void flow_free(tfs_flow *f) {
@@ -321,7 +193,7 @@ int tfs_flow_create(int num_flow, int num_bodies, int segs_per_body, int blobs_p
       (rc = alloc_dev((void **)&f->x_bodies, 24 * (size_t)num_bodies)) ||
       (rc = alloc_dev((void **)&f->origin, 32)) ||
       (rc = alloc_dev(&f->rec_segs, record_bytes(0, 6) * (size_t)ns)) ||
-      (rc = alloc_dev(&f->rec_blobs, record_bytes(0, 3) * (size_t)nb)) ||
+      (rc = alloc_dev(&f->rec_blobs, record_bytes(0, 3) * ((size_t)nb + num_bodies))) ||
       (rc = alloc_dev((void **)&f->scratch, 8 * f->scratch_elems))) {
     flow_free(f);
     delete f;
@@ -389,31 +261,90 @@ int tfs_flow_velocities(tfs_flow *f, double mu, int remove_net_force) {
   if (f == nullptr) return fail(TFS_EINVAL, "null flow handle");
   if (!(mu > 0.0)) return fail(TFS_EINVAL, "mu must be positive");
   const int fp32 = f->precision == TFS_FP32C;
-  cudaError_t e;
   const double *origin = fp32 ? f->origin : nullptr;  // FP64 records stay absolute
+  cudaError_t e;
   if (f->ns > 0 && (e = launch_pack(fp32, 6, f->rec_segs, f->x_segs, f->f_segs, f->ns, origin,
                                     f->stream)) != cudaSuccess)
     return cuda_fail(e, "pack kernel");
   if (f->nb > 0 && (e = launch_pack(fp32, 3, f->rec_blobs, f->x_blobs, f->f_blobs, f->nb, origin,
                                     f->stream)) != cudaSuccess)
     return cuda_fail(e, "pack kernel");
+  int n_points = f->nb;
+  if (remove_net_force) {
+    char *body_rec = static_cast<char *>(f->rec_blobs) + record_bytes(fp32, 3) * (size_t)f->nb;
+    e = launch_body_points(fp32, body_rec, f->f_segs, f->segs_per_body, f->f_blobs,
+                           f->blobs_per_body, f->x_bodies, f->nbod, origin, f->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "body-point kernel");
+    n_points += f->nbod;
+  }
   FlowArgs a{};
   a.x_flow = f->x_flow;
   a.n_flow = f->nflow;
   a.rec_segs = f->rec_segs;
   a.n_segs = f->ns;
-  a.segs_per_body = std::max(1, f->segs_per_body);
-  a.rec_blobs = f->rec_blobs;
-  a.n_blobs = f->nb;
-  a.blobs_per_body = std::max(1, f->blobs_per_body);
-  a.x_bodies = f->x_bodies;
-  a.n_bodies = f->nbod;
+  a.rec_points = f->rec_blobs;
+  a.n_points = n_points;
   a.origin = f->origin;
   a.prefac = 1.0 / (8.0 * 3.14159265358979323846264338327950288 * mu);
   a.out = f->v_flow;
-  e = launch_flow(a, fp32, f->blobs_per_body == 0, remove_net_force != 0, f->scratch,
+  e = launch_flow(a, fp32, f->blobs_per_body == 0, f->variant[fp32], f->scratch,
                   f->scratch_elems, f->stream);
   if (e != cudaSuccess) return cuda_fail(e, "flow kernel");
+  return TFS_OK;
+}
+
+int tfs_flow_num_variants(int precision) {
+  return precision == TFS_FP32C ? kFlowVariantsF32 : kFlowVariantsF64;
+}
+
+int tfs_flow_set_variant(tfs_flow *f, int variant) {
+  if (f == nullptr) return fail(TFS_EINVAL, "null flow handle");
+  if (variant < 0 || variant >= tfs_flow_num_variants(f->precision))
+    return fail(TFS_EINVAL, "variant %d out of range", variant);
+  f->variant[f->precision == TFS_FP32C] = variant;
+  return TFS_OK;
+}
+
+int tfs_flow_autotune(tfs_flow *f, double mu, int remove_net_force, int reps, int *best,
+                      double *best_ms) {
+  if (f == nullptr) return fail(TFS_EINVAL, "null flow handle");
+  if (reps < 1) reps = 1;
+  const int fp32 = f->precision == TFS_FP32C;
+  const int nvar = tfs_flow_num_variants(f->precision);
+  cudaEvent_t ev[2];
+  cudaError_t e = cudaEventCreate(&ev[0]);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+  e = cudaEventCreate(&ev[1]);
+  if (e != cudaSuccess) {
+    cudaEventDestroy(ev[0]);
+    return cuda_fail(e, "cudaEventCreate");
+  }
+  int chosen = 0, rc = TFS_OK;
+  float chosen_ms = 0.f;
+  for (int v = 0; v < nvar && rc == TFS_OK; ++v) {
+    f->variant[fp32] = v;
+    if ((rc = tfs_flow_velocities(f, mu, remove_net_force)) != TFS_OK) break;  // warm-up
+    cudaEventRecord(ev[0], f->stream);
+    for (int r = 0; r < reps && rc == TFS_OK; ++r) rc = tfs_flow_velocities(f, mu, remove_net_force);
+    cudaEventRecord(ev[1], f->stream);
+    if ((e = cudaEventSynchronize(ev[1])) != cudaSuccess) {
+      rc = cuda_fail(e, "flow autotune");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    ms /= reps;
+    if (v == 0 || ms < chosen_ms) {
+      chosen = v;
+      chosen_ms = ms;
+    }
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  f->variant[fp32] = chosen;
+  if (rc != TFS_OK) return rc;
+  if (best) *best = chosen;
+  if (best_ms) *best_ms = chosen_ms;
   return TFS_OK;
 }
 

@@ -98,6 +98,20 @@ class FlowFieldEvaluator:
         self._call("tfs_flow_copy_velocities_to_host", _ptr(self.v_flow_host))
         return self.v_flow_host.reshape(self.NFLOW, 3)
 
+    def autotune(self, reps: int = 1) -> tuple[int, float]:
+        """Time every launch variant on the current device inputs and keep the
+        fastest; returns (variant, ms per evaluation)."""
+        best, ms = ctypes.c_int(), ctypes.c_double()
+        self._call("tfs_flow_autotune", float(self.MU), int(self.REMOVE_NET_FORCE_STOKESLET),
+                   int(reps), ctypes.byref(best), ctypes.byref(ms))
+        return best.value, ms.value
+
+    def set_variant(self, variant: int) -> None:
+        self._call("tfs_flow_set_variant", int(variant))
+
+    def num_variants(self) -> int:
+        return int(self.lib.tfs_flow_num_variants(PRECISIONS[self.precision]))
+
     def wait(self) -> None:
         self._call("tfs_flow_wait")
 

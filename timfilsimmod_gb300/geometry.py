@@ -146,3 +146,12 @@ def make_config(name: str, seed: int = 0, **overrides) -> Swimmer:
     kw = dict(CONFIGS[name])
     kw.update(overrides)
     return make_swimmer(seed=seed, **kw)
+
+
+def flow_grid(n: int, half_width: float, centre=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """n^3 evaluation points at the cell centres of a uniform grid over the
+    cube centre +- half_width, x fastest, as an (n^3, 3) float64 array."""
+    c = (np.arange(n, dtype=np.float64) + 0.5) / n * (2.0 * half_width) - half_width
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    return np.ascontiguousarray(pts + np.asarray(centre, dtype=np.float64))

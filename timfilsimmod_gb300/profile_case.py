@@ -14,18 +14,44 @@ from .geometry import make_config
 from .mobility import RpyMobilitySolver
 
 
+def run_flow(sw, args):
+    import numpy as np
+
+    from .flow_field import FlowFieldEvaluator
+    from .geometry import flow_grid
+
+    reach = float(np.max(np.linalg.norm(sw.x_segs, axis=1)))
+    xf = flow_grid(args.flow_grid, 1.25 * reach)
+    ev = FlowFieldEvaluator(1, sw.nfil, sw.nseg, sw.num_blobs, xf.shape[0],
+                            precision=args.precision)
+    ev.read_positions_and_forces(xf, sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs, sw.body_x)
+    if args.variant is not None:
+        ev.set_variant(args.variant)
+    t0 = time.perf_counter()
+    for _ in range(args.reps):
+        ev.velocities(copy_to_host=False)
+    ev.wait()
+    dt = time.perf_counter() - t0
+    print(f"flow {args.precision} {xf.shape[0]} points x {sw.num_segs + sw.num_blobs} sources: "
+          f"{dt / args.reps * 1e3:.3f} ms per evaluation")
+    ev.close()
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--config", default="medium")
     p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     p.add_argument("--reps", type=int, default=2)
-    p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier", "solve"])
+    p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier", "solve", "flow"])
+    p.add_argument("--flow-grid", type=int, default=64, help="flow points per axis (op flow)")
     p.add_argument("--variant", type=int, default=None,
                    help="pin every combination to this tile-kernel variant")
     p.add_argument("--waves", type=int, default=1)
     p.add_argument("--autotune", action="store_true", help="print the autotuner's table")
     args = p.parse_args()
     sw = make_config(args.config, seed=1)
+    if args.op == "flow":
+        return run_flow(sw, args)
     s = RpyMobilitySolver(1, sw.nfil, sw.nseg, sw.num_blobs, precision=args.precision)
     s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
     if args.autotune:
