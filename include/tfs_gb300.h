@@ -142,6 +142,13 @@ int tfs_set_refinement(tfs_solver *s, double inner_tol, int max_cycles);
  * from the blob references and the 6x6 body mobility from six solves with
  * rhs = -e_{n-1-j}, at the current pose. Leaves the last solution as the next
  * warm start, as the reference does. */
+/* FP32C only: run each inner GMRES solve of the refinement as one
+ * cooperative kernel (enable = 1, the default where the device supports
+ * cooperative launch and the system has at most 64 blobs per SM pair of
+ * CTAs) or as a sequence of kernels per Arnoldi step (enable = 0). Both
+ * compute the same iteration; the cooperative kernel removes the launch
+ * gaps between its phases. TFS_ESTATE if enable = 1 cannot be honoured. */
+int tfs_set_persistent_gmres(tfs_solver *s, int enable);
 int tfs_make_body_reference_matrices(tfs_solver *s);
 /* The two 6x6 matrices (column-major, body frame); either pointer may be NULL. */
 int tfs_get_body_reference_matrices(tfs_solver *s, double *body_mobility, double *ktkinv);

@@ -10,7 +10,9 @@ implementations agree to about that level, not to rounding):
   FP32C: the pairwise sums (Mss, Mbs, Msb and the blob-blob products inside
          GMRES) run in FP32 with compensated accumulation, so results carry
          their ~1e-6 relative error: <= 2e-5; the linear system itself is
-         refined to the FP64 residual tolerance (checked)
+         refined to the FP64 residual tolerance (checked). "fp32c" runs each
+         inner GMRES as one cooperative kernel (the default), "fp32c_kernels"
+         as a sequence of kernels per Arnoldi step; both meet the same bars.
 """
 import os
 
@@ -19,7 +21,8 @@ import pytest
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 TOL = 1e-8
-TOLS = {"fp64": 1e-8, "fp32c": 2e-5}
+TOLS = {"fp64": 1e-8, "fp32c": 2e-5, "fp32c_kernels": 2e-5}
+FORMS = ["fp64", "fp32c", "fp32c_kernels"]
 
 pytestmark = pytest.mark.gpu
 
@@ -33,11 +36,21 @@ def load(name):
     return np.load(os.path.join(GOLD, f"{name}.npz"))
 
 
-def make_solver(d, precision):
+def new_solver(nfil, nseg, nblob, form, **kw):
+    """A solver in one of FORMS."""
     from timfilsimmod_gb300.mobility import RpyMobilitySolver
 
-    s = RpyMobilitySolver(1, int(d["nfil"]), int(d["nseg"]), d["blob_refs"].shape[0],
-                          precision=precision, end_force_magnitude=int(d["end_force_magnitude"]))
+    s = RpyMobilitySolver(1, nfil, nseg, nblob, precision=form.split("_")[0], **kw)
+    if form == "fp32c":
+        s.set_persistent_gmres(True)  # raises if the cooperative kernel cannot run
+    elif form == "fp32c_kernels":
+        s.set_persistent_gmres(False)
+    return s
+
+
+def make_solver(d, precision):
+    s = new_solver(int(d["nfil"]), int(d["nseg"]), d["blob_refs"].shape[0], precision,
+                   end_force_magnitude=int(d["end_force_magnitude"]))
     s.set_blob_references(d["blob_refs"])
     s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
     s.set_linear_solver(float(d["tol"]))
@@ -51,7 +64,7 @@ def set_segments(s, xs, fs):
     s.copy_segment_forces_to_device()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("precision", FORMS)
 def test_solve_sequence_matches_reference(precision):
     d = load("solve_small")
     s = make_solver(d, precision)
@@ -104,7 +117,7 @@ def test_zero_rhs_and_warm_start_exit():
     s.finalise()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("precision", FORMS)
 def test_medium_swimmer_solve_vs_oracle(precision):
     """compute_velocities of the medium swimmer (12 800 segments, 2562 blobs)
     against the oracle's restatement, at LINEAR_SYSTEM_TOL = 1e-10, after
@@ -113,15 +126,13 @@ def test_medium_swimmer_solve_vs_oracle(precision):
     from oracle import OracleSolver
 
     from timfilsimmod_gb300.geometry import make_config
-    from timfilsimmod_gb300.mobility import RpyMobilitySolver
 
     sw = make_config("medium", seed=3)
     efm = int(220.0 * 1800.0 / (2.6 * 2.6 * sw.nseg ** 2))
     F = sw.f_segs[:, :3].sum(0)
     T = (np.cross(sw.x_segs, sw.f_segs[:, :3]) + sw.f_segs[:, 3:]).sum(0)
     sf = np.concatenate([F, T])
-    s = RpyMobilitySolver(1, sw.nfil, sw.nseg, sw.num_blobs, precision=precision,
-                          end_force_magnitude=efm)
+    s = new_solver(sw.nfil, sw.nseg, sw.num_blobs, precision, end_force_magnitude=efm)
     s.set_blob_references(sw.blob_references)
     s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
     s.set_linear_solver(1e-10)
@@ -147,10 +158,41 @@ def test_medium_swimmer_solve_vs_oracle(precision):
     # two correct GMRES runs that stop at a relative residual of 1e-10 one
     # iteration apart differ by that residual times the conditioning of the
     # saddle-point system (~1e4 here): bound at 1e-6 for FP64
-    tol = {"fp64": 1e-6, "fp32c": 2e-5}[precision]
+    tol = {"fp64": 1e-6, "fp32c": 2e-5, "fp32c_kernels": 2e-5}[precision]
     for k, v in (("v_segs", vs), ("f_blobs", fb), ("v_bodies", vb)):
         e = rel_max(v, r[k])
         print(precision, k, e)
         assert e < tol, (k, e)
     if precision == "fp64":
         assert abs(it - r["iters"]) <= 1
+
+
+def test_persistent_and_kernel_sequence_agree():
+    """The cooperative-kernel inner GMRES and the kernel-sequence one solve
+    the same refinement: same results to the FP32 product error, iteration
+    totals within a few (their FP32 sums round differently)."""
+    from timfilsimmod_gb300.geometry import make_config
+
+    sw = make_config("medium", seed=11)
+    F = sw.f_segs[:, :3].sum(0)
+    T = (np.cross(sw.x_segs, sw.f_segs[:, :3]) + sw.f_segs[:, 3:]).sum(0)
+    out = {}
+    for form in ("fp32c", "fp32c_kernels"):
+        s = new_solver(sw.nfil, sw.nseg, sw.num_blobs, form)
+        s.set_blob_references(sw.blob_references)
+        s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+        s.set_linear_solver(1e-8)
+        set_segments(s, sw.x_segs, sw.f_segs)
+        bm, _ = s.make_body_reference_matrices()
+        it, _ = s.compute_velocities(np.concatenate([F, T]))
+        s.copy_segment_velocities_to_host()
+        s.wait_for_device()
+        out[form] = (it, s.v_segs_host.copy(), s.blob_forces(), s.body_velocities(), bm,
+                     s.solve_info())
+        s.finalise()
+    a, b = out["fp32c"], out["fp32c_kernels"]
+    print("iters", a[0], b[0], a[5], b[5])
+    assert a[5]["rel_residual"] <= 1e-8 and b[5]["rel_residual"] <= 1e-8
+    assert abs(a[0] - b[0]) <= max(3, b[0] // 10)
+    for x, y in zip(a[1:5], b[1:5]):
+        assert rel_max(x, y) < 2e-5

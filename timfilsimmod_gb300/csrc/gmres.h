@@ -49,6 +49,45 @@ struct GmresArgs {
   double *h1, *h2;          // max_iter + 1 each: the two Gram-Schmidt passes
 };
 
+// Persistent (cooperative) inner GMRES with an FP32 M_bb product
+// (gmres_persistent.cu): launch shape and arguments.
+constexpr int kMaxPgBlobsPerCta = 64;                  // rows per CTA <= 192
+constexpr int kMaxPgCtas = 256;                        // one CTA per SM
+constexpr unsigned long long kPgTimeoutNs = 2000000000ull;  // one barrier wait
+struct PgShape {
+  int P;                  // CTAs (all resident: cooperative launch)
+  int G, blobs_per_cta;   // CTAs owning blob slices, blobs per slice
+  int TB, tbs;            // M_bb target blocks and their size
+  int S, chunk;           // M_bb source splits and their size
+  int Kr;                 // Krylov columns resident in shared memory
+  size_t dyn_smem;        // dynamic shared memory per CTA (bytes)
+};
+struct PgArgs {
+  GmresArgs g;            // vectors, body data, tolerance; g.G / g.blobs_per_cta = slices
+  float *x32;             // 3 nb: blob positions minus the origin, FP32
+  float *rec;             // 8 nb: FP32 blob records of the current z
+  float2 *mpart;          // S * 3 nb: split partial products of M_bb, (hi, lo)
+  double *p6, *ps;        // per-CTA partial 6-vectors and sums of squares
+  double *pd1, *pd2;      // per-CTA Gram-Schmidt partial dots ((max_iter + 2) * G each)
+  double *aux;            // control words (3) + 3 x 352: h1, h2, y published by CTAs
+  unsigned *bar;          // 4: barrier count, generation, abort
+  int P, TB, tbs, S, chunk, Kr;
+  size_t dyn_smem;
+  float a;                // blob radius
+  float pc_asum2, pc_s, pc_s3;  // FP32 pair constants: (2a)^2, 2a^2/3, -2a^2
+  double scale;           // 1 / (8 pi mu)
+  double minv;            // 6 pi mu a (the preconditioner's blob block)
+};
+// Launch shape for nb blobs on `sms` SMs; 0 when the kernel cannot be used
+// (no occupancy, or more than kMaxPgBlobsPerCta blobs per CTA).
+int pg_grid(int nb, int sms, int max_iter, PgShape *shape);
+// Buffer sizes (elements) of one shape.
+inline size_t pg_p6_elems(const PgShape &s) { return 6 * 6 * (size_t)s.G; }
+inline size_t pg_ps_elems(const PgShape &s) { return 3 * (size_t)s.G; }
+inline size_t pg_pd_elems(const PgShape &s) { return 352 * (size_t)s.G; }
+constexpr size_t kPgAuxElems = 3 + 3 * 352;
+cudaError_t launch_gmres_persistent(const PgArgs &p, cudaStream_t st);
+
 // CTAs and blobs per CTA of the GMRES kernels for nb blobs on `sms` SMs.
 int gmres_grid(int nb, int sms, int *blobs_per_cta);
 cudaError_t launch_gmres_finish(const GmresArgs &a, cudaStream_t st);

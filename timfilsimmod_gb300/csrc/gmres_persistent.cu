@@ -1,0 +1,887 @@
+// gmres_persistent.cu -- the inner GMRES of the FP32C iterative refinement
+// as one cooperative (persistent) kernel.
+//
+// Same system, preconditioner, Givens convention, warm-start tests and
+// stopping rule as the multi-kernel GMRES of gmres.cu (the reference's
+// solve_linear_system, mobility_solver.cpp:2092-2570, free-body branches),
+// with the blob-blob product M_bb in FP32 (compensated per tile). At the
+// medium swimmer (2 562 blobs) an Arnoldi step is ~10 us of arithmetic;
+// issued as seven kernels per step it took ~150-190 us of launch gaps and
+// serialised reductions. Here one launch runs the whole solve:
+//
+//   start | M_bb | residual | scale + preconditioner | { M_bb | w, CGS pass 1 |
+//   CGS pass 2 | norm | Givens + scale + preconditioner } x k | Q y | update
+//
+// with a grid barrier between phases (seven per Arnoldi step), one CTA per
+// SM. Every CTA owns a contiguous slice of blobs (its rows of every vector).
+// Reductions are deterministic (per-CTA partials added in CTA order):
+// the 6-vectors and squared norms, which every CTA needs at once, are summed
+// by every CTA itself (identical bits everywhere); the k Gram-Schmidt
+// coefficients of each pass are summed one per warp across the grid and
+// read back after a barrier, because GB300's FP64 rate (2 FMA/clk/SM) makes
+// k x G redundant additions per CTA the dominant cost. Givens rotations,
+// the convergence test and the final triangular solve run in CTA 0, which
+// publishes its decision for the others to read after the next barrier.
+// The M_bb product is cut into (target block x source split) units spread
+// over all CTAs; partial sums go to global memory and each row's owner adds
+// the splits in order.
+//
+// Grid barrier: a counter and a generation word in global memory. Every
+// wait is bounded (2 s of globaltimer, plus an iteration cap); a CTA that
+// gives up raises an abort word that ends every other wait at once, and the
+// solve reports TFS_ETIMEOUT. The launch is cooperative, so all CTAs are
+// resident together (or the launch fails and the multi-kernel path runs).
+// Data other CTAs wrote is read with ld.global.cg (L2), never through L1.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "gmres.h"
+#include "rpy_tile.cuh"
+#include "tfs_kernels.h"
+
+namespace tfs {
+
+namespace {
+
+constexpr int kPB = 512;       // threads per CTA (one CTA per SM)
+constexpr int kPW = kPB / 32;  // warps per CTA
+constexpr int kPTS = 128;      // sources per shared-memory tile of M_bb
+constexpr int kPK = 352;       // Krylov columns + 1 (max_iter <= 350)
+constexpr int kMaxRows = 3 * kMaxPgBlobsPerCta;
+constexpr int kHB = 4096;      // doubles of the staging buffer (H columns, M_bb partials)
+
+constexpr int kPgDynFixed = kHB + 8 * kMaxPgCtas + 6 * kPK;  // doubles before qres
+
+// control words CTA 0 publishes each Arnoldi step
+enum { C_FINISH = 0, C_REL, C_STATUS, kCtl };
+
+// p6 slots: per-CTA partial 6-vectors sum_m (l_m ; d_m x l_m)
+enum { K_SOLN = 0, K_R0, K_RHS, K_Z, K_W, K_T, kP6Slots };
+// ps slots: per-CTA partial sums of squares
+enum { S_RHS = 0, S_R0, S_NORM, kPsSlots };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
+
+// Bounded grid barrier; false in every thread of the CTA if it was abandoned.
+__device__ bool pg_barrier(const PgArgs &p) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *vb = p.bar;
+    int good = 1;
+    const unsigned gen = vb[1];
+    __threadfence();
+    const unsigned arrived = atomicAdd(p.bar, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(p.bar, 0u);  // no CTA arrives again before the generation moves
+      __threadfence();
+      atomicAdd(p.bar + 1, 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      unsigned spins = 0;
+      while (vb[1] == gen) {
+        if (vb[2] != 0u) {  // another CTA gave up
+          good = 0;
+          break;
+        }
+        ++spins;
+        if (spins > (1u << 25) || ((spins & 63u) == 0 && global_ns() - t0 > kPgTimeoutNs)) {
+          atomicExch(p.bar + 2, 1u);
+          good = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (!good) {
+      atomicExch(&p.g.st->status, 2);
+      atomicExch(&p.g.st->done, 1);
+    }
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+struct PSlice {
+  int m0, m1;       // blobs [m0, m1)
+  int rows;         // 3 (m1 - m0)
+  bool owner;       // this CTA owns a slice (blockIdx.x < G)
+  bool body;        // this CTA writes the six body rows of global vectors
+  const double *d;  // the slice's d_m = R ref_m, d[3 (m - m0) + j] (shared memory)
+};
+
+__device__ __forceinline__ PSlice pg_slice(const PgArgs &p, const double *dsl) {
+  PSlice s;
+  s.d = dsl;
+  const int c = blockIdx.x;
+  s.owner = c < p.g.G;
+  s.m0 = s.owner ? min(p.g.nb, c * p.g.blobs_per_cta) : p.g.nb;
+  s.m1 = s.owner ? min(p.g.nb, s.m0 + p.g.blobs_per_cta) : p.g.nb;
+  s.rows = 3 * (s.m1 - s.m0);
+  s.body = c == p.g.G - 1;
+  return s;
+}
+
+// Warp sum with a fixed shuffle pattern (the same bits in every lane).
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Stage elems doubles of buf (global) into dst (shared); no barrier.
+__device__ __forceinline__ void stage(const double *buf, int elems, double *dst) {
+  for (int q = threadIdx.x; q < elems; q += kPB) dst[q] = ldcg(buf + q);
+}
+
+// out[j] = sum over c < G of cst[j * G + c], j < count <= kPW: warp j adds
+// lane-strided subsets then a fixed shuffle tree. No barrier.
+__device__ __forceinline__ void sum_staged(const double *cst, int G, int count, double *out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (wid < count) {
+    double s = 0.0;
+    for (int c = lane; c < G; c += 32) s += cst[wid * G + c];
+    s = warp_sum(s);
+    if (lane == 0) out[wid] = s;
+  }
+}
+
+// Stage and sum count vectors of per-CTA partials (buf[j * G + c]) into
+// out[0..count); ends with a barrier.
+__device__ void cta_sums(const double *buf, int G, int count, double *out, double *cst) {
+  stage(buf, count * G, cst);
+  __syncthreads();
+  sum_staged(cst, G, count, out);
+  __syncthreads();
+}
+
+// Warp 0: this CTA's partials of the slice rows ls: sum_m (l_m ; d_m x l_m)
+// into p6 slot kt_slot and, with sq_slot >= 0, the sum of squares into ps
+// slot sq_slot. No barrier; ls must be complete.
+__device__ void slice_partials(const PgArgs &p, const PSlice &sl, const double *ls, int kt_slot,
+                               int sq_slot) {
+  if (threadIdx.x >= 32 || !sl.owner) return;
+  const int lane = threadIdx.x;
+  double s[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int m = sl.m0 + lane; m < sl.m1; m += 32) {
+    const double *d = sl.d + 3 * (m - sl.m0);
+    const double *v = ls + 3 * (m - sl.m0);
+    s[0] += v[0];
+    s[1] += v[1];
+    s[2] += v[2];
+    s[3] += d[1] * v[2] - d[2] * v[1];
+    s[4] += d[2] * v[0] - d[0] * v[2];
+    s[5] += d[0] * v[1] - d[1] * v[0];
+  }
+  if (sq_slot >= 0)
+    for (int r = lane; r < sl.rows; r += 32) s[6] += ls[r] * ls[r];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) s[j] = warp_sum(s[j]);
+  if (sq_slot >= 0) s[6] = warp_sum(s[6]);
+  if (lane == 0) {
+    const int G = p.g.G, c = blockIdx.x;
+    for (int j = 0; j < 6; ++j) p.p6[(size_t)(kt_slot * 6 + j) * G + c] = s[j];
+    if (sq_slot >= 0) p.ps[(size_t)sq_slot * G + c] = s[6];
+  }
+}
+
+// z = P^-1 (q rows of the slice in shared memory, q_vel), given
+// bsum = sum_m (q_m ; d_m x q_m) / bscale: b = -bsum * bscale, the body part
+// (U', Omega') = KTKinv b - N q_vel (mobility_solver.cpp:1437-1509), then
+// z_m = 6 pi mu a (q_m + U' + Omega' x d_m). Writes zv (6, shared) and the
+// slice's z rows into zs (shared); ends with a barrier.
+__device__ void precond(const PgArgs &p, const PSlice &sl, const double *qs, const double *qvel,
+                        const double *bsum, double bscale, double *zs, double *zv,
+                        const double *mats) {
+  if (threadIdx.x < 6) {
+    const int i = threadIdx.x;
+    const double *N = mats, *Kinv = mats + 36;
+    double t1 = 0.0, t2 = 0.0;
+    for (int k = 0; k < 6; ++k) t1 += Kinv[i + 6 * k] * (-bsum[k] * bscale);
+    for (int k = 0; k < 6; ++k) t2 += N[i + 6 * k] * qvel[k];
+    zv[i] = t1 - t2;
+  }
+  __syncthreads();
+  const double u0 = zv[0], u1 = zv[1], u2 = zv[2], w0 = zv[3], w1 = zv[4], w2 = zv[5];
+  for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += kPB) {
+    const double minv = p.minv;
+    const double *d = sl.d + 3 * (m - sl.m0);
+    const double *l = qs + 3 * (m - sl.m0);
+    double b0 = l[0] + u0, b1 = l[1] + u1, b2 = l[2] + u2;
+    b0 += w1 * d[2] - w2 * d[1];
+    b1 += w2 * d[0] - w0 * d[2];
+    b2 += w0 * d[1] - w1 * d[0];
+    double *o = zs + 3 * (m - sl.m0);
+    o[0] = minv * b0;
+    o[1] = minv * b1;
+    o[2] = minv * b2;
+  }
+  __syncthreads();
+}
+
+// FP32 source records {x - origin, f, 0, 0} of the slice's blobs for M_bb.
+__device__ void pack_records(const PgArgs &p, const PSlice &sl, const double *fs) {
+  for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += kPB) {
+    const double *f = fs + 3 * (m - sl.m0);
+    float4 a, b;
+    a.x = p.x32[3 * (size_t)m];
+    a.y = p.x32[3 * (size_t)m + 1];
+    a.z = p.x32[3 * (size_t)m + 2];
+    a.w = float(f[0]);
+    b.x = float(f[1]);
+    b.y = float(f[2]);
+    b.z = 0.f;
+    b.w = 0.f;
+    float4 *r = reinterpret_cast<float4 *>(p.rec + 8 * (size_t)m);
+    r[0] = a;
+    r[1] = b;
+  }
+}
+
+// M_bb of the packed records: (target block x source split) units over the
+// CTAs other than CTA 0 (which meanwhile runs the Givens step), two targets
+// per thread, FP32 pairs, per-tile compensated sums; each split's sum is
+// written as its (hi, lo) FP32 pair mpart[(split * nb + target) * 3 + k]
+// (the consumer adds the splits compensated and scales by 1 / (8 pi mu)).
+__device__ void mbb_units(const PgArgs &p, float *src) {
+  const int nb = p.g.nb;
+  const int units = p.TB * p.S;
+  const int first = gridDim.x > 1 ? 1 : 0, workers = gridDim.x - first;
+  if ((int)blockIdx.x < first) return;
+  PairConst<float> pc;
+  pc.ai = p.a;
+  pc.aj = p.a;
+  pc.asum2 = p.pc_asum2;
+  pc.s = p.pc_s;
+  pc.s3 = p.pc_s3;
+  for (int u = blockIdx.x - first; u < units; u += workers) {
+    const int tb = u / p.S, sp = u - tb * p.S;
+    const int t0 = tb * p.tbs, t1 = min(nb, t0 + p.tbs);
+    const int s0 = sp * p.chunk, s1 = min(nb, s0 + p.chunk);
+    if (t0 >= t1 || s0 >= s1) continue;  // CTA-uniform
+    int i[2];
+    bool act[2];
+    float xt[2], yt[2], zt[2], hi[2][3], lo[2][3];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      i[t] = t0 + (int)threadIdx.x + t * kPB;
+      act[t] = i[t] < t1;
+      if (!act[t]) i[t] = t1 - 1;
+      xt[t] = __ldcg(p.x32 + 3 * (size_t)i[t]);
+      yt[t] = __ldcg(p.x32 + 3 * (size_t)i[t] + 1);
+      zt[t] = __ldcg(p.x32 + 3 * (size_t)i[t] + 2);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) hi[t][k] = lo[t][k] = 0.f;
+    }
+    const bool warp_active = __any_sync(0xffffffffu, act[0] || act[1]);
+    for (int base = s0; base < s1; base += kPTS) {
+      const int cnt = min(kPTS, s1 - base);
+      __syncthreads();
+      const float4 *g = reinterpret_cast<const float4 *>(p.rec + 8 * (size_t)base);
+      float4 *d = reinterpret_cast<float4 *>(src);
+      for (int q = threadIdx.x; q < 2 * cnt; q += kPB) d[q] = __ldcg(g + q);
+      __syncthreads();
+      if (!warp_active) continue;
+      float v[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      unsigned nl[2] = {0u, 0u};
+#pragma unroll 2
+      for (int j = 0; j < cnt; ++j) {
+        float sx, sy, sz, f[3];
+        RecLoad<float, 3>::get(src + 8 * j, sx, sy, sz, f);
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+          const float dx = xt[t] - sx, dy = yt[t] - sy, dz = zt[t] - sz;
+          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          const bool far = r2 > pc.asum2;
+          if (!far) nl[t] = NearList::push(nl[t], j);
+          const float rs = rsqrt_far(r2);
+          far_pair<float, 3, 3>(v[t], dx, dy, dz, far ? rs : 0.f, f, pc);
+        }
+      }
+      if (__any_sync(0xffffffffu, (nl[0] | nl[1]) != 0u))
+        near_pass<float, 3, 3, 2>(v, xt, yt, zt, nl, src, cnt, pc);
+#pragma unroll
+      for (int t = 0; t < 2; ++t)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) two_sum(hi[t][k], lo[t][k], v[t][k]);
+    }
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      if (!act[t]) continue;
+      float2 *o = p.mpart + ((size_t)sp * nb + i[t]) * 3;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) o[k] = make_float2(hi[t][k], lo[t][k]);
+    }
+  }
+}
+
+// ws (slice rows) = M_bb z - (U + Omega x d_m) with v = sum over splits of
+// the partial products (in split order), (U, Omega) = zv. The slice's
+// partials are staged through stage (kHB doubles) with parallel loads.
+__device__ void apply_rows(const PgArgs &p, const PSlice &sl, const double *zv, double *ws,
+                           double *stage) {
+  const int nb = p.g.nb, rows = sl.rows;
+  const int per = rows > 0 ? max(1, kHB / rows) : 1;  // splits per staging round
+  float2 *st2 = reinterpret_cast<float2 *>(stage);
+  float *acc = reinterpret_cast<float *>(ws);  // (hi, lo) per row while summing
+  for (int r = threadIdx.x; r < rows; r += kPB) acc[2 * r] = acc[2 * r + 1] = 0.f;
+  for (int s0 = 0; s0 < p.S; s0 += per) {
+    const int s1 = min(p.S, s0 + per);
+    __syncthreads();
+    for (int q = threadIdx.x; q < (s1 - s0) * rows; q += kPB) {
+      const int s = s0 + q / rows, r = q - (q / rows) * rows;
+      st2[q] = __ldcg(p.mpart + ((size_t)s * nb + sl.m0) * 3 + r);
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < rows; r += kPB) {
+      float h = acc[2 * r], l = acc[2 * r + 1];
+      for (int s = 0; s < s1 - s0; ++s) {
+        two_sum(h, l, st2[s * rows + r].x);
+        l += st2[s * rows + r].y;
+      }
+      acc[2 * r] = h;
+      acc[2 * r + 1] = l;
+    }
+  }
+  __syncthreads();
+  // convert in place: every thread reads its rows' pairs before any row is overwritten
+  double vrow[kMaxRows / kPB + 1];
+  int nr = 0;
+  for (int r = threadIdx.x; r < rows; r += kPB)
+    vrow[nr++] = p.scale * ((double)acc[2 * r] + (double)acc[2 * r + 1]);
+  __syncthreads();
+  nr = 0;
+  for (int r = threadIdx.x; r < rows; r += kPB) ws[r] = vrow[nr++];
+  __syncthreads();
+  for (int r = threadIdx.x; r < rows; r += kPB) {
+    const int m = sl.m0 + r / 3, j = r - 3 * (r / 3);
+    const double *d = sl.d + 3 * (m - sl.m0);
+    double body;
+    if (j == 0) body = zv[0] - d[1] * zv[5] + d[2] * zv[4];
+    else if (j == 1) body = zv[1] - d[2] * zv[3] + d[0] * zv[5];
+    else body = zv[2] - d[0] * zv[4] + d[1] * zv[3];
+    ws[r] = -body + ws[r];
+  }
+  __syncthreads();
+}
+
+// Row r of the slice's Krylov vector i: from the CTA's resident copy
+// (columns i < Kr, shared memory) or from global memory.
+__device__ __forceinline__ double qrow(const PgArgs &p, const PSlice &sl, const double *qres,
+                                       int i, int r) {
+  return i < p.Kr ? qres[(size_t)i * sl.rows + r]
+                  : ldcg(p.g.Q + (size_t)i * p.g.n + 3 * (size_t)sl.m0 + r);
+}
+
+// Store the slice rows ws as Krylov vector i (resident copy and global).
+__device__ void store_q(const PgArgs &p, const PSlice &sl, double *qres, int i, const double *ws) {
+  for (int r = threadIdx.x; r < sl.rows; r += kPB) {
+    if (i < p.Kr) qres[(size_t)i * sl.rows + r] = ws[r];
+    p.g.Q[(size_t)i * p.g.n + 3 * (size_t)sl.m0 + r] = ws[r];
+  }
+}
+
+// dots of the slice rows ws with Q_i, i < k (one thread per i, rows in
+// order) into pd[i * G + c]
+__device__ void slice_dots(const PgArgs &p, const PSlice &sl, const double *ws, int k,
+                           double *pd, const double *qres) {
+  if (!sl.owner) return;
+  // four threads (adjacent lanes) per i, rows r = part (mod 4), then a fixed
+  // two-level shuffle; k <= kPB / 4 per pass
+  const int part = threadIdx.x & 3;
+  for (int i0 = 0; i0 < k; i0 += kPB / 4) {
+    const int i = i0 + (threadIdx.x >> 2);
+    double s = 0.0;
+    if (i < k) {
+      if (i < p.Kr) {
+        const double *q = qres + (size_t)i * sl.rows;
+        for (int r = part; r < sl.rows; r += 4) s += ws[r] * q[r];
+      } else {
+        for (int r = part; r < sl.rows; r += 4) s += ws[r] * qrow(p, sl, qres, i, r);
+      }
+    }
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (i < k && part == 0) pd[(size_t)i * p.g.G + blockIdx.x] = s;
+  }
+}
+
+// ws (slice rows) += sign * sum_{i<k} h_i Q_i (one thread per row, i in order)
+__device__ void slice_axpy(const PgArgs &p, const PSlice &sl, const double *h, int k, double *ws,
+                           double sign, const double *qres) {
+  for (int r = threadIdx.x; r < sl.rows; r += kPB) {
+    double t = 0.0;
+    for (int i = 0; i < k; ++i) t += h[i] * qrow(p, sl, qres, i, r);
+    ws[r] += sign * t;
+  }
+  __syncthreads();
+}
+
+// v[l] += sign * sum_{i<k} h_i Q_i,vel(l): warp l < 6, lanes over i, fixed
+// tree; the body rows of every Krylov vector are resident in qvres[6 i + l].
+__device__ void vel_axpy(const double *qvres, const double *h, int k, double *v, double sign) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (wid < 6) {
+    double s = 0.0;
+    for (int i = lane; i < k; i += 32) s += h[i] * qvres[6 * i + wid];
+    s = warp_sum(s);
+    if (lane == 0) v[wid] += sign * s;
+  }
+  __syncthreads();
+}
+
+// Gram-Schmidt coefficients, spread over the grid: warp w of CTA c sums
+// h_j = sum_c' pd[j * G + c'] + w_vel . Q_j,vel for j = c + P (w + kPW t),
+// into hg[j] (global).
+__device__ void reduce_dots(const PgArgs &p, const double *pd, int k, const double *wv,
+                            const double *qvres, double *hg) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int G = p.g.G;
+  for (int j = blockIdx.x + gridDim.x * wid; j < k; j += gridDim.x * kPW) {
+    double s = 0.0;
+    for (int c = lane; c < G; c += 32) s += ldcg(pd + (size_t)j * G + c);
+    s = warp_sum(s);
+    if (lane == 0) {
+      double t = 0.0;
+      for (int l = 0; l < 6; ++l) t += wv[l] * qvres[6 * j + l];
+      hg[j] = s + t;
+    }
+  }
+}
+
+// Givens rotations of the new Hessenberg column (mobility_solver.cpp:
+// 2370-2413): hcol[0..k] in, rotated in place; updates cs, sn, beta;
+// returns |beta_k| / norm_rhs. One thread.
+__device__ double givens_step(int k, double *hcol, double *cs, double *sn, double *beta,
+                              double norm_rhs) {
+  for (int i = 1; i < k; ++i) {
+    const double tt = cs[i - 1] * hcol[i - 1] + sn[i - 1] * hcol[i];
+    hcol[i] = cs[i - 1] * hcol[i] - sn[i - 1] * hcol[i - 1];
+    hcol[i - 1] = tt;
+  }
+  const double hd = hcol[k - 1], hs = hcol[k];
+  if (hs == 0.0) {
+    cs[k - 1] = 1.0;
+    sn[k - 1] = 0.0;
+  } else if (fabs(hs) > fabs(hd)) {
+    const double tt = hd / hs;
+    sn[k - 1] = (2.0 * (double)(hs > 0) - 1.0) / sqrt(1.0 + tt * tt);
+    cs[k - 1] = tt * sn[k - 1];
+  } else {
+    const double tt = hs / hd;
+    cs[k - 1] = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + tt * tt);
+    sn[k - 1] = tt * cs[k - 1];
+  }
+  hcol[k - 1] = cs[k - 1] * hd + sn[k - 1] * hs;
+  hcol[k] = 0.0;
+  beta[k] = -sn[k - 1] * beta[k - 1];
+  beta[k - 1] = cs[k - 1] * beta[k - 1];
+  return fabs(beta[k]) / norm_rhs;
+}
+
+// y = H^-1 beta (:2419-2438) in yv (shared), by the whole CTA: columns
+// j < k - 1 of H staged from global memory into hb (kHB doubles) in chunks,
+// column k - 1 from hcol; warp 0 substitutes column by column.
+__device__ void back_substitute(const PgArgs &p, int k, const double *hcol, const double *beta,
+                                double *yv, double *hb) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int ld = p.g.max_iter + 1;
+  for (int i = threadIdx.x; i < k; i += kPB) yv[i] = beta[i];
+  int jhi = k - 1;
+  while (jhi >= 0) {
+    // columns jhi, jhi-1, ..., jlo (rows 0..j each) fit in hb
+    int jlo = jhi, used = jhi + 1;
+    while (jlo > 0 && used + jlo <= kHB) {
+      used += jlo;
+      --jlo;
+    }
+    __syncthreads();
+    int off = 0;
+    for (int j = jhi; j >= jlo; --j) {
+      for (int i = threadIdx.x; i <= j; i += kPB)
+        hb[off + i] = (j == k - 1) ? hcol[i] : ldcg(p.g.H + i + (size_t)j * ld);
+      off += j + 1;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      off = 0;
+      for (int j = jhi; j >= jlo; --j) {
+        const double yj = yv[j] / hb[off + j];
+        __syncwarp();
+        for (int i = lane; i < j; i += 32) yv[i] -= hb[off + i] * yj;
+        __syncwarp();
+        if (lane == 0) yv[j] = yj;
+        __syncwarp();
+        off += j + 1;
+      }
+    }
+    jhi = jlo - 1;
+  }
+  __syncthreads();
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(PgArgs p) {
+  __shared__ __align__(16) float src[8 * kPTS];
+  __shared__ double ws[kMaxRows];            // w (then Q_k, tmp) rows of the slice
+  __shared__ double zs[kMaxRows];            // z = P^-1 q rows of the slice
+  __shared__ double h1[kPK], h2[kPK], cs[kPK], sn[kPK], beta[kPK], hcol[kPK], yv[kPK];
+  __shared__ double tmp8[8];
+  __shared__ double wvel[6], qvel[6], zv[6];
+  __shared__ double dsl[kMaxRows], mats[72], qn_s[2];
+  // dynamic: staging buffer (kHB), staged per-CTA partials (8 x kMaxPgCtas),
+  // body rows of every Krylov vector (6 x kPK), resident Krylov rows (Kr x rows)
+  extern __shared__ double dyn[];
+  double *hb = dyn, *cst = hb + kHB, *qvres = cst + 8 * kMaxPgCtas, *qres = qvres + 6 * kPK;
+
+  const GmresArgs &g = p.g;
+  GmresScalars *st = g.st;
+  const PSlice sl = pg_slice(p, dsl);
+  const int nb = g.nb, vel = 3 * nb, G = g.G;
+  const size_t n = g.n;
+
+  // ---- start: the slice's d_m and the body matrices into shared memory,
+  //      warm start into soln, FP32 targets, records, ||rhs|| partials
+  for (int r = threadIdx.x; r < sl.rows; r += kPB) dsl[r] = g.diff[3 * (size_t)sl.m0 + r];
+  for (int q = threadIdx.x; q < 72; q += kPB) mats[q] = g.mats[q];
+  for (int r = threadIdx.x; r < sl.rows; r += kPB) {
+    const int t = 3 * sl.m0 + r;
+    ws[r] = g.f_blobs[t];
+    g.soln[t] = ws[r];
+    zs[r] = g.rhs[t];
+  }
+  for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += kPB)
+    for (int k = 0; k < 3; ++k)
+      p.x32[3 * (size_t)m + k] = float(g.x_blobs[3 * (size_t)m + k] - g.origin[k]);
+  if (sl.body && threadIdx.x < 6) g.soln[vel + threadIdx.x] = g.v_bodies[threadIdx.x];
+  __syncthreads();
+  pack_records(p, sl, ws);
+  slice_partials(p, sl, zs, K_RHS, S_RHS);
+  slice_partials(p, sl, ws, K_SOLN, -1);
+  if (!pg_barrier(p)) return;
+
+  // ---- M_bb of the warm start
+  mbb_units(p, src);
+  if (!pg_barrier(p)) return;
+
+  // ---- residual r0 = rhs - A soln (slice rows), partials
+  if (threadIdx.x < 6) zv[threadIdx.x] = g.v_bodies[threadIdx.x];
+  __syncthreads();
+  apply_rows(p, sl, zv, ws, hb);  // ws = A soln (blob rows)
+  for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = zs[r] - ws[r];  // zs = rhs rows
+  __syncthreads();
+  slice_partials(p, sl, ws, K_R0, S_R0);
+  if (!pg_barrier(p)) return;
+
+  // ---- beta_0, warm-start tests (mobility_solver.cpp:2279-2320), Q_0,
+  //      preconditioner of Q_0, records (every CTA decides the same)
+  double norm_rhs;
+  {
+    cta_sums(p.ps + (size_t)S_RHS * G, G, 1, tmp8, cst);
+    double rhs_vel[6], t = tmp8[0];
+    for (int j = 0; j < 6; ++j) {
+      rhs_vel[j] = g.rhs[vel + j];
+      t += rhs_vel[j] * rhs_vel[j];
+    }
+    norm_rhs = sqrt(t);
+    cta_sums(p.p6 + (size_t)K_SOLN * 6 * G, G, 6, tmp8, cst);
+    double r0v[6];
+    for (int j = 0; j < 6; ++j) r0v[j] = rhs_vel[j] - (-tmp8[j]);
+    __syncthreads();
+    cta_sums(p.ps + (size_t)S_R0 * G, G, 1, tmp8, cst);
+    double bb = tmp8[0];
+    for (int j = 0; j < 6; ++j) bb += r0v[j] * r0v[j];
+    double beta0 = sqrt(bb);
+    int flag = 0;
+    if (norm_rhs == 0.0) flag = 3;
+    else if (fabs(beta0) <= g.tol * norm_rhs) flag = 1;
+    else if (fabs(beta0) > norm_rhs) {
+      flag = 2;
+      beta0 = norm_rhs;
+    }
+    __syncthreads();
+    if (flag == 1 || flag == 3) {
+      if (flag == 3) {
+        for (int r = threadIdx.x; r < sl.rows; r += kPB) g.f_blobs[3 * sl.m0 + r] = 0.0;
+        if (sl.body && threadIdx.x < 6) g.v_bodies[threadIdx.x] = 0.0;
+      }
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->norm_rhs = norm_rhs;
+        st->flag = flag;
+        st->iters = 0;
+        st->rel = 0.0;
+        st->status = 0;
+        st->done = 1;
+      }
+      return;
+    }
+    // Q_0: r0 / beta0, or rhs / ||rhs|| with a zero start (flag 2)
+    int kslot;
+    double inv;
+    if (flag == 2) {
+      for (int r = threadIdx.x; r < sl.rows; r += kPB) {
+        ws[r] = zs[r];
+        g.soln[3 * sl.m0 + r] = 0.0;
+      }
+      if (sl.body && threadIdx.x < 6) g.soln[vel + threadIdx.x] = 0.0;
+      if (threadIdx.x < 6) qvel[threadIdx.x] = rhs_vel[threadIdx.x] / norm_rhs;
+      kslot = K_RHS;
+      inv = norm_rhs;
+    } else {
+      if (threadIdx.x < 6) qvel[threadIdx.x] = r0v[threadIdx.x] / beta0;
+      kslot = K_R0;
+      inv = beta0;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = ws[r] / inv;
+    __syncthreads();
+    store_q(p, sl, qres, 0, ws);
+    if (threadIdx.x < 6) {
+      qvres[threadIdx.x] = qvel[threadIdx.x];
+      if (sl.body) g.Q[vel + threadIdx.x] = qvel[threadIdx.x];
+    }
+    if (threadIdx.x == 0) beta[0] = beta0;
+    // z = P^-1 Q_0: sum_m (Q_0 ; d x Q_0) = (partials of the unscaled vector) / inv
+    cta_sums(p.p6 + (size_t)kslot * 6 * G, G, 6, tmp8, cst);
+    precond(p, sl, ws, qvel, tmp8, 1.0 / inv, zs, zv, mats);
+    pack_records(p, sl, zs);
+    slice_partials(p, sl, zs, K_Z, -1);
+  }
+  if (!pg_barrier(p)) return;
+
+  // ---- Arnoldi steps. Step k: M_bb z_{k-1} (CTA 0 meanwhile finishes step
+  //      k-1's Givens rotation and convergence test), w = A z_{k-1}, two
+  //      classical Gram-Schmidt passes, ||w||, Q_k = w / ||w||, z_k = P^-1 Q_k.
+  double *h1g = p.aux + kCtl, *h2g = h1g + kPK, *yg = h2g + kPK;
+  int k = 1;
+  double qn = 0.0;
+  for (;;) {
+    mbb_units(p, src);
+    if (blockIdx.x == 0 && k > 1) {
+      // Givens rotation (mobility_solver.cpp:2370-2413) of step kk = k - 1
+      const int kk = k - 1;
+      if (threadIdx.x == 0) {
+        for (int i = 0; i < kk; ++i) hcol[i] = h1[i] + h2[i];
+        hcol[kk] = qn;
+        const double rel = givens_step(kk, hcol, cs, sn, beta, norm_rhs);
+        int fin = rel <= g.tol || kk == g.max_iter;
+        int stt = 0;
+        if (!(rel == rel)) {
+          fin = 1;
+          stt = 1;
+        }
+        tmp8[0] = fin;
+        tmp8[1] = rel;
+        tmp8[2] = stt;
+      }
+      __syncthreads();
+      const int ld = g.max_iter + 1;
+      for (int i = threadIdx.x; i <= kk; i += kPB) g.H[i + (size_t)(kk - 1) * ld] = hcol[i];
+      if (tmp8[0] != 0.0) {
+        back_substitute(p, kk, hcol, beta, yv, hb);
+        for (int i = threadIdx.x; i < kk; i += kPB) yg[i] = yv[i];
+      }
+      if (threadIdx.x == 0) {
+        p.aux[C_FINISH] = tmp8[0];
+        p.aux[C_REL] = tmp8[1];
+        p.aux[C_STATUS] = tmp8[2];
+      }
+    }
+    if (!pg_barrier(p)) return;
+    if (k > 1 && ldcg(p.aux + C_FINISH) != 0.0) {
+      k -= 1;
+      break;
+    }
+
+    // w = A z (slice rows; body rows w_vel = -sum (z ; d x z) in every CTA),
+    // CGS pass 1 partial dots
+    stage(p.p6 + (size_t)K_Z * 6 * G, 6 * G, cst);
+    if (p.S * sl.rows <= kHB) {
+      float2 *st2 = reinterpret_cast<float2 *>(hb);
+      for (int q = threadIdx.x; q < p.S * sl.rows; q += kPB) {
+        const int sp = q / sl.rows, r = q - sp * sl.rows;
+        st2[q] = __ldcg(p.mpart + ((size_t)sp * nb + sl.m0) * 3 + r);
+      }
+      __syncthreads();
+      sum_staged(cst, G, 6, tmp8);
+      for (int r = threadIdx.x; r < sl.rows; r += kPB) {
+        float h = 0.f, l = 0.f;
+        for (int sp = 0; sp < p.S; ++sp) {
+          two_sum(h, l, st2[sp * sl.rows + r].x);
+          l += st2[sp * sl.rows + r].y;
+        }
+        const double v = p.scale * ((double)h + (double)l);
+        const int m = sl.m0 + r / 3, j = r - 3 * (r / 3);
+        const double *d = sl.d + 3 * (m - sl.m0);
+        double body;
+        if (j == 0) body = zv[0] - d[1] * zv[5] + d[2] * zv[4];
+        else if (j == 1) body = zv[1] - d[2] * zv[3] + d[0] * zv[5];
+        else body = zv[2] - d[0] * zv[4] + d[1] * zv[3];
+        ws[r] = -body + v;
+      }
+      __syncthreads();
+    } else {
+      __syncthreads();
+      sum_staged(cst, G, 6, tmp8);
+      apply_rows(p, sl, zv, ws, hb);
+    }
+    if (threadIdx.x < 6) wvel[threadIdx.x] = -tmp8[threadIdx.x];
+    slice_dots(p, sl, ws, k, p.pd1, qres);
+    if (!pg_barrier(p)) return;
+    reduce_dots(p, p.pd1, k, wvel, qvres, h1g);
+    if (!pg_barrier(p)) return;
+
+    // h1; w -= Q h1; CGS pass 2 partial dots
+    for (int i = threadIdx.x; i < k; i += kPB) h1[i] = ldcg(h1g + i);
+    __syncthreads();
+    slice_axpy(p, sl, h1, k, ws, -1.0, qres);
+    vel_axpy(qvres, h1, k, wvel, -1.0);
+    slice_dots(p, sl, ws, k, p.pd2, qres);
+    if (!pg_barrier(p)) return;
+    reduce_dots(p, p.pd2, k, wvel, qvres, h2g);
+    if (!pg_barrier(p)) return;
+
+    // h2; w -= Q h2; ||w|| and sum (w ; d x w) partials
+    for (int i = threadIdx.x; i < k; i += kPB) h2[i] = ldcg(h2g + i);
+    __syncthreads();
+    slice_axpy(p, sl, h2, k, ws, -1.0, qres);
+    vel_axpy(qvres, h2, k, wvel, -1.0);
+    slice_partials(p, sl, ws, K_W, S_NORM);
+    if (!pg_barrier(p)) return;
+
+    // ||w||, Q_k = w / ||w||, z_k = P^-1 Q_k (sum (Q_k ; d x Q_k) = K_W / ||w||)
+    stage(p.ps + (size_t)S_NORM * G, G, cst);
+    stage(p.p6 + (size_t)K_W * 6 * G, 6 * G, cst + G);
+    __syncthreads();
+    sum_staged(cst, G, 7, tmp8);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = tmp8[0];
+      for (int j = 0; j < 6; ++j) t += wvel[j] * wvel[j];
+      qn_s[0] = sqrt(t);
+      qn_s[1] = 1.0 / qn_s[0];
+    }
+    __syncthreads();
+    qn = qn_s[0];
+    const double rqn = qn_s[1];
+    for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = ws[r] * rqn;
+    __syncthreads();
+    store_q(p, sl, qres, k, ws);
+    if (threadIdx.x < 6) {
+      qvel[threadIdx.x] = wvel[threadIdx.x] * rqn;
+      qvres[6 * k + threadIdx.x] = qvel[threadIdx.x];
+      if (sl.body) g.Q[(size_t)k * n + vel + threadIdx.x] = qvel[threadIdx.x];
+    }
+    __syncthreads();
+    precond(p, sl, ws, qvel, tmp8 + 1, rqn, zs, zv, mats);
+    pack_records(p, sl, zs);
+    slice_partials(p, sl, zs, K_Z, -1);
+    if (!pg_barrier(p)) return;
+    ++k;
+  }
+
+  // ---- tmp = Q y (slice rows in ws, body rows in qvel), z = P^-1 tmp,
+  //      soln += z -> (f_blobs, v_bodies) (:2440-2563)
+  for (int i = threadIdx.x; i < k; i += kPB) yv[i] = ldcg(yg + i);
+  for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = 0.0;
+  if (threadIdx.x < 6) qvel[threadIdx.x] = 0.0;
+  __syncthreads();
+  slice_axpy(p, sl, yv, k, ws, 1.0, qres);
+  vel_axpy(qvres, yv, k, qvel, 1.0);
+  slice_partials(p, sl, ws, K_T, -1);
+  if (!pg_barrier(p)) return;
+  cta_sums(p.p6 + (size_t)K_T * 6 * G, G, 6, tmp8, cst);
+  precond(p, sl, ws, qvel, tmp8, 1.0, zs, zv, mats);
+  for (int r = threadIdx.x; r < sl.rows; r += kPB) {
+    const int t = 3 * sl.m0 + r;
+    const double x = g.soln[t] + zs[r];
+    g.soln[t] = x;
+    g.f_blobs[t] = x;
+  }
+  if (sl.body && threadIdx.x < 6) {
+    const double x = g.soln[vel + threadIdx.x] + zv[threadIdx.x];
+    g.soln[vel + threadIdx.x] = x;
+    g.v_bodies[threadIdx.x] = x;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->norm_rhs = norm_rhs;
+    st->rel = ldcg(p.aux + C_REL);
+    st->iters = k;
+    st->flag = 0;
+    st->status = (int)ldcg(p.aux + C_STATUS);
+    st->done = 1;
+  }
+}
+
+int pg_grid(int nb, int sms, int max_iter, PgShape *shape) {
+  int dev = 0, optin = 0;
+  cudaFuncAttributes fa{};
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+          cudaSuccess ||
+      cudaFuncGetAttributes(&fa, gmres_persistent_kernel) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int P = sms;  // one CTA per SM
+  if (P > kMaxPgCtas) return 0;
+  int G = std::max(1, std::min(P, (nb + 3) / 4));
+  int per = std::max(1, (nb + G - 1) / G);
+  G = std::max(1, (nb + per - 1) / per);
+  if (per > kMaxPgBlobsPerCta) return 0;
+  const int rows = 3 * per;
+  // dynamic shared memory: the staging buffer, then as many resident Krylov
+  // columns of the slice as fit (all max_iter + 1 when possible)
+  const long avail = (long)optin - (long)fa.sharedSizeBytes - 1024;
+  const long cols = (avail / 8 - kPgDynFixed) / rows;
+  if (cols < 1) return 0;
+  const int Kr = (int)std::min<long>(max_iter + 1, cols);
+  const size_t dyn = sizeof(double) * (kPgDynFixed + (size_t)Kr * rows);
+  int occ = 0;
+  if (cudaFuncSetAttribute(gmres_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)dyn) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gmres_persistent_kernel, kPB, dyn) !=
+          cudaSuccess ||
+      occ < 1) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int workers = P > 1 ? P - 1 : 1;  // CTA 0 runs the Givens step meanwhile
+  const int TB = std::max(1, (nb + 2 * kPB - 1) / (2 * kPB));
+  const int tbs = (nb + TB - 1) / TB;
+  int S = std::max(1, std::min(workers / TB, nb / 32));
+  const int chunk = (nb + S - 1) / S;
+  S = (nb + chunk - 1) / chunk;
+  shape->P = P;
+  shape->G = G;
+  shape->blobs_per_cta = per;
+  shape->TB = TB;
+  shape->tbs = tbs;
+  shape->S = S;
+  shape->chunk = chunk;
+  shape->Kr = Kr;
+  shape->dyn_smem = dyn;
+  return 1;
+}
+
+cudaError_t launch_gmres_persistent(const PgArgs &p, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(p.bar, 0, 4 * sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  void *args[] = {const_cast<PgArgs *>(&p)};
+  e = cudaLaunchCooperativeKernel((const void *)gmres_persistent_kernel, dim3(p.P), dim3(kPB),
+                                  args, p.dyn_smem, st);
+  count_launch();
+  return e;
+}
+
+}  // namespace tfs

@@ -193,6 +193,50 @@ int gmres_run(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodie
   return TFS_OK;
 }
 
+// Inner GMRES of the refinement as one cooperative kernel (FP32 M_bb).
+int gmres_run_persistent(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies,
+                         double tol, int *iters) {
+  GmresArgs g = gmres_args(s, rhs, f_blobs, v_bodies, s->gst, tol, 1);
+  g.G = s->pg.G;
+  g.blobs_per_cta = s->pg.blobs_per_cta;
+  PgArgs p{};
+  p.g = g;
+  p.x32 = s->pg_x32;
+  p.rec = s->pg_rec;
+  p.mpart = s->pg_mpart;
+  p.p6 = s->pg_p6;
+  p.ps = s->pg_ps;
+  p.pd1 = s->pg_pd1;
+  p.pd2 = s->pg_pd2;
+  p.aux = s->pg_aux;
+  p.bar = s->pg_bar;
+  p.P = s->pg.P;
+  p.TB = s->pg.TB;
+  p.tbs = s->pg.tbs;
+  p.S = s->pg.S;
+  p.chunk = s->pg.chunk;
+  p.Kr = s->pg.Kr;
+  p.dyn_smem = s->pg.dyn_smem;
+  p.a = (float)s->cfg.a_blob;
+  const double ab = s->cfg.a_blob;
+  p.pc_asum2 = (float)((2.0 * ab) * (2.0 * ab));
+  p.pc_s = (float)(2.0 * ab * ab / 3.0);
+  p.pc_s3 = (float)(-2.0 * ab * ab);
+  p.minv = 6.0 * 3.14159265358979323846264338327950288 * s->cfg.mu * ab;
+  p.scale = 1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu);
+  cudaError_t e = launch_gmres_persistent(p, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "persistent GMRES");
+  GmresScalars h{};
+  int rc;
+  if ((rc = poll(s, 0, &h)) != TFS_OK) return rc;
+  if (h.status == 2) return fail(TFS_ETIMEOUT, "persistent GMRES: a grid barrier timed out");
+  if (h.status == 1) return fail(TFS_ENAN, "GMRES residual is not finite");
+  if (!h.done) return fail(TFS_ESTATE, "persistent GMRES ended without a result");
+  *iters = h.iters;
+  s->last_rel = h.rel;
+  return TFS_OK;
+}
+
 // The linear solve of compute_velocities on s->rhs: plain FP64 GMRES, or
 // FP32C iterative refinement.
 int linear_solve(tfs_solver *s, int *iters) {
@@ -225,7 +269,9 @@ int linear_solve(tfs_solver *s, int *iters) {
     if (h.status) return fail(TFS_ENAN, "refinement residual is not finite");
     if (h.done || it == s->max_outer) break;
     int inner = 0;
-    rc = gmres_run(s, s->r, s->dx, s->dx + vel, s->inner_tol, 1, &inner);
+    rc = (s->pg_ok && s->pg_enabled)
+             ? gmres_run_persistent(s, s->r, s->dx, s->dx + vel, s->inner_tol, &inner)
+             : gmres_run(s, s->r, s->dx, s->dx + vel, s->inner_tol, 1, &inner);
     if (rc != TFS_OK && rc != TFS_ENOTCONV) return rc;
     total += inner;
     ++cycles;
@@ -280,6 +326,23 @@ int solve_alloc(tfs_solver *s) {
       (rc = alloc_dev((void **)&s->gcounters, 8 * sizeof(unsigned))))
     return rc;
   cudaMemsetAsync(s->gcounters, 0, 8 * sizeof(unsigned), s->stream);
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->device);
+  if (coop && s->nb > 0 && s->max_iter <= 350 && pg_grid(s->nb, num_sms(), s->max_iter, &s->pg)) {
+    const size_t nb = s->nb;
+    if ((rc = alloc_dev((void **)&s->pg_x32, 4 * 3 * nb)) ||
+        (rc = alloc_dev((void **)&s->pg_rec, 4 * 8 * nb)) ||
+        (rc = alloc_dev((void **)&s->pg_mpart, 8 * 3 * nb * (size_t)s->pg.S)) ||
+        (rc = alloc_dev((void **)&s->pg_p6, 8 * pg_p6_elems(s->pg))) ||
+        (rc = alloc_dev((void **)&s->pg_ps, 8 * pg_ps_elems(s->pg))) ||
+        (rc = alloc_dev((void **)&s->pg_pd1, 8 * pg_pd_elems(s->pg))) ||
+        (rc = alloc_dev((void **)&s->pg_pd2, 8 * pg_pd_elems(s->pg))) ||
+        (rc = alloc_dev((void **)&s->pg_aux, 8 * kPgAuxElems)) ||
+        (rc = alloc_dev((void **)&s->pg_bar, 4 * sizeof(unsigned))))
+      return rc;
+    s->pg_ok = 1;
+  }
+  cudaGetLastError();
   if (cudaHostAlloc((void **)&s->gst_host, 2 * sizeof(GmresScalars), cudaHostAllocDefault) !=
           cudaSuccess ||
       cudaHostAlloc((void **)&s->f6_host, 8 * 6, cudaHostAllocDefault) != cudaSuccess) {
@@ -313,6 +376,15 @@ void solve_free(tfs_solver *s) {
                     s->dx, s->gpart, s->gpart6, s->gh1, s->gh2};
   for (double *b : bufs) cudaFree(b);
   cudaFree(s->gcounters);
+  cudaFree(s->pg_x32);
+  cudaFree(s->pg_rec);
+  cudaFree(s->pg_mpart);
+  cudaFree(s->pg_p6);
+  cudaFree(s->pg_ps);
+  cudaFree(s->pg_pd1);
+  cudaFree(s->pg_pd2);
+  cudaFree(s->pg_aux);
+  cudaFree(s->pg_bar);
   cudaFree(s->gst);
   if (s->gst_host) cudaFreeHost(s->gst_host);
   if (s->f6_host) cudaFreeHost(s->f6_host);
@@ -367,6 +439,14 @@ int tfs_set_refinement(tfs_solver *s, double inner_tol, int max_cycles) {
     return fail(TFS_EINVAL, "inner_tol in (0, 1), max_cycles >= 1");
   s->inner_tol = inner_tol;
   s->max_outer = max_cycles;
+  return TFS_OK;
+}
+
+int tfs_set_persistent_gmres(tfs_solver *s, int enable) {
+  TFS_CHECK_SOLVER(s);
+  if (enable && !s->pg_ok)
+    return fail(TFS_ESTATE, "the persistent GMRES kernel cannot run for this system or device");
+  s->pg_enabled = enable != 0;
   return TFS_OK;
 }
 

@@ -55,6 +55,14 @@ struct tfs_solver {
   int gG = 1, g_blobs_per_cta = 1;    // GMRES kernel grid
   double *gpart = nullptr, *gpart6 = nullptr, *gh1 = nullptr, *gh2 = nullptr;
   unsigned *gcounters = nullptr;
+  // persistent inner GMRES (FP32C); pg_ok = 0 when it cannot run here
+  int pg_ok = 0, pg_enabled = 1;
+  tfs::PgShape pg{};
+  float *pg_x32 = nullptr, *pg_rec = nullptr;
+  float2 *pg_mpart = nullptr;
+  double *pg_p6 = nullptr, *pg_ps = nullptr, *pg_pd1 = nullptr,
+         *pg_pd2 = nullptr, *pg_aux = nullptr;
+  unsigned *pg_bar = nullptr;
   tfs::GmresScalars *gst_host = nullptr;  // pinned copies
   double *f6_host = nullptr;              // pinned 6
   int last_iters = 0, last_outer = 0;

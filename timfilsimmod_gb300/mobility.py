@@ -245,6 +245,11 @@ class RpyMobilitySolver:
     def set_refinement(self, inner_tol: float = 1e-4, max_cycles: int = 12) -> None:
         self._call("tfs_set_refinement", float(inner_tol), int(max_cycles))
 
+    def set_persistent_gmres(self, enable: bool = True) -> None:
+        """FP32C inner GMRES as one cooperative kernel (default) or as a
+        sequence of kernels per Arnoldi step."""
+        self._call("tfs_set_persistent_gmres", int(bool(enable)))
+
     def make_body_reference_matrices(self) -> tuple[np.ndarray, np.ndarray]:
         """Returns (body_mobility_reference, KTKinv_reference), 6x6 column-major flat."""
         self._call("tfs_make_body_reference_matrices")
