@@ -324,3 +324,106 @@ class ReferenceSolver:
                                              _ptr(vb), _ptr(fb), _ptr(vbod), _ptr(sfo))
         return dict(iters=it, v_segs=vs, v_blobs_rhs=vb, f_blobs=fb, v_bodies=vbod,
                     swimmer_f=sfo)
+
+
+class ReferenceStep:
+    """The reference's implicit time step (cilia_sim_main.cu:355-527 with
+    swimmer.cpp, filament.cpp, rigid_body.cpp, segment.cpp,
+    broyden_solver.cpp and mobility_solver.cpp compiled unchanged by
+    `make -C oracle ref`; LINEAR_SYSTEM_TOL = 1e-10, DT = 1e-3, the
+    reference's Broyden TOL 1e-4), for one free swimmer with elastic
+    filaments; single instance per process. The pair sums come from the
+    pinned C restatement (multi-threaded). The stage methods mirror the main
+    loop so tests can compare every stage."""
+
+    def __init__(self, nfil, nseg, blob_refs, fil_refs, fil_dirs, end_force_magnitude_real,
+                 seg_sep=2.2, body_length=40.0, body_x=(0, 0, 0), body_q=(1, 0, 0, 0),
+                 threads=None):
+        threads = threads or (os.cpu_count() or 1)
+        path = os.path.join(REF_DIR, "libref_solver_s1.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+        self.nfil, self.nseg = nfil, nseg
+        self.refs = _c(blob_refs)
+        self.nblob = self.refs.size // 3
+        self.ns = nfil * nseg
+        self.nbroy = 6 * (self.ns + 1)
+        fr, fd, bx, bq = _c(fil_refs), _c(fil_dirs), _c(body_x), _c(body_q)
+        self.lib.ref_use_port_kernels(int(threads))
+        self.lib.ref_step_setup(nfil, nseg, self.nblob, ctypes.c_double(end_force_magnitude_real),
+                                ctypes.c_double(seg_sep), ctypes.c_double(body_length),
+                                _ptr(self.refs), _ptr(fr), _ptr(fd), _ptr(bx), _ptr(bq))
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(os.path.join(REF_DIR, "libref_solver_s1.so"))
+
+    def make_body_reference_matrices(self):
+        bm, kt = np.zeros(36), np.zeros(36)
+        self.lib.ref_step_make_body_reference_matrices(_ptr(bm), _ptr(kt))
+        return bm, kt
+
+    def initial_guess(self, nt):
+        self.lib.ref_step_initial_guess(int(nt))
+
+    def forces(self, nt):
+        fs, sf = np.zeros(6 * self.ns), np.zeros(6)
+        self.lib.ref_step_forces(int(nt), _ptr(fs), _ptr(sf))
+        return fs, sf
+
+    def compute_velocities(self, nt):
+        vs, vb, fb = np.zeros(6 * self.ns), np.zeros(6), np.zeros(3 * self.nblob)
+        it = self.lib.ref_step_compute_velocities(int(nt), _ptr(vs), _ptr(vb), _ptr(fb))
+        return it, vs, vb, fb
+
+    def compute_errors(self, nt, which=0):
+        e = np.zeros(self.nbroy)
+        big = self.lib.ref_step_compute_errors(int(nt), int(which), _ptr(e))
+        return bool(big), e
+
+    def prepare_jacobian_inv(self, nt):
+        si = np.zeros(36)
+        self.lib.ref_step_prepare_jacobian_inv(int(nt), _ptr(si))
+        return si
+
+    def inverse_jacobian(self, i):
+        n = 6 * self.nseg
+        out = np.zeros(n * n)
+        self.lib.ref_step_inverse_jacobian(int(i), _ptr(out))
+        return out.reshape(n, n, order="F")
+
+    def jacobian_inv_mult(self, nt, v):
+        v = _c(v)
+        out = np.zeros(self.nbroy)
+        self.lib.ref_step_jacobian_inv_mult(int(nt), _ptr(v), _ptr(out))
+        return out
+
+    def broyden_reset(self):
+        self.lib.ref_step_broyden_reset()
+
+    def find_update(self, nt):
+        u = np.zeros(self.nbroy)
+        self.lib.ref_step_find_update(int(nt), _ptr(u))
+        return u
+
+    def apply_update(self, nt):
+        self.lib.ref_step_apply_update(int(nt))
+
+    def end_of_iter(self, nt, big):
+        self.lib.ref_step_end_of_iter(int(nt), int(bool(big)))
+
+    def run(self, nt):
+        g = ctypes.c_int(0)
+        it = self.lib.ref_step_run(int(nt), ctypes.byref(g))
+        return it, g.value
+
+    def state(self):
+        ns, nf, sg = self.ns, self.nfil, self.nseg
+        out = dict(x=np.zeros(3 * ns), q=np.zeros(4 * ns), u=np.zeros(3 * ns),
+                   lam=np.zeros(3 * (sg - 1) * nf), tether=np.zeros(3 * nf),
+                   clamp=np.zeros(3 * nf), body_x=np.zeros(3), body_q=np.zeros(4),
+                   body_u=np.zeros(3))
+        self.lib.ref_step_state(*[_ptr(out[k]) for k in ("x", "q", "u", "lam", "tether", "clamp",
+                                                         "body_x", "body_q", "body_u")])
+        return out

@@ -120,6 +120,18 @@ void ref_mbs(double *, const double *, const double *, const double *, int);
 void ref_barrier_forces(double *, double *, const double *, const double *, int, int);
 }
 
+// The C restatement of the same kernels (tfs_oracle.c, pinned to these to
+// ~5e-16 by tests/test_oracle.py), multi-threaded: the implicit-step runs
+// switch to it with ref_use_port_kernels, because the emulated kernels (one
+// host thread per CUDA thread) take minutes per Broyden iteration.
+#include "../tfs_oracle.h"
+static int g_use_port = 0;
+static orc_params g_port_params = {1.0, 1.0, 1.0};
+extern "C" void ref_use_port_kernels(int threads) {
+  g_use_port = threads > 0;
+  if (threads > 0) orc_set_threads(threads);
+}
+
 void seed_blobs(Real *const, Real *const, Real *const, Real *const) { std::abort(); }
 void seed_filaments(Real *const, Real *const, Real *const, Real *const) { std::abort(); }
 void check_seeding(Real *const, Real *const, Real *const, Real *const) { std::abort(); }
@@ -157,16 +169,28 @@ class emu_rpy_mobility_solver : public mobility_solver {
   void copy_blob_velocities_to_host() override { std::memcpy(v_blobs_host, vb_d.data(), 8 * vb_d.size()); }
   void copy_segment_velocities_to_host() override { std::memcpy(v_segs_host, vs_d.data(), 8 * vs_d.size()); }
   void apply_interparticle_forces() override {
-    ref_barrier_forces(fs_d.data(), frep_d.data(), xs_d.data(), xb_d.data(), ns(), nb());
+    if (g_use_port)
+      orc_barrier_forces(&g_port_params, fs_d.data(), frep_d.data(), xs_d.data(), xb_d.data(), ns(),
+                         nb(), NSEG, (int)END_FORCE_MAGNITUDE, REPULSIVE_FORCE_FACTOR, 1);
+    else
+      ref_barrier_forces(fs_d.data(), frep_d.data(), xs_d.data(), xb_d.data(), ns(), nb());
   }
   void wait_for_device() override {}
-  void evaluate_segment_segment_mobility() override { ref_mss(vs_d.data(), fs_d.data(), xs_d.data(), ns()); }
-  void evaluate_segment_blob_mobility() override {
-    ref_msb(vs_d.data(), fb_d.data(), xs_d.data(), xb_d.data(), ns());
+  void evaluate_segment_segment_mobility() override {
+    if (g_use_port) orc_mss(&g_port_params, vs_d.data(), fs_d.data(), xs_d.data(), ns());
+    else ref_mss(vs_d.data(), fs_d.data(), xs_d.data(), ns());
   }
-  void evaluate_blob_blob_mobility() override { ref_mbb(vb_d.data(), fb_d.data(), xb_d.data(), nb()); }
+  void evaluate_segment_blob_mobility() override {
+    if (g_use_port) orc_msb(&g_port_params, vs_d.data(), fb_d.data(), xs_d.data(), xb_d.data(), ns(), nb());
+    else ref_msb(vs_d.data(), fb_d.data(), xs_d.data(), xb_d.data(), ns());
+  }
+  void evaluate_blob_blob_mobility() override {
+    if (g_use_port) orc_mbb(&g_port_params, vb_d.data(), fb_d.data(), xb_d.data(), nb());
+    else ref_mbb(vb_d.data(), fb_d.data(), xb_d.data(), nb());
+  }
   void evaluate_blob_segment_mobility() override {
-    ref_mbs(vb_d.data(), fs_d.data(), xb_d.data(), xs_d.data(), nb());
+    if (g_use_port) orc_mbs(&g_port_params, vb_d.data(), fs_d.data(), xb_d.data(), xs_d.data(), nb(), ns());
+    else ref_mbs(vb_d.data(), fs_d.data(), xb_d.data(), xs_d.data(), nb());
   }
   void evaluate_full_mobility() override {
     evaluate_segment_segment_mobility(); evaluate_segment_blob_mobility();
@@ -256,5 +280,195 @@ void ref_set_body(const double *body_x, const double *body_q) {
 
 double ref_linear_system_tol(void) { return LINEAR_SYSTEM_TOL; }
 int ref_max_linear_system_iter(void) { return MAX_LINEAR_SYSTEM_ITER; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Implicit time steps (src/cilia/cilia_sim_main.cu:355-527) of one free
+// swimmer with elastic filaments, driven stage by stage so that tests can
+// compare every stage: initial guess, forces, compute_velocities,
+// compute_errors, the approximate Jacobian, Broyden updates, end of step.
+#include "broyden_solver.hpp"
+
+static broyden_solver *g_broyden = nullptr;
+
+extern "C" {
+
+// Geometry: blob references (body frame, blob_refs[3*NBLOB]), filament base
+// offsets (body frame, fil_refs[3*NFIL], as swimmer::initial_setup leaves
+// filament_references: already including the (RBLOB + DL/2) normal offset),
+// filament directions fil_dirs[3*NFIL], body position/orientation, and the
+// body length AXIS_DIR_BODY_LENGTH = 2R used by the sphere correction of
+// swimmer::prepare_jacobian_inv.
+int ref_step_setup(int nfil, int nseg, int nblob, double end_force_magnitude, double seg_sep,
+                   double axis_dir_body_length, const double *blob_refs, const double *fil_refs,
+                   const double *fil_dirs, const double *body_x, const double *body_q) {
+  NSWIM = 1; NFIL = nfil; NSEG = nseg; NBLOB = nblob;
+  SEG_SEP = seg_sep; DL = seg_sep;
+  AXIS_DIR_BODY_LENGTH = axis_dir_body_length;
+  END_FORCE_MAGNITUDE = end_force_magnitude;
+  NTOTAL = NSWIM * (NFIL * NSEG + NBLOB);
+  ref_sync_var(NSWIM, NSEG, NFIL, NBLOB, (int)END_FORCE_MAGNITUDE, SEG_SEP);
+  delete g_swimmers;
+  delete g_broyden;
+  if (g_solver) { g_solver->finalise(); delete g_solver; }
+  g_solver = new emu_rpy_mobility_solver();
+  g_solver->initialise();
+  g_broyden = new broyden_solver();
+  g_swimmers = new std::vector<swimmer>(1);
+  swimmer &s = (*g_swimmers)[0];
+  s.f = matrix(6, 1);
+  s.f.zero();
+  s.schur_mat_inv = matrix(6, 6);
+  s.jacobian_B_blocks = std::vector<matrix>(NFIL);
+  rigid_body &b = s.body;
+  b.blob_references.assign(blob_refs, blob_refs + 3 * nblob);
+  b.Q_init = matrix(3, 3);
+  for (int k = 0; k < 3; ++k) {
+    b.x[k] = b.xm1[k] = b.xm2[k] = body_x[k];
+    b.u[k] = b.um1[k] = 0.0;
+  }
+  b.q = quaternion(body_q[0], body_q[1], body_q[2], body_q[3]);
+  b.qm1 = b.q;
+  s.filament_references.assign(fil_refs, fil_refs + 3 * nfil);
+  s.normal_refs.assign(fil_dirs, fil_dirs + 3 * nfil);
+  s.filaments = std::vector<filament>(NFIL);
+  const Real strain_twist[3] = {0.0, 0.0, 0.0};
+  for (int i = 0; i < NFIL; ++i) {
+    const Real pos[3] = {b.x[0] + fil_refs[3 * i], b.x[1] + fil_refs[3 * i + 1],
+                         b.x[2] + fil_refs[3 * i + 2]};
+    s.filaments[i].initial_setup(pos, &fil_dirs[3 * i], strain_twist, nullptr,
+                                 &g_solver->x_segs_host[3 * i * NSEG],
+                                 &g_solver->f_segs_host[6 * i * NSEG], i);
+  }
+  return 0;
+}
+
+void ref_step_make_body_reference_matrices(double *body_mobility, double *ktkinv) {
+  g_solver->make_body_reference_matrices(*g_swimmers);
+  (*g_swimmers)[0].body_mobility_reference = g_solver->body_mobility_reference;
+  for (int k = 0; k < 36; ++k) {
+    body_mobility[k] = g_solver->body_mobility_reference.data[k];
+    ktkinv[k] = g_solver->KTKinv_reference.data[k];
+  }
+}
+
+void ref_step_initial_guess(int nt) { (*g_swimmers)[0].initial_guess(nt); }
+
+// forces_and_torques; returns the host segment forces and the swimmer force.
+void ref_step_forces(int nt, double *f_segs, double *swimmer_f) {
+  swimmer &s = (*g_swimmers)[0];
+  s.forces_and_torques(nt, 0);
+  std::memcpy(f_segs, g_solver->f_segs_host, 8 * 6 * g_solver->ns());
+  for (int k = 0; k < 6; ++k) swimmer_f[k] = s.f(k);
+}
+
+// compute_velocities on the current state; returns GMRES iterations.
+int ref_step_compute_velocities(int nt, double *v_segs, double *v_bodies, double *f_blobs) {
+  int iters = 0;
+  g_solver->compute_velocities(*g_swimmers, iters, nt);
+  std::memcpy(v_segs, g_solver->v_segs_host, 8 * 6 * g_solver->ns());
+  std::memcpy(f_blobs, g_solver->f_blobs_host, 8 * 3 * g_solver->nb());
+  for (int k = 0; k < 6; ++k) v_bodies[k] = g_solver->v_bodies(k);
+  return iters;
+}
+
+// compute_errors into broyden.error (which = 0) or broyden.new_error (1).
+int ref_step_compute_errors(int nt, int which, double *error) {
+  matrix &e = which ? g_broyden->new_error : g_broyden->error;
+  const bool big = g_solver->compute_errors(e, *g_swimmers, nt);
+  std::memcpy(error, e.data.data(), 8 * e.data.size());
+  return big ? 1 : 0;
+}
+
+void ref_step_prepare_jacobian_inv(int nt, double *schur_inv) {
+  swimmer &s = (*g_swimmers)[0];
+  s.prepare_jacobian_inv(nt);
+  for (int k = 0; k < 36; ++k) schur_inv[k] = s.schur_mat_inv.data[k];
+}
+
+// Filament i's inverse approximate Jacobian (6 NSEG x 6 NSEG, column-major).
+void ref_step_inverse_jacobian(int i, double *out) {
+  const matrix &J = (*g_swimmers)[0].filaments[i].inverse_jacobian;
+  std::memcpy(out, J.data.data(), 8 * J.data.size());
+}
+
+// swimmer.jacobian_inv_mult(in) (the approximate inverse Jacobian product).
+void ref_step_jacobian_inv_mult(int nt, const double *in, double *out) {
+  const int nbroy = 6 * (NFIL * NSEG + 1);
+  matrix m(nbroy, 1);
+  std::memcpy(m.data.data(), in, 8 * nbroy);
+  const matrix r = (*g_swimmers)[0].jacobian_inv_mult(m, nt);
+  std::memcpy(out, r.data.data(), 8 * nbroy);
+}
+
+void ref_step_broyden_reset(void) { g_broyden->iter = 0; }
+
+void ref_step_find_update(int nt, double *update) {
+  g_broyden->find_update(*g_swimmers, nt);
+  std::memcpy(update, g_broyden->update.data.data(), 8 * g_broyden->update.data.size());
+}
+
+// swimmer.update(broyden.update) then forces_and_torques (the loop body).
+void ref_step_apply_update(int nt) {
+  swimmer &s = (*g_swimmers)[0];
+  s.update(&g_broyden->update.data[0]);
+  s.forces_and_torques(nt, 0);
+}
+
+void ref_step_end_of_iter(int nt, int error_is_too_large) {
+  g_broyden->end_of_iter(*g_swimmers, nt, 0, error_is_too_large != 0);
+}
+
+// One whole time step (the loop of cilia_sim_main.cu:355-527); returns the
+// Broyden iteration count (-1 if Broyden diverged), total GMRES iterations in
+// *gmres_iters.
+int ref_step_run(int nt, int *gmres_iters) {
+  swimmer &s = (*g_swimmers)[0];
+  s.initial_guess(nt);
+  s.forces_and_torques(nt, 0);
+  int it = 0, total = 0;
+  g_solver->compute_velocities(*g_swimmers, it, nt);
+  total += it;
+  bool big = g_solver->compute_errors(g_broyden->error, *g_swimmers, nt);
+  if (big) s.prepare_jacobian_inv(nt);
+  g_broyden->iter = 0;
+  while (big && g_broyden->iter < MAX_BROYDEN_ITER) {
+    g_broyden->find_update(*g_swimmers, nt);
+    s.update(&g_broyden->update.data[0]);
+    s.forces_and_torques(nt, 0);
+    g_solver->compute_velocities(*g_swimmers, it, nt);
+    total += it;
+    big = g_solver->compute_errors(g_broyden->new_error, *g_swimmers, nt);
+    if (!g_broyden->new_error.is_finite()) return -1;
+    g_broyden->end_of_iter(*g_swimmers, nt, 0, big);
+  }
+  s.end_of_step(nt);
+  if (gmres_iters) *gmres_iters = total;
+  return g_broyden->iter;
+}
+
+// State: segment positions x[3 Ns], quaternions q[4 Ns] (scalar first),
+// Lie algebra u[3 Ns]; per filament lambda[3 (NSEG-1)], tether[3], clamp[3];
+// body x[3], q[4], u[3].
+void ref_step_state(double *x, double *q, double *u, double *lambda, double *tether,
+                    double *clamp, double *body_x, double *body_q, double *body_u) {
+  swimmer &s = (*g_swimmers)[0];
+  for (int i = 0; i < NFIL; ++i) {
+    filament &fl = s.filaments[i];
+    for (int j = 0; j < NSEG; ++j) {
+      const segment &sg = fl.segments[j];
+      const int id = i * NSEG + j;
+      for (int k = 0; k < 3; ++k) { x[3 * id + k] = sg.x[k]; u[3 * id + k] = sg.u[k]; }
+      q[4 * id] = sg.q.scalar_part;
+      for (int k = 0; k < 3; ++k) q[4 * id + 1 + k] = sg.q.vector_part[k];
+    }
+    for (int k = 0; k < 3 * (NSEG - 1); ++k) lambda[3 * (NSEG - 1) * i + k] = fl.lambda[k];
+    for (int k = 0; k < 3; ++k) { tether[3 * i + k] = fl.tether_lambda[k]; clamp[3 * i + k] = fl.clamp_lambda[k]; }
+  }
+  for (int k = 0; k < 3; ++k) { body_x[k] = s.body.x[k]; body_u[k] = s.body.u[k]; }
+  body_q[0] = s.body.q.scalar_part;
+  for (int k = 0; k < 3; ++k) body_q[1 + k] = s.body.q.vector_part[k];
+}
 
 }  // extern "C"
