@@ -197,6 +197,77 @@ int tfs_num_tile_variants(int precision);
  * len); *needed (if non-NULL) gets the full size including the NUL. */
 int tfs_solver_tuning_report(tfs_solver *s, char *buf, size_t len, size_t *needed);
 
+/* --- implicit time step -------------------------------------------------- */
+/* The reference's time step for one free swimmer with elastic filaments
+ * (CILIA_TYPE 0: filaments tethered and clamped to the body, an end force
+ * along the distal tangent), driven through this solver's mobility solve:
+ * the loop body of src/cilia/cilia_sim_main.cu:355-527 -- initial guess
+ * (swimmer::initial_guess, swimmer.cpp:433-467), internal forces
+ * (filament::internal_forces_and_torques, filament.cpp:1467-1575;
+ * swimmer::forces_and_torques, swimmer.cpp:469-533), compute_velocities, the
+ * BDF residuals (mobility_solver::compute_errors, mobility_solver.cpp:2661-2946)
+ * and Broyden's method (broyden_solver.cpp:21-129) with the approximate
+ * inverse Jacobian (filament::invert_approx_jacobian, filament.cpp:1761-1894;
+ * swimmer::prepare_jacobian_inv and jacobian_inv_mult, swimmer.cpp:535-1070).
+ * Segments, filaments and the Broyden matrices live on the device; the
+ * body's 6 degrees of freedom and its 6x6 Schur complement on the host.
+ * The solver must have its blob references and body reference matrices set
+ * (tfs_make_body_reference_matrices) before the first step. */
+typedef struct tfs_stepper tfs_stepper; /* opaque */
+typedef struct tfs_step_config {
+  int nfil, nseg;              /* must match the solver's */
+  double seg_sep;              /* DL (SEG_SEP, config.hpp:259) */
+  double dt;                   /* DT */
+  double tol;                  /* TOL of Broyden's method (config.hpp:302) */
+  int max_broyden_iter;        /* MAX_BROYDEN_ITER (config.hpp:301) */
+  double kb, kt;               /* bending and twisting moduli KB, KT */
+  double end_force_magnitude;  /* END_FORCE_MAGNITUDE (the real value) */
+  double jacobian_confidence;  /* JACOBIAN_CONFIDENCE_FACTOR (config.hpp:299) */
+  double body_radius;          /* 0.5 AXIS_DIR_BODY_LENGTH of the spherical body */
+  int perturb_first_step;      /* CILIA_IC_TYPE 0 perturbation at step 0 (filament.cpp:520-528) */
+  double body_x[3];            /* initial body position */
+  double body_q[4];            /* initial body orientation (scalar first) */
+} tfs_step_config;
+/* Defaults: DL 2.2, DT 36.3833/300, TOL 1e-4, 400 iterations, KB = KT = 1800,
+ * END_FORCE_MAGNITUDE = 220 KB/(2.6 NSEG)^2, confidence 0.1, body radius 1,
+ * perturbation on, body at the origin with identity orientation. */
+int tfs_step_config_default(tfs_step_config *cfg, int nfil, int nseg);
+/* Straight filaments along fil_dirs[3 nfil] from the bases X + R fil_refs
+ * (fil_refs[3 nfil] in the body frame), at rest (filament::initial_setup,
+ * filament.cpp:219-346). Segment positions live in the solver's x_segs. */
+int tfs_stepper_create(tfs_solver *s, const tfs_step_config *cfg, const double *fil_refs,
+                       const double *fil_dirs, tfs_stepper **out);
+int tfs_stepper_destroy(tfs_stepper *st);
+/* One whole step nt (0-based): returns TFS_OK when Broyden's method met TOL,
+ * TFS_ENOTCONV when it stopped at max_broyden_iter (the state is advanced as
+ * the reference leaves it), TFS_ENAN if the residual went non-finite. */
+int tfs_stepper_step(tfs_stepper *st, int nt, int *broyden_iters, int *gmres_iters);
+/* The stages of a step, in the order tfs_stepper_step runs them. */
+int tfs_stepper_initial_guess(tfs_stepper *st, int nt);
+/* Internal forces into f_segs; swimmer_f[6] (may be NULL) gets swimmer::f. */
+int tfs_stepper_forces(tfs_stepper *st, int nt, double *swimmer_f);
+int tfs_stepper_compute_velocities(tfs_stepper *st, int nt, int *gmres_iters);
+/* Residuals into Broyden's error (which = 0) or new_error (which = 1);
+ * err (may be NULL) gets a copy, 6 (NFIL NSEG + 1) values. */
+int tfs_stepper_compute_errors(tfs_stepper *st, int nt, int which, double *err, int *too_large);
+/* schur_inv (may be NULL): the inverted 6x6 Schur complement, column-major. */
+int tfs_stepper_prepare_jacobian_inv(tfs_stepper *st, int nt, double *schur_inv);
+/* Filament fil's inverse approximate Jacobian, (6 NSEG)^2 column-major. */
+int tfs_stepper_inverse_jacobian(tfs_stepper *st, int fil, double *out);
+int tfs_stepper_jacobian_inv_mult(tfs_stepper *st, int nt, const double *in, double *out);
+int tfs_stepper_broyden_reset(tfs_stepper *st);
+/* update (may be NULL) gets broyden.update. */
+int tfs_stepper_find_update(tfs_stepper *st, int nt, double *update);
+/* swimmer::update with the last update, then the internal forces. */
+int tfs_stepper_apply_update(tfs_stepper *st, int nt);
+int tfs_stepper_end_of_iter(tfs_stepper *st, int nt, int too_large);
+/* The state (any pointer may be NULL): x[3 Ns], q[4 Ns], u[3 Ns] per
+ * segment; lambda[3 (NSEG-1) NFIL], tether[3 NFIL], clamp[3 NFIL]; the body's
+ * x[3], q[4], u[3]. */
+int tfs_stepper_state(tfs_stepper *st, double *x, double *q, double *u, double *lambda,
+                      double *tether, double *clamp, double *body_x, double *body_q,
+                      double *body_u);
+
 /* --- flow-field evaluator ---------------------------------------------- */
 /* Replaces the reference's flow_field_evaluator
  * (src/flow_field/flow_field_evaluator.hpp:8-61): the fluid velocity at

@@ -47,8 +47,19 @@ class DeviceBuffers(ctypes.Structure):
                                                 "f_blobs", "v_blobs", "f_blobs_repulsion")]
 
 
+class StepConfig(ctypes.Structure):
+    _fields_ = [("nfil", ctypes.c_int), ("nseg", ctypes.c_int), ("seg_sep", ctypes.c_double),
+                ("dt", ctypes.c_double), ("tol", ctypes.c_double),
+                ("max_broyden_iter", ctypes.c_int), ("kb", ctypes.c_double),
+                ("kt", ctypes.c_double), ("end_force_magnitude", ctypes.c_double),
+                ("jacobian_confidence", ctypes.c_double), ("body_radius", ctypes.c_double),
+                ("perturb_first_step", ctypes.c_int), ("body_x", ctypes.c_double * 3),
+                ("body_q", ctypes.c_double * 4)]
+
+
 _P = ctypes.c_void_p
 _H = ctypes.c_void_p  # opaque handle
+_IP = ctypes.POINTER(ctypes.c_int)
 
 # name -> argument types (all return int unless listed in _RESTYPES)
 _SIGNATURES = {
@@ -112,6 +123,22 @@ _SIGNATURES = {
     "tfs_flow_autotune": [_H, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
     "tfs_mss_noalloc": [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P],
+    "tfs_step_config_default": [ctypes.POINTER(StepConfig), ctypes.c_int, ctypes.c_int],
+    "tfs_stepper_create": [_H, ctypes.POINTER(StepConfig), _P, _P, ctypes.POINTER(_H)],
+    "tfs_stepper_destroy": [_H],
+    "tfs_stepper_step": [_H, ctypes.c_int, _IP, _IP],
+    "tfs_stepper_initial_guess": [_H, ctypes.c_int],
+    "tfs_stepper_forces": [_H, ctypes.c_int, _P],
+    "tfs_stepper_compute_velocities": [_H, ctypes.c_int, _IP],
+    "tfs_stepper_compute_errors": [_H, ctypes.c_int, ctypes.c_int, _P, _IP],
+    "tfs_stepper_prepare_jacobian_inv": [_H, ctypes.c_int, _P],
+    "tfs_stepper_inverse_jacobian": [_H, ctypes.c_int, _P],
+    "tfs_stepper_jacobian_inv_mult": [_H, ctypes.c_int, _P, _P],
+    "tfs_stepper_broyden_reset": [_H],
+    "tfs_stepper_find_update": [_H, ctypes.c_int, _P],
+    "tfs_stepper_apply_update": [_H, ctypes.c_int],
+    "tfs_stepper_end_of_iter": [_H, ctypes.c_int, ctypes.c_int],
+    "tfs_stepper_state": [_H, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "tfs_last_error": [],
     "tfs_kernel_launch_count": [],
     "tfs_measure_fma_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],
