@@ -6,7 +6,7 @@ compiled unchanged for the CPU by `make -C oracle ref` (see oracle/Makefile).
 That needs the reference tree, so this script runs only where it is present;
 the .npz files it writes are committed and travel with the tests.
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -19,9 +19,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-from oracle import ReferenceFlow, ReferenceKernels, ReferenceSolver  # noqa: E402
+from oracle import ReferenceFlow, ReferenceKernels, ReferenceSolver, ReferenceStep  # noqa: E402
 
-from timfilsimmod_gb300.geometry import make_config  # noqa: E402
+from timfilsimmod_gb300.geometry import fibonacci_sphere, make_config  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 END_FORCE = 100      # integer device copy of END_FORCE_MAGNITUDE (globals.hpp:14)
@@ -165,9 +165,97 @@ def case_solve():
     return res
 
 
+def step_setup(nfil=None):
+    """The small swimmer's body (R = 20, 642 blobs) with 32 straight
+    filaments of 20 segments along the surface normals, bases one blob radius
+    plus half a segment gap above the surface; END_FORCE_MAGNITUDE with the
+    default DL = 2.6."""
+    sw = make_config("small", seed=1)
+    nfil = nfil or sw.nfil
+    normals = fibonacci_sphere(nfil)
+    fil_refs = (sw.radius + 1.0 + 0.5 * 2.2) * normals
+    efm = 220.0 * 1800.0 / (2.6 * 2.6 * sw.nseg ** 2)
+    return sw, nfil, normals, fil_refs, efm
+
+
+def case_step():
+    """The reference's implicit time step (DT = 1e-3, Broyden TOL 1e-4,
+    LINEAR_SYSTEM_TOL 1e-10) on the small swimmer with elastic filaments:
+    step 0 stage by stage (internal forces, velocities, residuals, Schur
+    complement, inverse approximate Jacobians, a jacobian_inv_mult probe, the
+    first Broyden iteration), then the whole of steps 0-9 with the state
+    after each."""
+    sw, nfil, normals, fil_refs, efm = step_setup()
+    nseg = sw.nseg
+    ref = ReferenceStep(nfil, nseg, sw.blob_references, fil_refs, normals, efm, seg_sep=2.2,
+                        body_length=2.0 * sw.radius)
+    res = dict(blob_refs=sw.blob_references, fil_refs=fil_refs, fil_dirs=normals, nfil=nfil,
+               nseg=nseg, end_force_magnitude_real=efm, body_radius=sw.radius, dt=1e-3,
+               tol=1e-4, linear_tol=ref.lib.ref_linear_system_tol())
+    bm, ktk = ref.make_body_reference_matrices()
+    res.update(body_mobility=bm, ktkinv=ktk)
+    nt = 0
+    ref.initial_guess(nt)
+    res["s0_guess"] = ref.state()["x"]
+    fs, sf = ref.forces(nt)
+    res.update(s0_f_segs=fs, s0_swimmer_f=sf)
+    it, vs, vb, fb = ref.compute_velocities(nt)
+    res.update(s0_v_segs=vs, s0_v_bodies=vb, s0_f_blobs=fb, s0_gmres=it)
+    big, err = ref.compute_errors(nt, 0)
+    res.update(s0_error=err, s0_big=int(big))
+    res["s0_schur_inv"] = ref.prepare_jacobian_inv(nt)
+    res["s0_jinv_first"] = ref.inverse_jacobian(0)
+    res["s0_jinv_last_rows"] = ref.inverse_jacobian(nfil - 1)[:12]
+    probe = np.random.default_rng(5).normal(size=ref.nbroy)
+    res.update(s0_probe=probe, s0_probe_out=ref.jacobian_inv_mult(nt, probe))
+    ref.broyden_reset()
+    iters, gm = 0, it
+    while big:
+        upd = ref.find_update(nt)
+        if iters < 1:
+            res[f"s0_update{iters}"] = upd
+        ref.apply_update(nt)
+        it, vs, vb, fb = ref.compute_velocities(nt)
+        gm += it
+        big, nerr = ref.compute_errors(nt, 1)
+        if iters < 1:
+            res[f"s0_new_error{iters}"] = nerr
+            res[f"s0_state{iters}_x"] = ref.state()["x"]
+        ref.end_of_iter(nt, big)
+        iters += 1
+    st = ref.state()
+    traj = {k: [v] for k, v in st.items()}
+    broy, gmres = [iters], [gm]
+    for nt in range(1, 10):
+        b, g = ref.run(nt)
+        broy.append(b)
+        gmres.append(g)
+        for k, v in ref.state().items():
+            traj[k].append(v)
+    for k, v in traj.items():
+        if k in ("q", "u", "lam"):
+            res[f"final_{k}"] = v[-1]
+        elif k == "x":
+            res["traj_x_first"], res["traj_x_last"] = v[0], v[-1]
+        else:
+            res[f"traj_{k}"] = np.array(v)
+    res.update(broyden_iters=np.array(broy), gmres_iters=np.array(gmres))
+    return res
+
+
+CASES = {"small_matvec": case_small, "overlap_a16": case_overlap, "tiny": case_tiny,
+         "flow_small": case_flow, "solve_small": case_solve, "step_small": case_step}
+
+
 def main():
-    for name, fn in (("small_matvec", case_small), ("overlap_a16", case_overlap),
-                     ("tiny", case_tiny), ("flow_small", case_flow), ("solve_small", case_solve)):
+    # one case per process: the reference's solver library keeps global state
+    names = sys.argv[1:] or list(CASES)
+    if len(names) > 1:
+        import subprocess
+        for name in names:
+            subprocess.run([sys.executable, os.path.abspath(__file__), name], check=True)
+        return
+    for name, fn in ((n, CASES[n]) for n in names):
         data = fn()
         path = os.path.join(OUT, f"{name}.npz")
         np.savez_compressed(path, **{k: np.asarray(v) for k, v in data.items()})

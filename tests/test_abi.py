@@ -65,3 +65,21 @@ def test_last_error_and_argument_checks_without_gpu():
     assert lib.tfs_solver_create(ctypes.byref(bad), ctypes.byref(h)) == N.TFS_EINVAL
     assert lib.tfs_evaluate_segment_segment_mobility(None) == N.TFS_EINVAL
     assert lib.tfs_wait_for_device(None) == N.TFS_EINVAL
+
+
+def test_stepper_argument_checks_without_gpu():
+    """The implicit-step entry points validate handles before any CUDA call."""
+    from timfilsimmod_gb300 import _native as N
+
+    if not os.path.exists(N.lib_path()):
+        pytest.skip("libtfs_gb300.so not built")
+    lib = N.load()
+    cfg = N.StepConfig()
+    assert lib.tfs_step_config_default(ctypes.byref(cfg), 32, 20) == N.TFS_OK
+    assert cfg.tol == 1e-4 and cfg.max_broyden_iter == 400 and cfg.body_q[0] == 1.0
+    assert abs(cfg.end_force_magnitude - 220.0 * 1800.0 / (2.6 * 2.6 * 400)) < 1e-12
+    h = ctypes.c_void_p()
+    assert lib.tfs_stepper_create(None, ctypes.byref(cfg), None, None, ctypes.byref(h)) == N.TFS_EINVAL
+    assert b"null" in lib.tfs_last_error()
+    assert lib.tfs_stepper_step(None, 0, None, None) == N.TFS_EINVAL
+    assert lib.tfs_stepper_destroy(None) == N.TFS_OK

@@ -242,14 +242,15 @@ __global__ void k_forces(StepDev d, int nt, double bx0, double bx1, double bx2,
 }
 
 // BDF residuals (mobility_solver.cpp:2661-2946), one thread per segment; the
-// body's six entries by thread 0. Sets *flag if any entry exceeds the
-// tolerance (TOL DL for positions, TOL for Lie-algebra elements).
+// body's six entries by thread 0. Sets bit 0 of *flag if any entry exceeds
+// the tolerance (TOL DL for positions, TOL for Lie-algebra elements) and
+// bit 1 if any entry is not finite.
 __global__ void k_errors(StepDev d, BodyArgs b, int nt, double tol, const double *__restrict__ v_segs,
                          const double *__restrict__ v_bodies, double *__restrict__ err,
                          int *__restrict__ flag) {
   const double c1 = -4.0 / 3.0, c2 = 1.0 / 3.0, c3 = -2.0 / 3.0;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  bool big = false;
+  bool big = false, bad = false;
   if (s < d.ns) {
     const int fil = s / d.nseg, j = s - fil * d.nseg;
     const double *v = v_segs + 6 * (size_t)s, *w = v + 3;
@@ -260,6 +261,7 @@ __global__ void k_errors(StepDev d, BodyArgs b, int nt, double tol, const double
                               : x[k] + c1 * xm1[k] + c2 * xm2[k] + c3 * d.dt * v[k];
       err[id + k] = e;
       big |= fabs(e) > d.dl * tol;
+      bad |= !isfinite(e);
     }
     double W[3];
     const double *u = d.u + 3 * s, *um1 = d.um1 + 3 * s;
@@ -268,6 +270,7 @@ __global__ void k_errors(StepDev d, BodyArgs b, int nt, double tol, const double
       const double e = nt < 1 ? u[k] - d.dt * W[k] : u[k] - c2 * um1[k] + c3 * d.dt * W[k];
       err[id + 3 * d.nseg + k] = e;
       big |= fabs(e) > tol;
+      bad |= !isfinite(e);
     }
   }
   if (s == 0) {
@@ -282,9 +285,11 @@ __global__ void k_errors(StepDev d, BodyArgs b, int nt, double tol, const double
       err[id + 3 + k] = eu;
       big |= fabs(ex) > tol * d.dl;
       big |= fabs(eu) > tol;
+      bad |= !isfinite(ex) || !isfinite(eu);
     }
   }
-  if (__any_sync(0xffffffffu, big) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+  const int bits = (__any_sync(0xffffffffu, big) ? 1 : 0) | (__any_sync(0xffffffffu, bad) ? 2 : 0);
+  if (bits && (threadIdx.x & 31) == 0) atomicOr(flag, bits);
 }
 
 // ---------------------------------------------------------------------------
