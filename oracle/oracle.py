@@ -344,6 +344,7 @@ class ReferenceStep:
         if not os.path.exists(path):
             raise FileNotFoundError(path)
         self.lib = ctypes.CDLL(path)
+        self.lib.ref_linear_system_tol.restype = ctypes.c_double
         self.nfil, self.nseg = nfil, nseg
         self.refs = _c(blob_refs)
         self.nblob = self.refs.size // 3
