@@ -18,6 +18,9 @@ inputs/outputs). Printed: one JSON line (rank 0).
 
   solve    compute_velocities (the free-body GMRES solve of one Broyden
            iteration) at a 1e-8 linear residual, FP64 vs FP32C refinement
+  implicit_steps  whole implicit time steps (forces, solve, residuals,
+           Broyden) at a 1e-8 linear residual, FP64 vs FP32C, steps/s with
+           p50/p99 per-step latency
   flow     the flow-field evaluator on a 128^3 grid around the large swimmer
            (80 000 segments, 10 242 blobs), FP32C, with an FP64 subset
 
@@ -244,6 +247,8 @@ def bench_ours(args):
     v64 = np.concatenate([s64.v_segs_host, s64.v_blobs_host]).copy()
     # --- the mobility solve of one Broyden iteration (compute_velocities) -----
     solve = None if args.no_solve else solve_bench(sw, stream, args, RpyMobilitySolver)
+    # --- implicit time steps (initial guess, forces, solve, Broyden) -----------
+    steps = None if args.no_steps else step_bench(sw, stream, args)
     # --- the flow-field evaluator on a 128^3 grid around the large swimmer -----
     flow = None if args.no_flow else flow_bench(stream, flush, args, peak32, peak64, rank)
     clocks = sampler.stop()
@@ -313,6 +318,8 @@ def bench_ours(args):
             result["cpu_baseline"] = cpu
         if solve is not None:
             result["solve"] = solve
+        if steps is not None:
+            result["implicit_steps"] = steps
         if flow is not None:
             result["flow"] = flow
     for sv in (s32, s64):
@@ -400,6 +407,78 @@ def solve_bench(sw, stream, args, RpyMobilitySolver):
                         "linear residual 1e-8", **out,
             "speedup_fp32c_vs_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
             "fp32c_rel_l2_error_v_segs_vs_fp64": err}
+
+
+def step_bench(sw, stream, args):
+    """Implicit time steps of the swimmer with elastic filaments (the
+    reference's cilia_sim_main.cu:355-527 loop: initial guess, internal
+    forces, compute_velocities, BDF residuals, Broyden's method with the
+    approximate inverse Jacobian), everything on the device, FP64 vs FP32C at
+    a 1e-8 relative linear residual, DT = 1e-3, Broyden TOL 1e-4. The
+    filaments start straight along the surface normals; step 0 (where
+    Broyden iterates from the straight start) is reported apart, then
+    `warmup` steps run untimed and the timed steps follow. Each step is
+    bracketed by CUDA events on the solver's stream (host gaps inside the
+    step included), giving per-step latency percentiles. The FP32C segment
+    positions are compared with the FP64 trajectory after every step."""
+    import torch
+
+    from timfilsimmod_gb300.geometry import fibonacci_sphere
+    from timfilsimmod_gb300.mobility import RpyMobilitySolver, kernel_launch_count
+    from timfilsimmod_gb300.stepper import ImplicitStepper
+
+    nfil, nseg, nb = sw.nfil, sw.nseg, sw.num_blobs
+    normals = fibonacci_sphere(nfil)
+    fil_refs = (sw.radius + 1.0 + 0.5 * sw.seg_sep) * normals
+    efm = 220.0 * 1800.0 / (2.6 * 2.6 * nseg * nseg)
+    timed = max(3, min(args.steps, 20))
+    warm = max(3, args.warmup)
+    out, traj = {}, {}
+    for precision in ("fp64", "fp32c"):
+        s = RpyMobilitySolver(1, nfil, nseg, nb, precision=precision,
+                              end_force_magnitude=int(efm))
+        s.set_stream(stream.cuda_stream)
+        s.set_blob_references(sw.blob_references)
+        s.set_linear_solver(1e-8)
+        st = ImplicitStepper(s, nfil, nseg, fil_refs, normals, seg_sep=sw.seg_sep, dt=1e-3,
+                             tol=1e-4, end_force_magnitude=efm, body_radius=sw.radius)
+        lat, broy, gm, xs = [], [], [], []
+        launches = 0
+        for nt in range(1 + warm + timed):
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0 = kernel_launch_count()
+            a.record(stream)
+            bi, gi = st.step(nt, allow_unconverged=True)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if nt > warm:
+                launches += kernel_launch_count() - l0
+            lat.append(a.elapsed_time(b))
+            broy.append(bi)
+            gm.append(gi)
+            xs.append(st.state()["x"])
+        traj[precision] = xs
+        tl = np.array(lat[1 + warm:])
+        out[precision] = {
+            "value": timed / (tl.sum() * 1e-3), "unit": "implicit steps/s",
+            "ms_per_step": float(tl.mean()), "p50_ms": float(np.percentile(tl, 50)),
+            "p99_ms": float(np.percentile(tl, 99)), "timed_steps": timed,
+            "broyden_iters_timed": int(sum(broy[1 + warm:])),
+            "gmres_iters_per_step": float(np.mean(gm[1 + warm:])),
+            "step0": {"ms": lat[0], "broyden_iters": broy[0], "gmres_iters": gm[0]},
+            "gpu_launches_per_step": launches / timed,
+        }
+        st.close()
+        s.finalise()
+    x64, x32 = np.array(traj["fp64"]), np.array(traj["fp32c"])
+    scale = np.max(np.abs(x64), axis=1)
+    dev = np.max(np.abs(x32 - x64), axis=1) / scale
+    return {"workload": f"{nfil} filaments x {nseg} segments, {nb} blobs; dt 1e-3, "
+                        "Broyden TOL 1e-4, linear residual 1e-8",
+            **out, "speedup_fp32c_vs_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
+            "fp32c_max_rel_position_dev_vs_fp64": float(dev.max()),
+            "fp32c_rel_position_dev_vs_fp64_last": float(dev[-1])}
 
 
 FLOW_SEG, FLOW_BLOB, FLOW_POINT = 44, 28, 3  # canonical flops per source, per point
@@ -606,6 +685,7 @@ def main():
     p.add_argument("--no-tune", action="store_true", help="skip the launch autotuner")
     p.add_argument("--no-solve", action="store_true", help="skip the solve timing")
     p.add_argument("--no-flow", action="store_true", help="skip the flow-field timing")
+    p.add_argument("--no-steps", action="store_true", help="skip the implicit-step timing")
     p.add_argument("--flow-grid", type=int, default=128, help="flow points per grid axis")
     args = p.parse_args()
     if args.warmup < 3 and args.impl == "ours":
