@@ -3,7 +3,9 @@
     python -m timfilsimmod_gb300.profile_case --config medium --precision fp32c --reps 2
 
 Each repetition is one tfs_apply_grand_mobility call (pack, tile and reduce
-kernels). Meant to be run under `ncu -k regex:rpy_tile_kernel -c N`.
+kernels), or with --op the named block, solve, flow evaluation or implicit
+time step. Meant to be run under `ncu -k regex:rpy_tile_kernel -c N` (or
+`ncu --metrics gpu__time_duration.sum` for a launch list).
 """
 from __future__ import annotations
 
@@ -37,12 +39,39 @@ def run_flow(sw, args):
     ev.close()
 
 
+def run_steps(sw, args):
+    """Implicit time steps 0 .. reps-1 of the swimmer with straight elastic
+    filaments (DT 1e-3, Broyden TOL 1e-4, linear residual 1e-8); step 0
+    iterates Broyden's method from the straight start."""
+    from .geometry import fibonacci_sphere
+    from .stepper import ImplicitStepper
+
+    normals = fibonacci_sphere(sw.nfil)
+    fil_refs = (sw.radius + 1.0 + 0.5 * sw.seg_sep) * normals
+    efm = 220.0 * 1800.0 / (2.6 * 2.6 * sw.nseg * sw.nseg)
+    s = RpyMobilitySolver(1, sw.nfil, sw.nseg, sw.num_blobs, precision=args.precision,
+                          end_force_magnitude=int(efm))
+    s.set_blob_references(sw.blob_references)
+    s.set_linear_solver(1e-8)
+    st = ImplicitStepper(s, sw.nfil, sw.nseg, fil_refs, normals, seg_sep=sw.seg_sep, dt=1e-3,
+                         tol=1e-4, end_force_magnitude=efm, body_radius=sw.radius)
+    t0 = time.perf_counter()
+    for nt in range(args.reps):
+        b, g = st.step(nt, allow_unconverged=True)
+        print(f"step {nt}: {b} Broyden iterations, {g} GMRES iterations")
+    s.wait_for_device()
+    dt = time.perf_counter() - t0
+    print(f"{args.reps} steps ({args.precision}, {args.config}): {dt * 1e3:.2f} ms")
+    st.close()
+    s.finalise()
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--config", default="medium")
     p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     p.add_argument("--reps", type=int, default=2)
-    p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier", "solve", "flow"])
+    p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier", "solve", "flow", "step"])
     p.add_argument("--flow-grid", type=int, default=64, help="flow points per axis (op flow)")
     p.add_argument("--variant", type=int, default=None,
                    help="pin every combination to this tile-kernel variant")
@@ -52,6 +81,8 @@ def main():
     sw = make_config(args.config, seed=1)
     if args.op == "flow":
         return run_flow(sw, args)
+    if args.op == "step":
+        return run_steps(sw, args)
     s = RpyMobilitySolver(1, sw.nfil, sw.nseg, sw.num_blobs, precision=args.precision)
     s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
     if args.autotune:
