@@ -67,22 +67,8 @@ struct BodyArgs {
 };
 
 // ---------------------------------------------------------------------------
-// per-filament helpers (one thread)
+// segment and filament mechanics
 // ---------------------------------------------------------------------------
-
-__device__ void robot_arm(const StepDev &d, int fil) {
-  const int s0 = fil * d.nseg;
-  double t1[3], t2[3];
-  tangent(load_q(d.q + 4 * s0), t1);
-  for (int j = 1; j < d.nseg; ++j) {
-    const int s = s0 + j;
-    tangent(load_q(d.q + 4 * s), t2);
-    for (int k = 0; k < 3; ++k) {
-      d.x[3 * s + k] = d.x[3 * (s - 1) + k] + 0.5 * d.dl * (t1[k] + t2[k]);
-      t1[k] = t2[k];
-    }
-  }
-}
 
 // segment::update: u += du, q = exp(u) qm1
 __device__ void seg_update(const StepDev &d, int s, const double *du) {
@@ -91,21 +77,6 @@ __device__ void seg_update(const StepDev &d, int s, const double *du) {
   u[1] += du[1];
   u[2] += du[2];
   store_q(d.q + 4 * s, qmul(lie_exp(u), load_q(d.qm1 + 4 * s)));
-}
-
-// filament::accept_state_from_rigid_body (filament.cpp:649-661)
-__device__ void accept_base(const StepDev &d, const BodyArgs &b, int fil) {
-  const int s0 = fil * d.nseg;
-  const double *ref = d.fil_refs + 3 * fil;
-  for (int i = 0; i < 3; ++i) {
-    double s = 0.0;
-    for (int k = 0; k < 3; ++k) s += b.R[3 * i + k] * ref[k];
-    d.x[3 * s0 + i] = b.x[i] + s;
-  }
-  const double *u0 = d.u + 3 * s0;
-  const double du[3] = {b.u[0] - u0[0], b.u[1] - u0[1], b.u[2] - u0[2]};
-  seg_update(d, s0, du);
-  robot_arm(d, fil);
 }
 
 // BDF2 extrapolation of a multiplier from its last values (filament::initial_guess)
@@ -130,106 +101,170 @@ __device__ void extrapolate(double *v, double *m1, double *m2, int n, int nt) {
 // kernels
 // ---------------------------------------------------------------------------
 
-// swimmer::initial_guess per filament: segments (segment.cpp:48-76), the
-// base from the body, robot arm, multiplier extrapolation.
-__global__ void k_initial_guess(StepDev d, BodyArgs b, int nt) {
+// The base segment at X + R ref and the robot arm
+// x_j = x_{j-1} + DL/2 (t_{j-1} + t_j) (accept_state_from_rigid_body and
+// robot_arm, filament.cpp:625-661), one thread per filament. In
+// swimmer::update the reference runs the robot arm twice (after the base
+// segment's update and after the whole filament's); the first result is
+// overwritten by the second, which depends only on x_0 and the final
+// orientations, so it runs once here, after every segment is updated.
+__global__ void k_robot_arm(StepDev d, BodyArgs b) {
   const int fil = blockIdx.x * blockDim.x + threadIdx.x;
   if (fil >= d.nfil) return;
-  for (int j = 0; j < d.nseg; ++j) {
-    const int s = fil * d.nseg + j;
-    for (int k = 0; k < 3; ++k) {
-      d.xm2[3 * s + k] = d.xm1[3 * s + k];
-      d.xm1[3 * s + k] = d.x[3 * s + k];
-    }
-    double *u = d.u + 3 * s, *um1 = d.um1 + 3 * s;
-    for (int k = 0; k < 3; ++k) {
-      if (nt <= 1) {
-        um1[k] = u[k];
-      } else {
-        const double t = 2.0 * u[k] - um1[k];
-        um1[k] = u[k];
-        u[k] = t;
-      }
-    }
-    const Quat q = load_q(d.q + 4 * s);
-    store_q(d.qm1 + 4 * s, q);
-    store_q(d.q + 4 * s, qmul(lie_exp(u), q));
+  const int s0 = fil * d.nseg;
+  const double *ref = d.fil_refs + 3 * fil;
+  double xp[3];
+  for (int i = 0; i < 3; ++i) {
+    double s = 0.0;
+    for (int k = 0; k < 3; ++k) s += b.R[3 * i + k] * ref[k];
+    xp[i] = b.x[i] + s;
+    d.x[3 * s0 + i] = xp[i];
   }
-  accept_base(d, b, fil);
-  const int nl = 3 * (d.nseg - 1);
-  extrapolate(d.lam + (size_t)nl * fil, d.lamm1 + (size_t)nl * fil, d.lamm2 + (size_t)nl * fil, nl,
-              nt);
-  extrapolate(d.teth + 3 * fil, d.tethm1 + 3 * fil, d.tethm2 + 3 * fil, 3, nt);
-  extrapolate(d.clamp + 3 * fil, d.clampm1 + 3 * fil, d.clampm2 + 3 * fil, 3, nt);
+  double t1[3], t2[3];
+  tangent(load_q(d.q + 4 * s0), t1);
+  for (int j = 1; j < d.nseg; ++j) {
+    const int s = s0 + j;
+    tangent(load_q(d.q + 4 * s), t2);
+    for (int k = 0; k < 3; ++k) {
+      xp[k] = xp[k] + 0.5 * d.dl * (t1[k] + t2[k]);
+      d.x[3 * s + k] = xp[k];
+      t1[k] = t2[k];
+    }
+  }
 }
 
-// swimmer::update per filament: base from the updated body, then the
-// filament's multipliers and segment Lie-algebra elements, robot arm.
-__global__ void k_apply_update(StepDev d, BodyArgs b, const double *__restrict__ upd) {
-  const int fil = blockIdx.x * blockDim.x + threadIdx.x;
-  if (fil >= d.nfil) return;
-  accept_base(d, b, fil);
-  const int n = d.nseg;
+// swimmer::initial_guess, one thread per segment: segment::initial_guess
+// (segment.cpp:38-76); for the base segment then the body's Lie algebra
+// element (accept_state_from_rigid_body); multiplier extrapolation
+// (filament.cpp:1275-1385): link j-1 by segment j, tether and clamp by the
+// base segment. The robot arm follows (k_robot_arm).
+__global__ void k_guess_segments(StepDev d, BodyArgs b, int nt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.ns) return;
+  const int fil = s / d.nseg, j = s - fil * d.nseg;
+  for (int k = 0; k < 3; ++k) {
+    d.xm2[3 * s + k] = d.xm1[3 * s + k];
+    d.xm1[3 * s + k] = d.x[3 * s + k];
+  }
+  double *u = d.u + 3 * s, *um1 = d.um1 + 3 * s;
+  for (int k = 0; k < 3; ++k) {
+    if (nt <= 1) {
+      um1[k] = u[k];
+    } else {
+      const double t = 2.0 * u[k] - um1[k];
+      um1[k] = u[k];
+      u[k] = t;
+    }
+  }
+  const Quat q = load_q(d.q + 4 * s);
+  store_q(d.qm1 + 4 * s, q);
+  store_q(d.q + 4 * s, qmul(lie_exp(u), q));
+  if (j == 0) {
+    const double du[3] = {b.u[0] - u[0], b.u[1] - u[1], b.u[2] - u[2]};
+    seg_update(d, s, du);
+    extrapolate(d.teth + 3 * fil, d.tethm1 + 3 * fil, d.tethm2 + 3 * fil, 3, nt);
+    extrapolate(d.clamp + 3 * fil, d.clampm1 + 3 * fil, d.clampm2 + 3 * fil, 3, nt);
+  } else {
+    const size_t l = (size_t)3 * ((d.nseg - 1) * fil + j - 1);
+    extrapolate(d.lam + l, d.lamm1 + l, d.lamm2 + l, 3, nt);
+  }
+}
+
+// swimmer::update, one thread per segment: the base segment takes the
+// updated body's Lie algebra element (accept_state_from_rigid_body) and adds
+// the tether and clamp increments; segment j >= 1 adds its link's
+// inextensibility increment and its Lie algebra increment (filament::update,
+// filament.cpp:1896-1930). The robot arm follows (k_robot_arm).
+__global__ void k_update_segments(StepDev d, BodyArgs b, const double *__restrict__ upd) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.ns) return;
+  const int n = d.nseg, fil = s / n, j = s - fil * n;
   const double *uf = upd + (size_t)6 * n * fil;
-  for (int k = 0; k < 3; ++k) d.teth[3 * fil + k] += uf[k];
-  double *lam = d.lam + (size_t)3 * (n - 1) * fil;
-  for (int j = 1; j < n; ++j) {
-    for (int k = 0; k < 3; ++k) lam[3 * (j - 1) + k] += uf[3 * j + k];
-    seg_update(d, fil * n + j, uf + 3 * (n + j));
+  if (j == 0) {
+    const double *u0 = d.u + 3 * s;
+    const double du[3] = {b.u[0] - u0[0], b.u[1] - u0[1], b.u[2] - u0[2]};
+    seg_update(d, s, du);
+    for (int k = 0; k < 3; ++k) {
+      d.teth[3 * fil + k] += uf[k];
+      d.clamp[3 * fil + k] += uf[3 * n + k];
+    }
+  } else {
+    double *lam = d.lam + (size_t)3 * ((n - 1) * fil + j - 1);
+    for (int k = 0; k < 3; ++k) lam[k] += uf[3 * j + k];
+    seg_update(d, s, uf + 3 * (n + j));
   }
-  for (int k = 0; k < 3; ++k) d.clamp[3 * fil + k] += uf[3 * n + k];
-  robot_arm(d, fil);
 }
 
-// filament::internal_forces_and_torques (filament.cpp:1467-1575) into the
-// internal force array and the solver's f_segs, and this filament's part of
-// the swimmer force: -sum (f ; (x - X) x f + torque) (swimmer.cpp:469-529).
-__global__ void k_forces(StepDev d, int nt, double bx0, double bx1, double bx2,
-                         double *__restrict__ swf_part) {
-  const int fil = blockIdx.x * blockDim.x + threadIdx.x;
-  if (fil >= d.nfil) return;
-  const int n = d.nseg, s0 = fil * n;
-  double *f = d.f + (size_t)6 * s0;
-  for (int k = 0; k < 6 * n; ++k) f[k] = 0.0;
+// filament::internal_forces_and_torques (filament.cpp:1467-1575), one thread
+// per segment, accumulating in the reference's order: link j-1 (its
+// inextensibility force, the torque of that force about the segment, minus
+// the link's elastic moment), then link j (the same with the opposite
+// signs), then the tether force and clamping torque (base segment), the tip
+// follower force (last segment) and the step-0 perturbation (segment 4).
+// Written to the internal force array and to the solver's f_segs.
+__global__ void k_forces(StepDev d, int nt) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.ns) return;
+  const int n = d.nseg, fil = s / n, j = s - fil * n;
   const double *lamf = d.lam + (size_t)3 * (n - 1) * fil;
   const double strain[3] = {0.0, 0.0, 0.0};
+  const Quat qj = load_q(d.q + 4 * s);
   double t[3];
-  for (int i = 0; i < n - 1; ++i) {
-    const double *lam = lamf + 3 * i;
-    for (int k = 0; k < 3; ++k) {
-      f[6 * i + k] -= lam[k];
-      f[6 * (i + 1) + k] += lam[k];
-    }
-    const Quat qi = load_q(d.q + 4 * (s0 + i)), qj = load_q(d.q + 4 * (s0 + i + 1));
-    tangent(qi, t);
-    f[6 * i + 3] -= 0.5 * d.dl * (t[1] * lam[2] - t[2] * lam[1]);
-    f[6 * i + 4] -= 0.5 * d.dl * (t[2] * lam[0] - t[0] * lam[2]);
-    f[6 * i + 5] -= 0.5 * d.dl * (t[0] * lam[1] - t[1] * lam[0]);
-    tangent(qj, t);
-    f[6 * (i + 1) + 3] -= 0.5 * d.dl * (t[1] * lam[2] - t[2] * lam[1]);
-    f[6 * (i + 1) + 4] -= 0.5 * d.dl * (t[2] * lam[0] - t[0] * lam[2]);
-    f[6 * (i + 1) + 5] -= 0.5 * d.dl * (t[0] * lam[1] - t[1] * lam[0]);
+  tangent(qj, t);
+  double f[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (j > 0) {  // link j-1: this segment is its upper end
+    const double *lam = lamf + 3 * (j - 1);
+    for (int k = 0; k < 3; ++k) f[k] += lam[k];
+    f[3] -= 0.5 * d.dl * (t[1] * lam[2] - t[2] * lam[1]);
+    f[4] -= 0.5 * d.dl * (t[2] * lam[0] - t[0] * lam[2]);
+    f[5] -= 0.5 * d.dl * (t[0] * lam[1] - t[1] * lam[0]);
+    const Quat qi = load_q(d.q + 4 * (s - 1));
     double R[9], Mb[3], M[3];
     rot_mat(midpoint(qi, qj), R);
     link_moment(qi, qj, d.dl, d.kb, d.kt, strain, Mb);
     m3_vec(m3_from(R), Mb, M);
-    for (int k = 0; k < 3; ++k) {
-      f[6 * i + 3 + k] += M[k];
-      f[6 * (i + 1) + 3 + k] -= M[k];
-    }
+    for (int k = 0; k < 3; ++k) f[3 + k] -= M[k];
   }
-  for (int k = 0; k < 3; ++k) f[k] += d.teth[3 * fil + k];
-  tangent(load_q(d.q + 4 * (s0 + n - 1)), t);
-  for (int k = 0; k < 3; ++k) f[6 * (n - 1) + k] -= d.efm * t[k];
-  if (nt == 0 && d.perturb && 4 < n) f[6 * 4] += d.pert;  // filament.cpp:1540-1555
-  double ct[3];
-  dexpinv_s(ct, d.u + 3 * s0, d.clamp + 3 * fil, 1.0);
-  for (int k = 0; k < 3; ++k) f[3 + k] += ct[k];
+  if (j < n - 1) {  // link j: this segment is its lower end
+    const double *lam = lamf + 3 * j;
+    for (int k = 0; k < 3; ++k) f[k] -= lam[k];
+    f[3] -= 0.5 * d.dl * (t[1] * lam[2] - t[2] * lam[1]);
+    f[4] -= 0.5 * d.dl * (t[2] * lam[0] - t[0] * lam[2]);
+    f[5] -= 0.5 * d.dl * (t[0] * lam[1] - t[1] * lam[0]);
+    const Quat qk = load_q(d.q + 4 * (s + 1));
+    double R[9], Mb[3], M[3];
+    rot_mat(midpoint(qj, qk), R);
+    link_moment(qj, qk, d.dl, d.kb, d.kt, strain, Mb);
+    m3_vec(m3_from(R), Mb, M);
+    for (int k = 0; k < 3; ++k) f[3 + k] += M[k];
+  }
+  if (j == 0)
+    for (int k = 0; k < 3; ++k) f[k] += d.teth[3 * fil + k];
+  if (j == n - 1)
+    for (int k = 0; k < 3; ++k) f[k] -= d.efm * t[k];
+  if (nt == 0 && d.perturb && j == 4) f[0] += d.pert;  // filament.cpp:1540-1555
+  if (j == 0) {
+    double ct[3];
+    dexpinv_s(ct, d.u + 3 * s, d.clamp + 3 * fil, 1.0);
+    for (int k = 0; k < 3; ++k) f[3 + k] += ct[k];
+  }
+  for (int k = 0; k < 6; ++k) {
+    d.f[6 * (size_t)s + k] = f[k];
+    d.fs[6 * (size_t)s + k] = f[k];
+  }
+}
+
+// This filament's part of the swimmer force, -sum (f ; (x - X) x f + torque)
+// in segment order (swimmer.cpp:469-529), one thread per filament.
+__global__ void k_swimmer_force(StepDev d, double bx0, double bx1, double bx2,
+                                double *__restrict__ swf_part) {
+  const int fil = blockIdx.x * blockDim.x + threadIdx.x;
+  if (fil >= d.nfil) return;
+  const int n = d.nseg, s0 = fil * n;
   double sw[6] = {0, 0, 0, 0, 0, 0};
   for (int m = 0; m < n; ++m) {
-    const double *fm = f + 6 * m;
-    const double *xm = d.x + 3 * (s0 + m);
-    for (int k = 0; k < 6; ++k) d.fs[6 * (size_t)(s0 + m) + k] = fm[k];
+    const double *fm = d.f + 6 * (size_t)(s0 + m);
+    const double *xm = d.x + 3 * (size_t)(s0 + m);
     sw[0] -= fm[0];
     sw[1] -= fm[1];
     sw[2] -= fm[2];
@@ -524,7 +559,7 @@ __device__ M3 base_cross(const StepDev &d, const BodyArgs &b, int fil) {
 // invert it in place (Gauss-Jordan, partial pivoting), store the inverse,
 // the product JB = B J^-1 and this filament's share of the Schur complement
 // (JB A) and of the body's Lie-algebra self-dependence.
-__global__ void __launch_bounds__(512) k_jacobian(StepDev d, BodyArgs b, int nt) {
+__global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt) {
   extern __shared__ double sm[];
   const int n = d.nseg, n6 = 6 * n, fil = blockIdx.x, tid = threadIdx.x, nth = blockDim.x;
   double *J = sm;                          // n6 * n6
@@ -604,6 +639,8 @@ __global__ void __launch_bounds__(512) k_jacobian(StepDev d, BodyArgs b, int nt)
   __syncthreads();
   // Gauss-Jordan inversion in place
   const int warp = tid >> 5, lane = tid & 31;
+  const int ng = nth / n6 > 0 ? nth / n6 : 1;  // row groups
+  const int g = tid / n6, jcol = g < ng ? tid - g * n6 : n6;
   for (int k = 0; k < n6; ++k) {
     if (warp == 0) {
       double best = -1.0;
@@ -639,14 +676,17 @@ __global__ void __launch_bounds__(512) k_jacobian(StepDev d, BodyArgs b, int nt)
     __syncthreads();
     for (int j = tid; j < n6; j += nth) J[(size_t)k * n6 + j] = j == k ? 1.0 / piv : J[(size_t)k * n6 + j] / piv;
     __syncthreads();
-    for (int idx = tid; idx < n6 * n6; idx += nth) {
-      const int i = idx / n6, j = idx - i * n6;
-      if (i == k) continue;
-      const double ci = col[i];
-      if (j == k)
-        J[idx] = -ci * J[(size_t)k * n6 + k];
-      else
-        J[idx] -= ci * J[(size_t)k * n6 + j];
+    // thread (g, j) owns column j of rows g, g + ng, ...: the pivot row's
+    // entry stays in a register and col[i] is a broadcast read
+    if (jcol < n6) {
+      const double rk = J[(size_t)k * n6 + jcol];
+      if (jcol == k) {
+        for (int i = g; i < n6; i += ng)
+          if (i != k) J[(size_t)i * n6 + jcol] = -col[i] * rk;
+      } else {
+        for (int i = g; i < n6; i += ng)
+          if (i != k) J[(size_t)i * n6 + jcol] -= col[i] * rk;
+      }
     }
     __syncthreads();
   }
@@ -723,24 +763,36 @@ __global__ void k_jb_dot(StepDev d, const double *__restrict__ in, double *__res
   if (lane == 0) p6[6 * fil + r] = s;
 }
 
-// b2 and the body's part of the output (one warp; filaments summed in order)
-__global__ void k_body_solve(StepDev d, const double *__restrict__ in, const double *__restrict__ p6,
-                             const double *__restrict__ schur_inv, double *__restrict__ out,
-                             double *__restrict__ ob) {
+// b2 = in_body - sum_i JB_i in_i and the body's part of the output
+// S^-1 b2 (one CTA; the filament partials summed by a fixed tree)
+__global__ void __launch_bounds__(256) k_body_solve(StepDev d, const double *__restrict__ in,
+                                                    const double *__restrict__ p6,
+                                                    const double *__restrict__ schur_inv,
+                                                    double *__restrict__ out, double *__restrict__ ob) {
+  __shared__ double sh[8][6];
   __shared__ double b2[6];
-  const int r = threadIdx.x;
-  const size_t nb = (size_t)6 * d.ns;
-  if (r < 6) {
-    double v = in[nb + r];
-    for (int i = 0; i < d.nfil; ++i) v -= p6[6 * i + r];
-    b2[r] = v;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = tid; i < d.nfil; i += blockDim.x)
+    for (int r = 0; r < 6; ++r) acc[r] += p6[6 * i + r];
+  for (int r = 0; r < 6; ++r) {
+    double v = acc[r];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) sh[warp][r] = v;
   }
-  __syncwarp();
-  if (r < 6) {
+  __syncthreads();
+  const size_t nb = (size_t)6 * d.ns;
+  if (tid < 6) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w][tid];
+    b2[tid] = in[nb + tid] - t;
+  }
+  __syncthreads();
+  if (tid < 6) {
     double v = 0.0;
-    for (int c = 0; c < 6; ++c) v += schur_inv[6 * r + c] * b2[c];
-    out[nb + r] = v;
-    ob[r] = v;
+    for (int c = 0; c < 6; ++c) v += schur_inv[6 * tid + c] * b2[c];
+    out[nb + tid] = v;
+    ob[tid] = v;
   }
 }
 
@@ -784,6 +836,7 @@ __global__ void k_jinv_apply(StepDev d, BodyArgs b, const double *__restrict__ i
 
 constexpr int kRedThreads = 256;
 constexpr int kNormBlocks = 128;
+constexpr int kMaxDotChunks = 64;
 
 __device__ double block_sum(double v, double *sh) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -798,15 +851,27 @@ __device__ double block_sum(double v, double *sh) {
   return t;  // valid in thread 0
 }
 
-// coef[i] = a . D_i for i < ncols, one CTA per column
+// part[i * nchunk + c] = a . D_i over rows of chunk c (grid nchunk x ncols)
 __global__ void __launch_bounds__(kRedThreads) k_col_dots(const double *__restrict__ a,
                                                           const double *__restrict__ Dm, long nbroy,
-                                                          double *__restrict__ coef) {
+                                                          long rows_per_chunk,
+                                                          double *__restrict__ part) {
   __shared__ double sh[32];
-  const double *col = Dm + (size_t)blockIdx.x * nbroy;
+  const double *col = Dm + (size_t)blockIdx.y * nbroy;
+  const long r0 = blockIdx.x * rows_per_chunk;
+  const long r1 = r0 + rows_per_chunk < nbroy ? r0 + rows_per_chunk : nbroy;
   double s = 0.0;
-  for (long r = threadIdx.x; r < nbroy; r += blockDim.x) s += a[r] * col[r];
+  for (long r = r0 + threadIdx.x; r < r1; r += blockDim.x) s += a[r] * col[r];
   s = block_sum(s, sh);
+  if (threadIdx.x == 0) part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = s;
+}
+
+// coef[i] = sum over chunks of part[i * nchunk + c] (one warp per column)
+__global__ void k_col_dots_final(const double *__restrict__ part, int nchunk,
+                                 double *__restrict__ coef) {
+  double s = 0.0;
+  for (int c = threadIdx.x; c < nchunk; c += 32) s += part[(size_t)blockIdx.x * nchunk + c];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
   if (threadIdx.x == 0) coef[blockIdx.x] = s;
 }
 
@@ -869,7 +934,7 @@ struct tfs_stepper {
   double schur_inv[36];   // row-major
   double *schur_dev = nullptr;
   double *err = nullptr, *nerr = nullptr, *upd = nullptr, *tin = nullptr, *tout = nullptr;
-  double *Cm = nullptr, *Dm = nullptr, *coef = nullptr;
+  double *Cm = nullptr, *Dm = nullptr, *coef = nullptr, *dotpart = nullptr;
   double *p6 = nullptr, *ob = nullptr, *partial = nullptr, *swpart = nullptr;
   int *flag = nullptr;
   double *hbuf = nullptr;  // pinned: max(45, 6) nfil + 8
@@ -980,7 +1045,7 @@ int jinv_mult_dev(tfs_stepper *st, int nt, const double *in, double *out) {
   const BodyArgs b = body_args(st, nt);
   k_jb_dot<<<d.nfil, 192, 0, str>>>(d, in, st->p6);
   ST_LAUNCH("jacobian_inv_mult (JB in)");
-  k_body_solve<<<1, 32, 0, str>>>(d, in, st->p6, st->schur_dev, out, st->ob);
+  k_body_solve<<<1, 256, 0, str>>>(d, in, st->p6, st->schur_dev, out, st->ob);
   ST_LAUNCH("jacobian_inv_mult (body)");
   k_jinv_apply<<<d.nfil, 256, sizeof(double) * 6 * d.nseg, str>>>(d, b, in, st->ob, out);
   ST_LAUNCH("jacobian_inv_mult (filaments)");
@@ -991,8 +1056,14 @@ int jinv_mult_dev(tfs_stepper *st, int nt, const double *in, double *out) {
 int low_rank(tfs_stepper *st, const double *a, double *v, int ncols) {
   cudaStream_t str = st->s->stream;
   if (ncols > 0) {
-    k_col_dots<<<ncols, kRedThreads, 0, str>>>(a, st->Dm, st->nbroy, st->coef);
+    long nchunk = (st->nbroy + 4095) / 4096;
+    if (nchunk > kMaxDotChunks) nchunk = kMaxDotChunks;
+    const long rows = (st->nbroy + nchunk - 1) / nchunk;
+    k_col_dots<<<dim3((unsigned)nchunk, (unsigned)ncols), kRedThreads, 0, str>>>(a, st->Dm, st->nbroy,
+                                                                               rows, st->dotpart);
     ST_LAUNCH("Broyden column dots");
+    k_col_dots_final<<<ncols, 32, 0, str>>>(st->dotpart, (int)nchunk, st->coef);
+    ST_LAUNCH("Broyden column dots (sum)");
   }
   k_scale_sub_cols<<<grid_for(st->nbroy, 256), 256, 0, str>>>(v, st->Cm, st->coef, ncols,
                                                               st->cfg.jacobian_confidence, st->nbroy);
@@ -1029,7 +1100,7 @@ int tfs_stepper_destroy(tfs_stepper *st) {
   double *bufs[] = {d.q,     d.qm1,  d.u,       d.um1,    d.xm1,    d.xm2,     d.f,       d.lam,
                     d.lamm1, d.lamm2, d.teth,   d.tethm1, d.tethm2, d.clamp,   d.clampm1, d.clampm2,
                     d.jinv,  d.jb,   d.ecb,     d.part,   st->schur_dev, st->err, st->nerr, st->upd,
-                    st->tin, st->tout, st->Cm,  st->Dm,   st->coef, st->p6,    st->ob,    st->partial,
+                    st->tin, st->tout, st->Cm,  st->Dm,   st->coef, st->dotpart, st->p6,    st->ob,    st->partial,
                     st->swpart};
   for (double *p : bufs)
     if (p) cudaFree(p);
@@ -1105,7 +1176,8 @@ int tfs_stepper_create(tfs_solver *s, const tfs_step_config *cfg, const double *
                 {&st->schur_dev, 36},  {&st->err, (size_t)d.nbroy}, {&st->nerr, (size_t)d.nbroy},
                 {&st->upd, (size_t)d.nbroy}, {&st->tin, (size_t)d.nbroy}, {&st->tout, (size_t)d.nbroy},
                 {&st->Cm, (size_t)d.nbroy * mi}, {&st->Dm, (size_t)d.nbroy * mi},
-                {&st->coef, mi},       {&st->p6, 6 * nf},      {&st->ob, 8},
+                {&st->coef, mi},       {&st->dotpart, mi * kMaxDotChunks},
+                {&st->p6, 6 * nf},     {&st->ob, 8},
                 {&st->partial, kNormBlocks}, {&st->swpart, 6 * nf}};
   for (auto &a : allocs) {
     if (cudaMalloc(reinterpret_cast<void **>(a.p), sizeof(double) * a.n) != cudaSuccess) {
@@ -1221,8 +1293,10 @@ int tfs_stepper_initial_guess(tfs_stepper *st, int nt) {
   rot_rm(st->bq, st->Qinit);
   st->jac_ready = 0;
   const BodyArgs b = body_args(st, nt);
-  k_initial_guess<<<(st->d.nfil + 63) / 64, 64, 0, st->s->stream>>>(st->d, b, nt);
+  k_guess_segments<<<(st->d.ns + 127) / 128, 128, 0, st->s->stream>>>(st->d, b, nt);
   ST_LAUNCH("initial guess");
+  k_robot_arm<<<(st->d.nfil + 63) / 64, 64, 0, st->s->stream>>>(st->d, b);
+  ST_LAUNCH("robot arm");
   st->s->origin_dirty = true;
   return TFS_OK;
 }
@@ -1231,8 +1305,10 @@ int tfs_stepper_forces(tfs_stepper *st, int nt, double *swimmer_f) {
   TFS_CHECK_STEPPER(st);
   const StepDev &d = st->d;
   cudaStream_t str = st->s->stream;
-  k_forces<<<(d.nfil + 63) / 64, 64, 0, str>>>(d, nt, st->bx[0], st->bx[1], st->bx[2], st->swpart);
+  k_forces<<<(d.ns + 127) / 128, 128, 0, str>>>(d, nt);
   ST_LAUNCH("internal forces");
+  k_swimmer_force<<<(d.nfil + 63) / 64, 64, 0, str>>>(d, st->bx[0], st->bx[1], st->bx[2], st->swpart);
+  ST_LAUNCH("swimmer force");
   ST_CUDA(cudaMemcpyAsync(st->hbuf, st->swpart, sizeof(double) * 6 * d.nfil, cudaMemcpyDeviceToHost, str),
           "swimmer force");
   ST_CUDA(cudaStreamSynchronize(str), "internal forces");
@@ -1277,7 +1353,7 @@ int tfs_stepper_prepare_jacobian_inv(tfs_stepper *st, int nt, double *schur_inv)
   const StepDev &d = st->d;
   cudaStream_t str = st->s->stream;
   const BodyArgs b = body_args(st, nt);
-  k_jacobian<<<d.nfil, 512, st->jac_smem, str>>>(d, b, nt);
+  k_jacobian<<<d.nfil, 256, st->jac_smem, str>>>(d, b, nt);
   ST_LAUNCH("approximate Jacobian");
   ST_CUDA(cudaMemcpyAsync(st->hbuf, d.part, sizeof(double) * 45 * d.nfil, cudaMemcpyDeviceToHost, str),
           "Schur parts");
@@ -1378,8 +1454,10 @@ int tfs_stepper_apply_update(tfs_stepper *st, int nt) {
   }
   store_q(st->bq, qmul(lie_exp(st->bu), load_q(st->bqm1)));
   const BodyArgs b = body_args(st, nt);
-  k_apply_update<<<(st->d.nfil + 63) / 64, 64, 0, str>>>(st->d, b, st->upd);
+  k_update_segments<<<(st->d.ns + 127) / 128, 128, 0, str>>>(st->d, b, st->upd);
   ST_LAUNCH("apply update");
+  k_robot_arm<<<(st->d.nfil + 63) / 64, 64, 0, str>>>(st->d, b);
+  ST_LAUNCH("robot arm");
   st->s->origin_dirty = true;
   return tfs_stepper_forces(st, nt, nullptr);
 }
