@@ -261,12 +261,83 @@ int tfs_stepper_find_update(tfs_stepper *st, int nt, double *update);
 /* swimmer::update with the last update, then the internal forces. */
 int tfs_stepper_apply_update(tfs_stepper *st, int nt);
 int tfs_stepper_end_of_iter(tfs_stepper *st, int nt, int too_large);
+/* Back to the straight start of tfs_stepper_create (state, histories,
+ * Broyden memory, and the solver's warm start as it was at creation), with
+ * each segment first turned by exp(seg_rotation[3 j..3 j+2]) when
+ * seg_rotation (3 Ns values) is not NULL; positions then follow from the
+ * robot arm (filament.cpp:625-647). The next step is step 0. */
+int tfs_stepper_reset(tfs_stepper *st, const double *seg_rotation);
 /* The state (any pointer may be NULL): x[3 Ns], q[4 Ns], u[3 Ns] per
  * segment; lambda[3 (NSEG-1) NFIL], tether[3 NFIL], clamp[3 NFIL]; the body's
  * x[3], q[4], u[3]. */
 int tfs_stepper_state(tfs_stepper *st, double *x, double *q, double *u, double *lambda,
                       double *tether, double *clamp, double *body_x, double *body_q,
                       double *body_u);
+
+/* --- many swimmers: batches and a request server ---------------------- */
+/* No counterpart in the reference (one swimmer set per process). Each
+ * swimmer is an instance -- its own tfs_solver and tfs_stepper on its own
+ * stream -- and a pool of host worker threads runs the instances' step
+ * pipelines so that their kernels overlap on the GPU. Instances share
+ * nothing on the device: a swimmer's result is the same alone and in a
+ * batch. FP32C instances run the kernel-sequence inner GMRES (the
+ * cooperative form needs the whole GPU). */
+typedef struct tfs_batch tfs_batch;
+int tfs_batch_create(int num_workers, tfs_batch **out);
+int tfs_batch_destroy(tfs_batch *b);   /* does not destroy the instances */
+/* Adds a swimmer (its stepper; the solver comes with it). */
+int tfs_batch_add(tfs_batch *b, tfs_stepper *st, int *index);
+int tfs_batch_size(tfs_batch *b, int *n);
+/* Step nt of every swimmer. The per-swimmer arrays (any may be NULL) get
+ * Broyden and GMRES iterations and the step's status; the return value is
+ * TFS_OK or the first failing swimmer's status (the others still step). */
+int tfs_batch_step(tfs_batch *b, int nt, int *broyden_iters, int *gmres_iters, int *status);
+
+/* A request: num_steps implicit steps (0 .. num_steps-1) of a swimmer
+ * given by its geometry (blob references, filament bases and directions;
+ * all arrays must stay valid until the request completes) from the
+ * straight start, each segment turned by seg_rotation (3 Ns, may be NULL)
+ * as in tfs_stepper_reset. Results: x_out[3 Ns] segment positions and
+ * body_out[7] = body x, q (either may be NULL). */
+typedef struct tfs_request {
+  int nfil, nseg, nblob;
+  const double *blob_refs, *fil_refs, *fil_dirs;
+  double body_radius;         /* 0: the server's step setting */
+  const double *seg_rotation;
+  int num_steps;
+  double *x_out, *body_out;
+} tfs_request;
+typedef struct tfs_server_config {
+  int num_workers;            /* requests in flight at once */
+  size_t hbm_budget_bytes;    /* device memory for resident instances */
+  int precision;              /* TFS_FP64 or TFS_FP32C */
+  double linear_tol;          /* LINEAR_SYSTEM_TOL of every solve */
+  tfs_step_config step;       /* step settings (nfil, nseg come from each request) */
+} tfs_server_config;
+typedef struct tfs_server_counters {
+  long long resident_instances, created, reused, evicted, queued, inflight;
+  size_t bytes_in_use;
+} tfs_server_counters;
+typedef struct tfs_server tfs_server;
+/* Defaults: 8 workers, 160 GB, FP32C, linear tolerance 1e-8, the step
+ * defaults of tfs_step_config_default. */
+int tfs_server_config_default(tfs_server_config *cfg);
+int tfs_server_create(const tfs_server_config *cfg, tfs_server **out);
+/* Queues a request (arrival time = now); TFS_ENOMEM if its swimmer alone
+ * exceeds the budget. Instances stay resident between requests, keyed by
+ * geometry; a request is admitted, in arrival order, when an idle instance
+ * of its geometry exists or a new one fits in the budget after evicting
+ * idle instances (least recently used first). Memory is accounted from
+ * each instance's estimated size at admission. */
+int tfs_server_submit(tfs_server *sv, const tfs_request *r, long long *ticket);
+/* *status: 1 while pending, else the request's TFS status (the ticket is
+ * then released). wait != 0 blocks until it completes. latency_ms: arrival
+ * to completion. */
+int tfs_server_poll(tfs_server *sv, long long ticket, int wait, int *status, double *latency_ms,
+                    int *broyden_iters, int *gmres_iters);
+int tfs_server_drain(tfs_server *sv);   /* until every submitted request completed */
+int tfs_server_stats(tfs_server *sv, tfs_server_counters *out);
+int tfs_server_destroy(tfs_server *sv); /* drains first */
 
 /* --- flow-field evaluator ---------------------------------------------- */
 /* Replaces the reference's flow_field_evaluator

@@ -1,0 +1,141 @@
+"""Many swimmers on one GPU: a batch of uneven swimmers stepped together, and
+the request server (timfilsimmod_gb300.serving).
+
+Each instance owns its solver, stepper and stream and shares nothing on the
+device with the others, and every reduction is in a fixed order, so a
+swimmer's result is the same -- bit for bit -- alone and in the mix: that is
+the bar here (tolerance 0), in FP64 and FP32C. The parity of a single
+swimmer's step with the reference is covered by test_gpu_step.py.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# uneven swimmers: (sphere subdivisions -> blobs, filaments), 20 segments each
+SHAPES = [(2, 12), (3, 24), (2, 7)]
+DT, TOL = 1e-3, 1e-4
+
+
+def geometry(subdiv, nfil, radius=None):
+    from timfilsimmod_gb300.geometry import fibonacci_sphere, icosphere
+
+    radius = radius or (10.0 if subdiv == 2 else 20.0)
+    blob_refs = radius * icosphere(subdiv)
+    normals = fibonacci_sphere(nfil)
+    fil_refs = (radius + 1.0 + 1.1) * normals
+    return blob_refs, fil_refs, normals, radius
+
+
+def efm(nseg=20):
+    return 220.0 * 1800.0 / (2.6 * 2.6 * nseg * nseg)
+
+
+def make_instance(subdiv, nfil, precision):
+    from timfilsimmod_gb300.mobility import RpyMobilitySolver
+    from timfilsimmod_gb300.stepper import ImplicitStepper
+
+    blob_refs, fil_refs, normals, radius = geometry(subdiv, nfil)
+    s = RpyMobilitySolver(1, nfil, 20, blob_refs.shape[0], precision=precision,
+                          end_force_magnitude=int(efm()))
+    if precision == "fp32c":
+        s.set_persistent_gmres(False)  # as in a batch
+    s.set_blob_references(blob_refs)
+    s.set_linear_solver(1e-8, min(350, 3 * blob_refs.shape[0] + 6))
+    st = ImplicitStepper(s, nfil, 20, fil_refs, normals, seg_sep=2.2, dt=DT, tol=TOL,
+                         end_force_magnitude=efm(), body_radius=radius)
+    return s, st
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_batch_same_as_alone(precision):
+    from timfilsimmod_gb300.serving import SwimmerBatch
+
+    steps = 3
+    alone = []
+    for subdiv, nfil in SHAPES:
+        s, st = make_instance(subdiv, nfil, precision)
+        for nt in range(steps):
+            st.step(nt, allow_unconverged=True)
+        alone.append(st.state())
+        st.close()
+        s.finalise()
+    inst = [make_instance(subdiv, nfil, precision) for subdiv, nfil in SHAPES]
+    batch = SwimmerBatch(num_workers=3)
+    for _, st in inst:
+        batch.add(st)
+    for nt in range(steps):
+        out = batch.step(nt, allow_unconverged=True)
+        assert np.all(out["gmres_iters"] > 0)
+    for (s, st), ref in zip(inst, alone):
+        got = st.state()
+        for k in ("x", "q", "lam", "body_x", "body_q"):
+            assert np.array_equal(got[k], ref[k]), k
+    batch.close()
+    for s, st in inst:
+        st.close()
+        s.finalise()
+
+
+def requests(seed=3, repeat=2):
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(repeat):
+        for subdiv, nfil in SHAPES:
+            rot = 1e-6 * rng.normal(size=(nfil * 20, 3))
+            out.append((subdiv, nfil, rot))
+    return out
+
+
+def serve(reqs, workers, budget_gb=160.0, one_at_a_time=False, precision="fp32c"):
+    from timfilsimmod_gb300.serving import StepServer
+
+    sv = StepServer(num_workers=workers, hbm_budget_gb=budget_gb, precision=precision,
+                    linear_tol=1e-8, dt=DT, tol=TOL, seg_sep=2.2, end_force_magnitude=efm())
+    results, tickets = [], []
+    for subdiv, nfil, rot in reqs:
+        blob_refs, fil_refs, normals, radius = geometry(subdiv, nfil)
+        t = sv.submit(blob_refs, fil_refs, normals, 20, num_steps=2, seg_rotation=rot,
+                      body_radius=radius)
+        if one_at_a_time:
+            results.append(sv.poll(t, wait=True))
+        else:
+            tickets.append(t)
+    results += [sv.poll(t, wait=True) for t in tickets]
+    stats = sv.stats()
+    sv.close()
+    return results, stats
+
+
+def test_server_results_same_alone_and_in_mix():
+    reqs = requests()
+    alone, _ = serve(reqs, workers=1, one_at_a_time=True)
+    mix, stats = serve(reqs, workers=4)
+    for a, m in zip(alone, mix):
+        assert np.array_equal(a["x"], m["x"])
+        assert np.array_equal(a["body"], m["body"])
+        assert m["latency_ms"] > 0 and m["broyden_iters"] > 0
+    # repeated geometries reuse resident instances
+    assert stats["created"] <= len(SHAPES) + 3 and stats["reused"] >= 1
+    # the perturbation moved the result off the unperturbed one
+    assert not np.array_equal(mix[0]["x"], mix[len(SHAPES)]["x"])
+
+
+def test_server_budget_evicts_and_rejects():
+    from timfilsimmod_gb300 import _native as N
+    from timfilsimmod_gb300.serving import StepServer
+
+    reqs = requests(repeat=1)
+    full, _ = serve(reqs, workers=2)
+    # room for one instance at a time (the largest is ~31 MB by the server's
+    # estimate): admissions evict
+    tight, stats = serve(reqs, workers=2, budget_gb=0.035)
+    assert stats["evicted"] >= 1
+    for a, b in zip(full, tight):
+        assert np.array_equal(a["x"], b["x"])
+    sv = StepServer(num_workers=1, hbm_budget_gb=0.001)
+    blob_refs, fil_refs, normals, _ = geometry(3, 24)
+    with pytest.raises(N.TfsError) as e:
+        sv.submit(blob_refs, fil_refs, normals, 20)
+    assert e.value.code == N.TFS_ENOMEM
+    sv.close()

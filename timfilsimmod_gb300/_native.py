@@ -57,9 +57,31 @@ class StepConfig(ctypes.Structure):
                 ("body_q", ctypes.c_double * 4)]
 
 
+class Request(ctypes.Structure):
+    _fields_ = [("nfil", ctypes.c_int), ("nseg", ctypes.c_int), ("nblob", ctypes.c_int),
+                ("blob_refs", ctypes.c_void_p), ("fil_refs", ctypes.c_void_p),
+                ("fil_dirs", ctypes.c_void_p), ("body_radius", ctypes.c_double),
+                ("seg_rotation", ctypes.c_void_p),
+                ("num_steps", ctypes.c_int), ("x_out", ctypes.c_void_p),
+                ("body_out", ctypes.c_void_p)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("num_workers", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t),
+                ("precision", ctypes.c_int), ("linear_tol", ctypes.c_double),
+                ("step", StepConfig)]
+
+
+class ServerCounters(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_longlong) for n in ("resident_instances", "created", "reused",
+                                                  "evicted", "queued", "inflight")] + \
+               [("bytes_in_use", ctypes.c_size_t)]
+
+
 _P = ctypes.c_void_p
 _H = ctypes.c_void_p  # opaque handle
 _IP = ctypes.POINTER(ctypes.c_int)
+_LLP = ctypes.POINTER(ctypes.c_longlong)
 
 # name -> argument types (all return int unless listed in _RESTYPES)
 _SIGNATURES = {
@@ -139,6 +161,20 @@ _SIGNATURES = {
     "tfs_stepper_apply_update": [_H, ctypes.c_int],
     "tfs_stepper_end_of_iter": [_H, ctypes.c_int, ctypes.c_int],
     "tfs_stepper_state": [_H, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "tfs_stepper_reset": [_H, _P],
+    "tfs_batch_create": [ctypes.c_int, ctypes.POINTER(_H)],
+    "tfs_batch_destroy": [_H],
+    "tfs_batch_add": [_H, _H, _IP],
+    "tfs_batch_size": [_H, _IP],
+    "tfs_batch_step": [_H, ctypes.c_int, _P, _P, _P],
+    "tfs_server_config_default": [ctypes.POINTER(ServerConfig)],
+    "tfs_server_create": [ctypes.POINTER(ServerConfig), ctypes.POINTER(_H)],
+    "tfs_server_submit": [_H, ctypes.POINTER(Request), _LLP],
+    "tfs_server_poll": [_H, ctypes.c_longlong, ctypes.c_int, _IP,
+                        ctypes.POINTER(ctypes.c_double), _IP, _IP],
+    "tfs_server_drain": [_H],
+    "tfs_server_stats": [_H, ctypes.POINTER(ServerCounters)],
+    "tfs_server_destroy": [_H],
     "tfs_last_error": [],
     "tfs_kernel_launch_count": [],
     "tfs_measure_fma_peak": [ctypes.c_int, ctypes.POINTER(ctypes.c_double)],

@@ -943,6 +943,11 @@ struct tfs_stepper {
   int jac_ready = 0;
   size_t jac_smem = 0;
   long nbroy = 0;
+  // the straight start (for tfs_stepper_reset): unit directions, base
+  // quaternions, body frame references; the solver's warm start as it was
+  // when the stepper was created
+  std::vector<double> dirs, q0, refs;
+  double *warm = nullptr;  // 3 nblob + 6
 };
 
 namespace {
@@ -1071,6 +1076,70 @@ int low_rank(tfs_stepper *st, const double *a, double *v, int ncols) {
   return TFS_OK;
 }
 
+// The straight start (filament::initial_setup, filament.cpp:219-346): the
+// body at rest at its configured pose, filaments along their directions from
+// the bases X + R ref, all multipliers and histories zero. With rot (3 values
+// per segment) each segment is first turned by exp(rot) and the positions
+// follow from the robot arm; without it they are base + j DL dir, accumulated
+// as the reference does.
+int load_start(tfs_stepper *st, const double *rot) {
+  const StepDev &d = st->d;
+  const tfs_step_config *cfg = &st->cfg;
+  const size_t ns = d.ns, nf = d.nfil, nl = 3 * (size_t)(d.nseg - 1) * nf;
+  for (int k = 0; k < 3; ++k) st->bx[k] = st->bxm1[k] = st->bxm2[k] = cfg->body_x[k];
+  for (int k = 0; k < 3; ++k) st->bu[k] = st->bum1[k] = 0.0;
+  for (int k = 0; k < 4; ++k) st->bq[k] = st->bqm1[k] = cfg->body_q[k];
+  rot_rm(st->bq, st->Qinit);
+  std::vector<double> hx(3 * ns), hq(4 * ns), hu(3 * ns, 0.0), zero(std::max(nl, 6 * ns), 0.0);
+  for (size_t i = 0; i < nf; ++i) {
+    const double *ud = &st->dirs[3 * i];
+    const Quat q0 = load_q(&st->q0[4 * i]);
+    double pos[3];
+    for (int k = 0; k < 3; ++k) {
+      double r = 0.0;
+      for (int c = 0; c < 3; ++c) r += st->Qinit[3 * k + c] * st->refs[3 * i + c];
+      pos[k] = st->bx[k] + r;
+    }
+    double tprev[3] = {0.0, 0.0, 0.0};
+    for (int j = 0; j < d.nseg; ++j) {
+      const size_t sg = i * d.nseg + j;
+      const Quat q = rot ? qmul(lie_exp(rot + 3 * sg), q0) : q0;
+      store_q(&hq[4 * sg], q);
+      if (rot) {
+        double t[3];
+        tangent(q, t);
+        if (j > 0)
+          for (int k = 0; k < 3; ++k) pos[k] = pos[k] + 0.5 * d.dl * (tprev[k] + t[k]);
+        for (int k = 0; k < 3; ++k) tprev[k] = t[k];
+        for (int k = 0; k < 3; ++k) hx[3 * sg + k] = pos[k];
+      } else {
+        for (int k = 0; k < 3; ++k) hx[3 * sg + k] = pos[k];
+        for (int k = 0; k < 3; ++k) pos[k] += d.dl * ud[k];
+      }
+    }
+  }
+  cudaStream_t str = st->s->stream;
+  struct C {
+    double *dst;
+    const double *src;
+    size_t n;
+  } copies[] = {{d.x, hx.data(), 3 * ns},    {d.xm1, hx.data(), 3 * ns}, {d.xm2, hx.data(), 3 * ns},
+                {d.q, hq.data(), 4 * ns},    {d.qm1, hq.data(), 4 * ns}, {d.u, hu.data(), 3 * ns},
+                {d.um1, hu.data(), 3 * ns},  {d.f, zero.data(), 6 * ns}, {d.lam, zero.data(), nl},
+                {d.lamm1, zero.data(), nl},  {d.lamm2, zero.data(), nl}, {d.teth, zero.data(), 3 * nf},
+                {d.tethm1, zero.data(), 3 * nf}, {d.tethm2, zero.data(), 3 * nf},
+                {d.clamp, zero.data(), 3 * nf}, {d.clampm1, zero.data(), 3 * nf},
+                {d.clampm2, zero.data(), 3 * nf}, {const_cast<double *>(d.fil_refs), st->refs.data(), 3 * nf}};
+  for (auto &c : copies)
+    ST_CUDA(cudaMemcpyAsync(c.dst, c.src, sizeof(double) * c.n, cudaMemcpyHostToDevice, str),
+            "stepper state");
+  ST_CUDA(cudaStreamSynchronize(str), "stepper state");
+  st->iter = 0;
+  st->jac_ready = 0;
+  st->s->origin_dirty = true;
+  return TFS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1106,6 +1175,7 @@ int tfs_stepper_destroy(tfs_stepper *st) {
     if (p) cudaFree(p);
   if (d.fil_refs) cudaFree(const_cast<double *>(d.fil_refs));
   if (st->flag) cudaFree(st->flag);
+  if (st->warm) cudaFree(st->warm);
   if (st->hbuf) cudaFreeHost(st->hbuf);
   if (st->hflag) cudaFreeHost(st->hflag);
   delete st;
@@ -1197,10 +1267,19 @@ int tfs_stepper_create(tfs_solver *s, const tfs_step_config *cfg, const double *
     return fail(TFS_ENOMEM, "stepper allocation");
   }
   d.fil_refs = refs_dev;
-  // initial state: the body at rest, straight filaments along fil_dirs from
-  // their base X + R ref (filament::initial_setup, filament.cpp:219-346)
-  for (int k = 0; k < 3; ++k) st->bx[k] = st->bxm1[k] = st->bxm2[k] = cfg->body_x[k];
-  for (int k = 0; k < 3; ++k) st->bu[k] = st->bum1[k] = 0.0;
+  st->dirs.resize(3 * nf);
+  st->q0.resize(4 * nf);
+  st->refs.assign(fil_refs, fil_refs + 3 * nf);
+  for (size_t i = 0; i < nf; ++i) {
+    const double *dir = fil_dirs + 3 * i;
+    const double dn = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    if (!(dn > 0.0)) {
+      tfs_stepper_destroy(st);
+      return fail(TFS_EINVAL, "filament %zu: zero direction", i);
+    }
+    for (int k = 0; k < 3; ++k) st->dirs[3 * i + k] = dir[k] / dn;
+    store_q(&st->q0[4 * i], along_direction(dir));
+  }
   {
     double nq = 0.0;
     for (int k = 0; k < 4; ++k) nq += cfg->body_q[k] * cfg->body_q[k];
@@ -1209,54 +1288,27 @@ int tfs_stepper_create(tfs_solver *s, const tfs_step_config *cfg, const double *
       return fail(TFS_EINVAL, "zero body quaternion");
     }
   }
-  for (int k = 0; k < 4; ++k) st->bq[k] = st->bqm1[k] = cfg->body_q[k];
-  rot_rm(st->bq, st->Qinit);
-  std::vector<double> hx(3 * ns), hq(4 * ns), zero(std::max(nl, 6 * ns), 0.0);
-  for (size_t i = 0; i < nf; ++i) {
-    const double *dir = fil_dirs + 3 * i;
-    const double dn = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
-    if (!(dn > 0.0)) {
-      tfs_stepper_destroy(st);
-      return fail(TFS_EINVAL, "filament %zu: zero direction", i);
-    }
-    const double ud[3] = {dir[0] / dn, dir[1] / dn, dir[2] / dn};
-    const Quat q0 = along_direction(dir);
-    double pos[3];
-    for (int k = 0; k < 3; ++k) {
-      double r = 0.0;
-      for (int c = 0; c < 3; ++c) r += st->Qinit[3 * k + c] * fil_refs[3 * i + c];
-      pos[k] = st->bx[k] + r;
-    }
-    for (int j = 0; j < d.nseg; ++j) {
-      const size_t sg = i * d.nseg + j;
-      for (int k = 0; k < 3; ++k) hx[3 * sg + k] = pos[k];
-      store_q(&hq[4 * sg], q0);
-      for (int k = 0; k < 3; ++k) pos[k] += d.dl * ud[k];
-    }
+  int rc = load_start(st, nullptr);
+  if (rc != TFS_OK) {
+    tfs_stepper_destroy(st);
+    return rc;
   }
-  cudaStream_t str = s->stream;
-  struct C {
-    double *dst;
-    const double *src;
-    size_t n;
-  } copies[] = {{d.x, hx.data(), 3 * ns},    {d.xm1, hx.data(), 3 * ns}, {d.xm2, hx.data(), 3 * ns},
-                {d.q, hq.data(), 4 * ns},    {d.qm1, hq.data(), 4 * ns}, {d.u, zero.data(), 3 * ns},
-                {d.um1, zero.data(), 3 * ns}, {d.f, zero.data(), 6 * ns}, {d.lam, zero.data(), nl},
-                {d.lamm1, zero.data(), nl},  {d.lamm2, zero.data(), nl}, {d.teth, zero.data(), 3 * nf},
-                {d.tethm1, zero.data(), 3 * nf}, {d.tethm2, zero.data(), 3 * nf},
-                {d.clamp, zero.data(), 3 * nf}, {d.clampm1, zero.data(), 3 * nf},
-                {d.clampm2, zero.data(), 3 * nf}, {refs_dev, fil_refs, 3 * nf}};
-  for (auto &c : copies) {
-    cudaError_t e = cudaMemcpyAsync(c.dst, c.src, sizeof(double) * c.n, cudaMemcpyHostToDevice, str);
-    if (e != cudaSuccess) {
-      tfs_stepper_destroy(st);
-      return cuda_fail(e, "stepper initial state");
-    }
+  // the warm start of the first solve, restored by tfs_stepper_reset
+  const size_t nw = 3 * (size_t)s->nb + 6;
+  if (cudaMalloc(&st->warm, sizeof(double) * nw) != cudaSuccess) {
+    cudaGetLastError();
+    tfs_stepper_destroy(st);
+    return fail(TFS_ENOMEM, "stepper allocation");
   }
-  cudaError_t e = cudaStreamSynchronize(str);
+  cudaError_t e = cudaMemcpyAsync(st->warm, s->f_blobs, sizeof(double) * 3 * s->nb,
+                                  cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(st->warm + 3 * s->nb, s->v_bodies, sizeof(double) * 6,
+                        cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) {
     tfs_stepper_destroy(st);
-    return cuda_fail(e, "stepper initial state");
+    return cuda_fail(e, "stepper warm start");
   }
   s->origin_dirty = true;
   *out = st;
@@ -1527,4 +1579,36 @@ int tfs_stepper_state(tfs_stepper *st, double *x, double *q, double *u, double *
   return TFS_OK;
 }
 
+int tfs_stepper_reset(tfs_stepper *st, const double *seg_rotation) {
+  TFS_CHECK_STEPPER(st);
+  int rc = load_start(st, seg_rotation);
+  if (rc != TFS_OK) return rc;
+  tfs_solver *s = st->s;
+  ST_CUDA(cudaMemcpyAsync(s->f_blobs, st->warm, sizeof(double) * 3 * s->nb, cudaMemcpyDeviceToDevice,
+                          s->stream),
+          "warm start");
+  ST_CUDA(cudaMemcpyAsync(s->v_bodies, st->warm + 3 * s->nb, sizeof(double) * 6,
+                          cudaMemcpyDeviceToDevice, s->stream),
+          "warm start");
+  ST_CUDA(cudaStreamSynchronize(s->stream), "warm start");
+  return TFS_OK;
+}
+
 }  // extern "C"
+
+namespace tfs {
+tfs_solver *stepper_solver(tfs_stepper *st) { return st ? st->s : nullptr; }
+long stepper_segments(const tfs_stepper *st) { return st ? (long)st->d.ns : 0; }
+}  // namespace tfs
+
+namespace tfs {
+// Device bytes of a stepper (tfs_stepper_create's allocations).
+size_t stepper_bytes_estimate(int nfil, int nseg, int max_broyden_iter) {
+  const size_t nf = nfil, ns = (size_t)nfil * nseg, n6 = 6 * (size_t)nseg;
+  const size_t nbroy = 6 * (ns + 1);
+  const size_t doubles = 31 * ns + 12 * nf * nseg + nf * (n6 * n6 + 6 * n6 + 18 + 45 + 6 + 6 + 3) +
+                         nbroy * (5 + 2 * (size_t)max_broyden_iter) +
+                         (size_t)max_broyden_iter * (1 + kMaxDotChunks) + 256;
+  return 8 * doubles;
+}
+}  // namespace tfs

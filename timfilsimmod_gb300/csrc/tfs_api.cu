@@ -635,3 +635,16 @@ const char *tfs_last_error(void) { return g_last_error.c_str(); }
 long long tfs_kernel_launch_count(void) { return g_launches.load(); }
 
 }  // extern "C"
+
+namespace tfs {
+// Device bytes of a solver of these sizes (tfs_solver_create's and the
+// solve's allocations, the cooperative-GMRES buffers at their largest),
+// plus 1 MB for the small ones.
+size_t solver_bytes_estimate(const tfs_config *cfg) {
+  const size_t ns = (size_t)cfg->nswim * cfg->nfil * cfg->nseg, nb = (size_t)cfg->nswim * cfg->nblob;
+  const size_t n = 3 * nb + 6, m = std::min<size_t>(350, n);
+  const size_t doubles = 15 * ns + 12 * nb + (size_t)kMaxSplits * std::max(6 * ns, 3 * nb) +
+                         n * (m + 1) + (m + 1) * (m + 1) + 16 * n + 57 * nb + 256 * (m + 1);
+  return 8 * doubles + 200 * ns + 200 * nb + ((size_t)1 << 20);
+}
+}  // namespace tfs

@@ -1,0 +1,142 @@
+"""Many independent swimmers on one GPU (tfs_batch_*, tfs_server_* of the C ABI).
+
+SwimmerBatch advances a set of swimmers (ImplicitStepper instances, each
+with its own solver and stream) one implicit step at a time: host worker
+threads run the instances' step pipelines so that their kernels overlap on
+the GPU. StepServer takes requests -- num_steps implicit steps of a swimmer
+from a perturbed straight start -- keeps instances resident between
+requests, admits requests by a device-memory budget and reports each
+request's latency. There is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from .mobility import PRECISIONS
+from .stepper import ImplicitStepper
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64).reshape(-1))
+
+
+class SwimmerBatch:
+    def __init__(self, num_workers: int = 8):
+        self.lib = N.load()
+        h = ctypes.c_void_p()
+        N.check(self.lib.tfs_batch_create(int(num_workers), ctypes.byref(h)))
+        self._h = h
+        self.steppers: list[ImplicitStepper] = []
+
+    def add(self, stepper: ImplicitStepper) -> int:
+        idx = ctypes.c_int(0)
+        N.check(self.lib.tfs_batch_add(self._h, stepper._h, ctypes.byref(idx)))
+        self.steppers.append(stepper)
+        return idx.value
+
+    def step(self, nt: int, allow_unconverged: bool = False) -> dict:
+        """Step nt of every swimmer; per-swimmer Broyden/GMRES counts and statuses."""
+        n = len(self.steppers)
+        b, g, st = (np.zeros(n, dtype=np.int32) for _ in range(3))
+        rc = self.lib.tfs_batch_step(self._h, int(nt), b.ctypes.data, g.ctypes.data,
+                                     st.ctypes.data)
+        if rc != N.TFS_OK and not (allow_unconverged and np.all(
+                (st == N.TFS_OK) | (st == N.TFS_ENOTCONV))):
+            N.check(rc)
+        return {"broyden_iters": b, "gmres_iters": g, "status": st}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            self.lib.tfs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class StepServer:
+    """Request server. precision "fp64" or "fp32c"; step settings as keyword
+    arguments of tfs_step_config (dt, tol, seg_sep, end_force_magnitude,
+    body_radius, max_broyden_iter, ...)."""
+
+    def __init__(self, num_workers: int = 8, hbm_budget_gb: float = 160.0,
+                 precision: str = "fp32c", linear_tol: float = 1e-8, **step):
+        self.lib = N.load()
+        cfg = N.ServerConfig()
+        N.check(self.lib.tfs_server_config_default(ctypes.byref(cfg)))
+        cfg.num_workers = int(num_workers)
+        cfg.hbm_budget_bytes = int(hbm_budget_gb * (1 << 30))
+        cfg.precision = PRECISIONS[precision]
+        cfg.linear_tol = float(linear_tol)
+        for k, v in step.items():
+            if k in ("body_x", "body_q"):
+                arr = getattr(cfg.step, k)
+                for i, x in enumerate(v):
+                    arr[i] = float(x)
+            elif not hasattr(cfg.step, k):
+                raise TypeError(f"unknown step setting {k!r}")
+            else:
+                setattr(cfg.step, k, type(getattr(cfg.step, k))(v))
+        h = ctypes.c_void_p()
+        N.check(self.lib.tfs_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._live: dict[int, tuple] = {}  # ticket -> arrays the request points into
+
+    def submit(self, blob_refs, fil_refs, fil_dirs, nseg: int, num_steps: int = 1,
+               seg_rotation=None) -> int:
+        br, fr, fd = _f64(blob_refs), _f64(fil_refs), _f64(fil_dirs)
+        nfil, nblob = fr.size // 3, br.size // 3
+        rot = None if seg_rotation is None else _f64(seg_rotation)
+        if rot is not None and rot.size != 3 * nfil * nseg:
+            raise ValueError("seg_rotation needs 3 values per segment")
+        x = np.zeros(3 * nfil * nseg)
+        body = np.zeros(7)
+        r = N.Request(nfil=nfil, nseg=int(nseg), nblob=nblob, blob_refs=br.ctypes.data,
+                      fil_refs=fr.ctypes.data, fil_dirs=fd.ctypes.data,
+                      seg_rotation=None if rot is None else rot.ctypes.data,
+                      num_steps=int(num_steps), x_out=x.ctypes.data, body_out=body.ctypes.data)
+        t = ctypes.c_longlong(0)
+        N.check(self.lib.tfs_server_submit(self._h, ctypes.byref(r), ctypes.byref(t)))
+        self._live[t.value] = (br, fr, fd, rot, x, body)
+        return t.value
+
+    def poll(self, ticket: int, wait: bool = False) -> dict | None:
+        """None while pending; else the result (x, body, latency_ms, counts).
+        A failed request raises."""
+        st, lat = ctypes.c_int(0), ctypes.c_double(0.0)
+        b, g = ctypes.c_int(0), ctypes.c_int(0)
+        N.check(self.lib.tfs_server_poll(self._h, ctypes.c_longlong(ticket), int(bool(wait)),
+                                         ctypes.byref(st), ctypes.byref(lat), ctypes.byref(b),
+                                         ctypes.byref(g)))
+        if st.value == 1:
+            return None
+        arrays = self._live.pop(ticket)
+        if st.value != N.TFS_OK:
+            raise N.TfsError(st.value, f"request {ticket} failed")
+        return {"x": arrays[4], "body": arrays[5], "latency_ms": lat.value,
+                "broyden_iters": b.value, "gmres_iters": g.value}
+
+    def drain(self) -> None:
+        N.check(self.lib.tfs_server_drain(self._h))
+
+    def stats(self) -> dict:
+        c = N.ServerCounters()
+        N.check(self.lib.tfs_server_stats(self._h, ctypes.byref(c)))
+        return {k: getattr(c, k) for k, _ in c._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            self.lib.tfs_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -155,6 +155,17 @@ class ImplicitStepper:
     def end_of_iter(self, nt: int, big: bool) -> None:
         N.check(self._call("tfs_stepper_end_of_iter", int(nt), int(bool(big))))
 
+    def reset(self, seg_rotation=None) -> None:
+        """Back to the straight start (and the solver's warm start at creation),
+        each segment turned by exp(seg_rotation[j]) if given (Ns x 3)."""
+        if seg_rotation is None:
+            N.check(self._call("tfs_stepper_reset", None))
+        else:
+            r = _f64(seg_rotation)
+            if r.size != 3 * self.ns:
+                raise ValueError("seg_rotation needs 3 values per segment")
+            N.check(self._call("tfs_stepper_reset", _p(r)))
+
     def state(self) -> dict:
         ns, nf, sg = self.ns, self.nfil, self.nseg
         out = dict(x=np.zeros(3 * ns), q=np.zeros(4 * ns), u=np.zeros(3 * ns),
