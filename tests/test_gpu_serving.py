@@ -109,15 +109,15 @@ def serve(reqs, workers, budget_gb=160.0, one_at_a_time=False, precision="fp32c"
 
 def test_server_results_same_alone_and_in_mix():
     reqs = requests()
-    alone, _ = serve(reqs, workers=1, one_at_a_time=True)
-    mix, stats = serve(reqs, workers=4)
+    alone, stats = serve(reqs, workers=1, one_at_a_time=True)
+    # one request at a time: each geometry's instance is built once, then reused
+    assert stats["created"] == len(SHAPES) and stats["reused"] == len(reqs) - len(SHAPES)
+    mix, _ = serve(reqs, workers=4)
     for a, m in zip(alone, mix):
         assert np.array_equal(a["x"], m["x"])
         assert np.array_equal(a["body"], m["body"])
         assert m["latency_ms"] > 0 and m["broyden_iters"] > 0
-    # repeated geometries reuse resident instances
-    assert stats["created"] <= len(SHAPES) + 3 and stats["reused"] >= 1
-    # the perturbation moved the result off the unperturbed one
+    # two perturbations of one geometry give two different results
     assert not np.array_equal(mix[0]["x"], mix[len(SHAPES)]["x"])
 
 
