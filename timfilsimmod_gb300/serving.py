@@ -89,7 +89,7 @@ class StepServer:
         self._live: dict[int, tuple] = {}  # ticket -> arrays the request points into
 
     def submit(self, blob_refs, fil_refs, fil_dirs, nseg: int, num_steps: int = 1,
-               seg_rotation=None) -> int:
+               seg_rotation=None, body_radius: float = 0.0) -> int:
         br, fr, fd = _f64(blob_refs), _f64(fil_refs), _f64(fil_dirs)
         nfil, nblob = fr.size // 3, br.size // 3
         rot = None if seg_rotation is None else _f64(seg_rotation)
@@ -99,6 +99,7 @@ class StepServer:
         body = np.zeros(7)
         r = N.Request(nfil=nfil, nseg=int(nseg), nblob=nblob, blob_refs=br.ctypes.data,
                       fil_refs=fr.ctypes.data, fil_dirs=fd.ctypes.data,
+                      body_radius=float(body_radius),
                       seg_rotation=None if rot is None else rot.ctypes.data,
                       num_steps=int(num_steps), x_out=x.ctypes.data, body_out=body.ctypes.data)
         t = ctypes.c_longlong(0)
