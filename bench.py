@@ -21,6 +21,11 @@ inputs/outputs). Printed: one JSON line (rank 0).
   implicit_steps  whole implicit time steps (forces, solve, residuals,
            Broyden) at a 1e-8 linear residual, FP64 vs FP32C, steps/s with
            p50/p99 per-step latency
+  batched  64 uneven swimmers stepped together (FP32C, host worker pool)
+           vs the FP64 drop-in one swimmer at a time, swimmer-steps/s
+  served   Poisson streams of step requests of log-uniform size into the
+           request server: steps/s and p50/p99 latency per arrival rate, vs
+           FP64 requests served one at a time
   flow     the flow-field evaluator on a 128^3 grid around the large swimmer
            (80 000 segments, 10 242 blobs), FP32C, with an FP64 subset
 
@@ -249,6 +254,9 @@ def bench_ours(args):
     solve = None if args.no_solve else solve_bench(sw, stream, args, RpyMobilitySolver)
     # --- implicit time steps (initial guess, forces, solve, Broyden) -----------
     steps = None if args.no_steps else step_bench(sw, stream, args)
+    # --- many swimmers: a batch stepped together, and a request stream ---------
+    batched = None if args.no_batch else batch_bench(args)
+    served = None if args.no_serve else serve_bench(args)
     # --- the flow-field evaluator on a 128^3 grid around the large swimmer -----
     flow = None if args.no_flow else flow_bench(stream, flush, args, peak32, peak64, rank)
     clocks = sampler.stop()
@@ -320,6 +328,10 @@ def bench_ours(args):
             result["solve"] = solve
         if steps is not None:
             result["implicit_steps"] = steps
+        if batched is not None:
+            result["batched"] = batched
+        if served is not None:
+            result["served"] = served
         if flow is not None:
             result["flow"] = flow
     for sv in (s32, s64):
@@ -479,6 +491,169 @@ def step_bench(sw, stream, args):
             **out, "speedup_fp32c_vs_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
             "fp32c_max_rel_position_dev_vs_fp64": float(dev.max()),
             "fp32c_rel_position_dev_vs_fp64_last": float(dev[-1])}
+
+
+def _step_instance(nf, precision, cache, rot_seed=None):
+    """One swimmer for the batch and serving legs: solver + stepper (DT 1e-3,
+    TOL 1e-4, linear residual 1e-8); body reference matrices made once per
+    (precision, blob count) and shared."""
+    from timfilsimmod_gb300.geometry import elastic_swimmer
+    from timfilsimmod_gb300.mobility import RpyMobilitySolver
+    from timfilsimmod_gb300.stepper import ImplicitStepper
+
+    blob_refs, fil_refs, dirs, radius = elastic_swimmer(int(nf))
+    nb = blob_refs.shape[0]
+    efm = 220.0 * 1800.0 / (2.6 * 2.6 * 400)
+    s = RpyMobilitySolver(1, int(nf), 20, nb, precision=precision, end_force_magnitude=int(efm))
+    if precision == "fp32c":
+        s.set_persistent_gmres(False)
+    s.set_blob_references(blob_refs)
+    s.set_linear_solver(1e-8, min(350, 3 * nb + 6))
+    key = (precision, nb)
+    if key not in cache:
+        s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+        cache[key] = s.make_body_reference_matrices()
+    else:
+        s.set_body_reference_matrices(*cache[key])
+    st = ImplicitStepper(s, int(nf), 20, fil_refs, dirs, make_body_matrices=False, seg_sep=2.2,
+                         dt=1e-3, tol=1e-4, end_force_magnitude=efm, body_radius=radius)
+    if rot_seed is not None:
+        st.reset(1e-6 * np.random.default_rng(rot_seed).normal(size=(int(nf) * 20, 3)))
+    return s, st
+
+
+def batch_bench(args):
+    """Uneven swimmers stepped together (filaments U[16, 512] x 20 segments,
+    642 blobs below 128 filaments, else 2562; per-swimmer seeded N(0, 1e-6)
+    segment rotations of the straight start): the FP32C batch (host worker
+    pool, one stream per swimmer, all in flight at once) against the plain
+    FP64 drop-in stepping the same swimmers one at a time. Steps 0-2 warm up
+    (step 0 iterates Broyden from the start); the timed steps follow, timed
+    on the host clock around whole batch steps (every swimmer's step ends
+    with its stream synchronised)."""
+    from timfilsimmod_gb300.serving import SwimmerBatch
+
+    rng = np.random.default_rng(4242)
+    nfils = rng.integers(16, 513, size=args.batch_size)
+    warm, timed = 3, max(2, min(args.steps, 4))
+    out, final = {}, {}
+    for precision in ("fp32c", "fp64"):
+        cache = {}
+        inst = [_step_instance(nf, precision, cache, rot_seed=1000 + i) for i, nf in enumerate(nfils)]
+        if precision == "fp32c":
+            batch = SwimmerBatch(num_workers=args.batch_workers)
+            for _, st in inst:
+                batch.add(st)
+            for nt in range(warm):
+                batch.step(nt, allow_unconverged=True)
+            t0 = time.perf_counter()
+            iters = []
+            for nt in range(warm, warm + timed):
+                iters.append(batch.step(nt, allow_unconverged=True)["gmres_iters"].mean())
+            sec = time.perf_counter() - t0
+            batch.close()
+        else:
+            for nt in range(warm):
+                for _, st in inst:
+                    st.step(nt, allow_unconverged=True)
+            t0 = time.perf_counter()
+            iters = []
+            for nt in range(warm, warm + timed):
+                iters.append(np.mean([st.step(nt, allow_unconverged=True)[1] for _, st in inst]))
+            sec = time.perf_counter() - t0
+        final[precision] = [st.state()["x"] for _, st in inst]
+        n = len(inst)
+        out[precision] = {"value": n * timed / sec, "unit": "swimmer-steps/s",
+                          "ms_per_batch_step": 1e3 * sec / timed,
+                          "gmres_iters_per_swimmer_step": float(np.mean(iters)),
+                          "mode": (f"batch, {args.batch_workers} host workers, one stream per swimmer"
+                                   if precision == "fp32c" else "one swimmer at a time")}
+        for s, st in inst:
+            st.close()
+            s.finalise()
+    dev = max(float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+              for a, b in zip(final["fp32c"], final["fp64"]))
+    return {"workload": f"{len(nfils)} swimmers, filaments {int(nfils.min())}-{int(nfils.max())} "
+                        f"x 20 segments ({int(nfils.sum()) * 20} segments in all), 642/2562 blobs; "
+                        "dt 1e-3, Broyden TOL 1e-4, linear residual 1e-8",
+            **out, "speedup_fp32c_batch_vs_fp64_one_at_a_time":
+                out["fp32c"]["value"] / out["fp64"]["value"],
+            "fp32c_max_rel_position_dev_vs_fp64": dev}
+
+
+def serve_bench(args):
+    """Request stream: implicit-step requests (step 0 of a base swimmer with
+    N(0, 1e-6) segment rotations, as an orbit search perturbs a state), sizes
+    log-uniform in 64-20 000 segments over a fixed set of base swimmers
+    (filaments = segments / 20; 642 blobs below 128 filaments, else 2562),
+    Poisson arrivals at each rate. FP32C server (worker pool, instances kept
+    resident, admission by a device-memory budget) after one warm-up request
+    per base; latency = arrival to completion. Baseline: the plain FP64
+    drop-in serving the same requests one at a time."""
+    from timfilsimmod_gb300.geometry import elastic_swimmer
+    from timfilsimmod_gb300.serving import StepServer
+
+    rng = np.random.default_rng(777)
+    ns = np.exp(rng.uniform(np.log(64), np.log(20000), size=args.serve_bases))
+    bases = sorted({max(4, int(round(x / 20))) for x in ns})
+    geo = {nf: elastic_swimmer(nf) for nf in bases}
+    efm = 220.0 * 1800.0 / (2.6 * 2.6 * 400)
+    nreq = args.serve_requests
+
+    def stream(seed):
+        r = np.random.default_rng(seed)
+        picks = r.integers(0, len(bases), size=nreq)
+        return [(bases[k], 1e-6 * r.normal(size=(bases[k] * 20, 3))) for k in picks]
+
+    def submit(sv, nf, rot):
+        b, f, d, radius = geo[nf]
+        return sv.submit(b, f, d, 20, num_steps=1, seg_rotation=rot, body_radius=radius)
+
+    def server(precision, workers):
+        sv = StepServer(num_workers=workers, hbm_budget_gb=160.0, precision=precision,
+                        linear_tol=1e-8, dt=1e-3, tol=1e-4, seg_sep=2.2, end_force_magnitude=efm)
+        for t in [submit(sv, nf, None) for nf in bases]:
+            sv.poll(t, wait=True)
+        return sv
+
+    rates = {}
+    sv = server("fp32c", args.serve_workers)
+    for lam in args.serve_rates:
+        reqs = stream(int(lam))
+        gaps = np.random.default_rng(int(lam) + 1).exponential(1.0 / lam, size=nreq)
+        t0 = time.perf_counter()
+        arrive, tickets = t0, []
+        for (nf, rot), gap in zip(reqs, gaps):
+            arrive += gap
+            while time.perf_counter() < arrive:
+                time.sleep(min(1e-3, max(0.0, arrive - time.perf_counter())))
+            tickets.append(submit(sv, nf, rot))
+        lat = np.array([sv.poll(t, wait=True)["latency_ms"] for t in tickets])
+        sec = time.perf_counter() - t0
+        rates[str(lam)] = {"offered_req_per_s": lam, "steps_per_s": nreq / sec,
+                           "p50_ms": float(np.percentile(lat, 50)),
+                           "p99_ms": float(np.percentile(lat, 99)), "requests": nreq}
+    stats = sv.stats()
+    sv.close()
+    sv = server("fp64", 1)
+    reqs = stream(int(args.serve_rates[0]))
+    t0 = time.perf_counter()
+    lat = np.array([sv.poll(submit(sv, nf, rot), wait=True)["latency_ms"] for nf, rot in reqs])
+    sec = time.perf_counter() - t0
+    sv.close()
+    base = {"steps_per_s": nreq / sec, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "requests": nreq,
+            "mode": "one request at a time (service time, no queueing)"}
+    best = max(v["steps_per_s"] for v in rates.values())
+    return {"workload": f"{len(bases)} base swimmers of {min(bases) * 20}-{max(bases) * 20} "
+                        "segments (log-uniform), step-0 requests with N(0,1e-6) segment "
+                        "rotations, Poisson arrivals; dt 1e-3, Broyden TOL 1e-4, linear "
+                        "residual 1e-8",
+            "fp32c_server": {"workers": args.serve_workers, "by_rate": rates,
+                             "resident_instances": stats["resident_instances"],
+                             "created": stats["created"], "reused": stats["reused"]},
+            "fp64_one_at_a_time": base,
+            "speedup_best_rate_vs_fp64": best / base["steps_per_s"]}
 
 
 FLOW_SEG, FLOW_BLOB, FLOW_POINT = 44, 28, 3  # canonical flops per source, per point
@@ -686,6 +861,15 @@ def main():
     p.add_argument("--no-solve", action="store_true", help="skip the solve timing")
     p.add_argument("--no-flow", action="store_true", help="skip the flow-field timing")
     p.add_argument("--no-steps", action="store_true", help="skip the implicit-step timing")
+    p.add_argument("--no-batch", action="store_true", help="skip the batched-swimmers timing")
+    p.add_argument("--no-serve", action="store_true", help="skip the request-stream timing")
+    p.add_argument("--batch-size", type=int, default=64, help="swimmers in the batch leg")
+    p.add_argument("--batch-workers", type=int, default=16, help="host workers of the batch")
+    p.add_argument("--serve-bases", type=int, default=12, help="base swimmers of the stream")
+    p.add_argument("--serve-requests", type=int, default=96, help="requests per arrival rate")
+    p.add_argument("--serve-workers", type=int, default=8, help="server workers")
+    p.add_argument("--serve-rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0],
+                   help="Poisson arrival rates (requests/s)")
     p.add_argument("--flow-grid", type=int, default=128, help="flow points per grid axis")
     args = p.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -155,3 +155,16 @@ def flow_grid(n: int, half_width: float, centre=(0.0, 0.0, 0.0)) -> np.ndarray:
     z, y, x = np.meshgrid(c, c, c, indexing="ij")
     pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
     return np.ascontiguousarray(pts + np.asarray(centre, dtype=np.float64))
+
+
+def elastic_swimmer(nfil: int, nseg: int = 20, seg_sep: float = 2.2, a_blob: float = 1.0):
+    """A swimmer for the implicit step: a sphere of 642 blobs (R = 20a) when
+    nfil < 128, else 2562 blobs (R = 60a), with nfil straight filaments
+    rooted on a Fibonacci lattice one blob radius plus half a segment gap
+    above the surface, along the normals. Returns (blob_refs (Nb, 3),
+    fil_refs (nfil, 3), fil_dirs (nfil, 3), radius)."""
+    radius, subdiv = (20.0, 3) if nfil < 128 else (60.0, 4)
+    blob_refs = radius * icosphere(subdiv)
+    normals = fibonacci_sphere(nfil)
+    fil_refs = (radius + a_blob + 0.5 * seg_sep) * normals
+    return blob_refs, fil_refs, normals, radius
