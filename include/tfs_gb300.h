@@ -331,8 +331,9 @@ int tfs_server_create(const tfs_server_config *cfg, tfs_server **out);
  * each instance's estimated size at admission. */
 int tfs_server_submit(tfs_server *sv, const tfs_request *r, long long *ticket);
 /* *status: 1 while pending, else the request's TFS status (the ticket is
- * then released). wait != 0 blocks until it completes. latency_ms: arrival
- * to completion. */
+ * then released; a failed request's message becomes the calling thread's
+ * tfs_last_error()). wait != 0 blocks until it completes. latency_ms:
+ * arrival to completion. */
 int tfs_server_poll(tfs_server *sv, long long ticket, int wait, int *status, double *latency_ms,
                     int *broyden_iters, int *gmres_iters);
 int tfs_server_drain(tfs_server *sv);   /* until every submitted request completed */

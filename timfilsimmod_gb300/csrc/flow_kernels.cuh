@@ -12,6 +12,8 @@
 // same for all of them that sum is S(x - X_b) (sum_j f_j).
 #pragma once
 
+#include <atomic>
+
 #include <cuda_runtime.h>
 
 #include "rpy_tile.cuh"
@@ -173,14 +175,15 @@ __global__ void __launch_bounds__(BLOCK) flow_kernel(const FlowArgs a) {
 
 template <typename T, bool WALL, int BLOCK, int TPT, int TS>
 cudaError_t flow_launch_fn(const FlowArgs &a, dim3 grid, cudaStream_t st, int *resident) {
-  static int occupancy = 0;
+  static std::atomic<int> occupancy{0};  // set once; host threads may race to set it
   auto kern = flow_kernel<T, WALL, BLOCK, TPT, TS>;
-  if (occupancy == 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occupancy, kern, BLOCK, 0);
+  if (occupancy.load() == 0) {
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, BLOCK, 0);
     if (e != cudaSuccess) return e;
-    if (occupancy < 1) occupancy = 1;
+    occupancy.store(occ < 1 ? 1 : occ);
   }
-  if (resident) *resident = occupancy;
+  if (resident) *resident = occupancy.load();
   if (grid.x == 0) return cudaSuccess;  // query only
   kern<<<grid, BLOCK, 0, st>>>(a);
   return cudaGetLastError();

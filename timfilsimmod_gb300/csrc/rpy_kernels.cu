@@ -23,6 +23,8 @@
 // sources in a fixed order, so results are deterministic.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <algorithm>
 
 #include "rpy_tile.cuh"
@@ -220,16 +222,16 @@ __global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
 // ---------------------------------------------------------------------------
 // Host-side launchers
 // ---------------------------------------------------------------------------
-static int g_num_sms = 0;
+static std::atomic<int> g_num_sms{0};  // set once; host threads may race to set it
 
 int num_sms() {
-  if (g_num_sms == 0) {
-    int dev = 0;
+  if (g_num_sms.load() == 0) {
+    int dev = 0, n = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_num_sms <= 0) g_num_sms = 1;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    g_num_sms.store(n > 0 ? n : 1);
   }
-  return g_num_sms;
+  return g_num_sms.load();
 }
 
 cudaError_t launch_reduce_partials(double *out, const double *partial, int n_elems, int splits,

@@ -2,6 +2,8 @@
 // for the layout and work decomposition) and the source-record formats.
 #pragma once
 
+#include <atomic>
+
 #include <cuda_runtime.h>
 
 #include "tfs_device.cuh"
@@ -303,16 +305,17 @@ constexpr size_t tile_smem_bytes() {
 template <typename T, int VD, int FDA, int FDB, int BLOCK, int TPT, int TS, int MINB>
 cudaError_t tile_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st, int *resident) {
   constexpr size_t smem = tile_smem_bytes<T, VD, FDA, FDB, BLOCK, TPT, TS>();
-  static int occupancy = 0;
+  static std::atomic<int> occupancy{0};  // set once; host threads may race to set it
   auto kern = rpy_tile_kernel<T, VD, FDA, FDB, BLOCK, TPT, TS, MINB>;
-  if (occupancy == 0) {
+  if (occupancy.load() == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occupancy, kern, BLOCK, smem);
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, BLOCK, smem);
     if (e != cudaSuccess) return e;
-    if (occupancy < 1) occupancy = 1;
+    occupancy.store(occ < 1 ? 1 : occ);
   }
-  if (resident) *resident = occupancy;
+  if (resident) *resident = occupancy.load();
   if (grid.x == 0) return cudaSuccess;  // query only
   kern<<<grid, BLOCK, smem, st>>>(a);
   return cudaGetLastError();

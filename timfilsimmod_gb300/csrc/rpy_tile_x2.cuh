@@ -11,6 +11,8 @@
 // Accumulation, near-pair replay and compensation follow rpy_tile.cuh.
 #pragma once
 
+#include <atomic>
+
 #include <cuda_runtime.h>
 
 #include "rpy_tile.cuh"
@@ -275,16 +277,17 @@ constexpr size_t tile_x2_smem_bytes() {
 template <int VD, int FDA, int FDB, int BLOCK, int TPT, int TS>
 cudaError_t tile_x2_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st, int *resident) {
   constexpr size_t smem = tile_x2_smem_bytes<VD, FDA, FDB, BLOCK, TPT, TS>();
-  static int occupancy = 0;
+  static std::atomic<int> occupancy{0};  // set once; host threads may race to set it
   auto kern = rpy_tile_x2_kernel<VD, FDA, FDB, BLOCK, TPT, TS>;
-  if (occupancy == 0) {
+  if (occupancy.load() == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occupancy, kern, BLOCK, smem);
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, BLOCK, smem);
     if (e != cudaSuccess) return e;
-    if (occupancy < 1) occupancy = 1;
+    occupancy.store(occ < 1 ? 1 : occ);
   }
-  if (resident) *resident = occupancy;
+  if (resident) *resident = occupancy.load();
   if (grid.x == 0) return cudaSuccess;  // query only
   kern<<<grid, BLOCK, smem, st>>>(a);
   return cudaGetLastError();

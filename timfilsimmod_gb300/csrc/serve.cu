@@ -31,6 +31,7 @@
 #include <memory>
 #include <mutex>
 #include <new>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -202,6 +203,7 @@ struct Request {
   Clock::time_point arrival{}, done{};
   int status = 1;  // 1 = pending
   int broyden = 0, gmres = 0;
+  std::string message;  // the failing call's message
 };
 
 unsigned long long fnv(unsigned long long h, const void *p, size_t n) {
@@ -350,6 +352,7 @@ void tfs_server::worker() {
       rc = tfs_stepper_state(in->st, q->r.x_out, nullptr, nullptr, nullptr, nullptr, nullptr,
                              q->r.body_out, q->r.body_out ? q->r.body_out + 3 : nullptr, nullptr);
     const bool drop = rc != TFS_OK;  // an instance that failed is not reused
+    const std::string fail_msg = drop ? std::string(tfs_last_error()) : std::string();
     if (drop) {
       g.lock();
       pool.erase(std::find(pool.begin(), pool.end(), in));
@@ -358,6 +361,7 @@ void tfs_server::worker() {
       destroy_instance(in);
     }
     g.lock();
+    q->message = fail_msg;
     if (!drop) {
       in->busy = false;
       in->last_used = Clock::now();
@@ -440,6 +444,8 @@ int tfs_server_poll(tfs_server *sv, long long ticket, int wait, int *status, dou
   if (wait) sv->done_cv.wait(g, [&] { return q->status != 1; });
   *status = q->status;
   if (q->status == 1) return TFS_OK;
+  if (q->status != TFS_OK)  // the request's message becomes this thread's last error
+    fail(q->status, "request %lld: %s", ticket, q->message.c_str());
   if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(q->done - q->arrival).count();
   if (broyden_iters) *broyden_iters = q->broyden;
   if (gmres_iters) *gmres_iters = q->gmres;

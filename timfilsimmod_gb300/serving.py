@@ -119,7 +119,7 @@ class StepServer:
             return None
         arrays = self._live.pop(ticket)
         if st.value != N.TFS_OK:
-            raise N.TfsError(st.value, f"request {ticket} failed")
+            raise N.TfsError(st.value, self.lib.tfs_last_error().decode(errors="replace"))
         return {"x": arrays[4], "body": arrays[5], "latency_ms": lat.value,
                 "broyden_iters": b.value, "gmres_iters": g.value}
 
