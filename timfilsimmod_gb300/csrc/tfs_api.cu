@@ -266,7 +266,16 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
     return rc;
   }
   // GMRES warm starts read f_blobs before any force is written
-  // (mobility_solver.cpp:35-39 zeroes the host copy); zero everything.
+  // (mobility_solver.cpp:35-39 zeroes the host copy), and the FP32 origin
+  // (the mean particle position) reads the segment positions even before a
+  // caller sets them (the body reference matrices need only the blobs):
+  // zero every particle array, so that no earlier allocation's contents can
+  // leak into a result.
+  cudaMemsetAsync(s->x_segs, 0, dsz * 3 * ns, s->stream);
+  cudaMemsetAsync(s->f_segs, 0, dsz * 6 * ns, s->stream);
+  cudaMemsetAsync(s->v_segs, 0, dsz * 6 * ns, s->stream);
+  cudaMemsetAsync(s->x_blobs, 0, dsz * 3 * nb, s->stream);
+  cudaMemsetAsync(s->v_blobs, 0, dsz * 3 * nb, s->stream);
   cudaMemsetAsync(s->f_blobs, 0, dsz * 3 * nb, s->stream);
   cudaMemsetAsync(s->f_rep, 0, dsz * 3 * nb, s->stream);
   cudaMemsetAsync(s->origin, 0, dsz * 4, s->stream);
