@@ -123,7 +123,10 @@ __device__ void block_dots(const GmresArgs &a, const Slice &sl, bool with_body, 
 
 // Last-CTA election: every CTA calls this after writing its partials; it
 // returns true in exactly one CTA (the last to arrive), which then sees all
-// partials and must reset the counter.
+// partials and must reset the counter. The last CTA reads the other CTAs'
+// partials with ld.global.cg (__ldcg, L2): L1 is not coherent across SMs, and
+// a line of the partial array cached by an earlier launch's last CTA on the
+// same SM could otherwise be read stale while other streams keep the SM busy.
 __device__ bool last_cta(unsigned *counter) {
   __shared__ bool last;
   __threadfence();
@@ -188,7 +191,7 @@ __device__ void kt_partial(const GmresArgs &a, const Slice &sl, const double *l,
 __device__ void sum_part6(const double *part6, int G, double *sh) {
   if (threadIdx.x < 6) {
     double t = 0.0;
-    for (int c = 0; c < G; ++c) t += part6[6 * c + threadIdx.x];
+    for (int c = 0; c < G; ++c) t += __ldcg(part6 + 6 * c + threadIdx.x);
     sh[threadIdx.x] = t;
   }
   __syncthreads();
@@ -273,7 +276,7 @@ __global__ void __launch_bounds__(kGT) gmres_start_kernel(GmresArgs a) {
   if (!last_cta(a.counters + 1)) return;
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[c];
+    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + c);
     st->norm_rhs = sqrt(t);
     st->iter = 0;
     st->done = 0;
@@ -318,7 +321,7 @@ __global__ void __launch_bounds__(kGT) gmres_residual_kernel(GmresArgs a) {
   sum_part6(a.part6, gridDim.x, sh);
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[c];
+    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + c);
     for (int k = 0; k < 6; ++k) {
       const double r = a.rhs[vel + k] - (-sh[k]);
       q0[vel + k] = r;
@@ -399,7 +402,7 @@ __global__ void __launch_bounds__(kGT) arnoldi_dot1_kernel(GmresArgs a) {
   __syncthreads();
   for (int i = threadIdx.x; i < k; i += blockDim.x) {
     double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[(size_t)c * a.part_stride + i];
+    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + (size_t)c * a.part_stride + i);
     const double *qi = a.Q + (size_t)i * n;
     for (int j = 0; j < 6; ++j) t += w[vel + j] * qi[vel + j];
     a.h1[i] = t;
@@ -429,7 +432,7 @@ __global__ void __launch_bounds__(kGT) arnoldi_dot2_kernel(GmresArgs a) {
   const int ld = a.max_iter + 1;
   for (int i = threadIdx.x; i < k; i += blockDim.x) {
     double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[(size_t)c * a.part_stride + i];
+    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + (size_t)c * a.part_stride + i);
     a.h2[i] = t;
     a.H[i + (size_t)(k - 1) * ld] = a.h1[i] + t;
   }
@@ -460,7 +463,7 @@ __global__ void __launch_bounds__(kGT) arnoldi_norm_kernel(GmresArgs a) {
   if (!last_cta(a.counters + 5)) return;
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += a.part[c];
+    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + c);
     const double qn = sqrt(t);
     st->qnorm = qn;
     const int ld = a.max_iter + 1;
@@ -601,8 +604,8 @@ __global__ void __launch_bounds__(kGT) refine_residual_kernel(GmresArgs a, const
   if (threadIdx.x == 0) {
     double rr = 0.0, bb = 0.0;
     for (int c = 0; c < (int)gridDim.x; ++c) {
-      rr += a.part[2 * c];
-      bb += a.part[2 * c + 1];
+      rr += __ldcg(a.part + 2 * c);
+      bb += __ldcg(a.part + 2 * c + 1);
     }
     for (int k = 0; k < 6; ++k) {
       const double b = a.rhs[vel + k];
