@@ -174,7 +174,10 @@ int tfs_set_body_velocities(tfs_solver *s, const double *v_bodies);
 /* The solved blob forces (f_blobs_host after the reference's GMRES). */
 int tfs_copy_blob_forces_to_host(tfs_solver *s, double *f_blobs_host);
 /* Iterations (summed over refinement cycles), refinement cycles and final
- * relative residual of the last solve. */
+ * relative residual of the last solve. FP32C: a refinement cycle that does
+ * not reduce the FP64 residual ends the refinement and the solve finishes as
+ * plain FP64 GMRES from the caller's warm start; cycles is then negative
+ * (minus the cycles run before). */
 int tfs_solve_info(tfs_solver *s, int *iters, int *cycles, double *rel_residual);
 
 /* --- autotuning ---------------------------------------------------------- */
