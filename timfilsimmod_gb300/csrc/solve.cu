@@ -158,6 +158,59 @@ int poll(tfs_solver *s, int which, GmresScalars *out) {
   return TFS_OK;
 }
 
+// One chunk of Arnoldi steps (preconditioner, M_bb product, CGS2, norm,
+// Givens) as launched by gmres_run. Every kernel reads the step index from
+// the device scalars and skips once the solve is done, so a chunk is the same
+// launch sequence every time for given arguments.
+int launch_chunk(tfs_solver *s, const GmresArgs &g, int fp32) {
+  cudaError_t e;
+  int rc;
+  for (int k = 0; k < s->chunk; ++k) {
+    if ((e = launch_gmres_precond(g, s->stream)) != cudaSuccess)
+      return cuda_fail(e, "gmres preconditioner");
+    if ((rc = mbb_product(s, fp32, &s->gst->done)) != TFS_OK) return rc;
+    if ((e = launch_gmres_arnoldi(g, s->stream)) != cudaSuccess) return cuda_fail(e, "gmres arnoldi");
+  }
+  return TFS_OK;
+}
+
+// The chunk as a CUDA graph, captured on first use for these arguments
+// (nullptr: launch the kernels directly -- kernel timing on, or capture
+// unavailable).
+cudaGraphExec_t chunk_graph(tfs_solver *s, const GmresArgs &g, int fp32, long long *kernels) {
+  if (!s->graphs_enabled || s->timing) return nullptr;
+  const TileTuning tune = s->tune[fp32][C_BB];
+  for (auto &c : s->chunk_graphs)
+    if (c.chunk == s->chunk && c.tune.variant == tune.variant && c.tune.waves == tune.waves &&
+        std::memcmp(&c.args, &g, sizeof g) == 0) {
+      *kernels = c.kernels;
+      return c.exec;
+    }
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const long long before = launch_count();
+  if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    s->graphs_enabled = false;
+    return nullptr;
+  }
+  const int rc = launch_chunk(s, g, fp32);
+  const cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+  const long long recorded = launch_count() - before;
+  count_launch_n(-recorded);  // recorded, not launched
+  if (rc != TFS_OK || e != cudaSuccess || graph == nullptr ||
+      cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+    cudaGetLastError();
+    if (graph) cudaGraphDestroy(graph);
+    s->graphs_enabled = false;
+    return nullptr;
+  }
+  cudaGraphDestroy(graph);
+  s->chunk_graphs.push_back({g, tune, s->chunk, exec, recorded});
+  *kernels = recorded;
+  return exec;
+}
+
 // GMRES on rhs with warm start / solution (f_blobs, v_bodies).
 int gmres_run(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies, double tol,
               int fp32, int *iters) {
@@ -175,12 +228,12 @@ int gmres_run(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodie
   for (int c = 0; c < max_chunks; ++c) {
     if ((rc = poll(s, 0, &h)) != TFS_OK) return rc;
     if (h.done) break;
-    for (int k = 0; k < s->chunk; ++k) {
-      if ((e = launch_gmres_precond(g, s->stream)) != cudaSuccess)
-        return cuda_fail(e, "gmres preconditioner");
-      if ((rc = mbb_product(s, fp32, &st->done)) != TFS_OK) return rc;
-      if ((e = launch_gmres_arnoldi(g, s->stream)) != cudaSuccess)
-        return cuda_fail(e, "gmres arnoldi");
+    long long kernels = 0;
+    if (cudaGraphExec_t exec = chunk_graph(s, g, fp32, &kernels)) {
+      if ((e = cudaGraphLaunch(exec, s->stream)) != cudaSuccess) return cuda_fail(e, "gmres chunk");
+      count_launch_n(kernels);
+    } else if ((rc = launch_chunk(s, g, fp32)) != TFS_OK) {
+      return rc;
     }
   }
   if ((rc = poll(s, 0, &h)) != TFS_OK) return rc;
@@ -385,6 +438,8 @@ int solve_alloc(tfs_solver *s) {
 }
 
 void solve_free(tfs_solver *s) {
+  for (auto &g : s->chunk_graphs) cudaGraphExecDestroy(g.exec);
+  s->chunk_graphs.clear();
   double *bufs[] = {s->refs, s->diff, s->mats, s->Q, s->H, s->beta, s->cs, s->sn, s->y, s->z,
                     s->tmp, s->soln, s->rhs, s->vtmp, s->v_bodies, s->swimmer_f, s->xr, s->r,
                     s->dx, s->gpart, s->gpart6, s->gh1, s->gh2};

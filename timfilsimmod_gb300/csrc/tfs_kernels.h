@@ -84,6 +84,7 @@ int combo_of(int vd, int fda, int fdb);
 
 int num_sms();
 void count_launch();
+void count_launch_n(long long n);  // n may be negative (launches recorded into a graph)
 size_t record_bytes(int fp32, int fd);
 
 cudaError_t launch_origin(const double *xa, int na, const double *xb, int nb, double *out,

@@ -15,6 +15,7 @@
 namespace tfs {
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
+long long launch_count();
 }  // namespace tfs
 
 struct tfs_solver {
@@ -70,6 +71,17 @@ struct tfs_solver {
   // launch tuning per precision and (target, source-set) combination
   tfs::TileTuning tune[2][tfs::kNumCombos];
   std::string tuning_report = "{}";
+  // kernel-sequence GMRES: one chunk of Arnoldi steps captured as a CUDA
+  // graph per argument set (solve.cu), replayed once per chunk
+  struct ChunkGraph {
+    tfs::GmresArgs args;
+    tfs::TileTuning tune;
+    int chunk;
+    cudaGraphExec_t exec;
+    long long kernels;
+  };
+  std::vector<ChunkGraph> chunk_graphs;
+  bool graphs_enabled = true;
   // dominant-kernel timing (tfs_solver_enable_kernel_timing)
   bool timing = false;
   std::vector<cudaEvent_t> events;  // pairs, in launch order
