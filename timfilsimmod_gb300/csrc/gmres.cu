@@ -681,8 +681,13 @@ __global__ void unit_rhs_kernel(double *rhs, int n, int j) {
 // launchers
 // ---------------------------------------------------------------------------
 
+// CTAs of the kernel-sequence GMRES: at least 32 blobs per CTA. Its kernels
+// are latency-bound (a few grid-wide reductions per Arnoldi step); fewer CTAs
+// shorten each last-CTA reduction and leave SMs to other swimmers' streams
+// (measured on GB300: 32 blobs per CTA beats 4 by ~20% per step for 642 and
+// 2562 blobs, results unchanged).
 int gmres_grid(int nb, int sms, int *blobs_per_cta) {
-  int G = std::max(1, std::min(sms, (nb + 3) / 4));
+  int G = std::max(1, std::min(sms, (nb + 31) / 32));
   int per = std::max(1, (nb + G - 1) / G);
   G = std::max(1, (nb + per - 1) / per);
   *blobs_per_cta = per;
