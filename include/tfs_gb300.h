@@ -277,6 +277,30 @@ int tfs_stepper_state(tfs_stepper *st, double *x, double *q, double *u, double *
                       double *tether, double *clamp, double *body_x, double *body_q,
                       double *body_u);
 
+/* --- the reference's data files for the step -------------------------- */
+/* The backup record of the swimmer (swimmer::write_backup: per filament
+ * 9 + 28 NSEG numbers, then 19 for the body; filament.cpp:1952-2037,
+ * rigid_body.cpp:556-579) as doubles, its size, and restoring one (as the
+ * reference reads a backup, filament.cpp:140-215: q^{n-1} = q; Broyden's
+ * memory cleared; the solver's warm start as at creation). */
+int tfs_stepper_backup_size(tfs_stepper *st, size_t *n);
+int tfs_stepper_get_backup(tfs_stepper *st, double *values);
+int tfs_stepper_set_backup(tfs_stepper *st, const double *values);
+/* The reference's text files, formatted as its streams write them
+ * (std::scientific, 10 digits): the backup "<save_step> <values...>"
+ * (cilia_sim_main.cu:590-597), overwritten; reading one checks the count
+ * and restores it (*save_step = the step to run next,
+ * cilia_sim_main.cu:336-350). */
+int tfs_stepper_write_backup(tfs_stepper *st, int save_step, const char *path);
+int tfs_stepper_read_backup(tfs_stepper *st, const char *path, int *save_step);
+/* A plot step after step nt (cilia_sim_main.cu:563-600): appends one record
+ * to <prefix>_seg_states.dat, _body_states.dat, _tether_force.dat (step
+ * nt+1) and, as mobility_solver::write_data (mobility_solver.cpp:3051-3173),
+ * to _body_vels.dat, _blob_forces.dat, _seg_vels.dat, _seg_forces.dat (step
+ * nt; segment forces before barrier forces, as the reference's host copy);
+ * backup != 0 also writes <prefix>.backup. */
+int tfs_stepper_write_files(tfs_stepper *st, int nt, const char *prefix, int backup);
+
 /* --- many swimmers: batches and a request server ---------------------- */
 /* No counterpart in the reference (one swimmer set per process). Each
  * swimmer is an instance -- its own tfs_solver and tfs_stepper on its own

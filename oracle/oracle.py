@@ -419,6 +419,10 @@ class ReferenceStep:
         it = self.lib.ref_step_run(int(nt), ctypes.byref(g))
         return it, g.value
 
+    def write_files(self, prefix, nt):
+        """The reference's own plot-step writers after step nt (data files and backup)."""
+        self.lib.ref_step_write_files(prefix.encode(), int(nt))
+
     def state(self):
         ns, nf, sg = self.ns, self.nfil, self.nseg
         out = dict(x=np.zeros(3 * ns), q=np.zeros(4 * ns), u=np.zeros(3 * ns),

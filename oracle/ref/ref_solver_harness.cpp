@@ -19,6 +19,8 @@
 //   - stubs for the seeding functions (seeding.cu needs a GPU), which the
 //     harness never calls: geometry is injected directly.
 #include <cmath>
+#include <fstream>
+#include <iomanip>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -469,6 +471,40 @@ void ref_step_state(double *x, double *q, double *u, double *lambda, double *tet
   for (int k = 0; k < 3; ++k) { body_x[k] = s.body.x[k]; body_u[k] = s.body.u[k]; }
   body_q[0] = s.body.q.scalar_part;
   for (int k = 0; k < 3; ++k) body_q[1 + k] = s.body.q.vector_part[k];
+}
+
+// The reference's own writers at a plot step after step nt, in the order
+// its main loop calls them (cilia_sim_main.cu:563-600): swimmer::write_data
+// into <prefix>_seg_states.dat, _body_states.dat, _tether_force.dat (step
+// nt+1), mobility_solver::write_data into the velocity and force files (step
+// nt), swimmer::write_backup into <prefix>.backup. File names as
+// cilia_sim_main.cu:94-102 derives them.
+void ref_step_write_files(const char *prefix, int nt) {
+  swimmer &s = (*g_swimmers)[0];
+  SIMULATION_NAME = prefix;
+  SIMULATION_BACKUP_NAME = SIMULATION_NAME + ".backup";
+  SIMULATION_BODY_STATE_NAME = SIMULATION_NAME + "_body_states.dat";
+  SIMULATION_SEG_STATE_NAME = SIMULATION_NAME + "_seg_states.dat";
+  SIMULATION_BODY_VEL_NAME = SIMULATION_NAME + "_body_vels.dat";
+  SIMULATION_SEG_VEL_NAME = SIMULATION_NAME + "_seg_vels.dat";
+  SIMULATION_BLOB_FORCES_NAME = SIMULATION_NAME + "_blob_forces.dat";
+  SIMULATION_SEG_FORCES_NAME = SIMULATION_NAME + "_seg_forces.dat";
+  SIMULATION_TETHERLAM_NAME = SIMULATION_NAME + "_tether_force.dat";
+  const int save_step = nt + 1;
+  std::ofstream seg(SIMULATION_SEG_STATE_NAME, std::ios::app);
+  std::ofstream body(SIMULATION_BODY_STATE_NAME, std::ios::app);
+  std::ofstream tether(SIMULATION_TETHERLAM_NAME, std::ios::app);
+  for (std::ofstream *f : {&seg, &body, &tether}) *f << save_step << " " << std::scientific << std::setprecision(10);
+  s.write_data(seg, body, tether);
+  for (std::ofstream *f : {&seg, &body, &tether}) *f << std::endl;
+  seg.close();
+  body.close();
+  tether.close();
+  g_solver->write_data(nt, *g_swimmers);
+  std::ofstream backup(SIMULATION_BACKUP_NAME);
+  backup << save_step << " " << std::scientific << std::setprecision(10);
+  s.write_backup(backup);
+  backup << std::endl;
 }
 
 }  // extern "C"

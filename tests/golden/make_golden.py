@@ -243,8 +243,43 @@ def case_step():
     return res
 
 
+def case_step_io():
+    """The reference's data files and backup (its own writers) after steps
+    0-2 of a small swimmer (162 blobs, R = 10, 3 filaments x 14 segments),
+    written to tests/golden/step_io/ref*, and the states after steps 3 and 4
+    continuing from there."""
+    from timfilsimmod_gb300.geometry import icosphere
+
+    radius, nfil, nseg = 10.0, 3, 14
+    blob_refs = radius * icosphere(2)
+    normals = fibonacci_sphere(nfil)
+    fil_refs = (radius + 1.0 + 1.1) * normals
+    efm = 220.0 * 1800.0 / (2.6 * 2.6 * nseg ** 2)
+    ref = ReferenceStep(nfil, nseg, blob_refs, fil_refs, normals, efm, seg_sep=2.2,
+                        body_length=2.0 * radius)
+    ref.make_body_reference_matrices()
+    d = os.path.join(OUT, "step_io")
+    os.makedirs(d, exist_ok=True)
+    for f in os.listdir(d):
+        if f.startswith("ref"):
+            os.remove(os.path.join(d, f))
+    broy = [ref.run(nt)[0] for nt in range(3)]
+    ref.write_files(os.path.join(d, "ref"), 2)
+    later = []
+    for nt in (3, 4):
+        broy.append(ref.run(nt)[0])
+        later.append(ref.state())
+    res = dict(blob_refs=blob_refs, fil_refs=fil_refs, fil_dirs=normals, nfil=nfil, nseg=nseg,
+               end_force_magnitude_real=efm, body_radius=radius, dt=1e-3, tol=1e-4,
+               linear_tol=ref.lib.ref_linear_system_tol(), broyden_iters=np.array(broy))
+    for i, st in enumerate(later):
+        res.update({f"after{3 + i}_{k}": v for k, v in st.items()})
+    return res
+
+
 CASES = {"small_matvec": case_small, "overlap_a16": case_overlap, "tiny": case_tiny,
-         "flow_small": case_flow, "solve_small": case_solve, "step_small": case_step}
+         "flow_small": case_flow, "solve_small": case_solve, "step_small": case_step,
+         "step_io": case_step_io}
 
 
 def main():

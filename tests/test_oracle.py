@@ -201,3 +201,28 @@ def test_oracle_flow_matches_reference_build():
         b = r.flow_velocities(xf, sw.x_segs, sw.f_segs, sw.num_segs, sw.x_blobs, sw.f_blobs, nb,
                               xbod, 0.04, rnf)
         assert rel(a, b) < TOL
+
+
+def test_reference_data_files_have_the_record_layout():
+    """The reference's plot-step files and backup (tests/golden/step_io/ref*,
+    written by its own swimmer::write_data / write_backup and
+    mobility_solver::write_data) have the record sizes the C ABI writer
+    follows: backup 1 + NFIL (9 + 28 NSEG) + 19 numbers, one quaternion per
+    segment, body x and q, a tether force per filament, 6 velocities or
+    forces per segment, 3 forces per blob, 6 body velocities."""
+    d = np.load(os.path.join(GOLD, "step_io.npz"))
+    nfil, nseg, nb = int(d["nfil"]), int(d["nseg"]), d["blob_refs"].shape[0]
+    ns = nfil * nseg
+    io = os.path.join(GOLD, "step_io", "ref")
+    sizes = {".backup": 1 + nfil * (9 + 28 * nseg) + 19, "_seg_states.dat": 1 + 4 * ns,
+             "_body_states.dat": 1 + 7, "_tether_force.dat": 1 + 3 * nfil,
+             "_seg_vels.dat": 1 + 6 * ns, "_seg_forces.dat": 1 + 6 * ns,
+             "_blob_forces.dat": 1 + 3 * nb, "_body_vels.dat": 6}
+    for suffix, n in sizes.items():
+        text = open(io + suffix).read()
+        assert text.endswith(" \n") and text.count("\n") == 1, suffix
+        toks = text.split()
+        assert len(toks) == n, (suffix, len(toks), n)
+        if suffix != "_body_vels.dat":
+            assert toks[0] in ("2", "3"), suffix  # step nt = 2, save step 3
+            assert all(len(t.split("e")[0].split(".")[-1]) == 10 for t in toks[1:]), suffix

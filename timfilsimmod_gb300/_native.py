@@ -162,6 +162,12 @@ _SIGNATURES = {
     "tfs_stepper_end_of_iter": [_H, ctypes.c_int, ctypes.c_int],
     "tfs_stepper_state": [_H, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "tfs_stepper_reset": [_H, _P],
+    "tfs_stepper_backup_size": [_H, ctypes.POINTER(ctypes.c_size_t)],
+    "tfs_stepper_get_backup": [_H, _P],
+    "tfs_stepper_set_backup": [_H, _P],
+    "tfs_stepper_write_backup": [_H, ctypes.c_int, ctypes.c_char_p],
+    "tfs_stepper_read_backup": [_H, ctypes.c_char_p, _IP],
+    "tfs_stepper_write_files": [_H, ctypes.c_int, ctypes.c_char_p, ctypes.c_int],
     "tfs_batch_create": [ctypes.c_int, ctypes.POINTER(_H)],
     "tfs_batch_destroy": [_H],
     "tfs_batch_add": [_H, _H, _IP],

@@ -1597,6 +1597,164 @@ int tfs_stepper_reset(tfs_stepper *st, const double *seg_rotation) {
 }  // extern "C"
 
 namespace tfs {
+// The reference's backup record of one swimmer (filament::write_backup,
+// filament.cpp:1952-2037, then rigid_body::write_backup, rigid_body.cpp:
+// 556-579): per filament, per segment q, x, xm1, xm2, u, um1; tether, clamp
+// multipliers with their two previous values; per link the multiplier and
+// its two previous values; then the body's q, x, xm1, xm2, u, um1.
+size_t backup_values(const tfs_stepper *st) {
+  return (size_t)st->d.nfil * (9 + 28 * (size_t)st->d.nseg) + 19;
+}
+
+int stepper_backup(tfs_stepper *st, std::vector<double> &out) {
+  const StepDev &d = st->d;
+  const size_t ns = d.ns, nf = d.nfil, nl = 3 * (size_t)(d.nseg - 1) * nf;
+  std::vector<double> q(4 * ns), x(3 * ns), xm1(3 * ns), xm2(3 * ns), u(3 * ns), um1(3 * ns),
+      t0(3 * nf), t1(3 * nf), t2(3 * nf), c0(3 * nf), c1(3 * nf), c2(3 * nf), l0(nl), l1(nl), l2(nl);
+  struct C {
+    double *dst;
+    const double *src;
+    size_t n;
+  } copies[] = {{q.data(), d.q, 4 * ns},         {x.data(), d.x, 3 * ns},
+                {xm1.data(), d.xm1, 3 * ns},     {xm2.data(), d.xm2, 3 * ns},
+                {u.data(), d.u, 3 * ns},         {um1.data(), d.um1, 3 * ns},
+                {t0.data(), d.teth, 3 * nf},     {t1.data(), d.tethm1, 3 * nf},
+                {t2.data(), d.tethm2, 3 * nf},   {c0.data(), d.clamp, 3 * nf},
+                {c1.data(), d.clampm1, 3 * nf},  {c2.data(), d.clampm2, 3 * nf},
+                {l0.data(), d.lam, nl},          {l1.data(), d.lamm1, nl},
+                {l2.data(), d.lamm2, nl}};
+  cudaStream_t str = st->s->stream;
+  for (auto &c : copies)
+    ST_CUDA(cudaMemcpyAsync(c.dst, c.src, sizeof(double) * c.n, cudaMemcpyDeviceToHost, str), "backup");
+  ST_CUDA(cudaStreamSynchronize(str), "backup");
+  out.clear();
+  out.reserve(backup_values(st));
+  auto put3 = [&](const std::vector<double> &v, size_t i) {
+    out.push_back(v[3 * i]);
+    out.push_back(v[3 * i + 1]);
+    out.push_back(v[3 * i + 2]);
+  };
+  for (size_t f = 0; f < nf; ++f) {
+    for (int j = 0; j < d.nseg; ++j) {
+      const size_t sg = f * d.nseg + j;
+      for (int k = 0; k < 4; ++k) out.push_back(q[4 * sg + k]);
+      put3(x, sg);
+      put3(xm1, sg);
+      put3(xm2, sg);
+      put3(u, sg);
+      put3(um1, sg);
+    }
+    put3(t0, f);
+    put3(t1, f);
+    put3(t2, f);
+    put3(c0, f);
+    put3(c1, f);
+    put3(c2, f);
+    for (int j = 0; j < d.nseg - 1; ++j) {
+      const size_t l = f * (d.nseg - 1) + j;
+      put3(l0, l);
+      put3(l1, l);
+      put3(l2, l);
+    }
+  }
+  for (int k = 0; k < 4; ++k) out.push_back(st->bq[k]);
+  for (int k = 0; k < 3; ++k) out.push_back(st->bx[k]);
+  for (int k = 0; k < 3; ++k) out.push_back(st->bxm1[k]);
+  for (int k = 0; k < 3; ++k) out.push_back(st->bxm2[k]);
+  for (int k = 0; k < 3; ++k) out.push_back(st->bu[k]);
+  for (int k = 0; k < 3; ++k) out.push_back(st->bum1[k]);
+  return TFS_OK;
+}
+
+// Restore a backup record (as filament::initial_setup and
+// rigid_body::initial_setup read one, filament.cpp:140-215,
+// rigid_body.cpp:16-60: q^{n-1} = q); Broyden's memory is cleared and the
+// solver's warm start is the one it had when the stepper was created.
+int stepper_load(tfs_stepper *st, const double *v) {
+  const StepDev &d = st->d;
+  const size_t ns = d.ns, nf = d.nfil, nl = 3 * (size_t)(d.nseg - 1) * nf;
+  std::vector<double> q(4 * ns), x(3 * ns), xm1(3 * ns), xm2(3 * ns), u(3 * ns), um1(3 * ns),
+      t0(3 * nf), t1(3 * nf), t2(3 * nf), c0(3 * nf), c1(3 * nf), c2(3 * nf), l0(nl), l1(nl), l2(nl);
+  size_t p = 0;
+  auto get3 = [&](std::vector<double> &w, size_t i) {
+    w[3 * i] = v[p++];
+    w[3 * i + 1] = v[p++];
+    w[3 * i + 2] = v[p++];
+  };
+  for (size_t f = 0; f < nf; ++f) {
+    for (int j = 0; j < d.nseg; ++j) {
+      const size_t sg = f * d.nseg + j;
+      for (int k = 0; k < 4; ++k) q[4 * sg + k] = v[p++];
+      get3(x, sg);
+      get3(xm1, sg);
+      get3(xm2, sg);
+      get3(u, sg);
+      get3(um1, sg);
+    }
+    get3(t0, f);
+    get3(t1, f);
+    get3(t2, f);
+    get3(c0, f);
+    get3(c1, f);
+    get3(c2, f);
+    for (int j = 0; j < d.nseg - 1; ++j) {
+      const size_t l = f * (d.nseg - 1) + j;
+      get3(l0, l);
+      get3(l1, l);
+      get3(l2, l);
+    }
+  }
+  for (int k = 0; k < 4; ++k) st->bq[k] = st->bqm1[k] = v[p++];
+  for (int k = 0; k < 3; ++k) st->bx[k] = v[p++];
+  for (int k = 0; k < 3; ++k) st->bxm1[k] = v[p++];
+  for (int k = 0; k < 3; ++k) st->bxm2[k] = v[p++];
+  for (int k = 0; k < 3; ++k) st->bu[k] = v[p++];
+  for (int k = 0; k < 3; ++k) st->bum1[k] = v[p++];
+  rot_rm(st->bq, st->Qinit);
+  struct C {
+    double *dst;
+    const double *src;
+    size_t n;
+  } copies[] = {{d.q, q.data(), 4 * ns},        {d.qm1, q.data(), 4 * ns},
+                {d.x, x.data(), 3 * ns},        {d.xm1, xm1.data(), 3 * ns},
+                {d.xm2, xm2.data(), 3 * ns},    {d.u, u.data(), 3 * ns},
+                {d.um1, um1.data(), 3 * ns},    {d.teth, t0.data(), 3 * nf},
+                {d.tethm1, t1.data(), 3 * nf},  {d.tethm2, t2.data(), 3 * nf},
+                {d.clamp, c0.data(), 3 * nf},   {d.clampm1, c1.data(), 3 * nf},
+                {d.clampm2, c2.data(), 3 * nf}, {d.lam, l0.data(), nl},
+                {d.lamm1, l1.data(), nl},       {d.lamm2, l2.data(), nl}};
+  tfs_solver *s = st->s;
+  for (auto &c : copies)
+    ST_CUDA(cudaMemcpyAsync(c.dst, c.src, sizeof(double) * c.n, cudaMemcpyHostToDevice, s->stream),
+            "restore");
+  ST_CUDA(cudaMemcpyAsync(s->f_blobs, st->warm, sizeof(double) * 3 * s->nb, cudaMemcpyDeviceToDevice,
+                          s->stream),
+          "warm start");
+  ST_CUDA(cudaMemcpyAsync(s->v_bodies, st->warm + 3 * s->nb, sizeof(double) * 6,
+                          cudaMemcpyDeviceToDevice, s->stream),
+          "warm start");
+  ST_CUDA(cudaStreamSynchronize(s->stream), "restore");
+  st->iter = 0;
+  st->jac_ready = 0;
+  s->origin_dirty = true;
+  return TFS_OK;
+}
+
+// Internal forces (the reference's f_segs_host, before barrier forces) to the host.
+int stepper_internal_forces(tfs_stepper *st, double *f) {
+  ST_CUDA(cudaMemcpyAsync(f, st->d.f, sizeof(double) * 6 * st->d.ns, cudaMemcpyDeviceToHost,
+                          st->s->stream),
+          "internal forces");
+  ST_CUDA(cudaStreamSynchronize(st->s->stream), "internal forces");
+  return TFS_OK;
+}
+
+int stepper_dims(const tfs_stepper *st, int *nfil, int *nseg) {
+  *nfil = st->d.nfil;
+  *nseg = st->d.nseg;
+  return TFS_OK;
+}
+
 tfs_solver *stepper_solver(tfs_stepper *st) { return st ? st->s : nullptr; }
 long stepper_segments(const tfs_stepper *st) { return st ? (long)st->d.ns : 0; }
 }  // namespace tfs

@@ -166,6 +166,32 @@ class ImplicitStepper:
                 raise ValueError("seg_rotation needs 3 values per segment")
             N.check(self._call("tfs_stepper_reset", _p(r)))
 
+    # -- the reference's data files ------------------------------------------------
+    def backup(self) -> np.ndarray:
+        """The swimmer's backup record (swimmer::write_backup order)."""
+        n = ctypes.c_size_t(0)
+        N.check(self._call("tfs_stepper_backup_size", ctypes.byref(n)))
+        v = np.zeros(n.value)
+        N.check(self._call("tfs_stepper_get_backup", _p(v)))
+        return v
+
+    def restore(self, values) -> None:
+        v = _f64(values)
+        N.check(self._call("tfs_stepper_set_backup", _p(v)))
+
+    def write_backup(self, save_step: int, path: str) -> None:
+        N.check(self._call("tfs_stepper_write_backup", int(save_step), path.encode()))
+
+    def read_backup(self, path: str) -> int:
+        """Restore from a backup file; returns the step to run next."""
+        step = ctypes.c_int(0)
+        N.check(self._call("tfs_stepper_read_backup", path.encode(), ctypes.byref(step)))
+        return step.value
+
+    def write_files(self, nt: int, prefix: str, backup: bool = True) -> None:
+        """The reference's plot-step records after step nt (and the backup)."""
+        N.check(self._call("tfs_stepper_write_files", int(nt), prefix.encode(), int(bool(backup))))
+
     def state(self) -> dict:
         ns, nf, sg = self.ns, self.nfil, self.nseg
         out = dict(x=np.zeros(3 * ns), q=np.zeros(4 * ns), u=np.zeros(3 * ns),
