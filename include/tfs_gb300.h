@@ -359,7 +359,9 @@ int tfs_server_create(const tfs_server_config *cfg, tfs_server **out);
 int tfs_server_submit(tfs_server *sv, const tfs_request *r, long long *ticket);
 /* *status: 1 while pending, else the request's TFS status (the ticket is
  * then released; a failed request's message becomes the calling thread's
- * tfs_last_error()). wait != 0 blocks until it completes. latency_ms:
+ * tfs_last_error()). TFS_ENOTCONV: Broyden's method reached its cap at some
+ * step; the run stopped there, as the reference's does, and x_out/body_out
+ * hold that state. wait != 0 blocks until it completes. latency_ms:
  * arrival to completion. */
 int tfs_server_poll(tfs_server *sv, long long ticket, int wait, int *status, double *latency_ms,
                     int *broyden_iters, int *gmres_iters);

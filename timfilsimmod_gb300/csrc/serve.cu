@@ -346,13 +346,18 @@ void tfs_server::worker() {
       rc = tfs_stepper_step(in->st, nt, &b, &gm);
       bsum += b;
       gsum += gm;
-      if (rc == TFS_ENOTCONV) rc = TFS_OK;  // the reference carries on past MAX_BROYDEN_ITER
     }
-    if (rc == TFS_OK)
-      rc = tfs_stepper_state(in->st, q->r.x_out, nullptr, nullptr, nullptr, nullptr, nullptr,
-                             q->r.body_out, q->r.body_out ? q->r.body_out + 3 : nullptr, nullptr);
-    const bool drop = rc != TFS_OK;  // an instance that failed is not reused
-    const std::string fail_msg = drop ? std::string(tfs_last_error()) : std::string();
+    // Broyden's method at its iteration cap ends the run, as the reference
+    // stops there (cilia_sim_main.cu:542-557); the state so far is returned
+    const bool unconverged = rc == TFS_ENOTCONV;
+    if (rc == TFS_OK || unconverged) {
+      const int rs = tfs_stepper_state(in->st, q->r.x_out, nullptr, nullptr, nullptr, nullptr,
+                                       nullptr, q->r.body_out,
+                                       q->r.body_out ? q->r.body_out + 3 : nullptr, nullptr);
+      if (rs != TFS_OK) rc = rs;
+    }
+    const bool drop = rc != TFS_OK && !(unconverged && rc == TFS_ENOTCONV);  // broken: not reused
+    const std::string fail_msg = rc != TFS_OK ? std::string(tfs_last_error()) : std::string();
     if (drop) {
       g.lock();
       pool.erase(std::find(pool.begin(), pool.end(), in));
