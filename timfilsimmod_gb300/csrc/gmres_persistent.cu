@@ -292,7 +292,7 @@ __device__ void mbb_units(const PgArgs &p, float *src) {
       __syncthreads();
       if (!warp_active) continue;
       float v[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-      unsigned nl[2] = {0u, 0u};
+      unsigned nf[2] = {0u, 0u};
 #pragma unroll 2
       for (int j = 0; j < cnt; ++j) {
         float sx, sy, sz, f[3];
@@ -302,13 +302,13 @@ __device__ void mbb_units(const PgArgs &p, float *src) {
           const float dx = xt[t] - sx, dy = yt[t] - sy, dz = zt[t] - sz;
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
           const bool far = r2 > pc.asum2;
-          if (!far) nl[t] = NearList::push(nl[t], j);
+          nf[t] |= far ? 0u : 1u;
           const float rs = rsqrt_far(r2);
           far_pair<float, 3, 3>(v[t], dx, dy, dz, far ? rs : 0.f, f, pc);
         }
       }
-      if (__any_sync(0xffffffffu, (nl[0] | nl[1]) != 0u))
-        near_pass<float, 3, 3, 2>(v, xt, yt, zt, nl, src, cnt, pc);
+      if (__any_sync(0xffffffffu, (nf[0] | nf[1]) != 0u))
+        near_pass<float, 3, 3, 2>(v, xt, yt, zt, nf, src, cnt, pc);
 #pragma unroll
       for (int t = 0; t < 2; ++t)
 #pragma unroll

@@ -113,45 +113,23 @@ struct Comp<float, VD, BLOCK, TPT> {
   }
 };
 
-// Near pairs met in one tile, per target: up to two source indices within
-// the tile (< 256) and their count packed in one word; bit 18 marks a third.
-struct NearList {
-  __device__ static __forceinline__ unsigned push(unsigned n, int j) {
-    const unsigned c = (n >> 16) & 3u;
-    return c < 2u ? ((n & ~(3u << 16)) | ((unsigned)j << (8 * c)) | ((c + 1u) << 16))
-                  : (n | (1u << 18));
-  }
-  __device__ static __forceinline__ int count(unsigned n) { return (n >> 16) & 3; }
-  __device__ static __forceinline__ bool overflow(unsigned n) { return (n >> 18) & 1u; }
-  __device__ static __forceinline__ int index(unsigned n, int q) { return (n >> (8 * q)) & 255; }
-};
-
-// The exact three-regime pairs of one tile that the far-field pass skipped:
-// each lane evaluates its own recorded pairs (all lanes at once); a target
-// with more than two (overlapping particles) rescans the tile.
+// The exact three-regime pairs of one tile that the far-field pass skipped
+// (r^2 <= (ai+aj)^2: self, overlapping or touching particles): a lane whose
+// target met one rescans the tile and evaluates them in source order.
 template <typename T, int VD, int FD, int TPT>
 __device__ __forceinline__ void near_pass(T (&v)[TPT][VD], const T (&xt)[TPT], const T (&yt)[TPT],
-                                          const T (&zt)[TPT], const unsigned (&nl)[TPT],
+                                          const T (&zt)[TPT], const unsigned (&nf)[TPT],
                                           const T *smem, int cnt, const PairConst<T> &pc) {
   constexpr int L = Rec<T, FD>::len;
 #pragma unroll
   for (int t = 0; t < TPT; ++t) {
-    if (nl[t] == 0u) continue;
-    if (!NearList::overflow(nl[t])) {
-      for (int q = 0; q < NearList::count(nl[t]); ++q) {
-        T sx, sy, sz, f[FD];
-        RecLoad<T, FD>::get(smem + NearList::index(nl[t], q) * L, sx, sy, sz, f);
-        const T dx = xt[t] - sx, dy = yt[t] - sy, dz = zt[t] - sz;
-        near_pair<T, VD, FD>(v[t], dx, dy, dz, fma(dx, dx, fma(dy, dy, dz * dz)), f, pc);
-      }
-    } else {
-      for (int j = 0; j < cnt; ++j) {
-        T sx, sy, sz, f[FD];
-        RecLoad<T, FD>::get(smem + j * L, sx, sy, sz, f);
-        const T dx = xt[t] - sx, dy = yt[t] - sy, dz = zt[t] - sz;
-        const T r2 = fma(dx, dx, fma(dy, dy, dz * dz));
-        if (!(r2 > pc.asum2)) near_pair<T, VD, FD>(v[t], dx, dy, dz, r2, f, pc);
-      }
+    if (nf[t] == 0u) continue;
+    for (int j = 0; j < cnt; ++j) {
+      T sx, sy, sz, f[FD];
+      RecLoad<T, FD>::get(smem + j * L, sx, sy, sz, f);
+      const T dx = xt[t] - sx, dy = yt[t] - sy, dz = zt[t] - sz;
+      const T r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+      if (!(r2 > pc.asum2)) near_pair<T, VD, FD>(v[t], dx, dy, dz, r2, f, pc);
     }
   }
 }
@@ -160,11 +138,11 @@ __device__ __forceinline__ void near_pass(T (&v)[TPT][VD], const T (&xt)[TPT], c
 //
 // Far-field pass (every pair): the far-field formula without a branch; pairs
 // inside the contact distance (r^2 <= (ai+aj)^2, which includes self pairs)
-// get 1/r = 0, which zeroes every far-field term, and their source index is
-// recorded for the target. After the tile, each lane evaluates its recorded
-// pairs with the exact three-regime formula (near_pass), all lanes in
-// parallel. In the swimmer configurations only the tiles that hold a
-// target's own particle or a touching neighbour record anything.
+// get 1/r = 0, which zeroes every far-field term, and set a per-target flag
+// (one logic op per pair). After the tile, a flagged lane rescans it and adds
+// those pairs with the exact three-regime formula (near_pass). In the swimmer
+// configurations only the tiles that hold a target's own particle or a
+// touching neighbour flag anything.
 template <typename T, int VD, int FD, int BLOCK, int TPT, int TS>
 __device__ __forceinline__ void sum_source_range(T (&v)[TPT][VD], const T (&xt)[TPT],
                                                  const T (&yt)[TPT], const T (&zt)[TPT],
@@ -181,9 +159,9 @@ __device__ __forceinline__ void sum_source_range(T (&v)[TPT][VD], const T (&xt)[
     const int nvec = cnt * VEC_PER_REC;
     for (int q = threadIdx.x; q < nvec; q += BLOCK) dst[q] = __ldg(src + q);
     __syncthreads();
-    unsigned nl[TPT];
+    unsigned nf[TPT];
 #pragma unroll
-    for (int t = 0; t < TPT; ++t) nl[t] = 0u;
+    for (int t = 0; t < TPT; ++t) nf[t] = 0u;
 #pragma unroll 2
     for (int j = 0; j < cnt; ++j) {
       T sx, sy, sz, f[FD];
@@ -193,15 +171,15 @@ __device__ __forceinline__ void sum_source_range(T (&v)[TPT][VD], const T (&xt)[
         const T dx = xt[t] - sx, dy = yt[t] - sy, dz = zt[t] - sz;
         const T r2 = fma(dx, dx, fma(dy, dy, dz * dz));
         const bool far = r2 > pc.asum2;
-        if (!far) nl[t] = NearList::push(nl[t], j);
+        nf[t] |= far ? 0u : 1u;
         const T rs = rsqrt_far(r2);
         far_pair<T, VD, FD>(v[t], dx, dy, dz, far ? rs : T(0), f, pc);
       }
     }
     unsigned any = 0u;
 #pragma unroll
-    for (int t = 0; t < TPT; ++t) any |= nl[t];
-    if (__any_sync(0xffffffffu, any != 0u)) near_pass<T, VD, FD, TPT>(v, xt, yt, zt, nl, smem, cnt, pc);
+    for (int t = 0; t < TPT; ++t) any |= nf[t];
+    if (__any_sync(0xffffffffu, any != 0u)) near_pass<T, VD, FD, TPT>(v, xt, yt, zt, nf, smem, cnt, pc);
     Comp<T, VD, BLOCK, TPT>::fold(v, hl);
   }
 }
