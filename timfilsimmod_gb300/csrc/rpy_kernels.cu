@@ -38,44 +38,65 @@ namespace tfs {
 // particles of max |x_k - origin_k|. One CTA; used for FP32 centring and for
 // the FP32 candidate test of the barrier kernel.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) origin_kernel(const double *__restrict__ xa, int na,
+constexpr int kOriginCTAs = 64;
+
+// Two passes over all particles, kOriginCTAs CTAs each: pass 0 sums the
+// positions (the mean goes to out[0..2]), pass 1 takes the largest
+// |x_k - o_k| (out[3]). Per-CTA partials live in out[4..], the last CTA to
+// finish combines them in CTA order (deterministic).
+__global__ void __launch_bounds__(256) origin_kernel(const double *__restrict__ xa, int na,
                                                      const double *__restrict__ xb, int nb,
-                                                     double *__restrict__ out /* [4] */) {
-  __shared__ double red[512][3];
-  const int tid = threadIdx.x;
+                                                     double *__restrict__ out /* [4 + 4 kOriginCTAs] */,
+                                                     unsigned *__restrict__ counter, int pass) {
+  __shared__ double red[256][3];
+  __shared__ bool last;
+  const int tid = threadIdx.x, n = na + nb;
+  double *part = out + 4;
   double s[3] = {0, 0, 0};
-  for (int i = tid; i < na; i += blockDim.x)
-    for (int k = 0; k < 3; ++k) s[k] += xa[3 * (size_t)i + k];
-  for (int i = tid; i < nb; i += blockDim.x)
-    for (int k = 0; k < 3; ++k) s[k] += xb[3 * (size_t)i + k];
+  double o[3] = {0, 0, 0};
+  if (pass == 1)
+    for (int k = 0; k < 3; ++k) o[k] = out[k];
+  for (int i = blockIdx.x * blockDim.x + tid; i < n; i += gridDim.x * blockDim.x) {
+    const double *x = i < na ? xa + 3 * (size_t)i : xb + 3 * (size_t)(i - na);
+    if (pass == 0) {
+      for (int k = 0; k < 3; ++k) s[k] += x[k];
+    } else {
+      for (int k = 0; k < 3; ++k) s[0] = fmax(s[0], fabs(x[k] - o[k]));
+    }
+  }
   for (int k = 0; k < 3; ++k) red[tid][k] = s[k];
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (tid < w)
-      for (int k = 0; k < 3; ++k) red[tid][k] += red[tid + w][k];
-    __syncthreads();
-  }
-  const int n = na + nb;
-  double o[3];
-  for (int k = 0; k < 3; ++k) o[k] = n > 0 ? red[0][k] / n : 0.0;
-  __syncthreads();
-  double m = 0.0;
-  for (int i = tid; i < na; i += blockDim.x)
-    for (int k = 0; k < 3; ++k) m = fmax(m, fabs(xa[3 * (size_t)i + k] - o[k]));
-  for (int i = tid; i < nb; i += blockDim.x)
-    for (int k = 0; k < 3; ++k) m = fmax(m, fabs(xb[3 * (size_t)i + k] - o[k]));
-  red[tid][0] = m;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (tid < w) red[tid][0] = fmax(red[tid][0], red[tid + w][0]);
+    if (tid < w) {
+      if (pass == 0)
+        for (int k = 0; k < 3; ++k) red[tid][k] += red[tid + w][k];
+      else
+        red[tid][0] = fmax(red[tid][0], red[tid + w][0]);
+    }
     __syncthreads();
   }
   if (tid == 0) {
-    out[0] = o[0];
-    out[1] = o[1];
-    out[2] = o[2];
-    out[3] = red[0][0];
+    if (pass == 0)
+      for (int k = 0; k < 3; ++k) part[3 * blockIdx.x + k] = red[0][k];
+    else
+      part[3 * kOriginCTAs + blockIdx.x] = red[0][0];
+    __threadfence();
+    last = atomicAdd(counter + pass, 1u) == gridDim.x - 1;
   }
+  __syncthreads();
+  if (!last || tid != 0) return;
+  __threadfence();
+  if (pass == 0) {
+    double t[3] = {0, 0, 0};
+    for (int c = 0; c < (int)gridDim.x; ++c)
+      for (int k = 0; k < 3; ++k) t[k] += __ldcg(part + 3 * c + k);
+    for (int k = 0; k < 3; ++k) out[k] = n > 0 ? t[k] / n : 0.0;
+  } else {
+    double m = 0.0;
+    for (int c = 0; c < (int)gridDim.x; ++c) m = fmax(m, __ldcg(part + 3 * kOriginCTAs + c));
+    out[3] = m;
+  }
+  counter[pass] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -244,11 +265,16 @@ cudaError_t launch_reduce_partials(double *out, const double *partial, int n_ele
 }
 
 cudaError_t launch_origin(const double *xa, int na, const double *xb, int nb, double *out,
-                          cudaStream_t st) {
-  origin_kernel<<<1, 512, 0, st>>>(xa, na, xb, nb, out);
-  count_launch();
+                          unsigned *counter, cudaStream_t st) {
+  const int ctas = std::max(1, std::min(kOriginCTAs, (na + nb + 255) / 256));
+  for (int pass = 0; pass < 2; ++pass) {
+    origin_kernel<<<ctas, 256, 0, st>>>(xa, na, xb, nb, out, counter, pass);
+    count_launch();
+  }
   return cudaGetLastError();
 }
+
+size_t origin_elems() { return 4 + 4 * (size_t)kOriginCTAs; }
 
 template <typename T, int FD>
 static cudaError_t pack_t(void *rec, const double *x, const double *f, int n,

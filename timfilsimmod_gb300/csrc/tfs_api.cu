@@ -94,6 +94,7 @@ static void free_all(tfs_solver *s) {
   cudaFree(s->v_blobs);
   cudaFree(s->f_rep);
   cudaFree(s->origin);
+  cudaFree(s->origin_cnt);
   cudaFree(s->rec_segs);
   cudaFree(s->rec_blobs);
   cudaFree(s->rec_segs_x2);
@@ -114,7 +115,8 @@ int tfs::alloc_dev(void **p, size_t bytes) {
 
 int tfs::ensure_origin(tfs_solver *s) {
   if (!s->origin_dirty) return TFS_OK;
-  cudaError_t e = launch_origin(s->x_segs, s->ns, s->x_blobs, s->nb, s->origin, s->stream);
+  cudaError_t e = launch_origin(s->x_segs, s->ns, s->x_blobs, s->nb, s->origin, s->origin_cnt,
+                                s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "origin kernel");
   s->origin_dirty = false;
   return TFS_OK;
@@ -256,7 +258,8 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
       (rc = alloc_dev((void **)&s->f_blobs, dsz * 3 * nb)) ||
       (rc = alloc_dev((void **)&s->v_blobs, dsz * 3 * nb)) ||
       (rc = alloc_dev((void **)&s->f_rep, dsz * 3 * nb)) ||
-      (rc = alloc_dev((void **)&s->origin, dsz * 4)) ||
+      (rc = alloc_dev((void **)&s->origin, dsz * origin_elems())) ||
+      (rc = alloc_dev((void **)&s->origin_cnt, 2 * sizeof(unsigned))) ||
       (rc = alloc_dev(&s->rec_segs, record_bytes(0, 6) * ns)) ||
       (rc = alloc_dev(&s->rec_blobs, record_bytes(0, 3) * nb)) ||
       (rc = alloc_dev(&s->rec_segs_x2, 80 * (size_t)ns)) ||
@@ -280,7 +283,8 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
   cudaMemsetAsync(s->v_blobs, 0, dsz * 3 * nb, s->stream);
   cudaMemsetAsync(s->f_blobs, 0, dsz * 3 * nb, s->stream);
   cudaMemsetAsync(s->f_rep, 0, dsz * 3 * nb, s->stream);
-  cudaMemsetAsync(s->origin, 0, dsz * 4, s->stream);
+  cudaMemsetAsync(s->origin, 0, dsz * origin_elems(), s->stream);
+  cudaMemsetAsync(s->origin_cnt, 0, 2 * sizeof(unsigned), s->stream);
   e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) {
     free_all(s);

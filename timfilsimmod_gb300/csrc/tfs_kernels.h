@@ -88,7 +88,8 @@ void count_launch_n(long long n);  // n may be negative (launches recorded into 
 size_t record_bytes(int fp32, int fd);
 
 cudaError_t launch_origin(const double *xa, int na, const double *xb, int nb, double *out,
-                          cudaStream_t st);
+                          unsigned *counter, cudaStream_t st);
+size_t origin_elems();  // doubles of the origin buffer: [4] result + partials
 cudaError_t launch_pack(int fp32, int fd, void *rec, const double *x, const double *f, int n,
                         const double *origin, cudaStream_t st);
 // FP32x2 records (positions negated, every value duplicated), 80 B per

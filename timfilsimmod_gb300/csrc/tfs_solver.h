@@ -26,7 +26,8 @@ struct tfs_solver {
   cudaStream_t stream = nullptr;
   double *x_segs = nullptr, *f_segs = nullptr, *v_segs = nullptr;
   double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
-  double *origin = nullptr;  // [4]: mean position and extent
+  double *origin = nullptr;  // [4]: mean position and extent, then partials
+  unsigned *origin_cnt = nullptr;  // [2] last-CTA counters of the origin passes
   void *rec_segs = nullptr, *rec_blobs = nullptr;
   void *rec_segs_x2 = nullptr, *rec_blobs_x2 = nullptr;  // FP32x2 records
   double *scratch = nullptr;
