@@ -338,9 +338,10 @@ class ReferenceStep:
 
     def __init__(self, nfil, nseg, blob_refs, fil_refs, fil_dirs, end_force_magnitude_real,
                  seg_sep=2.2, body_length=40.0, body_x=(0, 0, 0), body_q=(1, 0, 0, 0),
-                 threads=None):
+                 threads=None, config="s1"):
+        """config "s1": DT = 1e-3; "s2": the reference's default DT = 36.3833/300."""
         threads = threads or (os.cpu_count() or 1)
-        path = os.path.join(REF_DIR, "libref_solver_s1.so")
+        path = os.path.join(REF_DIR, f"libref_solver_{config}.so")
         if not os.path.exists(path):
             raise FileNotFoundError(path)
         self.lib = ctypes.CDLL(path)

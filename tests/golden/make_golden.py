@@ -277,9 +277,40 @@ def case_step_io():
     return res
 
 
+def case_step_default_dt():
+    """Steps 0-9 of the small swimmer at the reference's default time step
+    (DT = 36.3833/300; Broyden TOL 1e-4, LINEAR_SYSTEM_TOL 1e-10), where
+    every step iterates Broyden's method: per-step Broyden counts, body pose
+    and tether forces after each step, segment positions after steps 0 and 9,
+    the final orientations, Lie algebra elements and multipliers."""
+    sw, nfil, normals, fil_refs, efm = step_setup()
+    ref = ReferenceStep(nfil, sw.nseg, sw.blob_references, fil_refs, normals, efm, seg_sep=2.2,
+                        body_length=2.0 * sw.radius, config="s2")
+    ref.make_body_reference_matrices()
+    res = dict(blob_refs=sw.blob_references, fil_refs=fil_refs, fil_dirs=normals, nfil=nfil,
+               nseg=sw.nseg, end_force_magnitude_real=efm, body_radius=sw.radius,
+               dt=36.3833 / 300.0, tol=1e-4, linear_tol=ref.lib.ref_linear_system_tol())
+    broy, gm, traj = [], [], {}
+    for nt in range(10):
+        b, g = ref.run(nt)
+        broy.append(b)
+        gm.append(g)
+        for k, v in ref.state().items():
+            traj.setdefault(k, []).append(v)
+    for k, v in traj.items():
+        if k in ("q", "u", "lam"):
+            res[f"final_{k}"] = v[-1]
+        elif k == "x":
+            res["traj_x_first"], res["traj_x_last"] = v[0], v[-1]
+        else:
+            res[f"traj_{k}"] = np.array(v)
+    res.update(broyden_iters=np.array(broy), gmres_iters=np.array(gm))
+    return res
+
+
 CASES = {"small_matvec": case_small, "overlap_a16": case_overlap, "tiny": case_tiny,
          "flow_small": case_flow, "solve_small": case_solve, "step_small": case_step,
-         "step_io": case_step_io}
+         "step_io": case_step_io, "step_default_dt": case_step_default_dt}
 
 
 def main():

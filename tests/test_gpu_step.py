@@ -141,3 +141,26 @@ def test_ten_steps_fp32c_within_1e8():
     R = float(d["body_radius"])
     assert np.max(np.abs(states[-1]["body_x"] - d["traj_body_x"][-1])) / R < 1e-8
     assert abs(sum(broy) - int(np.sum(d["broyden_iters"]))) <= 2, broy
+
+
+def run_steps_default_dt(precision):
+    d = np.load(os.path.join(GOLD, "step_default_dt.npz"))
+    broy, states = run_steps(d, precision)
+    return d, broy, states
+
+
+def test_ten_steps_at_the_default_time_step():
+    """The reference's default DT = 36.3833/300, where every step iterates
+    Broyden's method (25, 10, 10, 8, 6, 4, 4, 4, 6, 5 iterations): FP64 keeps
+    the same counts and positions and body pose within 1e-10; FP32C the same
+    counts and positions within 1e-6 of the largest position."""
+    for precision, bar in (("fp64", 1e-10), ("fp32c", 1e-6)):
+        d, broy, states = run_steps_default_dt(precision)
+        assert broy == list(d["broyden_iters"]), (precision, broy)
+        scale = np.max(np.abs(d["traj_x_last"]))
+        assert np.max(np.abs(states[0]["x"] - d["traj_x_first"])) / scale < bar, precision
+        assert np.max(np.abs(states[-1]["x"] - d["traj_x_last"])) / scale < bar, precision
+        R = float(d["body_radius"])
+        for nt, stt in enumerate(states):
+            assert np.max(np.abs(stt["body_x"] - d["traj_body_x"][nt])) / R < bar, (precision, nt)
+            assert np.max(np.abs(stt["body_q"] - d["traj_body_q"][nt])) < bar, (precision, nt)
