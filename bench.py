@@ -21,6 +21,8 @@ inputs/outputs). Printed: one JSON line (rank 0).
   implicit_steps  whole implicit time steps (forces, solve, residuals,
            Broyden) at a 1e-8 linear residual, FP64 vs FP32C, steps/s with
            p50/p99 per-step latency
+  implicit_steps_default_dt  the same at the reference's default
+           DT = 36.3833/300, where every step iterates Broyden's method
   batched  64 uneven swimmers stepped together (FP32C, host worker pool)
            vs the FP64 drop-in one swimmer at a time, swimmer-steps/s
   served   Poisson streams of step requests of log-uniform size into the
@@ -254,6 +256,9 @@ def bench_ours(args):
     solve = None if args.no_solve else solve_bench(sw, stream, args, RpyMobilitySolver)
     # --- implicit time steps (initial guess, forces, solve, Broyden) -----------
     steps = None if args.no_steps else step_bench(sw, stream, args)
+    # the reference's default DT = 36.3833/300: every step iterates Broyden's method
+    steps_dt = None if args.no_steps else step_bench(sw, stream, args, dt=36.3833 / 300.0,
+                                                     timed=3, warm=2)
     # --- many swimmers: a batch stepped together, and a request stream ---------
     batched = None if args.no_batch else batch_bench(args)
     served = None if args.no_serve else serve_bench(args)
@@ -328,6 +333,8 @@ def bench_ours(args):
             result["solve"] = solve
         if steps is not None:
             result["implicit_steps"] = steps
+        if steps_dt is not None:
+            result["implicit_steps_default_dt"] = steps_dt
         if batched is not None:
             result["batched"] = batched
         if served is not None:
@@ -421,7 +428,7 @@ def solve_bench(sw, stream, args, RpyMobilitySolver):
             "fp32c_rel_l2_error_v_segs_vs_fp64": err}
 
 
-def step_bench(sw, stream, args):
+def step_bench(sw, stream, args, dt=1e-3, timed=None, warm=None):
     """Implicit time steps of the swimmer with elastic filaments (the
     reference's cilia_sim_main.cu:355-527 loop: initial guess, internal
     forces, compute_velocities, BDF residuals, Broyden's method with the
@@ -443,8 +450,8 @@ def step_bench(sw, stream, args):
     normals = fibonacci_sphere(nfil)
     fil_refs = (sw.radius + 1.0 + 0.5 * sw.seg_sep) * normals
     efm = 220.0 * 1800.0 / (2.6 * 2.6 * nseg * nseg)
-    timed = max(3, min(args.steps, 20))
-    warm = max(3, args.warmup)
+    timed = timed or max(3, min(args.steps, 20))
+    warm = warm or max(3, args.warmup)
     out, traj = {}, {}
     for precision in ("fp64", "fp32c"):
         s = RpyMobilitySolver(1, nfil, nseg, nb, precision=precision,
@@ -452,7 +459,7 @@ def step_bench(sw, stream, args):
         s.set_stream(stream.cuda_stream)
         s.set_blob_references(sw.blob_references)
         s.set_linear_solver(1e-8)
-        st = ImplicitStepper(s, nfil, nseg, fil_refs, normals, seg_sep=sw.seg_sep, dt=1e-3,
+        st = ImplicitStepper(s, nfil, nseg, fil_refs, normals, seg_sep=sw.seg_sep, dt=dt,
                              tol=1e-4, end_force_magnitude=efm, body_radius=sw.radius)
         lat, broy, gm, xs = [], [], [], []
         launches = 0
@@ -486,7 +493,7 @@ def step_bench(sw, stream, args):
     x64, x32 = np.array(traj["fp64"]), np.array(traj["fp32c"])
     scale = np.max(np.abs(x64), axis=1)
     dev = np.max(np.abs(x32 - x64), axis=1) / scale
-    return {"workload": f"{nfil} filaments x {nseg} segments, {nb} blobs; dt 1e-3, "
+    return {"workload": f"{nfil} filaments x {nseg} segments, {nb} blobs; dt {dt:.6g}, "
                         "Broyden TOL 1e-4, linear residual 1e-8",
             **out, "speedup_fp32c_vs_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
             "fp32c_max_rel_position_dev_vs_fp64": float(dev.max()),
