@@ -512,8 +512,6 @@ def _step_instance(nf, precision, cache, rot_seed=None):
     nb = blob_refs.shape[0]
     efm = 220.0 * 1800.0 / (2.6 * 2.6 * 400)
     s = RpyMobilitySolver(1, int(nf), 20, nb, precision=precision, end_force_magnitude=int(efm))
-    if precision == "fp32c":
-        s.set_persistent_gmres(False)
     s.set_blob_references(blob_refs)
     s.set_linear_solver(1e-8, min(350, 3 * nb + 6))
     key = (precision, nb)
@@ -558,6 +556,7 @@ def batch_bench(args):
             for nt in range(warm, warm + timed):
                 iters.append(batch.step(nt, allow_unconverged=True)["gmres_iters"].mean())
             sec = time.perf_counter() - t0
+            shared = batch.shared_solves()
             batch.close()
         else:
             for nt in range(warm):
@@ -575,6 +574,8 @@ def batch_bench(args):
                           "gmres_iters_per_swimmer_step": float(np.mean(iters)),
                           "mode": (f"batch, {args.batch_workers} host workers, one stream per swimmer"
                                    if precision == "fp32c" else "one swimmer at a time")}
+        if precision == "fp32c":
+            out[precision]["shared_inner_solves"] = shared
         for s, st in inst:
             st.close()
             s.finalise()
@@ -641,6 +642,7 @@ def serve_bench(args):
                            "p50_ms": float(np.percentile(lat, 50)),
                            "p99_ms": float(np.percentile(lat, 99)), "requests": nreq}
     stats = sv.stats()
+    shared = sv.shared_solves()
     sv.close()
     sv = server("fp64", 1)
     reqs = stream(int(args.serve_rates[0]))
@@ -658,7 +660,8 @@ def serve_bench(args):
                         "residual 1e-8",
             "fp32c_server": {"workers": args.serve_workers, "by_rate": rates,
                              "resident_instances": stats["resident_instances"],
-                             "created": stats["created"], "reused": stats["reused"]},
+                             "created": stats["created"], "reused": stats["reused"],
+                             "shared_inner_solves": shared},
             "fp64_one_at_a_time": base,
             "speedup_best_rate_vs_fp64": best / base["steps_per_s"]}
 

@@ -306,9 +306,15 @@ int tfs_stepper_write_files(tfs_stepper *st, int nt, const char *prefix, int bac
  * swimmer is an instance -- its own tfs_solver and tfs_stepper on its own
  * stream -- and a pool of host worker threads runs the instances' step
  * pipelines so that their kernels overlap on the GPU. Instances share
- * nothing on the device: a swimmer's result is the same alone and in a
- * batch. FP32C instances run the kernel-sequence inner GMRES (the
- * cooperative form needs the whole GPU). */
+ * no state on the device: a swimmer's result is the same alone (a batch of
+ * one) and in a batch. The inner GMRES solves of FP32C instances can run
+ * in shared cooperative launches of the persistent kernel (always in the
+ * server; in a batch after tfs_batch_share_inner_solves): a solve waiting for
+ * the GPU is gathered with the others waiting (up to the SM count of CTAs),
+ * each on a fixed number of CTAs chosen from its own blob count (about one
+ * per 64 blobs), so its arithmetic does not depend on the others. FP32C
+ * swimmers the persistent kernel cannot take, and FP64 swimmers, solve on
+ * their own with the kernel sequence. */
 typedef struct tfs_batch tfs_batch;
 int tfs_batch_create(int num_workers, tfs_batch **out);
 int tfs_batch_destroy(tfs_batch *b);   /* does not destroy the instances */
@@ -319,6 +325,12 @@ int tfs_batch_size(tfs_batch *b, int *n);
  * Broyden and GMRES iterations and the step's status; the return value is
  * TFS_OK or the first failing swimmer's status (the others still step). */
 int tfs_batch_step(tfs_batch *b, int nt, int *broyden_iters, int *gmres_iters, int *status);
+/* enable = 1: FP32C inner solves share launches; 0 (the default): every
+ * swimmer solves on its own with the kernel sequence, as FP64 swimmers do
+ * (faster for a mix dominated by large swimmers, which fill the GPU alone). */
+int tfs_batch_share_inner_solves(tfs_batch *b, int enable);
+/* Inner solves run in shared launches so far, and those launches. */
+int tfs_batch_shared_solves(tfs_batch *b, long long *launches, long long *solves);
 
 /* A request: num_steps implicit steps (0 .. num_steps-1) of a swimmer
  * given by its geometry (blob references, filament bases and directions;
@@ -367,6 +379,7 @@ int tfs_server_poll(tfs_server *sv, long long ticket, int wait, int *status, dou
                     int *broyden_iters, int *gmres_iters);
 int tfs_server_drain(tfs_server *sv);   /* until every submitted request completed */
 int tfs_server_stats(tfs_server *sv, tfs_server_counters *out);
+int tfs_server_shared_solves(tfs_server *sv, long long *launches, long long *solves);
 int tfs_server_destroy(tfs_server *sv); /* drains first */
 
 /* --- flow-field evaluator ---------------------------------------------- */

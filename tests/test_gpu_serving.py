@@ -1,10 +1,12 @@
 """Many swimmers on one GPU: a batch of uneven swimmers stepped together, and
 the request server (timfilsimmod_gb300.serving).
 
-Each instance owns its solver, stepper and stream and shares nothing on the
-device with the others, and every reduction is in a fixed order, so a
-swimmer's result is the same -- bit for bit -- alone and in the mix: that is
-the bar here (tolerance 0), in FP64 and FP32C. The parity of a single
+Each instance owns its solver, stepper and stream and keeps no state on the
+device that others touch; FP32C inner solves share cooperative launches, but
+each runs on a fixed number of CTAs chosen from its own size, and every
+reduction is in a fixed order. So a swimmer's result is the same -- bit for
+bit -- alone (a batch of one; a server with one worker) and in the mix: that
+is the bar here (tolerance 0), in FP64 and FP32C. The parity of a single
 swimmer's step with the reference is covered by test_gpu_step.py.
 """
 import numpy as np
@@ -38,8 +40,6 @@ def make_instance(subdiv, nfil, precision):
     blob_refs, fil_refs, normals, radius = geometry(subdiv, nfil)
     s = RpyMobilitySolver(1, nfil, 20, blob_refs.shape[0], precision=precision,
                           end_force_magnitude=int(efm()))
-    if precision == "fp32c":
-        s.set_persistent_gmres(False)  # as in a batch
     s.set_blob_references(blob_refs)
     s.set_linear_solver(1e-8, min(350, 3 * blob_refs.shape[0] + 6))
     st = ImplicitStepper(s, nfil, 20, fil_refs, normals, seg_sep=2.2, dt=DT, tol=TOL,
@@ -47,26 +47,39 @@ def make_instance(subdiv, nfil, precision):
     return s, st
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
-def test_batch_same_as_alone(precision):
+@pytest.mark.parametrize("precision,share", [("fp64", False), ("fp32c", False), ("fp32c", True)])
+def test_batch_same_as_alone(precision, share):
     from timfilsimmod_gb300.serving import SwimmerBatch
 
     steps = 3
     alone = []
     for subdiv, nfil in SHAPES:
         s, st = make_instance(subdiv, nfil, precision)
+        one = SwimmerBatch(num_workers=1)
+        one.share_inner_solves(share)
+        one.add(st)
         for nt in range(steps):
-            st.step(nt, allow_unconverged=True)
+            one.step(nt, allow_unconverged=True)
+        if share:
+            sh = one.shared_solves()
+            assert sh["solves"] > 0 and sh["launches"] == sh["solves"], sh
         alone.append(st.state())
+        one.close()
         st.close()
         s.finalise()
     inst = [make_instance(subdiv, nfil, precision) for subdiv, nfil in SHAPES]
     batch = SwimmerBatch(num_workers=3)
+    batch.share_inner_solves(share)
     for _, st in inst:
         batch.add(st)
     for nt in range(steps):
         out = batch.step(nt, allow_unconverged=True)
         assert np.all(out["gmres_iters"] > 0)
+    sh = batch.shared_solves()
+    if share:
+        assert sh["solves"] > 0 and 0 < sh["launches"] <= sh["solves"], sh
+    else:
+        assert sh == {"launches": 0, "solves": 0}
     for (s, st), ref in zip(inst, alone):
         got = st.state()
         for k in ("x", "q", "lam", "body_x", "body_q"):
@@ -103,6 +116,7 @@ def serve(reqs, workers, budget_gb=160.0, one_at_a_time=False, precision="fp32c"
             tickets.append(t)
     results += [sv.poll(t, wait=True) for t in tickets]
     stats = sv.stats()
+    stats.update(sv.shared_solves())
     sv.close()
     return results, stats
 
@@ -112,7 +126,9 @@ def test_server_results_same_alone_and_in_mix():
     alone, stats = serve(reqs, workers=1, one_at_a_time=True)
     # one request at a time: each geometry's instance is built once, then reused
     assert stats["created"] == len(SHAPES) and stats["reused"] == len(reqs) - len(SHAPES)
-    mix, _ = serve(reqs, workers=4)
+    assert stats["solves"] > 0 and stats["launches"] == stats["solves"]
+    mix, mstats = serve(reqs, workers=4)
+    assert 0 < mstats["launches"] <= mstats["solves"]
     for a, m in zip(alone, mix):
         assert np.array_equal(a["x"], m["x"])
         assert np.array_equal(a["body"], m["body"])

@@ -172,6 +172,8 @@ _SIGNATURES = {
     "tfs_batch_destroy": [_H],
     "tfs_batch_add": [_H, _H, _IP],
     "tfs_batch_size": [_H, _IP],
+    "tfs_batch_share_inner_solves": [_H, ctypes.c_int],
+    "tfs_batch_shared_solves": [_H, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "tfs_batch_step": [_H, ctypes.c_int, _P, _P, _P],
     "tfs_server_config_default": [ctypes.POINTER(ServerConfig)],
     "tfs_server_create": [ctypes.POINTER(ServerConfig), ctypes.POINTER(_H)],
@@ -180,6 +182,7 @@ _SIGNATURES = {
                         ctypes.POINTER(ctypes.c_double), _IP, _IP],
     "tfs_server_drain": [_H],
     "tfs_server_stats": [_H, ctypes.POINTER(ServerCounters)],
+    "tfs_server_shared_solves": [_H, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "tfs_server_destroy": [_H],
     "tfs_last_error": [],
     "tfs_kernel_launch_count": [],

@@ -71,7 +71,8 @@ struct PgArgs {
   double *pd1, *pd2;      // per-CTA Gram-Schmidt partial dots ((max_iter + 2) * G each)
   double *aux;            // control words (3) + 3 x 352: h1, h2, y published by CTAs
   unsigned *bar;          // 4: barrier count, generation, abort
-  int P, TB, tbs, S, chunk, Kr;
+  int P, TB, tbs, S, chunk, Kr;  // P: the CTAs of this solve
+  int rank;               // this CTA's index among them (set on the device)
   size_t dyn_smem;
   float a;                // blob radius
   float pc_asum2, pc_s, pc_s3;  // FP32 pair constants: (2a)^2, 2a^2/3, -2a^2
@@ -86,7 +87,11 @@ inline size_t pg_p6_elems(const PgShape &s) { return 6 * 6 * (size_t)s.G; }
 inline size_t pg_ps_elems(const PgShape &s) { return 3 * (size_t)s.G; }
 inline size_t pg_pd_elems(const PgShape &s) { return 352 * (size_t)s.G; }
 constexpr size_t kPgAuxElems = 3 + 3 * 352;
-cudaError_t launch_gmres_persistent(const PgArgs &p, cudaStream_t st);
+// One cooperative launch of `ctas` CTAs running the solves in gp[] (device
+// array): CTA c works for solve cmap[c].x as its CTA cmap[c].y. Every solve's
+// barrier words must be zero.
+cudaError_t launch_gmres_persistent(const PgArgs *gp, const int2 *cmap, int ctas, size_t dyn_smem,
+                                    cudaStream_t st);
 
 // CTAs and blobs per CTA of the GMRES kernels for nb blobs on `sms` SMs.
 int gmres_grid(int nb, int sms, int *blobs_per_cta);

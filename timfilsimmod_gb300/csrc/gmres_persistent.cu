@@ -79,7 +79,7 @@ __device__ bool pg_barrier(const PgArgs &p) {
     const unsigned gen = vb[1];
     __threadfence();
     const unsigned arrived = atomicAdd(p.bar, 1u);
-    if (arrived == gridDim.x - 1) {
+    if (arrived == (unsigned)p.P - 1) {
       atomicExch(p.bar, 0u);  // no CTA arrives again before the generation moves
       __threadfence();
       atomicAdd(p.bar + 1, 1u);
@@ -114,7 +114,7 @@ __device__ bool pg_barrier(const PgArgs &p) {
 struct PSlice {
   int m0, m1;       // blobs [m0, m1)
   int rows;         // 3 (m1 - m0)
-  bool owner;       // this CTA owns a slice (blockIdx.x < G)
+  bool owner;       // this CTA owns a slice (rank < G)
   bool body;        // this CTA writes the six body rows of global vectors
   const double *d;  // the slice's d_m = R ref_m, d[3 (m - m0) + j] (shared memory)
 };
@@ -122,7 +122,7 @@ struct PSlice {
 __device__ __forceinline__ PSlice pg_slice(const PgArgs &p, const double *dsl) {
   PSlice s;
   s.d = dsl;
-  const int c = blockIdx.x;
+  const int c = p.rank;
   s.owner = c < p.g.G;
   s.m0 = s.owner ? min(p.g.nb, c * p.g.blobs_per_cta) : p.g.nb;
   s.m1 = s.owner ? min(p.g.nb, s.m0 + p.g.blobs_per_cta) : p.g.nb;
@@ -188,7 +188,7 @@ __device__ void slice_partials(const PgArgs &p, const PSlice &sl, const double *
   for (int j = 0; j < 6; ++j) s[j] = warp_sum(s[j]);
   if (sq_slot >= 0) s[6] = warp_sum(s[6]);
   if (lane == 0) {
-    const int G = p.g.G, c = blockIdx.x;
+    const int G = p.g.G, c = p.rank;
     for (int j = 0; j < 6; ++j) p.p6[(size_t)(kt_slot * 6 + j) * G + c] = s[j];
     if (sq_slot >= 0) p.ps[(size_t)sq_slot * G + c] = s[6];
   }
@@ -255,15 +255,15 @@ __device__ void pack_records(const PgArgs &p, const PSlice &sl, const double *fs
 __device__ void mbb_units(const PgArgs &p, float *src) {
   const int nb = p.g.nb;
   const int units = p.TB * p.S;
-  const int first = gridDim.x > 1 ? 1 : 0, workers = gridDim.x - first;
-  if ((int)blockIdx.x < first) return;
+  const int first = p.P > 1 ? 1 : 0, workers = p.P - first;
+  if (p.rank < first) return;
   PairConst<float> pc;
   pc.ai = p.a;
   pc.aj = p.a;
   pc.asum2 = p.pc_asum2;
   pc.s = p.pc_s;
   pc.s3 = p.pc_s3;
-  for (int u = blockIdx.x - first; u < units; u += workers) {
+  for (int u = p.rank - first; u < units; u += workers) {
     const int tb = u / p.S, sp = u - tb * p.S;
     const int t0 = tb * p.tbs, t1 = min(nb, t0 + p.tbs);
     const int s0 = sp * p.chunk, s1 = min(nb, s0 + p.chunk);
@@ -411,7 +411,7 @@ __device__ void slice_dots(const PgArgs &p, const PSlice &sl, const double *ws, 
     }
     s += __shfl_xor_sync(0xffffffffu, s, 1);
     s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (i < k && part == 0) pd[(size_t)i * p.g.G + blockIdx.x] = s;
+    if (i < k && part == 0) pd[(size_t)i * p.g.G + p.rank] = s;
   }
 }
 
@@ -446,7 +446,7 @@ __device__ void reduce_dots(const PgArgs &p, const double *pd, int k, const doub
                             const double *qvres, double *hg) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int G = p.g.G;
-  for (int j = blockIdx.x + gridDim.x * wid; j < k; j += gridDim.x * kPW) {
+  for (int j = p.rank + p.P * wid; j < k; j += p.P * kPW) {
     double s = 0.0;
     for (int c = lane; c < G; c += 32) s += ldcg(pd + (size_t)j * G + c);
     s = warp_sum(s);
@@ -531,7 +531,18 @@ __device__ void back_substitute(const PgArgs &p, int k, const double *hcol, cons
 
 }  // namespace
 
-__global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(PgArgs p) {
+__global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *__restrict__ gp,
+                                                                  const int2 *__restrict__ cmap) {
+  // this CTA's solve (several independent solves may share one launch, each
+  // on its own CTAs with its own barrier words)
+  __shared__ PgArgs pshared;
+  if (threadIdx.x == 0) {
+    const int2 m = cmap[blockIdx.x];
+    pshared = gp[m.x];
+    pshared.rank = m.y;
+  }
+  __syncthreads();
+  const PgArgs &p = pshared;
   __shared__ __align__(16) float src[8 * kPTS];
   __shared__ double ws[kMaxRows];            // w (then Q_k, tmp) rows of the slice
   __shared__ double zs[kMaxRows];            // z = P^-1 q rows of the slice
@@ -615,7 +626,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(PgArgs p) {
         for (int r = threadIdx.x; r < sl.rows; r += kPB) g.f_blobs[3 * sl.m0 + r] = 0.0;
         if (sl.body && threadIdx.x < 6) g.v_bodies[threadIdx.x] = 0.0;
       }
-      if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (p.rank == 0 && threadIdx.x == 0) {
         st->norm_rhs = norm_rhs;
         st->flag = flag;
         st->iters = 0;
@@ -667,7 +678,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(PgArgs p) {
   double qn = 0.0;
   for (;;) {
     mbb_units(p, src);
-    if (blockIdx.x == 0 && k > 1) {
+    if (p.rank == 0 && k > 1) {
       // Givens rotation (mobility_solver.cpp:2370-2413) of step kk = k - 1
       const int kk = k - 1;
       if (threadIdx.x == 0) {
@@ -813,7 +824,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(PgArgs p) {
     g.soln[vel + threadIdx.x] = x;
     g.v_bodies[threadIdx.x] = x;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (p.rank == 0 && threadIdx.x == 0) {
     st->norm_rhs = norm_rhs;
     st->rel = ldcg(p.aux + C_REL);
     st->iters = k;
@@ -848,8 +859,10 @@ int pg_grid(int nb, int sms, int max_iter, PgShape *shape) {
   const int Kr = (int)std::min<long>(max_iter + 1, cols);
   const size_t dyn = sizeof(double) * (kPgDynFixed + (size_t)Kr * rows);
   int occ = 0;
+  // the attribute is the largest dynamic size any shape may use, so that one
+  // setting serves every shape (solves of several shapes share launches)
   if (cudaFuncSetAttribute(gmres_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)dyn) != cudaSuccess ||
+                           (int)(optin - (long)fa.sharedSizeBytes)) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gmres_persistent_kernel, kPB, dyn) !=
           cudaSuccess ||
       occ < 1) {
@@ -874,12 +887,11 @@ int pg_grid(int nb, int sms, int max_iter, PgShape *shape) {
   return 1;
 }
 
-cudaError_t launch_gmres_persistent(const PgArgs &p, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(p.bar, 0, 4 * sizeof(unsigned), st);
-  if (e != cudaSuccess) return e;
-  void *args[] = {const_cast<PgArgs *>(&p)};
-  e = cudaLaunchCooperativeKernel((const void *)gmres_persistent_kernel, dim3(p.P), dim3(kPB),
-                                  args, p.dyn_smem, st);
+cudaError_t launch_gmres_persistent(const PgArgs *gp, const int2 *cmap, int ctas, size_t dyn_smem,
+                                    cudaStream_t st) {
+  void *args[] = {const_cast<PgArgs **>(&gp), const_cast<int2 **>(&cmap)};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void *)gmres_persistent_kernel, dim3(ctas),
+                                              dim3(kPB), args, dyn_smem, st);
   count_launch();
   return e;
 }

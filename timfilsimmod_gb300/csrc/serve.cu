@@ -111,6 +111,10 @@ class WorkerPool {
 struct tfs_batch {
   std::unique_ptr<WorkerPool> pool;
   std::vector<tfs_stepper *> inst;
+  std::vector<char> shared;  // the instance's inner solves can go through the service
+  tfs::GmresService *service = nullptr;
+  bool share = false;
+  ~tfs_batch() { tfs::service_destroy(service); }
 };
 
 extern "C" {
@@ -133,14 +137,25 @@ int tfs_batch_destroy(tfs_batch *b) {
   return TFS_OK;
 }
 
+// FP32C swimmers whose inner solve the persistent kernel can run share
+// cooperative launches during tfs_batch_step (the service is attached to the
+// solver only for the step); the others, and FP32C swimmers the kernel cannot
+// run, solve alone with the kernel sequence.
 int tfs_batch_add(tfs_batch *b, tfs_stepper *st, int *index) {
   if (b == nullptr || st == nullptr) return fail(TFS_EINVAL, "null handle");
   tfs_solver *s = tfs::stepper_solver(st);
+  char shared = 0;
   if (s->cfg.precision == TFS_FP32C) {
-    int rc = tfs_set_persistent_gmres(s, 0);
-    if (rc != TFS_OK) return rc;
+    if (b->service == nullptr && (b->service = tfs::service_create()) == nullptr)
+      return fail(TFS_ECUDA, "GMRES service creation failed");
+    int rc = tfs::service_attach(b->service, s);
+    s->service = nullptr;
+    if (rc == TFS_OK) shared = 1;
+    else if (rc != TFS_ESTATE) return rc;
+    if ((rc = tfs_set_persistent_gmres(s, 0)) != TFS_OK) return rc;
   }
   b->inst.push_back(st);
+  b->shared.push_back(shared);
   if (index) *index = (int)b->inst.size() - 1;
   return TFS_OK;
 }
@@ -148,6 +163,20 @@ int tfs_batch_add(tfs_batch *b, tfs_stepper *st, int *index) {
 int tfs_batch_size(tfs_batch *b, int *n) {
   if (b == nullptr || n == nullptr) return fail(TFS_EINVAL, "null argument");
   *n = (int)b->inst.size();
+  return TFS_OK;
+}
+
+int tfs_batch_share_inner_solves(tfs_batch *b, int enable) {
+  if (b == nullptr) return fail(TFS_EINVAL, "null batch");
+  b->share = enable != 0;
+  return TFS_OK;
+}
+
+int tfs_batch_shared_solves(tfs_batch *b, long long *launches, long long *solves) {
+  if (b == nullptr) return fail(TFS_EINVAL, "null batch");
+  if (launches) *launches = 0;
+  if (solves) *solves = 0;
+  if (b->service) tfs::service_stats(b->service, launches, solves);
   return TFS_OK;
 }
 
@@ -159,10 +188,13 @@ int tfs_batch_step(tfs_batch *b, int nt, int *broyden_iters, int *gmres_iters, i
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
     return tfs::stepper_segments(b->inst[x]) > tfs::stepper_segments(b->inst[y]);
   });
+  for (int i = 0; i < n; ++i)
+    if (b->share && b->shared[i]) tfs::stepper_solver(b->inst[i])->service = b->service;
   b->pool->run(n, [&](int k) {
     const int i = order[k];
     rc[i] = tfs_stepper_step(b->inst[i], nt, &bi[i], &gi[i]);
   });
+  for (int i = 0; i < n; ++i) tfs::stepper_solver(b->inst[i])->service = nullptr;
   int first = TFS_OK;
   for (int i = 0; i < n; ++i) {
     if (broyden_iters) broyden_iters[i] = bi[i];
@@ -249,6 +281,7 @@ struct tfs_server {
   long long created = 0, evicted = 0, reused = 0;
   bool stop = false;
   std::vector<std::thread> workers;
+  tfs::GmresService *service = nullptr;  // shared inner solves of FP32C instances
   Clock::time_point t0 = Clock::now();
 
   void worker();
@@ -265,7 +298,11 @@ int tfs_server::build(Instance *in, const tfs_request &r) {
   if ((rc = tfs_solver_create(&c, &in->s)) != TFS_OK) return rc;
   if ((rc = tfs_set_linear_solver(in->s, cfg.linear_tol, std::min(350, 3 * r.nblob + 6))) != TFS_OK)
     return rc;
-  if (cfg.precision == TFS_FP32C && (rc = tfs_set_persistent_gmres(in->s, 0)) != TFS_OK) return rc;
+  if (cfg.precision == TFS_FP32C) {
+    rc = tfs::service_attach(service, in->s);
+    if (rc != TFS_OK && rc != TFS_ESTATE) return rc;
+    if ((rc = tfs_set_persistent_gmres(in->s, 0)) != TFS_OK) return rc;
+  }
   if ((rc = tfs_set_blob_references(in->s, r.blob_refs)) != TFS_OK) return rc;
   tfs_step_config sc = cfg.step;
   sc.nfil = r.nfil;
@@ -407,6 +444,10 @@ int tfs_server_create(const tfs_server_config *cfg, tfs_server **out) {
     delete sv;
     return tfs::cuda_fail(e, "device");
   }
+  if (cfg->precision == TFS_FP32C && (sv->service = tfs::service_create()) == nullptr) {
+    delete sv;
+    return fail(TFS_ECUDA, "GMRES service creation failed");
+  }
   for (int i = 0; i < cfg->num_workers; ++i) sv->workers.emplace_back([sv] { sv->worker(); });
   *out = sv;
   return TFS_OK;
@@ -478,6 +519,14 @@ int tfs_server_stats(tfs_server *sv, tfs_server_counters *out) {
   return TFS_OK;
 }
 
+int tfs_server_shared_solves(tfs_server *sv, long long *launches, long long *solves) {
+  if (sv == nullptr) return fail(TFS_EINVAL, "null server");
+  if (launches) *launches = 0;
+  if (solves) *solves = 0;
+  if (sv->service) tfs::service_stats(sv->service, launches, solves);
+  return TFS_OK;
+}
+
 int tfs_server_destroy(tfs_server *sv) {
   if (sv == nullptr) return TFS_OK;
   {
@@ -488,6 +537,7 @@ int tfs_server_destroy(tfs_server *sv) {
   sv->cv.notify_all();
   for (auto &t : sv->workers) t.join();
   for (Instance *in : sv->pool) destroy_instance(in);
+  tfs::service_destroy(sv->service);
   delete sv;
   return TFS_OK;
 }

@@ -9,6 +9,12 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
+#include <new>
+#include <mutex>
+#include <deque>
+#include <condition_variable>
+#include <chrono>
 
 #include "tfs_solver.h"
 
@@ -247,11 +253,12 @@ int gmres_run(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodie
 }
 
 // Inner GMRES of the refinement as one cooperative kernel (FP32 M_bb).
-int gmres_run_persistent(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies,
-                         double tol, int *iters) {
+// The persistent kernel's arguments for one inner solve of s in shape sh.
+PgArgs persistent_args(tfs_solver *s, const PgShape &sh, const double *rhs, double *f_blobs,
+                       double *v_bodies, double tol) {
   GmresArgs g = gmres_args(s, rhs, f_blobs, v_bodies, s->gst, tol, 1);
-  g.G = s->pg.G;
-  g.blobs_per_cta = s->pg.blobs_per_cta;
+  g.G = sh.G;
+  g.blobs_per_cta = sh.blobs_per_cta;
   PgArgs p{};
   p.g = g;
   p.x32 = s->pg_x32;
@@ -263,13 +270,13 @@ int gmres_run_persistent(tfs_solver *s, const double *rhs, double *f_blobs, doub
   p.pd2 = s->pg_pd2;
   p.aux = s->pg_aux;
   p.bar = s->pg_bar;
-  p.P = s->pg.P;
-  p.TB = s->pg.TB;
-  p.tbs = s->pg.tbs;
-  p.S = s->pg.S;
-  p.chunk = s->pg.chunk;
-  p.Kr = s->pg.Kr;
-  p.dyn_smem = s->pg.dyn_smem;
+  p.P = sh.P;
+  p.TB = sh.TB;
+  p.tbs = sh.tbs;
+  p.S = sh.S;
+  p.chunk = sh.chunk;
+  p.Kr = sh.Kr;
+  p.dyn_smem = sh.dyn_smem;
   p.a = (float)s->cfg.a_blob;
   const double ab = s->cfg.a_blob;
   p.pc_asum2 = (float)((2.0 * ab) * (2.0 * ab));
@@ -277,8 +284,11 @@ int gmres_run_persistent(tfs_solver *s, const double *rhs, double *f_blobs, doub
   p.pc_s3 = (float)(-2.0 * ab * ab);
   p.minv = 6.0 * 3.14159265358979323846264338327950288 * s->cfg.mu * ab;
   p.scale = 1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu);
-  cudaError_t e = launch_gmres_persistent(p, s->stream);
-  if (e != cudaSuccess) return cuda_fail(e, "persistent GMRES");
+  return p;
+}
+
+// The result of an inner persistent solve (its scalars, read on s->stream).
+int persistent_result(tfs_solver *s, int *iters) {
   GmresScalars h{};
   int rc;
   if ((rc = poll(s, 0, &h)) != TFS_OK) return rc;
@@ -289,6 +299,206 @@ int gmres_run_persistent(tfs_solver *s, const double *rhs, double *f_blobs, doub
   s->last_rel = h.rel;
   return TFS_OK;
 }
+
+int gmres_run_persistent(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies,
+                         double tol, int *iters) {
+  const PgArgs p = persistent_args(s, s->pg, rhs, f_blobs, v_bodies, tol);
+  TFS_CUDA(cudaMemcpyAsync(s->pg_gp, &p, sizeof p, cudaMemcpyHostToDevice, s->stream),
+           "persistent GMRES arguments");
+  TFS_CUDA(cudaMemsetAsync(p.bar, 0, 4 * sizeof(unsigned), s->stream), "persistent GMRES barrier");
+  cudaError_t e = launch_gmres_persistent(s->pg_gp, s->pg_cmap, p.P, p.dyn_smem, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "persistent GMRES");
+  return persistent_result(s, iters);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Inner solves of several swimmers in one cooperative launch. A swimmer's
+// solve runs on a fixed number of CTAs chosen from its size alone, so its
+// result does not depend on which others share the launch. A waiting thread
+// that finds no launch being prepared becomes the leader: while the previous
+// launch still runs on the GPU (and the waiting solves fill fewer CTAs than
+// the SMs) it lets requests gather, then takes them in arrival order up to
+// the SM count, queues their launch on the service's stream behind each
+// swimmer's inputs, marks each swimmer's completion event and wakes the
+// owners, who wait for that event on their own streams. Launches queue back
+// to back on the service's stream; the host never waits for one to finish
+// except to reuse one of its argument staging slots.
+// ---------------------------------------------------------------------------
+namespace tfs {
+
+struct GmresService {
+  struct Req {
+    tfs_solver *s;
+    PgArgs args;
+    bool done;
+    int rc;
+  };
+  static constexpr int kSlots = 8;  // host staging of the launch arguments
+  struct Slot {
+    PgArgs *args = nullptr;
+    int2 *map = nullptr;
+    cudaEvent_t copied = nullptr;
+  };
+  std::mutex m;
+  std::condition_variable cv;
+  std::deque<Req *> pending;
+  bool busy = false;
+  int sms = 1;
+  cudaStream_t stream = nullptr;
+  PgArgs *dev_args = nullptr;
+  int2 *dev_map = nullptr;
+  Slot slot[kSlots];
+  int next_slot = 0;
+  cudaEvent_t last = nullptr;  // the latest launch's completion
+  bool launched = false;
+  long long launches = 0, solves = 0;
+
+  int waiting_ctas() const {
+    int c = 0;
+    for (const Req *q : pending) c += q->args.P;
+    return c;
+  }
+  bool gpu_busy() const { return launched && cudaEventQuery(last) == cudaErrorNotReady; }
+
+  // Queues one launch of the solves in batch (the leader, without the lock).
+  int launch(std::vector<Req *> &batch) {
+    Slot &sl = slot[next_slot];
+    next_slot = (next_slot + 1) % kSlots;
+    TFS_CUDA(cudaEventSynchronize(sl.copied), "service: staging slot");
+    int ctas = 0;
+    size_t dyn = 0;
+    for (size_t q = 0; q < batch.size(); ++q) {
+      Req *r = batch[q];
+      TFS_CUDA(cudaStreamWaitEvent(stream, r->s->ready_ev, 0), "service: wait for inputs");
+      TFS_CUDA(cudaMemsetAsync(r->args.bar, 0, 4 * sizeof(unsigned), stream), "service: barrier");
+      sl.args[q] = r->args;
+      for (int c = 0; c < r->args.P; ++c) sl.map[ctas + c] = make_int2((int)q, c);
+      ctas += r->args.P;
+      dyn = std::max(dyn, r->args.dyn_smem);
+    }
+    TFS_CUDA(cudaMemcpyAsync(dev_args, sl.args, sizeof(PgArgs) * batch.size(),
+                             cudaMemcpyHostToDevice, stream),
+             "service: arguments");
+    TFS_CUDA(cudaMemcpyAsync(dev_map, sl.map, sizeof(int2) * ctas, cudaMemcpyHostToDevice, stream),
+             "service: map");
+    TFS_CUDA(cudaEventRecord(sl.copied, stream), "service: staging slot");
+    cudaError_t e = launch_gmres_persistent(dev_args, dev_map, ctas, dyn, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "service: persistent GMRES");
+    for (Req *r : batch) TFS_CUDA(cudaEventRecord(r->s->done_ev, stream), "service: completion");
+    TFS_CUDA(cudaEventRecord(last, stream), "service: completion");
+    return TFS_OK;
+  }
+
+  int solve(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies, double tol,
+            int *iters) {
+    Req r{s, persistent_args(s, s->pg_group, rhs, f_blobs, v_bodies, tol), false, TFS_OK};
+    TFS_CUDA(cudaEventRecord(s->ready_ev, s->stream), "service: inputs ready");
+    std::unique_lock<std::mutex> g(m);
+    pending.push_back(&r);
+    cv.notify_all();
+    while (!r.done) {
+      if (busy) {
+        cv.wait(g);
+        continue;
+      }
+      busy = true;
+      while (waiting_ctas() < sms && gpu_busy()) cv.wait_for(g, std::chrono::microseconds(20));
+      std::vector<Req *> batch;
+      int ctas = 0;
+      while (!pending.empty() && (batch.empty() || ctas + pending.front()->args.P <= sms)) {
+        ctas += pending.front()->args.P;
+        batch.push_back(pending.front());
+        pending.pop_front();
+      }
+      g.unlock();
+      const int lrc = launch(batch);
+      g.lock();
+      if (lrc == TFS_OK) {
+        launched = true;
+        ++launches;
+        solves += (long long)batch.size();
+      }
+      for (Req *q : batch) {
+        q->done = true;
+        q->rc = lrc;
+      }
+      busy = false;
+      cv.notify_all();
+    }
+    g.unlock();
+    if (r.rc != TFS_OK) return r.rc;
+    TFS_CUDA(cudaStreamWaitEvent(s->stream, s->done_ev, 0), "service: wait for the solve");
+    return persistent_result(s, iters);
+  }
+};
+
+GmresService *service_create() {
+  GmresService *sv = new (std::nothrow) GmresService();
+  if (sv == nullptr) return nullptr;
+  sv->sms = num_sms();
+  bool ok = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaMalloc(&sv->dev_args, sizeof(PgArgs) * kMaxPgCtas) == cudaSuccess &&
+            cudaMalloc(&sv->dev_map, sizeof(int2) * kMaxPgCtas) == cudaSuccess &&
+            cudaEventCreateWithFlags(&sv->last, cudaEventDisableTiming) == cudaSuccess;
+  for (auto &sl : sv->slot)
+    ok = ok && cudaHostAlloc(&sl.args, sizeof(PgArgs) * kMaxPgCtas, cudaHostAllocDefault) == cudaSuccess &&
+         cudaHostAlloc(&sl.map, sizeof(int2) * kMaxPgCtas, cudaHostAllocDefault) == cudaSuccess &&
+         cudaEventCreateWithFlags(&sl.copied, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    service_destroy(sv);
+    return nullptr;
+  }
+  return sv;
+}
+
+void service_destroy(GmresService *sv) {
+  if (sv == nullptr) return;
+  if (sv->stream) cudaStreamSynchronize(sv->stream);
+  if (sv->dev_args) cudaFree(sv->dev_args);
+  if (sv->dev_map) cudaFree(sv->dev_map);
+  for (auto &sl : sv->slot) {
+    if (sl.args) cudaFreeHost(sl.args);
+    if (sl.map) cudaFreeHost(sl.map);
+    if (sl.copied) cudaEventDestroy(sl.copied);
+  }
+  if (sv->last) cudaEventDestroy(sv->last);
+  if (sv->stream) cudaStreamDestroy(sv->stream);
+  delete sv;
+}
+
+// CTAs of a swimmer's solve in a shared launch: the fewest the kernel allows
+// (kMaxPgBlobsPerCta blobs each), at most the SMs.
+int service_attach(GmresService *sv, tfs_solver *s) {
+  if (sv == nullptr || s == nullptr) return fail(TFS_EINVAL, "null argument");
+  if (s->cfg.precision != TFS_FP32C) return fail(TFS_ESTATE, "only FP32C inner solves are shared");
+  if (!s->pg_ok) return fail(TFS_ESTATE, "the persistent GMRES kernel cannot serve this swimmer");
+  const int nb = s->nb;
+  const int want = std::min(sv->sms, (nb + kMaxPgBlobsPerCta - 1) / kMaxPgBlobsPerCta);
+  PgShape sh{};
+  if (!pg_grid(nb, want, s->max_iter, &sh) || sh.G > s->pg.G || sh.S > s->pg.S)
+    return fail(TFS_ESTATE, "no persistent GMRES shape for %d blobs on %d CTAs", nb, want);
+  for (cudaEvent_t *ev : {&s->ready_ev, &s->done_ev})
+    if (*ev == nullptr && cudaEventCreateWithFlags(ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(TFS_ECUDA, "event creation failed");
+    }
+  s->pg_group = sh;
+  s->service = sv;
+  return TFS_OK;
+}
+
+void service_stats(GmresService *sv, long long *launches, long long *solves) {
+  std::lock_guard<std::mutex> g(sv->m);
+  if (launches) *launches = sv->launches;
+  if (solves) *solves = sv->solves;
+}
+
+}  // namespace tfs
+
+namespace {
 
 // The linear solve of compute_velocities on s->rhs: plain FP64 GMRES, or
 // FP32C iterative refinement.
@@ -330,7 +540,8 @@ int linear_solve(tfs_solver *s, int *iters) {
     }
     prev_rel = h.rel;
     int inner = 0;
-    rc = (s->pg_ok && s->pg_enabled)
+    rc = s->service ? s->service->solve(s, s->r, s->dx, s->dx + vel, s->inner_tol, &inner)
+         : (s->pg_ok && s->pg_enabled)
              ? gmres_run_persistent(s, s->r, s->dx, s->dx + vel, s->inner_tol, &inner)
              : gmres_run(s, s->r, s->dx, s->dx + vel, s->inner_tol, 1, &inner);
     if (rc != TFS_OK && rc != TFS_ENOTCONV) return rc;
@@ -405,8 +616,14 @@ int solve_alloc(tfs_solver *s) {
         (rc = alloc_dev((void **)&s->pg_pd1, 8 * pg_pd_elems(s->pg))) ||
         (rc = alloc_dev((void **)&s->pg_pd2, 8 * pg_pd_elems(s->pg))) ||
         (rc = alloc_dev((void **)&s->pg_aux, 8 * kPgAuxElems)) ||
-        (rc = alloc_dev((void **)&s->pg_bar, 4 * sizeof(unsigned))))
+        (rc = alloc_dev((void **)&s->pg_bar, 4 * sizeof(unsigned))) ||
+        (rc = alloc_dev((void **)&s->pg_gp, sizeof(PgArgs))) ||
+        (rc = alloc_dev((void **)&s->pg_cmap, sizeof(int2) * (size_t)s->pg.P)))
       return rc;
+    std::vector<int2> cmap(s->pg.P);
+    for (int c = 0; c < s->pg.P; ++c) cmap[c] = make_int2(0, c);
+    TFS_CUDA(cudaMemcpy(s->pg_cmap, cmap.data(), sizeof(int2) * cmap.size(), cudaMemcpyHostToDevice),
+             "persistent GMRES map");
     s->pg_ok = 1;
   }
   cudaGetLastError();
@@ -438,6 +655,9 @@ int solve_alloc(tfs_solver *s) {
 }
 
 void solve_free(tfs_solver *s) {
+  if (s->ready_ev) cudaEventDestroy(s->ready_ev);
+  if (s->done_ev) cudaEventDestroy(s->done_ev);
+  s->ready_ev = s->done_ev = nullptr;
   for (auto &g : s->chunk_graphs) cudaGraphExecDestroy(g.exec);
   s->chunk_graphs.clear();
   double *bufs[] = {s->refs, s->diff, s->mats, s->Q, s->H, s->beta, s->cs, s->sn, s->y, s->z,
@@ -454,6 +674,8 @@ void solve_free(tfs_solver *s) {
   cudaFree(s->pg_pd2);
   cudaFree(s->pg_aux);
   cudaFree(s->pg_bar);
+  cudaFree(s->pg_gp);
+  cudaFree(s->pg_cmap);
   cudaFree(s->gst);
   if (s->gst_host) cudaFreeHost(s->gst_host);
   if (s->f6_host) cudaFreeHost(s->f6_host);

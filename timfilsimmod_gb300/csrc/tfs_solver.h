@@ -13,6 +13,7 @@
 #include "tfs_kernels.h"
 
 namespace tfs {
+struct GmresService;
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 long long launch_count();
@@ -65,6 +66,14 @@ struct tfs_solver {
   double *pg_p6 = nullptr, *pg_ps = nullptr, *pg_pd1 = nullptr,
          *pg_pd2 = nullptr, *pg_aux = nullptr;
   unsigned *pg_bar = nullptr;
+  tfs::PgArgs *pg_gp = nullptr;  // device copy of this solve's arguments
+  int2 *pg_cmap = nullptr;       // CTA c -> (0, c)
+  // inner solves shared with other swimmers' (one cooperative launch for all
+  // that are waiting): the service, this swimmer's fixed shape within such a
+  // launch, and events marking its inputs ready and its solve ended
+  tfs::GmresService *service = nullptr;
+  tfs::PgShape pg_group{};
+  cudaEvent_t ready_ev = nullptr, done_ev = nullptr;
   tfs::GmresScalars *gst_host = nullptr;  // pinned copies
   double *f6_host = nullptr;              // pinned 6
   int last_iters = 0, last_outer = 0;
@@ -110,4 +119,9 @@ int product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mod
 int alloc_dev(void **p, size_t bytes);
 int solve_alloc(tfs_solver *s);
 void solve_free(tfs_solver *s);
+// Inner solves of FP32C swimmers batched into shared cooperative launches.
+GmresService *service_create();
+void service_destroy(GmresService *sv);
+int service_attach(GmresService *sv, tfs_solver *s);  // TFS_ESTATE if the kernel cannot serve s
+void service_stats(GmresService *sv, long long *launches, long long *solves);
 }  // namespace tfs

@@ -3,7 +3,7 @@
 SwimmerBatch advances a set of swimmers (ImplicitStepper instances, each
 with its own solver and stream) one implicit step at a time: host worker
 threads run the instances' step pipelines so that their kernels overlap on
-the GPU. StepServer takes requests -- num_steps implicit steps of a swimmer
+the GPU, and the inner solves of FP32C swimmers share cooperative launches. StepServer takes requests -- num_steps implicit steps of a swimmer
 from a perturbed straight start -- keeps instances resident between
 requests, admits requests by a device-memory budget and reports each
 request's latency. There is no CPU path.
@@ -47,6 +47,16 @@ class SwimmerBatch:
                 (st == N.TFS_OK) | (st == N.TFS_ENOTCONV))):
             N.check(rc)
         return {"broyden_iters": b, "gmres_iters": g, "status": st}
+
+    def share_inner_solves(self, enable: bool) -> None:
+        """False: every swimmer solves on its own (kernel sequence)."""
+        N.check(self.lib.tfs_batch_share_inner_solves(self._h, int(bool(enable))))
+
+    def shared_solves(self) -> dict:
+        """Inner solves run in shared cooperative launches, and the launches."""
+        la, so = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        N.check(self.lib.tfs_batch_shared_solves(self._h, ctypes.byref(la), ctypes.byref(so)))
+        return {"launches": la.value, "solves": so.value}
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
@@ -130,6 +140,11 @@ class StepServer:
         c = N.ServerCounters()
         N.check(self.lib.tfs_server_stats(self._h, ctypes.byref(c)))
         return {k: getattr(c, k) for k, _ in c._fields_}
+
+    def shared_solves(self) -> dict:
+        la, so = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        N.check(self.lib.tfs_server_shared_solves(self._h, ctypes.byref(la), ctypes.byref(so)))
+        return {"launches": la.value, "solves": so.value}
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
