@@ -110,6 +110,11 @@ int tfs_evaluate_segment_segment_mobility(tfs_solver *s); /* v_segs  = Mss f_seg
 int tfs_evaluate_segment_blob_mobility(tfs_solver *s);    /* v_segs += Msb f_blobs (:276-292, :551-636) */
 int tfs_evaluate_blob_blob_mobility(tfs_solver *s);       /* v_blobs = Mbb f_blobs (:294-310, :476-549) */
 int tfs_evaluate_blob_segment_mobility(tfs_solver *s);    /* v_blobs = Mbs f_segs  (:312-328, :638-757) */
+/* v_blobs = Mbb f_blobs in float-float arithmetic (each pair quantity an
+ * unevaluated sum of two FP32 numbers, about 1e-13 relative), whatever the
+ * solver's precision: the product FP32C refinement computes its residuals
+ * with. No counterpart in the reference. */
+int tfs_evaluate_blob_blob_mobility_ff(tfs_solver *s);
 /* evaluate_full_mobility (rpy_mobility_solver.cu:330-337): Mss + Msb into
  * v_segs and Mbb, then Mbs into v_blobs -- the reference's sequence assigns
  * v_blobs twice, so v_blobs ends as Mbs f_segs; this entry reproduces that.

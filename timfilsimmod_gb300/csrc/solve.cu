@@ -525,9 +525,12 @@ int linear_solve(tfs_solver *s, int *iters) {
   double prev_rel = 0.0;
   bool stalled = false;
   for (int it = 0; it <= s->max_outer; ++it) {
-    cudaError_t e = launch_pack(0, 3, s->rec_blobs, s->x_blobs, s->xr, s->nb, nullptr, s->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "pack");
-    if ((rc = mbb_product(s, 0, nullptr)) != TFS_OK) return rc;
+    // the residual's M_bb product in float-float arithmetic (FP64-grade
+    // accuracy at FP32 instruction rates)
+    cudaError_t e = launch_bb_ff(s->x_blobs, s->xr, s->nb, s->origin, s->cfg.a_blob,
+                                 1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu), s->rec_ff, s->vtmp, s->scratch,
+                                 s->scratch_elems, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "refinement residual product");
     if ((e = launch_refine_residual(g64, s->xr, s->r, s->dx, it, s->stream)) != cudaSuccess)
       return cuda_fail(e, "refinement residual");
     if ((rc = poll(s, 1, &h)) != TFS_OK) return rc;

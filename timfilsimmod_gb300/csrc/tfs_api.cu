@@ -99,6 +99,7 @@ static void free_all(tfs_solver *s) {
   cudaFree(s->rec_blobs);
   cudaFree(s->rec_segs_x2);
   cudaFree(s->rec_blobs_x2);
+  cudaFree(s->rec_ff);
   cudaFree(s->scratch);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
@@ -264,6 +265,7 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
       (rc = alloc_dev(&s->rec_blobs, record_bytes(0, 3) * nb)) ||
       (rc = alloc_dev(&s->rec_segs_x2, 80 * (size_t)ns)) ||
       (rc = alloc_dev(&s->rec_blobs_x2, 48 * (size_t)nb)) ||
+      (rc = alloc_dev(&s->rec_ff, ff_record_bytes() * nb)) ||
       (rc = alloc_dev((void **)&s->scratch, dsz * s->scratch_elems)) ||
       (rc = solve_alloc(s))) {
     free_all(s);
@@ -428,6 +430,16 @@ int tfs_evaluate_segment_blob_mobility(tfs_solver *s) {
 int tfs_evaluate_blob_blob_mobility(tfs_solver *s) {
   TFS_CHECK_SOLVER(s);
   return product(s, false, false, true, OUT_ASSIGN);
+}
+int tfs_evaluate_blob_blob_mobility_ff(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  int rc;
+  if ((rc = ensure_origin(s)) != TFS_OK) return rc;
+  cudaError_t e = launch_bb_ff(s->x_blobs, s->f_blobs, s->nb, s->origin, s->cfg.a_blob,
+                               1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu), s->rec_ff, s->v_blobs, s->scratch,
+                               s->scratch_elems, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "float-float blob-blob product");
+  return TFS_OK;
 }
 int tfs_evaluate_blob_segment_mobility(tfs_solver *s) {
   TFS_CHECK_SOLVER(s);

@@ -106,6 +106,15 @@ cudaError_t launch_tile(const TileArgs &a, int vd, int fda, int fdb, TileTuning 
                         double *scratch, size_t scratch_elems, int mode, cudaStream_t st,
                         cudaEvent_t *ev = nullptr);
 cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st);
+// out = M_bb f_blobs in float-float arithmetic (rpy_ff.cu): packs the source
+// records into rec (ff_record_bytes() per blob), then the pair kernel and,
+// with source splits, the split reduction (scratch as for launch_tile). ev
+// (optional): events around the pair kernel.
+size_t ff_record_bytes();
+cudaError_t launch_bb_ff(const double *x_blobs, const double *f_blobs, int nb,
+                         const double *origin, double a_blob, double scale, void *rec, double *out,
+                         double *scratch, size_t scratch_elems, cudaStream_t st,
+                         cudaEvent_t *ev = nullptr);
 // out[i] (= or += with accumulate) sum over splits s, in order, of
 // partial[s * n_elems + i].
 cudaError_t launch_reduce_partials(double *out, const double *partial, int n_elems, int splits,

@@ -31,6 +31,7 @@ struct tfs_solver {
   unsigned *origin_cnt = nullptr;  // [2] last-CTA counters of the origin passes
   void *rec_segs = nullptr, *rec_blobs = nullptr;
   void *rec_segs_x2 = nullptr, *rec_blobs_x2 = nullptr;  // FP32x2 records
+  void *rec_ff = nullptr;  // float-float blob records (the refinement residual)
   double *scratch = nullptr;
   size_t scratch_elems = 0;
   bool origin_dirty = true;

@@ -209,6 +209,11 @@ class RpyMobilitySolver:
     def evaluate_blob_blob_mobility(self):
         self._call("tfs_evaluate_blob_blob_mobility")
 
+    def evaluate_blob_blob_mobility_ff(self):
+        """v_blobs = Mbb f_blobs in float-float arithmetic (~1e-13): the
+        product FP32C refinement computes its residuals with."""
+        self._call("tfs_evaluate_blob_blob_mobility_ff")
+
     def evaluate_blob_segment_mobility(self):
         self._call("tfs_evaluate_blob_segment_mobility")
 
