@@ -47,7 +47,8 @@ def make_instance(subdiv, nfil, precision):
     return s, st
 
 
-@pytest.mark.parametrize("precision,share", [("fp64", False), ("fp32c", False), ("fp32c", True)])
+@pytest.mark.parametrize("precision,share", [("fp64", False), ("fp32c", False), ("fp32c", True),
+                                             ("fp32c", -1)])
 def test_batch_same_as_alone(precision, share):
     from timfilsimmod_gb300.serving import SwimmerBatch
 
@@ -60,7 +61,7 @@ def test_batch_same_as_alone(precision, share):
         one.add(st)
         for nt in range(steps):
             one.step(nt, allow_unconverged=True)
-        if share:
+        if share is True:
             sh = one.shared_solves()
             assert sh["solves"] > 0 and sh["launches"] == sh["solves"], sh
         alone.append(st.state())
@@ -76,7 +77,7 @@ def test_batch_same_as_alone(precision, share):
         out = batch.step(nt, allow_unconverged=True)
         assert np.all(out["gmres_iters"] > 0)
     sh = batch.shared_solves()
-    if share:
+    if share is not False:  # these swimmers (<= 642 blobs, 11 CTAs) share by default too
         assert sh["solves"] > 0 and 0 < sh["launches"] <= sh["solves"], sh
     else:
         assert sh == {"launches": 0, "solves": 0}

@@ -61,8 +61,6 @@ __device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {
   return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 
-__device__ __forceinline__ FF ff_norm(FF a) { return ff_fast_two_sum(a.h, a.l); }
-
 // a * b; the exact product of the high words plus the cross terms (the
 // product of the low words, ~2^-48 relative, is dropped); unnormalised.
 __device__ __forceinline__ FF ff_mul(FF a, FF b) {

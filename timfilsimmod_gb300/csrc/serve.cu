@@ -35,6 +35,7 @@
 #include <thread>
 #include <vector>
 
+#include "tfs_kernels.h"
 #include "tfs_solver.h"
 
 using tfs::fail;
@@ -112,8 +113,9 @@ struct tfs_batch {
   std::unique_ptr<WorkerPool> pool;
   std::vector<tfs_stepper *> inst;
   std::vector<char> shared;  // the instance's inner solves can go through the service
+  std::vector<int> shared_ctas;  // CTAs of its solve in a shared launch
   tfs::GmresService *service = nullptr;
-  bool share = false;
+  int share_max_ctas = -1;  // -1: one eighth of the SMs
   ~tfs_batch() { tfs::service_destroy(service); }
 };
 
@@ -156,6 +158,7 @@ int tfs_batch_add(tfs_batch *b, tfs_stepper *st, int *index) {
   }
   b->inst.push_back(st);
   b->shared.push_back(shared);
+  b->shared_ctas.push_back(shared ? s->pg_group.P : 0);
   if (index) *index = (int)b->inst.size() - 1;
   return TFS_OK;
 }
@@ -166,9 +169,9 @@ int tfs_batch_size(tfs_batch *b, int *n) {
   return TFS_OK;
 }
 
-int tfs_batch_share_inner_solves(tfs_batch *b, int enable) {
+int tfs_batch_share_inner_solves(tfs_batch *b, int max_ctas) {
   if (b == nullptr) return fail(TFS_EINVAL, "null batch");
-  b->share = enable != 0;
+  b->share_max_ctas = max_ctas < 0 ? -1 : max_ctas;
   return TFS_OK;
 }
 
@@ -188,8 +191,10 @@ int tfs_batch_step(tfs_batch *b, int nt, int *broyden_iters, int *gmres_iters, i
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
     return tfs::stepper_segments(b->inst[x]) > tfs::stepper_segments(b->inst[y]);
   });
+  const int cap = b->share_max_ctas >= 0 ? b->share_max_ctas : std::max(1, tfs::num_sms() / 8);
   for (int i = 0; i < n; ++i)
-    if (b->share && b->shared[i]) tfs::stepper_solver(b->inst[i])->service = b->service;
+    if (b->shared[i] && b->shared_ctas[i] <= cap)
+      tfs::stepper_solver(b->inst[i])->service = b->service;
   b->pool->run(n, [&](int k) {
     const int i = order[k];
     rc[i] = tfs_stepper_step(b->inst[i], nt, &bi[i], &gi[i]);

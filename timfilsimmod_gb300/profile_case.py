@@ -56,7 +56,11 @@ def run_steps(sw, args):
     st = ImplicitStepper(s, sw.nfil, sw.nseg, fil_refs, normals, seg_sep=sw.seg_sep, dt=1e-3,
                          tol=1e-4, end_force_magnitude=efm, body_radius=sw.radius)
     t0 = time.perf_counter()
+    from .mobility import kernel_launch_count
+
     for nt in range(args.reps):
+        # the launch index where step nt begins (ncu -s skips the ones before)
+        print(f"kernel launches before step {nt}: {kernel_launch_count()}")
         b, g = st.step(nt, allow_unconverged=True)
         print(f"step {nt}: {b} Broyden iterations, {g} GMRES iterations")
     s.wait_for_device()

@@ -48,9 +48,13 @@ class SwimmerBatch:
             N.check(rc)
         return {"broyden_iters": b, "gmres_iters": g, "status": st}
 
-    def share_inner_solves(self, enable: bool) -> None:
-        """False: every swimmer solves on its own (kernel sequence)."""
-        N.check(self.lib.tfs_batch_share_inner_solves(self._h, int(bool(enable))))
+    def share_inner_solves(self, max_ctas: int | bool = -1) -> None:
+        """FP32C swimmers whose inner solve takes at most max_ctas CTAs (one
+        per 64 blobs) share cooperative launches; True: all, False / 0: none,
+        -1 (the default): one eighth of the SMs."""
+        if max_ctas is True:
+            max_ctas = 1 << 30
+        N.check(self.lib.tfs_batch_share_inner_solves(self._h, int(max_ctas)))
 
     def shared_solves(self) -> dict:
         """Inner solves run in shared cooperative launches, and the launches."""
