@@ -51,7 +51,7 @@ constexpr int kPK = 352;       // Krylov columns + 1 (max_iter <= 350)
 constexpr int kMaxRows = 3 * kMaxPgBlobsPerCta;
 constexpr int kHB = 4096;      // doubles of the staging buffer (H columns, M_bb partials)
 
-constexpr int kPgDynFixed = kHB + 8 * kMaxPgCtas + 6 * kPK;  // doubles before qres
+constexpr int kPgDynFixed = kHB + 8 * kMaxPgCtas + 12 * kPK;  // doubles before qres
 
 // control words CTA 0 publishes each Arnoldi step
 enum { C_FINISH = 0, C_REL, C_STATUS, kCtl };
@@ -70,34 +70,34 @@ __device__ __forceinline__ unsigned long long global_ns() {
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
 
 // Bounded grid barrier; false in every thread of the CTA if it was abandoned.
-__device__ bool pg_barrier(const PgArgs &p) {
+// bar[0] counts arrivals over the whole launch (zeroed before it): the e-th
+// barrier of a solve is passed once it reaches e * P, so no CTA has to reset
+// it (each CTA keeps its own count e in *epoch, shared memory). bar[2] is
+// the abort word. Every CTA's prior writes are ordered before its arrival by
+// the CTA barrier plus a device-scope fence, and reads after the barrier
+// bypass L1 (ld.global.cg) wherever they read other CTAs' data.
+__device__ bool pg_barrier(const PgArgs &p, unsigned *epoch) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned *vb = p.bar;
     int good = 1;
-    const unsigned gen = vb[1];
+    const unsigned target = (*epoch + 1u) * (unsigned)p.P;
+    *epoch += 1u;
     __threadfence();
-    const unsigned arrived = atomicAdd(p.bar, 1u);
-    if (arrived == (unsigned)p.P - 1) {
-      atomicExch(p.bar, 0u);  // no CTA arrives again before the generation moves
-      __threadfence();
-      atomicAdd(p.bar + 1, 1u);
-    } else {
-      const unsigned long long t0 = global_ns();
-      unsigned spins = 0;
-      while (vb[1] == gen) {
-        if (vb[2] != 0u) {  // another CTA gave up
-          good = 0;
-          break;
-        }
-        ++spins;
-        if (spins > (1u << 25) || ((spins & 63u) == 0 && global_ns() - t0 > kPgTimeoutNs)) {
-          atomicExch(p.bar + 2, 1u);
-          good = 0;
-          break;
-        }
-        __nanosleep(32);
+    atomicAdd(p.bar, 1u);
+    const unsigned long long t0 = global_ns();
+    unsigned spins = 0;
+    while (vb[0] < target) {
+      if (vb[2] != 0u) {  // another CTA gave up
+        good = 0;
+        break;
+      }
+      ++spins;
+      if (spins > (1u << 25) || ((spins & 63u) == 0 && global_ns() - t0 > kPgTimeoutNs)) {
+        atomicExch(p.bar + 2, 1u);
+        good = 0;
+        break;
       }
     }
     __threadfence();
@@ -458,6 +458,44 @@ __device__ void reduce_dots(const PgArgs &p, const double *pd, int k, const doub
   }
 }
 
+// The same sums as reduce_dots, h[j] for j < k into shared memory, in every
+// CTA (identical bits: the same order), when the k x G partials fit the
+// staging buffers stg (hb and the partial-sum staging after it): false, with
+// nothing done, otherwise. The partials are staged with eight loads in
+// flight per thread. Ends with a barrier.
+__device__ bool local_dots(const PgArgs &p, const double *pd, int k, const double *wv,
+                           const double *qvres, double *h, double *stg) {
+  const int G = p.g.G, tot = k * G;
+  if (tot > kHB + 8 * kMaxPgCtas) return false;
+  for (int q0 = 0; q0 < tot; q0 += 8 * kPB) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + u * kPB + (int)threadIdx.x;
+      v[u] = q < tot ? ldcg(pd + q) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + u * kPB + (int)threadIdx.x;
+      if (q < tot) stg[q] = v[u];
+    }
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j = wid; j < k; j += kPW) {
+    double s = 0.0;
+    for (int c = lane; c < G; c += 32) s += stg[(size_t)j * G + c];
+    s = warp_sum(s);
+    if (lane == 0) {
+      double t = 0.0;
+      for (int l = 0; l < 6; ++l) t += wv[l] * qvres[6 * j + l];
+      h[j] = s + t;
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
 // Givens rotations of the new Hessenberg column (mobility_solver.cpp:
 // 2370-2413): hcol[0..k] in, rotated in place; updates cs, sn, beta;
 // returns |beta_k| / norm_rhs. One thread.
@@ -543,17 +581,21 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
   }
   __syncthreads();
   const PgArgs &p = pshared;
+  __shared__ unsigned epoch;  // grid barriers passed (thread 0)
+  if (threadIdx.x == 0) epoch = 0u;
   __shared__ __align__(16) float src[8 * kPTS];
   __shared__ double ws[kMaxRows];            // w (then Q_k, tmp) rows of the slice
   __shared__ double zs[kMaxRows];            // z = P^-1 q rows of the slice
   __shared__ double h1[kPK], h2[kPK], cs[kPK], sn[kPK], beta[kPK], hcol[kPK], yv[kPK];
   __shared__ double tmp8[8];
-  __shared__ double wvel[6], qvel[6], zv[6];
+  __shared__ double wvel[6], qvel[6], zv[6], wsum6[6];
   __shared__ double dsl[kMaxRows], mats[72], qn_s[2];
   // dynamic: staging buffer (kHB), staged per-CTA partials (8 x kMaxPgCtas),
-  // body rows of every Krylov vector (6 x kPK), resident Krylov rows (Kr x rows)
+  // body rows of every Krylov vector (6 x kPK), sum_m (Q_i,m ; d_m x Q_i,m)
+  // of every Krylov vector (6 x kPK), resident Krylov rows (Kr x rows)
   extern __shared__ double dyn[];
-  double *hb = dyn, *cst = hb + kHB, *qvres = cst + 8 * kMaxPgCtas, *qres = qvres + 6 * kPK;
+  double *hb = dyn, *cst = hb + kHB, *qvres = cst + 8 * kMaxPgCtas, *qsres = qvres + 6 * kPK,
+         *qres = qsres + 6 * kPK;
 
   const GmresArgs &g = p.g;
   GmresScalars *st = g.st;
@@ -579,11 +621,11 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
   pack_records(p, sl, ws);
   slice_partials(p, sl, zs, K_RHS, S_RHS);
   slice_partials(p, sl, ws, K_SOLN, -1);
-  if (!pg_barrier(p)) return;
+  if (!pg_barrier(p, &epoch)) return;
 
   // ---- M_bb of the warm start
   mbb_units(p, src);
-  if (!pg_barrier(p)) return;
+  if (!pg_barrier(p, &epoch)) return;
 
   // ---- residual r0 = rhs - A soln (slice rows), partials
   if (threadIdx.x < 6) zv[threadIdx.x] = g.v_bodies[threadIdx.x];
@@ -592,7 +634,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
   for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = zs[r] - ws[r];  // zs = rhs rows
   __syncthreads();
   slice_partials(p, sl, ws, K_R0, S_R0);
-  if (!pg_barrier(p)) return;
+  if (!pg_barrier(p, &epoch)) return;
 
   // ---- beta_0, warm-start tests (mobility_solver.cpp:2279-2320), Q_0,
   //      preconditioner of Q_0, records (every CTA decides the same)
@@ -664,11 +706,12 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     if (threadIdx.x == 0) beta[0] = beta0;
     // z = P^-1 Q_0: sum_m (Q_0 ; d x Q_0) = (partials of the unscaled vector) / inv
     cta_sums(p.p6 + (size_t)kslot * 6 * G, G, 6, tmp8, cst);
+    if (threadIdx.x < 6) qsres[threadIdx.x] = tmp8[threadIdx.x] * (1.0 / inv);
     precond(p, sl, ws, qvel, tmp8, 1.0 / inv, zs, zv, mats);
     pack_records(p, sl, zs);
     slice_partials(p, sl, zs, K_Z, -1);
   }
-  if (!pg_barrier(p)) return;
+  if (!pg_barrier(p, &epoch)) return;
 
   // ---- Arnoldi steps. Step k: M_bb z_{k-1} (CTA 0 meanwhile finishes step
   //      k-1's Givens rotation and convergence test), w = A z_{k-1}, two
@@ -708,7 +751,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
         p.aux[C_STATUS] = tmp8[2];
       }
     }
-    if (!pg_barrier(p)) return;
+    if (!pg_barrier(p, &epoch)) return;
     if (k > 1 && ldcg(p.aux + C_FINISH) != 0.0) {
       k -= 1;
       break;
@@ -748,41 +791,54 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     }
     if (threadIdx.x < 6) wvel[threadIdx.x] = -tmp8[threadIdx.x];
     slice_dots(p, sl, ws, k, p.pd1, qres);
-    if (!pg_barrier(p)) return;
-    reduce_dots(p, p.pd1, k, wvel, qvres, h1g);
-    if (!pg_barrier(p)) return;
+    if (!pg_barrier(p, &epoch)) return;
+    // h1 (summed by every CTA while the partials fit the staging buffers,
+    // else spread over the grid and published)
+    if (!local_dots(p, p.pd1, k, wvel, qvres, h1, hb)) {
+      reduce_dots(p, p.pd1, k, wvel, qvres, h1g);
+      if (!pg_barrier(p, &epoch)) return;
+      for (int i = threadIdx.x; i < k; i += kPB) h1[i] = ldcg(h1g + i);
+      __syncthreads();
+    }
 
-    // h1; w -= Q h1; CGS pass 2 partial dots
-    for (int i = threadIdx.x; i < k; i += kPB) h1[i] = ldcg(h1g + i);
-    __syncthreads();
+    // w' = w - Q h1; CGS pass 2 partial dots, and ||w'||^2 and
+    // sum (w' ; d x w') partials
     slice_axpy(p, sl, h1, k, ws, -1.0, qres);
     vel_axpy(qvres, h1, k, wvel, -1.0);
     slice_dots(p, sl, ws, k, p.pd2, qres);
-    if (!pg_barrier(p)) return;
-    reduce_dots(p, p.pd2, k, wvel, qvres, h2g);
-    if (!pg_barrier(p)) return;
-
-    // h2; w -= Q h2; ||w|| and sum (w ; d x w) partials
-    for (int i = threadIdx.x; i < k; i += kPB) h2[i] = ldcg(h2g + i);
-    __syncthreads();
-    slice_axpy(p, sl, h2, k, ws, -1.0, qres);
-    vel_axpy(qvres, h2, k, wvel, -1.0);
     slice_partials(p, sl, ws, K_W, S_NORM);
-    if (!pg_barrier(p)) return;
+    if (!pg_barrier(p, &epoch)) return;
+    if (!local_dots(p, p.pd2, k, wvel, qvres, h2, hb)) {
+      reduce_dots(p, p.pd2, k, wvel, qvres, h2g);
+      if (!pg_barrier(p, &epoch)) return;
+      for (int i = threadIdx.x; i < k; i += kPB) h2[i] = ldcg(h2g + i);
+      __syncthreads();
+    }
 
-    // ||w||, Q_k = w / ||w||, z_k = P^-1 Q_k (sum (Q_k ; d x Q_k) = K_W / ||w||)
+    // w'' = w' - Q h2; with Q orthonormal, ||w''||^2 = ||w'||^2 - ||h2||^2
+    // and sum (w'' ; d x w'') = sum (w' ; d x w') - sum_i h2_i S_i, S_i the
+    // sums of Q_i (kept in qsres); Q_k = w'' / ||w''||, z_k = P^-1 Q_k.
     stage(p.ps + (size_t)S_NORM * G, G, cst);
     stage(p.p6 + (size_t)K_W * 6 * G, 6 * G, cst + G);
     __syncthreads();
     sum_staged(cst, G, 7, tmp8);
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = tmp8[0];
+    if (threadIdx.x < 6) {  // the body sums of w'' (thread j: component j)
+      const int j = threadIdx.x;
+      double t = 0.0;
+      for (int i = 0; i < k; ++i) t += h2[i] * qsres[6 * i + j];
+      wsum6[j] = tmp8[1 + j] - t;
+    }
+    if (threadIdx.x == 32) {
+      double t = tmp8[0], hh = 0.0;
       for (int j = 0; j < 6; ++j) t += wvel[j] * wvel[j];
-      qn_s[0] = sqrt(t);
+      for (int i = 0; i < k; ++i) hh += h2[i] * h2[i];
+      qn_s[0] = sqrt(t - hh);
       qn_s[1] = 1.0 / qn_s[0];
     }
     __syncthreads();
+    slice_axpy(p, sl, h2, k, ws, -1.0, qres);
+    vel_axpy(qvres, h2, k, wvel, -1.0);
     qn = qn_s[0];
     const double rqn = qn_s[1];
     for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = ws[r] * rqn;
@@ -791,13 +847,14 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     if (threadIdx.x < 6) {
       qvel[threadIdx.x] = wvel[threadIdx.x] * rqn;
       qvres[6 * k + threadIdx.x] = qvel[threadIdx.x];
+      qsres[6 * k + threadIdx.x] = wsum6[threadIdx.x] * rqn;
       if (sl.body) g.Q[(size_t)k * n + vel + threadIdx.x] = qvel[threadIdx.x];
     }
     __syncthreads();
-    precond(p, sl, ws, qvel, tmp8 + 1, rqn, zs, zv, mats);
+    precond(p, sl, ws, qvel, wsum6, rqn, zs, zv, mats);
     pack_records(p, sl, zs);
     slice_partials(p, sl, zs, K_Z, -1);
-    if (!pg_barrier(p)) return;
+    if (!pg_barrier(p, &epoch)) return;
     ++k;
   }
 
@@ -810,7 +867,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
   slice_axpy(p, sl, yv, k, ws, 1.0, qres);
   vel_axpy(qvres, yv, k, qvel, 1.0);
   slice_partials(p, sl, ws, K_T, -1);
-  if (!pg_barrier(p)) return;
+  if (!pg_barrier(p, &epoch)) return;
   cta_sums(p.p6 + (size_t)K_T * 6 * G, G, 6, tmp8, cst);
   precond(p, sl, ws, qvel, tmp8, 1.0, zs, zv, mats);
   for (int r = threadIdx.x; r < sl.rows; r += kPB) {
