@@ -138,9 +138,42 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Stage elems doubles of buf (global) into dst (shared); no barrier.
+// Stage elems doubles of buf (global) into dst (shared), eight loads in
+// flight per thread; no barrier.
 __device__ __forceinline__ void stage(const double *buf, int elems, double *dst) {
-  for (int q = threadIdx.x; q < elems; q += kPB) dst[q] = ldcg(buf + q);
+  for (int q0 = 0; q0 < elems; q0 += 8 * kPB) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + u * kPB + (int)threadIdx.x;
+      v[u] = q < elems ? ldcg(buf + q) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + u * kPB + (int)threadIdx.x;
+      if (q < elems) dst[q] = v[u];
+    }
+  }
+}
+
+// Stage the slice's rows of the S split products (mpart, (hi, lo) FP32
+// pairs) into dst[sp * rows + r], eight loads in flight per thread; no barrier.
+__device__ __forceinline__ void stage_splits(const PgArgs &p, const PSlice &sl, float2 *dst) {
+  const int rows = sl.rows, tot = p.S * rows, nb = p.g.nb;
+  for (int q0 = 0; q0 < tot; q0 += 8 * kPB) {
+    float2 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + u * kPB + (int)threadIdx.x;
+      const int sp = q / max(rows, 1), r = q - sp * rows;
+      v[u] = q < tot ? __ldcg(p.mpart + ((size_t)sp * nb + sl.m0) * 3 + r) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + u * kPB + (int)threadIdx.x;
+      if (q < tot) dst[q] = v[u];
+    }
+  }
 }
 
 // out[j] = sum over c < G of cst[j * G + c], j < count <= kPW: warp j adds
@@ -164,33 +197,32 @@ __device__ void cta_sums(const double *buf, int G, int count, double *out, doubl
   __syncthreads();
 }
 
-// Warp 0: this CTA's partials of the slice rows ls: sum_m (l_m ; d_m x l_m)
-// into p6 slot kt_slot and, with sq_slot >= 0, the sum of squares into ps
-// slot sq_slot. No barrier; ls must be complete.
+// This CTA's partials of the slice rows ls: warp j < 6 sums component j of
+// sum_m (l_m ; d_m x l_m) into p6 slot kt_slot and, with sq_slot >= 0, warp
+// 6 the sum of squares into ps slot sq_slot (lanes stride over blobs or
+// rows, then a fixed shuffle tree). No barrier; ls must be complete.
 __device__ void slice_partials(const PgArgs &p, const PSlice &sl, const double *ls, int kt_slot,
                                int sq_slot) {
-  if (threadIdx.x >= 32 || !sl.owner) return;
-  const int lane = threadIdx.x;
-  double s[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (int m = sl.m0 + lane; m < sl.m1; m += 32) {
-    const double *d = sl.d + 3 * (m - sl.m0);
-    const double *v = ls + 3 * (m - sl.m0);
-    s[0] += v[0];
-    s[1] += v[1];
-    s[2] += v[2];
-    s[3] += d[1] * v[2] - d[2] * v[1];
-    s[4] += d[2] * v[0] - d[0] * v[2];
-    s[5] += d[0] * v[1] - d[1] * v[0];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (!sl.owner || wid >= (sq_slot >= 0 ? 7 : 6)) return;
+  double s = 0.0;
+  if (wid < 3) {
+    for (int m = sl.m0 + lane; m < sl.m1; m += 32) s += ls[3 * (m - sl.m0) + wid];
+  } else if (wid < 6) {  // (d x l)_j = d_a l_b - d_b l_a, (a, b) = (j + 1, j + 2) mod 3
+    const int a = (wid - 2) % 3, b = (wid - 1) % 3;
+    for (int m = sl.m0 + lane; m < sl.m1; m += 32) {
+      const double *d = sl.d + 3 * (m - sl.m0);
+      const double *v = ls + 3 * (m - sl.m0);
+      s += d[a] * v[b] - d[b] * v[a];
+    }
+  } else {
+    for (int r = lane; r < sl.rows; r += 32) s += ls[r] * ls[r];
   }
-  if (sq_slot >= 0)
-    for (int r = lane; r < sl.rows; r += 32) s[6] += ls[r] * ls[r];
-#pragma unroll
-  for (int j = 0; j < 6; ++j) s[j] = warp_sum(s[j]);
-  if (sq_slot >= 0) s[6] = warp_sum(s[6]);
+  s = warp_sum(s);
   if (lane == 0) {
     const int G = p.g.G, c = p.rank;
-    for (int j = 0; j < 6; ++j) p.p6[(size_t)(kt_slot * 6 + j) * G + c] = s[j];
-    if (sq_slot >= 0) p.ps[(size_t)sq_slot * G + c] = s[6];
+    if (wid < 6) p.p6[(size_t)(kt_slot * 6 + wid) * G + c] = s;
+    else p.ps[(size_t)sq_slot * G + c] = s;
   }
 }
 
@@ -206,9 +238,14 @@ __device__ void precond(const PgArgs &p, const PSlice &sl, const double *qs, con
     const int i = threadIdx.x;
     const double *N = mats, *Kinv = mats + 36;
     double t1 = 0.0, t2 = 0.0;
-    for (int k = 0; k < 6; ++k) t1 += Kinv[i + 6 * k] * (-bsum[k] * bscale);
-    for (int k = 0; k < 6; ++k) t2 += N[i + 6 * k] * qvel[k];
-    zv[i] = t1 - t2;
+    double u1 = 0.0, u2 = 0.0;
+    for (int k = 0; k < 6; k += 2) {
+      t1 += Kinv[i + 6 * k] * (-bsum[k] * bscale);
+      u1 += Kinv[i + 6 * (k + 1)] * (-bsum[k + 1] * bscale);
+      t2 += N[i + 6 * k] * qvel[k];
+      u2 += N[i + 6 * (k + 1)] * qvel[k + 1];
+    }
+    zv[i] = (t1 + u1) - (t2 + u2);
   }
   __syncthreads();
   const double u0 = zv[0], u1 = zv[1], u2 = zv[2], w0 = zv[3], w1 = zv[4], w2 = zv[5];
@@ -390,38 +427,66 @@ __device__ void store_q(const PgArgs &p, const PSlice &sl, double *qres, int i, 
   }
 }
 
-// dots of the slice rows ws with Q_i, i < k (one thread per i, rows in
-// order) into pd[i * G + c]
+// dots of the slice rows ws with Q_i, i < k, into pd[i * G + c]: tpi
+// adjacent threads per i (16, 8 or 4 as k allows one pass; four per pass
+// beyond), rows r = part (mod tpi), then a fixed shuffle tree.
 __device__ void slice_dots(const PgArgs &p, const PSlice &sl, const double *ws, int k,
                            double *pd, const double *qres) {
   if (!sl.owner) return;
-  // four threads (adjacent lanes) per i, rows r = part (mod 4), then a fixed
-  // two-level shuffle; k <= kPB / 4 per pass
-  const int part = threadIdx.x & 3;
-  for (int i0 = 0; i0 < k; i0 += kPB / 4) {
-    const int i = i0 + (threadIdx.x >> 2);
-    double s = 0.0;
+  const int tpi = k <= kPB / 16 ? 16 : k <= kPB / 8 ? 8 : 4;
+  const int part = threadIdx.x & (tpi - 1);
+  for (int i0 = 0; i0 < k; i0 += kPB / tpi) {
+    const int i = i0 + (int)threadIdx.x / tpi;
+    double s = 0.0, u = 0.0;
     if (i < k) {
+      int r = part;
       if (i < p.Kr) {
         const double *q = qres + (size_t)i * sl.rows;
-        for (int r = part; r < sl.rows; r += 4) s += ws[r] * q[r];
+        for (; r + tpi < sl.rows; r += 2 * tpi) {
+          s += ws[r] * q[r];
+          u += ws[r + tpi] * q[r + tpi];
+        }
+        if (r < sl.rows) s += ws[r] * q[r];
       } else {
-        for (int r = part; r < sl.rows; r += 4) s += ws[r] * qrow(p, sl, qres, i, r);
+        for (; r < sl.rows; r += tpi) s += ws[r] * qrow(p, sl, qres, i, r);
       }
     }
-    s += __shfl_xor_sync(0xffffffffu, s, 1);
-    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    s += u;
+    for (int o = 1; o < tpi; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (i < k && part == 0) pd[(size_t)i * p.g.G + p.rank] = s;
   }
 }
 
-// ws (slice rows) += sign * sum_{i<k} h_i Q_i (one thread per row, i in order)
+// ws (slice rows) += sign * sum_{i<k} h_i Q_i: four adjacent threads per row
+// (when the rows allow), each over i = sub (mod 4) with two running sums,
+// then a fixed shuffle tree; one thread per row with four sums otherwise.
 __device__ void slice_axpy(const PgArgs &p, const PSlice &sl, const double *h, int k, double *ws,
                            double sign, const double *qres) {
-  for (int r = threadIdx.x; r < sl.rows; r += kPB) {
-    double t = 0.0;
-    for (int i = 0; i < k; ++i) t += h[i] * qrow(p, sl, qres, i, r);
-    ws[r] += sign * t;
+  if (4 * sl.rows <= kPB) {
+    const int r = threadIdx.x >> 2, sub = threadIdx.x & 3;
+    double t = 0.0, u = 0.0;
+    if (r < sl.rows) {
+      int i = sub;
+      for (; i + 4 < k; i += 8) {
+        t += h[i] * qrow(p, sl, qres, i, r);
+        u += h[i + 4] * qrow(p, sl, qres, i + 4, r);
+      }
+      if (i < k) t += h[i] * qrow(p, sl, qres, i, r);
+    }
+    t += u;
+    t += __shfl_xor_sync(0xffffffffu, t, 1);
+    t += __shfl_xor_sync(0xffffffffu, t, 2);
+    if (r < sl.rows && sub == 0) ws[r] += sign * t;
+  } else {
+    for (int r = threadIdx.x; r < sl.rows; r += kPB) {
+      double t[4] = {0.0, 0.0, 0.0, 0.0};
+      int i = 0;
+      for (; i + 3 < k; i += 4)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) t[u] += h[i + u] * qrow(p, sl, qres, i + u, r);
+      for (; i < k; ++i) t[0] += h[i] * qrow(p, sl, qres, i, r);
+      ws[r] += sign * ((t[0] + t[1]) + (t[2] + t[3]));
+    }
   }
   __syncthreads();
 }
@@ -441,20 +506,17 @@ __device__ void vel_axpy(const double *qvres, const double *h, int k, double *v,
 
 // Gram-Schmidt coefficients, spread over the grid: warp w of CTA c sums
 // h_j = sum_c' pd[j * G + c'] + w_vel . Q_j,vel for j = c + P (w + kPW t),
-// into hg[j] (global).
+// into hg[j] (global); lanes l < 6 start from the body term w_vel,l Q_j,vel(l),
+// lanes stride over c', then a fixed shuffle tree.
 __device__ void reduce_dots(const PgArgs &p, const double *pd, int k, const double *wv,
                             const double *qvres, double *hg) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int G = p.g.G;
   for (int j = p.rank + p.P * wid; j < k; j += p.P * kPW) {
-    double s = 0.0;
+    double s = lane < 6 ? wv[lane] * qvres[6 * j + lane] : 0.0;
     for (int c = lane; c < G; c += 32) s += ldcg(pd + (size_t)j * G + c);
     s = warp_sum(s);
-    if (lane == 0) {
-      double t = 0.0;
-      for (int l = 0; l < 6; ++l) t += wv[l] * qvres[6 * j + l];
-      hg[j] = s + t;
-    }
+    if (lane == 0) hg[j] = s;
   }
 }
 
@@ -483,14 +545,10 @@ __device__ bool local_dots(const PgArgs &p, const double *pd, int k, const doubl
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int j = wid; j < k; j += kPW) {
-    double s = 0.0;
+    double s = lane < 6 ? wv[lane] * qvres[6 * j + lane] : 0.0;
     for (int c = lane; c < G; c += 32) s += stg[(size_t)j * G + c];
     s = warp_sum(s);
-    if (lane == 0) {
-      double t = 0.0;
-      for (int l = 0; l < 6; ++l) t += wv[l] * qvres[6 * j + l];
-      h[j] = s + t;
-    }
+    if (lane == 0) h[j] = s;
   }
   __syncthreads();
   return true;
@@ -762,26 +820,36 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     stage(p.p6 + (size_t)K_Z * 6 * G, 6 * G, cst);
     if (p.S * sl.rows <= kHB) {
       float2 *st2 = reinterpret_cast<float2 *>(hb);
-      for (int q = threadIdx.x; q < p.S * sl.rows; q += kPB) {
-        const int sp = q / sl.rows, r = q - sp * sl.rows;
-        st2[q] = __ldcg(p.mpart + ((size_t)sp * nb + sl.m0) * 3 + r);
-      }
+      stage_splits(p, sl, st2);
       __syncthreads();
       sum_staged(cst, G, 6, tmp8);
-      for (int r = threadIdx.x; r < sl.rows; r += kPB) {
+      // tpr adjacent threads per row add the splits sp = sub (mod tpr),
+      // compensated, then combine their (hi, lo) pairs by a fixed shuffle tree
+      const int tpr = 8 * sl.rows <= kPB ? 8 : 4 * sl.rows <= kPB ? 4 : 2 * sl.rows <= kPB ? 2 : 1;
+      for (int r0 = 0; r0 < sl.rows; r0 += kPB / tpr) {
+        const int r = r0 + (int)threadIdx.x / tpr, sub = threadIdx.x & (tpr - 1);
         float h = 0.f, l = 0.f;
-        for (int sp = 0; sp < p.S; ++sp) {
-          two_sum(h, l, st2[sp * sl.rows + r].x);
-          l += st2[sp * sl.rows + r].y;
+        if (r < sl.rows)
+          for (int sp = sub; sp < p.S; sp += tpr) {
+            two_sum(h, l, st2[sp * sl.rows + r].x);
+            l += st2[sp * sl.rows + r].y;
+          }
+        for (int o = 1; o < tpr; o <<= 1) {
+          const float ho = __shfl_xor_sync(0xffffffffu, h, o);
+          const float lo = __shfl_xor_sync(0xffffffffu, l, o);
+          two_sum(h, l, ho);
+          l += lo;
         }
-        const double v = p.scale * ((double)h + (double)l);
-        const int m = sl.m0 + r / 3, j = r - 3 * (r / 3);
-        const double *d = sl.d + 3 * (m - sl.m0);
-        double body;
-        if (j == 0) body = zv[0] - d[1] * zv[5] + d[2] * zv[4];
-        else if (j == 1) body = zv[1] - d[2] * zv[3] + d[0] * zv[5];
-        else body = zv[2] - d[0] * zv[4] + d[1] * zv[3];
-        ws[r] = -body + v;
+        if (r < sl.rows && sub == 0) {
+          const double v = p.scale * ((double)h + (double)l);
+          const int m = sl.m0 + r / 3, j = r - 3 * (r / 3);
+          const double *d = sl.d + 3 * (m - sl.m0);
+          double body;
+          if (j == 0) body = zv[0] - d[1] * zv[5] + d[2] * zv[4];
+          else if (j == 1) body = zv[1] - d[2] * zv[3] + d[0] * zv[5];
+          else body = zv[2] - d[0] * zv[4] + d[1] * zv[3];
+          ws[r] = -body + v;
+        }
       }
       __syncthreads();
     } else {
@@ -823,18 +891,29 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     __syncthreads();
     sum_staged(cst, G, 7, tmp8);
     __syncthreads();
-    if (threadIdx.x < 6) {  // the body sums of w'' (thread j: component j)
-      const int j = threadIdx.x;
-      double t = 0.0;
-      for (int i = 0; i < k; ++i) t += h2[i] * qsres[6 * i + j];
-      wsum6[j] = tmp8[1 + j] - t;
-    }
-    if (threadIdx.x == 32) {
-      double t = tmp8[0], hh = 0.0;
-      for (int j = 0; j < 6; ++j) t += wvel[j] * wvel[j];
-      for (int i = 0; i < k; ++i) hh += h2[i] * h2[i];
-      qn_s[0] = sqrt(t - hh);
-      qn_s[1] = 1.0 / qn_s[0];
+    {
+      // warp j < 6: the body sum j of w''; warp 6: ||w''||^2 (lanes over i)
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      if (wid < 7) {
+        double t = 0.0;
+        if (wid < 6) {
+          for (int i = lane; i < k; i += 32) t += h2[i] * qsres[6 * i + wid];
+        } else {
+          for (int i = lane; i < k; i += 32) t -= h2[i] * h2[i];
+          if (lane < 6) t += wvel[lane] * wvel[lane];
+        }
+        t = warp_sum(t);
+        if (lane == 0) {
+          if (wid < 6) {
+            wsum6[wid] = tmp8[1 + wid] - t;
+          } else {  // 1/||w''|| by the refined FP32 estimate (a few ulp)
+            const double w2 = tmp8[0] + t;
+            const double y = rsqrt_far(w2);
+            qn_s[0] = w2 * y;
+            qn_s[1] = y;
+          }
+        }
+      }
     }
     __syncthreads();
     slice_axpy(p, sl, h2, k, ws, -1.0, qres);
