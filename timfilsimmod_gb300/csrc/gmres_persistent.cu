@@ -329,7 +329,7 @@ __device__ void mbb_units(const PgArgs &p, float *src) {
       __syncthreads();
       if (!warp_active) continue;
       float v[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-      unsigned nf[2] = {0u, 0u};
+      unsigned nf[2] = {0u, 0u};  // pairs inside the contact distance
 #pragma unroll 2
       for (int j = 0; j < cnt; ++j) {
         float sx, sy, sz, f[3];
@@ -339,9 +339,28 @@ __device__ void mbb_units(const PgArgs &p, float *src) {
           const float dx = xt[t] - sx, dy = yt[t] - sy, dz = zt[t] - sz;
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
           const bool far = r2 > pc.asum2;
-          nf[t] |= far ? 0u : 1u;
+          nf[t] += far ? 0u : 1u;
           const float rs = rsqrt_far(r2);
           far_pair<float, 3, 3>(v[t], dx, dy, dz, far ? rs : 0.f, f, pc);
+        }
+      }
+      // a target whose only pair inside the contact distance in this tile is
+      // its own blob (r = 0) takes the self term 4/(3a) F here (the nested
+      // branch of the pair function at r = 0); targets with any other such
+      // pair rescan the tile with the full formula, self pair included
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int js = i[t] - base;
+        const unsigned self_in = (js >= 0 && js < cnt) ? 1u : 0u;
+        if (nf[t] == self_in) {
+          if (self_in) {
+            float sx, sy, sz, f[3];
+            RecLoad<float, 3>::get(src + 8 * js, sx, sy, sz, f);
+            const float A = 4.f / (3.f * pc.ai);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) v[t][k] += A * f[k];
+          }
+          nf[t] = 0u;
         }
       }
       if (__any_sync(0xffffffffu, (nf[0] | nf[1]) != 0u))

@@ -34,68 +34,14 @@
 #include <algorithm>
 #include <cmath>
 
+#include "ff_arith.cuh"
 #include "tfs_kernels.h"
 
 namespace tfs {
 
 namespace {
 
-// h + l, |l| <= ulp(h)/2 after normalisation (many intermediate values are
-// left unnormalised: |l| a few ulp of h).
-struct FF {
-  float h, l;
-};
-
-// Knuth's TwoSum: s + e = a + b exactly. The _rn intrinsics are never
-// contracted into FMAs, which would break the transformation.
-__device__ __forceinline__ FF ff_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return {s, e};
-}
-
-// Dekker's Fast2Sum (|a| >= |b|): s + e = a + b exactly.
-__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-
-// a * b; the exact product of the high words plus the cross terms (the
-// product of the low words, ~2^-48 relative, is dropped); unnormalised.
-__device__ __forceinline__ FF ff_mul(FF a, FF b) {
-  const float p = __fmul_rn(a.h, b.h);
-  float e = fmaf(a.h, b.h, -p);
-  e = fmaf(a.h, b.l, fmaf(a.l, b.h, e));
-  return {p, e};
-}
-
-// a + b, normalised (the "sloppy" double-word sum: its error is bounded
-// relative to |a| + |b|, which is what the velocity sums need).
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-  const FF s = ff_two_sum(a.h, b.h);
-  return ff_fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
-}
-
-// a - b for positions (unnormalised).
-__device__ __forceinline__ FF ff_sub(FF a, FF b) {
-  FF s = ff_two_sum(a.h, -b.h);
-  s.l = __fadd_rn(s.l, __fsub_rn(a.l, b.l));
-  return s;
-}
-
-// Compensated accumulation: v.h carries the running sum, v.l every rounding
-// error and low word.
-__device__ __forceinline__ void ff_acc(FF &v, FF t) {
-  const FF s = ff_two_sum(v.h, t.h);
-  v.h = s.h;
-  v.l = __fadd_rn(v.l, __fadd_rn(s.l, t.l));
-}
-
-__device__ __forceinline__ FF ff_split(double x) {
-  const float h = __double2float_rn(x);
-  return {h, __double2float_rn(x - (double)h)};
-}
+using namespace ff;
 
 // One source record: position (relative to the origin) and force, as three
 // float4: (xh, yh, zh, fxh), (fyh, fzh, xl, yl), (zl, fxl, fyl, fzl).

@@ -30,6 +30,7 @@
 #include <new>
 #include <vector>
 
+#include "ff_arith.cuh"
 #include "step_math.cuh"
 #include "tfs_solver.h"
 
@@ -555,10 +556,132 @@ __device__ M3 base_cross(const StepDev &d, const BodyArgs &b, int fil) {
   return rcross(v);
 }
 
+// JB A and the body's Lie-algebra self-dependence for filament fil, from the
+// stored JB (after a CTA barrier).
+__device__ void jac_tail(const StepDev &d, const BodyArgs &b, int fil, int n6, int n) {
+  const int tid = threadIdx.x;
+  const int s0 = fil * n;
+  const double *jb = d.jb + (size_t)6 * n6 * fil;
+  // JB A (6 x 6) with A = [I, D] per segment row block plus the elastic clamping blocks
+  if (tid < 36) {
+    const int r = tid / 6, c = tid % 6;
+    const M3 D = base_cross(d, b, fil);
+    const double *e1 = d.ecb + 18 * fil, *e2 = e1 + 9;
+    const double *row = jb + (size_t)r * n6;
+    double s = 0.0;
+    for (int k = 0; k < 3 * n; ++k) {
+      const int m = k % 3;
+      s += row[k] * (c < 3 ? (m == c ? 1.0 : 0.0) : D.a[3 * m + c - 3]);
+    }
+    if (c >= 3) {
+      for (int m = 0; m < 3; ++m) s += row[3 * n + m] * e1[3 * m + c - 3];
+      for (int m = 0; m < 3; ++m) s += row[3 * n + 3 + m] * e2[3 * m + c - 3];
+    }
+    d.part[45 * fil + tid] = s;
+  }
+  if (tid == 64) {  // this filament's share of the body's Lie-algebra self-dependence
+    double fbd[3];
+    m3_vec(m3_from(b.Q), d.fil_refs + 3 * fil, fbd);
+    const double *tl = d.teth + 3 * fil, *cl = d.clamp + 3 * fil;
+    const double ucl[3] = {b.u[1] * cl[2] - b.u[2] * cl[1], b.u[2] * cl[0] - b.u[0] * cl[2],
+                           b.u[0] * cl[1] - b.u[1] * cl[0]};
+    M3 o = m3_scale(-1.0, m3_mul(rcross(tl), rcross(fbd)));
+    o = m3_add(o, m3_sub(m3_scale(0.5, rcross(cl)),
+                         m3_div(m3_add(rcross(ucl), m3_mul(m3_from(b.blc), rcross(cl))), 12.0)));
+    double t[3];
+    tangent(load_q(d.q + 4 * (s0 + n - 1)), t);
+    const double et[3] = {d.efm * t[0], d.efm * t[1], d.efm * t[2]};
+    o = m3_add(o, m3_mul(rcross(et), base_cross(d, b, fil)));
+    for (int k = 0; k < 9; ++k) d.part[45 * fil + 36 + k] = o.a[k];
+  }
+}
+
+// Gauss-Jordan inversion in place of the n6 x n6 matrix in shared memory
+// (row-major), in float-float arithmetic on the same 8-byte slots: each
+// double is first turned into its (h, l) pair in place. The same steps as
+// the FP64 elimination below: partial pivoting on the largest |entry| of
+// the column at or below the diagonal (first index on ties, by the high
+// words), the pivot row scaled by 1/piv (its own entry becoming 1/piv), every
+// other row i minus col_i times the pivot row (column k becoming
+// -col_i / piv), and the columns unscrambled at the end.
+__device__ void gj_invert_ff(double *Jd, int n6, double *cold, int *perm) {
+  using namespace tfs::ff;
+  FF *J = reinterpret_cast<FF *>(Jd);
+  FF *col = reinterpret_cast<FF *>(cold);
+  const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
+  for (int q = tid; q < n6 * n6; q += nth) J[q] = ff_split(Jd[q]);
+  __shared__ FF rp_s;
+  __syncthreads();
+  const int ng = nth / n6 > 0 ? nth / n6 : 1;
+  const int g = tid / n6, jcol = g < ng ? tid - g * n6 : n6;
+  for (int k = 0; k < n6; ++k) {
+    if (warp == 0) {
+      float best = -1.0f;
+      int bi = k;
+      for (int i = k + lane; i < n6; i += 32) {
+        const float v = fabsf(J[(size_t)i * n6 + k].h);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const float ov = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (lane == 0) perm[k] = bi;
+    }
+    __syncthreads();
+    const int p = perm[k];
+    if (p != k)
+      for (int j = tid; j < n6; j += nth) {
+        const FF t = J[(size_t)k * n6 + j];
+        J[(size_t)k * n6 + j] = J[(size_t)p * n6 + j];
+        J[(size_t)p * n6 + j] = t;
+      }
+    __syncthreads();
+    for (int i = tid; i < n6; i += nth) col[i] = i == k ? FF{0.f, 0.f} : J[(size_t)i * n6 + k];
+    if (tid == 0) rp_s = ff_recip(J[(size_t)k * n6 + k]);
+    __syncthreads();
+    const FF rp = rp_s;
+    for (int j = tid; j < n6; j += nth)
+      J[(size_t)k * n6 + j] = j == k ? rp : ff_mul_norm(J[(size_t)k * n6 + j], rp);
+    __syncthreads();
+    if (jcol < n6) {
+      const FF rk = J[(size_t)k * n6 + jcol];
+      if (jcol == k) {
+        for (int i = g; i < n6; i += ng)
+          if (i != k) J[(size_t)i * n6 + jcol] = ff_neg(ff_mul_norm(col[i], rk));
+      } else {
+        for (int i = g; i < n6; i += ng)
+          if (i != k) J[(size_t)i * n6 + jcol] = ff_add(J[(size_t)i * n6 + jcol], ff_neg(ff_mul(col[i], rk)));
+      }
+    }
+    __syncthreads();
+  }
+  for (int k = n6 - 1; k >= 0; --k) {
+    const int p = perm[k];
+    if (p != k)
+      for (int i = tid; i < n6; i += nth) {
+        const FF t = J[(size_t)i * n6 + k];
+        J[(size_t)i * n6 + k] = J[(size_t)i * n6 + p];
+        J[(size_t)i * n6 + p] = t;
+      }
+    __syncthreads();
+  }
+}
+
 // One CTA per filament: assemble the approximate Jacobian in shared memory,
-// invert it in place (Gauss-Jordan, partial pivoting), store the inverse,
-// the product JB = B J^-1 and this filament's share of the Schur complement
-// (JB A) and of the body's Lie-algebra self-dependence.
+// invert it in place (Gauss-Jordan, partial pivoting; float-float arithmetic
+// with kFF, which FP32C solvers use: the inverse only preconditions Broyden's
+// method), store the inverse, the product JB = B J^-1 and this filament's
+// share of the Schur complement (JB A) and of the body's Lie-algebra
+// self-dependence.
+template <bool kFF>
 __global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt) {
   extern __shared__ double sm[];
   const int n = d.nseg, n6 = 6 * n, fil = blockIdx.x, tid = threadIdx.x, nth = blockDim.x;
@@ -637,6 +760,23 @@ __global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt)
     put_block(J, n6, 3 * n + 3, 3 * n, m3_zero());
   }
   __syncthreads();
+  if constexpr (kFF) {
+    gj_invert_ff(J, n6, col, perm);
+    using namespace tfs::ff;
+    const FF *Jf = reinterpret_cast<const FF *>(J);
+    double *jinv = d.jinv + (size_t)n6 * n6 * fil;
+    for (int i = tid; i < n6 * n6; i += nth) jinv[i] = ff_to_double(Jf[i]);
+    double *jb = d.jb + (size_t)6 * n6 * fil;
+    for (int idx = tid; idx < 6 * n6; idx += nth) {
+      const int r = idx / n6, c = idx - r * n6;
+      FF s{0.f, 0.f};
+      for (int k = 0; k < n6; ++k) ff_acc(s, ff_mul(ff_split(Bm[r * n6 + k]), Jf[(size_t)k * n6 + c]));
+      jb[idx] = ff_to_double(s);
+    }
+    __syncthreads();
+    jac_tail(d, b, fil, n6, n);
+    return;
+  }
   // Gauss-Jordan inversion in place
   const int warp = tid >> 5, lane = tid & 31;
   const int ng = nth / n6 > 0 ? nth / n6 : 1;  // row groups
@@ -711,38 +851,7 @@ __global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt)
     jb[idx] = s;
   }
   __syncthreads();
-  // JB A (6 x 6) with A = [I, D] per segment row block plus the elastic clamping blocks
-  if (tid < 36) {
-    const int r = tid / 6, c = tid % 6;
-    const M3 D = base_cross(d, b, fil);
-    const double *e1 = d.ecb + 18 * fil, *e2 = e1 + 9;
-    const double *row = jb + (size_t)r * n6;
-    double s = 0.0;
-    for (int k = 0; k < 3 * n; ++k) {
-      const int m = k % 3;
-      s += row[k] * (c < 3 ? (m == c ? 1.0 : 0.0) : D.a[3 * m + c - 3]);
-    }
-    if (c >= 3) {
-      for (int m = 0; m < 3; ++m) s += row[3 * n + m] * e1[3 * m + c - 3];
-      for (int m = 0; m < 3; ++m) s += row[3 * n + 3 + m] * e2[3 * m + c - 3];
-    }
-    d.part[45 * fil + tid] = s;
-  }
-  if (tid == 64) {  // this filament's share of the body's Lie-algebra self-dependence
-    double fbd[3];
-    m3_vec(m3_from(b.Q), d.fil_refs + 3 * fil, fbd);
-    const double *tl = d.teth + 3 * fil, *cl = d.clamp + 3 * fil;
-    const double ucl[3] = {b.u[1] * cl[2] - b.u[2] * cl[1], b.u[2] * cl[0] - b.u[0] * cl[2],
-                           b.u[0] * cl[1] - b.u[1] * cl[0]};
-    M3 o = m3_scale(-1.0, m3_mul(rcross(tl), rcross(fbd)));
-    o = m3_add(o, m3_sub(m3_scale(0.5, rcross(cl)),
-                         m3_div(m3_add(rcross(ucl), m3_mul(m3_from(b.blc), rcross(cl))), 12.0)));
-    double t[3];
-    tangent(load_q(d.q + 4 * (s0 + n - 1)), t);
-    const double et[3] = {d.efm * t[0], d.efm * t[1], d.efm * t[2]};
-    o = m3_add(o, m3_mul(rcross(et), base_cross(d, b, fil)));
-    for (int k = 0; k < 9; ++k) d.part[45 * fil + 36 + k] = o.a[k];
-  }
+  jac_tail(d, b, fil, n6, n);
 }
 
 // ---------------------------------------------------------------------------
@@ -1206,7 +1315,9 @@ int tfs_stepper_create(tfs_solver *s, const tfs_step_config *cfg, const double *
   if (smem > (size_t)optin)
     return fail(TFS_EINVAL, "nseg %d: the approximate Jacobian (%zu bytes) does not fit in shared memory",
                 cfg->nseg, smem);
-  ST_CUDA(cudaFuncSetAttribute(k_jacobian, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+  ST_CUDA(cudaFuncSetAttribute(k_jacobian<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+          "jacobian shared memory");
+  ST_CUDA(cudaFuncSetAttribute(k_jacobian<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
           "jacobian shared memory");
   tfs_stepper *st = new (std::nothrow) tfs_stepper();
   if (st == nullptr) return fail(TFS_ENOMEM, "host allocation");
@@ -1405,7 +1516,10 @@ int tfs_stepper_prepare_jacobian_inv(tfs_stepper *st, int nt, double *schur_inv)
   const StepDev &d = st->d;
   cudaStream_t str = st->s->stream;
   const BodyArgs b = body_args(st, nt);
-  k_jacobian<<<d.nfil, 256, st->jac_smem, str>>>(d, b, nt);
+  // FP32C: the inverse in float-float arithmetic (it only preconditions
+  // Broyden's method, and FP64 is this GPU's slowest pipe)
+  if (st->s->cfg.precision == TFS_FP32C) k_jacobian<true><<<d.nfil, 256, st->jac_smem, str>>>(d, b, nt);
+  else k_jacobian<false><<<d.nfil, 256, st->jac_smem, str>>>(d, b, nt);
   ST_LAUNCH("approximate Jacobian");
   ST_CUDA(cudaMemcpyAsync(st->hbuf, d.part, sizeof(double) * 45 * d.nfil, cudaMemcpyDeviceToHost, str),
           "Schur parts");
