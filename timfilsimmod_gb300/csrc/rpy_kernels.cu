@@ -146,10 +146,40 @@ __global__ void reduce_partials_kernel(double *__restrict__ out,
 // neighbours on the same filament; adds into f_segs) or blobs (kind 1: skip
 // self; assigns f_blobs_repulsion).
 // ---------------------------------------------------------------------------
+// Bounds of the FP32 origin-relative positions of each tile of BLOCK
+// consecutive sources (segments then blobs): boxes[6 t ..] = min xyz, max xyz.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) tile_box_kernel(const BarrierArgs a, int n_src) {
+  __shared__ float red[BLOCK / 32][6];
+  const int j = blockIdx.x * BLOCK + threadIdx.x;
+  float v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  if (j < n_src) {
+    const double *xs = j < a.num_segs ? a.x_segs + 3 * (size_t)j
+                                      : a.x_blobs + 3 * (size_t)(j - a.num_segs);
+    for (int k = 0; k < 3; ++k) v[k] = v[k + 3] = float(xs[k] - a.origin[k]);
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int k = 0; k < 6; ++k) {
+      const float w = __shfl_xor_sync(0xffffffffu, v[k], o);
+      v[k] = k < 3 ? fminf(v[k], w) : fmaxf(v[k], w);
+    }
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < 6; ++k) red[threadIdx.x >> 5][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int k = threadIdx.x;
+    float b = red[0][k];
+    for (int w = 1; w < BLOCK / 32; ++w) b = k < 3 ? fminf(b, red[w][k]) : fmaxf(b, red[w][k]);
+    a.boxes[6 * (size_t)blockIdx.x + k] = b;
+  }
+}
+
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
+  static_assert(BLOCK == 128, "source tiles are the 128-source tiles of tile_box_kernel");
   __shared__ double sxd[BLOCK][3];
   __shared__ float sxf[BLOCK][3];
+  __shared__ float cbox_w[BLOCK / 32][6], cbox[6];
   const int i = blockIdx.x * BLOCK + threadIdx.x;
   const int n_tgt = a.target_blobs ? a.num_blobs : a.num_segs;
   const bool active = i < n_tgt;
@@ -177,8 +207,43 @@ __global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
   // this CTA's share of the sources (grid.y splits them)
   const int s0 = blockIdx.y * a.chunk;
   const int s1 = min(s0 + a.chunk, n_src);
+  // bounds of this CTA's targets; a source tile whose bounds lie farther than
+  // the larger candidate threshold (with a 0.1% margin over the FP32
+  // rounding of both tests) has no pair the filter below would pass, and is
+  // skipped by the whole CTA
+  const float cull2 = 1.001f * fmaxf(thr2_seg, thr2_blob);
+  if (a.boxes != nullptr) {
+    float v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    if (active) {
+      v[0] = v[3] = xif;
+      v[1] = v[4] = yif;
+      v[2] = v[5] = zif;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+      for (int k = 0; k < 6; ++k) {
+        const float w = __shfl_xor_sync(0xffffffffu, v[k], o);
+        v[k] = k < 3 ? fminf(v[k], w) : fmaxf(v[k], w);
+      }
+    if ((threadIdx.x & 31) == 0)
+      for (int k = 0; k < 6; ++k) cbox_w[threadIdx.x >> 5][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+      const int k = threadIdx.x;
+      float b = cbox_w[0][k];
+      for (int w = 1; w < BLOCK / 32; ++w) b = k < 3 ? fminf(b, cbox_w[w][k]) : fmaxf(b, cbox_w[w][k]);
+      cbox[k] = b;
+    }
+    __syncthreads();
+  }
   double fx = 0.0, fy = 0.0, fz = 0.0;
   for (int base = s0; base < s1; base += BLOCK) {
+    if (a.boxes != nullptr) {  // CTA-uniform: the same values in every thread
+      const float *tb = a.boxes + 6 * (size_t)(base / BLOCK);
+      const float gx = fmaxf(0.f, fmaxf(tb[0] - cbox[3], cbox[0] - tb[3]));
+      const float gy = fmaxf(0.f, fmaxf(tb[1] - cbox[4], cbox[1] - tb[4]));
+      const float gz = fmaxf(0.f, fmaxf(tb[2] - cbox[5], cbox[2] - tb[5]));
+      if (gx * gx + gy * gy + gz * gz >= cull2) continue;
+    }
     const int j = base + threadIdx.x;
     __syncthreads();
     if (j < s1) {
@@ -461,6 +526,12 @@ static cudaError_t barrier_launch(BarrierArgs a, int target_blobs, cudaStream_t 
 
 cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
+  const int n_src = a.num_segs + a.num_blobs;
+  if (a.boxes != nullptr && n_src > 0) {
+    tile_box_kernel<128><<<(n_src + 127) / 128, 128, 0, st>>>(a, n_src);
+    count_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
   if (a.num_segs > 0 && (e = barrier_launch(a, 0, st)) != cudaSuccess) return e;
   if (a.free_body && a.num_blobs > 0) e = barrier_launch(a, 1, st);
   return e;

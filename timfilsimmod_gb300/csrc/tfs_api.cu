@@ -100,6 +100,7 @@ static void free_all(tfs_solver *s) {
   cudaFree(s->rec_segs_x2);
   cudaFree(s->rec_blobs_x2);
   cudaFree(s->rec_ff);
+  cudaFree(s->tile_boxes);
   cudaFree(s->scratch);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
@@ -266,6 +267,7 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
       (rc = alloc_dev(&s->rec_segs_x2, 80 * (size_t)ns)) ||
       (rc = alloc_dev(&s->rec_blobs_x2, 48 * (size_t)nb)) ||
       (rc = alloc_dev(&s->rec_ff, ff_record_bytes() * nb)) ||
+      (rc = alloc_dev((void **)&s->tile_boxes, sizeof(float) * 6 * ((ns + nb + 127) / 128 + 1))) ||
       (rc = alloc_dev((void **)&s->scratch, dsz * s->scratch_elems)) ||
       (rc = solve_alloc(s))) {
     free_all(s);
@@ -407,6 +409,7 @@ int tfs_apply_interparticle_forces(tfs_solver *s) {
   a.free_body = s->cfg.free_body;
   a.scratch = s->scratch;
   a.scratch_elems = s->scratch_elems;
+  a.boxes = s->tile_boxes;
   cudaError_t e = launch_barrier(a, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "barrier kernel");
   return TFS_OK;

@@ -46,6 +46,8 @@ struct BarrierArgs {
   double repulsive_force_factor;
   int free_body;
   double *scratch;            // split partial forces (kMaxSplits * 6 * max(Ns, Nb) doubles)
+  float *boxes;               // 6 per 128-source tile (segments then blobs): FP32 bounds of the
+                              // origin-relative positions, for culling whole tiles (null: none)
   size_t scratch_elems;
   int target_blobs;           // set by the launcher
   int chunk, splits;          // set by the launcher
