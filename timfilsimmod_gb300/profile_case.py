@@ -41,8 +41,8 @@ def run_flow(sw, args):
 
 def run_steps(sw, args):
     """Implicit time steps 0 .. reps-1 of the swimmer with straight elastic
-    filaments (DT 1e-3, Broyden TOL 1e-4, linear residual 1e-8); step 0
-    iterates Broyden's method from the straight start."""
+    filaments (DT --dt, default 1e-3; Broyden TOL 1e-4, linear residual
+    1e-8); step 0 iterates Broyden's method from the straight start."""
     from .geometry import fibonacci_sphere
     from .stepper import ImplicitStepper
 
@@ -53,7 +53,7 @@ def run_steps(sw, args):
                           end_force_magnitude=int(efm))
     s.set_blob_references(sw.blob_references)
     s.set_linear_solver(1e-8)
-    st = ImplicitStepper(s, sw.nfil, sw.nseg, fil_refs, normals, seg_sep=sw.seg_sep, dt=1e-3,
+    st = ImplicitStepper(s, sw.nfil, sw.nseg, fil_refs, normals, seg_sep=sw.seg_sep, dt=args.dt,
                          tol=1e-4, end_force_magnitude=efm, body_radius=sw.radius)
     t0 = time.perf_counter()
     from .mobility import kernel_launch_count
@@ -75,6 +75,7 @@ def main():
     p.add_argument("--config", default="medium")
     p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--dt", type=float, default=1e-3, help="time step (op step)")
     p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier", "solve", "flow", "step"])
     p.add_argument("--flow-grid", type=int, default=64, help="flow points per axis (op flow)")
     p.add_argument("--variant", type=int, default=None,
