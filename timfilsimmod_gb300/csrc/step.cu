@@ -30,7 +30,6 @@
 #include <new>
 #include <vector>
 
-#include "ff_arith.cuh"
 #include "step_math.cuh"
 #include "tfs_solver.h"
 
@@ -596,21 +595,32 @@ __device__ void jac_tail(const StepDev &d, const BodyArgs &b, int fil, int n6, i
   }
 }
 
+// Element arithmetic of the low-precision inversion (FP32).
+struct GjF32 {
+  using E = float;
+  static __device__ __forceinline__ E zero() { return 0.f; }
+  static __device__ __forceinline__ float mag(E a) { return fabsf(a); }
+  static __device__ __forceinline__ E recip(E a) { return 1.0f / a; }
+  static __device__ __forceinline__ E mul(E a, E b) { return a * b; }
+  static __device__ __forceinline__ E neg_mul(E c, E r) { return -(c * r); }
+  static __device__ __forceinline__ E sub_mul(E x, E c, E r) { return fmaf(-c, r, x); }
+  static __device__ __forceinline__ void acc(E &s, E a, E b) { s = fmaf(a, b, s); }
+  static __device__ __forceinline__ E from(double v) { return (float)v; }
+  static __device__ __forceinline__ double to(E a) { return (double)a; }
+};
+
 // Gauss-Jordan inversion in place of the n6 x n6 matrix in shared memory
-// (row-major), in float-float arithmetic on the same 8-byte slots: each
-// double is first turned into its (h, l) pair in place. The same steps as
-// the FP64 elimination below: partial pivoting on the largest |entry| of
-// the column at or below the diagonal (first index on ties, by the high
-// words), the pivot row scaled by 1/piv (its own entry becoming 1/piv), every
-// other row i minus col_i times the pivot row (column k becoming
-// -col_i / piv), and the columns unscrambled at the end.
-__device__ void gj_invert_ff(double *Jd, int n6, double *cold, int *perm) {
-  using namespace tfs::ff;
-  FF *J = reinterpret_cast<FF *>(Jd);
-  FF *col = reinterpret_cast<FF *>(cold);
+// (row-major, elements of Ops), by the whole CTA. The same steps as the FP64
+// elimination below: partial pivoting on the largest |entry| of the column
+// at or below the diagonal (first index on ties), the pivot row scaled by
+// 1/piv (its own entry becoming 1/piv), every other row i minus col_i times
+// the pivot row (column k becoming -col_i / piv), and the columns
+// unscrambled at the end.
+template <class Ops>
+__device__ void gj_invert_lo(typename Ops::E *J, int n6, typename Ops::E *col, int *perm) {
+  using E = typename Ops::E;
   const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31;
-  for (int q = tid; q < n6 * n6; q += nth) J[q] = ff_split(Jd[q]);
-  __shared__ FF rp_s;
+  __shared__ E rp_s;
   __syncthreads();
   const int ng = nth / n6 > 0 ? nth / n6 : 1;
   const int g = tid / n6, jcol = g < ng ? tid - g * n6 : n6;
@@ -619,7 +629,7 @@ __device__ void gj_invert_ff(double *Jd, int n6, double *cold, int *perm) {
       float best = -1.0f;
       int bi = k;
       for (int i = k + lane; i < n6; i += 32) {
-        const float v = fabsf(J[(size_t)i * n6 + k].h);
+        const float v = Ops::mag(J[(size_t)i * n6 + k]);
         if (v > best) {
           best = v;
           bi = i;
@@ -639,26 +649,36 @@ __device__ void gj_invert_ff(double *Jd, int n6, double *cold, int *perm) {
     const int p = perm[k];
     if (p != k)
       for (int j = tid; j < n6; j += nth) {
-        const FF t = J[(size_t)k * n6 + j];
+        const E t = J[(size_t)k * n6 + j];
         J[(size_t)k * n6 + j] = J[(size_t)p * n6 + j];
         J[(size_t)p * n6 + j] = t;
       }
     __syncthreads();
-    for (int i = tid; i < n6; i += nth) col[i] = i == k ? FF{0.f, 0.f} : J[(size_t)i * n6 + k];
-    if (tid == 0) rp_s = ff_recip(J[(size_t)k * n6 + k]);
+    for (int i = tid; i < n6; i += nth) col[i] = i == k ? Ops::zero() : J[(size_t)i * n6 + k];
+    if (tid == 0) rp_s = Ops::recip(J[(size_t)k * n6 + k]);
     __syncthreads();
-    const FF rp = rp_s;
+    const E rp = rp_s;
     for (int j = tid; j < n6; j += nth)
-      J[(size_t)k * n6 + j] = j == k ? rp : ff_mul_norm(J[(size_t)k * n6 + j], rp);
+      J[(size_t)k * n6 + j] = j == k ? rp : Ops::mul(J[(size_t)k * n6 + j], rp);
     __syncthreads();
     if (jcol < n6) {
-      const FF rk = J[(size_t)k * n6 + jcol];
-      if (jcol == k) {
-        for (int i = g; i < n6; i += ng)
-          if (i != k) J[(size_t)i * n6 + jcol] = ff_neg(ff_mul_norm(col[i], rk));
-      } else {
-        for (int i = g; i < n6; i += ng)
-          if (i != k) J[(size_t)i * n6 + jcol] = ff_add(J[(size_t)i * n6 + jcol], ff_neg(ff_mul(col[i], rk)));
+      // four rows at a time, their loads issued together (the shared-memory
+      // latency would otherwise be paid row by row)
+      const E rk = J[(size_t)k * n6 + jcol];
+      for (int i0 = g; i0 < n6; i0 += 4 * ng) {
+        E c[4], x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = i0 + u * ng;
+          c[u] = i < n6 ? col[i] : Ops::zero();
+          x[u] = i < n6 ? J[(size_t)i * n6 + jcol] : Ops::zero();
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int i = i0 + u * ng;
+          if (i < n6 && i != k)
+            J[(size_t)i * n6 + jcol] = jcol == k ? Ops::neg_mul(c[u], rk) : Ops::sub_mul(x[u], c[u], rk);
+        }
       }
     }
     __syncthreads();
@@ -667,7 +687,7 @@ __device__ void gj_invert_ff(double *Jd, int n6, double *cold, int *perm) {
     const int p = perm[k];
     if (p != k)
       for (int i = tid; i < n6; i += nth) {
-        const FF t = J[(size_t)i * n6 + k];
+        const E t = J[(size_t)i * n6 + k];
         J[(size_t)i * n6 + k] = J[(size_t)i * n6 + p];
         J[(size_t)i * n6 + p] = t;
       }
@@ -676,11 +696,11 @@ __device__ void gj_invert_ff(double *Jd, int n6, double *cold, int *perm) {
 }
 
 // One CTA per filament: assemble the approximate Jacobian in shared memory,
-// invert it in place (Gauss-Jordan, partial pivoting; float-float arithmetic
-// with kFF, which FP32C solvers use: the inverse only preconditions Broyden's
-// method), store the inverse, the product JB = B J^-1 and this filament's
-// share of the Schur complement (JB A) and of the body's Lie-algebra
-// self-dependence.
+// invert it in place (Gauss-Jordan, partial pivoting), store the inverse,
+// the product JB = B J^-1 and this filament's share of the Schur complement
+// (JB A) and of the body's Lie-algebra self-dependence. With kFF (FP32C
+// solvers) the assembled J and B go to global memory instead and
+// k_jacobian_lo inverts.
 template <bool kFF>
 __global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt) {
   extern __shared__ double sm[];
@@ -760,21 +780,10 @@ __global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt)
     put_block(J, n6, 3 * n + 3, 3 * n, m3_zero());
   }
   __syncthreads();
-  if constexpr (kFF) {
-    gj_invert_ff(J, n6, col, perm);
-    using namespace tfs::ff;
-    const FF *Jf = reinterpret_cast<const FF *>(J);
-    double *jinv = d.jinv + (size_t)n6 * n6 * fil;
-    for (int i = tid; i < n6 * n6; i += nth) jinv[i] = ff_to_double(Jf[i]);
-    double *jb = d.jb + (size_t)6 * n6 * fil;
-    for (int idx = tid; idx < 6 * n6; idx += nth) {
-      const int r = idx / n6, c = idx - r * n6;
-      FF s{0.f, 0.f};
-      for (int k = 0; k < n6; ++k) ff_acc(s, ff_mul(ff_split(Bm[r * n6 + k]), Jf[(size_t)k * n6 + c]));
-      jb[idx] = ff_to_double(s);
-    }
-    __syncthreads();
-    jac_tail(d, b, fil, n6, n);
+  if constexpr (kFF) {  // J and B to global memory; k_jacobian_lo inverts
+    double *jg = d.jinv + (size_t)n6 * n6 * fil, *bg = d.jb + (size_t)6 * n6 * fil;
+    for (int i = tid; i < n6 * n6; i += nth) jg[i] = J[i];
+    for (int i = tid; i < 6 * n6; i += nth) bg[i] = Bm[i];
     return;
   }
   // Gauss-Jordan inversion in place
@@ -854,6 +863,46 @@ __global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt)
   jac_tail(d, b, fil, n6, n);
 }
 
+// The low-precision half of the FP32C approximate Jacobian: one CTA per
+// filament of kJacLoThreads threads (a separate kernel, so that the
+// elimination runs with many warps and few registers): J and B as k_jacobian
+// left them in jinv and jb (FP64), J^-1 in place in Ops arithmetic,
+// JB = B J^-1, then this filament's Schur and body partials. The inverse
+// only seeds Broyden's method (its initial inverse Jacobian): FP32 elements
+// keep the reference's Broyden iteration counts (tested at DT 1e-3 and at
+// the reference's default DT) at a third of the float-float form's time.
+constexpr int kJacLoThreads = 512;
+template <class Ops>
+__global__ void __launch_bounds__(kJacLoThreads) k_jacobian_lo(StepDev d, BodyArgs b) {
+  using E = typename Ops::E;
+  extern __shared__ double sm[];
+  const int n = d.nseg, n6 = 6 * n, fil = blockIdx.x, tid = threadIdx.x, nth = blockDim.x;
+  E *J = reinterpret_cast<E *>(sm);   // n6 * n6
+  E *Bf = J + (size_t)n6 * n6;        // 6 * n6
+  E *col = Bf + 6 * n6;               // n6
+  int *perm = reinterpret_cast<int *>(col + n6);
+  double *jg = d.jinv + (size_t)n6 * n6 * fil, *bg = d.jb + (size_t)6 * n6 * fil;
+  for (int i = tid; i < n6 * n6; i += nth) J[i] = Ops::from(jg[i]);
+  for (int i = tid; i < 6 * n6; i += nth) Bf[i] = Ops::from(bg[i]);
+  gj_invert_lo<Ops>(J, n6, col, perm);
+  E *jo = reinterpret_cast<E *>(jg);  // J^-1 as E at the start of the filament's slot
+  for (int i = tid; i < n6 * n6; i += nth) jo[i] = J[i];
+  for (int idx = tid; idx < 6 * n6; idx += nth) {
+    const int r = idx / n6, c = idx - r * n6;
+    E s0 = Ops::zero(), s1 = Ops::zero();
+    int k = 0;
+    for (; k + 1 < n6; k += 2) {
+      Ops::acc(s0, Bf[r * n6 + k], J[(size_t)k * n6 + c]);
+      Ops::acc(s1, Bf[r * n6 + k + 1], J[(size_t)(k + 1) * n6 + c]);
+    }
+    if (k < n6) Ops::acc(s0, Bf[r * n6 + k], J[(size_t)k * n6 + c]);
+    bg[idx] = Ops::to(s0) + Ops::to(s1);
+  }
+  __syncthreads();
+  jac_tail(d, b, fil, n6, n);
+}
+using JacLoOps = GjF32;  // the arithmetic FP32C solvers invert in
+
 // ---------------------------------------------------------------------------
 // swimmer::jacobian_inv_mult (swimmer.cpp:915-1070), free-body branch:
 //   b2 = in_body - sum_i JB_i in_i,  out_body = S^-1 b2,
@@ -906,9 +955,13 @@ __global__ void __launch_bounds__(256) k_body_solve(StepDev d, const double *__r
 }
 
 // out_i = J_i^-1 (in_i - A_i ob), one CTA per filament, one warp per row
+// J^-1 is stored as T per filament at the start of its (6N)^2-double slot
+// (FP32 for FP32C solvers, whose inverse is computed in FP32).
+template <typename T>
 __global__ void k_jinv_apply(StepDev d, BodyArgs b, const double *__restrict__ in,
                              const double *__restrict__ ob_dev, double *__restrict__ out) {
-  extern __shared__ double rhs[];
+  extern __shared__ double rhs_sm[];
+  T *rhs = reinterpret_cast<T *>(rhs_sm);
   const int fil = blockIdx.x, n = d.nseg, n6 = 6 * n;
   const double *v = in + (size_t)n6 * fil;
   double ob[6];
@@ -924,17 +977,17 @@ __global__ void k_jinv_apply(StepDev d, BodyArgs b, const double *__restrict__ i
       const double *e = k < 3 * n + 3 ? e1 + 3 * (k - 3 * n) : e2 + 3 * (k - 3 * n - 3);
       a = e[0] * ob[3] + e[1] * ob[4] + e[2] * ob[5];
     }
-    rhs[k] = v[k] - a;
+    rhs[k] = (T)(v[k] - a);
   }
   __syncthreads();
-  const double *jinv = d.jinv + (size_t)n6 * n6 * fil;
+  const T *jinv = reinterpret_cast<const T *>(d.jinv + (size_t)n6 * n6 * fil);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int row = warp; row < n6; row += nw) {
-    const double *jr = jinv + (size_t)row * n6;
-    double s = 0.0;
+    const T *jr = jinv + (size_t)row * n6;
+    T s = 0;
     for (int k = lane; k < n6; k += 32) s += jr[k] * rhs[k];
     for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-    if (lane == 0) out[(size_t)n6 * fil + row] = s;
+    if (lane == 0) out[(size_t)n6 * fil + row] = (double)s;
   }
 }
 
@@ -1050,7 +1103,8 @@ struct tfs_stepper {
   int *hflag = nullptr;    // pinned
   int iter = 0;
   int jac_ready = 0;
-  size_t jac_smem = 0;
+  size_t jac_smem = 0, jac_ff_smem = 0;
+  bool jinv_f32 = false;  // the stored J^-1 is FP32 (FP32C solvers)
   long nbroy = 0;
   // the straight start (for tfs_stepper_reset): unit directions, base
   // quaternions, body frame references; the solver's warm start as it was
@@ -1161,7 +1215,8 @@ int jinv_mult_dev(tfs_stepper *st, int nt, const double *in, double *out) {
   ST_LAUNCH("jacobian_inv_mult (JB in)");
   k_body_solve<<<1, 256, 0, str>>>(d, in, st->p6, st->schur_dev, out, st->ob);
   ST_LAUNCH("jacobian_inv_mult (body)");
-  k_jinv_apply<<<d.nfil, 256, sizeof(double) * 6 * d.nseg, str>>>(d, b, in, st->ob, out);
+  if (st->jinv_f32) k_jinv_apply<float><<<d.nfil, 256, sizeof(double) * 6 * d.nseg, str>>>(d, b, in, st->ob, out);
+  else k_jinv_apply<double><<<d.nfil, 256, sizeof(double) * 6 * d.nseg, str>>>(d, b, in, st->ob, out);
   ST_LAUNCH("jacobian_inv_mult (filaments)");
   return TFS_OK;
 }
@@ -1317,6 +1372,9 @@ int tfs_stepper_create(tfs_solver *s, const tfs_step_config *cfg, const double *
                 cfg->nseg, smem);
   ST_CUDA(cudaFuncSetAttribute(k_jacobian<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
           "jacobian shared memory");
+  const size_t ff_smem = sizeof(typename JacLoOps::E) * ((size_t)n6 * n6 + 7 * (size_t)n6) + sizeof(int) * n6;
+  ST_CUDA(cudaFuncSetAttribute(k_jacobian_lo<JacLoOps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff_smem),
+          "jacobian shared memory");
   ST_CUDA(cudaFuncSetAttribute(k_jacobian<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
           "jacobian shared memory");
   tfs_stepper *st = new (std::nothrow) tfs_stepper();
@@ -1324,6 +1382,7 @@ int tfs_stepper_create(tfs_solver *s, const tfs_step_config *cfg, const double *
   st->s = s;
   st->cfg = *cfg;
   st->jac_smem = smem;
+  st->jac_ff_smem = ff_smem;
   StepDev &d = st->d;
   d.nfil = cfg->nfil;
   d.nseg = cfg->nseg;
@@ -1516,10 +1575,16 @@ int tfs_stepper_prepare_jacobian_inv(tfs_stepper *st, int nt, double *schur_inv)
   const StepDev &d = st->d;
   cudaStream_t str = st->s->stream;
   const BodyArgs b = body_args(st, nt);
-  // FP32C: the inverse in float-float arithmetic (it only preconditions
-  // Broyden's method, and FP64 is this GPU's slowest pipe)
-  if (st->s->cfg.precision == TFS_FP32C) k_jacobian<true><<<d.nfil, 256, st->jac_smem, str>>>(d, b, nt);
-  else k_jacobian<false><<<d.nfil, 256, st->jac_smem, str>>>(d, b, nt);
+  // FP32C: the inverse in FP32 (it only seeds Broyden's method, and FP64 is
+  // this GPU's slowest pipe)
+  st->jinv_f32 = st->s->cfg.precision == TFS_FP32C;
+  if (st->jinv_f32) {
+    k_jacobian<true><<<d.nfil, 256, st->jac_smem, str>>>(d, b, nt);
+    ST_LAUNCH("approximate Jacobian");
+    k_jacobian_lo<JacLoOps><<<d.nfil, kJacLoThreads, st->jac_ff_smem, str>>>(d, b);
+  } else {
+    k_jacobian<false><<<d.nfil, 256, st->jac_smem, str>>>(d, b, nt);
+  }
   ST_LAUNCH("approximate Jacobian");
   ST_CUDA(cudaMemcpyAsync(st->hbuf, d.part, sizeof(double) * 45 * d.nfil, cudaMemcpyDeviceToHost, str),
           "Schur parts");
@@ -1562,10 +1627,19 @@ int tfs_stepper_inverse_jacobian(tfs_stepper *st, int fil, double *out) {
   if (!st->jac_ready) return fail(TFS_ESTATE, "prepare_jacobian_inv has not run this step");
   const int n6 = 6 * st->d.nseg;
   std::vector<double> h((size_t)n6 * n6);
-  ST_CUDA(cudaMemcpyAsync(h.data(), st->d.jinv + (size_t)n6 * n6 * fil, sizeof(double) * h.size(),
-                          cudaMemcpyDeviceToHost, st->s->stream),
-          "inverse Jacobian");
-  ST_CUDA(cudaStreamSynchronize(st->s->stream), "inverse Jacobian");
+  if (st->jinv_f32) {
+    std::vector<float> hf(h.size());
+    ST_CUDA(cudaMemcpyAsync(hf.data(), st->d.jinv + (size_t)n6 * n6 * fil, sizeof(float) * hf.size(),
+                            cudaMemcpyDeviceToHost, st->s->stream),
+            "inverse Jacobian");
+    ST_CUDA(cudaStreamSynchronize(st->s->stream), "inverse Jacobian");
+    for (size_t i = 0; i < h.size(); ++i) h[i] = hf[i];
+  } else {
+    ST_CUDA(cudaMemcpyAsync(h.data(), st->d.jinv + (size_t)n6 * n6 * fil, sizeof(double) * h.size(),
+                            cudaMemcpyDeviceToHost, st->s->stream),
+            "inverse Jacobian");
+    ST_CUDA(cudaStreamSynchronize(st->s->stream), "inverse Jacobian");
+  }
   for (int i = 0; i < n6; ++i)
     for (int j = 0; j < n6; ++j) out[i + (size_t)n6 * j] = h[(size_t)n6 * i + j];
   return TFS_OK;
