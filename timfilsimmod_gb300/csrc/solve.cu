@@ -543,9 +543,9 @@ int linear_solve(tfs_solver *s, int *iters) {
     }
     prev_rel = h.rel;
     // the inner solve asks only for the reduction the outer target still
-    // needs (with a factor 4 to spare), at most inner_tol's: a good warm
+    // needs (with a factor 2 to spare), at most inner_tol's: a good warm
     // start then costs a few Arnoldi steps instead of a full 1e-4 reduction
-    const double itol = std::max(s->inner_tol, std::min(0.5, 0.25 * s->tol / h.rel));
+    const double itol = std::max(s->inner_tol, std::min(0.5, 0.5 * s->tol / h.rel));
     int inner = 0;
     rc = s->service ? s->service->solve(s, s->r, s->dx, s->dx + vel, itol, &inner)
          : (s->pg_ok && s->pg_enabled)
