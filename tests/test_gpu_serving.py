@@ -77,7 +77,7 @@ def test_batch_same_as_alone(precision, share):
         out = batch.step(nt, allow_unconverged=True)
         assert np.all(out["gmres_iters"] > 0)
     sh = batch.shared_solves()
-    if share is not False:  # these swimmers (<= 642 blobs, 11 CTAs) share by default too
+    if share is not False:  # -1 (the default) shares every FP32C solve
         assert sh["solves"] > 0 and 0 < sh["launches"] <= sh["solves"], sh
     else:
         assert sh == {"launches": 0, "solves": 0}

@@ -115,7 +115,7 @@ struct tfs_batch {
   std::vector<char> shared;  // the instance's inner solves can go through the service
   std::vector<int> shared_ctas;  // CTAs of its solve in a shared launch
   tfs::GmresService *service = nullptr;
-  int share_max_ctas = -1;  // -1: one eighth of the SMs
+  int share_max_ctas = -1;  // -1: every solve the persistent kernel can take
   ~tfs_batch() { tfs::service_destroy(service); }
 };
 
@@ -191,7 +191,7 @@ int tfs_batch_step(tfs_batch *b, int nt, int *broyden_iters, int *gmres_iters, i
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
     return tfs::stepper_segments(b->inst[x]) > tfs::stepper_segments(b->inst[y]);
   });
-  const int cap = b->share_max_ctas >= 0 ? b->share_max_ctas : std::max(1, tfs::num_sms() / 8);
+  const int cap = b->share_max_ctas >= 0 ? b->share_max_ctas : tfs::num_sms();
   for (int i = 0; i < n; ++i)
     if (b->shared[i] && b->shared_ctas[i] <= cap)
       tfs::stepper_solver(b->inst[i])->service = b->service;

@@ -50,8 +50,8 @@ class SwimmerBatch:
 
     def share_inner_solves(self, max_ctas: int | bool = -1) -> None:
         """FP32C swimmers whose inner solve takes at most max_ctas CTAs (one
-        per 64 blobs) share cooperative launches; True: all, False / 0: none,
-        -1 (the default): one eighth of the SMs."""
+        per 64 blobs) share cooperative launches; True or -1 (the default):
+        all, False / 0: none."""
         if max_ctas is True:
             max_ctas = 1 << 30
         N.check(self.lib.tfs_batch_share_inner_solves(self._h, int(max_ctas)))
