@@ -127,6 +127,24 @@ class ClockSampler:
                 "power_w_max": float(max(power)) if power else None}
 
 
+def max_over_ranks(values, world: int, device: str):
+    """Each value's maximum over the ranks (the slowest replica's time); with
+    one rank, the values themselves."""
+    import torch
+
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units processed by all replicas per second of the slowest one."""
+    return world * units_per_rank / seconds
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -267,15 +285,12 @@ def bench_ours(args):
     clocks = sampler.stop()
 
     # max over ranks
-    t = torch.tensor([ms32, t_e2e, ms64], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms32, t_e2e, ms64 = t.tolist()
+    ms32, t_e2e, ms64 = max_over_ranks([ms32, t_e2e, ms64], world, "cuda")
 
     per_step_ms = ms32 / args.steps
-    value = world * args.steps / (ms32 * 1e-3)
-    e2e_value = world * e2e_steps / (t_e2e * 1e-3)
-    value64 = world * steps64 / (ms64 * 1e-3)
+    value = whole_job_rate(args.steps, world, ms32 * 1e-3)
+    e2e_value = whole_job_rate(e2e_steps, world, t_e2e * 1e-3)
+    value64 = whole_job_rate(steps64, world, ms64 * 1e-3)
     seg_flops = ns * ns * FLOPS_66 + ns * nb * FLOPS_63
     seg_ms = float(np.mean(seg_launches)) if seg_launches else float("nan")
     achieved = seg_flops / (seg_ms * 1e-3) / 1e12
