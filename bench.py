@@ -127,6 +127,12 @@ class ClockSampler:
                 "power_w_max": float(max(power)) if power else None}
 
 
+# DRAM bytes per launch of the segment-target tile kernel (FP32C grand
+# mobility), from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum,
+# rpy_tile_kernel<float,6,6,3,128,1,256,8>, medium swimmer): 1 043 200 + 0.
+TILE_TRAFFIC = {"medium": 1043200}
+
+
 def max_over_ranks(values, world: int, device: str):
     """Each value's maximum over the ranks (the slowest replica's time); with
     one rank, the values themselves."""
@@ -329,7 +335,12 @@ def bench_ours(args):
                          "frac": achieved / (peak32 / 1e12),
                          "peak_source": "measured live (FMA-chain microbenchmark, this run)",
                          "flops_per_launch": seg_flops, "avg_launch_ms": seg_ms,
-                         "traffic": None},
+                         "traffic": TILE_TRAFFIC.get(args.config),
+                         "traffic_note": "bytes per launch, dram__bytes_read.sum + "
+                                         "dram__bytes_write.sum of one ncu capture of the "
+                                         "tuned segment-target launch on this workload; "
+                                         "algorithmic bytes ~1.0 MB (source records + "
+                                         "targets; split partials stay in L2)"},
             "fp64": {"value": value64, "unit": "matvecs/s", "steps": steps64,
                      "roofline": {"bound": "fp64-fma", "achieved": achieved64,
                                   "peak": peak64 / 1e12, "unit": "TFLOP/s",

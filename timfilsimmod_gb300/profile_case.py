@@ -104,6 +104,11 @@ def main():
         s.set_linear_solver(1e-8)
         s.make_body_reference_matrices()
         rng = np.random.default_rng(5)
+    from .mobility import kernel_launch_count
+
+    s.wait_for_device()
+    # the launch index where the timed repetitions begin (ncu -s skips the ones before)
+    print(f"kernel launches before timed reps: {kernel_launch_count()}")
     t0 = time.perf_counter()
     for _ in range(args.reps):
         if args.op == "grand":
