@@ -110,6 +110,17 @@ int tfs_evaluate_segment_segment_mobility(tfs_solver *s); /* v_segs  = Mss f_seg
 int tfs_evaluate_segment_blob_mobility(tfs_solver *s);    /* v_segs += Msb f_blobs (:276-292, :551-636) */
 int tfs_evaluate_blob_blob_mobility(tfs_solver *s);       /* v_blobs = Mbb f_blobs (:294-310, :476-549) */
 int tfs_evaluate_blob_segment_mobility(tfs_solver *s);    /* v_blobs = Mbs f_segs  (:312-328, :638-757) */
+/* The weakly coupled filaments' segment-segment product of the reference's
+ * weakly_coupled_filaments_rpy_mobility_solver (its position and force
+ * uploads compute each filament's mean position and total force,
+ * weakly_coupled_filaments_rpy_mobility_solver.cu:50-89; its
+ * evaluate_segment_segment_mobility runs Msf_mult, cuda_functions.cu:
+ * 1129-1229, free space): v_segs from x_segs and f_segs -- full RPY
+ * (translation only) within a filament, the Stokeslet of every other
+ * filament's total force at its mean position; rotational velocities zero.
+ * FP64 whatever the solver's precision. The segments must form whole
+ * filaments of nseg. */
+int tfs_evaluate_weakly_coupled_segment_mobility(tfs_solver *s);
 /* v_blobs = Mbb f_blobs in float-float arithmetic (each pair quantity an
  * unevaluated sum of two FP32 numbers, about 1e-13 relative), whatever the
  * solver's precision: the product FP32C refinement computes its residuals

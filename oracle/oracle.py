@@ -62,6 +62,13 @@ class Oracle:
         self.lib.orc_mss(ctypes.byref(self.p), _ptr(v), _ptr(f), _ptr(x), ns)
         return v
 
+    def msf(self, x_segs, f_segs, nfil, nseg):
+        """Weakly coupled filaments' segment product (orc_msf)."""
+        x, f = _c(x_segs), _c(f_segs)
+        v = np.zeros(f.size)
+        self.lib.orc_msf(ctypes.byref(self.p), _ptr(v), _ptr(f), _ptr(x), int(nfil), int(nseg))
+        return v
+
     def msb(self, x_segs, x_blobs, f_blobs, v_segs=None):
         xs, xb, fb = _c(x_segs), _c(x_blobs), _c(f_blobs)
         ns, nb = xs.size // 3, xb.size // 3
@@ -178,6 +185,14 @@ class ReferenceKernels:
         xb, xs, fs = _c(x_blobs), _c(x_segs), _c(f_segs)
         v = np.zeros(xb.size)
         self.lib.ref_mbs(_ptr(v), _ptr(fs), _ptr(xb), _ptr(xs), xb.size // 3)
+        return v
+
+    def msf(self, x_segs, f_segs, nfil, nseg):
+        """The reference's weakly coupled filaments' product (filament means,
+        total forces, Msf_mult); sync() first with these nfil and nseg."""
+        x, f = _c(x_segs), _c(f_segs)
+        v = np.zeros(f.size)
+        self.lib.ref_msf(_ptr(v), _ptr(f), _ptr(x), x.size // 3, int(nfil))
         return v
 
     def barrier_forces(self, x_segs, x_blobs, f_segs):

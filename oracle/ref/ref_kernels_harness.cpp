@@ -9,6 +9,7 @@
 // Launch shapes follow rpy_mobility_solver.cu:258-328 (single device:
 // start = 0, count = all) and :207-245 for barrier_forces.
 #include <algorithm>
+#include <vector>
 
 #include "cuda_emu.hpp"
 #include "cuda_functions.hpp"
@@ -49,6 +50,28 @@ void ref_mbs(double *v_blobs, const double *f_segs, const double *x_blobs, const
              int num_blobs) {
   emu_launch(blocks_for(num_blobs), THREADS_PER_BLOCK,
              [&] { Mbs_mult(v_blobs, f_segs, x_blobs, x_segs, 0, num_blobs); });
+}
+
+// The weakly coupled filaments' segment product, as
+// weakly_coupled_filaments_rpy_mobility_solver.cu:50-107 runs it: filament
+// means (reset_mean_fil_posns, write_mean_fil_posns), total forces
+// (reset_mean_fil_force_and_moment, find_total_fil_force_and_first_moment),
+// then Msf_mult over every segment. The first-moment array is the
+// reference's one-element placeholder (its moment code is commented out).
+void ref_msf(double *v_segs, const double *f_segs, const double *x_segs, int num_segs,
+             int num_fils) {
+  std::vector<double> Z(3 * (size_t)num_fils), F(3 * (size_t)num_fils), S(1);
+  emu_launch(blocks_for(3 * num_segs), THREADS_PER_BLOCK, [&] { reset_mean_fil_posns(Z.data()); });
+  emu_launch(blocks_for(num_segs), THREADS_PER_BLOCK,
+             [&] { write_mean_fil_posns(Z.data(), x_segs); });
+  emu_launch(blocks_for(3 * num_segs), THREADS_PER_BLOCK,
+             [&] { reset_mean_fil_force_and_moment(F.data(), S.data()); });
+  emu_launch(blocks_for(num_segs), THREADS_PER_BLOCK, [&] {
+    find_total_fil_force_and_first_moment(F.data(), S.data(), f_segs, x_segs, Z.data());
+  });
+  emu_launch(blocks_for(num_segs), THREADS_PER_BLOCK, [&] {
+    Msf_mult(v_segs, f_segs, F.data(), S.data(), x_segs, Z.data(), 0, num_segs);
+  });
 }
 
 void ref_barrier_forces(double *f_segs, double *f_blobs_repulsion, const double *x_segs,

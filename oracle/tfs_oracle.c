@@ -3,6 +3,7 @@
 #include "tfs_oracle.h"
 
 #include <math.h>
+#include <stdlib.h>
 #include <stddef.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -126,6 +127,64 @@ void orc_rpy_pair(int vd, int fd, double *V, const double *F, double xi, double 
       V[5] += A * F[5] + B * ez;
     }
   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Weakly coupled filaments (the reference's                                 */
+/* weakly_coupled_filaments_rpy_mobility_solver.cu:50-107: filament means    */
+/* and total forces on upload, then Msf_mult, cuda_functions.cu:991-1080 and */
+/* :1129-1229, free space). Z_f = sum_k x_{f,k} / NSEG and Ftot_f = sum_k    */
+/* F_{f,k}; segment i of filament f sums, over filaments j in order, the     */
+/* translation-only RPY pairs of its own filament's segments (j = f) or the  */
+/* Stokeslet (1/8 pi mu)(Ftot_j / r + (r.Ftot_j) r / r^3), r = x_i - Z_j     */
+/* (j != f). The rotational velocities are zero (:1220-1225).                */
+/* ------------------------------------------------------------------------ */
+void orc_msf(const orc_params *p, double *v_segs, const double *f_segs, const double *x_segs,
+             int nfil, int nseg) {
+  double *Z = (double *)calloc(3 * (size_t)nfil, sizeof(double));
+  double *Ft = (double *)calloc(3 * (size_t)nfil, sizeof(double));
+  for (int fi = 0; fi < nfil; ++fi)
+    for (int k = 0; k < nseg; ++k) {
+      const size_t sg = (size_t)fi * nseg + k;
+      for (int d = 0; d < 3; ++d) {
+        Z[3 * fi + d] += x_segs[3 * sg + d] / (double)nseg;
+        Ft[3 * fi + d] += f_segs[6 * sg + d];
+      }
+    }
+  const double ff = 1.0 / (8.0 * ORC_PI * p->mu);
+  const int ns = nfil * nseg;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(g_threads)
+  for (int i = 0; i < ns; ++i) {
+    const int fil = i / nseg;
+    const double *xi = x_segs + 3 * (size_t)i;
+    double v[3] = {0, 0, 0};
+    for (int j = 0; j < nfil; ++j) {
+      if (j == fil) {
+        for (int k = 0; k < nseg; ++k) {
+          const size_t jj = (size_t)j * nseg + k;
+          const double *xj = x_segs + 3 * jj;
+          orc_rpy_pair(3, 3, v, f_segs + 6 * jj, xi[0], xi[1], xi[2], p->a_seg, xj[0], xj[1],
+                       xj[2], p->a_seg, p->mu);
+        }
+      } else {
+        const double rx = xi[0] - Z[3 * j], ry = xi[1] - Z[3 * j + 1], rz = xi[2] - Z[3 * j + 2];
+        const double rm1 = 1.0 / sqrt(rx * rx + ry * ry + rz * rz);
+        const double rm3 = rm1 * rm1 * rm1;
+        const double *F = Ft + 3 * j;
+        const double rF = rx * F[0] + ry * F[1] + rz * F[2];
+        v[0] += ff * (rm1 * F[0] + rm3 * rx * rF);
+        v[1] += ff * (rm1 * F[1] + rm3 * ry * rF);
+        v[2] += ff * (rm1 * F[2] + rm3 * rz * rF);
+      }
+    }
+    double *o = v_segs + 6 * (size_t)i;
+    o[0] = v[0];
+    o[1] = v[1];
+    o[2] = v[2];
+    o[3] = o[4] = o[5] = 0.0;
+  }
+  free(Z);
+  free(Ft);
 }
 
 /* ------------------------------------------------------------------------ */

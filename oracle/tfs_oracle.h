@@ -40,6 +40,11 @@ void orc_rpy_pair(int vd, int fd, double *V, const double *F, double xi, double 
                   double ai, double xj, double yj, double zj, double aj, double mu);
 
 /* Mss_mult, cuda_functions.cu:362-474: v_segs = M_ss f_segs (assigns). */
+/* Weakly coupled filaments' segment product (Msf_mult with its filament
+ * means and total forces): v_segs[6 Ns] from x_segs[3 Ns], f_segs[6 Ns],
+ * Ns = nfil * nseg. */
+void orc_msf(const orc_params *p, double *v_segs, const double *f_segs, const double *x_segs,
+             int nfil, int nseg);
 void orc_mss(const orc_params *p, double *v_segs, const double *f_segs, const double *x_segs,
              int num_segs);
 /* Msb_mult, cuda_functions.cu:551-636: v_segs += M_sb f_blobs (accumulates). */

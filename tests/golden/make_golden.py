@@ -95,6 +95,30 @@ def case_tiny():
     return res
 
 
+def case_weak():
+    """Weakly coupled filaments' product (the reference's filament means,
+    total forces and Msf_mult, a1 config): 6 filaments x 20 segments leaving
+    a sphere of radius 10 along random directions, two of them crossing
+    close by; and a ragged 5 x 7 case."""
+    rng = np.random.default_rng(21)
+    ref = ReferenceKernels("a1")
+    res = {}
+    for tag, nfil, nseg in (("six", 6, 20), ("ragged", 5, 7)):
+        d = rng.normal(size=(nfil, 3))
+        d /= np.linalg.norm(d, axis=1)[:, None]
+        xs = np.concatenate([10.0 * u + 2.2 * np.arange(nseg)[:, None] * u for u in d])
+        xs += rng.normal(scale=0.05, size=xs.shape)
+        if tag == "six":
+            xs[25] = xs[3] + np.array([0.4, 0.3, -0.2])  # overlapping segments of two filaments
+        fs = rng.normal(size=(nfil * nseg, 6))
+        ref.sync(1, nseg, nfil, 0)
+        v = ref.msf(xs, fs, nfil, nseg)
+        res.update({f"{tag}_x_segs": xs, f"{tag}_f_segs": fs, f"{tag}_v_segs": v,
+                    f"{tag}_nfil": nfil, f"{tag}_nseg": nseg})
+    res.update(a_seg=ref.a_seg, mu=ref.mu)
+    return res
+
+
 def case_flow():
     """Flow field of the small swimmer at 333 points, with blobs (free space)
     with and without the net-force Stokeslet removed, and with no blobs (the
@@ -310,7 +334,8 @@ def case_step_default_dt():
 
 CASES = {"small_matvec": case_small, "overlap_a16": case_overlap, "tiny": case_tiny,
          "flow_small": case_flow, "solve_small": case_solve, "step_small": case_step,
-         "step_io": case_step_io, "step_default_dt": case_step_default_dt}
+         "step_io": case_step_io, "step_default_dt": case_step_default_dt,
+         "weak_coupled": case_weak}
 
 
 def main():

@@ -143,6 +143,40 @@ def test_blocks_fp32c_error_bound(case):
     assert max(errs.values()) < TOL32, errs
 
 
+def test_weakly_coupled_product_matches_reference():
+    """tfs_evaluate_weakly_coupled_segment_mobility against the reference's
+    own kernels (tests/golden/weak_coupled.npz: 6 x 20 segments with an
+    overlapping pair, and 5 x 7) and the oracle on the medium swimmer's
+    12 800 segments: max-abs error <= 1e-12 x max-abs value, in both solver
+    precisions (the product is FP64 in both)."""
+    d = load("weak_coupled")
+    for tag in ("six", "ragged"):
+        nfil, nseg = int(d[f"{tag}_nfil"]), int(d[f"{tag}_nseg"])
+        xs, fs = d[f"{tag}_x_segs"], d[f"{tag}_f_segs"]
+        for precision in ("fp64", "fp32c"):
+            s = make_solver(nfil * nseg, 1, nseg, precision=precision, a_seg=float(d["a_seg"]),
+                            mu=float(d["mu"]))
+            s.set_state(xs, fs, np.zeros((1, 3)), np.zeros((1, 3)))
+            s.evaluate_weakly_coupled_segment_mobility()
+            s.copy_segment_velocities_to_host()
+            s.wait_for_device()
+            err = rel_max(s.v_segs_host, d[f"{tag}_v_segs"])
+            s.finalise()
+            assert err < TOL64, (tag, precision, err)
+    from timfilsimmod_gb300.geometry import make_config
+
+    sw = make_config("medium", seed=9)
+    s = make_solver(sw.num_segs, sw.num_blobs, sw.nseg)
+    s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
+    s.evaluate_weakly_coupled_segment_mobility()
+    s.copy_segment_velocities_to_host()
+    s.wait_for_device()
+    got = s.v_segs_host.copy()
+    s.finalise()
+    ref = Oracle(threads=os.cpu_count() or 1).msf(sw.x_segs, sw.f_segs, sw.nfil, sw.nseg)
+    assert rel_max(got, ref) < TOL64, rel_max(got, ref)
+
+
 TOLFF = 1e-12
 
 

@@ -226,3 +226,19 @@ def test_reference_data_files_have_the_record_layout():
         if suffix != "_body_vels.dat":
             assert toks[0] in ("2", "3"), suffix  # step nt = 2, save step 3
             assert all(len(t.split("e")[0].split(".")[-1]) == 10 for t in toks[1:]), suffix
+
+
+def test_weakly_coupled_oracle_matches_reference_golden():
+    """orc_msf (the weakly coupled filaments' product) against the
+    reference's own filament-mean, total-force and Msf_mult kernels
+    (tests/golden/weak_coupled.npz): the reference sums means and totals
+    with atomic adds, so agreement is to rounding, <= 1e-14 of the largest
+    velocity."""
+    d = np.load(os.path.join(GOLD, "weak_coupled.npz"))
+    o = Oracle(mu=float(d["mu"]), a_seg=float(d["a_seg"]))
+    for tag in ("six", "ragged"):
+        v = o.msf(d[f"{tag}_x_segs"], d[f"{tag}_f_segs"], int(d[f"{tag}_nfil"]),
+                  int(d[f"{tag}_nseg"]))
+        ref = d[f"{tag}_v_segs"]
+        assert np.max(np.abs(v - ref)) <= 1e-14 * np.max(np.abs(ref)), tag
+        assert np.all(ref.reshape(-1, 6)[:, 3:] == 0.0)

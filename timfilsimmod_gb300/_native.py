@@ -106,6 +106,7 @@ _SIGNATURES = {
     "tfs_evaluate_segment_blob_mobility": [_H],
     "tfs_evaluate_blob_blob_mobility": [_H],
     "tfs_evaluate_blob_blob_mobility_ff": [_H],
+    "tfs_evaluate_weakly_coupled_segment_mobility": [_H],
     "tfs_evaluate_blob_segment_mobility": [_H],
     "tfs_evaluate_full_mobility": [_H, _P, _P],
     "tfs_apply_grand_mobility": [_H],

@@ -101,6 +101,8 @@ static void free_all(tfs_solver *s) {
   cudaFree(s->rec_blobs_x2);
   cudaFree(s->rec_ff);
   cudaFree(s->tile_boxes);
+  cudaFree(s->wc_z);
+  cudaFree(s->wc_f);
   cudaFree(s->scratch);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
@@ -434,6 +436,23 @@ int tfs_evaluate_blob_blob_mobility(tfs_solver *s) {
   TFS_CHECK_SOLVER(s);
   return product(s, false, false, true, OUT_ASSIGN);
 }
+int tfs_evaluate_weakly_coupled_segment_mobility(tfs_solver *s) {
+  TFS_CHECK_SOLVER(s);
+  const int nseg = s->cfg.nseg;
+  if (nseg < 1 || s->ns % nseg != 0)
+    return fail(TFS_EINVAL, "the segments must form whole filaments of nseg = %d", nseg);
+  const int nfil = s->ns / nseg;
+  int rc;
+  if (s->wc_z == nullptr &&
+      ((rc = alloc_dev((void **)&s->wc_z, sizeof(double) * 3 * nfil)) != TFS_OK ||
+       (rc = alloc_dev((void **)&s->wc_f, sizeof(double) * 3 * nfil)) != TFS_OK))
+    return rc;
+  cudaError_t e = launch_msf(s->x_segs, s->f_segs, nfil, nseg, s->cfg.a_seg, s->cfg.mu, s->wc_z,
+                             s->wc_f, s->v_segs, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "weakly coupled segment product");
+  return TFS_OK;
+}
+
 int tfs_evaluate_blob_blob_mobility_ff(tfs_solver *s) {
   TFS_CHECK_SOLVER(s);
   int rc;

@@ -108,6 +108,11 @@ cudaError_t launch_tile(const TileArgs &a, int vd, int fda, int fdb, TileTuning 
                         double *scratch, size_t scratch_elems, int mode, cudaStream_t st,
                         cudaEvent_t *ev = nullptr);
 cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st);
+// The weakly coupled filaments' segment product (weak.cu): filament means
+// Z and total forces Ft (3 nfil each, written), then v_segs (6 Ns).
+cudaError_t launch_msf(const double *x_segs, const double *f_segs, int nfil, int nseg,
+                       double a_seg, double mu, double *Z, double *Ft, double *v_segs,
+                       cudaStream_t st);
 // out = M_bb f_blobs in float-float arithmetic (rpy_ff.cu): packs the source
 // records into rec (ff_record_bytes() per blob), then the pair kernel and,
 // with source splits, the split reduction (scratch as for launch_tile). ev

@@ -214,6 +214,12 @@ class RpyMobilitySolver:
         product FP32C refinement computes its residuals with."""
         self._call("tfs_evaluate_blob_blob_mobility_ff")
 
+    def evaluate_weakly_coupled_segment_mobility(self):
+        """The weakly coupled filaments' segment product (the reference's
+        weakly_coupled_filaments_rpy_mobility_solver: RPY within a filament,
+        Stokeslets of the other filaments' total forces at their means)."""
+        self._call("tfs_evaluate_weakly_coupled_segment_mobility")
+
     def evaluate_blob_segment_mobility(self):
         self._call("tfs_evaluate_blob_segment_mobility")
 
