@@ -7,31 +7,41 @@
 // with the blob-blob product M_bb in FP32 (compensated per tile). At the
 // medium swimmer (2 562 blobs) an Arnoldi step is ~10 us of arithmetic;
 // issued as seven kernels per step it took ~150-190 us of launch gaps and
-// serialised reductions. Here one launch runs the whole solve:
+// serialised reductions. Here one launch runs the whole solve (~39 us per
+// Arnoldi step at the medium swimmer):
 //
-//   start | M_bb | residual | scale + preconditioner | { M_bb | w, CGS pass 1 |
-//   CGS pass 2 | norm | Givens + scale + preconditioner } x k | Q y | update
+//   start | M_bb | residual | scale + preconditioner | { M_bb + Givens |
+//   w, CGS pass-1 dots | h1, w -= Q h1, pass-2 dots, partials of w' |
+//   h2, ||w''||, Q_k, z_k = P^-1 Q_k } x k | Q y | update
 //
-// with a grid barrier between phases (seven per Arnoldi step), one CTA per
+// with a grid barrier between phases (four per Arnoldi step), one CTA per
 // SM. Every CTA owns a contiguous slice of blobs (its rows of every vector).
-// Reductions are deterministic (per-CTA partials added in CTA order):
-// the 6-vectors and squared norms, which every CTA needs at once, are summed
-// by every CTA itself (identical bits everywhere); the k Gram-Schmidt
-// coefficients of each pass are summed one per warp across the grid and
-// read back after a barrier, because GB300's FP64 rate (2 FMA/clk/SM) makes
-// k x G redundant additions per CTA the dominant cost. Givens rotations,
-// the convergence test and the final triangular solve run in CTA 0, which
+// Reductions are deterministic (per-CTA partials added in CTA order, fixed
+// shuffle trees): the Gram-Schmidt coefficients, 6-vectors and squared norms,
+// which every CTA needs at once, are summed by every CTA itself from the
+// staged partials (identical bits everywhere); when k x G exceeds the staging
+// buffers the coefficients are summed one per warp across the grid and read
+// back after an extra barrier. The new vector's norm and body sums follow
+// from the Pythagorean identity (||w''||^2 = ||w'||^2 - ||h2||^2, and the
+// stored sums of earlier vectors), so no barrier separates them from the
+// second pass. FP64 work is split across warps and accumulators: on GB300 an
+// FP64 warp instruction costs ~19 SM cycles, so serial chains in one warp
+// cost microseconds. Givens rotations, the convergence test and the final
+// triangular solve run in CTA 0 while the others start the next M_bb; CTA 0
 // publishes its decision for the others to read after the next barrier.
 // The M_bb product is cut into (target block x source split) units spread
-// over all CTAs; partial sums go to global memory and each row's owner adds
-// the splits in order.
+// over all CTAs (a target whose only pair inside contact in a tile is its own
+// blob adds the r = 0 term directly); partial sums go to global memory and
+// each row's owner adds the splits in order. One launch may carry several
+// independent solves (PgArgs array + CTA map), each on its own CTAs.
 //
-// Grid barrier: a counter and a generation word in global memory. Every
-// wait is bounded (2 s of globaltimer, plus an iteration cap); a CTA that
-// gives up raises an abort word that ends every other wait at once, and the
-// solve reports TFS_ETIMEOUT. The launch is cooperative, so all CTAs are
-// resident together (or the launch fails and the multi-kernel path runs).
-// Data other CTAs wrote is read with ld.global.cg (L2), never through L1.
+// Grid barrier: one monotonic arrival counter per solve in global memory
+// (the e-th barrier passes at e x P arrivals). Every wait is bounded (2 s of
+// globaltimer, plus an iteration cap); a CTA that gives up raises an abort
+// word that ends every other wait at once, and the solve reports
+// TFS_ETIMEOUT. The launch is cooperative, so all CTAs are resident together
+// (or the launch fails and the multi-kernel path runs). Data other CTAs wrote
+// is read with ld.global.cg (L2), never through L1.
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -6,11 +6,13 @@
 // non-blocking stream. A pool of host worker threads runs the instances'
 // step pipelines; the pipelines' kernels overlap on the GPU, so small
 // swimmers that cannot fill the GPU alone fill it together. Work is handed to
-// the workers largest first. Instances share nothing on the device, so each
-// result is the same as when the instance runs alone. The cooperative inner
-// GMRES kernel of the FP32C solve needs every SM at once and must not run
-// beside another instance's copy, so instances here use the kernel-sequence
-// inner GMRES (same iteration).
+// the workers largest first. The FP32C instances' inner GMRES solves run
+// through a GMRES service (solve.cu): several solves share one cooperative
+// launch of the persistent kernel, each on a fixed number of CTAs chosen from
+// its own size; instances the kernel cannot take, and FP64 instances, use the
+// kernel-sequence GMRES on their own streams. No instance's arithmetic
+// depends on the others, so each result is the same as when the instance runs
+// alone (a batch of one).
 //
 // The server keeps instances resident between requests (state, Krylov
 // basis, Broyden matrices) in a pool keyed by the swimmer's geometry, admits
