@@ -534,7 +534,11 @@ int linear_solve(tfs_solver *s, int *iters) {
     if ((e = launch_refine_residual(g64, s->xr, s->r, s->dx, it, s->stream)) != cudaSuccess)
       return cuda_fail(e, "refinement residual");
     if ((rc = poll(s, 1, &h)) != TFS_OK) return rc;
-    if (h.done) break;
+    // a non-finite residual (the kernel then marks the solve done with
+    // status 1): of the input itself at the first cycle, else a stall
+    if (h.status && it == 0)
+      return fail(TFS_ENAN, "non-finite right-hand side or warm start in the mobility solve");
+    if (h.done && !h.status) break;
     // a cycle that did not reduce the residual (or a non-finite one): the
     // FP32 inner products cannot make progress on this system
     if (h.status || !(h.rel == h.rel) || (it > 0 && !(h.rel < prev_rel)) || it == s->max_outer) {
