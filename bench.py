@@ -903,7 +903,7 @@ def main():
     p.add_argument("--batch-workers", type=int, default=16, help="host workers of the batch")
     p.add_argument("--serve-bases", type=int, default=12, help="base swimmers of the stream")
     p.add_argument("--serve-requests", type=int, default=96, help="requests per arrival rate")
-    p.add_argument("--serve-workers", type=int, default=8, help="server workers")
+    p.add_argument("--serve-workers", type=int, default=16, help="server workers")
     p.add_argument("--serve-rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0],
                    help="Poisson arrival rates (requests/s)")
     p.add_argument("--flow-grid", type=int, default=128, help="flow points per grid axis")

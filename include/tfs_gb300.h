@@ -377,7 +377,7 @@ typedef struct tfs_server_counters {
   size_t bytes_in_use;
 } tfs_server_counters;
 typedef struct tfs_server tfs_server;
-/* Defaults: 8 workers, 160 GB, FP32C, linear tolerance 1e-8, the step
+/* Defaults: 16 workers, 160 GB, FP32C, linear tolerance 1e-8, the step
  * defaults of tfs_step_config_default. */
 int tfs_server_config_default(tfs_server_config *cfg);
 int tfs_server_create(const tfs_server_config *cfg, tfs_server **out);

@@ -430,7 +430,7 @@ extern "C" {
 int tfs_server_config_default(tfs_server_config *cfg) {
   if (cfg == nullptr) return fail(TFS_EINVAL, "null config");
   std::memset(cfg, 0, sizeof *cfg);
-  cfg->num_workers = 8;
+  cfg->num_workers = 16;
   cfg->hbm_budget_bytes = (size_t)160 << 30;
   cfg->precision = TFS_FP32C;
   cfg->linear_tol = 1e-8;

@@ -79,7 +79,7 @@ class StepServer:
     arguments of tfs_step_config (dt, tol, seg_sep, end_force_magnitude,
     body_radius, max_broyden_iter, ...)."""
 
-    def __init__(self, num_workers: int = 8, hbm_budget_gb: float = 160.0,
+    def __init__(self, num_workers: int = 16, hbm_budget_gb: float = 160.0,
                  precision: str = "fp32c", linear_tol: float = 1e-8, **step):
         self.lib = N.load()
         cfg = N.ServerConfig()
