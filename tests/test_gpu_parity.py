@@ -200,6 +200,24 @@ def test_blob_blob_float_float_matches_reference(case):
         assert err < TOLFF, (case, precision, err)
 
 
+@pytest.mark.parametrize("tag", ["one", "tile"])
+def test_blob_blob_float_float_tiny(tag):
+    """The float-float M_bb on the reference's tiny cases (1 blob: only the
+    self term; 3 blobs beside 65 segments) against the reference's M_bb."""
+    d = load("tiny")
+    xs, fs = d[f"{tag}_x_segs"], d[f"{tag}_f_segs"]
+    xb, fb = d[f"{tag}_x_blobs"], d[f"{tag}_f_blobs"]
+    s = make_solver(xs.shape[0], xb.shape[0], int(d[f"{tag}_nseg"]), precision="fp32c",
+                    a_seg=float(d["a_seg"]), a_blob=float(d["a_blob"]), mu=float(d["mu"]))
+    s.set_state(xs, fs, xb, fb)
+    s.evaluate_blob_blob_mobility_ff()
+    s.copy_blob_velocities_to_host()
+    s.wait_for_device()
+    err = rel_max(s.v_blobs_host, d[f"{tag}_v_mbb"])
+    s.finalise()
+    assert err < TOLFF, (tag, err)
+
+
 def test_blob_blob_float_float_large_vs_fp64():
     """The same on the large swimmer's 10 242 blobs with N(0, 1) forces
     against the FP64 hook. The float-float rounding error is a fixed fraction
