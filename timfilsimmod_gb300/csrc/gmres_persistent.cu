@@ -15,7 +15,8 @@
 //   h2, ||w''||, Q_k, z_k = P^-1 Q_k } x k | Q y | update
 //
 // with a grid barrier between phases (four per Arnoldi step), one CTA per
-// SM. Every CTA owns a contiguous slice of blobs (its rows of every vector).
+// SM; with a zero warm start (PgArgs::zero_start) the first M_bb and the
+// residual are skipped (r0 = rhs). Every CTA owns a contiguous slice of blobs (its rows of every vector).
 // Reductions are deterministic (per-CTA partials added in CTA order, fixed
 // shuffle trees): the Gram-Schmidt coefficients, 6-vectors and squared norms,
 // which every CTA needs at once, are summed by every CTA itself from the
@@ -705,23 +706,31 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
       p.x32[3 * (size_t)m + k] = float(g.x_blobs[3 * (size_t)m + k] - g.origin[k]);
   if (sl.body && threadIdx.x < 6) g.soln[vel + threadIdx.x] = g.v_bodies[threadIdx.x];
   __syncthreads();
-  pack_records(p, sl, ws);
+  if (!p.zero_start) pack_records(p, sl, ws);
   slice_partials(p, sl, zs, K_RHS, S_RHS);
   slice_partials(p, sl, ws, K_SOLN, -1);
   if (!pg_barrier(p, &epoch)) return;
 
-  // ---- M_bb of the warm start
-  mbb_units(p, src);
-  if (!pg_barrier(p, &epoch)) return;
+  // the residual's slots: r0 = rhs with a zero warm start (A 0 = 0: its
+  // M_bb, the residual pass and two barriers are skipped)
+  const int k_r0 = p.zero_start ? K_RHS : K_R0, s_r0 = p.zero_start ? S_RHS : S_R0;
+  if (p.zero_start) {
+    for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = zs[r];
+    __syncthreads();
+  } else {
+    // ---- M_bb of the warm start
+    mbb_units(p, src);
+    if (!pg_barrier(p, &epoch)) return;
 
-  // ---- residual r0 = rhs - A soln (slice rows), partials
-  if (threadIdx.x < 6) zv[threadIdx.x] = g.v_bodies[threadIdx.x];
-  __syncthreads();
-  apply_rows(p, sl, zv, ws, hb);  // ws = A soln (blob rows)
-  for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = zs[r] - ws[r];  // zs = rhs rows
-  __syncthreads();
-  slice_partials(p, sl, ws, K_R0, S_R0);
-  if (!pg_barrier(p, &epoch)) return;
+    // ---- residual r0 = rhs - A soln (slice rows), partials
+    if (threadIdx.x < 6) zv[threadIdx.x] = g.v_bodies[threadIdx.x];
+    __syncthreads();
+    apply_rows(p, sl, zv, ws, hb);  // ws = A soln (blob rows)
+    for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = zs[r] - ws[r];  // zs = rhs rows
+    __syncthreads();
+    slice_partials(p, sl, ws, K_R0, S_R0);
+    if (!pg_barrier(p, &epoch)) return;
+  }
 
   // ---- beta_0, warm-start tests (mobility_solver.cpp:2279-2320), Q_0,
   //      preconditioner of Q_0, records (every CTA decides the same)
@@ -738,7 +747,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     double r0v[6];
     for (int j = 0; j < 6; ++j) r0v[j] = rhs_vel[j] - (-tmp8[j]);
     __syncthreads();
-    cta_sums(p.ps + (size_t)S_R0 * G, G, 1, tmp8, cst);
+    cta_sums(p.ps + (size_t)s_r0 * G, G, 1, tmp8, cst);
     double bb = tmp8[0];
     for (int j = 0; j < 6; ++j) bb += r0v[j] * r0v[j];
     double beta0 = sqrt(bb);
@@ -779,7 +788,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
       inv = norm_rhs;
     } else {
       if (threadIdx.x < 6) qvel[threadIdx.x] = r0v[threadIdx.x] / beta0;
-      kslot = K_R0;
+      kslot = k_r0;
       inv = beta0;
     }
     __syncthreads();

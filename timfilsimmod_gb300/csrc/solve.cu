@@ -284,6 +284,9 @@ PgArgs persistent_args(tfs_solver *s, const PgShape &sh, const double *rhs, doub
   p.pc_s3 = (float)(-2.0 * ab * ab);
   p.minv = 6.0 * 3.14159265358979323846264338327950288 * s->cfg.mu * ab;
   p.scale = 1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu);
+  // its only use is the refinement's inner solve, whose warm start (the
+  // correction dx) refine_residual_kernel has just set to zero
+  p.zero_start = 1;
   return p;
 }
 
