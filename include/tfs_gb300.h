@@ -154,10 +154,6 @@ int tfs_set_linear_solver(tfs_solver *s, double tol, int max_iter);
  * r = rhs - A x around inner GMRES solves with FP32 blob-blob products, each
  * to inner_tol relative to |r|, at most max_cycles cycles. */
 int tfs_set_refinement(tfs_solver *s, double inner_tol, int max_cycles);
-/* make_body_reference_matrices (mobility_solver.cpp:2950-3047): (K^T K)^-1
- * from the blob references and the 6x6 body mobility from six solves with
- * rhs = -e_{n-1-j}, at the current pose. Leaves the last solution as the next
- * warm start, as the reference does. */
 /* FP32C only: run each inner GMRES solve of the refinement as one
  * cooperative kernel (enable = 1, the default where the device supports
  * cooperative launch and the system has at most 64 blobs per SM pair of
@@ -165,6 +161,17 @@ int tfs_set_refinement(tfs_solver *s, double inner_tol, int max_cycles);
  * compute the same iteration; the cooperative kernel removes the launch
  * gaps between its phases. TFS_ESTATE if enable = 1 cannot be honoured. */
 int tfs_set_persistent_gmres(tfs_solver *s, int enable);
+/* Fault injection on the host, for tests of the bounded waits (no reference
+ * counterpart): with on = 1 the grid barriers of this solver's cooperative
+ * inner GMRES wait for one arrival more than the launch has CTAs, so every
+ * wait runs out its bound (2 s); the kernel then ends with an error status
+ * and the solve returns TFS_ETIMEOUT, leaving the device usable. on = 0
+ * (the default) restores normal solves. */
+int tfs_inject_barrier_stall(tfs_solver *s, int on);
+/* make_body_reference_matrices (mobility_solver.cpp:2950-3047): (K^T K)^-1
+ * from the blob references and the 6x6 body mobility from six solves with
+ * rhs = -e_{n-1-j}, at the current pose. Leaves the last solution as the next
+ * warm start, as the reference does. */
 int tfs_make_body_reference_matrices(tfs_solver *s);
 /* The two 6x6 matrices (column-major, body frame); either pointer may be NULL. */
 int tfs_get_body_reference_matrices(tfs_solver *s, double *body_mobility, double *ktkinv);

@@ -237,3 +237,47 @@ def test_shared_launches_repeatable_under_load():
     for i, (x, y) in enumerate(zip(a, b)):
         for k in ("x", "q", "lam", "body_x", "body_q"):
             assert np.array_equal(x[k], y[k]), (i, k)
+
+
+def test_stalled_swimmer_does_not_stall_batch():
+    """A swimmer whose inner solves' grid barriers are made (on the host) to
+    wait for one CTA more than their launch has fails alone with TFS_ETIMEOUT
+    once the 2 s bound runs out; the others -- whose inner solves share
+    cooperative launches with it, each solve on its own CTAs and barrier
+    words -- complete, bit for bit as alone."""
+    from timfilsimmod_gb300 import _native as N
+    from timfilsimmod_gb300.serving import SwimmerBatch
+
+    alone = []
+    for subdiv, nfil in SHAPES:
+        s, st = make_instance(subdiv, nfil, "fp32c")
+        one = SwimmerBatch(num_workers=1)
+        one.add(st)
+        one.step(0, allow_unconverged=True)
+        alone.append(st.state())
+        one.close()
+        st.close()
+        s.finalise()
+    inst = [make_instance(subdiv, nfil, "fp32c") for subdiv, nfil in SHAPES]
+    bad = 1
+    inst[bad][0].inject_barrier_stall(True)
+    batch = SwimmerBatch(num_workers=3)
+    for _, st in inst:
+        batch.add(st)
+    n = len(inst)
+    b, g, status = (np.zeros(n, dtype=np.int32) for _ in range(3))
+    rc = batch.lib.tfs_batch_step(batch._h, 0, b.ctypes.data, g.ctypes.data, status.ctypes.data)
+    assert rc != N.TFS_OK
+    assert status[bad] == N.TFS_ETIMEOUT, status
+    for i, ((s, st), ref) in enumerate(zip(inst, alone)):
+        if i == bad:
+            continue
+        assert status[i] in (N.TFS_OK, N.TFS_ENOTCONV), (i, status)
+        got = st.state()
+        for k in ("x", "q", "lam", "body_x", "body_q"):
+            assert np.array_equal(got[k], ref[k]), (i, k)
+    assert batch.shared_solves()["solves"] > 0
+    batch.close()
+    for s, st in inst:
+        st.close()
+        s.finalise()

@@ -196,3 +196,59 @@ def test_persistent_and_kernel_sequence_agree():
     assert abs(a[0] - b[0]) <= max(3, b[0] // 10)
     for x, y in zip(a[1:5], b[1:5]):
         assert rel_max(x, y) < 2e-5
+
+
+def test_barrier_stall_times_out_and_solver_recovers():
+    """Fault injection on the host: the cooperative inner GMRES's grid
+    barriers wait for one CTA more than the launch has. Every wait runs out
+    its bound (2 s of globaltimer), the kernel ends with an error status, the
+    solve raises TFS_ETIMEOUT, and the same solver -- the injection removed --
+    then solves bit for bit as a solver that never failed (the context stays
+    usable; a failed refinement leaves the warm start untouched)."""
+    import time
+
+    from timfilsimmod_gb300 import _native as N
+    from timfilsimmod_gb300.geometry import make_config
+
+    sw = make_config("medium", seed=11)
+    F = sw.f_segs[:, :3].sum(0)
+    T = (np.cross(sw.x_segs, sw.f_segs[:, :3]) + sw.f_segs[:, 3:]).sum(0)
+    sf = np.concatenate([F, T])
+
+    def setup():
+        s = new_solver(sw.nfil, sw.nseg, sw.num_blobs, "fp32c")
+        s.set_blob_references(sw.blob_references)
+        s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+        s.set_linear_solver(1e-8)
+        set_segments(s, sw.x_segs, sw.f_segs)
+        s.make_body_reference_matrices()
+        return s
+
+    def result(s):
+        # compute_velocities adds the barrier forces into the device's segment
+        # forces (as the reference's apply_interparticle_forces does): upload
+        # them afresh before each call
+        set_segments(s, sw.x_segs, sw.f_segs)
+        it, sf_out = s.compute_velocities(sf)
+        s.copy_segment_velocities_to_host()
+        s.wait_for_device()
+        return it, sf_out, s.v_segs_host.copy(), s.blob_forces(), s.body_velocities()
+
+    clean = setup()
+    want = result(clean)
+    clean.finalise()
+
+    s = setup()
+    s.inject_barrier_stall(True)
+    t0 = time.perf_counter()
+    with pytest.raises(N.TfsError) as e:
+        result(s)
+    took = time.perf_counter() - t0
+    assert e.value.code == N.TFS_ETIMEOUT, e.value
+    assert 1.5 < took < 60.0, took
+    s.inject_barrier_stall(False)
+    got = result(s)
+    assert got[0] == want[0]
+    for x, y in zip(got[1:], want[1:]):
+        assert np.array_equal(x, y)
+    s.finalise()

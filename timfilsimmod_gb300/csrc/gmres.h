@@ -74,6 +74,8 @@ struct PgArgs {
   int P, TB, tbs, S, chunk, Kr;  // P: the CTAs of this solve
   int rank;               // this CTA's index among them (set on the device)
   int zero_start;         // 1: the warm start is zero (A x0 = 0, r0 = rhs; its M_bb skipped)
+  unsigned bar_extra;     // arrivals each barrier waits for beyond the P CTAs: 0, or 1
+                          // under tfs_inject_barrier_stall (every wait then runs out)
   size_t dyn_smem;
   float a;                // blob radius
   float pc_asum2, pc_s, pc_s3;  // FP32 pair constants: (2a)^2, 2a^2/3, -2a^2

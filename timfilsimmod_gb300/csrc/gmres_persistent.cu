@@ -16,7 +16,8 @@
 //
 // with a grid barrier between phases (four per Arnoldi step), one CTA per
 // SM; with a zero warm start (PgArgs::zero_start) the first M_bb and the
-// residual are skipped (r0 = rhs). Every CTA owns a contiguous slice of blobs (its rows of every vector).
+// residual are skipped (r0 = rhs). Every CTA owns a contiguous slice of
+// blobs (its rows of every vector).
 // Reductions are deterministic (per-CTA partials added in CTA order, fixed
 // shuffle trees): the Gram-Schmidt coefficients, 6-vectors and squared norms,
 // which every CTA needs at once, are summed by every CTA itself from the
@@ -93,7 +94,7 @@ __device__ bool pg_barrier(const PgArgs &p, unsigned *epoch) {
   if (threadIdx.x == 0) {
     volatile unsigned *vb = p.bar;
     int good = 1;
-    const unsigned target = (*epoch + 1u) * (unsigned)p.P;
+    const unsigned target = (*epoch + 1u) * ((unsigned)p.P + p.bar_extra);
     *epoch += 1u;
     __threadfence();
     atomicAdd(p.bar, 1u);

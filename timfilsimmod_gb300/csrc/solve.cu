@@ -287,6 +287,7 @@ PgArgs persistent_args(tfs_solver *s, const PgShape &sh, const double *rhs, doub
   // its only use is the refinement's inner solve, whose warm start (the
   // correction dx) refine_residual_kernel has just set to zero
   p.zero_start = 1;
+  p.bar_extra = s->pg_stall ? 1u : 0u;
   return p;
 }
 
@@ -752,6 +753,12 @@ int tfs_set_persistent_gmres(tfs_solver *s, int enable) {
   if (enable && !s->pg_ok)
     return fail(TFS_ESTATE, "the persistent GMRES kernel cannot run for this system or device");
   s->pg_enabled = enable != 0;
+  return TFS_OK;
+}
+
+int tfs_inject_barrier_stall(tfs_solver *s, int on) {
+  TFS_CHECK_SOLVER(s);
+  s->pg_stall = on != 0;
   return TFS_OK;
 }
 

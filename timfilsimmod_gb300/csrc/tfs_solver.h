@@ -63,6 +63,7 @@ struct tfs_solver {
   unsigned *gcounters = nullptr;
   // persistent inner GMRES (FP32C); pg_ok = 0 when it cannot run here
   int pg_ok = 0, pg_enabled = 1;
+  int pg_stall = 0;  // tfs_inject_barrier_stall: barriers wait for one CTA more than run
   tfs::PgShape pg{};
   float *pg_x32 = nullptr, *pg_rec = nullptr;
   float2 *pg_mpart = nullptr;

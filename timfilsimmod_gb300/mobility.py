@@ -261,6 +261,12 @@ class RpyMobilitySolver:
         sequence of kernels per Arnoldi step."""
         self._call("tfs_set_persistent_gmres", int(bool(enable)))
 
+    def inject_barrier_stall(self, on: bool = True) -> None:
+        """Test hook: the cooperative inner GMRES's grid barriers wait for one
+        CTA more than the launch has, so each wait runs out its 2 s bound and
+        the solve raises TfsError(TFS_ETIMEOUT); off restores normal solves."""
+        self._call("tfs_inject_barrier_stall", int(bool(on)))
+
     def make_body_reference_matrices(self) -> tuple[np.ndarray, np.ndarray]:
         """Returns (body_mobility_reference, KTKinv_reference), 6x6 column-major flat."""
         self._call("tfs_make_body_reference_matrices")
