@@ -366,3 +366,47 @@ def test_autotune_table_and_parity():
     out = run_blocks(s, xs, fs, xb, fb)
     s.finalise()
     assert rel_max(out["v_mss"], d["v_mss"]) < TOL64
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("nfil,nblob", [(0, 40), (6, 0), (0, 0)])
+def test_one_sided_and_empty_systems(precision, nfil, nblob):
+    """Systems without segments, without blobs, or with neither (the
+    reference's NFIL = 0 and NBLOB = 0 builds): every hook returns TFS_OK, a
+    product with no sources assigns zero (or leaves an accumulation alone),
+    and what is there matches the oracle."""
+    nseg = 4
+    ns = nfil * nseg
+    rng = np.random.default_rng(17)
+    # distinct sites of a 2.3-spaced lattice: no pair inside contact
+    sites = 2.3 * np.stack(np.meshgrid(*[np.arange(5)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    pick = rng.permutation(len(sites))
+    xs, xb = sites[pick[:ns]], sites[pick[ns:ns + nblob]]
+    fs, fb = rng.normal(size=(ns, 6)), rng.normal(size=(nblob, 3))
+    s = make_solver(ns, nblob, nseg, precision=precision)
+    out = run_blocks(s, xs, fs, xb, fb)
+    s.apply_grand_mobility()
+    s.copy_segment_velocities_to_host()
+    s.copy_blob_velocities_to_host()
+    s.wait_for_device()
+    vs, vb = s.v_segs_host.copy(), s.v_blobs_host.copy()
+    s.apply_interparticle_forces()
+    s.wait_for_device()
+    s.finalise()
+    assert vs.size == 6 * ns and vb.size == 3 * nblob
+    o = Oracle()
+    cmp = rel_max if precision == "fp64" else rel_l2
+    tol = TOL64 if precision == "fp64" else TOL32
+    if ns:
+        ref_ss = o.mss(xs, fs)
+        assert cmp(out["v_mss"], ref_ss) < tol
+        # no blobs: Msb adds nothing to Mss
+        assert cmp(out["v_mss_plus_msb"], ref_ss if not nblob else
+                   o.msb(xs, xb, fb, ref_ss.copy())) < tol
+        assert cmp(vs, ref_ss) < tol
+    if nblob:
+        ref_bb = o.mbb(xb, fb)
+        assert cmp(out["v_mbb"], ref_bb) < tol
+        # no segments: Mbs assigns zero
+        assert np.all(out["v_mbs"] == 0.0)
+        assert cmp(vb, ref_bb) < tol
