@@ -103,33 +103,48 @@ __device__ void extrapolate(double *v, double *m1, double *m2, int n, int nt) {
 
 // The base segment at X + R ref and the robot arm
 // x_j = x_{j-1} + DL/2 (t_{j-1} + t_j) (accept_state_from_rigid_body and
-// robot_arm, filament.cpp:625-661), one thread per filament. In
+// robot_arm, filament.cpp:625-661), one warp per filament. In
 // swimmer::update the reference runs the robot arm twice (after the base
 // segment's update and after the whole filament's); the first result is
 // overwritten by the second, which depends only on x_0 and the final
 // orientations, so it runs once here, after every segment is updated.
-__global__ void k_robot_arm(StepDev d, BodyArgs b) {
-  const int fil = blockIdx.x * blockDim.x + threadIdx.x;
-  if (fil >= d.nfil) return;
+constexpr int kFilWarps = 4;  // filaments (one warp each) per CTA of the per-filament kernels
+
+__global__ void __launch_bounds__(32 * kFilWarps) k_robot_arm(StepDev d, BodyArgs b) {
+  __shared__ double tan_s[kFilWarps][32][3];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int fil = blockIdx.x * kFilWarps + w;
+  if (fil >= d.nfil) return;  // the whole warp
   const int s0 = fil * d.nseg;
-  const double *ref = d.fil_refs + 3 * fil;
-  double xp[3];
-  for (int i = 0; i < 3; ++i) {
-    double s = 0.0;
-    for (int k = 0; k < 3; ++k) s += b.R[3 * i + k] * ref[k];
-    xp[i] = b.x[i] + s;
-    d.x[3 * s0 + i] = xp[i];
-  }
-  double t1[3], t2[3];
-  tangent(load_q(d.q + 4 * s0), t1);
-  for (int j = 1; j < d.nseg; ++j) {
-    const int s = s0 + j;
-    tangent(load_q(d.q + 4 * s), t2);
-    for (int k = 0; k < 3; ++k) {
-      xp[k] = xp[k] + 0.5 * d.dl * (t1[k] + t2[k]);
-      d.x[3 * s + k] = xp[k];
-      t1[k] = t2[k];
+  double xp[3] = {0.0, 0.0, 0.0}, t1[3] = {0.0, 0.0, 0.0};
+  if (lane == 0) {
+    const double *ref = d.fil_refs + 3 * fil;
+    for (int i = 0; i < 3; ++i) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += b.R[3 * i + k] * ref[k];
+      xp[i] = b.x[i] + s;
+      d.x[3 * s0 + i] = xp[i];
     }
+  }
+  // the lanes form 32 segments' tangents at a time; lane 0 adds them up in
+  // segment order
+  for (int j0 = 0; j0 < d.nseg; j0 += 32) {
+    if (j0 + lane < d.nseg) tangent(load_q(d.q + 4 * (s0 + j0 + lane)), tan_s[w][lane]);
+    __syncwarp();
+    if (lane == 0) {
+      const int m = min(32, d.nseg - j0);
+      for (int q = 0; q < m; ++q) {
+        const double *t2 = tan_s[w][q];
+        const int s = s0 + j0 + q;
+        if (s > s0)
+          for (int k = 0; k < 3; ++k) {
+            xp[k] = xp[k] + 0.5 * d.dl * (t1[k] + t2[k]);
+            d.x[3 * s + k] = xp[k];
+          }
+        for (int k = 0; k < 3; ++k) t1[k] = t2[k];
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -255,25 +270,40 @@ __global__ void k_forces(StepDev d, int nt) {
 }
 
 // This filament's part of the swimmer force, -sum (f ; (x - X) x f + torque)
-// in segment order (swimmer.cpp:469-529), one thread per filament.
-__global__ void k_swimmer_force(StepDev d, double bx0, double bx1, double bx2,
-                                double *__restrict__ swf_part) {
-  const int fil = blockIdx.x * blockDim.x + threadIdx.x;
-  if (fil >= d.nfil) return;
+// in segment order (swimmer.cpp:469-529), one warp per filament: the lanes
+// form 32 segments' terms at a time, lane 0 subtracts them in order.
+__global__ void __launch_bounds__(32 * kFilWarps) k_swimmer_force(StepDev d, double bx0,
+                                                                  double bx1, double bx2,
+                                                                  double *__restrict__ swf_part) {
+  __shared__ double term[kFilWarps][32][6];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int fil = blockIdx.x * kFilWarps + w;
+  if (fil >= d.nfil) return;  // the whole warp
   const int n = d.nseg, s0 = fil * n;
   double sw[6] = {0, 0, 0, 0, 0, 0};
-  for (int m = 0; m < n; ++m) {
-    const double *fm = d.f + 6 * (size_t)(s0 + m);
-    const double *xm = d.x + 3 * (size_t)(s0 + m);
-    sw[0] -= fm[0];
-    sw[1] -= fm[1];
-    sw[2] -= fm[2];
-    const double xd = xm[0] - bx0, yd = xm[1] - bx1, zd = xm[2] - bx2;
-    sw[3] -= fm[3] + yd * fm[2] - zd * fm[1];
-    sw[4] -= fm[4] + zd * fm[0] - xd * fm[2];
-    sw[5] -= fm[5] + xd * fm[1] - yd * fm[0];
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    if (j0 + lane < n) {
+      const double *fm = d.f + 6 * (size_t)(s0 + j0 + lane);
+      const double *xm = d.x + 3 * (size_t)(s0 + j0 + lane);
+      double *t = term[w][lane];
+      t[0] = fm[0];
+      t[1] = fm[1];
+      t[2] = fm[2];
+      const double xd = xm[0] - bx0, yd = xm[1] - bx1, zd = xm[2] - bx2;
+      t[3] = fm[3] + yd * fm[2] - zd * fm[1];
+      t[4] = fm[4] + zd * fm[0] - xd * fm[2];
+      t[5] = fm[5] + xd * fm[1] - yd * fm[0];
+    }
+    __syncwarp();
+    if (lane == 0) {
+      const int m = min(32, n - j0);
+      for (int q = 0; q < m; ++q)
+        for (int k = 0; k < 6; ++k) sw[k] -= term[w][q][k];
+    }
+    __syncwarp();
   }
-  for (int k = 0; k < 6; ++k) swf_part[6 * fil + k] = sw[k];
+  if (lane == 0)
+    for (int k = 0; k < 6; ++k) swf_part[6 * fil + k] = sw[k];
 }
 
 // BDF residuals (mobility_solver.cpp:2661-2946), one thread per segment; the
@@ -1515,9 +1545,10 @@ int tfs_stepper_initial_guess(tfs_stepper *st, int nt) {
   rot_rm(st->bq, st->Qinit);
   st->jac_ready = 0;
   const BodyArgs b = body_args(st, nt);
-  k_guess_segments<<<(st->d.ns + 127) / 128, 128, 0, st->s->stream>>>(st->d, b, nt);
+  k_guess_segments<<<(st->d.ns + 63) / 64, 64, 0, st->s->stream>>>(st->d, b, nt);
   ST_LAUNCH("initial guess");
-  k_robot_arm<<<(st->d.nfil + 63) / 64, 64, 0, st->s->stream>>>(st->d, b);
+  k_robot_arm<<<(st->d.nfil + kFilWarps - 1) / kFilWarps, 32 * kFilWarps, 0, st->s->stream>>>(
+      st->d, b);
   ST_LAUNCH("robot arm");
   st->s->origin_dirty = true;
   return TFS_OK;
@@ -1527,9 +1558,10 @@ int tfs_stepper_forces(tfs_stepper *st, int nt, double *swimmer_f) {
   TFS_CHECK_STEPPER(st);
   const StepDev &d = st->d;
   cudaStream_t str = st->s->stream;
-  k_forces<<<(d.ns + 127) / 128, 128, 0, str>>>(d, nt);
+  k_forces<<<(d.ns + 63) / 64, 64, 0, str>>>(d, nt);
   ST_LAUNCH("internal forces");
-  k_swimmer_force<<<(d.nfil + 63) / 64, 64, 0, str>>>(d, st->bx[0], st->bx[1], st->bx[2], st->swpart);
+  k_swimmer_force<<<(d.nfil + kFilWarps - 1) / kFilWarps, 32 * kFilWarps, 0, str>>>(
+      d, st->bx[0], st->bx[1], st->bx[2], st->swpart);
   ST_LAUNCH("swimmer force");
   ST_CUDA(cudaMemcpyAsync(st->hbuf, st->swpart, sizeof(double) * 6 * d.nfil, cudaMemcpyDeviceToHost, str),
           "swimmer force");
@@ -1557,7 +1589,7 @@ int tfs_stepper_compute_errors(tfs_stepper *st, int nt, int which, double *err_h
   double *e = which ? st->nerr : st->err;
   ST_CUDA(cudaMemsetAsync(st->flag, 0, sizeof(int), str), "error flag");
   const BodyArgs b = body_args(st, nt);
-  k_errors<<<(d.ns + 255) / 256, 256, 0, str>>>(d, b, nt, st->cfg.tol, st->s->v_segs, st->s->v_bodies,
+  k_errors<<<(d.ns + 63) / 64, 64, 0, str>>>(d, b, nt, st->cfg.tol, st->s->v_segs, st->s->v_bodies,
                                                  e, st->flag);
   ST_LAUNCH("residuals");
   ST_CUDA(cudaMemcpyAsync(st->hflag, st->flag, sizeof(int), cudaMemcpyDeviceToHost, str), "error flag");
@@ -1694,9 +1726,9 @@ int tfs_stepper_apply_update(tfs_stepper *st, int nt) {
   }
   store_q(st->bq, qmul(lie_exp(st->bu), load_q(st->bqm1)));
   const BodyArgs b = body_args(st, nt);
-  k_update_segments<<<(st->d.ns + 127) / 128, 128, 0, str>>>(st->d, b, st->upd);
+  k_update_segments<<<(st->d.ns + 63) / 64, 64, 0, str>>>(st->d, b, st->upd);
   ST_LAUNCH("apply update");
-  k_robot_arm<<<(st->d.nfil + 63) / 64, 64, 0, str>>>(st->d, b);
+  k_robot_arm<<<(st->d.nfil + kFilWarps - 1) / kFilWarps, 32 * kFilWarps, 0, str>>>(st->d, b);
   ST_LAUNCH("robot arm");
   st->s->origin_dirty = true;
   return tfs_stepper_forces(st, nt, nullptr);
