@@ -12,8 +12,9 @@ inputs/outputs). Printed: one JSON line (rank 0).
   e2e      matvecs/s through the C-ABI hooks with pinned host buffers: the H2D
            copies of positions and forces and the D2H copies of velocities are
            inside the timed region
-  roofline the dominant kernel (the segment-target tile kernel) against the
-           measured FP32 FMA peak
+  roofline the dominant kernel (the work-queue kernel: both target kinds,
+           all four blocks and the source-split sums in one persistent launch)
+           against the measured FP32 FMA peak
   fp64     the same product in plain FP64 (the parity drop-in) for comparison
 
   solve    compute_velocities (the free-body GMRES solve of one Broyden
@@ -59,6 +60,13 @@ FLOPS_66, FLOPS_63, FLOPS_36, FLOPS_33 = 93, 56, 56, 40  # canonical flops per p
 
 def grand_flops(ns, nb):
     return ns * ns * FLOPS_66 + ns * nb * FLOPS_63 + nb * ns * FLOPS_36 + nb * nb * FLOPS_33
+
+
+def queue_bytes(ns, nb):
+    """Algorithmic bytes of one FP32C grand-mobility launch: the source
+    records read (48 B per segment, 32 B per blob), the FP64 target positions
+    read and the FP64 velocities written."""
+    return 48 * ns + 32 * nb + 24 * (ns + nb) + 8 * (6 * ns + 3 * nb)
 
 
 def grand_pairs(ns, nb):
@@ -130,7 +138,9 @@ class ClockSampler:
 # DRAM bytes per launch of the segment-target tile kernel (FP32C grand
 # mobility), from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum,
 # rpy_tile_kernel<float,6,6,3,128,1,256,8>, medium swimmer): 1 043 200 + 0.
-TILE_TRAFFIC = {"medium": 1043200}
+# DRAM bytes per launch of the grand-mobility work-queue launch (dram__bytes_read.sum +
+# dram__bytes_write.sum, one ncu capture of this workload); None until captured
+QUEUE_TRAFFIC = {}
 
 
 def max_over_ranks(values, world: int, device: str):
@@ -232,7 +242,7 @@ def bench_ours(args):
     # --- mixed precision, device resident (value) ---------------------------
     s32 = make("fp32c")
     ms32, launches, ktimes = timed_steps(s32, args.steps, args.warmup, timing=True)
-    seg_launches = ktimes[0::2]  # per step: segment-target launch, then blob-target launch
+    seg_launches = ktimes  # one work-queue launch per step
 
     # --- end to end through the C-ABI hooks, pinned host buffers ----------------
     s32.f_segs_host[:] = sw.f_segs.ravel()
@@ -297,10 +307,10 @@ def bench_ours(args):
     value = whole_job_rate(args.steps, world, ms32 * 1e-3)
     e2e_value = whole_job_rate(e2e_steps, world, t_e2e * 1e-3)
     value64 = whole_job_rate(steps64, world, ms64 * 1e-3)
-    seg_flops = ns * ns * FLOPS_66 + ns * nb * FLOPS_63
+    seg_flops = grand_flops(ns, nb)  # the launch computes the whole grand mobility
     seg_ms = float(np.mean(seg_launches)) if seg_launches else float("nan")
     achieved = seg_flops / (seg_ms * 1e-3) / 1e12
-    seg64 = ktimes64[0::2]
+    seg64 = ktimes64
     seg64_ms = float(np.mean(seg64)) if seg64 else float("nan")
     achieved64 = seg_flops / (seg64_ms * 1e-3) / 1e12
     err = float(np.linalg.norm(v32 - v64) / np.linalg.norm(v64))
@@ -330,17 +340,19 @@ def bench_ours(args):
             "pair_interactions_per_s": value * grand_pairs(ns, nb),
             "e2e": {"value": e2e_value, "unit": "matvecs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "fp32-fma", "kernel": "rpy_tile_kernel<float,6,6,3>",
+            "roofline": {"bound": "fp32-fma", "kernel": "rpy_queue_kernel<float,6,3>",
                          "achieved": achieved, "peak": peak32 / 1e12, "unit": "TFLOP/s",
                          "frac": achieved / (peak32 / 1e12),
                          "peak_source": "measured live (FMA-chain microbenchmark, this run)",
                          "flops_per_launch": seg_flops, "avg_launch_ms": seg_ms,
-                         "traffic": TILE_TRAFFIC.get(args.config),
+                         "traffic": QUEUE_TRAFFIC.get(args.config),
+                         "algorithmic_bytes": queue_bytes(ns, nb),
                          "traffic_note": "bytes per launch, dram__bytes_read.sum + "
                                          "dram__bytes_write.sum of one ncu capture of the "
-                                         "tuned segment-target launch on this workload; "
-                                         "algorithmic bytes ~1.0 MB (source records + "
-                                         "targets; split partials stay in L2)"},
+                                         "tuned grand-mobility launch on this workload; "
+                                         "algorithmic bytes: FP32 source records, FP64 "
+                                         "target positions and velocities (the chunk "
+                                         "partial sums stay in L2)"},
             "fp64": {"value": value64, "unit": "matvecs/s", "steps": steps64,
                      "roofline": {"bound": "fp64-fma", "achieved": achieved64,
                                   "peak": peak64 / 1e12, "unit": "TFLOP/s",

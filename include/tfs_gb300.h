@@ -204,15 +204,25 @@ int tfs_copy_blob_forces_to_host(tfs_solver *s, double *f_blobs_host);
 int tfs_solve_info(tfs_solver *s, int *iters, int *cycles, double *rel_residual);
 
 /* --- autotuning ---------------------------------------------------------- */
-/* Time every launch variant of the tile kernel (threads per CTA, targets per
- * thread, sources per tile, scalar or packed FP32x2) and every source-split
- * target (1, 2 or 4 full waves of resident CTAs) for each (target, source
- * set) combination the solver uses,
- * on its current positions and forces, and keep the fastest per combination.
- * precision_mask: bit 0 = TFS_FP64, bit 1 = TFS_FP32C. reps: timed
- * launches per candidate. Overwrites the solver's velocity buffers.
- * Synchronises the solver's stream. */
+/* Products run as work-queue launches: one persistent grid whose CTAs take
+ * (target block, source chunk) units of every product of the launch from a
+ * device counter, with the source-split sums added in chunk order inside the
+ * same launch. The launch variant (threads per CTA, targets per thread,
+ * sources per tile, register cap) changes the speed, never the result: the
+ * chunking depends on the system's sizes only.
+ * Autotune times every queue variant for each product kind the solver has
+ * (M_ss, M_bs, both at once, M_sb, M_bb, the grand mobility) and every
+ * variant and source-split target of the tile kernel for the blob-blob
+ * product of the kernel-sequence GMRES, on the current positions and forces,
+ * and keeps the fastest of each. precision_mask: bit 0 = TFS_FP64, bit 1 =
+ * TFS_FP32C. reps: timed launches per candidate. Overwrites the solver's
+ * velocity buffers. Synchronises the solver's stream. */
 int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps);
+/* Pin the work-queue variant of one product kind: kind 0..5 = M_ss, M_bs,
+ * M_ss with M_bs, M_sb, M_bb, grand mobility; variant in
+ * [0, tfs_num_queue_variants(precision)). */
+int tfs_solver_set_queue_variant(tfs_solver *s, int precision, int kind, int variant);
+int tfs_num_queue_variants(int precision);
 /* Pin the launch of one combination: combo 0..5 = seg<-seg, seg<-blob,
  * blob<-blob, blob<-seg, seg<-(seg,blob), blob<-(seg,blob); variant in
  * [0, tfs_num_tile_variants(precision)); waves in [1, 64] (the source split

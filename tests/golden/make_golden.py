@@ -332,10 +332,66 @@ def case_step_default_dt():
     return res
 
 
+def medium_setup():
+    """The medium swimmer's body (R = 60, 2562 blobs) with 640 straight
+    filaments of 20 segments along the surface normals."""
+    sw = make_config("medium", seed=1)
+    normals = fibonacci_sphere(sw.nfil)
+    fil_refs = (sw.radius + 1.0 + 0.5 * 2.2) * normals
+    efm = 220.0 * 1800.0 / (2.6 * 2.6 * sw.nseg ** 2)
+    return sw, normals, fil_refs, efm
+
+
+def _medium_trajectory(config, dt, nsteps, full_steps):
+    sw, normals, fil_refs, efm = medium_setup()
+    nfil, nseg = sw.nfil, sw.nseg
+    ref = ReferenceStep(nfil, nseg, sw.blob_references, fil_refs, normals, efm, seg_sep=2.2,
+                        body_length=2.0 * sw.radius, config=config)
+    bm, ktk = ref.make_body_reference_matrices()
+    res = dict(blob_refs=sw.blob_references, fil_refs=fil_refs, fil_dirs=normals, nfil=nfil,
+               nseg=nseg, end_force_magnitude_real=efm, body_radius=sw.radius, dt=dt,
+               tol=1e-4, linear_tol=ref.lib.ref_linear_system_tol(), body_mobility=bm,
+               ktkinv=ktk, full_steps=np.array(full_steps))
+    broy, gm, tips, keep = [], [], [], {}
+    for nt in range(nsteps):
+        b, g = ref.run(nt)
+        broy.append(b)
+        gm.append(g)
+        st = ref.state()
+        x = st["x"].reshape(nfil, nseg, 3)
+        tips.append(x[:, -1, :].ravel())
+        for k in ("body_x", "body_q", "body_u", "tether", "clamp"):
+            keep.setdefault(k, []).append(st[k])
+        if nt in full_steps:
+            res[f"x_step{nt}"] = st["x"]
+        print(f"  step {nt}: Broyden {b}, GMRES {g}", flush=True)
+    last = ref.state()
+    res.update(final_q=last["q"], final_u=last["u"], final_lam=last["lam"],
+               traj_tips=np.array(tips), broyden_iters=np.array(broy), gmres_iters=np.array(gm))
+    res.update({f"traj_{k}": np.array(v) for k, v in keep.items()})
+    return res
+
+
+def case_step_medium():
+    """The reference's implicit time step on the medium swimmer (R = 60,
+    2562 blobs, 640 straight filaments x 20 segments), DT = 1e-3, Broyden
+    TOL 1e-4, LINEAR_SYSTEM_TOL 1e-10: steps 0-9 with, after every step, the
+    filament tip positions, body pose and tether and clamp forces, and all
+    segment positions after steps 0, 4 and 9."""
+    return _medium_trajectory("s1", 1e-3, 10, (0, 4, 9))
+
+
+def case_step_medium_default_dt():
+    """The same swimmer at the reference's default DT = 36.3833/300, where
+    Broyden iterates every step: steps 0-3, all segment positions after each."""
+    return _medium_trajectory("s2", 36.3833 / 300.0, 4, (0, 1, 2, 3))
+
+
 CASES = {"small_matvec": case_small, "overlap_a16": case_overlap, "tiny": case_tiny,
          "flow_small": case_flow, "solve_small": case_solve, "step_small": case_step,
          "step_io": case_step_io, "step_default_dt": case_step_default_dt,
-         "weak_coupled": case_weak}
+         "weak_coupled": case_weak, "step_medium": case_step_medium,
+         "step_medium_default_dt": case_step_medium_default_dt}
 
 
 def main():

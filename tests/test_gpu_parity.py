@@ -324,19 +324,24 @@ def test_native_library_is_loaded_and_counts_launches():
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32c"])
 def test_every_launch_variant_matches_reference(precision):
-    """Every compiled tile-kernel variant, at two split targets, on the ragged
+    """Every compiled work-queue variant (the products) and tile-kernel
+    variant at two split targets (set for every combination; the
+    kernel-sequence GMRES's blob-blob product uses it), on the ragged
     unequal-radius case (all branches) and on the small swimmer."""
-    from timfilsimmod_gb300.mobility import num_tile_variants
+    from timfilsimmod_gb300.mobility import QUEUE_KINDS, num_queue_variants, num_tile_variants
 
+    nq = num_queue_variants(precision)
     for case in ("overlap_a16", "small_matvec"):
         d = load(case)
         xs, fs, xb, fb = d["x_segs"], d["f_segs"], d["x_blobs"], d["f_blobs"]
         s = make_solver(xs.shape[0], xb.shape[0], int(d["nseg"]), precision=precision,
                         a_seg=float(d["a_seg"]), a_blob=float(d["a_blob"]))
-        for var in range(num_tile_variants(precision)):
+        for var in range(max(num_tile_variants(precision), nq)):
             for cps in (1, 3):
                 for combo in range(6):
-                    s.set_tuning(combo, var, cps)
+                    s.set_tuning(combo, var % num_tile_variants(precision), cps)
+                for kind in range(len(QUEUE_KINDS)):
+                    s.set_queue_variant(kind, var % nq)
                 out = run_blocks(s, xs, fs, xb, fb)
                 s.apply_grand_mobility()
                 s.copy_segment_velocities_to_host()
@@ -362,7 +367,9 @@ def test_autotune_table_and_parity():
     s.set_state(xs, fs, xb, fb)
     table = s.autotune(reps=1)
     assert set(table) == {"fp64", "fp32c"}
-    assert "seg<-seg" in table["fp64"] and table["fp64"]["seg<-seg"]["ms"] > 0
+    for p in ("fp64", "fp32c"):
+        for k in ("queue seg<-seg", "queue grand", "queue seg,blob<-seg", "blob<-blob"):
+            assert table[p][k]["ms"] > 0, (p, k)
     out = run_blocks(s, xs, fs, xb, fb)
     s.finalise()
     assert rel_max(out["v_mss"], d["v_mss"]) < TOL64

@@ -134,6 +134,8 @@ _SIGNATURES = {
                                  ctypes.POINTER(ctypes.c_size_t)],
     "tfs_solver_set_tuning": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int],
     "tfs_num_tile_variants": [ctypes.c_int],
+    "tfs_solver_set_queue_variant": [_H, ctypes.c_int, ctypes.c_int, ctypes.c_int],
+    "tfs_num_queue_variants": [ctypes.c_int],
     "tfs_flow_create": [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                         ctypes.POINTER(_H)],
     "tfs_flow_destroy": [_H],

@@ -175,15 +175,19 @@ __global__ void __launch_bounds__(BLOCK) flow_kernel(const FlowArgs a) {
 
 template <typename T, bool WALL, int BLOCK, int TPT, int TS>
 cudaError_t flow_launch_fn(const FlowArgs &a, dim3 grid, cudaStream_t st, int *resident) {
-  static std::atomic<int> occupancy{0};  // set once; host threads may race to set it
+  static std::atomic<int> occupancy[kMaxDevices];  // set once per device; threads may race
   auto kern = flow_kernel<T, WALL, BLOCK, TPT, TS>;
-  if (occupancy.load() == 0) {
+  int dev = 0;
+  cudaError_t e0 = cudaGetDevice(&dev);
+  if (e0 != cudaSuccess) return e0;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (occupancy[dev].load() == 0) {
     int occ = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, BLOCK, 0);
     if (e != cudaSuccess) return e;
-    occupancy.store(occ < 1 ? 1 : occ);
+    occupancy[dev].store(occ < 1 ? 1 : occ);
   }
-  if (resident) *resident = occupancy.load();
+  if (resident) *resident = occupancy[dev].load();
   if (grid.x == 0) return cudaSuccess;  // query only
   kern<<<grid, BLOCK, 0, st>>>(a);
   return cudaGetLastError();

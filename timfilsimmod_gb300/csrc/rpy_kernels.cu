@@ -308,16 +308,19 @@ __global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
 // ---------------------------------------------------------------------------
 // Host-side launchers
 // ---------------------------------------------------------------------------
-static std::atomic<int> g_num_sms{0};  // set once; host threads may race to set it
+// SM count of each device, set once per device; host threads may race to set it.
+static std::atomic<int> g_num_sms[kMaxDevices];
 
 int num_sms() {
-  if (g_num_sms.load() == 0) {
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= kMaxDevices) dev = 0;
+  if (g_num_sms[dev].load() == 0) {
+    int n = 0;
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    g_num_sms.store(n > 0 ? n : 1);
+    g_num_sms[dev].store(n > 0 ? n : 1);
   }
-  return g_num_sms.load();
+  return g_num_sms[dev].load();
 }
 
 cudaError_t launch_reduce_partials(double *out, const double *partial, int n_elems, int splits,

@@ -143,11 +143,15 @@ __device__ __forceinline__ void near_pass(T (&v)[TPT][VD], const T (&xt)[TPT], c
 // those pairs with the exact three-regime formula (near_pass). In the swimmer
 // configurations only the tiles that hold a target's own particle or a
 // touching neighbour flag anything.
+//
+// compute = false (warp-uniform): the warp has no target of its own and only
+// helps stage the tiles.
 template <typename T, int VD, int FD, int BLOCK, int TPT, int TS>
 __device__ __forceinline__ void sum_source_range(T (&v)[TPT][VD], const T (&xt)[TPT],
                                                  const T (&yt)[TPT], const T (&zt)[TPT],
                                                  const T *__restrict__ rec, int lo, int hi,
-                                                 const PairConst<T> &pc, T *smem, float *hl) {
+                                                 const PairConst<T> &pc, T *smem, float *hl,
+                                                 bool compute = true) {
   static_assert(TS <= 256, "near-pair indices are 8-bit");
   constexpr int L = Rec<T, FD>::len;
   constexpr int VEC_PER_REC = L * (int)sizeof(T) / 16;
@@ -159,6 +163,7 @@ __device__ __forceinline__ void sum_source_range(T (&v)[TPT][VD], const T (&xt)[
     const int nvec = cnt * VEC_PER_REC;
     for (int q = threadIdx.x; q < nvec; q += BLOCK) dst[q] = __ldg(src + q);
     __syncthreads();
+    if (!compute) continue;
     unsigned nf[TPT];
 #pragma unroll
     for (int t = 0; t < TPT; ++t) nf[t] = 0u;
@@ -283,17 +288,23 @@ constexpr size_t tile_smem_bytes() {
 template <typename T, int VD, int FDA, int FDB, int BLOCK, int TPT, int TS, int MINB>
 cudaError_t tile_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st, int *resident) {
   constexpr size_t smem = tile_smem_bytes<T, VD, FDA, FDB, BLOCK, TPT, TS>();
-  static std::atomic<int> occupancy{0};  // set once; host threads may race to set it
+  // set once per device (the shared-memory attribute is per device too);
+  // host threads may race to set it
+  static std::atomic<int> occupancy[kMaxDevices];
   auto kern = rpy_tile_kernel<T, VD, FDA, FDB, BLOCK, TPT, TS, MINB>;
-  if (occupancy.load() == 0) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (occupancy[dev].load() == 0) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int occ = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, BLOCK, smem);
     if (e != cudaSuccess) return e;
-    occupancy.store(occ < 1 ? 1 : occ);
+    occupancy[dev].store(occ < 1 ? 1 : occ);
   }
-  if (resident) *resident = occupancy.load();
+  if (resident) *resident = occupancy[dev].load();
   if (grid.x == 0) return cudaSuccess;  // query only
   kern<<<grid, BLOCK, smem, st>>>(a);
   return cudaGetLastError();

@@ -277,17 +277,21 @@ constexpr size_t tile_x2_smem_bytes() {
 template <int VD, int FDA, int FDB, int BLOCK, int TPT, int TS>
 cudaError_t tile_x2_launch_fn(const TileArgs &a, dim3 grid, cudaStream_t st, int *resident) {
   constexpr size_t smem = tile_x2_smem_bytes<VD, FDA, FDB, BLOCK, TPT, TS>();
-  static std::atomic<int> occupancy{0};  // set once; host threads may race to set it
+  static std::atomic<int> occupancy[kMaxDevices];  // set once per device; threads may race
   auto kern = rpy_tile_x2_kernel<VD, FDA, FDB, BLOCK, TPT, TS>;
-  if (occupancy.load() == 0) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (occupancy[dev].load() == 0) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int occ = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, BLOCK, smem);
     if (e != cudaSuccess) return e;
-    occupancy.store(occ < 1 ? 1 : occ);
+    occupancy[dev].store(occ < 1 ? 1 : occ);
   }
-  if (resident) *resident = occupancy.load();
+  if (resident) *resident = occupancy[dev].load();
   if (grid.x == 0) return cudaSuccess;  // query only
   kern<<<grid, BLOCK, smem, st>>>(a);
   return cudaGetLastError();

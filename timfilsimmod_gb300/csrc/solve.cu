@@ -832,9 +832,14 @@ int tfs_compute_velocities(tfs_solver *s, double *swimmer_f, int *gmres_iters) {
   std::memcpy(s->f6_host, swimmer_f, 8 * 6);
   TFS_CUDA(cudaMemcpyAsync(s->swimmer_f, s->f6_host, 8 * 6, cudaMemcpyHostToDevice, s->stream),
            "copy swimmer force");
-  // v_segs = Mss f_segs, v_blobs = Mbs f_segs
-  if ((rc = tfs_evaluate_segment_segment_mobility(s)) != TFS_OK) return rc;
-  if ((rc = tfs_evaluate_blob_segment_mobility(s)) != TFS_OK) return rc;
+  // v_segs = Mss f_segs, v_blobs = Mbs f_segs (one work-queue launch when
+  // both target sets exist)
+  if (s->ns > 0 && s->nb > 0) {
+    if ((rc = queue_product(s, QK_SEGSRC)) != TFS_OK) return rc;
+  } else {
+    if ((rc = tfs_evaluate_segment_segment_mobility(s)) != TFS_OK) return rc;
+    if ((rc = tfs_evaluate_blob_segment_mobility(s)) != TFS_OK) return rc;
+  }
   const GmresArgs ga = gmres_args(s, s->rhs, s->f_blobs, s->v_bodies, s->gst, s->tol, 0);
   cudaError_t e = launch_rhs(ga, s->f_rep, s->v_blobs, s->swimmer_f, s->rhs, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "right-hand side");

@@ -21,6 +21,8 @@
 
 namespace tfs {
 
+static constexpr double kPiHost = 3.14159265358979323846264338327950288;
+
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void count_launch_n(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -31,6 +33,8 @@ static thread_local std::string g_last_error;
 // Process-wide tuning results: (precision, combination, Ns, Nb) -> tuning, so
 // solvers created after an autotune of the same sizes start tuned.
 static std::mutex g_tune_mutex;
+// queue kinds are cached under kQueueTuneKey + kind
+static constexpr int kQueueTuneKey = 100;
 static std::map<std::tuple<int, int, int, int>, TileTuning> g_tune_cache;
 
 void tune_cache_store(int precision, int combo, int ns, int nb, TileTuning t) {
@@ -104,6 +108,8 @@ static void free_all(tfs_solver *s) {
   cudaFree(s->wc_z);
   cudaFree(s->wc_f);
   cudaFree(s->scratch);
+  cudaFree(s->qjobs_dev);
+  cudaFree(s->qcount);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
@@ -151,50 +157,117 @@ TileArgs tfs::base_args(tfs_solver *s) {
   return a;
 }
 
-// Product of one block or fused pair of blocks into `out`.
-int tfs::product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mode) {
-  int rc;
-  if (s->cfg.precision == TFS_FP32C && (rc = ensure_origin(s)) != TFS_OK) return rc;
-  if (src_segs && (rc = pack(s, 1)) != TFS_OK) return rc;
-  if (src_blobs && (rc = pack(s, 0)) != TFS_OK) return rc;
-  TileArgs a = base_args(s);
-  a.x_tgt = tgt_segs ? s->x_segs : s->x_blobs;
-  a.n_tgt = tgt_segs ? s->ns : s->nb;
-  a.a_tgt = tgt_segs ? s->cfg.a_seg : s->cfg.a_blob;
-  a.out = tgt_segs ? s->v_segs : s->v_blobs;
-  int fda, fdb = 0;
+// ---------------------------------------------------------------------------
+// Work-queue products: the solver's job lists and one launch per product.
+// ---------------------------------------------------------------------------
+static QueueJob make_job(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mode) {
+  QueueJob j{};
+  j.tgt_rec = tgt_segs ? s->rec_segs : s->rec_blobs;
+  j.n_tgt = tgt_segs ? s->ns : s->nb;
+  j.a_tgt = tgt_segs ? s->cfg.a_seg : s->cfg.a_blob;
+  j.out = tgt_segs ? s->v_segs : s->v_blobs;
+  j.vd = tgt_segs ? 6 : 3;
+  j.mode = mode;
+  j.scale = 1.0 / (8.0 * kPiHost * s->cfg.mu);
   if (src_segs) {
-    a.src_a = s->rec_segs;
-    a.src_a2 = s->rec_segs_x2;
-    a.n_a = s->ns;
-    a.a_a = s->cfg.a_seg;
-    fda = 6;
+    j.src_a = s->rec_segs;
+    j.n_a = s->ns;
+    j.a_a = s->cfg.a_seg;
     if (src_blobs) {
-      a.src_b = s->rec_blobs;
-      a.src_b2 = s->rec_blobs_x2;
-      a.n_b = s->nb;
-      a.a_b = s->cfg.a_blob;
-      fdb = 3;
+      j.src_b = s->rec_blobs;
+      j.n_b = s->nb;
+      j.a_b = s->cfg.a_blob;
     }
   } else {
-    a.src_a = s->rec_blobs;
-    a.src_a2 = s->rec_blobs_x2;
-    a.n_a = s->nb;
-    a.a_a = s->cfg.a_blob;
-    fda = 3;
+    j.src_a = s->rec_blobs;
+    j.n_a = s->nb;
+    j.a_a = s->cfg.a_blob;
   }
-  if (a.n_tgt == 0) return TFS_OK;
-  if (a.n_a + a.n_b == 0) {
+  // the pair constants exactly as the tile kernel forms them (in FP64, then
+  // rounded to the kernel's precision)
+  for (int set = 0; set < 2; ++set) {
+    const double ai = j.a_tgt, aj = set == 0 ? j.a_a : j.a_b;
+    const double q[5] = {ai, aj, (ai + aj) * (ai + aj), (ai * ai + aj * aj) / 3.0,
+                         -(ai * ai + aj * aj)};
+    for (int k = 0; k < 5; ++k) {
+      j.pc64[set][k] = q[k];
+      j.pc32[set][k] = (float)q[k];
+    }
+  }
+  queue_chunking(j.n_a + j.n_b, s->ns + s->nb, &j.chunk, &j.n_chunks);
+  // segment-target and blob-target jobs of one launch use disjoint partials
+  // and arrival counters
+  j.partial = s->scratch + (tgt_segs ? (size_t)0 : (size_t)kMaxSplits * 6 * s->ns);
+  j.block_done = s->qcount + 2 + (tgt_segs ? 0 : (s->ns + 31) / 32);
+  return j;
+}
+
+static void add_job(tfs_solver *s, int kind, bool tgt_segs, bool src_segs, bool src_blobs,
+                    int mode) {
+  const QueueJob j = make_job(s, tgt_segs, src_segs, src_blobs, mode);
+  if (j.n_tgt > 0 && j.n_a + j.n_b > 0) s->qjobs[kind][s->qjobs_n[kind]++] = j;
+}
+
+// Job lists of every launch kind (segment-target jobs first: their pairs cost
+// more), copied to the device once.
+static int build_queue_jobs(tfs_solver *s) {
+  for (int k = 0; k < kNumQueueKinds; ++k) s->qjobs_n[k] = 0;
+  add_job(s, QK_MSS, true, true, false, OUT_ASSIGN);
+  add_job(s, QK_MBS, false, true, false, OUT_ASSIGN);
+  add_job(s, QK_SEGSRC, true, true, false, OUT_ASSIGN);
+  add_job(s, QK_SEGSRC, false, true, false, OUT_ASSIGN);
+  add_job(s, QK_MSB, true, false, true, OUT_ACCUMULATE);
+  add_job(s, QK_MBB, false, false, true, OUT_ASSIGN);
+  add_job(s, QK_GRAND, true, true, true, OUT_ASSIGN);
+  add_job(s, QK_GRAND, false, true, true, OUT_ASSIGN);
+  TFS_CUDA(cudaMemcpy(s->qjobs_dev, s->qjobs, sizeof s->qjobs, cudaMemcpyHostToDevice),
+           "copy queue jobs");
+  return TFS_OK;
+}
+
+static int queue_sources(int kind) {
+  return kind == QK_GRAND ? Q_SEG_BLOB : (kind == QK_MSB || kind == QK_MBB) ? Q_BLOB : Q_SEG;
+}
+
+int tfs::queue_product(tfs_solver *s, int kind) {
+  const int fp32 = s->cfg.precision == TFS_FP32C;
+  const int src = queue_sources(kind);
+  int rc;
+  if (fp32 && (rc = ensure_origin(s)) != TFS_OK) return rc;
+  // the records of both particle kinds: sources, and the targets' positions
+  cudaError_t e;
+  if (s->ns > 0) {
+    e = launch_pack(fp32, 6, s->rec_segs, s->x_segs, s->f_segs, s->ns, s->origin, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "pack kernel");
+  }
+  if (s->nb > 0) {
+    e = launch_pack(fp32, 3, s->rec_blobs, s->x_blobs, s->f_blobs, s->nb, s->origin, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "pack kernel");
+  }
+  e = launch_queue(fp32, s->qtune[fp32][kind], src, s->qjobs_dev + 2 * kind, s->qjobs[kind],
+                   s->qjobs_n[kind], s->qcount, s->stream, next_events(s));
+  if (e != cudaSuccess) return cuda_fail(e, "RPY work-queue kernel");
+  return TFS_OK;
+}
+
+// Product of one block into `out` (assign or accumulate).
+int tfs::product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mode) {
+  int rc;
+  if (src_segs == src_blobs) return fail(TFS_EINVAL, "one source set per block product");
+  const int n_tgt = tgt_segs ? s->ns : s->nb;
+  const int n_src = src_segs ? s->ns : s->nb;
+  if (n_tgt == 0) return TFS_OK;
+  if (n_src == 0) {
     if (mode == OUT_ASSIGN)
-      TFS_CUDA(cudaMemsetAsync(a.out, 0, sizeof(double) * (tgt_segs ? 6 : 3) * a.n_tgt, s->stream),
+      TFS_CUDA(cudaMemsetAsync(tgt_segs ? s->v_segs : s->v_blobs, 0,
+                               sizeof(double) * (tgt_segs ? 6 : 3) * n_tgt, s->stream),
                "cudaMemsetAsync");
     return TFS_OK;
   }
-  const int combo = combo_of(tgt_segs ? 6 : 3, fda, fdb);
-  const TileTuning tune = s->tune[s->cfg.precision == TFS_FP32C][combo];
-  cudaError_t e = launch_tile(a, tgt_segs ? 6 : 3, fda, fdb, tune, s->scratch, s->scratch_elems,
-                              mode, s->stream, next_events(s));
-  if (e != cudaSuccess) return cuda_fail(e, "RPY tile kernel");
+  const int kind = tgt_segs ? (src_segs ? QK_MSS : QK_MSB) : (src_segs ? QK_MBS : QK_MBB);
+  if ((kind == QK_MSB) != (mode == OUT_ACCUMULATE))
+    return fail(TFS_EINVAL, "M_sb accumulates, the other blocks assign");
+  if ((rc = queue_product(s, kind)) != TFS_OK) return rc;
   return TFS_OK;
 }
 
@@ -238,11 +311,17 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
   tfs_solver *s = new (std::nothrow) tfs_solver;
   if (s == nullptr) return fail(TFS_ENOMEM, "host allocation failed");
   s->cfg = *cfg;
-  for (int p = 0; p < 2; ++p)
+  for (int p = 0; p < 2; ++p) {
     for (int c = 0; c < kNumCombos; ++c) {
       s->tune[p][c] = TileTuning{0, 1};
       tune_cache_lookup(p, c, (int)ns, (int)nb, &s->tune[p][c]);
     }
+    for (int k = 0; k < kNumQueueKinds; ++k) {
+      TileTuning t{0, 1};
+      tune_cache_lookup(p, kQueueTuneKey + k, (int)ns, (int)nb, &t);
+      s->qtune[p][k] = t.variant;
+    }
+  }
   s->ns = (int)ns;
   s->nb = (int)nb;
   cudaGetDevice(&s->device);
@@ -254,7 +333,10 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
   }
   s->stream = s->own_stream;
   const size_t dsz = sizeof(double);
-  s->scratch_elems = (size_t)kMaxSplits * (size_t)std::max(6 * ns, 3 * nb);
+  // split partials: tile launches need kMaxSplits x the larger target set,
+  // a queue launch up to kMaxSplits chunks of both target sets at once
+  s->scratch_elems = (size_t)kMaxSplits * (size_t)(6 * ns + 3 * nb);
+  const size_t qcount_elems = 2 + (size_t)(ns + 31) / 32 + (size_t)(nb + 31) / 32;
   if ((rc = alloc_dev((void **)&s->x_segs, dsz * 3 * ns)) ||
       (rc = alloc_dev((void **)&s->f_segs, dsz * 6 * ns)) ||
       (rc = alloc_dev((void **)&s->v_segs, dsz * 6 * ns)) ||
@@ -271,6 +353,8 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
       (rc = alloc_dev(&s->rec_ff, ff_record_bytes() * nb)) ||
       (rc = alloc_dev((void **)&s->tile_boxes, sizeof(float) * 6 * ((ns + nb + 127) / 128 + 1))) ||
       (rc = alloc_dev((void **)&s->scratch, dsz * s->scratch_elems)) ||
+      (rc = alloc_dev((void **)&s->qjobs_dev, sizeof s->qjobs)) ||
+      (rc = alloc_dev((void **)&s->qcount, sizeof(unsigned) * qcount_elems)) ||
       (rc = solve_alloc(s))) {
     free_all(s);
     delete s;
@@ -291,7 +375,13 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
   cudaMemsetAsync(s->f_rep, 0, dsz * 3 * nb, s->stream);
   cudaMemsetAsync(s->origin, 0, dsz * origin_elems(), s->stream);
   cudaMemsetAsync(s->origin_cnt, 0, 2 * sizeof(unsigned), s->stream);
+  cudaMemsetAsync(s->qcount, 0, sizeof(unsigned) * qcount_elems, s->stream);
   e = cudaStreamSynchronize(s->stream);
+  if (e == cudaSuccess && (rc = build_queue_jobs(s)) != TFS_OK) {
+    free_all(s);
+    delete s;
+    return rc;
+  }
   if (e != cudaSuccess) {
     free_all(s);
     delete s;
@@ -484,35 +574,10 @@ int tfs_evaluate_full_mobility(tfs_solver *s, double *v_segs_host, double *v_blo
 
 int tfs_apply_grand_mobility(tfs_solver *s) {
   TFS_CHECK_SOLVER(s);
-  int rc;
-  if (s->ns > 0 && (rc = product(s, true, true, s->nb > 0, OUT_ASSIGN)) != TFS_OK) return rc;
-  if (s->nb > 0) {
-    if (s->ns > 0) {
-      // blob targets: segment sources (set A) then blob sources (set B);
-      // both record arrays are already packed.
-      int r2;
-      if (s->cfg.precision == TFS_FP32C && (r2 = ensure_origin(s)) != TFS_OK) return r2;
-      TileArgs a = base_args(s);
-      a.x_tgt = s->x_blobs;
-      a.n_tgt = s->nb;
-      a.a_tgt = s->cfg.a_blob;
-      a.out = s->v_blobs;
-      a.src_a = s->rec_segs;
-      a.src_a2 = s->rec_segs_x2;
-      a.n_a = s->ns;
-      a.a_a = s->cfg.a_seg;
-      a.src_b = s->rec_blobs;
-      a.src_b2 = s->rec_blobs_x2;
-      a.n_b = s->nb;
-      a.a_b = s->cfg.a_blob;
-      const TileTuning tune = s->tune[s->cfg.precision == TFS_FP32C][C_BX];
-      cudaError_t e = launch_tile(a, 3, 6, 3, tune, s->scratch, s->scratch_elems, OUT_ASSIGN,
-                                  s->stream, next_events(s));
-      if (e != cudaSuccess) return cuda_fail(e, "RPY tile kernel");
-    } else if ((rc = product(s, false, false, true, OUT_ASSIGN)) != TFS_OK) {
-      return rc;
-    }
-  }
+  // both target kinds against both source sets in one work-queue launch
+  if (s->ns > 0 && s->nb > 0) return queue_product(s, QK_GRAND);
+  if (s->ns > 0) return product(s, true, true, false, OUT_ASSIGN);
+  if (s->nb > 0) return product(s, false, false, true, OUT_ASSIGN);
   return TFS_OK;
 }
 
@@ -537,6 +602,12 @@ int tfs_solver_kernel_timing(tfs_solver *s, double *ms, int capacity, int *launc
   *launches = n;
   s->events_used = 0;
   return TFS_OK;
+}
+
+static const char *queue_kind_name(int k) {
+  static const char *names[kNumQueueKinds] = {"seg<-seg", "blob<-seg", "seg,blob<-seg",
+                                              "seg<-blob", "blob<-blob", "grand"};
+  return names[k];
 }
 
 static const char *combo_name(int c) {
@@ -568,7 +639,9 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
     if (report.size() > 1) report += ",";
     report += std::string("\"") + (p ? "fp32c" : "fp64") + "\":{";
     bool first_combo = true;
-    for (int c = 0; c < kNumCombos && rc == TFS_OK; ++c) {
+    // tile launches serve only the blob-blob product of the kernel-sequence
+    // GMRES now; every other product goes through the work queue (below)
+    for (int c = C_BB; c == C_BB && rc == TFS_OK; ++c) {
       const bool tgt_segs = (c == C_SS || c == C_SB || c == C_SX);
       const bool src_segs = (c != C_SB && c != C_BB);
       const bool src_blobs = (c == C_SB || c == C_BB || c == C_SX || c == C_BX);
@@ -645,6 +718,56 @@ int tfs_solver_autotune(tfs_solver *s, int precision_mask, int reps) {
       report += cands + "]}";
       first_combo = false;
     }
+    // work-queue launches: every variant of every kind the solver has
+    for (int k = 0; k < kNumQueueKinds && rc == TFS_OK; ++k) {
+      if (s->qjobs_n[k] == 0) continue;
+      const int nvar = p ? kNumQueueVariantsF32 : kNumQueueVariantsF64;
+      const int src = queue_sources(k);
+      float best_ms = 1e30f;
+      int best = 0;
+      std::string cands;
+      for (int v = 0; v < nvar && rc == TFS_OK; ++v) {
+        cudaError_t e = launch_queue(p, v, src, s->qjobs_dev + 2 * k, s->qjobs[k], s->qjobs_n[k],
+                                     s->qcount, s->stream);  // warm-up
+        float ms = 1e30f;
+        for (int trial = 0; trial < 3 && e == cudaSuccess; ++trial) {
+          cudaEventRecord(e0, s->stream);
+          for (int r = 0; r < reps && e == cudaSuccess; ++r)
+            e = launch_queue(p, v, src, s->qjobs_dev + 2 * k, s->qjobs[k], s->qjobs_n[k],
+                             s->qcount, s->stream);
+          cudaEventRecord(e1, s->stream);
+          if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+          float tm = 0.f;
+          if (e == cudaSuccess) cudaEventElapsedTime(&tm, e0, e1);
+          ms = std::min(ms, tm / reps);
+        }
+        if (e != cudaSuccess) {
+          rc = cuda_fail(e, "autotune queue launch");
+          break;
+        }
+        const QueueVariant qv = p ? g_qvariants_f32[v] : g_qvariants_f64[v];
+        char buf[96];
+        snprintf(buf, sizeof buf, "%s[%d,%d,%d,0,0,%.4f]", cands.empty() ? "" : ",", qv.block,
+                 qv.tpt, qv.ts, ms);
+        cands += buf;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = v;
+        }
+      }
+      if (rc != TFS_OK) break;
+      s->qtune[p][k] = best;
+      tune_cache_store(p, kQueueTuneKey + k, s->ns, s->nb, TileTuning{best, 1});
+      const QueueVariant bq = p ? g_qvariants_f32[best] : g_qvariants_f64[best];
+      char buf[256];
+      snprintf(buf, sizeof buf,
+               "%s\"queue %s\":{\"block\":%d,\"tpt\":%d,\"ts\":%d,\"x2\":0,\"waves\":0,"
+               "\"ms\":%.4f,\"candidates\":[",
+               first_combo ? "" : ",", queue_kind_name(k), bq.block, bq.tpt, bq.ts, best_ms);
+      report += buf;
+      report += cands + "]}";
+      first_combo = false;
+    }
     report += "}";
   }
   report += "}";
@@ -666,6 +789,21 @@ int tfs_solver_set_tuning(tfs_solver *s, int precision, int combo, int variant, 
   if (waves < 1 || waves > 64) return fail(TFS_EINVAL, "waves out of range");
   s->tune[precision][combo] = TileTuning{variant, waves};
   return TFS_OK;
+}
+
+int tfs_solver_set_queue_variant(tfs_solver *s, int precision, int kind, int variant) {
+  TFS_CHECK_SOLVER(s);
+  if (precision != TFS_FP64 && precision != TFS_FP32C)
+    return fail(TFS_EINVAL, "unknown precision %d", precision);
+  if (kind < 0 || kind >= kNumQueueKinds) return fail(TFS_EINVAL, "kind %d out of range", kind);
+  if (variant < 0 || variant >= tfs_num_queue_variants(precision))
+    return fail(TFS_EINVAL, "variant %d out of range", variant);
+  s->qtune[precision][kind] = variant;
+  return TFS_OK;
+}
+
+int tfs_num_queue_variants(int precision) {
+  return precision == TFS_FP32C ? kNumQueueVariantsF32 : kNumQueueVariantsF64;
 }
 
 int tfs_num_tile_variants(int precision) {
@@ -697,7 +835,7 @@ namespace tfs {
 size_t solver_bytes_estimate(const tfs_config *cfg) {
   const size_t ns = (size_t)cfg->nswim * cfg->nfil * cfg->nseg, nb = (size_t)cfg->nswim * cfg->nblob;
   const size_t n = 3 * nb + 6, m = std::min<size_t>(350, n);
-  const size_t doubles = 15 * ns + 12 * nb + (size_t)kMaxSplits * std::max(6 * ns, 3 * nb) +
+  const size_t doubles = 15 * ns + 12 * nb + (size_t)kMaxSplits * (6 * ns + 3 * nb) +
                          n * (m + 1) + (m + 1) * (m + 1) + 16 * n + 57 * nb + 256 * (m + 1);
   return 8 * doubles + 200 * ns + 200 * nb + ((size_t)1 << 20);
 }

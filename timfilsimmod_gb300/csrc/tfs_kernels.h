@@ -11,6 +11,8 @@ enum OutMode { OUT_ASSIGN = 0, OUT_ACCUMULATE = 1, OUT_PARTIAL = 2 };
 
 // Upper bound on source splits of one product (sizes the scratch buffer).
 constexpr int kMaxSplits = 64;
+// Devices whose per-kernel occupancy is cached.
+constexpr int kMaxDevices = 64;
 
 struct TileArgs {
   const double *x_tgt;  // target positions, AoS float64 [3*n_tgt]
@@ -75,6 +77,75 @@ extern const TileVariant g_variants_f64[kNumVariantsF64];
 extern const TileFn g_tile_f32[kNumVariantsF32Scalar][kNumCombos];
 extern const TileFn g_tile_f32x2[kNumVariantsF32X2][kNumCombos];
 extern const TileFn g_tile_f64[kNumVariantsF64][kNumCombos];
+
+// ---------------------------------------------------------------------------
+// Work-queue products (rpy_queue.cuh): one persistent launch over any number
+// of jobs, each a target set against one or two packed source sets.
+// ---------------------------------------------------------------------------
+struct QueueJob {
+  const void *tgt_rec;     // packed records of the targets (their positions are read)
+  const void *src_a;       // packed source records, set A
+  const void *src_b;       // packed source records, set B (or null)
+  double *out;             // velocities, AoS float64 [vd n_tgt]
+  void *partial;           // [n_chunks][n_tgt][vd] chunk sums, float2 (hi, lo) for FP32 and
+                           // double for FP64 (8 B either way; unused when n_chunks == 1)
+  unsigned *block_done;    // one arrival counter per target block (zero between launches)
+  const int *skip;         // device flag: the job does nothing when *skip != 0 (or null)
+  double a_tgt, a_a, a_b;  // radii
+  double scale;            // 1 / (8 pi mu)
+  // pair constants of (target, set A) and (target, set B), in both precisions:
+  // {a_tgt, a_src, (a_tgt + a_src)^2, (a_tgt^2 + a_src^2)/3, -(a_tgt^2 + a_src^2)}
+  double pc64[2][5];
+  float pc32[2][5];
+  int n_tgt, n_a, n_b;
+  int vd;                  // 6 (segment targets) or 3 (blob targets)
+  int mode;                // OUT_ASSIGN or OUT_ACCUMULATE
+  int chunk, n_chunks;     // sources per unit (a multiple of kQueueQuantum), chunks
+  int pad;
+};
+struct QueueArgs {
+  const QueueJob *jobs;    // device array, costliest pairs first
+  int n_jobs;
+  unsigned *counters;      // [2]: units handed out, CTAs finished (zero between launches)
+};
+// Source sets of a queue launch (every job of one launch has the same).
+enum QueueSources { Q_SEG = 0, Q_BLOB = 1, Q_SEG_BLOB = 2 };
+constexpr int kNumQueueSources = 3;
+struct QueueVariant {
+  int block, tpt, ts, min_blocks;
+};
+constexpr int kNumQueueVariantsF32 = 5;
+constexpr int kNumQueueVariantsF64 = 3;
+typedef cudaError_t (*QueueFn)(const QueueArgs &, int ctas, cudaStream_t, int *resident);
+extern const QueueVariant g_qvariants_f32[kNumQueueVariantsF32];
+extern const QueueVariant g_qvariants_f64[kNumQueueVariantsF64];
+extern const QueueFn g_queue_f32[kNumQueueVariantsF32][kNumQueueSources];
+extern const QueueFn g_queue_f64[kNumQueueVariantsF64][kNumQueueSources];
+// Chunks are whole multiples of this many sources (every variant's tile
+// size divides it).
+constexpr int kQueueQuantum = 256;
+// Largest number of jobs one launch may carry (the kernel keeps their unit
+// offsets in shared memory).
+constexpr int kQueueMaxJobs = 256;
+// Source chunking of a job with n_src sources in a system of n_particles
+// target particles: about 8192 units of 128 targets over the system, at
+// most kMaxSplits chunks. A function of the sizes alone, so a product is
+// split the same way whatever launch carries it.
+void queue_chunking(int n_src, int n_particles, int *chunk, int *n_chunks);
+// Launch the queue kernel of (precision, variant, sources) over the jobs
+// (device array `jobs`; `jobs_host` is the same array on the host, used to
+// size the grid). counters: [2] zeroed unsigned. ev (optional): events
+// recorded around the launch.
+cudaError_t launch_queue(int fp32, int variant, int sources, const QueueJob *jobs,
+                         const QueueJob *jobs_host, int n_jobs, unsigned *counters,
+                         cudaStream_t st, cudaEvent_t *ev = nullptr);
+// Work units of the jobs for a variant's target block (BLOCK * TPT targets).
+long long queue_units(const QueueJob *jobs_host, int n_jobs, int block_targets);
+// The products a solver launches through the queue: M_ss, M_bs, both at once
+// (segment sources, two jobs), M_sb (accumulating), M_bb, and the grand
+// mobility (all sources, both target kinds: two jobs).
+enum QueueKind { QK_MSS = 0, QK_MBS = 1, QK_SEGSRC = 2, QK_MSB = 3, QK_MBB = 4, QK_GRAND = 5 };
+constexpr int kNumQueueKinds = 6;
 
 // Tuning of one launch: variant and the number of full waves (resident CTAs
 // on every SM) the source splitting aims for.

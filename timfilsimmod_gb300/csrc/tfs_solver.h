@@ -82,6 +82,15 @@ struct tfs_solver {
   double *f6_host = nullptr;              // pinned 6
   int last_iters = 0, last_outer = 0;
   double last_rel = 0.0;
+  // work-queue products (rpy_queue.cuh): the job list of each launch kind,
+  // built once at creation (host copy and device copy), the launch counters
+  // and per-target-block arrival counters, and the tuned variant per
+  // (precision, kind)
+  tfs::QueueJob qjobs[tfs::kNumQueueKinds][2];
+  int qjobs_n[tfs::kNumQueueKinds] = {};
+  tfs::QueueJob *qjobs_dev = nullptr;  // [kNumQueueKinds][2]
+  unsigned *qcount = nullptr;          // [2] launch counters, then arrival counters
+  int qtune[2][tfs::kNumQueueKinds] = {};
   // launch tuning per precision and (target, source-set) combination
   tfs::TileTuning tune[2][tfs::kNumCombos];
   std::string tuning_report = "{}";
@@ -120,6 +129,8 @@ int ensure_origin(tfs_solver *s);
 int pack(tfs_solver *s, int segs);
 TileArgs base_args(tfs_solver *s);
 int product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mode);
+// One work-queue launch of the given kind (QueueKind) on the solver's stream.
+int queue_product(tfs_solver *s, int kind);
 int alloc_dev(void **p, size_t bytes);
 int solve_alloc(tfs_solver *s);
 void solve_free(tfs_solver *s);

@@ -140,15 +140,16 @@ class RpyMobilitySolver:
         self._call("tfs_solver_enable_kernel_timing", int(bool(enable)))
 
     def kernel_timing(self) -> list[float]:
-        """Durations (ms) of the RPY tile-kernel launches since the last call,
-        in launch order."""
+        """Durations (ms) of the RPY product launches (work-queue and tile
+        kernels) since the last call, in launch order."""
         buf = (ctypes.c_double * 4096)()
         n = ctypes.c_int()
         self._call("tfs_solver_kernel_timing", buf, 4096, ctypes.byref(n))
         return list(buf[:min(n.value, 4096)])
 
     def autotune(self, precisions=("fp64", "fp32c"), reps: int = 2) -> dict:
-        """Pick the fastest tile-kernel launch variant per block for this
+        """Pick the fastest work-queue variant per product kind (and tile
+        variant for the kernel-sequence GMRES's blob-blob product) for this
         solver's sizes (on its current data); returns the tuning table."""
         import json
 
@@ -161,6 +162,12 @@ class RpyMobilitySolver:
         """Pin the tile-kernel launch of one (target, source-set) combination."""
         prec = PRECISIONS[precision or self.precision]
         self._call("tfs_solver_set_tuning", prec, int(combo), int(variant), int(waves))
+
+    def set_queue_variant(self, kind: int, variant: int, precision: str | None = None) -> None:
+        """Pin the work-queue variant of one product kind (0..5: M_ss, M_bs,
+        M_ss with M_bs, M_sb, M_bb, grand mobility)."""
+        prec = PRECISIONS[precision or self.precision]
+        self._call("tfs_solver_set_queue_variant", prec, int(kind), int(variant))
 
     def tuning_report(self) -> str:
         need = ctypes.c_size_t()
@@ -339,6 +346,13 @@ def measure_fma_peak(precision: str = "fp64") -> float:
 
 def num_tile_variants(precision: str) -> int:
     return int(N.load().tfs_num_tile_variants(PRECISIONS[precision]))
+
+
+def num_queue_variants(precision: str) -> int:
+    return int(N.load().tfs_num_queue_variants(PRECISIONS[precision]))
+
+
+QUEUE_KINDS = ("seg<-seg", "blob<-seg", "seg,blob<-seg", "seg<-blob", "blob<-blob", "grand")
 
 
 def kernel_launch_count() -> int:

@@ -2,10 +2,11 @@
 
     python -m timfilsimmod_gb300.profile_case --config medium --precision fp32c --reps 2
 
-Each repetition is one tfs_apply_grand_mobility call (pack, tile and reduce
-kernels), or with --op the named block, solve, flow evaluation or implicit
-time step. Meant to be run under `ncu -k regex:rpy_tile_kernel -c N` (or
-`ncu --metrics gpu__time_duration.sum` for a launch list).
+Each repetition is one tfs_apply_grand_mobility call (the pack kernels and
+one work-queue launch), or with --op the named block, solve, flow
+evaluation or implicit time step. Meant to be run under
+`ncu -k regex:rpy_queue_kernel -c N` (or `ncu --metrics gpu__time_duration.sum`
+for a launch list).
 """
 from __future__ import annotations
 
@@ -81,6 +82,8 @@ def main():
     p.add_argument("--variant", type=int, default=None,
                    help="pin every combination to this tile-kernel variant")
     p.add_argument("--waves", type=int, default=1)
+    p.add_argument("--queue-variant", type=int, default=None,
+                   help="pin every work-queue product kind to this variant")
     p.add_argument("--autotune", action="store_true", help="print the autotuner's table")
     args = p.parse_args()
     sw = make_config(args.config, seed=1)
@@ -96,6 +99,9 @@ def main():
     if args.variant is not None:
         for combo in range(6):
             s.set_tuning(combo, args.variant, args.waves)
+    if args.queue_variant is not None:
+        for kind in range(6):
+            s.set_queue_variant(kind, args.queue_variant)
     if args.op == "solve":
         import numpy as np
 
