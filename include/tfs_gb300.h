@@ -6,7 +6,7 @@
  * pure-virtual device hooks of `mobility_solver`
  * (src/cilia/mobility/mobility_solver.hpp:26-46). Each hook has one entry
  * point here, taking an opaque solver handle; a replacement
- * rpy_mobility_solver.cu calls them one to one (INTEGRATION.md shows it).
+ * rpy_mobility_solver.cu calls them one to one.
  * Host arrays keep the reference's AoS float64 layouts
  * (rpy_mobility_solver.cu:65-71):
  *   x_segs[3*Ns]  f_segs[6*Ns] (fx,fy,fz,tx,ty,tz)  v_segs[6*Ns] (vx,vy,vz,wx,wy,wz)
@@ -466,16 +466,20 @@ int tfs_flow_wait(tfs_flow *f);
  * device arrays). For callers that cannot allocate device memory -- a driver
  * that reserves all device memory up front for its own pool, a real-time loop
  * that must not block on cudaMalloc, code running inside another framework's
- * stream capture: v_segs = M_ss f_segs in FP64 (the same arithmetic and
- * assign semantics as tfs_evaluate_segment_segment_mobility) on the caller's
+ * stream capture: v_segs = M_ss f_segs in FP64 (the assign semantics of
+ * tfs_evaluate_segment_segment_mobility, and its result to FP64 rounding:
+ * the sources are split into different chunks, so the sums are added in a
+ * different order and the two agree to ~1e-15, not bit for bit) on the caller's
  * device arrays x_segs[3n], f_segs[6n], v_segs[6n], on `stream` (a
  * cudaStream_t; NULL = the legacy default stream), asynchronously.
  * Working memory is one file-scope device array of fixed size that every GPU
  * loading this library holds until exit; it allows n <= TFS_NOALLOC_MAX_SEGS
  * (larger n returns TFS_EINVAL). The entry point calls no cudaMalloc, cudaFree
  * or other allocating routine. The first call on a device looks up the
- * array's device address there (cudaGetSymbolAddress); make that first call
- * outside any stream capture. Calls share the array: each call overwrites
+ * array's device address there (cudaGetSymbolAddress) and keeps it for the
+ * life of the process; make that first call outside any stream capture, and
+ * do not reset the device (cudaDeviceReset) after it: the kept address would
+ * then be stale. Calls share the array: each call overwrites
  * every entry it later reads, so nothing needs clearing, but two calls that
  * overlap on the GPU (different streams, no ordering) race on it. */
 #define TFS_NOALLOC_MAX_SEGS 12800
@@ -483,7 +487,8 @@ int tfs_mss_noalloc(const double *x_segs, const double *f_segs, double *v_segs, 
                     double mu, double a_seg, void *stream);
 
 /* --- diagnostics ------------------------------------------------------- */
-/* CUDA-event timing of the solver's RPY tile kernels (the dominant kernels;
+/* CUDA-event timing of the solver's RPY product launches (the work-queue
+ * kernel of each product, and the tile kernels of the kernel-sequence GMRES;
  * pack and reduce kernels excluded), on the solver's stream. Enabling resets
  * the record. tfs_solver_kernel_timing synchronises the stream, writes the
  * duration in ms of each timed launch since the last query, in launch order,

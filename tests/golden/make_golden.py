@@ -2,11 +2,12 @@
 
 The outputs come from the reference's own kernels (src/cilia/cuda_functions.cu
 and the flow_velocities kernel of src/flow_field/flow_field_evaluator.cu),
-compiled unchanged for the CPU by `make -C oracle ref` (see oracle/Makefile).
+compiled unchanged for the CPU by `make -C oracle ref REF=<reference checkout>`
+(see oracle/Makefile).
 That needs the reference tree, so this script runs only where it is present;
 the .npz files it writes are committed and travel with the tests.
 
-    make -C oracle ref && python tests/golden/make_golden.py [case ...]
+    make -C oracle ref REF=<reference checkout> && python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 

@@ -24,7 +24,11 @@ def rel_max(a, b):
     return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
 
 
-def test_noalloc_matches_solver_entry_point_twice():
+@pytest.mark.parametrize("config", ["small", "medium"])
+def test_noalloc_matches_solver_entry_point_twice(config):
+    """The small swimmer (640 segments) and the medium one (12 800 segments,
+    TFS_NOALLOC_MAX_SEGS: the record and partial-sum regions of the array
+    filled to their ends)."""
     import torch
 
     from timfilsimmod_gb300 import _native as N
@@ -32,7 +36,7 @@ def test_noalloc_matches_solver_entry_point_twice():
     from timfilsimmod_gb300.mobility import RpyMobilitySolver
 
     lib = N.load()
-    sw = make_config("small", seed=12)
+    sw = make_config(config, seed=12)
     rng = np.random.default_rng(4)
     forces = [sw.f_segs, rng.normal(size=sw.f_segs.shape)]
     dev = torch.device("cuda", 0)
@@ -61,6 +65,13 @@ def test_noalloc_matches_solver_entry_point_twice():
         print(f"call {call}: rel err {err:.2e}")
         assert err < TOL64
     solver.finalise()
+
+
+def test_noalloc_no_segments_is_ok():
+    from timfilsimmod_gb300 import _native as N
+
+    lib = N.load()
+    assert lib.tfs_mss_noalloc(None, None, None, 0, 1.0, 1.0, None) == N.TFS_OK
 
 
 def test_noalloc_rejects_oversize():
