@@ -19,9 +19,10 @@ inputs/outputs). Printed: one JSON line (rank 0).
 
   solve    compute_velocities (the free-body GMRES solve of one Broyden
            iteration) at a 1e-8 linear residual, FP64 vs FP32C refinement
-  implicit_steps  whole implicit time steps (forces, solve, residuals,
+  implicit_steps  100 whole implicit time steps (forces, solve, residuals,
            Broyden) at a 1e-8 linear residual, FP64 vs FP32C, steps/s with
-           p50/p99 per-step latency
+           p50/p99 per-step latency, the FP32C position error per step against
+           FP64 and the error of both against the reference's own trajectory
   implicit_steps_default_dt  the same at the reference's default
            DT = 36.3833/300, where every step iterates Broyden's method
   batched  64 uneven swimmers stepped together (FP32C, host worker pool)
@@ -31,6 +32,8 @@ inputs/outputs). Printed: one JSON line (rank 0).
            FP64 requests served one at a time
   flow     the flow-field evaluator on a 128^3 grid around the large swimmer
            (80 000 segments, 10 242 blobs), FP32C, with an FP64 subset
+  large    the large swimmer: grand mobility FP32C and FP64 with rooflines,
+           one mobility solve at a 1e-8 residual, FP32C implicit steps
 
 `--impl reference` times the reference's RPY sums on the host cores instead
 (the CPU restatement in oracle/, all threads), on a bounded sample of the
@@ -289,13 +292,18 @@ def bench_ours(args):
     # --- the mobility solve of one Broyden iteration (compute_velocities) -----
     solve = None if args.no_solve else solve_bench(sw, stream, args, RpyMobilitySolver)
     # --- implicit time steps (initial guess, forces, solve, Broyden) -----------
-    steps = None if args.no_steps else step_bench(sw, stream, args)
+    gold = os.path.join(ROOT, "tests", "golden", "step_medium.npz")
+    steps = None if args.no_steps else step_bench(sw, stream, args, total=100, warm=3,
+                                                  golden=gold)
     # the reference's default DT = 36.3833/300: every step iterates Broyden's method
+    gold_dt = os.path.join(ROOT, "tests", "golden", "step_medium_default_dt.npz")
     steps_dt = None if args.no_steps else step_bench(sw, stream, args, dt=36.3833 / 300.0,
-                                                     timed=3, warm=2)
+                                                     total=23, warm=2, golden=gold_dt)
     # --- many swimmers: a batch stepped together, and a request stream ---------
     batched = None if args.no_batch else batch_bench(args)
     served = None if args.no_serve else serve_bench(args)
+    # --- the large swimmer: grand mobility, one solve, implicit steps ----------
+    large = None if args.no_large else large_bench(stream, flush, args, peak32, peak64)
     # --- the flow-field evaluator on a 128^3 grid around the large swimmer -----
     flow = None if args.no_flow else flow_bench(stream, flush, args, peak32, peak64, rank)
     clocks = sampler.stop()
@@ -333,10 +341,7 @@ def bench_ours(args):
             "vs_baseline": None,
             "dtype": "fp32 pairs, compensated accumulation; fp64 in/out",
             "data": "synthetic (seeded icosphere + Fibonacci filaments, N(0,1) forces)",
-            "config": {"workload": f"grand mobility, {args.config} swimmer", "segments": ns,
-                       "blobs": nb, "pairs_per_matvec": grand_pairs(ns, nb),
-                       "l2": "flushed between steps (256 MB write, outside the timed events)",
-                       "parallelism": f"replicas x{world}"},
+            "config": bench_config(args.config, ns, nb, world),
             "pair_interactions_per_s": value * grand_pairs(ns, nb),
             "e2e": {"value": e2e_value, "unit": "matvecs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
@@ -379,6 +384,8 @@ def bench_ours(args):
             result["served"] = served
         if flow is not None:
             result["flow"] = flow
+        if large is not None:
+            result["large"] = large
     for sv in (s32, s64):
         sv.finalise()
     if world > 1:
@@ -387,7 +394,7 @@ def bench_ours(args):
     return result
 
 
-def solve_bench(sw, stream, args, RpyMobilitySolver):
+def solve_bench(sw, stream, args, RpyMobilitySolver, steps=None):
     """compute_velocities (barrier forces, Mss, Mbs, the free-body GMRES
     solve for blob forces and body velocity, Msb) per Broyden iteration, FP64
     vs FP32C (iterative refinement), at a 1e-8 relative linear residual. Each
@@ -400,7 +407,7 @@ def solve_bench(sw, stream, args, RpyMobilitySolver):
     F = sw.f_segs[:, :3].sum(0)
     T = (np.cross(sw.x_segs, sw.f_segs[:, :3]) + sw.f_segs[:, 3:]).sum(0)
     rng = np.random.default_rng(99)
-    steps = {"fp64": max(3, min(args.steps, 5)), "fp32c": max(3, min(args.steps, 20))}
+    steps = steps or {"fp64": max(3, min(args.steps, 5)), "fp32c": max(3, min(args.steps, 20))}
     perturb = [1e-3 * rng.normal(size=sw.f_segs.shape) for _ in range(max(steps.values()) + 2)]
     out, results = {}, {}
     for precision in ("fp64", "fp32c"):
@@ -466,18 +473,22 @@ def solve_bench(sw, stream, args, RpyMobilitySolver):
             "fp32c_rel_l2_error_v_segs_vs_fp64": err}
 
 
-def step_bench(sw, stream, args, dt=1e-3, timed=None, warm=None):
+def step_bench(sw, stream, args, dt=1e-3, total=100, warm=3, precisions=("fp64", "fp32c"),
+               golden=None):
     """Implicit time steps of the swimmer with elastic filaments (the
     reference's cilia_sim_main.cu:355-527 loop: initial guess, internal
     forces, compute_velocities, BDF residuals, Broyden's method with the
     approximate inverse Jacobian), everything on the device, FP64 vs FP32C at
-    a 1e-8 relative linear residual, DT = 1e-3, Broyden TOL 1e-4. The
-    filaments start straight along the surface normals; step 0 (where
-    Broyden iterates from the straight start) is reported apart, then
-    `warmup` steps run untimed and the timed steps follow. Each step is
-    bracketed by CUDA events on the solver's stream (host gaps inside the
-    step included), giving per-step latency percentiles. The FP32C segment
-    positions are compared with the FP64 trajectory after every step."""
+    a 1e-8 relative linear residual, Broyden TOL 1e-4. The filaments start
+    straight along the surface normals; steps 0 .. total-1 run, step 0 (where
+    Broyden iterates from the straight start) is reported apart, the next
+    `warm` steps run untimed and the rest are timed. Each step is bracketed by
+    CUDA events on the solver's stream (host gaps inside the step included),
+    giving per-step latency percentiles. The FP32C segment positions are
+    compared with the FP64 trajectory after every step (the error per step,
+    relative to the largest position); with `golden` (the reference's own
+    trajectory of this swimmer, tests/golden/step_medium*.npz) both are
+    compared with the reference's positions after the steps it holds."""
     import torch
 
     from timfilsimmod_gb300.geometry import fibonacci_sphere
@@ -488,10 +499,14 @@ def step_bench(sw, stream, args, dt=1e-3, timed=None, warm=None):
     normals = fibonacci_sphere(nfil)
     fil_refs = (sw.radius + 1.0 + 0.5 * sw.seg_sep) * normals
     efm = 220.0 * 1800.0 / (2.6 * 2.6 * nseg * nseg)
-    timed = timed or max(3, min(args.steps, 20))
-    warm = warm or max(3, args.warmup)
-    out, traj = {}, {}
-    for precision in ("fp64", "fp32c"):
+    timed = total - 1 - warm
+    out, traj, vs_ref = {}, {}, {}
+    gold = None
+    if golden is not None and os.path.exists(golden):
+        gold = np.load(golden)
+        if int(gold["nfil"]) != nfil or int(gold["nseg"]) != nseg or abs(float(gold["dt"]) - dt) > 0:
+            gold = None
+    for precision in precisions:
         s = RpyMobilitySolver(1, nfil, nseg, nb, precision=precision,
                               end_force_magnitude=int(efm))
         s.set_stream(stream.cuda_stream)
@@ -501,7 +516,7 @@ def step_bench(sw, stream, args, dt=1e-3, timed=None, warm=None):
                              tol=1e-4, end_force_magnitude=efm, body_radius=sw.radius)
         lat, broy, gm, xs = [], [], [], []
         launches = 0
-        for nt in range(1 + warm + timed):
+        for nt in range(total):
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             l0 = kernel_launch_count()
@@ -514,7 +529,13 @@ def step_bench(sw, stream, args, dt=1e-3, timed=None, warm=None):
             lat.append(a.elapsed_time(b))
             broy.append(bi)
             gm.append(gi)
-            xs.append(st.state()["x"])
+            x = st.state()["x"]
+            xs.append(x)
+            if gold is not None and nt < len(gold["broyden_iters"]):
+                tips = x.reshape(nfil, nseg, 3)[:, -1, :].ravel()
+                sc = np.max(np.abs(gold["traj_tips"][-1]))
+                vs_ref.setdefault(precision, []).append(
+                    float(np.max(np.abs(tips - gold["traj_tips"][nt])) / sc))
         traj[precision] = xs
         tl = np.array(lat[1 + warm:])
         out[precision] = {
@@ -528,14 +549,24 @@ def step_bench(sw, stream, args, dt=1e-3, timed=None, warm=None):
         }
         st.close()
         s.finalise()
-    x64, x32 = np.array(traj["fp64"]), np.array(traj["fp32c"])
-    scale = np.max(np.abs(x64), axis=1)
-    dev = np.max(np.abs(x32 - x64), axis=1) / scale
-    return {"workload": f"{nfil} filaments x {nseg} segments, {nb} blobs; dt {dt:.6g}, "
-                        "Broyden TOL 1e-4, linear residual 1e-8",
-            **out, "speedup_fp32c_vs_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
-            "fp32c_max_rel_position_dev_vs_fp64": float(dev.max()),
-            "fp32c_rel_position_dev_vs_fp64_last": float(dev[-1])}
+    res = {"workload": f"{nfil} filaments x {nseg} segments, {nb} blobs; dt {dt:.6g}, "
+                       f"steps 0-{total - 1} ({timed} timed), Broyden TOL 1e-4, linear residual 1e-8",
+           **out}
+    if "fp64" in out and "fp32c" in out:
+        x64, x32 = np.array(traj["fp64"]), np.array(traj["fp32c"])
+        scale = np.max(np.abs(x64), axis=1)
+        dev = np.max(np.abs(x32 - x64), axis=1) / scale
+        res.update({"speedup_fp32c_vs_fp64": out["fp32c"]["value"] / out["fp64"]["value"],
+                    "fp32c_max_rel_position_dev_vs_fp64": float(dev.max()),
+                    "fp32c_rel_position_dev_vs_fp64_last": float(dev[-1]),
+                    "fp32c_rel_position_dev_vs_fp64_per_step": [float(f"{v:.3e}") for v in dev]})
+    if vs_ref:
+        res["rel_tip_error_vs_reference_per_step"] = {
+            k: [float(f"{v:.3e}") for v in vals] for k, vals in vs_ref.items()}
+        res["reference_trajectory"] = ("the reference's own step code on this swimmer "
+                                       f"({os.path.basename(golden)}; its linear residual "
+                                       "1e-10, here 1e-8)")
+    return res
 
 
 def _step_instance(nf, precision, cache, rot_seed=None):
@@ -640,8 +671,10 @@ def serve_bench(args):
     from timfilsimmod_gb300.serving import StepServer
 
     rng = np.random.default_rng(777)
-    ns = np.exp(rng.uniform(np.log(64), np.log(20000), size=args.serve_bases))
-    bases = sorted({max(4, int(round(x / 20))) for x in ns})
+    # the ends of the size range (80 segments: the smallest whole number of
+    # 20-segment filaments >= 64; 20 000) and log-uniform sizes between them
+    ns = np.exp(rng.uniform(np.log(64), np.log(20000), size=max(0, args.serve_bases - 2)))
+    bases = sorted({4, 1000} | {max(4, min(1000, int(round(x / 20)))) for x in ns})
     geo = {nf: elastic_swimmer(nf) for nf in bases}
     efm = 220.0 * 1800.0 / (2.6 * 2.6 * 400)
     nreq = args.serve_requests
@@ -676,9 +709,18 @@ def serve_bench(args):
             tickets.append(submit(sv, nf, rot))
         lat = np.array([sv.poll(t, wait=True)["latency_ms"] for t in tickets])
         sec = time.perf_counter() - t0
+        segs = np.array([nf * 20 for nf, _ in reqs])
+        buckets = {}
+        for name, lo, hi in (("<1000 segments", 0, 1000), ("1000-5000", 1000, 5000),
+                             (">=5000", 5000, 1 << 30)):
+            sel = lat[(segs >= lo) & (segs < hi)]
+            if sel.size:
+                buckets[name] = {"requests": int(sel.size), "p50_ms": float(np.percentile(sel, 50)),
+                                 "p99_ms": float(np.percentile(sel, 99))}
         rates[str(lam)] = {"offered_req_per_s": lam, "steps_per_s": nreq / sec,
                            "p50_ms": float(np.percentile(lat, 50)),
-                           "p99_ms": float(np.percentile(lat, 99)), "requests": nreq}
+                           "p99_ms": float(np.percentile(lat, 99)), "requests": nreq,
+                           "by_size": buckets}
     stats = sv.stats()
     shared = sv.shared_solves()
     sv.close()
@@ -702,6 +744,68 @@ def serve_bench(args):
                              "shared_inner_solves": shared},
             "fp64_one_at_a_time": base,
             "speedup_best_rate_vs_fp64": best / base["steps_per_s"]}
+
+
+def large_bench(stream, flush, args, peak32, peak64):
+    """The large swimmer (R = 150a sphere of 10 242 blobs, 4 000 filaments x 20
+    segments = 80 000 segments in planar beat shapes at uniform-random phases,
+    N(0,1) forces): the grand mobility in FP32C (the work-queue launch against
+    the FP32 FMA peak; autotuned) and in FP64 (the launch against the FP64 FMA
+    peak; default variant), CUDA events per matvec, L2 flushed between them;
+    one compute_velocities solve per Broyden iteration at a 1e-8 linear
+    residual in both precisions; FP32C implicit steps from a straight start
+    (DT 1e-3): step 0, where Broyden iterates, and the steps after it."""
+    import torch
+
+    from timfilsimmod_gb300.geometry import make_config
+    from timfilsimmod_gb300.mobility import RpyMobilitySolver
+
+    sw = make_config("large", seed=4321)
+    ns, nb = sw.num_segs, sw.num_blobs
+    flops = grand_flops(ns, nb)
+    out, vel = {"workload": f"large swimmer: {ns} segments (beat shapes), {nb} blobs",
+                "pairs_per_matvec": grand_pairs(ns, nb), "flops_per_matvec": flops}, {}
+    for precision, reps, peak in (("fp32c", 5, peak32), ("fp64", 2, peak64)):
+        s = RpyMobilitySolver(1, sw.nfil, sw.nseg, nb, precision=precision)
+        s.set_stream(stream.cuda_stream)
+        s.set_state(sw.x_segs, sw.f_segs, sw.x_blobs, sw.f_blobs)
+        if precision == "fp32c" and not args.no_tune:
+            s.autotune(("fp32c",), reps=1)
+        s.apply_grand_mobility()  # warm-up
+        torch.cuda.synchronize()
+        s.enable_kernel_timing(True)
+        ms = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s.apply_grand_mobility()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+        kt = s.kernel_timing()
+        s.enable_kernel_timing(False)
+        s.copy_segment_velocities_to_host()
+        s.copy_blob_velocities_to_host()
+        s.wait_for_device()
+        vel[precision] = np.concatenate([s.v_segs_host, s.v_blobs_host]).copy()
+        launch_ms = float(np.mean(kt))
+        achieved = flops / (launch_ms * 1e-3) / 1e12
+        out[precision] = {"value": reps / (ms * 1e-3), "unit": "matvecs/s",
+                          "ms_per_matvec": ms / reps, "reps": reps,
+                          "pair_interactions_per_s": grand_pairs(ns, nb) * reps / (ms * 1e-3),
+                          "roofline": {"bound": f"{'fp32' if precision == 'fp32c' else 'fp64'}-fma",
+                                       "achieved": achieved, "peak": peak / 1e12,
+                                       "unit": "TFLOP/s", "frac": achieved / (peak / 1e12),
+                                       "avg_launch_ms": launch_ms}}
+        s.finalise()
+    out["fp32c_rel_l2_error_vs_fp64"] = float(np.linalg.norm(vel["fp32c"] - vel["fp64"])
+                                              / np.linalg.norm(vel["fp64"]))
+    out["speedup_fp32c_vs_fp64"] = out["fp32c"]["value"] / out["fp64"]["value"]
+    out["solve"] = solve_bench(sw, stream, args, RpyMobilitySolver,
+                               steps={"fp64": 1, "fp32c": 3})
+    out["implicit_steps"] = step_bench(sw, stream, args, total=5, warm=1, precisions=("fp32c",))
+    return out
 
 
 FLOW_SEG, FLOW_BLOB, FLOW_POINT = 44, 28, 3  # canonical flops per source, per point
@@ -812,28 +916,49 @@ def flow_bench(stream, flush, args, peak32, peak64, rank):
     return out
 
 
-def cpu_baseline(sw, stride: int):
+def cpu_sample_step(o, sw, stride):
+    """One sampled grand matvec on the host cores: every `stride`-th segment
+    and blob target against all sources, four blocks (the oracle port of
+    cuda_functions.cu:362-757). Returns the pair count."""
+    xs_t, xb_t = sw.x_segs[::stride], sw.x_blobs[::stride]
+    o.block(6, 6, xs_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
+    o.block(6, 3, xs_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
+    o.block(3, 6, xb_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
+    o.block(3, 3, xb_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
+    return (xs_t.shape[0] + xb_t.shape[0]) * (sw.num_segs + sw.num_blobs)
+
+
+def cpu_baseline(sw, stride: int, min_seconds: float = 0.5):
     """The reference's RPY sums on the host cores (oracle port, all threads):
-    every `stride`-th segment and blob target against all sources, four
-    blocks, extrapolated to a full grand matvec by the pair count."""
+    one warm-up sample, then repeated samples for at least `min_seconds`,
+    extrapolated to a full grand matvec by the pair count."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle
 
     threads = os.cpu_count() or 1
     o = Oracle(threads=threads)
-    xs_t, xb_t = sw.x_segs[::stride], sw.x_blobs[::stride]
+    cpu_sample_step(o, sw, stride)  # warm-up (thread pool, caches)
+    pairs, reps = 0, 0
     t0 = time.perf_counter()
-    o.block(6, 6, xs_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
-    o.block(6, 3, xs_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
-    o.block(3, 6, xb_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
-    o.block(3, 3, xb_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
-    dt = time.perf_counter() - t0
-    ns, nb = sw.num_segs, sw.num_blobs
-    pairs = (xs_t.shape[0] + xb_t.shape[0]) * (ns + nb)
-    rate = pairs / dt / grand_pairs(ns, nb)
+    while True:
+        pairs += cpu_sample_step(o, sw, stride)
+        reps += 1
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            break
+    rate = pairs / dt / grand_pairs(sw.num_segs, sw.num_blobs)
     return {"value": rate, "unit": "matvecs/s", "cores": threads, "kind": "port",
-            "sample": f"every {stride}th target of the full grand matvec ({pairs} pairs, "
-                      f"{dt:.2f} s), extrapolated by pair count"}
+            "sample": f"every {stride}th target of the full grand matvec, {reps} samples "
+                      f"after one warm-up ({pairs} pairs, {dt:.2f} s), extrapolated by pair count"}
+
+
+def bench_config(config, ns, nb, world):
+    """The `config` object of both arms' lines (the same keys and values)."""
+    return {"workload": f"grand mobility, {config} swimmer", "segments": ns, "blobs": nb,
+            "pairs_per_matvec": grand_pairs(ns, nb),
+            "l2": "GPU arm: flushed between steps (256 MB write, outside the timed events); "
+                  "CPU arm: no flush",
+            "parallelism": f"replicas x{world}"}
 
 
 def bench_reference(args):
@@ -850,21 +975,13 @@ def bench_reference(args):
     threads = os.cpu_count() or 1
     o = Oracle(threads=threads)
     stride = args.cpu_sample
-    xs_t, xb_t = sw.x_segs[::stride], sw.x_blobs[::stride]
     ns, nb = sw.num_segs, sw.num_blobs
-    pairs = (xs_t.shape[0] + xb_t.shape[0]) * (ns + nb)
-
-    def step():
-        o.block(6, 6, xs_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
-        o.block(6, 3, xs_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
-        o.block(3, 6, xb_t, 1.0, sw.x_segs, sw.f_segs, 1.0)
-        o.block(3, 3, xb_t, 1.0, sw.x_blobs, sw.f_blobs, 1.0)
-
+    pairs = 0
     for _ in range(args.warmup):
-        step()
+        cpu_sample_step(o, sw, stride)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        step()
+        pairs = cpu_sample_step(o, sw, stride)
     dt = time.perf_counter() - t0
     value = args.steps * pairs / dt / grand_pairs(ns, nb)
     sample = (f"every {stride}th target of the full grand matvec per step ({pairs} pairs), "
@@ -883,8 +1000,7 @@ def bench_reference(args):
         "vs_baseline": None,
         "dtype": "fp64",
         "data": "synthetic (seeded icosphere + Fibonacci filaments, N(0,1) forces)",
-        "config": {"workload": f"grand mobility, {args.config} swimmer", "segments": ns,
-                   "blobs": nb, "pairs_per_matvec": grand_pairs(ns, nb)},
+        "config": bench_config(args.config, ns, nb, world),
         "cpu_baseline": {"value": value, "unit": "matvecs/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "matvecs/s", "h2d_bytes_per_step": 0,
@@ -911,12 +1027,13 @@ def main():
     p.add_argument("--no-steps", action="store_true", help="skip the implicit-step timing")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-swimmers timing")
     p.add_argument("--no-serve", action="store_true", help="skip the request-stream timing")
+    p.add_argument("--no-large", action="store_true", help="skip the large-swimmer timing")
     p.add_argument("--batch-size", type=int, default=64, help="swimmers in the batch leg")
     p.add_argument("--batch-workers", type=int, default=16, help="host workers of the batch")
     p.add_argument("--serve-bases", type=int, default=12, help="base swimmers of the stream")
     p.add_argument("--serve-requests", type=int, default=96, help="requests per arrival rate")
     p.add_argument("--serve-workers", type=int, default=16, help="server workers")
-    p.add_argument("--serve-rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0],
+    p.add_argument("--serve-rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0, 2000.0],
                    help="Poisson arrival rates (requests/s)")
     p.add_argument("--flow-grid", type=int, default=128, help="flow points per grid axis")
     args = p.parse_args()

@@ -388,23 +388,30 @@ typedef struct tfs_server_config {
   int precision;              /* TFS_FP64 or TFS_FP32C */
   double linear_tol;          /* LINEAR_SYSTEM_TOL of every solve */
   tfs_step_config step;       /* step settings (nfil, nseg come from each request) */
+  double max_bypass_ms;       /* age bound of admission past a waiting request (below) */
 } tfs_server_config;
 typedef struct tfs_server_counters {
   long long resident_instances, created, reused, evicted, queued, inflight;
   size_t bytes_in_use;
+  long long bypassed;         /* requests admitted past an older waiting one */
 } tfs_server_counters;
 typedef struct tfs_server tfs_server;
 /* Defaults: 16 workers, 160 GB, FP32C, linear tolerance 1e-8, the step
- * defaults of tfs_step_config_default. */
+ * defaults of tfs_step_config_default, max_bypass_ms 1000. */
 int tfs_server_config_default(tfs_server_config *cfg);
 int tfs_server_create(const tfs_server_config *cfg, tfs_server **out);
 /* Queues a request (arrival time = now); TFS_ENOMEM if its swimmer alone
  * exceeds the budget. Instances stay resident between requests, keyed by
- * geometry; a request is admitted, in arrival order, when an idle instance
- * of its geometry exists or a new one fits in the budget after evicting
- * idle instances (least recently used first). Memory is accounted from
- * each instance's estimated size at admission. */
+ * geometry; a request can be admitted when an idle instance of its geometry
+ * exists or a new one fits in the budget after evicting idle instances
+ * (least recently used first). Requests are admitted in arrival order,
+ * except that while the oldest waits for device memory held by running
+ * requests, a later request that fits is admitted past it -- until the
+ * oldest has waited max_bypass_ms; from then on nothing passes it. Memory is
+ * accounted from each instance's estimated size at admission. */
 int tfs_server_submit(tfs_server *sv, const tfs_request *r, long long *ticket);
+/* The device bytes the server accounts for a request's instance. */
+int tfs_server_request_bytes(const tfs_server *sv, const tfs_request *r, size_t *bytes);
 /* *status: 1 while pending, else the request's TFS status (the ticket is
  * then released; a failed request's message becomes the calling thread's
  * tfs_last_error()). TFS_ENOTCONV: Broyden's method reached its cap at some
@@ -504,6 +511,13 @@ long long tfs_kernel_launch_count(void);
  * precision TFS_FP64 or TFS_FP32C (plain FP32 FMAs), from a dependent-chain
  * microbenchmark over every SM. */
 int tfs_measure_fma_peak(int precision, double *flops_per_second);
+/* y[i] = x[i]^(-1/2) by the FP64 reciprocal square root the FP64 pair
+ * kernels use for far-field separations (an FP32 hardware seed refined by one
+ * third-order Householder step), on device arrays x[n], y[n], on `stream`;
+ * valid for x in the FP32 normal range. For accuracy tests; no counterpart in
+ * the reference (its unbounded pair takes 1/(sqrt(r^2) + 1e-20),
+ * cuda_functions.cu:212-213). */
+int tfs_rsqrt_far(const double *x, double *y, int n, void *stream);
 
 #ifdef __cplusplus
 }

@@ -158,6 +158,43 @@ def test_server_budget_evicts_and_rejects():
     sv.close()
 
 
+def test_server_admits_past_a_request_waiting_for_memory():
+    """Two workers, a budget that holds one large instance and one small one:
+    while the first large request runs, a second large one (another
+    geometry) waits for memory, and a small request that arrives after it is
+    admitted past it; with max_bypass_ms = 0 nothing passes the waiting
+    request. Each result is the same, bit for bit, either way."""
+    from timfilsimmod_gb300.serving import StepServer
+
+    big_a, big_b, small = geometry(3, 24), geometry(3, 24, radius=20.5), geometry(2, 7)
+    probe = StepServer(num_workers=1)
+    nb_big = probe.request_bytes(*big_a[:3], 20)
+    nb_small = probe.request_bytes(*small[:3], 20)
+    probe.close()
+    budget_gb = (nb_big + nb_small + (1 << 20)) / float(1 << 30)
+    assert nb_big + nb_big > nb_big + nb_small + (1 << 20)  # two large ones never fit
+
+    def run(max_bypass_ms):
+        sv = StepServer(num_workers=2, hbm_budget_gb=budget_gb, precision="fp32c",
+                        linear_tol=1e-8, dt=DT, tol=TOL, seg_sep=2.2, end_force_magnitude=efm(),
+                        max_bypass_ms=max_bypass_ms)
+        t = [sv.submit(*g[:3], 20, num_steps=n, body_radius=g[3])
+             for g, n in ((big_a, 4), (big_b, 1), (small, 1))]
+        res = [sv.poll(k, wait=True) for k in t]
+        st = sv.stats()
+        sv.close()
+        return res, st
+
+    res, st = run(60_000.0)
+    assert st["bypassed"] == 1, st
+    # the small request did not wait for the second large one
+    assert res[2]["latency_ms"] < res[1]["latency_ms"]
+    fifo, st0 = run(0.0)
+    assert st0["bypassed"] == 0, st0
+    for a, b in zip(res, fifo):
+        assert np.array_equal(a["x"], b["x"]) and np.array_equal(a["body"], b["body"])
+
+
 def test_nan_swimmer_does_not_poison_batch():
     """A swimmer whose state is made non-finite on the host (NaN segment
     rotations) fails alone with TFS_ENAN; the others -- whose inner solves

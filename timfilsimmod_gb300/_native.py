@@ -69,13 +69,13 @@ class Request(ctypes.Structure):
 class ServerConfig(ctypes.Structure):
     _fields_ = [("num_workers", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t),
                 ("precision", ctypes.c_int), ("linear_tol", ctypes.c_double),
-                ("step", StepConfig)]
+                ("step", StepConfig), ("max_bypass_ms", ctypes.c_double)]
 
 
 class ServerCounters(ctypes.Structure):
     _fields_ = [(n, ctypes.c_longlong) for n in ("resident_instances", "created", "reused",
                                                   "evicted", "queued", "inflight")] + \
-               [("bytes_in_use", ctypes.c_size_t)]
+               [("bytes_in_use", ctypes.c_size_t), ("bypassed", ctypes.c_longlong)]
 
 
 _P = ctypes.c_void_p
@@ -150,6 +150,7 @@ _SIGNATURES = {
     "tfs_flow_autotune": [_H, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
     "tfs_mss_noalloc": [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P],
+    "tfs_rsqrt_far": [_P, _P, ctypes.c_int, _P],
     "tfs_step_config_default": [ctypes.POINTER(StepConfig), ctypes.c_int, ctypes.c_int],
     "tfs_stepper_create": [_H, ctypes.POINTER(StepConfig), _P, _P, ctypes.POINTER(_H)],
     "tfs_stepper_destroy": [_H],
@@ -183,6 +184,7 @@ _SIGNATURES = {
     "tfs_server_config_default": [ctypes.POINTER(ServerConfig)],
     "tfs_server_create": [ctypes.POINTER(ServerConfig), ctypes.POINTER(_H)],
     "tfs_server_submit": [_H, ctypes.POINTER(Request), _LLP],
+    "tfs_server_request_bytes": [_H, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_size_t)],
     "tfs_server_poll": [_H, ctypes.c_longlong, ctypes.c_int, _IP,
                         ctypes.POINTER(ctypes.c_double), _IP, _IP],
     "tfs_server_drain": [_H],

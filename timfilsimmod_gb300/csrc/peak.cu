@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/tfs_gb300.h"
+#include "tfs_device.cuh"
 #include "tfs_kernels.h"
 
 namespace tfs {
@@ -63,5 +64,28 @@ extern "C" int tfs_measure_fma_peak(int precision, double *flops_per_second) {
   if (e != cudaSuccess) return cuda_fail(e, "FMA microbenchmark");
   const double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
   *flops_per_second = flops / (best_ms * 1e-3);
+  return TFS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The FP64 reciprocal square root of far-field separations (rsqrt_far), on a
+// device array, for accuracy tests against CUDA's rsqrt and a host reference.
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void rsqrt_far_kernel(const double *__restrict__ x, double *__restrict__ y, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = tfs::rsqrt_far(x[i]);
+}
+}  // namespace
+
+extern "C" int tfs_rsqrt_far(const double *x, double *y, int n, void *stream) {
+  using namespace tfs;
+  if (n < 0) return fail(TFS_EINVAL, "negative count");
+  if (n == 0) return TFS_OK;
+  if (x == nullptr || y == nullptr) return fail(TFS_EINVAL, "null device pointer");
+  rsqrt_far_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, y, n);
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "rsqrt_far kernel");
   return TFS_OK;
 }

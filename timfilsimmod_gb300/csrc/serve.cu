@@ -285,7 +285,7 @@ struct tfs_server {
   size_t bytes_in_use = 0;
   long long next_ticket = 1;
   long long inflight = 0;
-  long long created = 0, evicted = 0, reused = 0;
+  long long created = 0, evicted = 0, reused = 0, bypassed = 0;
   bool stop = false;
   std::vector<std::thread> workers;
   tfs::GmresService *service = nullptr;  // shared inner solves of FP32C instances
@@ -293,6 +293,7 @@ struct tfs_server {
 
   void worker();
   bool can_admit(const Request *q) const;
+  std::deque<Request *>::iterator pick();
   Instance *acquire(const Request *q, std::vector<Instance *> &victims, bool *fresh);
   int build(Instance *in, const tfs_request &r);
 };
@@ -330,6 +331,22 @@ bool tfs_server::can_admit(const Request *q) const {
     idle += in->bytes;
   }
   return bytes_in_use - idle + q->bytes <= cfg.hbm_budget_bytes;
+}
+
+// With the lock held: the request to admit next, or queue.end(). The oldest
+// request goes first when it can be admitted; while it waits for device
+// memory held by running requests, a later one that fits now is admitted
+// past it -- unless the oldest has waited max_bypass_ms or more, in which
+// case nothing passes it, so that memory frees up for it (no starvation).
+std::deque<Request *>::iterator tfs_server::pick() {
+  if (queue.empty()) return queue.end();
+  if (can_admit(queue.front())) return queue.begin();
+  const double waited =
+      std::chrono::duration<double, std::milli>(Clock::now() - queue.front()->arrival).count();
+  if (waited >= cfg.max_bypass_ms) return queue.end();
+  for (auto it = queue.begin() + 1; it != queue.end(); ++it)
+    if (can_admit(*it)) return it;
+  return queue.end();
 }
 
 // With the lock held, after can_admit(q): the idle instance of q's geometry,
@@ -372,10 +389,18 @@ void tfs_server::worker() {
   cudaSetDevice(device);
   std::unique_lock<std::mutex> g(m);
   for (;;) {
-    cv.wait(g, [&] { return stop || (!queue.empty() && can_admit(queue.front())); });
-    if (stop) return;
-    Request *q = queue.front();
-    queue.pop_front();
+    // a request held back only by the age bound needs a wake-up when the
+    // bound runs out, so the wait is also bounded in time
+    std::deque<Request *>::iterator it;
+    for (;;) {
+      if (stop) return;
+      it = pick();
+      if (it != queue.end()) break;
+      cv.wait_for(g, std::chrono::milliseconds(20));
+    }
+    Request *q = *it;
+    if (it != queue.begin()) ++bypassed;
+    queue.erase(it);
     std::vector<Instance *> victims;
     bool fresh = false;
     Instance *in = acquire(q, victims, &fresh);
@@ -434,6 +459,7 @@ int tfs_server_config_default(tfs_server_config *cfg) {
   cfg->hbm_budget_bytes = (size_t)160 << 30;
   cfg->precision = TFS_FP32C;
   cfg->linear_tol = 1e-8;
+  cfg->max_bypass_ms = 1000.0;
   return tfs_step_config_default(&cfg->step, 1, 20);
 }
 
@@ -443,6 +469,7 @@ int tfs_server_create(const tfs_server_config *cfg, tfs_server **out) {
   if (cfg->num_workers < 1 || cfg->num_workers > 256) return fail(TFS_EINVAL, "num_workers must be in [1, 256]");
   if (cfg->precision != TFS_FP64 && cfg->precision != TFS_FP32C) return fail(TFS_EINVAL, "bad precision");
   if (!(cfg->linear_tol > 0) || cfg->hbm_budget_bytes == 0) return fail(TFS_EINVAL, "linear_tol and budget must be > 0");
+  if (!(cfg->max_bypass_ms >= 0)) return fail(TFS_EINVAL, "max_bypass_ms must be >= 0");
   tfs_server *sv = new (std::nothrow) tfs_server();
   if (sv == nullptr) return fail(TFS_ENOMEM, "host allocation");
   sv->cfg = *cfg;
@@ -460,19 +487,33 @@ int tfs_server_create(const tfs_server_config *cfg, tfs_server **out) {
   return TFS_OK;
 }
 
+static bool malformed(const tfs_request *r) {
+  return r->nfil < 1 || r->nseg < 3 || r->nblob < 1 || r->num_steps < 0 ||
+         r->blob_refs == nullptr || r->fil_refs == nullptr || r->fil_dirs == nullptr;
+}
+
+static size_t request_bytes(const tfs_server *sv, const tfs_request *r) {
+  tfs_config c;
+  tfs_config_default(&c, 1, r->nfil, r->nseg, r->nblob);
+  return tfs::solver_bytes_estimate(&c) +
+         tfs::stepper_bytes_estimate(r->nfil, r->nseg, sv->cfg.step.max_broyden_iter);
+}
+
+int tfs_server_request_bytes(const tfs_server *sv, const tfs_request *r, size_t *bytes) {
+  if (sv == nullptr || r == nullptr || bytes == nullptr) return fail(TFS_EINVAL, "null argument");
+  if (malformed(r)) return fail(TFS_EINVAL, "malformed request");
+  *bytes = request_bytes(sv, r);
+  return TFS_OK;
+}
+
 int tfs_server_submit(tfs_server *sv, const tfs_request *r, long long *ticket) {
   if (sv == nullptr || r == nullptr || ticket == nullptr) return fail(TFS_EINVAL, "null argument");
-  if (r->nfil < 1 || r->nseg < 3 || r->nblob < 1 || r->num_steps < 0 || r->blob_refs == nullptr ||
-      r->fil_refs == nullptr || r->fil_dirs == nullptr)
-    return fail(TFS_EINVAL, "malformed request");
+  if (malformed(r)) return fail(TFS_EINVAL, "malformed request");
   std::unique_ptr<Request> q(new (std::nothrow) Request());
   if (!q) return fail(TFS_ENOMEM, "host allocation");
   q->r = *r;
   q->key = geometry_key(*r);
-  tfs_config c;
-  tfs_config_default(&c, 1, r->nfil, r->nseg, r->nblob);
-  q->bytes = tfs::solver_bytes_estimate(&c) +
-             tfs::stepper_bytes_estimate(r->nfil, r->nseg, sv->cfg.step.max_broyden_iter);
+  q->bytes = request_bytes(sv, r);
   if (q->bytes > sv->cfg.hbm_budget_bytes)
     return fail(TFS_ENOMEM, "a swimmer of %d x %d segments and %d blobs needs ~%zu bytes, over the budget",
                 r->nfil, r->nseg, r->nblob, q->bytes);
@@ -518,6 +559,7 @@ int tfs_server_stats(tfs_server *sv, tfs_server_counters *out) {
   std::lock_guard<std::mutex> g(sv->m);
   out->resident_instances = (long long)sv->pool.size();
   out->bytes_in_use = sv->bytes_in_use;
+  out->bypassed = sv->bypassed;
   out->created = sv->created;
   out->reused = sv->reused;
   out->evicted = sv->evicted;

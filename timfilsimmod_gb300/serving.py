@@ -80,7 +80,8 @@ class StepServer:
     body_radius, max_broyden_iter, ...)."""
 
     def __init__(self, num_workers: int = 16, hbm_budget_gb: float = 160.0,
-                 precision: str = "fp32c", linear_tol: float = 1e-8, **step):
+                 precision: str = "fp32c", linear_tol: float = 1e-8,
+                 max_bypass_ms: float | None = None, **step):
         self.lib = N.load()
         cfg = N.ServerConfig()
         N.check(self.lib.tfs_server_config_default(ctypes.byref(cfg)))
@@ -88,6 +89,8 @@ class StepServer:
         cfg.hbm_budget_bytes = int(hbm_budget_gb * (1 << 30))
         cfg.precision = PRECISIONS[precision]
         cfg.linear_tol = float(linear_tol)
+        if max_bypass_ms is not None:
+            cfg.max_bypass_ms = float(max_bypass_ms)
         for k, v in step.items():
             if k in ("body_x", "body_q"):
                 arr = getattr(cfg.step, k)
@@ -120,6 +123,15 @@ class StepServer:
         N.check(self.lib.tfs_server_submit(self._h, ctypes.byref(r), ctypes.byref(t)))
         self._live[t.value] = (br, fr, fd, rot, x, body)
         return t.value
+
+    def request_bytes(self, blob_refs, fil_refs, fil_dirs, nseg: int) -> int:
+        """Device bytes the server accounts for a request of this geometry."""
+        br, fr, fd = _f64(blob_refs), _f64(fil_refs), _f64(fil_dirs)
+        r = N.Request(nfil=fr.size // 3, nseg=int(nseg), nblob=br.size // 3,
+                      blob_refs=br.ctypes.data, fil_refs=fr.ctypes.data, fil_dirs=fd.ctypes.data)
+        b = ctypes.c_size_t(0)
+        N.check(self.lib.tfs_server_request_bytes(self._h, ctypes.byref(r), ctypes.byref(b)))
+        return b.value
 
     def poll(self, ticket: int, wait: bool = False) -> dict | None:
         """None while pending; else the result (x, body, latency_ms, counts).
