@@ -626,6 +626,7 @@ def batch_bench(args):
                 iters.append(batch.step(nt, allow_unconverged=True)["gmres_iters"].mean())
             sec = time.perf_counter() - t0
             shared = batch.shared_solves()
+            shared_products = batch.shared_products()
             batch.close()
         else:
             for nt in range(warm):
@@ -641,10 +642,12 @@ def batch_bench(args):
         out[precision] = {"value": n * timed / sec, "unit": "swimmer-steps/s",
                           "ms_per_batch_step": 1e3 * sec / timed,
                           "gmres_iters_per_swimmer_step": float(np.mean(iters)),
-                          "mode": (f"batch, {args.batch_workers} host workers, one stream per swimmer"
+                          "mode": (f"batch, {args.batch_workers} host workers, one stream per "
+                                   "swimmer, inner solves and pair products in shared launches"
                                    if precision == "fp32c" else "one swimmer at a time")}
         if precision == "fp32c":
             out[precision]["shared_inner_solves"] = shared
+            out[precision]["shared_products"] = shared_products
         for s, st in inst:
             st.close()
             s.finalise()
@@ -723,6 +726,7 @@ def serve_bench(args):
                            "by_size": buckets}
     stats = sv.stats()
     shared = sv.shared_solves()
+    shared_products = sv.shared_products()
     sv.close()
     sv = server("fp64", 1)
     reqs = stream(int(args.serve_rates[0]))
@@ -741,7 +745,7 @@ def serve_bench(args):
             "fp32c_server": {"workers": args.serve_workers, "by_rate": rates,
                              "resident_instances": stats["resident_instances"],
                              "created": stats["created"], "reused": stats["reused"],
-                             "shared_inner_solves": shared},
+                             "shared_inner_solves": shared, "shared_products": shared_products},
             "fp64_one_at_a_time": base,
             "speedup_best_rate_vs_fp64": best / base["steps_per_s"]}
 
@@ -1029,7 +1033,7 @@ def main():
     p.add_argument("--no-serve", action="store_true", help="skip the request-stream timing")
     p.add_argument("--no-large", action="store_true", help="skip the large-swimmer timing")
     p.add_argument("--batch-size", type=int, default=64, help="swimmers in the batch leg")
-    p.add_argument("--batch-workers", type=int, default=16, help="host workers of the batch")
+    p.add_argument("--batch-workers", type=int, default=32, help="host workers of the batch")
     p.add_argument("--serve-bases", type=int, default=12, help="base swimmers of the stream")
     p.add_argument("--serve-requests", type=int, default=96, help="requests per arrival rate")
     p.add_argument("--serve-workers", type=int, default=16, help="server workers")

@@ -348,7 +348,15 @@ int tfs_stepper_write_files(tfs_stepper *st, int nt, const char *prefix, int bac
  * each on a fixed number of CTAs chosen from its own blob count (about one
  * per 64 blobs), so its arithmetic does not depend on the others. FP32C
  * swimmers the persistent kernel cannot take, and FP64 swimmers, solve on
- * their own with the kernel sequence. */
+ * their own with the kernel sequence.
+ * The pair products of every instance (M_ss with M_bs, M_sb, ...) run in
+ * shared work-queue launches (in the server, and in a batch unless
+ * tfs_batch_share_products says otherwise): products waiting while the
+ * previous shared launch runs are gathered (those of one precision and
+ * source set, up to 256 jobs) into one persistent launch whose CTAs take
+ * the (target block, source chunk) units of all of them from one counter.
+ * Each product keeps its own chunking, partial sums and ordered reduction,
+ * so its result is the same, bit for bit, alone and shared. */
 typedef struct tfs_batch tfs_batch;
 int tfs_batch_create(int num_workers, tfs_batch **out);
 int tfs_batch_destroy(tfs_batch *b);   /* does not destroy the instances */
@@ -367,6 +375,10 @@ int tfs_batch_step(tfs_batch *b, int nt, int *broyden_iters, int *gmres_iters, i
 int tfs_batch_share_inner_solves(tfs_batch *b, int max_ctas);
 /* Inner solves run in shared launches so far, and those launches. */
 int tfs_batch_shared_solves(tfs_batch *b, long long *launches, long long *solves);
+/* Whether the batch's products share work-queue launches (default 1), and
+ * the shared launches and the products they carried so far. */
+int tfs_batch_share_products(tfs_batch *b, int enable);
+int tfs_batch_shared_products(tfs_batch *b, long long *launches, long long *products);
 
 /* A request: num_steps implicit steps (0 .. num_steps-1) of a swimmer
  * given by its geometry (blob references, filament bases and directions;
@@ -423,6 +435,7 @@ int tfs_server_poll(tfs_server *sv, long long ticket, int wait, int *status, dou
 int tfs_server_drain(tfs_server *sv);   /* until every submitted request completed */
 int tfs_server_stats(tfs_server *sv, tfs_server_counters *out);
 int tfs_server_shared_solves(tfs_server *sv, long long *launches, long long *solves);
+int tfs_server_shared_products(tfs_server *sv, long long *launches, long long *products);
 int tfs_server_destroy(tfs_server *sv); /* drains first */
 
 /* --- flow-field evaluator ---------------------------------------------- */

@@ -47,30 +47,57 @@ def make_instance(subdiv, nfil, precision):
     return s, st
 
 
-@pytest.mark.parametrize("precision,share", [("fp64", False), ("fp32c", False), ("fp32c", True),
-                                             ("fp32c", -1)])
-def test_batch_same_as_alone(precision, share):
+@pytest.mark.parametrize("precision,share,products", [
+    ("fp64", False, True), ("fp64", False, False), ("fp32c", False, True), ("fp32c", True, True),
+    ("fp32c", -1, True), ("fp32c", -1, False)])
+def test_batch_same_as_alone(precision, share, products):
+    """Each swimmer in a batch of one with its products on its own launches
+    (the reference result), in a batch of one and in a batch of three with
+    inner solves and pair products shared or not: the same state, bit for
+    bit. FP64 swimmers also match a stepper outside any batch."""
     from timfilsimmod_gb300.serving import SwimmerBatch
 
     steps = 3
-    alone = []
-    for subdiv, nfil in SHAPES:
-        s, st = make_instance(subdiv, nfil, precision)
-        one = SwimmerBatch(num_workers=1)
-        one.share_inner_solves(share)
-        one.add(st)
-        for nt in range(steps):
-            one.step(nt, allow_unconverged=True)
-        if share is True:
-            sh = one.shared_solves()
-            assert sh["solves"] > 0 and sh["launches"] == sh["solves"], sh
-        alone.append(st.state())
-        one.close()
-        st.close()
-        s.finalise()
+
+    def one_by_one(share_products):
+        res = []
+        for subdiv, nfil in SHAPES:
+            s, st = make_instance(subdiv, nfil, precision)
+            one = SwimmerBatch(num_workers=1)
+            one.share_inner_solves(share)
+            one.share_products(share_products)
+            one.add(st)
+            for nt in range(steps):
+                one.step(nt, allow_unconverged=True)
+            if share is True:
+                sh = one.shared_solves()
+                assert sh["solves"] > 0 and sh["launches"] == sh["solves"], sh
+            sp = one.shared_products()
+            assert (sp["products"] > 0) == share_products, sp
+            res.append(st.state())
+            one.close()
+            st.close()
+            s.finalise()
+        return res
+
+    alone = one_by_one(False)
+    for got, ref in zip(one_by_one(products), alone):
+        for k in ("x", "q", "lam", "body_x", "body_q"):
+            assert np.array_equal(got[k], ref[k]), ("batch of one", k)
+    if precision == "fp64":  # the FP32C inner solve takes another form outside a batch
+        for (subdiv, nfil), ref in zip(SHAPES, alone):
+            s, st = make_instance(subdiv, nfil, precision)
+            for nt in range(steps):
+                st.step(nt, allow_unconverged=True)
+            got = st.state()
+            for k in ("x", "q", "lam", "body_x", "body_q"):
+                assert np.array_equal(got[k], ref[k]), ("outside a batch", k)
+            st.close()
+            s.finalise()
     inst = [make_instance(subdiv, nfil, precision) for subdiv, nfil in SHAPES]
     batch = SwimmerBatch(num_workers=3)
     batch.share_inner_solves(share)
+    batch.share_products(products)
     for _, st in inst:
         batch.add(st)
     for nt in range(steps):
@@ -81,6 +108,11 @@ def test_batch_same_as_alone(precision, share):
         assert sh["solves"] > 0 and 0 < sh["launches"] <= sh["solves"], sh
     else:
         assert sh == {"launches": 0, "solves": 0}
+    sp = batch.shared_products()
+    if products:
+        assert sp["products"] > 0 and 0 < sp["launches"] <= sp["products"], sp
+    else:
+        assert sp == {"launches": 0, "products": 0}
     for (s, st), ref in zip(inst, alone):
         got = st.state()
         for k in ("x", "q", "lam", "body_x", "body_q"):

@@ -180,6 +180,8 @@ _SIGNATURES = {
     "tfs_batch_size": [_H, _IP],
     "tfs_batch_share_inner_solves": [_H, ctypes.c_int],
     "tfs_batch_shared_solves": [_H, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
+    "tfs_batch_share_products": [_H, ctypes.c_int],
+    "tfs_batch_shared_products": [_H, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "tfs_batch_step": [_H, ctypes.c_int, _P, _P, _P],
     "tfs_server_config_default": [ctypes.POINTER(ServerConfig)],
     "tfs_server_create": [ctypes.POINTER(ServerConfig), ctypes.POINTER(_H)],
@@ -190,6 +192,7 @@ _SIGNATURES = {
     "tfs_server_drain": [_H],
     "tfs_server_stats": [_H, ctypes.POINTER(ServerCounters)],
     "tfs_server_shared_solves": [_H, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
+    "tfs_server_shared_products": [_H, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "tfs_server_destroy": [_H],
     "tfs_last_error": [],
     "tfs_kernel_launch_count": [],

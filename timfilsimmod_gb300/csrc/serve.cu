@@ -118,7 +118,12 @@ struct tfs_batch {
   std::vector<int> shared_ctas;  // CTAs of its solve in a shared launch
   tfs::GmresService *service = nullptr;
   int share_max_ctas = -1;  // -1: every solve the persistent kernel can take
-  ~tfs_batch() { tfs::service_destroy(service); }
+  tfs::ProductService *pservice = nullptr;  // shared work-queue launches of the products
+  bool share_products = true;
+  ~tfs_batch() {
+    tfs::service_destroy(service);
+    tfs::product_service_destroy(pservice);
+  }
 };
 
 extern "C" {
@@ -158,6 +163,10 @@ int tfs_batch_add(tfs_batch *b, tfs_stepper *st, int *index) {
     else if (rc != TFS_ESTATE) return rc;
     if ((rc = tfs_set_persistent_gmres(s, 0)) != TFS_OK) return rc;
   }
+  if (b->pservice == nullptr && (b->pservice = tfs::product_service_create()) == nullptr)
+    return fail(TFS_ECUDA, "product service creation failed");
+  int prc = tfs::product_service_attach(b->pservice, s);
+  if (prc != TFS_OK) return prc;
   b->inst.push_back(st);
   b->shared.push_back(shared);
   b->shared_ctas.push_back(shared ? s->pg_group.P : 0);
@@ -174,6 +183,20 @@ int tfs_batch_size(tfs_batch *b, int *n) {
 int tfs_batch_share_inner_solves(tfs_batch *b, int max_ctas) {
   if (b == nullptr) return fail(TFS_EINVAL, "null batch");
   b->share_max_ctas = max_ctas < 0 ? -1 : max_ctas;
+  return TFS_OK;
+}
+
+int tfs_batch_share_products(tfs_batch *b, int enable) {
+  if (b == nullptr) return fail(TFS_EINVAL, "null batch");
+  b->share_products = enable != 0;
+  return TFS_OK;
+}
+
+int tfs_batch_shared_products(tfs_batch *b, long long *launches, long long *products) {
+  if (b == nullptr) return fail(TFS_EINVAL, "null batch");
+  if (launches) *launches = 0;
+  if (products) *products = 0;
+  if (b->pservice) tfs::product_service_stats(b->pservice, launches, products);
   return TFS_OK;
 }
 
@@ -194,14 +217,19 @@ int tfs_batch_step(tfs_batch *b, int nt, int *broyden_iters, int *gmres_iters, i
     return tfs::stepper_segments(b->inst[x]) > tfs::stepper_segments(b->inst[y]);
   });
   const int cap = b->share_max_ctas >= 0 ? b->share_max_ctas : tfs::num_sms();
-  for (int i = 0; i < n; ++i)
+  for (int i = 0; i < n; ++i) {
     if (b->shared[i] && b->shared_ctas[i] <= cap)
       tfs::stepper_solver(b->inst[i])->service = b->service;
+    if (b->share_products) tfs::stepper_solver(b->inst[i])->product_service = b->pservice;
+  }
   b->pool->run(n, [&](int k) {
     const int i = order[k];
     rc[i] = tfs_stepper_step(b->inst[i], nt, &bi[i], &gi[i]);
   });
-  for (int i = 0; i < n; ++i) tfs::stepper_solver(b->inst[i])->service = nullptr;
+  for (int i = 0; i < n; ++i) {
+    tfs::stepper_solver(b->inst[i])->service = nullptr;
+    tfs::stepper_solver(b->inst[i])->product_service = nullptr;
+  }
   int first = TFS_OK;
   for (int i = 0; i < n; ++i) {
     if (broyden_iters) broyden_iters[i] = bi[i];
@@ -289,6 +317,7 @@ struct tfs_server {
   bool stop = false;
   std::vector<std::thread> workers;
   tfs::GmresService *service = nullptr;  // shared inner solves of FP32C instances
+  tfs::ProductService *pservice = nullptr;  // shared work-queue launches of the products
   Clock::time_point t0 = Clock::now();
 
   void worker();
@@ -311,6 +340,8 @@ int tfs_server::build(Instance *in, const tfs_request &r) {
     if (rc != TFS_OK && rc != TFS_ESTATE) return rc;
     if ((rc = tfs_set_persistent_gmres(in->s, 0)) != TFS_OK) return rc;
   }
+  if ((rc = tfs::product_service_attach(pservice, in->s)) != TFS_OK) return rc;
+  in->s->product_service = pservice;
   if ((rc = tfs_set_blob_references(in->s, r.blob_refs)) != TFS_OK) return rc;
   tfs_step_config sc = cfg.step;
   sc.nfil = r.nfil;
@@ -482,6 +513,11 @@ int tfs_server_create(const tfs_server_config *cfg, tfs_server **out) {
     delete sv;
     return fail(TFS_ECUDA, "GMRES service creation failed");
   }
+  if ((sv->pservice = tfs::product_service_create()) == nullptr) {
+    tfs::service_destroy(sv->service);
+    delete sv;
+    return fail(TFS_ECUDA, "product service creation failed");
+  }
   for (int i = 0; i < cfg->num_workers; ++i) sv->workers.emplace_back([sv] { sv->worker(); });
   *out = sv;
   return TFS_OK;
@@ -576,6 +612,14 @@ int tfs_server_shared_solves(tfs_server *sv, long long *launches, long long *sol
   return TFS_OK;
 }
 
+int tfs_server_shared_products(tfs_server *sv, long long *launches, long long *products) {
+  if (sv == nullptr) return fail(TFS_EINVAL, "null server");
+  if (launches) *launches = 0;
+  if (products) *products = 0;
+  if (sv->pservice) tfs::product_service_stats(sv->pservice, launches, products);
+  return TFS_OK;
+}
+
 int tfs_server_destroy(tfs_server *sv) {
   if (sv == nullptr) return TFS_OK;
   {
@@ -587,6 +631,7 @@ int tfs_server_destroy(tfs_server *sv) {
   for (auto &t : sv->workers) t.join();
   for (Instance *in : sv->pool) destroy_instance(in);
   tfs::service_destroy(sv->service);
+  tfs::product_service_destroy(sv->pservice);
   delete sv;
   return TFS_OK;
 }

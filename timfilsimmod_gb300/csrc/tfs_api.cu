@@ -89,6 +89,8 @@ static cudaEvent_t *next_events(tfs_solver *s) {
 static void free_all(tfs_solver *s) {
   for (cudaEvent_t e : s->events) cudaEventDestroy(e);
   s->events.clear();
+  if (s->pready_ev) cudaEventDestroy(s->pready_ev);
+  if (s->pdone_ev) cudaEventDestroy(s->pdone_ev);
   solve_free(s);
   cudaFree(s->x_segs);
   cudaFree(s->f_segs);
@@ -244,6 +246,8 @@ int tfs::queue_product(tfs_solver *s, int kind) {
     e = launch_pack(fp32, 3, s->rec_blobs, s->x_blobs, s->f_blobs, s->nb, s->origin, s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "pack kernel");
   }
+  if (s->product_service != nullptr)  // one launch shared with other swimmers' products
+    return product_service_run(s->product_service, s, kind, fp32, src);
   e = launch_queue(fp32, s->qtune[fp32][kind], src, s->qjobs_dev + 2 * kind, s->qjobs[kind],
                    s->qjobs_n[kind], s->qcount, s->stream, next_events(s));
   if (e != cudaSuccess) return cuda_fail(e, "RPY work-queue kernel");

@@ -14,6 +14,7 @@
 
 namespace tfs {
 struct GmresService;
+struct ProductService;
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 long long launch_count();
@@ -91,6 +92,11 @@ struct tfs_solver {
   tfs::QueueJob *qjobs_dev = nullptr;  // [kNumQueueKinds][2]
   unsigned *qcount = nullptr;          // [2] launch counters, then arrival counters
   int qtune[2][tfs::kNumQueueKinds] = {};
+  // products shared with other swimmers' (one work-queue launch for all that
+  // are waiting): the service, and events marking this swimmer's records
+  // ready and its product done
+  tfs::ProductService *product_service = nullptr;
+  cudaEvent_t pready_ev = nullptr, pdone_ev = nullptr;
   // launch tuning per precision and (target, source-set) combination
   tfs::TileTuning tune[2][tfs::kNumCombos];
   std::string tuning_report = "{}";
@@ -139,4 +145,11 @@ GmresService *service_create();
 void service_destroy(GmresService *sv);
 int service_attach(GmresService *sv, tfs_solver *s);  // TFS_ESTATE if the kernel cannot serve s
 void service_stats(GmresService *sv, long long *launches, long long *solves);
+// Pair products of many swimmers batched into shared work-queue launches
+// (product_service.cu).
+ProductService *product_service_create();
+void product_service_destroy(ProductService *sv);
+int product_service_attach(ProductService *sv, tfs_solver *s);
+int product_service_run(ProductService *sv, tfs_solver *s, int kind, int fp32, int src);
+void product_service_stats(ProductService *sv, long long *launches, long long *products);
 }  // namespace tfs

@@ -62,6 +62,17 @@ class SwimmerBatch:
         N.check(self.lib.tfs_batch_shared_solves(self._h, ctypes.byref(la), ctypes.byref(so)))
         return {"launches": la.value, "solves": so.value}
 
+    def share_products(self, enable: bool = True) -> None:
+        """Whether the swimmers' pair products share work-queue launches
+        (default on)."""
+        N.check(self.lib.tfs_batch_share_products(self._h, int(bool(enable))))
+
+    def shared_products(self) -> dict:
+        """Products run in shared work-queue launches, and the launches."""
+        la, pr = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        N.check(self.lib.tfs_batch_shared_products(self._h, ctypes.byref(la), ctypes.byref(pr)))
+        return {"launches": la.value, "products": pr.value}
+
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
             self.lib.tfs_batch_destroy(self._h)
@@ -161,6 +172,12 @@ class StepServer:
         la, so = ctypes.c_longlong(0), ctypes.c_longlong(0)
         N.check(self.lib.tfs_server_shared_solves(self._h, ctypes.byref(la), ctypes.byref(so)))
         return {"launches": la.value, "solves": so.value}
+
+    def shared_products(self) -> dict:
+        """Products run in shared work-queue launches, and the launches."""
+        la, pr = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        N.check(self.lib.tfs_server_shared_products(self._h, ctypes.byref(la), ctypes.byref(pr)))
+        return {"launches": la.value, "products": pr.value}
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
