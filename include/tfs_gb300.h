@@ -101,6 +101,19 @@ int tfs_copy_blob_forces_to_device(tfs_solver *s, const double *f_blobs_host);  
 int tfs_copy_interparticle_blob_forces_to_host(tfs_solver *s, double *f_blobs_repulsion_host); /* :163-175 */
 int tfs_copy_blob_velocities_to_host(tfs_solver *s, double *v_blobs_host);           /* :177-189 */
 int tfs_copy_segment_velocities_to_host(tfs_solver *s, double *v_segs_host);         /* :191-205 */
+/* The same seven copies for host arrays of float, the reference's Real in its
+ * shipped configuration (config.hpp:53, FIL_USE_DOUBLE_PRECISION false;
+ * rpy_mobility_solver.cu:54-71 allocates Real host arrays): the floats cross
+ * the bus as floats and are converted to or from the solver's float64
+ * device arrays on the device, on the solver's stream (a float staging
+ * buffer of the largest array is allocated on the first such call). */
+int tfs_copy_segment_positions_to_device_f32(tfs_solver *s, const float *x_segs_host);
+int tfs_copy_segment_forces_to_device_f32(tfs_solver *s, const float *f_segs_host);
+int tfs_copy_blob_positions_to_device_f32(tfs_solver *s, const float *x_blobs_host);
+int tfs_copy_blob_forces_to_device_f32(tfs_solver *s, const float *f_blobs_host);
+int tfs_copy_interparticle_blob_forces_to_host_f32(tfs_solver *s, float *f_blobs_repulsion_host);
+int tfs_copy_blob_velocities_to_host_f32(tfs_solver *s, float *v_blobs_host);
+int tfs_copy_segment_velocities_to_host_f32(tfs_solver *s, float *v_segs_host);
 /* barrier_forces: adds segment repulsion into the device f_segs and writes
  * the blob repulsion (free body) (rpy_mobility_solver.cu:207-245,
  * cuda_functions.cu:1240-1436). */
@@ -196,6 +209,7 @@ int tfs_get_body_velocities(tfs_solver *s, double *v_bodies);
 int tfs_set_body_velocities(tfs_solver *s, const double *v_bodies);
 /* The solved blob forces (f_blobs_host after the reference's GMRES). */
 int tfs_copy_blob_forces_to_host(tfs_solver *s, double *f_blobs_host);
+int tfs_copy_blob_forces_to_host_f32(tfs_solver *s, float *f_blobs_host);
 /* Iterations (summed over refinement cycles), refinement cycles and final
  * relative residual of the last solve. FP32C: a refinement cycle that does
  * not reduce the FP64 residual ends the refinement and the solve finishes as

@@ -417,3 +417,51 @@ def test_one_sided_and_empty_systems(precision, nfil, nblob):
         # no segments: Mbs assigns zero
         assert np.all(out["v_mbs"] == 0.0)
         assert cmp(vb, ref_bb) < tol
+
+
+def test_float_host_arrays_match_float64_path():
+    """The float host-array copies (the reference's Real = float build):
+    positions and forces given as float32, velocities and the blob repulsion
+    read back as float32, equal bit for bit to the float32 rounding of the
+    float64 path on the same (float32-representable) inputs."""
+    import ctypes
+
+    d = load("small_matvec")
+    xs, fs = d["x_segs"].astype(np.float32), d["f_segs"].astype(np.float32)
+    xb, fb = d["x_blobs"].astype(np.float32), d["f_blobs"].astype(np.float32)
+    ns, nb = xs.shape[0], xb.shape[0]
+
+    def p(a):
+        return ctypes.c_void_p(a.ctypes.data)
+
+    s64 = make_solver(ns, nb, int(d["nseg"]))
+    s64.set_state(xs, fs, xb, fb)
+    s64.apply_interparticle_forces()
+    s64.evaluate_segment_segment_mobility()
+    s64.evaluate_segment_blob_mobility()
+    s64.evaluate_blob_segment_mobility()
+    s64.copy_segment_velocities_to_host()
+    s64.copy_blob_velocities_to_host()
+    s64.copy_interparticle_blob_forces_to_host()
+    s64.wait_for_device()
+    want = [s64.v_segs_host.copy(), s64.v_blobs_host.copy(), s64.f_blobs_repulsion_host.copy()]
+    s64.finalise()
+
+    s = make_solver(ns, nb, int(d["nseg"]))
+    xs_, fs_, xb_, fb_ = (np.ascontiguousarray(a.ravel()) for a in (xs, fs, xb, fb))
+    s._call("tfs_copy_segment_positions_to_device_f32", p(xs_))
+    s._call("tfs_copy_segment_forces_to_device_f32", p(fs_))
+    s._call("tfs_copy_blob_positions_to_device_f32", p(xb_))
+    s._call("tfs_copy_blob_forces_to_device_f32", p(fb_))
+    s.apply_interparticle_forces()
+    s.evaluate_segment_segment_mobility()
+    s.evaluate_segment_blob_mobility()
+    s.evaluate_blob_segment_mobility()
+    got = [np.empty(6 * ns, np.float32), np.empty(3 * nb, np.float32), np.empty(3 * nb, np.float32)]
+    s._call("tfs_copy_segment_velocities_to_host_f32", p(got[0]))
+    s._call("tfs_copy_blob_velocities_to_host_f32", p(got[1]))
+    s._call("tfs_copy_interparticle_blob_forces_to_host_f32", p(got[2]))
+    s.wait_for_device()
+    s.finalise()
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w.astype(np.float32))

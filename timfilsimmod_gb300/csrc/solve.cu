@@ -900,6 +900,11 @@ int tfs_copy_blob_forces_to_host(tfs_solver *s, double *f_blobs_host) {
   return TFS_OK;
 }
 
+int tfs_copy_blob_forces_to_host_f32(tfs_solver *s, float *f_blobs_host) {
+  TFS_CHECK_SOLVER(s);
+  return d2h_f32(s, f_blobs_host, s->f_blobs, 3 * (size_t)s->nb, "copy blob forces to host");
+}
+
 int tfs_solve_info(tfs_solver *s, int *iters, int *cycles, double *rel_residual) {
   TFS_CHECK_SOLVER(s);
   if (iters) *iters = s->last_iters;

@@ -110,6 +110,7 @@ static void free_all(tfs_solver *s) {
   cudaFree(s->wc_z);
   cudaFree(s->wc_f);
   cudaFree(s->scratch);
+  cudaFree(s->stage32);
   cudaFree(s->qjobs_dev);
   cudaFree(s->qcount);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -452,6 +453,83 @@ static int d2h(tfs_solver *s, double *dst, const double *src, size_t n, const ch
   if (dst == nullptr) return fail(TFS_EINVAL, "%s: null host pointer", what);
   TFS_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream), what);
   return TFS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+__global__ void widen_kernel(double *__restrict__ dst, const float *__restrict__ src, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (double)src[i];
+}
+__global__ void narrow_kernel(float *__restrict__ dst, const double *__restrict__ src, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+int ensure_stage32(tfs_solver *s) {
+  if (s->stage32 != nullptr) return TFS_OK;
+  return alloc_dev((void **)&s->stage32,
+                   sizeof(float) * std::max<size_t>(6 * (size_t)s->ns, 3 * (size_t)s->nb));
+}
+}  // namespace
+
+int tfs::h2d_f32(tfs_solver *s, double *dst, const float *src, size_t n, const char *what) {
+  if (n == 0) return TFS_OK;
+  if (src == nullptr) return fail(TFS_EINVAL, "%s: null host pointer", what);
+  int rc = ensure_stage32(s);
+  if (rc != TFS_OK) return rc;
+  TFS_CUDA(cudaMemcpyAsync(s->stage32, src, n * sizeof(float), cudaMemcpyHostToDevice, s->stream),
+           what);
+  widen_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(dst, s->stage32, n);
+  count_launch();
+  TFS_CUDA(cudaGetLastError(), what);
+  return TFS_OK;
+}
+
+int tfs::d2h_f32(tfs_solver *s, float *dst, const double *src, size_t n, const char *what) {
+  if (n == 0) return TFS_OK;
+  if (dst == nullptr) return fail(TFS_EINVAL, "%s: null host pointer", what);
+  int rc = ensure_stage32(s);
+  if (rc != TFS_OK) return rc;
+  narrow_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(s->stage32, src, n);
+  count_launch();
+  TFS_CUDA(cudaGetLastError(), what);
+  TFS_CUDA(cudaMemcpyAsync(dst, s->stage32, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream),
+           what);
+  return TFS_OK;
+}
+
+extern "C" {
+
+int tfs_copy_segment_positions_to_device_f32(tfs_solver *s, const float *x) {
+  TFS_CHECK_SOLVER(s);
+  s->origin_dirty = true;
+  return h2d_f32(s, s->x_segs, x, 3 * (size_t)s->ns, "copy_segment_positions_to_device");
+}
+int tfs_copy_segment_forces_to_device_f32(tfs_solver *s, const float *f) {
+  TFS_CHECK_SOLVER(s);
+  return h2d_f32(s, s->f_segs, f, 6 * (size_t)s->ns, "copy_segment_forces_to_device");
+}
+int tfs_copy_blob_positions_to_device_f32(tfs_solver *s, const float *x) {
+  TFS_CHECK_SOLVER(s);
+  s->origin_dirty = true;
+  return h2d_f32(s, s->x_blobs, x, 3 * (size_t)s->nb, "copy_blob_positions_to_device");
+}
+int tfs_copy_blob_forces_to_device_f32(tfs_solver *s, const float *f) {
+  TFS_CHECK_SOLVER(s);
+  return h2d_f32(s, s->f_blobs, f, 3 * (size_t)s->nb, "copy_blob_forces_to_device");
+}
+int tfs_copy_interparticle_blob_forces_to_host_f32(tfs_solver *s, float *f) {
+  TFS_CHECK_SOLVER(s);
+  return d2h_f32(s, f, s->f_rep, 3 * (size_t)s->nb, "copy_interparticle_blob_forces_to_host");
+}
+int tfs_copy_blob_velocities_to_host_f32(tfs_solver *s, float *v) {
+  TFS_CHECK_SOLVER(s);
+  return d2h_f32(s, v, s->v_blobs, 3 * (size_t)s->nb, "copy_blob_velocities_to_host");
+}
+int tfs_copy_segment_velocities_to_host_f32(tfs_solver *s, float *v) {
+  TFS_CHECK_SOLVER(s);
+  return d2h_f32(s, v, s->v_segs, 6 * (size_t)s->ns, "copy_segment_velocities_to_host");
 }
 
 int tfs_copy_segment_positions_to_device(tfs_solver *s, const double *x) {

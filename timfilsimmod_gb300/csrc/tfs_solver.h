@@ -37,6 +37,7 @@ struct tfs_solver {
   double *wc_z = nullptr, *wc_f = nullptr;  // weakly coupled filaments: means, total forces
   double *scratch = nullptr;
   size_t scratch_elems = 0;
+  float *stage32 = nullptr;  // float host-array copies: staging of the largest array
   bool origin_dirty = true;
 
   // --- free-body solve (solve.cu) ---
@@ -137,6 +138,10 @@ TileArgs base_args(tfs_solver *s);
 int product(tfs_solver *s, bool tgt_segs, bool src_segs, bool src_blobs, int mode);
 // One work-queue launch of the given kind (QueueKind) on the solver's stream.
 int queue_product(tfs_solver *s, int kind);
+// Float host arrays: copy n floats to (from) a float64 device array,
+// converting on the device through the solver's float staging buffer.
+int h2d_f32(tfs_solver *s, double *dst, const float *src, size_t n, const char *what);
+int d2h_f32(tfs_solver *s, float *dst, const double *src, size_t n, const char *what);
 int alloc_dev(void **p, size_t bytes);
 int solve_alloc(tfs_solver *s);
 void solve_free(tfs_solver *s);
