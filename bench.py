@@ -724,6 +724,26 @@ def serve_bench(args):
                            "p50_ms": float(np.percentile(lat, 50)),
                            "p99_ms": float(np.percentile(lat, 99)), "requests": nreq,
                            "by_size": buckets}
+    # orbit-search requests: four Newton-Krylov searches at once (the client
+    # of timfilsimmod_gb300.orbit: one Newton iteration each, GMRES(4), a
+    # period of 2 steps, every period map one request) on a 128-filament base
+    from timfilsimmod_gb300.orbit import OrbitSearch, search_many
+
+    nf_o = 128
+    bo, fo, do, ro = elastic_swimmer(nf_o)
+    searches = [OrbitSearch(sv, bo, fo, do, 20, num_steps=2, body_radius=ro, eps_j=1e-2)
+                for _ in range(4)]
+    starts = [0.01 * np.random.default_rng(90 + k).normal(size=3 * nf_o * 20) for k in range(4)]
+    t0 = time.perf_counter()
+    recs = search_many(searches, starts, m=4, iters=1)
+    sec = time.perf_counter() - t0
+    lat = np.concatenate([np.array(o.latencies_ms) for o in searches])
+    nreq_o = int(sum(o.requests for o in searches))
+    orbit = {"workload": f"4 concurrent Newton-Krylov searches on a {nf_o * 20}-segment swimmer "
+                         "(GMRES(4), one Newton iteration, period = 2 steps, eps_j 1e-2)",
+             "requests": nreq_o, "requests_per_s": nreq_o / sec, "seconds": sec,
+             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+             "residual_norms": [[float(f"{v:.4e}") for v in r["residual"]] for r in recs]}
     stats = sv.stats()
     shared = sv.shared_solves()
     shared_products = sv.shared_products()
@@ -746,6 +766,7 @@ def serve_bench(args):
                              "resident_instances": stats["resident_instances"],
                              "created": stats["created"], "reused": stats["reused"],
                              "shared_inner_solves": shared, "shared_products": shared_products},
+            "orbit_search": orbit,
             "fp64_one_at_a_time": base,
             "speedup_best_rate_vs_fp64": best / base["steps_per_s"]}
 

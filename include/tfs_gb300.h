@@ -398,8 +398,9 @@ int tfs_batch_shared_products(tfs_batch *b, long long *launches, long long *prod
  * given by its geometry (blob references, filament bases and directions;
  * all arrays must stay valid until the request completes) from the
  * straight start, each segment turned by seg_rotation (3 Ns, may be NULL)
- * as in tfs_stepper_reset. Results: x_out[3 Ns] segment positions and
- * body_out[7] = body x, q (either may be NULL). */
+ * as in tfs_stepper_reset. Results: x_out[3 Ns] segment positions,
+ * body_out[7] = body x, q and q_out[4 Ns] segment orientations (any may be
+ * NULL). */
 typedef struct tfs_request {
   int nfil, nseg, nblob;
   const double *blob_refs, *fil_refs, *fil_dirs;
@@ -407,6 +408,7 @@ typedef struct tfs_request {
   const double *seg_rotation;
   int num_steps;
   double *x_out, *body_out;
+  double *q_out;
 } tfs_request;
 typedef struct tfs_server_config {
   int num_workers;            /* requests in flight at once */

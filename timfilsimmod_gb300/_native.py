@@ -63,7 +63,7 @@ class Request(ctypes.Structure):
                 ("fil_dirs", ctypes.c_void_p), ("body_radius", ctypes.c_double),
                 ("seg_rotation", ctypes.c_void_p),
                 ("num_steps", ctypes.c_int), ("x_out", ctypes.c_void_p),
-                ("body_out", ctypes.c_void_p)]
+                ("body_out", ctypes.c_void_p), ("q_out", ctypes.c_void_p)]
 
 
 class ServerConfig(ctypes.Structure):

@@ -451,7 +451,7 @@ void tfs_server::worker() {
     // stops there (cilia_sim_main.cu:542-557); the state so far is returned
     const bool unconverged = rc == TFS_ENOTCONV;
     if (rc == TFS_OK || unconverged) {
-      const int rs = tfs_stepper_state(in->st, q->r.x_out, nullptr, nullptr, nullptr, nullptr,
+      const int rs = tfs_stepper_state(in->st, q->r.x_out, q->r.q_out, nullptr, nullptr, nullptr,
                                        nullptr, q->r.body_out,
                                        q->r.body_out ? q->r.body_out + 3 : nullptr, nullptr);
       if (rs != TFS_OK) rc = rs;

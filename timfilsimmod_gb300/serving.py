@@ -124,15 +124,17 @@ class StepServer:
         if rot is not None and rot.size != 3 * nfil * nseg:
             raise ValueError("seg_rotation needs 3 values per segment")
         x = np.zeros(3 * nfil * nseg)
+        q = np.zeros(4 * nfil * nseg)
         body = np.zeros(7)
         r = N.Request(nfil=nfil, nseg=int(nseg), nblob=nblob, blob_refs=br.ctypes.data,
                       fil_refs=fr.ctypes.data, fil_dirs=fd.ctypes.data,
                       body_radius=float(body_radius),
                       seg_rotation=None if rot is None else rot.ctypes.data,
-                      num_steps=int(num_steps), x_out=x.ctypes.data, body_out=body.ctypes.data)
+                      num_steps=int(num_steps), x_out=x.ctypes.data, body_out=body.ctypes.data,
+                      q_out=q.ctypes.data)
         t = ctypes.c_longlong(0)
         N.check(self.lib.tfs_server_submit(self._h, ctypes.byref(r), ctypes.byref(t)))
-        self._live[t.value] = (br, fr, fd, rot, x, body)
+        self._live[t.value] = (br, fr, fd, rot, x, body, q)
         return t.value
 
     def request_bytes(self, blob_refs, fil_refs, fil_dirs, nseg: int) -> int:
@@ -145,7 +147,7 @@ class StepServer:
         return b.value
 
     def poll(self, ticket: int, wait: bool = False) -> dict | None:
-        """None while pending; else the result (x, body, latency_ms, counts).
+        """None while pending; else the result (x, body, q, latency_ms, counts).
         A failed request raises."""
         st, lat = ctypes.c_int(0), ctypes.c_double(0.0)
         b, g = ctypes.c_int(0), ctypes.c_int(0)
@@ -157,7 +159,7 @@ class StepServer:
         arrays = self._live.pop(ticket)
         if st.value != N.TFS_OK:
             raise N.TfsError(st.value, self.lib.tfs_last_error().decode(errors="replace"))
-        return {"x": arrays[4], "body": arrays[5], "latency_ms": lat.value,
+        return {"x": arrays[4], "body": arrays[5], "q": arrays[6], "latency_ms": lat.value,
                 "broyden_iters": b.value, "gmres_iters": g.value}
 
     def drain(self) -> None:
