@@ -66,10 +66,10 @@ def grand_flops(ns, nb):
 
 
 def queue_bytes(ns, nb):
-    """Algorithmic bytes of one FP32C grand-mobility launch: the source
-    records read (48 B per segment, 32 B per blob), the FP64 target positions
-    read and the FP64 velocities written."""
-    return 48 * ns + 32 * nb + 24 * (ns + nb) + 8 * (6 * ns + 3 * nb)
+    """Algorithmic bytes of one FP32C grand-mobility launch: the records read
+    (48 B per segment, 32 B per blob; the targets' positions come from the
+    same records) and the FP64 velocities written."""
+    return 48 * ns + 32 * nb + 8 * (6 * ns + 3 * nb)
 
 
 def grand_pairs(ns, nb):
@@ -143,7 +143,7 @@ class ClockSampler:
 # rpy_tile_kernel<float,6,6,3,128,1,256,8>, medium swimmer): 1 043 200 + 0.
 # DRAM bytes per launch of the grand-mobility work-queue launch (dram__bytes_read.sum +
 # dram__bytes_write.sum, one ncu capture of this workload); None until captured
-QUEUE_TRAFFIC = {}
+QUEUE_TRAFFIC = {"medium": 795392}
 
 
 def max_over_ranks(values, world: int, device: str):
@@ -354,10 +354,11 @@ def bench_ours(args):
                          "algorithmic_bytes": queue_bytes(ns, nb),
                          "traffic_note": "bytes per launch, dram__bytes_read.sum + "
                                          "dram__bytes_write.sum of one ncu capture of the "
-                                         "tuned grand-mobility launch on this workload; "
-                                         "algorithmic bytes: FP32 source records, FP64 "
-                                         "target positions and velocities (the chunk "
-                                         "partial sums stay in L2)"},
+                                         "grand-mobility launch on this workload "
+                                         "(profiles/rpy_queue_f32_grand_medium.md); "
+                                         "algorithmic bytes: FP32 records read, FP64 "
+                                         "velocities written (the written velocities and "
+                                         "the chunk partial sums stay in L2)"},
             "fp64": {"value": value64, "unit": "matvecs/s", "steps": steps64,
                      "roofline": {"bound": "fp64-fma", "achieved": achieved64,
                                   "peak": peak64 / 1e12, "unit": "TFLOP/s",
