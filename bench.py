@@ -987,6 +987,56 @@ def bench_config(config, ns, nb, world):
             "parallelism": f"replicas x{world}"}
 
 
+def reference_gpu_leg(sw, reps64=3, reps32=10):
+    """The reference's own kernels on this GPU (oracle/ref_gpu.py: its
+    cuda_functions.cu compiled unchanged for sm_103a, launched as its
+    rpy_mobility_solver launches them): one grand matvec = Mss, Msb, Mbb,
+    Mbs (rpy_mobility_solver.cu:258-328), CUDA events around each kernel,
+    FP64 and its shipped FP32 build. None when the kernels were not built
+    here (they need the reference tree at build time)."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_gpu
+
+    if not torch.cuda.is_available() or not (ref_gpu.available("fp64") and ref_gpu.available("fp32")):
+        return None
+    ns, nb = sw.num_segs, sw.num_blobs
+    out = {"kernels": "cuda_functions.cu Mss/Msb/Mbb/Mbs_mult, 64 threads per CTA, one target "
+                      "per thread (the reference's launches)", "pairs_per_matvec": grand_pairs(ns, nb)}
+    for precision, reps in (("fp64", reps64), ("fp32", reps32)):
+        k = ref_gpu.RefGpuKernels(precision)
+        dt = k.dtype
+        t = {n: torch.tensor(np.asarray(a).ravel(), dtype=dt, device="cuda")
+             for n, a in (("xs", sw.x_segs), ("fs", sw.f_segs), ("xb", sw.x_blobs),
+                          ("fb", sw.f_blobs))}
+        vs = torch.zeros(6 * ns, dtype=dt, device="cuda")
+        vb = torch.zeros(3 * nb, dtype=dt, device="cuda")
+        k.sync(1, sw.nseg, sw.nfil, nb)
+        calls = [("Mss", lambda: k.mss(vs, t["fs"], t["xs"])),
+                 ("Msb", lambda: k.msb(vs, t["fb"], t["xs"], t["xb"])),
+                 ("Mbb", lambda: k.mbb(vb, t["fb"], t["xb"])),
+                 ("Mbs", lambda: k.mbs(vb, t["fs"], t["xb"], t["xs"]))]
+        for _, c in calls:  # warm-up
+            c()
+        torch.cuda.synchronize()
+        per = {n: 0.0 for n, _ in calls}
+        for _ in range(reps):
+            for n, c in calls:
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                c()
+                b.record()
+                torch.cuda.synchronize()
+                per[n] += a.elapsed_time(b)
+        ms = sum(per.values()) / reps
+        out[precision] = {"value": 1e3 / ms, "unit": "matvecs/s", "ms_per_matvec": ms,
+                          "ms_per_kernel": {n: v / reps for n, v in per.items()}, "reps": reps,
+                          "achieved_tflops": grand_flops(ns, nb) / (ms * 1e-3) / 1e12}
+        k.close()
+    return out
+
+
 def bench_reference(args):
     """Reference arm: the reference's RPY sums on the host cores."""
     world, rank, _ = dist_setup()
@@ -1012,7 +1062,7 @@ def bench_reference(args):
     value = args.steps * pairs / dt / grand_pairs(ns, nb)
     sample = (f"every {stride}th target of the full grand matvec per step ({pairs} pairs), "
               f"extrapolated by pair count")
-    return {
+    line = {
         "impl": "reference",
         "metric": "RPY grand-mobility matvecs/s (4 blocks, medium swimmer)",
         "value": value,
@@ -1035,6 +1085,10 @@ def bench_reference(args):
                 "(oracle/tfs_oracle.c, pinned bit-close to the reference's own kernels), "
                 "OpenMP over targets on the host cores",
     }
+    gpu = reference_gpu_leg(sw)
+    if gpu is not None:
+        line["reference_gpu"] = gpu
+    return line
 
 
 def main():
