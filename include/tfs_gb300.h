@@ -547,6 +547,14 @@ int tfs_measure_fma_peak(int precision, double *flops_per_second);
  * the reference (its unbounded pair takes 1/(sqrt(r^2) + 1e-20),
  * cuda_functions.cu:212-213). */
 int tfs_rsqrt_far(const double *x, double *y, int n, void *stream);
+/* Phase trace of the cooperative inner GMRES, for profiling: in a library
+ * built with -DTFS_PG_TRACE, the globaltimer stamps (ns) of thread 0 of its
+ * first two CTAs at eight points of every Arnoldi step of the last solve run,
+ * stamps[(cta * steps + k) * 8 + phase] (phases: step start, M_bb done, w
+ * formed, first-pass dots reduced, h1 summed, second-pass dots reduced, h2
+ * summed, Q_k and z_k done); *steps gets the steps the buffer holds.
+ * TFS_ESTATE in other builds. No counterpart in the reference. */
+int tfs_pg_trace(unsigned long long *stamps, int capacity, int *steps);
 
 #ifdef __cplusplus
 }

@@ -151,6 +151,7 @@ _SIGNATURES = {
                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
     "tfs_mss_noalloc": [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P],
     "tfs_rsqrt_far": [_P, _P, ctypes.c_int, _P],
+    "tfs_pg_trace": [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int)],
     "tfs_copy_segment_positions_to_device_f32": [_H, _P],
     "tfs_copy_segment_forces_to_device_f32": [_H, _P],
     "tfs_copy_blob_positions_to_device_f32": [_H, _P],

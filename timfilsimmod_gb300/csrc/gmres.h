@@ -96,6 +96,11 @@ constexpr size_t kPgAuxElems = 3 + 3 * 352;
 cudaError_t launch_gmres_persistent(const PgArgs *gp, const int2 *cmap, int ctas, size_t dyn_smem,
                                     cudaStream_t st);
 
+// The phase trace of the persistent GMRES (builds with -DTFS_PG_TRACE):
+// [2 CTAs][steps][8 phases] globaltimer stamps into out (capacity elements);
+// 0, or -1 (capacity too small), -2 (copy failed), -3 (not a trace build).
+int pg_trace_read(unsigned long long *out, int capacity, int *steps);
+
 // CTAs and blobs per CTA of the GMRES kernels for nb blobs on `sms` SMs.
 int gmres_grid(int nb, int sms, int *blobs_per_cta);
 cudaError_t launch_gmres_finish(const GmresArgs &a, cudaStream_t st);

@@ -81,6 +81,28 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
 
+// Phase trace of the Arnoldi steps (builds with -DTFS_PG_TRACE only):
+// globaltimer stamps of thread 0 of CTAs 0 and 1 at eight points of every
+// step k, [cta][k][phase]: 0 step start (M_bb begins; CTA 0 meanwhile runs
+// the Givens step), 1 after the barrier that ends M_bb, 2 w = A z formed,
+// 3 after the barrier of the first-pass dots, 4 h1 summed, 5 after the
+// barrier of the second-pass dots and partials, 6 h2 summed, 7 Q_k, z_k and
+// the records done (the step's last barrier follows). The last solve of a
+// launch leaves its trace; tfs_pg_trace reads it.
+#ifdef TFS_PG_TRACE
+constexpr int kTraceSteps = 352, kTracePhases = 8;
+__device__ unsigned long long g_pg_trace[2][kTraceSteps][kTracePhases];
+#define PG_STAMP(kk, ph)                                                   \
+  do {                                                                     \
+    if (p.rank < 2 && threadIdx.x == 0 && (kk) < kTraceSteps)              \
+      g_pg_trace[p.rank][(kk)][(ph)] = global_ns();                        \
+  } while (0)
+#else
+#define PG_STAMP(kk, ph) \
+  do {                   \
+  } while (0)
+#endif
+
 // Bounded grid barrier; false in every thread of the CTA if it was abandoned.
 // bar[0] counts arrivals over the whole launch (zeroed before it): the e-th
 // barrier of a solve is passed once it reaches e * P, so no CTA has to reset
@@ -817,6 +839,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
   int k = 1;
   double qn = 0.0;
   for (;;) {
+    PG_STAMP(k, 0);
     mbb_units(p, src);
     if (p.rank == 0 && k > 1) {
       // Givens rotation (mobility_solver.cpp:2370-2413) of step kk = k - 1
@@ -853,6 +876,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
       k -= 1;
       break;
     }
+    PG_STAMP(k, 1);
 
     // w = A z (slice rows; body rows w_vel = -sum (z ; d x z) in every CTA),
     // CGS pass 1 partial dots
@@ -897,8 +921,10 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
       apply_rows(p, sl, zv, ws, hb);
     }
     if (threadIdx.x < 6) wvel[threadIdx.x] = -tmp8[threadIdx.x];
+    PG_STAMP(k, 2);
     slice_dots(p, sl, ws, k, p.pd1, qres);
     if (!pg_barrier(p, &epoch)) return;
+    PG_STAMP(k, 3);
     // h1 (summed by every CTA while the partials fit the staging buffers,
     // else spread over the grid and published)
     if (!local_dots(p, p.pd1, k, wvel, qvres, h1, hb)) {
@@ -907,6 +933,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
       for (int i = threadIdx.x; i < k; i += kPB) h1[i] = ldcg(h1g + i);
       __syncthreads();
     }
+    PG_STAMP(k, 4);
 
     // w' = w - Q h1; CGS pass 2 partial dots, and ||w'||^2 and
     // sum (w' ; d x w') partials
@@ -915,12 +942,14 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     slice_dots(p, sl, ws, k, p.pd2, qres);
     slice_partials(p, sl, ws, K_W, S_NORM);
     if (!pg_barrier(p, &epoch)) return;
+    PG_STAMP(k, 5);
     if (!local_dots(p, p.pd2, k, wvel, qvres, h2, hb)) {
       reduce_dots(p, p.pd2, k, wvel, qvres, h2g);
       if (!pg_barrier(p, &epoch)) return;
       for (int i = threadIdx.x; i < k; i += kPB) h2[i] = ldcg(h2g + i);
       __syncthreads();
     }
+    PG_STAMP(k, 6);
 
     // w'' = w' - Q h2; with Q orthonormal, ||w''||^2 = ||w'||^2 - ||h2||^2
     // and sum (w'' ; d x w'') = sum (w' ; d x w') - sum_i h2_i S_i, S_i the
@@ -972,6 +1001,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     precond(p, sl, ws, qvel, wsum6, rqn, zs, zv, mats);
     pack_records(p, sl, zs);
     slice_partials(p, sl, zs, K_Z, -1);
+    PG_STAMP(k, 7);
     if (!pg_barrier(p, &epoch)) return;
     ++k;
   }
@@ -1060,6 +1090,20 @@ int pg_grid(int nb, int sms, int max_iter, PgShape *shape) {
   shape->Kr = Kr;
   shape->dyn_smem = dyn;
   return 1;
+}
+
+int pg_trace_read(unsigned long long *out, int capacity, int *steps) {
+#ifdef TFS_PG_TRACE
+  const int n = 2 * kTraceSteps * kTracePhases;
+  if (steps) *steps = kTraceSteps;
+  if (out == nullptr || capacity < n) return -1;
+  return cudaMemcpyFromSymbol(out, g_pg_trace, sizeof(unsigned long long) * n) == cudaSuccess ? 0 : -2;
+#else
+  (void)out;
+  (void)capacity;
+  if (steps) *steps = 0;
+  return -3;
+#endif
 }
 
 cudaError_t launch_gmres_persistent(const PgArgs *gp, const int2 *cmap, int ctas, size_t dyn_smem,

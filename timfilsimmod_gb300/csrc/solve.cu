@@ -900,6 +900,14 @@ int tfs_copy_blob_forces_to_host(tfs_solver *s, double *f_blobs_host) {
   return TFS_OK;
 }
 
+int tfs_pg_trace(unsigned long long *stamps, int capacity, int *steps) {
+  const int rc = pg_trace_read(stamps, capacity, steps);
+  if (rc == -3) return fail(TFS_ESTATE, "the library was built without TFS_PG_TRACE");
+  if (rc == -1) return fail(TFS_EINVAL, "capacity below 2 x steps x 8 stamps");
+  if (rc != 0) return fail(TFS_ECUDA, "reading the trace failed");
+  return TFS_OK;
+}
+
 int tfs_copy_blob_forces_to_host_f32(tfs_solver *s, float *f_blobs_host) {
   TFS_CHECK_SOLVER(s);
   return d2h_f32(s, f_blobs_host, s->f_blobs, 3 * (size_t)s->nb, "copy blob forces to host");

@@ -357,3 +357,36 @@ QUEUE_KINDS = ("seg<-seg", "blob<-seg", "seg,blob<-seg", "seg<-blob", "blob<-blo
 
 def kernel_launch_count() -> int:
     return int(N.load().tfs_kernel_launch_count())
+
+
+PG_TRACE_PHASES = ("M_bb + barrier", "w = A z", "pass-1 dots + barrier", "h1 sum",
+                   "w' + pass-2 dots + barrier", "h2 sum", "Q_k, z_k, records",
+                   "last barrier")
+
+
+def pg_trace() -> np.ndarray:
+    """The phase trace of the last cooperative inner GMRES solve, from a
+    library built with -DTFS_PG_TRACE: per-phase durations (ns) of every
+    Arnoldi step of that solve, shape (2 CTAs, steps, 8 phases), phases as
+    PG_TRACE_PHASES (each phase ends where the next begins; the last ends at
+    the next step's start). Raises TfsError in other builds."""
+    lib = N.load()
+    steps = ctypes.c_int()
+    lib.tfs_pg_trace(None, 0, ctypes.byref(steps))  # the capacity it needs
+    if steps.value <= 0:
+        N.check(lib.tfs_pg_trace(None, 0, ctypes.byref(steps)))
+    buf = np.zeros((2, steps.value, 8), dtype=np.uint64)
+    N.check(lib.tfs_pg_trace(buf.ctypes.data_as(ctypes.c_void_p), buf.size,
+                             ctypes.byref(steps)))
+    t = buf.astype(np.int64)
+    # steps of the last solve (or restart cycle): from step 1 while the
+    # starts keep increasing (later entries are left over from longer,
+    # earlier solves, so they start earlier)
+    n = 1
+    while n + 1 < t.shape[1] and t[0, n + 1, 0] > t[0, n, 0] and t[1, n + 1, 0] > t[1, n, 0]:
+        n += 1
+    # step n (the last) stopped after its M_bb phase; steps 1 .. n-1 are whole
+    if n < 2:
+        return np.zeros((2, 0, 8), dtype=np.int64)
+    ends = np.concatenate([t[:, 1:n, 1:], t[:, 2:n + 1, :1]], axis=2)
+    return ends - t[:, 1:n, :]

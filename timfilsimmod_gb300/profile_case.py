@@ -67,8 +67,29 @@ def run_steps(sw, args):
     s.wait_for_device()
     dt = time.perf_counter() - t0
     print(f"{args.reps} steps ({args.precision}, {args.config}): {dt * 1e3:.2f} ms")
+    if args.pg_trace:
+        print_pg_trace()
     st.close()
     s.finalise()
+
+
+def print_pg_trace():
+    """Median duration (us) of each phase of an Arnoldi step of the last
+    cooperative GMRES solve, as CTA 0 (which also runs the Givens step) and
+    CTA 1 saw it."""
+    import numpy as np
+
+    from .mobility import PG_TRACE_PHASES, pg_trace
+
+    d = pg_trace()
+    if d.shape[1] == 0:
+        print("pg trace: the last solve took fewer than two Arnoldi steps")
+        return
+    print(f"pg trace: {d.shape[1]} Arnoldi steps, median us per step (CTA 0 / CTA 1)")
+    for ph, name in enumerate(PG_TRACE_PHASES):
+        print(f"  {name:28s} {np.median(d[0, :, ph]) / 1e3:8.2f} {np.median(d[1, :, ph]) / 1e3:8.2f}")
+    tot = d.sum(axis=2)
+    print(f"  {'step':28s} {np.median(tot[0]) / 1e3:8.2f} {np.median(tot[1]) / 1e3:8.2f}")
 
 
 def main():
@@ -85,6 +106,9 @@ def main():
     p.add_argument("--queue-variant", type=int, default=None,
                    help="pin every work-queue product kind to this variant")
     p.add_argument("--autotune", action="store_true", help="print the autotuner's table")
+    p.add_argument("--pg-trace", action="store_true",
+                   help="print the phase table of the last cooperative GMRES solve (ops solve, "
+                        "step; needs a library built with -DTFS_PG_TRACE)")
     args = p.parse_args()
     sw = make_config(args.config, seed=1)
     if args.op == "flow":
@@ -135,6 +159,8 @@ def main():
     s.wait_for_device()
     dt = time.perf_counter() - t0
     print(f"{args.reps} x {args.op} ({args.precision}, {args.config}): {dt * 1e3:.2f} ms")
+    if args.pg_trace:
+        print_pg_trace()
     s.finalise()
 
 
