@@ -211,11 +211,17 @@ int tfs_set_body_velocities(tfs_solver *s, const double *v_bodies);
 int tfs_copy_blob_forces_to_host(tfs_solver *s, double *f_blobs_host);
 int tfs_copy_blob_forces_to_host_f32(tfs_solver *s, float *f_blobs_host);
 /* Iterations (summed over refinement cycles), refinement cycles and final
- * relative residual of the last solve. FP32C: a refinement cycle that does
- * not reduce the FP64 residual ends the refinement and the solve finishes as
- * plain FP64 GMRES from the caller's warm start; cycles is then negative
+ * relative residual of the last solve. FP32C: the cooperative inner solves
+ * keep their Arnoldi vectors in FP32 (FP64 during
+ * tfs_make_body_reference_matrices). A refinement cycle that does not reduce
+ * the FP64 residual ends the refinement; it is run again from the caller's
+ * warm start with FP64 Arnoldi vectors, and if that stalls too the solve
+ * finishes as plain FP64 GMRES from the warm start; cycles is then negative
  * (minus the cycles run before). */
 int tfs_solve_info(tfs_solver *s, int *iters, int *cycles, double *rel_residual);
+/* FP32C refinements of this solver rerun with FP64 Arnoldi vectors after a
+ * stall (a count over the solver's life). */
+int tfs_refinement_retries(tfs_solver *s, long long *retries);
 
 /* --- autotuning ---------------------------------------------------------- */
 /* Products run as work-queue launches: one persistent grid whose CTAs take

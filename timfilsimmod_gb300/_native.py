@@ -124,6 +124,7 @@ _SIGNATURES = {
     "tfs_get_body_velocities": [_H, _P],
     "tfs_set_body_velocities": [_H, _P],
     "tfs_copy_blob_forces_to_host": [_H, _P],
+    "tfs_refinement_retries": [_H, ctypes.POINTER(ctypes.c_longlong)],
     "tfs_solve_info": [_H, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                        ctypes.POINTER(ctypes.c_double)],
     "tfs_solver_enable_kernel_timing": [_H, ctypes.c_int],

@@ -59,21 +59,24 @@ struct PgShape {
   int G, blobs_per_cta;   // CTAs owning blob slices, blobs per slice
   int TB, tbs;            // M_bb target blocks and their size
   int S, chunk;           // M_bb source splits and their size
-  int Kr;                 // Krylov columns resident in shared memory
-  size_t dyn_smem;        // dynamic shared memory per CTA (bytes)
+  int Kr, Kr64;           // Krylov columns resident in shared memory (FP32, FP64 vectors)
+  size_t dyn_smem;        // dynamic shared memory per CTA (bytes, FP32 vectors)
+  size_t dyn_smem64;      // the same with FP64 vectors
 };
 struct PgArgs {
   GmresArgs g;            // vectors, body data, tolerance; g.G / g.blobs_per_cta = slices
   float *x32;             // 3 nb: blob positions minus the origin, FP32
   float *rec;             // 8 nb: FP32 blob records of the current z
   float2 *mpart;          // S * 3 nb: split partial products of M_bb, (hi, lo)
-  double *p6, *ps;        // per-CTA partial 6-vectors and sums of squares
-  double *pd1, *pd2;      // per-CTA Gram-Schmidt partial dots ((max_iter + 2) * G each)
-  double *aux;            // control words (3) + 3 x 352: h1, h2, y published by CTAs
+  // per-CTA partials, FP64-sized buffers holding values of the vector type:
+  double *p6, *ps;        // partial 6-vectors and sums of squares
+  double *pd1, *pd2;      // Gram-Schmidt partial dots ((max_iter + 2) * G each)
+  double *aux;            // control words (3), then h1, h2, y (vector type) published by CTAs
   unsigned *bar;          // 4: barrier count, generation, abort
   int P, TB, tbs, S, chunk, Kr;  // P: the CTAs of this solve
   int rank;               // this CTA's index among them (set on the device)
   int zero_start;         // 1: the warm start is zero (A x0 = 0, r0 = rhs; its M_bb skipped)
+  int vec64;              // 1: FP64 Arnoldi vectors (else FP32); Kr and dyn_smem match
   unsigned bar_extra;     // arrivals each barrier waits for beyond the P CTAs: 0, or 1
                           // under tfs_inject_barrier_stall (every wait then runs out)
   size_t dyn_smem;
@@ -92,9 +95,9 @@ inline size_t pg_pd_elems(const PgShape &s) { return 352 * (size_t)s.G; }
 constexpr size_t kPgAuxElems = 3 + 3 * 352;
 // One cooperative launch of `ctas` CTAs running the solves in gp[] (device
 // array): CTA c works for solve cmap[c].x as its CTA cmap[c].y. Every solve's
-// barrier words must be zero.
+// barrier words must be zero, and every solve's vec64 equal to vec64.
 cudaError_t launch_gmres_persistent(const PgArgs *gp, const int2 *cmap, int ctas, size_t dyn_smem,
-                                    cudaStream_t st);
+                                    int vec64, cudaStream_t st);
 
 // The phase trace of the persistent GMRES (builds with -DTFS_PG_TRACE):
 // [2 CTAs][steps][8 phases] globaltimer stamps into out (capacity elements);

@@ -4,11 +4,18 @@
 // Same system, preconditioner, Givens convention, warm-start tests and
 // stopping rule as the multi-kernel GMRES of gmres.cu (the reference's
 // solve_linear_system, mobility_solver.cpp:2092-2570, free-body branches),
-// with the blob-blob product M_bb in FP32 (compensated per tile). At the
-// medium swimmer (2 562 blobs) an Arnoldi step is ~10 us of arithmetic;
-// issued as seven kernels per step it took ~150-190 us of launch gaps and
-// serialised reductions. Here one launch runs the whole solve (~39 us per
-// Arnoldi step at the medium swimmer):
+// in mixed precision: the blob-blob product M_bb in FP32 (compensated per
+// tile) and the Arnoldi vectors in FP32 -- the Krylov basis, the
+// Gram-Schmidt dots and updates, norms, body sums and the preconditioner --
+// with the Hessenberg matrix, Givens rotations, convergence test and
+// triangular solve in FP64. The inner solve of the refinement asks for a
+// 1e-4 reduction, and two Gram-Schmidt passes in FP32 keep the basis
+// orthogonal to ~1e-7, so the FP32 vectors cost no accuracy the outer
+// (float-float residual) loop needs; they take the FP64 pipe, at ~1/19 of
+// the SM's issue rate on GB300, off every phase. At the medium swimmer
+// (2 562 blobs) an Arnoldi step is ~10 us of arithmetic; issued as seven
+// kernels per step it took ~150-190 us of launch gaps and serialised
+// reductions. Here one launch runs the whole solve:
 //
 //   start | M_bb | residual | scale + preconditioner | { M_bb + Givens |
 //   w, CGS pass-1 dots | h1, w -= Q h1, pass-2 dots, partials of w' |
@@ -26,9 +33,7 @@
 // back after an extra barrier. The new vector's norm and body sums follow
 // from the Pythagorean identity (||w''||^2 = ||w'||^2 - ||h2||^2, and the
 // stored sums of earlier vectors), so no barrier separates them from the
-// second pass. FP64 work is split across warps and accumulators: on GB300 an
-// FP64 warp instruction costs ~19 SM cycles, so serial chains in one warp
-// cost microseconds. Givens rotations, the convergence test and the final
+// second pass. Givens rotations, the convergence test and the final
 // triangular solve run in CTA 0 while the others start the next M_bb; CTA 0
 // publishes its decision for the others to read after the next barrier.
 // The M_bb product is cut into (target block x source split) units spread
@@ -63,7 +68,11 @@ constexpr int kPK = 352;       // Krylov columns + 1 (max_iter <= 350)
 constexpr int kMaxRows = 3 * kMaxPgBlobsPerCta;
 constexpr int kHB = 4096;      // doubles of the staging buffer (H columns, M_bb partials)
 
-constexpr int kPgDynFixed = kHB + 8 * kMaxPgCtas + 12 * kPK;  // doubles before qres
+// bytes of dynamic shared memory before the resident Krylov rows (vectors of V)
+template <typename V>
+constexpr size_t pg_dyn_fixed() {
+  return 8 * (size_t)kHB + sizeof(V) * (8 * (size_t)kMaxPgCtas + 12 * kPK);
+}
 
 // control words CTA 0 publishes each Arnoldi step
 enum { C_FINISH = 0, C_REL, C_STATUS, kCtl };
@@ -80,6 +89,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
+
+// 1 / sqrt(x) of a Krylov vector's squared norm: the refined FP32 estimate
+// (a few ulp) for FP64 vectors, the hardware approximation for FP32 ones.
+__device__ __forceinline__ double vrsqrt(double x) { return rsqrt_far(x); }
+__device__ __forceinline__ float vrsqrt(float x) { return rsqrtf(x); }
 
 // Phase trace of the Arnoldi steps (builds with -DTFS_PG_TRACE only):
 // globaltimer stamps of thread 0 of CTAs 0 and 1 at eight points of every
@@ -145,16 +159,18 @@ __device__ bool pg_barrier(const PgArgs &p, unsigned *epoch) {
   return ok != 0;
 }
 
+template <typename V>
 struct PSlice {
   int m0, m1;       // blobs [m0, m1)
   int rows;         // 3 (m1 - m0)
   bool owner;       // this CTA owns a slice (rank < G)
   bool body;        // this CTA writes the six body rows of global vectors
-  const double *d;  // the slice's d_m = R ref_m, d[3 (m - m0) + j] (shared memory)
+  const V *d;       // the slice's d_m = R ref_m, d[3 (m - m0) + j] (shared memory)
 };
 
-__device__ __forceinline__ PSlice pg_slice(const PgArgs &p, const double *dsl) {
-  PSlice s;
+template <typename V>
+__device__ __forceinline__ PSlice<V> pg_slice(const PgArgs &p, const V *dsl) {
+  PSlice<V> s;
   s.d = dsl;
   const int c = p.rank;
   s.owner = c < p.g.G;
@@ -166,21 +182,23 @@ __device__ __forceinline__ PSlice pg_slice(const PgArgs &p, const double *dsl) {
 }
 
 // Warp sum with a fixed shuffle pattern (the same bits in every lane).
-__device__ __forceinline__ double warp_sum(double v) {
+template <typename V>
+__device__ __forceinline__ V warp_sum(V v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-// Stage elems doubles of buf (global) into dst (shared), eight loads in
+// Stage elems floats of buf (global) into dst (shared), eight loads in
 // flight per thread; no barrier.
-__device__ __forceinline__ void stage(const double *buf, int elems, double *dst) {
+template <typename V>
+__device__ __forceinline__ void stage(const V *buf, int elems, V *dst) {
   for (int q0 = 0; q0 < elems; q0 += 8 * kPB) {
-    double v[8];
+    V v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int q = q0 + u * kPB + (int)threadIdx.x;
-      v[u] = q < elems ? ldcg(buf + q) : 0.0;
+      v[u] = q < elems ? __ldcg(buf + q) : V(0);
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -192,7 +210,8 @@ __device__ __forceinline__ void stage(const double *buf, int elems, double *dst)
 
 // Stage the slice's rows of the S split products (mpart, (hi, lo) FP32
 // pairs) into dst[sp * rows + r], eight loads in flight per thread; no barrier.
-__device__ __forceinline__ void stage_splits(const PgArgs &p, const PSlice &sl, float2 *dst) {
+template <typename V>
+__device__ __forceinline__ void stage_splits(const PgArgs &p, const PSlice<V> &sl, float2 *dst) {
   const int rows = sl.rows, tot = p.S * rows, nb = p.g.nb;
   for (int q0 = 0; q0 < tot; q0 += 8 * kPB) {
     float2 v[8];
@@ -212,10 +231,11 @@ __device__ __forceinline__ void stage_splits(const PgArgs &p, const PSlice &sl, 
 
 // out[j] = sum over c < G of cst[j * G + c], j < count <= kPW: warp j adds
 // lane-strided subsets then a fixed shuffle tree. No barrier.
-__device__ __forceinline__ void sum_staged(const double *cst, int G, int count, double *out) {
+template <typename V>
+__device__ __forceinline__ void sum_staged(const V *cst, int G, int count, V *out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (wid < count) {
-    double s = 0.0;
+    V s = V(0);
     for (int c = lane; c < G; c += 32) s += cst[wid * G + c];
     s = warp_sum(s);
     if (lane == 0) out[wid] = s;
@@ -224,7 +244,8 @@ __device__ __forceinline__ void sum_staged(const double *cst, int G, int count, 
 
 // Stage and sum count vectors of per-CTA partials (buf[j * G + c]) into
 // out[0..count); ends with a barrier.
-__device__ void cta_sums(const double *buf, int G, int count, double *out, double *cst) {
+template <typename V>
+__device__ void cta_sums(const V *buf, int G, int count, V *out, V *cst) {
   stage(buf, count * G, cst);
   __syncthreads();
   sum_staged(cst, G, count, out);
@@ -235,18 +256,19 @@ __device__ void cta_sums(const double *buf, int G, int count, double *out, doubl
 // sum_m (l_m ; d_m x l_m) into p6 slot kt_slot and, with sq_slot >= 0, warp
 // 6 the sum of squares into ps slot sq_slot (lanes stride over blobs or
 // rows, then a fixed shuffle tree). No barrier; ls must be complete.
-__device__ void slice_partials(const PgArgs &p, const PSlice &sl, const double *ls, int kt_slot,
+template <typename V>
+__device__ void slice_partials(const PgArgs &p, const PSlice<V> &sl, const V *ls, int kt_slot,
                                int sq_slot) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (!sl.owner || wid >= (sq_slot >= 0 ? 7 : 6)) return;
-  double s = 0.0;
+  V s = V(0);
   if (wid < 3) {
     for (int m = sl.m0 + lane; m < sl.m1; m += 32) s += ls[3 * (m - sl.m0) + wid];
   } else if (wid < 6) {  // (d x l)_j = d_a l_b - d_b l_a, (a, b) = (j + 1, j + 2) mod 3
     const int a = (wid - 2) % 3, b = (wid - 1) % 3;
     for (int m = sl.m0 + lane; m < sl.m1; m += 32) {
-      const double *d = sl.d + 3 * (m - sl.m0);
-      const double *v = ls + 3 * (m - sl.m0);
+      const V *d = sl.d + 3 * (m - sl.m0);
+      const V *v = ls + 3 * (m - sl.m0);
       s += d[a] * v[b] - d[b] * v[a];
     }
   } else {
@@ -255,8 +277,8 @@ __device__ void slice_partials(const PgArgs &p, const PSlice &sl, const double *
   s = warp_sum(s);
   if (lane == 0) {
     const int G = p.g.G, c = p.rank;
-    if (wid < 6) p.p6[(size_t)(kt_slot * 6 + wid) * G + c] = s;
-    else p.ps[(size_t)sq_slot * G + c] = s;
+    if (wid < 6) reinterpret_cast<V *>(p.p6)[(size_t)(kt_slot * 6 + wid) * G + c] = s;
+    else reinterpret_cast<V *>(p.ps)[(size_t)sq_slot * G + c] = s;
   }
 }
 
@@ -265,14 +287,14 @@ __device__ void slice_partials(const PgArgs &p, const PSlice &sl, const double *
 // (U', Omega') = KTKinv b - N q_vel (mobility_solver.cpp:1437-1509), then
 // z_m = 6 pi mu a (q_m + U' + Omega' x d_m). Writes zv (6, shared) and the
 // slice's z rows into zs (shared); ends with a barrier.
-__device__ void precond(const PgArgs &p, const PSlice &sl, const double *qs, const double *qvel,
-                        const double *bsum, double bscale, double *zs, double *zv,
-                        const double *mats) {
+template <typename V>
+__device__ void precond(const PgArgs &p, const PSlice<V> &sl, const V *qs, const V *qvel,
+                        const V *bsum, V bscale, V *zs, V *zv, const V *mats) {
   if (threadIdx.x < 6) {
     const int i = threadIdx.x;
-    const double *N = mats, *Kinv = mats + 36;
-    double t1 = 0.0, t2 = 0.0;
-    double u1 = 0.0, u2 = 0.0;
+    const V *N = mats, *Kinv = mats + 36;
+    V t1 = V(0), t2 = V(0);
+    V u1 = V(0), u2 = V(0);
     for (int k = 0; k < 6; k += 2) {
       t1 += Kinv[i + 6 * k] * (-bsum[k] * bscale);
       u1 += Kinv[i + 6 * (k + 1)] * (-bsum[k + 1] * bscale);
@@ -282,16 +304,16 @@ __device__ void precond(const PgArgs &p, const PSlice &sl, const double *qs, con
     zv[i] = (t1 + u1) - (t2 + u2);
   }
   __syncthreads();
-  const double u0 = zv[0], u1 = zv[1], u2 = zv[2], w0 = zv[3], w1 = zv[4], w2 = zv[5];
+  const V u0 = zv[0], u1 = zv[1], u2 = zv[2], w0 = zv[3], w1 = zv[4], w2 = zv[5];
+  const V minv = V(p.minv);
   for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += kPB) {
-    const double minv = p.minv;
-    const double *d = sl.d + 3 * (m - sl.m0);
-    const double *l = qs + 3 * (m - sl.m0);
-    double b0 = l[0] + u0, b1 = l[1] + u1, b2 = l[2] + u2;
+    const V *d = sl.d + 3 * (m - sl.m0);
+    const V *l = qs + 3 * (m - sl.m0);
+    V b0 = l[0] + u0, b1 = l[1] + u1, b2 = l[2] + u2;
     b0 += w1 * d[2] - w2 * d[1];
     b1 += w2 * d[0] - w0 * d[2];
     b2 += w0 * d[1] - w1 * d[0];
-    double *o = zs + 3 * (m - sl.m0);
+    V *o = zs + 3 * (m - sl.m0);
     o[0] = minv * b0;
     o[1] = minv * b1;
     o[2] = minv * b2;
@@ -300,9 +322,10 @@ __device__ void precond(const PgArgs &p, const PSlice &sl, const double *qs, con
 }
 
 // FP32 source records {x - origin, f, 0, 0} of the slice's blobs for M_bb.
-__device__ void pack_records(const PgArgs &p, const PSlice &sl, const double *fs) {
+template <typename V>
+__device__ void pack_records(const PgArgs &p, const PSlice<V> &sl, const V *fs) {
   for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += kPB) {
-    const double *f = fs + 3 * (m - sl.m0);
+    const V *f = fs + 3 * (m - sl.m0);
     float4 a, b;
     a.x = p.x32[3 * (size_t)m];
     a.y = p.x32[3 * (size_t)m + 1];
@@ -415,15 +438,16 @@ __device__ void mbb_units(const PgArgs &p, float *src) {
 }
 
 // ws (slice rows) = M_bb z - (U + Omega x d_m) with v = sum over splits of
-// the partial products (in split order), (U, Omega) = zv. The slice's
-// partials are staged through stage (kHB doubles) with parallel loads.
-__device__ void apply_rows(const PgArgs &p, const PSlice &sl, const double *zv, double *ws,
-                           double *stage) {
+// the partial products (in split order, (hi, lo) row sums in acc), (U, Omega)
+// = zv. The slice's partials are staged through stage (kHB doubles) with
+// parallel loads.
+template <typename V>
+__device__ void apply_rows(const PgArgs &p, const PSlice<V> &sl, const V *zv, V *ws,
+                           double *stage, float2 *acc) {
   const int nb = p.g.nb, rows = sl.rows;
   const int per = rows > 0 ? max(1, kHB / rows) : 1;  // splits per staging round
   float2 *st2 = reinterpret_cast<float2 *>(stage);
-  float *acc = reinterpret_cast<float *>(ws);  // (hi, lo) per row while summing
-  for (int r = threadIdx.x; r < rows; r += kPB) acc[2 * r] = acc[2 * r + 1] = 0.f;
+  for (int r = threadIdx.x; r < rows; r += kPB) acc[r] = make_float2(0.f, 0.f);
   for (int s0 = 0; s0 < p.S; s0 += per) {
     const int s1 = min(p.S, s0 + per);
     __syncthreads();
@@ -433,68 +457,70 @@ __device__ void apply_rows(const PgArgs &p, const PSlice &sl, const double *zv, 
     }
     __syncthreads();
     for (int r = threadIdx.x; r < rows; r += kPB) {
-      float h = acc[2 * r], l = acc[2 * r + 1];
+      float h = acc[r].x, l = acc[r].y;
       for (int s = 0; s < s1 - s0; ++s) {
         two_sum(h, l, st2[s * rows + r].x);
         l += st2[s * rows + r].y;
       }
-      acc[2 * r] = h;
-      acc[2 * r + 1] = l;
+      acc[r] = make_float2(h, l);
     }
   }
   __syncthreads();
-  // convert in place: every thread reads its rows' pairs before any row is overwritten
-  double vrow[kMaxRows / kPB + 1];
-  int nr = 0;
-  for (int r = threadIdx.x; r < rows; r += kPB)
-    vrow[nr++] = p.scale * ((double)acc[2 * r] + (double)acc[2 * r + 1]);
-  __syncthreads();
-  nr = 0;
-  for (int r = threadIdx.x; r < rows; r += kPB) ws[r] = vrow[nr++];
-  __syncthreads();
+  const V scale = V(p.scale);
   for (int r = threadIdx.x; r < rows; r += kPB) {
     const int m = sl.m0 + r / 3, j = r - 3 * (r / 3);
-    const double *d = sl.d + 3 * (m - sl.m0);
-    double body;
+    const V *d = sl.d + 3 * (m - sl.m0);
+    V body;
     if (j == 0) body = zv[0] - d[1] * zv[5] + d[2] * zv[4];
     else if (j == 1) body = zv[1] - d[2] * zv[3] + d[0] * zv[5];
     else body = zv[2] - d[0] * zv[4] + d[1] * zv[3];
-    ws[r] = -body + ws[r];
+    ws[r] = -body + scale * (V(acc[r].x) + V(acc[r].y));
   }
   __syncthreads();
+}
+
+// The Krylov basis in global memory, FP32: row r of vector i at
+// [i n + r] of the (FP64-sized) basis buffer.
+template <typename V>
+__device__ __forceinline__ V *qglobal(const PgArgs &p) {
+  return reinterpret_cast<V *>(p.g.Q);
 }
 
 // Row r of the slice's Krylov vector i: from the CTA's resident copy
 // (columns i < Kr, shared memory) or from global memory.
-__device__ __forceinline__ double qrow(const PgArgs &p, const PSlice &sl, const double *qres,
-                                       int i, int r) {
+template <typename V>
+__device__ __forceinline__ V qrow(const PgArgs &p, const PSlice<V> &sl, const V *qres, int i,
+                                      int r) {
   return i < p.Kr ? qres[(size_t)i * sl.rows + r]
-                  : ldcg(p.g.Q + (size_t)i * p.g.n + 3 * (size_t)sl.m0 + r);
+                  : __ldcg(qglobal<V>(p) + (size_t)i * p.g.n + 3 * (size_t)sl.m0 + r);
 }
 
-// Store the slice rows ws as Krylov vector i (resident copy and global).
-__device__ void store_q(const PgArgs &p, const PSlice &sl, double *qres, int i, const double *ws) {
+// Store the slice rows ws as Krylov vector i (resident copy, or global
+// memory beyond the resident columns).
+template <typename V>
+__device__ void store_q(const PgArgs &p, const PSlice<V> &sl, V *qres, int i, const V *ws) {
   for (int r = threadIdx.x; r < sl.rows; r += kPB) {
     if (i < p.Kr) qres[(size_t)i * sl.rows + r] = ws[r];
-    p.g.Q[(size_t)i * p.g.n + 3 * (size_t)sl.m0 + r] = ws[r];
+    else qglobal<V>(p)[(size_t)i * p.g.n + 3 * (size_t)sl.m0 + r] = ws[r];
   }
 }
 
 // dots of the slice rows ws with Q_i, i < k, into pd[i * G + c]: tpi
 // adjacent threads per i (16, 8 or 4 as k allows one pass; four per pass
 // beyond), rows r = part (mod tpi), then a fixed shuffle tree.
-__device__ void slice_dots(const PgArgs &p, const PSlice &sl, const double *ws, int k,
-                           double *pd, const double *qres) {
+template <typename V>
+__device__ void slice_dots(const PgArgs &p, const PSlice<V> &sl, const V *ws, int k, V *pd,
+                           const V *qres) {
   if (!sl.owner) return;
   const int tpi = k <= kPB / 16 ? 16 : k <= kPB / 8 ? 8 : 4;
   const int part = threadIdx.x & (tpi - 1);
   for (int i0 = 0; i0 < k; i0 += kPB / tpi) {
     const int i = i0 + (int)threadIdx.x / tpi;
-    double s = 0.0, u = 0.0;
+    V s = V(0), u = V(0);
     if (i < k) {
       int r = part;
       if (i < p.Kr) {
-        const double *q = qres + (size_t)i * sl.rows;
+        const V *q = qres + (size_t)i * sl.rows;
         for (; r + tpi < sl.rows; r += 2 * tpi) {
           s += ws[r] * q[r];
           u += ws[r + tpi] * q[r + tpi];
@@ -513,11 +539,12 @@ __device__ void slice_dots(const PgArgs &p, const PSlice &sl, const double *ws, 
 // ws (slice rows) += sign * sum_{i<k} h_i Q_i: four adjacent threads per row
 // (when the rows allow), each over i = sub (mod 4) with two running sums,
 // then a fixed shuffle tree; one thread per row with four sums otherwise.
-__device__ void slice_axpy(const PgArgs &p, const PSlice &sl, const double *h, int k, double *ws,
-                           double sign, const double *qres) {
+template <typename V>
+__device__ void slice_axpy(const PgArgs &p, const PSlice<V> &sl, const V *h, int k, V *ws,
+                           V sign, const V *qres) {
   if (4 * sl.rows <= kPB) {
     const int r = threadIdx.x >> 2, sub = threadIdx.x & 3;
-    double t = 0.0, u = 0.0;
+    V t = V(0), u = V(0);
     if (r < sl.rows) {
       int i = sub;
       for (; i + 4 < k; i += 8) {
@@ -532,7 +559,7 @@ __device__ void slice_axpy(const PgArgs &p, const PSlice &sl, const double *h, i
     if (r < sl.rows && sub == 0) ws[r] += sign * t;
   } else {
     for (int r = threadIdx.x; r < sl.rows; r += kPB) {
-      double t[4] = {0.0, 0.0, 0.0, 0.0};
+      V t[4] = {V(0), V(0), V(0), V(0)};
       int i = 0;
       for (; i + 3 < k; i += 4)
 #pragma unroll
@@ -546,10 +573,11 @@ __device__ void slice_axpy(const PgArgs &p, const PSlice &sl, const double *h, i
 
 // v[l] += sign * sum_{i<k} h_i Q_i,vel(l): warp l < 6, lanes over i, fixed
 // tree; the body rows of every Krylov vector are resident in qvres[6 i + l].
-__device__ void vel_axpy(const double *qvres, const double *h, int k, double *v, double sign) {
+template <typename V>
+__device__ void vel_axpy(const V *qvres, const V *h, int k, V *v, V sign) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (wid < 6) {
-    double s = 0.0;
+    V s = V(0);
     for (int i = lane; i < k; i += 32) s += h[i] * qvres[6 * i + wid];
     s = warp_sum(s);
     if (lane == 0) v[wid] += sign * s;
@@ -561,13 +589,14 @@ __device__ void vel_axpy(const double *qvres, const double *h, int k, double *v,
 // h_j = sum_c' pd[j * G + c'] + w_vel . Q_j,vel for j = c + P (w + kPW t),
 // into hg[j] (global); lanes l < 6 start from the body term w_vel,l Q_j,vel(l),
 // lanes stride over c', then a fixed shuffle tree.
-__device__ void reduce_dots(const PgArgs &p, const double *pd, int k, const double *wv,
-                            const double *qvres, double *hg) {
+template <typename V>
+__device__ void reduce_dots(const PgArgs &p, const V *pd, int k, const V *wv,
+                            const V *qvres, V *hg) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int G = p.g.G;
   for (int j = p.rank + p.P * wid; j < k; j += p.P * kPW) {
-    double s = lane < 6 ? wv[lane] * qvres[6 * j + lane] : 0.0;
-    for (int c = lane; c < G; c += 32) s += ldcg(pd + (size_t)j * G + c);
+    V s = lane < 6 ? wv[lane] * qvres[6 * j + lane] : V(0);
+    for (int c = lane; c < G; c += 32) s += __ldcg(pd + (size_t)j * G + c);
     s = warp_sum(s);
     if (lane == 0) hg[j] = s;
   }
@@ -576,18 +605,19 @@ __device__ void reduce_dots(const PgArgs &p, const double *pd, int k, const doub
 // The same sums as reduce_dots, h[j] for j < k into shared memory, in every
 // CTA (identical bits: the same order), when the k x G partials fit the
 // staging buffers stg (hb and the partial-sum staging after it): false, with
-// nothing done, otherwise. The partials are staged with eight loads in
-// flight per thread. Ends with a barrier.
-__device__ bool local_dots(const PgArgs &p, const double *pd, int k, const double *wv,
-                           const double *qvres, double *h, double *stg) {
+// nothing done, otherwise. The partials are staged with eight
+// loads in flight per thread. Ends with a barrier.
+template <typename V>
+__device__ bool local_dots(const PgArgs &p, const V *pd, int k, const V *wv,
+                           const V *qvres, V *h, V *stg) {
   const int G = p.g.G, tot = k * G;
-  if (tot > kHB + 8 * kMaxPgCtas) return false;
+  if (tot > kHB * (int)(sizeof(double) / sizeof(V)) + 8 * kMaxPgCtas) return false;
   for (int q0 = 0; q0 < tot; q0 += 8 * kPB) {
-    double v[8];
+    V v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int q = q0 + u * kPB + (int)threadIdx.x;
-      v[u] = q < tot ? ldcg(pd + q) : 0.0;
+      v[u] = q < tot ? __ldcg(pd + q) : V(0);
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -598,7 +628,7 @@ __device__ bool local_dots(const PgArgs &p, const double *pd, int k, const doubl
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int j = wid; j < k; j += kPW) {
-    double s = lane < 6 ? wv[lane] * qvres[6 * j + lane] : 0.0;
+    V s = lane < 6 ? wv[lane] * qvres[6 * j + lane] : V(0);
     for (int c = lane; c < G; c += 32) s += stg[(size_t)j * G + c];
     s = warp_sum(s);
     if (lane == 0) h[j] = s;
@@ -680,6 +710,7 @@ __device__ void back_substitute(const PgArgs &p, int k, const double *hcol, cons
 
 }  // namespace
 
+template <typename V>
 __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *__restrict__ gp,
                                                                   const int2 *__restrict__ cmap) {
   // this CTA's solve (several independent solves may share one launch, each
@@ -695,34 +726,43 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
   __shared__ unsigned epoch;  // grid barriers passed (thread 0)
   if (threadIdx.x == 0) epoch = 0u;
   __shared__ __align__(16) float src[8 * kPTS];
-  __shared__ double ws[kMaxRows];            // w (then Q_k, tmp) rows of the slice
-  __shared__ double zs[kMaxRows];            // z = P^-1 q rows of the slice
-  __shared__ double h1[kPK], h2[kPK], cs[kPK], sn[kPK], beta[kPK], hcol[kPK], yv[kPK];
+  __shared__ V ws[kMaxRows];        // w (then Q_k, tmp) rows of the slice
+  __shared__ V zs[kMaxRows];        // z = P^-1 q rows of the slice
+  __shared__ float2 acc[kMaxRows];  // (hi, lo) row sums of the M_bb splits
+  __shared__ V h1[kPK], h2[kPK], yf[kPK];
+  __shared__ double cs[kPK], sn[kPK], beta[kPK], hcol[kPK], yv[kPK];
   __shared__ double tmp8[8];
-  __shared__ double wvel[6], qvel[6], zv[6], wsum6[6];
-  __shared__ double dsl[kMaxRows], mats[72], qn_s[2];
-  // dynamic: staging buffer (kHB), staged per-CTA partials (8 x kMaxPgCtas),
-  // body rows of every Krylov vector (6 x kPK), sum_m (Q_i,m ; d_m x Q_i,m)
-  // of every Krylov vector (6 x kPK), resident Krylov rows (Kr x rows)
+  __shared__ V tf[8];
+  __shared__ V wvel[6], qvel[6], zv[6], wsum6[6];
+  __shared__ V dsl[kMaxRows], mats[72], qn_s[2];
+  // dynamic: staging buffer (kHB doubles), then of the vector type: staged
+  // per-CTA partials (8 x kMaxPgCtas), body rows of every Krylov vector
+  // (6 x kPK), sum_m (Q_i,m ; d_m x Q_i,m) of every Krylov vector (6 x kPK),
+  // resident Krylov rows (Kr x rows)
   extern __shared__ double dyn[];
-  double *hb = dyn, *cst = hb + kHB, *qvres = cst + 8 * kMaxPgCtas, *qsres = qvres + 6 * kPK,
-         *qres = qsres + 6 * kPK;
+  double *hb = dyn;
+  V *cst = reinterpret_cast<V *>(hb + kHB), *qvres = cst + 8 * kMaxPgCtas,
+    *qsres = qvres + 6 * kPK, *qres = qsres + 6 * kPK;
+  // per-CTA partials in the vector type
+  V *p6 = reinterpret_cast<V *>(p.p6), *ps = reinterpret_cast<V *>(p.ps);
+  V *pd1 = reinterpret_cast<V *>(p.pd1), *pd2 = reinterpret_cast<V *>(p.pd2);
 
   const GmresArgs &g = p.g;
   GmresScalars *st = g.st;
   const PSlice sl = pg_slice(p, dsl);
   const int nb = g.nb, vel = 3 * nb, G = g.G;
-  const size_t n = g.n;
+  const V scale = V(p.scale);
 
   // ---- start: the slice's d_m and the body matrices into shared memory,
   //      warm start into soln, FP32 targets, records, ||rhs|| partials
-  for (int r = threadIdx.x; r < sl.rows; r += kPB) dsl[r] = g.diff[3 * (size_t)sl.m0 + r];
-  for (int q = threadIdx.x; q < 72; q += kPB) mats[q] = g.mats[q];
+  for (int r = threadIdx.x; r < sl.rows; r += kPB) dsl[r] = V(g.diff[3 * (size_t)sl.m0 + r]);
+  for (int q = threadIdx.x; q < 72; q += kPB) mats[q] = V(g.mats[q]);
   for (int r = threadIdx.x; r < sl.rows; r += kPB) {
     const int t = 3 * sl.m0 + r;
-    ws[r] = g.f_blobs[t];
-    g.soln[t] = ws[r];
-    zs[r] = g.rhs[t];
+    const double x0 = g.f_blobs[t];
+    g.soln[t] = x0;
+    ws[r] = V(x0);
+    zs[r] = V(g.rhs[t]);
   }
   for (int m = sl.m0 + threadIdx.x; m < sl.m1; m += kPB)
     for (int k = 0; k < 3; ++k)
@@ -746,9 +786,9 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     if (!pg_barrier(p, &epoch)) return;
 
     // ---- residual r0 = rhs - A soln (slice rows), partials
-    if (threadIdx.x < 6) zv[threadIdx.x] = g.v_bodies[threadIdx.x];
+    if (threadIdx.x < 6) zv[threadIdx.x] = V(g.v_bodies[threadIdx.x]);
     __syncthreads();
-    apply_rows(p, sl, zv, ws, hb);  // ws = A soln (blob rows)
+    apply_rows(p, sl, zv, ws, hb, acc);  // ws = A soln (blob rows)
     for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = zs[r] - ws[r];  // zs = rhs rows
     __syncthreads();
     slice_partials(p, sl, ws, K_R0, S_R0);
@@ -759,19 +799,19 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
   //      preconditioner of Q_0, records (every CTA decides the same)
   double norm_rhs;
   {
-    cta_sums(p.ps + (size_t)S_RHS * G, G, 1, tmp8, cst);
-    double rhs_vel[6], t = tmp8[0];
+    cta_sums(ps + (size_t)S_RHS * G, G, 1, tf, cst);
+    double rhs_vel[6], t = tf[0];
     for (int j = 0; j < 6; ++j) {
       rhs_vel[j] = g.rhs[vel + j];
       t += rhs_vel[j] * rhs_vel[j];
     }
     norm_rhs = sqrt(t);
-    cta_sums(p.p6 + (size_t)K_SOLN * 6 * G, G, 6, tmp8, cst);
+    cta_sums(p6 + (size_t)K_SOLN * 6 * G, G, 6, tf, cst);
     double r0v[6];
-    for (int j = 0; j < 6; ++j) r0v[j] = rhs_vel[j] - (-tmp8[j]);
+    for (int j = 0; j < 6; ++j) r0v[j] = rhs_vel[j] - (-(double)tf[j]);
     __syncthreads();
-    cta_sums(p.ps + (size_t)s_r0 * G, G, 1, tmp8, cst);
-    double bb = tmp8[0];
+    cta_sums(ps + (size_t)s_r0 * G, G, 1, tf, cst);
+    double bb = tf[0];
     for (int j = 0; j < 6; ++j) bb += r0v[j] * r0v[j];
     double beta0 = sqrt(bb);
     int flag = 0;
@@ -806,27 +846,25 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
         g.soln[3 * sl.m0 + r] = 0.0;
       }
       if (sl.body && threadIdx.x < 6) g.soln[vel + threadIdx.x] = 0.0;
-      if (threadIdx.x < 6) qvel[threadIdx.x] = rhs_vel[threadIdx.x] / norm_rhs;
+      if (threadIdx.x < 6) qvel[threadIdx.x] = V(rhs_vel[threadIdx.x] / norm_rhs);
       kslot = K_RHS;
       inv = norm_rhs;
     } else {
-      if (threadIdx.x < 6) qvel[threadIdx.x] = r0v[threadIdx.x] / beta0;
+      if (threadIdx.x < 6) qvel[threadIdx.x] = V(r0v[threadIdx.x] / beta0);
       kslot = k_r0;
       inv = beta0;
     }
+    const V rinv = V(1.0 / inv);
     __syncthreads();
-    for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = ws[r] / inv;
+    for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = ws[r] * rinv;
     __syncthreads();
     store_q(p, sl, qres, 0, ws);
-    if (threadIdx.x < 6) {
-      qvres[threadIdx.x] = qvel[threadIdx.x];
-      if (sl.body) g.Q[vel + threadIdx.x] = qvel[threadIdx.x];
-    }
+    if (threadIdx.x < 6) qvres[threadIdx.x] = qvel[threadIdx.x];
     if (threadIdx.x == 0) beta[0] = beta0;
     // z = P^-1 Q_0: sum_m (Q_0 ; d x Q_0) = (partials of the unscaled vector) / inv
-    cta_sums(p.p6 + (size_t)kslot * 6 * G, G, 6, tmp8, cst);
-    if (threadIdx.x < 6) qsres[threadIdx.x] = tmp8[threadIdx.x] * (1.0 / inv);
-    precond(p, sl, ws, qvel, tmp8, 1.0 / inv, zs, zv, mats);
+    cta_sums(p6 + (size_t)kslot * 6 * G, G, 6, tf, cst);
+    if (threadIdx.x < 6) qsres[threadIdx.x] = tf[threadIdx.x] * rinv;
+    precond(p, sl, ws, qvel, tf, rinv, zs, zv, mats);
     pack_records(p, sl, zs);
     slice_partials(p, sl, zs, K_Z, -1);
   }
@@ -835,7 +873,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
   // ---- Arnoldi steps. Step k: M_bb z_{k-1} (CTA 0 meanwhile finishes step
   //      k-1's Givens rotation and convergence test), w = A z_{k-1}, two
   //      classical Gram-Schmidt passes, ||w||, Q_k = w / ||w||, z_k = P^-1 Q_k.
-  double *h1g = p.aux + kCtl, *h2g = h1g + kPK, *yg = h2g + kPK;
+  V *h1g = reinterpret_cast<V *>(p.aux + kCtl), *h2g = h1g + kPK, *yg = h2g + kPK;
   int k = 1;
   double qn = 0.0;
   for (;;) {
@@ -845,7 +883,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
       // Givens rotation (mobility_solver.cpp:2370-2413) of step kk = k - 1
       const int kk = k - 1;
       if (threadIdx.x == 0) {
-        for (int i = 0; i < kk; ++i) hcol[i] = h1[i] + h2[i];
+        for (int i = 0; i < kk; ++i) hcol[i] = (double)h1[i] + (double)h2[i];
         hcol[kk] = qn;
         const double rel = givens_step(kk, hcol, cs, sn, beta, norm_rhs);
         int fin = rel <= g.tol || kk == g.max_iter;
@@ -863,7 +901,7 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
       for (int i = threadIdx.x; i <= kk; i += kPB) g.H[i + (size_t)(kk - 1) * ld] = hcol[i];
       if (tmp8[0] != 0.0) {
         back_substitute(p, kk, hcol, beta, yv, hb);
-        for (int i = threadIdx.x; i < kk; i += kPB) yg[i] = yv[i];
+        for (int i = threadIdx.x; i < kk; i += kPB) yg[i] = V(yv[i]);
       }
       if (threadIdx.x == 0) {
         p.aux[C_FINISH] = tmp8[0];
@@ -880,12 +918,12 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
 
     // w = A z (slice rows; body rows w_vel = -sum (z ; d x z) in every CTA),
     // CGS pass 1 partial dots
-    stage(p.p6 + (size_t)K_Z * 6 * G, 6 * G, cst);
+    stage(p6 + (size_t)K_Z * 6 * G, 6 * G, cst);
     if (p.S * sl.rows <= kHB) {
       float2 *st2 = reinterpret_cast<float2 *>(hb);
       stage_splits(p, sl, st2);
       __syncthreads();
-      sum_staged(cst, G, 6, tmp8);
+      sum_staged(cst, G, 6, tf);
       // tpr adjacent threads per row add the splits sp = sub (mod tpr),
       // compensated, then combine their (hi, lo) pairs by a fixed shuffle tree
       const int tpr = 8 * sl.rows <= kPB ? 8 : 4 * sl.rows <= kPB ? 4 : 2 * sl.rows <= kPB ? 2 : 1;
@@ -904,49 +942,49 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
           l += lo;
         }
         if (r < sl.rows && sub == 0) {
-          const double v = p.scale * ((double)h + (double)l);
           const int m = sl.m0 + r / 3, j = r - 3 * (r / 3);
-          const double *d = sl.d + 3 * (m - sl.m0);
-          double body;
+          const V *d = sl.d + 3 * (m - sl.m0);
+          V body;
           if (j == 0) body = zv[0] - d[1] * zv[5] + d[2] * zv[4];
           else if (j == 1) body = zv[1] - d[2] * zv[3] + d[0] * zv[5];
           else body = zv[2] - d[0] * zv[4] + d[1] * zv[3];
-          ws[r] = -body + v;
+          ws[r] = -body + scale * (V(h) + V(l));
         }
       }
       __syncthreads();
     } else {
       __syncthreads();
-      sum_staged(cst, G, 6, tmp8);
-      apply_rows(p, sl, zv, ws, hb);
+      sum_staged(cst, G, 6, tf);
+      apply_rows(p, sl, zv, ws, hb, acc);
     }
-    if (threadIdx.x < 6) wvel[threadIdx.x] = -tmp8[threadIdx.x];
+    if (threadIdx.x < 6) wvel[threadIdx.x] = -tf[threadIdx.x];
     PG_STAMP(k, 2);
-    slice_dots(p, sl, ws, k, p.pd1, qres);
+    slice_dots(p, sl, ws, k, pd1, qres);
     if (!pg_barrier(p, &epoch)) return;
     PG_STAMP(k, 3);
     // h1 (summed by every CTA while the partials fit the staging buffers,
     // else spread over the grid and published)
-    if (!local_dots(p, p.pd1, k, wvel, qvres, h1, hb)) {
-      reduce_dots(p, p.pd1, k, wvel, qvres, h1g);
+    V *stg = reinterpret_cast<V *>(hb);
+    if (!local_dots(p, pd1, k, wvel, qvres, h1, stg)) {
+      reduce_dots(p, pd1, k, wvel, qvres, h1g);
       if (!pg_barrier(p, &epoch)) return;
-      for (int i = threadIdx.x; i < k; i += kPB) h1[i] = ldcg(h1g + i);
+      for (int i = threadIdx.x; i < k; i += kPB) h1[i] = __ldcg(h1g + i);
       __syncthreads();
     }
     PG_STAMP(k, 4);
 
     // w' = w - Q h1; CGS pass 2 partial dots, and ||w'||^2 and
     // sum (w' ; d x w') partials
-    slice_axpy(p, sl, h1, k, ws, -1.0, qres);
-    vel_axpy(qvres, h1, k, wvel, -1.0);
-    slice_dots(p, sl, ws, k, p.pd2, qres);
+    slice_axpy(p, sl, h1, k, ws, V(-1), qres);
+    vel_axpy(qvres, h1, k, wvel, V(-1));
+    slice_dots(p, sl, ws, k, pd2, qres);
     slice_partials(p, sl, ws, K_W, S_NORM);
     if (!pg_barrier(p, &epoch)) return;
     PG_STAMP(k, 5);
-    if (!local_dots(p, p.pd2, k, wvel, qvres, h2, hb)) {
-      reduce_dots(p, p.pd2, k, wvel, qvres, h2g);
+    if (!local_dots(p, pd2, k, wvel, qvres, h2, stg)) {
+      reduce_dots(p, pd2, k, wvel, qvres, h2g);
       if (!pg_barrier(p, &epoch)) return;
-      for (int i = threadIdx.x; i < k; i += kPB) h2[i] = ldcg(h2g + i);
+      for (int i = threadIdx.x; i < k; i += kPB) h2[i] = __ldcg(h2g + i);
       __syncthreads();
     }
     PG_STAMP(k, 6);
@@ -954,16 +992,18 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
     // w'' = w' - Q h2; with Q orthonormal, ||w''||^2 = ||w'||^2 - ||h2||^2
     // and sum (w'' ; d x w'') = sum (w' ; d x w') - sum_i h2_i S_i, S_i the
     // sums of Q_i (kept in qsres); Q_k = w'' / ||w''||, z_k = P^-1 Q_k.
-    stage(p.ps + (size_t)S_NORM * G, G, cst);
-    stage(p.p6 + (size_t)K_W * 6 * G, 6 * G, cst + G);
+    // After the first pass h2 is small against w' (the lost orthogonality),
+    // so the difference carries no cancellation.
+    stage(ps + (size_t)S_NORM * G, G, cst);
+    stage(p6 + (size_t)K_W * 6 * G, 6 * G, cst + G);
     __syncthreads();
-    sum_staged(cst, G, 7, tmp8);
+    sum_staged(cst, G, 7, tf);
     __syncthreads();
     {
       // warp j < 6: the body sum j of w''; warp 6: ||w''||^2 (lanes over i)
       const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
       if (wid < 7) {
-        double t = 0.0;
+        V t = V(0);
         if (wid < 6) {
           for (int i = lane; i < k; i += 32) t += h2[i] * qsres[6 * i + wid];
         } else {
@@ -973,10 +1013,10 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
         t = warp_sum(t);
         if (lane == 0) {
           if (wid < 6) {
-            wsum6[wid] = tmp8[1 + wid] - t;
-          } else {  // 1/||w''|| by the refined FP32 estimate (a few ulp)
-            const double w2 = tmp8[0] + t;
-            const double y = rsqrt_far(w2);
+            wsum6[wid] = tf[1 + wid] - t;
+          } else {
+            const V w2 = tf[0] + t;
+            const V y = vrsqrt(w2);
             qn_s[0] = w2 * y;
             qn_s[1] = y;
           }
@@ -984,10 +1024,10 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
       }
     }
     __syncthreads();
-    slice_axpy(p, sl, h2, k, ws, -1.0, qres);
-    vel_axpy(qvres, h2, k, wvel, -1.0);
+    slice_axpy(p, sl, h2, k, ws, V(-1), qres);
+    vel_axpy(qvres, h2, k, wvel, V(-1));
     qn = qn_s[0];
-    const double rqn = qn_s[1];
+    const V rqn = qn_s[1];
     for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = ws[r] * rqn;
     __syncthreads();
     store_q(p, sl, qres, k, ws);
@@ -995,7 +1035,6 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
       qvel[threadIdx.x] = wvel[threadIdx.x] * rqn;
       qvres[6 * k + threadIdx.x] = qvel[threadIdx.x];
       qsres[6 * k + threadIdx.x] = wsum6[threadIdx.x] * rqn;
-      if (sl.body) g.Q[(size_t)k * n + vel + threadIdx.x] = qvel[threadIdx.x];
     }
     __syncthreads();
     precond(p, sl, ws, qvel, wsum6, rqn, zs, zv, mats);
@@ -1008,24 +1047,24 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
 
   // ---- tmp = Q y (slice rows in ws, body rows in qvel), z = P^-1 tmp,
   //      soln += z -> (f_blobs, v_bodies) (:2440-2563)
-  for (int i = threadIdx.x; i < k; i += kPB) yv[i] = ldcg(yg + i);
-  for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = 0.0;
-  if (threadIdx.x < 6) qvel[threadIdx.x] = 0.0;
+  for (int i = threadIdx.x; i < k; i += kPB) yf[i] = __ldcg(yg + i);
+  for (int r = threadIdx.x; r < sl.rows; r += kPB) ws[r] = V(0);
+  if (threadIdx.x < 6) qvel[threadIdx.x] = V(0);
   __syncthreads();
-  slice_axpy(p, sl, yv, k, ws, 1.0, qres);
-  vel_axpy(qvres, yv, k, qvel, 1.0);
+  slice_axpy(p, sl, yf, k, ws, V(1), qres);
+  vel_axpy(qvres, yf, k, qvel, V(1));
   slice_partials(p, sl, ws, K_T, -1);
   if (!pg_barrier(p, &epoch)) return;
-  cta_sums(p.p6 + (size_t)K_T * 6 * G, G, 6, tmp8, cst);
-  precond(p, sl, ws, qvel, tmp8, 1.0, zs, zv, mats);
+  cta_sums(p6 + (size_t)K_T * 6 * G, G, 6, tf, cst);
+  precond(p, sl, ws, qvel, tf, V(1), zs, zv, mats);
   for (int r = threadIdx.x; r < sl.rows; r += kPB) {
     const int t = 3 * sl.m0 + r;
-    const double x = g.soln[t] + zs[r];
+    const double x = g.soln[t] + (double)zs[r];
     g.soln[t] = x;
     g.f_blobs[t] = x;
   }
   if (sl.body && threadIdx.x < 6) {
-    const double x = g.soln[vel + threadIdx.x] + zv[threadIdx.x];
+    const double x = g.soln[vel + threadIdx.x] + (double)zv[threadIdx.x];
     g.soln[vel + threadIdx.x] = x;
     g.v_bodies[threadIdx.x] = x;
   }
@@ -1039,13 +1078,44 @@ __global__ void __launch_bounds__(kPB, 1) gmres_persistent_kernel(const PgArgs *
   }
 }
 
+// Resident Krylov columns and dynamic shared memory of the kernel with
+// vectors of V for slices of `rows` rows; false when not even one column fits.
+template <typename V>
+bool pg_smem(long avail, int rows, int max_iter, int *Kr, size_t *dyn) {
+  const long cols = (avail - (long)pg_dyn_fixed<V>()) / (long)(sizeof(V) * rows);
+  if (cols < 1) return false;
+  *Kr = (int)std::min<long>(max_iter + 1, cols);
+  *dyn = pg_dyn_fixed<V>() + sizeof(V) * (size_t)*Kr * rows;
+  return true;
+}
+
+// The largest dynamic shared memory a CTA of the instantiation may use (set
+// once per instantiation, so that one setting serves every shape: solves of
+// several shapes share launches); false when no CTA of it fits an SM.
+template <typename V>
+bool pg_ready(int optin, size_t dyn) {
+  cudaFuncAttributes fa{};
+  int occ = 0;
+  if (cudaFuncGetAttributes(&fa, gmres_persistent_kernel<V>) != cudaSuccess ||
+      cudaFuncSetAttribute(gmres_persistent_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(optin - (long)fa.sharedSizeBytes)) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gmres_persistent_kernel<V>, kPB, dyn) !=
+          cudaSuccess ||
+      occ < 1) {
+    cudaGetLastError();
+    return false;
+  }
+  return true;
+}
+
 int pg_grid(int nb, int sms, int max_iter, PgShape *shape) {
   int dev = 0, optin = 0;
-  cudaFuncAttributes fa{};
+  cudaFuncAttributes f32{}, f64{};
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
           cudaSuccess ||
-      cudaFuncGetAttributes(&fa, gmres_persistent_kernel) != cudaSuccess) {
+      cudaFuncGetAttributes(&f32, gmres_persistent_kernel<float>) != cudaSuccess ||
+      cudaFuncGetAttributes(&f64, gmres_persistent_kernel<double>) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -1056,24 +1126,14 @@ int pg_grid(int nb, int sms, int max_iter, PgShape *shape) {
   G = std::max(1, (nb + per - 1) / per);
   if (per > kMaxPgBlobsPerCta) return 0;
   const int rows = 3 * per;
-  // dynamic shared memory: the staging buffer, then as many resident Krylov
+  // dynamic shared memory: the staging buffers, then as many resident Krylov
   // columns of the slice as fit (all max_iter + 1 when possible)
-  const long avail = (long)optin - (long)fa.sharedSizeBytes - 1024;
-  const long cols = (avail / 8 - kPgDynFixed) / rows;
-  if (cols < 1) return 0;
-  const int Kr = (int)std::min<long>(max_iter + 1, cols);
-  const size_t dyn = sizeof(double) * (kPgDynFixed + (size_t)Kr * rows);
-  int occ = 0;
-  // the attribute is the largest dynamic size any shape may use, so that one
-  // setting serves every shape (solves of several shapes share launches)
-  if (cudaFuncSetAttribute(gmres_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(optin - (long)fa.sharedSizeBytes)) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gmres_persistent_kernel, kPB, dyn) !=
-          cudaSuccess ||
-      occ < 1) {
-    cudaGetLastError();
+  if (!pg_smem<float>((long)optin - (long)f32.sharedSizeBytes - 1024, rows, max_iter, &shape->Kr,
+                      &shape->dyn_smem) ||
+      !pg_smem<double>((long)optin - (long)f64.sharedSizeBytes - 1024, rows, max_iter,
+                       &shape->Kr64, &shape->dyn_smem64) ||
+      !pg_ready<float>(optin, shape->dyn_smem) || !pg_ready<double>(optin, shape->dyn_smem64))
     return 0;
-  }
   const int workers = P > 1 ? P - 1 : 1;  // CTA 0 runs the Givens step meanwhile
   const int TB = std::max(1, (nb + 2 * kPB - 1) / (2 * kPB));
   const int tbs = (nb + TB - 1) / TB;
@@ -1087,8 +1147,6 @@ int pg_grid(int nb, int sms, int max_iter, PgShape *shape) {
   shape->tbs = tbs;
   shape->S = S;
   shape->chunk = chunk;
-  shape->Kr = Kr;
-  shape->dyn_smem = dyn;
   return 1;
 }
 
@@ -1107,10 +1165,11 @@ int pg_trace_read(unsigned long long *out, int capacity, int *steps) {
 }
 
 cudaError_t launch_gmres_persistent(const PgArgs *gp, const int2 *cmap, int ctas, size_t dyn_smem,
-                                    cudaStream_t st) {
+                                    int vec64, cudaStream_t st) {
   void *args[] = {const_cast<PgArgs **>(&gp), const_cast<int2 **>(&cmap)};
-  cudaError_t e = cudaLaunchCooperativeKernel((const void *)gmres_persistent_kernel, dim3(ctas),
-                                              dim3(kPB), args, dyn_smem, st);
+  const void *fn = vec64 ? (const void *)gmres_persistent_kernel<double>
+                         : (const void *)gmres_persistent_kernel<float>;
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(ctas), dim3(kPB), args, dyn_smem, st);
   count_launch();
   return e;
 }

@@ -255,7 +255,7 @@ int gmres_run(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodie
 // Inner GMRES of the refinement as one cooperative kernel (FP32 M_bb).
 // The persistent kernel's arguments for one inner solve of s in shape sh.
 PgArgs persistent_args(tfs_solver *s, const PgShape &sh, const double *rhs, double *f_blobs,
-                       double *v_bodies, double tol) {
+                       double *v_bodies, double tol, int vec64) {
   GmresArgs g = gmres_args(s, rhs, f_blobs, v_bodies, s->gst, tol, 1);
   g.G = sh.G;
   g.blobs_per_cta = sh.blobs_per_cta;
@@ -275,8 +275,9 @@ PgArgs persistent_args(tfs_solver *s, const PgShape &sh, const double *rhs, doub
   p.tbs = sh.tbs;
   p.S = sh.S;
   p.chunk = sh.chunk;
-  p.Kr = sh.Kr;
-  p.dyn_smem = sh.dyn_smem;
+  p.vec64 = vec64;
+  p.Kr = vec64 ? sh.Kr64 : sh.Kr;
+  p.dyn_smem = vec64 ? sh.dyn_smem64 : sh.dyn_smem;
   p.a = (float)s->cfg.a_blob;
   const double ab = s->cfg.a_blob;
   p.pc_asum2 = (float)((2.0 * ab) * (2.0 * ab));
@@ -305,12 +306,12 @@ int persistent_result(tfs_solver *s, int *iters) {
 }
 
 int gmres_run_persistent(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies,
-                         double tol, int *iters) {
-  const PgArgs p = persistent_args(s, s->pg, rhs, f_blobs, v_bodies, tol);
+                         double tol, int vec64, int *iters) {
+  const PgArgs p = persistent_args(s, s->pg, rhs, f_blobs, v_bodies, tol, vec64);
   TFS_CUDA(cudaMemcpyAsync(s->pg_gp, &p, sizeof p, cudaMemcpyHostToDevice, s->stream),
            "persistent GMRES arguments");
   TFS_CUDA(cudaMemsetAsync(p.bar, 0, 4 * sizeof(unsigned), s->stream), "persistent GMRES barrier");
-  cudaError_t e = launch_gmres_persistent(s->pg_gp, s->pg_cmap, p.P, p.dyn_smem, s->stream);
+  cudaError_t e = launch_gmres_persistent(s->pg_gp, s->pg_cmap, p.P, p.dyn_smem, vec64, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "persistent GMRES");
   return persistent_result(s, iters);
 }
@@ -388,7 +389,7 @@ struct GmresService {
     TFS_CUDA(cudaMemcpyAsync(dev_map, sl.map, sizeof(int2) * ctas, cudaMemcpyHostToDevice, stream),
              "service: map");
     TFS_CUDA(cudaEventRecord(sl.copied, stream), "service: staging slot");
-    cudaError_t e = launch_gmres_persistent(dev_args, dev_map, ctas, dyn, stream);
+    cudaError_t e = launch_gmres_persistent(dev_args, dev_map, ctas, dyn, 0, stream);
     if (e != cudaSuccess) return cuda_fail(e, "service: persistent GMRES");
     for (Req *r : batch) TFS_CUDA(cudaEventRecord(r->s->done_ev, stream), "service: completion");
     TFS_CUDA(cudaEventRecord(last, stream), "service: completion");
@@ -397,7 +398,7 @@ struct GmresService {
 
   int solve(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies, double tol,
             int *iters) {
-    Req r{s, persistent_args(s, s->pg_group, rhs, f_blobs, v_bodies, tol), false, TFS_OK};
+    Req r{s, persistent_args(s, s->pg_group, rhs, f_blobs, v_bodies, tol, 0), false, TFS_OK};
     TFS_CUDA(cudaEventRecord(s->ready_ev, s->stream), "service: inputs ready");
     std::unique_lock<std::mutex> g(m);
     pending.push_back(&r);
@@ -504,8 +505,79 @@ void service_stats(GmresService *sv, long long *launches, long long *solves) {
 
 namespace {
 
+// Refinement cycles from the iterate in s->xr: the residual in float-float
+// arithmetic, an inner GMRES on it, the update. vec64 runs the cooperative
+// inner solve with FP64 Arnoldi vectors (on the solver's own launch) instead
+// of FP32 ones. *stalled: a cycle did not reduce the residual (the inner
+// solves cannot make progress on this system).
+int refine_cycles(tfs_solver *s, const GmresArgs &g64, int vec64, int *total, int *cycles,
+                  GmresScalars *h, bool *stalled) {
+  const int vel = 3 * s->nb;
+  const bool coop = s->pg_ok && s->pg_enabled;
+  double prev_rel = 0.0;
+  int rc;
+  *stalled = false;
+  for (int it = 0; it <= s->max_outer; ++it) {
+    // the residual's M_bb product in float-float arithmetic (FP64-grade
+    // accuracy at FP32 instruction rates)
+    cudaError_t e = launch_bb_ff(s->x_blobs, s->xr, s->nb, s->origin, s->cfg.a_blob,
+                                 1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu), s->rec_ff, s->vtmp, s->scratch,
+                                 s->scratch_elems, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "refinement residual product");
+    if ((e = launch_refine_residual(g64, s->xr, s->r, s->dx, it, s->stream)) != cudaSuccess)
+      return cuda_fail(e, "refinement residual");
+    if ((rc = poll(s, 1, h)) != TFS_OK) return rc;
+    // a non-finite residual (the kernel then marks the solve done with
+    // status 1): of the input itself at the first cycle, else a stall
+    if (h->status && it == 0)
+      return fail(TFS_ENAN, "non-finite right-hand side or warm start in the mobility solve");
+    if (h->done && !h->status) break;
+    // a cycle that did not reduce the residual (or a non-finite one): the
+    // inner solves cannot make progress on this system
+    if (h->status || !(h->rel == h->rel) || (it > 0 && !(h->rel < prev_rel)) ||
+        it == s->max_outer) {
+      *stalled = true;
+      break;
+    }
+    prev_rel = h->rel;
+    // the inner solve asks only for the reduction the outer target still
+    // needs (with a factor 2 to spare), at most inner_tol's: a good warm
+    // start then costs a few Arnoldi steps instead of a full 1e-4 reduction
+    const double itol = std::max(s->inner_tol, std::min(0.5, 0.5 * s->tol / h->rel));
+    int inner = 0;
+    rc = (coop && vec64) ? gmres_run_persistent(s, s->r, s->dx, s->dx + vel, itol, 1, &inner)
+         : s->service    ? s->service->solve(s, s->r, s->dx, s->dx + vel, itol, &inner)
+         : coop          ? gmres_run_persistent(s, s->r, s->dx, s->dx + vel, itol, 0, &inner)
+                         : gmres_run(s, s->r, s->dx, s->dx + vel, itol, 1, &inner);
+    if (rc != TFS_OK && rc != TFS_ENOTCONV) return rc;
+    *total += inner;
+    ++*cycles;
+    if ((e = launch_axpy(s->xr, s->dx, s->n, s->stream)) != cudaSuccess)
+      return cuda_fail(e, "refinement update");
+  }
+  return TFS_OK;
+}
+
+// xr = the caller's warm start (f_blobs, v_bodies)
+int refine_start(tfs_solver *s) {
+  const int vel = 3 * s->nb;
+  TFS_CUDA(cudaMemcpyAsync(s->xr, s->f_blobs, sizeof(double) * vel, cudaMemcpyDeviceToDevice,
+                           s->stream),
+           "refinement start");
+  TFS_CUDA(cudaMemcpyAsync(s->xr + vel, s->v_bodies, sizeof(double) * 6,
+                           cudaMemcpyDeviceToDevice, s->stream),
+           "refinement start");
+  return TFS_OK;
+}
+
 // The linear solve of compute_velocities on s->rhs: plain FP64 GMRES, or
-// FP32C iterative refinement.
+// FP32C iterative refinement. The cooperative inner solves run with FP32
+// Arnoldi vectors, except while the body mobility is still the identity
+// make_body_reference_matrices starts from: that preconditioner leaves the
+// body rows unscaled against the blob rows, beyond what an FP32 basis
+// resolves, so those solves take FP64 vectors. A refinement that stalls
+// with FP32 vectors is run again from the warm start with FP64 ones, and
+// one that stalls with those finishes in plain FP64 GMRES.
 int linear_solve(tfs_solver *s, int *iters) {
   const int fp32 = s->cfg.precision == TFS_FP32C;
   int rc;
@@ -516,54 +588,21 @@ int linear_solve(tfs_solver *s, int *iters) {
   }
   if ((rc = ensure_origin(s)) != TFS_OK) return rc;
   const int vel = 3 * s->nb;
-  TFS_CUDA(cudaMemcpyAsync(s->xr, s->f_blobs, sizeof(double) * vel, cudaMemcpyDeviceToDevice,
-                           s->stream),
-           "refinement start");
-  TFS_CUDA(cudaMemcpyAsync(s->xr + vel, s->v_bodies, sizeof(double) * 6,
-                           cudaMemcpyDeviceToDevice, s->stream),
-           "refinement start");
   GmresScalars *outer = s->gst + 1;
   const GmresArgs g64 = gmres_args(s, s->rhs, nullptr, nullptr, outer, s->tol, 0);
   int total = 0, cycles = 0;
   GmresScalars h{};
-  double prev_rel = 0.0;
   bool stalled = false;
-  for (int it = 0; it <= s->max_outer; ++it) {
-    // the residual's M_bb product in float-float arithmetic (FP64-grade
-    // accuracy at FP32 instruction rates)
-    cudaError_t e = launch_bb_ff(s->x_blobs, s->xr, s->nb, s->origin, s->cfg.a_blob,
-                                 1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu), s->rec_ff, s->vtmp, s->scratch,
-                                 s->scratch_elems, s->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "refinement residual product");
-    if ((e = launch_refine_residual(g64, s->xr, s->r, s->dx, it, s->stream)) != cudaSuccess)
-      return cuda_fail(e, "refinement residual");
-    if ((rc = poll(s, 1, &h)) != TFS_OK) return rc;
-    // a non-finite residual (the kernel then marks the solve done with
-    // status 1): of the input itself at the first cycle, else a stall
-    if (h.status && it == 0)
-      return fail(TFS_ENAN, "non-finite right-hand side or warm start in the mobility solve");
-    if (h.done && !h.status) break;
-    // a cycle that did not reduce the residual (or a non-finite one): the
-    // FP32 inner products cannot make progress on this system
-    if (h.status || !(h.rel == h.rel) || (it > 0 && !(h.rel < prev_rel)) || it == s->max_outer) {
-      stalled = true;
-      break;
-    }
-    prev_rel = h.rel;
-    // the inner solve asks only for the reduction the outer target still
-    // needs (with a factor 2 to spare), at most inner_tol's: a good warm
-    // start then costs a few Arnoldi steps instead of a full 1e-4 reduction
-    const double itol = std::max(s->inner_tol, std::min(0.5, 0.5 * s->tol / h.rel));
-    int inner = 0;
-    rc = s->service ? s->service->solve(s, s->r, s->dx, s->dx + vel, itol, &inner)
-         : (s->pg_ok && s->pg_enabled)
-             ? gmres_run_persistent(s, s->r, s->dx, s->dx + vel, itol, &inner)
-             : gmres_run(s, s->r, s->dx, s->dx + vel, itol, 1, &inner);
-    if (rc != TFS_OK && rc != TFS_ENOTCONV) return rc;
-    total += inner;
-    ++cycles;
-    if ((e = launch_axpy(s->xr, s->dx, s->n, s->stream)) != cudaSuccess)
-      return cuda_fail(e, "refinement update");
+  int vec64 = s->bootstrap ? 1 : 0;
+  if ((rc = refine_start(s)) != TFS_OK ||
+      (rc = refine_cycles(s, g64, vec64, &total, &cycles, &h, &stalled)) != TFS_OK)
+    return rc;
+  if (stalled && !vec64 && s->pg_ok && s->pg_enabled) {
+    vec64 = 1;
+    ++s->vec64_retries;
+    if ((rc = refine_start(s)) != TFS_OK ||
+        (rc = refine_cycles(s, g64, vec64, &total, &cycles, &h, &stalled)) != TFS_OK)
+      return rc;
   }
   if (stalled) {
     // finish in FP64 from the caller's warm start (f_blobs, v_bodies are
@@ -796,7 +835,10 @@ int tfs_make_body_reference_matrices(tfs_solver *s) {
     cudaError_t e = launch_unit_rhs(s->rhs, s->n, j, s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "unit rhs");
     int iters = 0;
-    if ((rc = linear_solve(s, &iters)) != TFS_OK) return rc;
+    s->bootstrap = true;
+    rc = linear_solve(s, &iters);
+    s->bootstrap = false;
+    if (rc != TFS_OK) return rc;
     TFS_CUDA(cudaMemcpyAsync(s->f6_host, s->v_bodies, 8 * 6, cudaMemcpyDeviceToHost, s->stream),
              "read body velocity");
     TFS_CUDA(cudaStreamSynchronize(s->stream), "read body velocity");
@@ -911,6 +953,13 @@ int tfs_pg_trace(unsigned long long *stamps, int capacity, int *steps) {
 int tfs_copy_blob_forces_to_host_f32(tfs_solver *s, float *f_blobs_host) {
   TFS_CHECK_SOLVER(s);
   return d2h_f32(s, f_blobs_host, s->f_blobs, 3 * (size_t)s->nb, "copy blob forces to host");
+}
+
+int tfs_refinement_retries(tfs_solver *s, long long *retries) {
+  TFS_CHECK_SOLVER(s);
+  if (retries == nullptr) return fail(TFS_EINVAL, "null argument");
+  *retries = s->vec64_retries;
+  return TFS_OK;
 }
 
 int tfs_solve_info(tfs_solver *s, int *iters, int *cycles, double *rel_residual) {

@@ -45,6 +45,8 @@ struct tfs_solver {
   int max_iter = 350;        // MAX_LINEAR_SYSTEM_ITER, capped at n
   double tol = 1e-4;         // LINEAR_SYSTEM_TOL
   double inner_tol = 1e-4;   // FP32C: inner GMRES tolerance of each refinement cycle
+  bool bootstrap = false;    // the solves of make_body_reference_matrices are running
+  long long vec64_retries = 0;  // FP32C refinements rerun with FP64 Arnoldi vectors
   int max_outer = 12;        // FP32C: refinement cycles
   int chunk = 8;             // Arnoldi steps launched between polls of the done flag
   bool have_refs = false;

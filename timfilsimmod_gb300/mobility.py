@@ -324,6 +324,12 @@ class RpyMobilitySolver:
         self._call("tfs_solve_info", ctypes.byref(it), ctypes.byref(cyc), ctypes.byref(rel))
         return {"iters": it.value, "cycles": cyc.value, "rel_residual": rel.value}
 
+    def refinement_retries(self) -> int:
+        """FP32C refinements rerun with FP64 Arnoldi vectors after a stall."""
+        n = ctypes.c_longlong()
+        self._call("tfs_refinement_retries", ctypes.byref(n))
+        return n.value
+
     # -- convenience: set all inputs from arrays (AoS float64)
     def set_state(self, x_segs, f_segs, x_blobs, f_blobs) -> None:
         self.x_segs_host[:] = np.asarray(x_segs, dtype=np.float64).ravel()
