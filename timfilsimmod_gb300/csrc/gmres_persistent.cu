@@ -117,13 +117,25 @@ __device__ unsigned long long g_pg_trace[2][kTraceSteps][kTracePhases];
   } while (0)
 #endif
 
+// Release-add to and acquire-load of a barrier word at GPU scope.
+__device__ __forceinline__ void red_release(unsigned *w, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(w), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *w) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(w) : "memory");
+  return v;
+}
+
 // Bounded grid barrier; false in every thread of the CTA if it was abandoned.
 // bar[0] counts arrivals over the whole launch (zeroed before it): the e-th
 // barrier of a solve is passed once it reaches e * P, so no CTA has to reset
 // it (each CTA keeps its own count e in *epoch, shared memory). bar[2] is
-// the abort word. Every CTA's prior writes are ordered before its arrival by
-// the CTA barrier plus a device-scope fence, and reads after the barrier
-// bypass L1 (ld.global.cg) wherever they read other CTAs' data.
+// the abort word. After the CTA barrier, thread 0 arrives with a release
+// reduction (cumulative: it orders every write the CTA made before the CTA
+// barrier) and polls with acquire loads, so the CTA's later reads see what
+// every CTA wrote before arriving; those reads bypass L1 (ld.global.cg)
+// wherever they read other CTAs' data.
 __device__ bool pg_barrier(const PgArgs &p, unsigned *epoch) {
   __shared__ int ok;
   __syncthreads();
@@ -132,23 +144,21 @@ __device__ bool pg_barrier(const PgArgs &p, unsigned *epoch) {
     int good = 1;
     const unsigned target = (*epoch + 1u) * ((unsigned)p.P + p.bar_extra);
     *epoch += 1u;
-    __threadfence();
-    atomicAdd(p.bar, 1u);
+    red_release(p.bar, 1u);
     const unsigned long long t0 = global_ns();
     unsigned spins = 0;
-    while (vb[0] < target) {
-      if (vb[2] != 0u) {  // another CTA gave up
+    while (ld_acquire(p.bar) < target) {
+      ++spins;
+      if ((spins & 15u) == 0u && vb[2] != 0u) {  // another CTA gave up
         good = 0;
         break;
       }
-      ++spins;
       if (spins > (1u << 25) || ((spins & 63u) == 0 && global_ns() - t0 > kPgTimeoutNs)) {
         atomicExch(p.bar + 2, 1u);
         good = 0;
         break;
       }
     }
-    __threadfence();
     if (!good) {
       atomicExch(&p.g.st->status, 2);
       atomicExch(&p.g.st->done, 1);
@@ -341,11 +351,74 @@ __device__ void pack_records(const PgArgs &p, const PSlice<V> &sl, const V *fs) 
   }
 }
 
+// One staged tile of M_bb for the NT targets of this thread (NT = 1 in a
+// warp where no lane has a second target), FP32 pairs; the tile's sum is
+// added compensated into (hi, lo).
+template <int NT>
+__device__ __forceinline__ void mbb_tile(const float (&xt)[2], const float (&yt)[2],
+                                         const float (&zt)[2], const int (&i)[2], int base,
+                                         int cnt, const float *src, const PairConst<float> &pc,
+                                         float (&hi)[2][3], float (&lo)[2][3]) {
+  float x[NT], y[NT], z[NT], v[NT][3];
+  unsigned nf[NT];  // pairs inside the contact distance
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    x[t] = xt[t];
+    y[t] = yt[t];
+    z[t] = zt[t];
+    nf[t] = 0u;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v[t][k] = 0.f;
+  }
+#pragma unroll 2
+  for (int j = 0; j < cnt; ++j) {
+    float sx, sy, sz, f[3];
+    RecLoad<float, 3>::get(src + 8 * j, sx, sy, sz, f);
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const float dx = x[t] - sx, dy = y[t] - sy, dz = z[t] - sz;
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const bool far = r2 > pc.asum2;
+      nf[t] += far ? 0u : 1u;
+      const float rs = rsqrt_far(r2);
+      far_pair<float, 3, 3>(v[t], dx, dy, dz, far ? rs : 0.f, f, pc);
+    }
+  }
+  // a target whose only pair inside the contact distance in this tile is
+  // its own blob (r = 0) takes the self term 4/(3a) F here (the nested
+  // branch of the pair function at r = 0); targets with any other such
+  // pair rescan the tile with the full formula, self pair included
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    const int js = i[t] - base;
+    const unsigned self_in = (js >= 0 && js < cnt) ? 1u : 0u;
+    if (nf[t] == self_in) {
+      if (self_in) {
+        float sx, sy, sz, f[3];
+        RecLoad<float, 3>::get(src + 8 * js, sx, sy, sz, f);
+        const float A = 4.f / (3.f * pc.ai);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v[t][k] += A * f[k];
+      }
+      nf[t] = 0u;
+    }
+  }
+  unsigned any = 0u;
+#pragma unroll
+  for (int t = 0; t < NT; ++t) any |= nf[t];
+  if (__any_sync(0xffffffffu, any != 0u)) near_pass<float, 3, 3, NT>(v, x, y, z, nf, src, cnt, pc);
+#pragma unroll
+  for (int t = 0; t < NT; ++t)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) two_sum(hi[t][k], lo[t][k], v[t][k]);
+}
+
 // M_bb of the packed records: (target block x source split) units over the
-// CTAs other than CTA 0 (which meanwhile runs the Givens step), two targets
-// per thread, FP32 pairs, per-tile compensated sums; each split's sum is
-// written as its (hi, lo) FP32 pair mpart[(split * nb + target) * 3 + k]
-// (the consumer adds the splits compensated and scales by 1 / (8 pi mu)).
+// CTAs other than CTA 0 (which meanwhile runs the Givens step), up to two
+// targets per thread (warps whose lanes all have one take the one-target
+// pass), FP32 pairs, per-tile compensated sums; each split's sum is written
+// as its (hi, lo) FP32 pair mpart[(split * nb + target) * 3 + k] (the
+// consumer adds the splits compensated and scales by 1 / (8 pi mu)).
 __device__ void mbb_units(const PgArgs &p, float *src) {
   const int nb = p.g.nb;
   const int units = p.TB * p.S;
@@ -377,6 +450,7 @@ __device__ void mbb_units(const PgArgs &p, float *src) {
       for (int k = 0; k < 3; ++k) hi[t][k] = lo[t][k] = 0.f;
     }
     const bool warp_active = __any_sync(0xffffffffu, act[0] || act[1]);
+    const bool two = __any_sync(0xffffffffu, act[1]);
     for (int base = s0; base < s1; base += kPTS) {
       const int cnt = min(kPTS, s1 - base);
       __syncthreads();
@@ -385,47 +459,8 @@ __device__ void mbb_units(const PgArgs &p, float *src) {
       for (int q = threadIdx.x; q < 2 * cnt; q += kPB) d[q] = __ldcg(g + q);
       __syncthreads();
       if (!warp_active) continue;
-      float v[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-      unsigned nf[2] = {0u, 0u};  // pairs inside the contact distance
-#pragma unroll 2
-      for (int j = 0; j < cnt; ++j) {
-        float sx, sy, sz, f[3];
-        RecLoad<float, 3>::get(src + 8 * j, sx, sy, sz, f);
-#pragma unroll
-        for (int t = 0; t < 2; ++t) {
-          const float dx = xt[t] - sx, dy = yt[t] - sy, dz = zt[t] - sz;
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const bool far = r2 > pc.asum2;
-          nf[t] += far ? 0u : 1u;
-          const float rs = rsqrt_far(r2);
-          far_pair<float, 3, 3>(v[t], dx, dy, dz, far ? rs : 0.f, f, pc);
-        }
-      }
-      // a target whose only pair inside the contact distance in this tile is
-      // its own blob (r = 0) takes the self term 4/(3a) F here (the nested
-      // branch of the pair function at r = 0); targets with any other such
-      // pair rescan the tile with the full formula, self pair included
-#pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        const int js = i[t] - base;
-        const unsigned self_in = (js >= 0 && js < cnt) ? 1u : 0u;
-        if (nf[t] == self_in) {
-          if (self_in) {
-            float sx, sy, sz, f[3];
-            RecLoad<float, 3>::get(src + 8 * js, sx, sy, sz, f);
-            const float A = 4.f / (3.f * pc.ai);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) v[t][k] += A * f[k];
-          }
-          nf[t] = 0u;
-        }
-      }
-      if (__any_sync(0xffffffffu, (nf[0] | nf[1]) != 0u))
-        near_pass<float, 3, 3, 2>(v, xt, yt, zt, nf, src, cnt, pc);
-#pragma unroll
-      for (int t = 0; t < 2; ++t)
-#pragma unroll
-        for (int k = 0; k < 3; ++k) two_sum(hi[t][k], lo[t][k], v[t][k]);
+      if (two) mbb_tile<2>(xt, yt, zt, i, base, cnt, src, pc, hi, lo);
+      else mbb_tile<1>(xt, yt, zt, i, base, cnt, src, pc, hi, lo);
     }
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
