@@ -82,14 +82,25 @@ bool invert6(double *A) {
   return true;
 }
 
+// The 72 doubles of the rotated body matrices, passed to the device as a
+// kernel argument (copied at launch, so the host needs no staging buffer that
+// must outlive the copy, and no wait).
+struct Mats72 {
+  double v[72];
+};
+
+__global__ void set_mats_kernel(Mats72 m, double *__restrict__ dst) {
+  if (threadIdx.x < 72) dst[threadIdx.x] = m.v[threadIdx.x];
+}
+
 int upload_mats(tfs_solver *s) {
   rotate_blocks(s->mats_host, s->body_mob_ref, s->pose.R);
   rotate_blocks(s->mats_host + 36, s->ktkinv_ref, s->pose.R);
-  TFS_CUDA(cudaMemcpyAsync(s->mats, s->mats_host, sizeof s->mats_host, cudaMemcpyHostToDevice,
-                           s->stream),
-           "upload body matrices");
-  // the staging buffer may change before an asynchronous copy runs
-  TFS_CUDA(cudaStreamSynchronize(s->stream), "upload body matrices");
+  Mats72 m;
+  std::memcpy(m.v, s->mats_host, sizeof m.v);
+  set_mats_kernel<<<1, 96, 0, s->stream>>>(m, s->mats);
+  TFS_CUDA(cudaGetLastError(), "upload body matrices");
+  count_launch();
   return TFS_OK;
 }
 
@@ -161,6 +172,17 @@ int poll(tfs_solver *s, int which, GmresScalars *out) {
            "read solver state");
   TFS_CUDA(cudaStreamSynchronize(s->stream), "read solver state");
   *out = s->gst_host[which];
+  return TFS_OK;
+}
+
+// Both scalar sets (inner solve, refinement) with one copy and one wait.
+int poll_both(tfs_solver *s, GmresScalars *inner, GmresScalars *outer) {
+  TFS_CUDA(cudaMemcpyAsync(s->gst_host, s->gst, 2 * sizeof(GmresScalars), cudaMemcpyDeviceToHost,
+                           s->stream),
+           "read solver state");
+  TFS_CUDA(cudaStreamSynchronize(s->stream), "read solver state");
+  *inner = s->gst_host[0];
+  *outer = s->gst_host[1];
   return TFS_OK;
 }
 
@@ -292,28 +314,26 @@ PgArgs persistent_args(tfs_solver *s, const PgShape &sh, const double *rhs, doub
   return p;
 }
 
-// The result of an inner persistent solve (its scalars, read on s->stream).
-int persistent_result(tfs_solver *s, int *iters) {
-  GmresScalars h{};
-  int rc;
-  if ((rc = poll(s, 0, &h)) != TFS_OK) return rc;
+// The result of a finished inner persistent solve from its scalars.
+int persistent_result(const GmresScalars &h, int *iters) {
   if (h.status == 2) return fail(TFS_ETIMEOUT, "persistent GMRES: a grid barrier timed out");
   if (h.status == 1) return fail(TFS_ENAN, "GMRES residual is not finite");
   if (!h.done) return fail(TFS_ESTATE, "persistent GMRES ended without a result");
   *iters = h.iters;
-  s->last_rel = h.rel;
   return TFS_OK;
 }
 
-int gmres_run_persistent(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies,
-                         double tol, int vec64, int *iters) {
+// Queues an inner persistent solve on s->stream; its scalars (s->gst[0])
+// are read by the caller's next poll.
+int gmres_launch_persistent(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies,
+                            double tol, int vec64) {
   const PgArgs p = persistent_args(s, s->pg, rhs, f_blobs, v_bodies, tol, vec64);
   TFS_CUDA(cudaMemcpyAsync(s->pg_gp, &p, sizeof p, cudaMemcpyHostToDevice, s->stream),
            "persistent GMRES arguments");
   TFS_CUDA(cudaMemsetAsync(p.bar, 0, 4 * sizeof(unsigned), s->stream), "persistent GMRES barrier");
   cudaError_t e = launch_gmres_persistent(s->pg_gp, s->pg_cmap, p.P, p.dyn_smem, vec64, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "persistent GMRES");
-  return persistent_result(s, iters);
+  return TFS_OK;
 }
 
 }  // namespace
@@ -396,8 +416,9 @@ struct GmresService {
     return TFS_OK;
   }
 
-  int solve(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies, double tol,
-            int *iters) {
+  // Queues s's inner solve in a shared launch; s->stream waits for it, and
+  // its scalars (s->gst[0]) are read by the caller's next poll.
+  int solve(tfs_solver *s, const double *rhs, double *f_blobs, double *v_bodies, double tol) {
     Req r{s, persistent_args(s, s->pg_group, rhs, f_blobs, v_bodies, tol, 0), false, TFS_OK};
     TFS_CUDA(cudaEventRecord(s->ready_ev, s->stream), "service: inputs ready");
     std::unique_lock<std::mutex> g(m);
@@ -435,7 +456,7 @@ struct GmresService {
     g.unlock();
     if (r.rc != TFS_OK) return r.rc;
     TFS_CUDA(cudaStreamWaitEvent(s->stream, s->done_ev, 0), "service: wait for the solve");
-    return persistent_result(s, iters);
+    return TFS_OK;
   }
 };
 
@@ -506,16 +527,23 @@ void service_stats(GmresService *sv, long long *launches, long long *solves) {
 namespace {
 
 // Refinement cycles from the iterate in s->xr: the residual in float-float
-// arithmetic, an inner GMRES on it, the update. vec64 runs the cooperative
-// inner solve with FP64 Arnoldi vectors (on the solver's own launch) instead
-// of FP32 ones. *stalled: a cycle did not reduce the residual (the inner
-// solves cannot make progress on this system).
+// arithmetic, an inner GMRES on it, the update. The inner solve runs in the
+// shared launch of s->service, else on the solver's own cooperative launch
+// (when enabled), else as the kernel sequence; vec64 runs the cooperative
+// solve with FP64 Arnoldi vectors (on the solver's own launch) instead of
+// FP32 ones. *stalled: a cycle did not reduce the residual (the inner solves
+// cannot make progress on this system).
 int refine_cycles(tfs_solver *s, const GmresArgs &g64, int vec64, int *total, int *cycles,
                   GmresScalars *h, bool *stalled) {
   const int vel = 3 * s->nb;
-  const bool coop = s->pg_ok && s->pg_enabled;
+  // the solver's own cooperative launch: when enabled, and for FP64 vectors
+  // of a swimmer whose FP32 solves go to a shared launch
+  const bool own = s->pg_ok && (s->pg_enabled || (vec64 && s->service));
   double prev_rel = 0.0;
   int rc;
+  // a queued cooperative inner solve whose scalars are read with the next
+  // residual's (one host wait per cycle)
+  bool pending = false;
   *stalled = false;
   for (int it = 0; it <= s->max_outer; ++it) {
     // the residual's M_bb product in float-float arithmetic (FP64-grade
@@ -526,7 +554,16 @@ int refine_cycles(tfs_solver *s, const GmresArgs &g64, int vec64, int *total, in
     if (e != cudaSuccess) return cuda_fail(e, "refinement residual product");
     if ((e = launch_refine_residual(g64, s->xr, s->r, s->dx, it, s->stream)) != cudaSuccess)
       return cuda_fail(e, "refinement residual");
-    if ((rc = poll(s, 1, h)) != TFS_OK) return rc;
+    if (pending) {
+      GmresScalars hin{};
+      int inner = 0;
+      if ((rc = poll_both(s, &hin, h)) != TFS_OK || (rc = persistent_result(hin, &inner)) != TFS_OK)
+        return rc;
+      *total += inner;
+      pending = false;
+    } else if ((rc = poll(s, 1, h)) != TFS_OK) {
+      return rc;
+    }
     // a non-finite residual (the kernel then marks the solve done with
     // status 1): of the input itself at the first cycle, else a stall
     if (h->status && it == 0)
@@ -545,12 +582,18 @@ int refine_cycles(tfs_solver *s, const GmresArgs &g64, int vec64, int *total, in
     // start then costs a few Arnoldi steps instead of a full 1e-4 reduction
     const double itol = std::max(s->inner_tol, std::min(0.5, 0.5 * s->tol / h->rel));
     int inner = 0;
-    rc = (coop && vec64) ? gmres_run_persistent(s, s->r, s->dx, s->dx + vel, itol, 1, &inner)
-         : s->service    ? s->service->solve(s, s->r, s->dx, s->dx + vel, itol, &inner)
-         : coop          ? gmres_run_persistent(s, s->r, s->dx, s->dx + vel, itol, 0, &inner)
-                         : gmres_run(s, s->r, s->dx, s->dx + vel, itol, 1, &inner);
-    if (rc != TFS_OK && rc != TFS_ENOTCONV) return rc;
-    *total += inner;
+    if (s->service && !vec64) {  // a shared launch (FP32 vectors)
+      if ((rc = s->service->solve(s, s->r, s->dx, s->dx + vel, itol)) != TFS_OK) return rc;
+      pending = true;
+    } else if (own) {
+      if ((rc = gmres_launch_persistent(s, s->r, s->dx, s->dx + vel, itol, vec64)) != TFS_OK)
+        return rc;
+      pending = true;
+    } else {
+      rc = gmres_run(s, s->r, s->dx, s->dx + vel, itol, 1, &inner);
+      if (rc != TFS_OK && rc != TFS_ENOTCONV) return rc;
+      *total += inner;
+    }
     ++*cycles;
     if ((e = launch_axpy(s->xr, s->dx, s->n, s->stream)) != cudaSuccess)
       return cuda_fail(e, "refinement update");
@@ -597,7 +640,7 @@ int linear_solve(tfs_solver *s, int *iters) {
   if ((rc = refine_start(s)) != TFS_OK ||
       (rc = refine_cycles(s, g64, vec64, &total, &cycles, &h, &stalled)) != TFS_OK)
     return rc;
-  if (stalled && !vec64 && s->pg_ok && s->pg_enabled) {
+  if (stalled && !vec64 && s->pg_ok && (s->pg_enabled || s->service)) {
     vec64 = 1;
     ++s->vec64_retries;
     if ((rc = refine_start(s)) != TFS_OK ||
@@ -863,17 +906,20 @@ int tfs_set_body_reference_matrices(tfs_solver *s, const double *body_mobility,
   return upload_mats(s);
 }
 
-int tfs_compute_velocities(tfs_solver *s, double *swimmer_f, int *gmres_iters) {
-  TFS_CHECK_SOLVER(s);
-  if (swimmer_f == nullptr) return fail(TFS_EINVAL, "null swimmer force");
+}  // extern "C"
+
+namespace tfs {
+
+// compute_velocities on the swimmer force already on the device
+// (s->swimmer_f, updated in place with the blob repulsion's sums as the
+// reference updates swimmer::f): queued on s->stream with one host wait per
+// refinement cycle and none at the end.
+int compute_velocities_dev(tfs_solver *s, int *gmres_iters) {
   if (s->cfg.nswim != 1) return fail(TFS_EINVAL, "compute_velocities solves one swimmer per solver");
   if (!s->have_refs) return fail(TFS_ESTATE, "set the blob references first");
   int rc;
   // read_positions_and_forces: barrier forces (device f_segs, blob repulsion)
   if ((rc = tfs_apply_interparticle_forces(s)) != TFS_OK) return rc;
-  std::memcpy(s->f6_host, swimmer_f, 8 * 6);
-  TFS_CUDA(cudaMemcpyAsync(s->swimmer_f, s->f6_host, 8 * 6, cudaMemcpyHostToDevice, s->stream),
-           "copy swimmer force");
   // v_segs = Mss f_segs, v_blobs = Mbs f_segs (one work-queue launch when
   // both target sets exist)
   if (s->ns > 0 && s->nb > 0) {
@@ -889,12 +935,27 @@ int tfs_compute_velocities(tfs_solver *s, double *swimmer_f, int *gmres_iters) {
   if ((rc = linear_solve(s, &iters)) != TFS_OK) return rc;
   // v_segs += Msb f_blobs (the solved blob forces)
   if ((rc = tfs_evaluate_segment_blob_mobility(s)) != TFS_OK) return rc;
+  s->last_iters = iters;
+  if (gmres_iters) *gmres_iters = iters;
+  return TFS_OK;
+}
+
+}  // namespace tfs
+
+extern "C" {
+
+int tfs_compute_velocities(tfs_solver *s, double *swimmer_f, int *gmres_iters) {
+  TFS_CHECK_SOLVER(s);
+  if (swimmer_f == nullptr) return fail(TFS_EINVAL, "null swimmer force");
+  std::memcpy(s->f6_host, swimmer_f, 8 * 6);
+  TFS_CUDA(cudaMemcpyAsync(s->swimmer_f, s->f6_host, 8 * 6, cudaMemcpyHostToDevice, s->stream),
+           "copy swimmer force");
+  int rc = compute_velocities_dev(s, gmres_iters);
+  if (rc != TFS_OK) return rc;
   TFS_CUDA(cudaMemcpyAsync(s->f6_host, s->swimmer_f, 8 * 6, cudaMemcpyDeviceToHost, s->stream),
            "read swimmer force");
   TFS_CUDA(cudaStreamSynchronize(s->stream), "compute_velocities");
   std::memcpy(swimmer_f, s->f6_host, 8 * 6);
-  s->last_iters = iters;
-  if (gmres_iters) *gmres_iters = iters;
   return TFS_OK;
 }
 

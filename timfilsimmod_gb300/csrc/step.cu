@@ -306,6 +306,17 @@ __global__ void __launch_bounds__(32 * kFilWarps) k_swimmer_force(StepDev d, dou
     for (int k = 0; k < 6; ++k) swf_part[6 * fil + k] = sw[k];
 }
 
+// swimmer::f = the sum of the filaments' partial force and torque sums
+// (swimmer.cpp:469-529): warp k adds component k over the
+// filaments, lanes strided, then a fixed shuffle tree.
+__global__ void k_swimmer_sum(const double *__restrict__ part, int nfil, double *__restrict__ out) {
+  const int lane = threadIdx.x & 31, k = threadIdx.x >> 5;
+  double s = 0.0;
+  for (int i = lane; i < nfil; i += 32) s += part[6 * (size_t)i + k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[k] = s;
+}
+
 // BDF residuals (mobility_solver.cpp:2661-2946), one thread per segment; the
 // body's six entries by thread 0. Sets bit 0 of *flag if any entry exceeds
 // the tolerance (TOL DL for positions, TOL for Lie-algebra elements) and
@@ -1122,7 +1133,6 @@ struct tfs_stepper {
   // body state (rigid_body::x, xm1, xm2, u, um1, q, qm1, Q_init)
   double bx[3], bxm1[3], bxm2[3], bu[3], bum1[3], bq[4], bqm1[4];
   double Qinit[9];
-  double swf[6];          // swimmer force and torque (swimmer::f)
   double schur_inv[36];   // row-major
   double *schur_dev = nullptr;
   double *err = nullptr, *nerr = nullptr, *upd = nullptr, *tin = nullptr, *tout = nullptr;
@@ -1563,23 +1573,39 @@ int tfs_stepper_forces(tfs_stepper *st, int nt, double *swimmer_f) {
   k_swimmer_force<<<(d.nfil + kFilWarps - 1) / kFilWarps, 32 * kFilWarps, 0, str>>>(
       d, st->bx[0], st->bx[1], st->bx[2], st->swpart);
   ST_LAUNCH("swimmer force");
-  ST_CUDA(cudaMemcpyAsync(st->hbuf, st->swpart, sizeof(double) * 6 * d.nfil, cudaMemcpyDeviceToHost, str),
-          "swimmer force");
-  ST_CUDA(cudaStreamSynchronize(str), "internal forces");
-  for (int k = 0; k < 6; ++k) st->swf[k] = 0.0;
-  for (int i = 0; i < d.nfil; ++i)
-    for (int k = 0; k < 6; ++k) st->swf[k] += st->hbuf[6 * i + k];
-  if (swimmer_f) std::memcpy(swimmer_f, st->swf, sizeof st->swf);
+  // swimmer::f on the device, where compute_velocities reads it
+  k_swimmer_sum<<<1, 6 * 32, 0, str>>>(st->swpart, d.nfil, st->s->swimmer_f);
+  ST_LAUNCH("swimmer force sum");
+  if (swimmer_f) {
+    ST_CUDA(cudaMemcpyAsync(st->hbuf, st->s->swimmer_f, sizeof(double) * 6, cudaMemcpyDeviceToHost,
+                            str),
+            "swimmer force");
+    ST_CUDA(cudaStreamSynchronize(str), "internal forces");
+    std::memcpy(swimmer_f, st->hbuf, sizeof(double) * 6);
+  }
   return TFS_OK;
 }
+
+namespace {
+
+// The solve of one Broyden iteration at the current pose, on the swimmer
+// force the last forces call left on the device; no host wait at the end.
+int stepper_velocities(tfs_stepper *st, int *gmres_iters) {
+  int rc = tfs_set_body_pose(st->s, st->bx, st->bq);
+  if (rc != TFS_OK) return rc;
+  st->s->origin_dirty = true;
+  return tfs::compute_velocities_dev(st->s, gmres_iters);
+}
+
+}  // namespace
 
 int tfs_stepper_compute_velocities(tfs_stepper *st, int nt, int *gmres_iters) {
   TFS_CHECK_STEPPER(st);
   (void)nt;
-  int rc = tfs_set_body_pose(st->s, st->bx, st->bq);
+  const int rc = stepper_velocities(st, gmres_iters);
   if (rc != TFS_OK) return rc;
-  st->s->origin_dirty = true;
-  return tfs_compute_velocities(st->s, st->swf, gmres_iters);
+  ST_CUDA(cudaStreamSynchronize(st->s->stream), "compute_velocities");
+  return TFS_OK;
 }
 
 int tfs_stepper_compute_errors(tfs_stepper *st, int nt, int which, double *err_host, int *too_large) {
@@ -1759,7 +1785,7 @@ int tfs_stepper_step(tfs_stepper *st, int nt, int *broyden_iters, int *gmres_ite
   int rc, it = 0, total = 0, big = 0;
   if ((rc = tfs_stepper_initial_guess(st, nt)) != TFS_OK) return rc;
   if ((rc = tfs_stepper_forces(st, nt, nullptr)) != TFS_OK) return rc;
-  if ((rc = tfs_stepper_compute_velocities(st, nt, &it)) != TFS_OK) return rc;
+  if ((rc = stepper_velocities(st, &it)) != TFS_OK) return rc;
   total += it;
   if ((rc = tfs_stepper_compute_errors(st, nt, 0, nullptr, &big)) != TFS_OK) return rc;
   if (big && (rc = tfs_stepper_prepare_jacobian_inv(st, nt, nullptr)) != TFS_OK) return rc;
@@ -1767,7 +1793,7 @@ int tfs_stepper_step(tfs_stepper *st, int nt, int *broyden_iters, int *gmres_ite
   while (big && st->iter < st->cfg.max_broyden_iter) {
     if ((rc = tfs_stepper_find_update(st, nt, nullptr)) != TFS_OK) return rc;
     if ((rc = tfs_stepper_apply_update(st, nt)) != TFS_OK) return rc;
-    if ((rc = tfs_stepper_compute_velocities(st, nt, &it)) != TFS_OK) return rc;
+    if ((rc = stepper_velocities(st, &it)) != TFS_OK) return rc;
     total += it;
     if ((rc = tfs_stepper_compute_errors(st, nt, 1, nullptr, &big)) != TFS_OK) return rc;
     if ((rc = tfs_stepper_end_of_iter(st, nt, big)) != TFS_OK) return rc;

@@ -159,4 +159,7 @@ void product_service_destroy(ProductService *sv);
 int product_service_attach(ProductService *sv, tfs_solver *s);
 int product_service_run(ProductService *sv, tfs_solver *s, int kind, int fp32, int src);
 void product_service_stats(ProductService *sv, long long *launches, long long *products);
+// compute_velocities on the swimmer force already in s->swimmer_f, queued on
+// s->stream without a host wait at the end (solve.cu).
+int compute_velocities_dev(tfs_solver *s, int *gmres_iters);
 }  // namespace tfs
