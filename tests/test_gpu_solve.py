@@ -198,6 +198,39 @@ def test_persistent_and_kernel_sequence_agree():
         assert rel_max(x, y) < 2e-5
 
 
+def test_persistent_large_slices_agree():
+    """10 242 blobs (the large swimmer's body, R = 150) with 64 filaments: 68
+    blobs per cooperative CTA on 152 SMs, beyond the 64 of the smaller
+    swimmers' slices. The cooperative inner GMRES and the kernel sequence
+    reach the same refined solve, as at the medium swimmer."""
+    from timfilsimmod_gb300.geometry import make_config
+
+    sw = make_config("large", seed=3, nfil=64, shape="straight")
+    F = sw.f_segs[:, :3].sum(0)
+    T = (np.cross(sw.x_segs, sw.f_segs[:, :3]) + sw.f_segs[:, 3:]).sum(0)
+    out = {}
+    for form in ("fp32c", "fp32c_kernels"):
+        s = new_solver(sw.nfil, sw.nseg, sw.num_blobs, form)
+        s.set_blob_references(sw.blob_references)
+        s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+        s.set_linear_solver(1e-8)
+        set_segments(s, sw.x_segs, sw.f_segs)
+        bm, _ = s.make_body_reference_matrices()
+        it, _ = s.compute_velocities(np.concatenate([F, T]))
+        s.copy_segment_velocities_to_host()
+        s.wait_for_device()
+        out[form] = (it, s.v_segs_host.copy(), s.blob_forces(), s.body_velocities(), bm,
+                     s.solve_info(), s.refinement_retries())
+        s.finalise()
+    a, b = out["fp32c"], out["fp32c_kernels"]
+    print("iters", a[0], b[0], a[5], b[5], "retries", a[6])
+    assert a[5]["rel_residual"] <= 1e-8 and b[5]["rel_residual"] <= 1e-8
+    assert a[5]["cycles"] > 0 and a[6] == 0  # refined with FP32 vectors, no fallback
+    assert abs(a[0] - b[0]) <= max(3, b[0] // 10)
+    for x, y in zip(a[1:5], b[1:5]):
+        assert rel_max(x, y) < 2e-5
+
+
 def test_barrier_stall_times_out_and_solver_recovers():
     """Fault injection on the host: the cooperative inner GMRES's grid
     barriers wait for one CTA more than the launch has. Every wait runs out

@@ -51,7 +51,8 @@ struct GmresArgs {
 
 // Persistent (cooperative) inner GMRES with an FP32 M_bb product
 // (gmres_persistent.cu): launch shape and arguments.
-constexpr int kMaxPgBlobsPerCta = 64;                  // rows per CTA <= 192
+constexpr int kMaxPgBlobsPerCta = 128;                 // rows per CTA <= 384
+constexpr int kPgServiceBlobsPerCta = 64;              // a shared launch's CTAs per swimmer
 constexpr int kMaxPgCtas = 256;                        // one CTA per SM
 constexpr unsigned long long kPgTimeoutNs = 2000000000ull;  // one barrier wait
 struct PgShape {

@@ -496,13 +496,14 @@ void service_destroy(GmresService *sv) {
 }
 
 // CTAs of a swimmer's solve in a shared launch: the fewest the kernel allows
-// (kMaxPgBlobsPerCta blobs each), at most the SMs.
+// (kPgServiceBlobsPerCta blobs each), at most the SMs.
 int service_attach(GmresService *sv, tfs_solver *s) {
   if (sv == nullptr || s == nullptr) return fail(TFS_EINVAL, "null argument");
   if (s->cfg.precision != TFS_FP32C) return fail(TFS_ESTATE, "only FP32C inner solves are shared");
   if (!s->pg_ok) return fail(TFS_ESTATE, "the persistent GMRES kernel cannot serve this swimmer");
   const int nb = s->nb;
-  const int want = std::min(sv->sms, (nb + kMaxPgBlobsPerCta - 1) / kMaxPgBlobsPerCta);
+  const int want =
+      std::min(sv->sms, (nb + kPgServiceBlobsPerCta - 1) / kPgServiceBlobsPerCta);
   PgShape sh{};
   if (!pg_grid(nb, want, s->max_iter, &sh) || sh.G > s->pg.G || sh.S > s->pg.S)
     return fail(TFS_ESTATE, "no persistent GMRES shape for %d blobs on %d CTAs", nb, want);
