@@ -139,169 +139,205 @@ __global__ void reduce_partials_kernel(double *__restrict__ out,
 
 // ---------------------------------------------------------------------------
 // Barrier (steric) forces, cuda_functions.cu:1240-1436 without a plane wall.
-// A candidate test on FP32 positions (relative to the origin, with a margin
-// that bounds their rounding) discards the vast majority of pairs on the FP32
-// pipe; candidates are then tested and evaluated in FP64 exactly as the
-// reference does. Targets are segments (kind 0: skip self and the nearest
-// neighbours on the same filament; adds into f_segs) or blobs (kind 1: skip
-// self; assigns f_blobs_repulsion).
+// Targets are segments (skip self and the nearest neighbours on the same
+// filament; adds into f_segs) or blobs (skip self; assigns
+// f_blobs_repulsion). A pair can act only inside 1.1 (a_i + a_j), so the
+// sources are binned on a hashed grid of cells at least that wide (FP32
+// positions relative to the origin, with a margin that bounds their
+// rounding): bar_bin_kernel puts every source into its cell's bucket, and
+// bar_pair_kernel tests each target against the 27 cells around it, keeps
+// the sources that pass the FP32 candidate test, sorts them by index and runs
+// the reference's FP64 test and force on them in that order -- the
+// reference's sequential sum over all sources, since pairs out of reach add
+// nothing. A bucket or candidate list that overflows marks the call, and
+// bar_apply_kernel then recomputes every target by the plain sequential loop
+// over all sources; otherwise it applies the binned sums.
 // ---------------------------------------------------------------------------
-// Bounds of the FP32 origin-relative positions of each tile of BLOCK
-// consecutive sources (segments then blobs): boxes[6 t ..] = min xyz, max xyz.
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) tile_box_kernel(const BarrierArgs a, int n_src) {
-  __shared__ float red[BLOCK / 32][6];
-  const int j = blockIdx.x * BLOCK + threadIdx.x;
-  float v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-  if (j < n_src) {
-    const double *xs = j < a.num_segs ? a.x_segs + 3 * (size_t)j
-                                      : a.x_blobs + 3 * (size_t)(j - a.num_segs);
-    for (int k = 0; k < 3; ++k) v[k] = v[k + 3] = float(xs[k] - a.origin[k]);
+constexpr int kBarSlots = 8;   // sources per bucket
+constexpr int kBarCand = 48;   // candidates per target
+
+// Hash of a cell (its integer coordinates) into buckets of T (a power of two).
+__device__ __forceinline__ unsigned bar_hash(int cx, int cy, int cz, unsigned T) {
+  return (((unsigned)cx * 73856093u) ^ ((unsigned)cy * 19349663u) ^ ((unsigned)cz * 83492791u)) &
+         (T - 1u);
+}
+
+// The pair constants of one target kind (the thresholds of the reference's
+// test and of the FP32 candidate test).
+struct BarPairConst {
+  double asum_seg, asum_blob, emag;
+  float thr2_seg, thr2_blob;
+};
+
+__device__ __forceinline__ BarPairConst bar_pair_const(const BarrierArgs &a, bool target_blob) {
+  BarPairConst c;
+  // |d_fp32 - d| <= 2 sqrt(3) extent 2^-24 =: delta (each coordinate is
+  // rounded once to FP32, relative 2^-24), plus FP32 arithmetic in d^2.
+  const float delta = float(4.0 * a.origin[3] * 5.9604644775390625e-08 + 1e-30);
+  c.asum_seg = target_blob ? a.a_blob + a.a_seg : 2.0 * a.a_seg;
+  c.asum_blob = target_blob ? 2.0 * a.a_blob : a.a_seg + a.a_blob;
+  const float thr_seg = float(1.1 * c.asum_seg) + 2.f * delta;
+  const float thr_blob = float(1.1 * c.asum_blob) + 2.f * delta;
+  c.thr2_seg = thr_seg * thr_seg * 1.0001f;
+  c.thr2_blob = thr_blob * thr_blob * 1.0001f;
+  c.emag = a.repulsive_force_factor * (double)a.end_force_magnitude;
+  return c;
+}
+
+__device__ __forceinline__ const double *bar_pos(const BarrierArgs &a, int j) {
+  return j < a.num_segs ? a.x_segs + 3 * (size_t)j : a.x_blobs + 3 * (size_t)(j - a.num_segs);
+}
+
+// The reference's pair (exclusions, FP64 test and force) of target i
+// (position xi, filament fil_i) with source jj, added into f.
+__device__ __forceinline__ void bar_pair(const BarrierArgs &a, const BarPairConst &c,
+                                         bool target_blob, int i, int fil_i, const double *xi,
+                                         int jj, double *f) {
+  const bool src_is_seg = jj < a.num_segs;
+  // exclusions, :1319 and :1410
+  if (target_blob) {
+    if (i + a.num_segs == jj) return;
+  } else if (src_is_seg) {
+    const int fil_j = jj / a.nseg;
+    if (fil_i == fil_j && (i - jj <= 1 && jj - i <= 1)) return;
   }
-  for (int o = 16; o > 0; o >>= 1)
-    for (int k = 0; k < 6; ++k) {
-      const float w = __shfl_xor_sync(0xffffffffu, v[k], o);
-      v[k] = k < 3 ? fminf(v[k], w) : fmaxf(v[k], w);
-    }
-  if ((threadIdx.x & 31) == 0)
-    for (int k = 0; k < 6; ++k) red[threadIdx.x >> 5][k] = v[k];
-  __syncthreads();
-  if (threadIdx.x < 6) {
-    const int k = threadIdx.x;
-    float b = red[0][k];
-    for (int w = 1; w < BLOCK / 32; ++w) b = k < 3 ? fminf(b, red[w][k]) : fmaxf(b, red[w][k]);
-    a.boxes[6 * (size_t)blockIdx.x + k] = b;
+  const double asum = src_is_seg ? c.asum_seg : c.asum_blob;
+  const double *xj = bar_pos(a, jj);
+  const double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+  const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+  if (dist < 1.1 * asum) {
+    const double chi = 10.0 / asum;
+    double fac = fmin(1.0, 1.0 - chi * (dist - asum));
+    fac *= c.emag * fac * fac * fac;
+    const double dm1 = 1.0 / dist;
+    f[0] += fac * dx * dm1;
+    f[1] += fac * dy * dm1;
+    f[2] += fac * dz * dm1;
   }
 }
 
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) barrier_kernel(const BarrierArgs a) {
-  static_assert(BLOCK == 128, "source tiles are the 128-source tiles of tile_box_kernel");
-  __shared__ double sxd[BLOCK][3];
-  __shared__ float sxf[BLOCK][3];
-  __shared__ float cbox_w[BLOCK / 32][6], cbox[6];
-  const int i = blockIdx.x * BLOCK + threadIdx.x;
-  const int n_tgt = a.target_blobs ? a.num_blobs : a.num_segs;
-  const bool active = i < n_tgt;
-  const double *xt = a.target_blobs ? a.x_blobs : a.x_segs;
-  const int ii = active ? i : 0;
-  const double o0 = a.origin[0], o1 = a.origin[1], o2 = a.origin[2];
-  const double extent = a.origin[3];
-  const double xi = n_tgt > 0 ? xt[3 * (size_t)ii] : 0.0;
-  const double yi = n_tgt > 0 ? xt[3 * (size_t)ii + 1] : 0.0;
-  const double zi = n_tgt > 0 ? xt[3 * (size_t)ii + 2] : 0.0;
-  const float xif = float(xi - o0), yif = float(yi - o1), zif = float(zi - o2);
-  // |d_fp32 - d| <= 2 sqrt(3) extent 2^-24 =: delta (each coordinate is
-  // rounded once to FP32, relative 2^-24), plus FP32 arithmetic in d^2.
-  const float delta = float(4.0 * extent * 5.9604644775390625e-08 + 1e-30);
-  const int fil_i = active && !a.target_blobs ? i / a.nseg : -1;
-  const double emag = a.repulsive_force_factor * (double)a.end_force_magnitude;
-  // contact distances of the two source kinds and their FP32 candidate
-  // thresholds (squared, with the rounding margin), hoisted out of the loop
-  const double asum_seg = a.target_blobs ? a.a_blob + a.a_seg : 2.0 * a.a_seg;
-  const double asum_blob = a.target_blobs ? 2.0 * a.a_blob : a.a_seg + a.a_blob;
-  const float thr_seg = float(1.1 * asum_seg) + 2.f * delta;
-  const float thr_blob = float(1.1 * asum_blob) + 2.f * delta;
-  const float thr2_seg = thr_seg * thr_seg * 1.0001f, thr2_blob = thr_blob * thr_blob * 1.0001f;
-  const int n_src = a.num_segs + a.num_blobs;
-  // this CTA's share of the sources (grid.y splits them)
-  const int s0 = blockIdx.y * a.chunk;
-  const int s1 = min(s0 + a.chunk, n_src);
-  // bounds of this CTA's targets; a source tile whose bounds lie farther than
-  // the larger candidate threshold (with a 0.1% margin over the FP32
-  // rounding of both tests) has no pair the filter below would pass, and is
-  // skipped by the whole CTA
-  const float cull2 = 1.001f * fmaxf(thr2_seg, thr2_blob);
-  if (a.boxes != nullptr) {
-    float v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-    if (active) {
-      v[0] = v[3] = xif;
-      v[1] = v[4] = yif;
-      v[2] = v[5] = zif;
-    }
-    for (int o = 16; o > 0; o >>= 1)
-      for (int k = 0; k < 6; ++k) {
-        const float w = __shfl_xor_sync(0xffffffffu, v[k], o);
-        v[k] = k < 3 ? fminf(v[k], w) : fmaxf(v[k], w);
-      }
-    if ((threadIdx.x & 31) == 0)
-      for (int k = 0; k < 6; ++k) cbox_w[threadIdx.x >> 5][k] = v[k];
-    __syncthreads();
-    if (threadIdx.x < 6) {
-      const int k = threadIdx.x;
-      float b = cbox_w[0][k];
-      for (int w = 1; w < BLOCK / 32; ++w) b = k < 3 ? fminf(b, cbox_w[w][k]) : fmaxf(b, cbox_w[w][k]);
-      cbox[k] = b;
-    }
-    __syncthreads();
+// Cell width: the larger candidate reach of either target kind, 1% wider so
+// that a pair within reach lies in neighbouring cells despite rounding.
+__device__ __forceinline__ float bar_cell(const BarrierArgs &a) {
+  const BarPairConst s = bar_pair_const(a, false), b = bar_pair_const(a, true);
+  const float r2 = 1.001f * fmaxf(fmaxf(s.thr2_seg, s.thr2_blob), fmaxf(b.thr2_seg, b.thr2_blob));
+  return 1.01f * sqrtf(r2);
+}
+
+// Bins every source: bucket of its cell, slot from the bucket's counter;
+// entry {x, y, z, index} with the FP32 origin-relative position.
+__global__ void bar_bin_kernel(const BarrierArgs a, BarGrid g) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.num_segs + a.num_blobs) return;
+  const double *x = bar_pos(a, j);
+  const float px = float(x[0] - a.origin[0]), py = float(x[1] - a.origin[1]),
+              pz = float(x[2] - a.origin[2]);
+  const float h = bar_cell(a);
+  const unsigned b = bar_hash((int)floorf(px / h), (int)floorf(py / h), (int)floorf(pz / h), g.T);
+  const unsigned slot = atomicAdd(g.count + b, 1u);
+  if (slot < (unsigned)kBarSlots) g.entry[(size_t)b * kBarSlots + slot] = make_float4(px, py, pz, __int_as_float(j));
+  else atomicExch(g.overflow, 1u);
+}
+
+// One thread per target (segments, then blobs): its binned sum into g.sum.
+__global__ void bar_pair_kernel(const BarrierArgs a, BarGrid g) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n_tgt = a.num_segs + (a.free_body ? a.num_blobs : 0);
+  if (t >= n_tgt) return;
+  const bool tb = t >= a.num_segs;
+  const int i = tb ? t - a.num_segs : t;
+  const double *xp = tb ? a.x_blobs + 3 * (size_t)i : a.x_segs + 3 * (size_t)i;
+  const double xi[3] = {xp[0], xp[1], xp[2]};
+  const float px = float(xi[0] - a.origin[0]), py = float(xi[1] - a.origin[1]),
+              pz = float(xi[2] - a.origin[2]);
+  const BarPairConst c = bar_pair_const(a, tb);
+  const float h = bar_cell(a);
+  const int cx = (int)floorf(px / h), cy = (int)floorf(py / h), cz = (int)floorf(pz / h);
+  // the 27 cells' buckets and counts, all loads in flight at once
+  unsigned bk[27];
+  int cnt[27];
+#pragma unroll
+  for (int k = 0; k < 27; ++k) {
+    bk[k] = bar_hash(cx + k % 3 - 1, cy + (k / 3) % 3 - 1, cz + k / 9 - 1, g.T);
+    cnt[k] = (int)min(__ldg(g.count + bk[k]), (unsigned)kBarSlots);
   }
-  double fx = 0.0, fy = 0.0, fz = 0.0;
-  for (int base = s0; base < s1; base += BLOCK) {
-    if (a.boxes != nullptr) {  // CTA-uniform: the same values in every thread
-      const float *tb = a.boxes + 6 * (size_t)(base / BLOCK);
-      const float gx = fmaxf(0.f, fmaxf(tb[0] - cbox[3], cbox[0] - tb[3]));
-      const float gy = fmaxf(0.f, fmaxf(tb[1] - cbox[4], cbox[1] - tb[4]));
-      const float gz = fmaxf(0.f, fmaxf(tb[2] - cbox[5], cbox[2] - tb[5]));
-      if (gx * gx + gy * gy + gz * gz >= cull2) continue;
-    }
-    const int j = base + threadIdx.x;
-    __syncthreads();
-    if (j < s1) {
-      const double *xs = j < a.num_segs ? a.x_segs + 3 * (size_t)j
-                                        : a.x_blobs + 3 * (size_t)(j - a.num_segs);
-      sxd[threadIdx.x][0] = xs[0];
-      sxd[threadIdx.x][1] = xs[1];
-      sxd[threadIdx.x][2] = xs[2];
-      sxf[threadIdx.x][0] = float(xs[0] - o0);
-      sxf[threadIdx.x][1] = float(xs[1] - o1);
-      sxf[threadIdx.x][2] = float(xs[2] - o2);
-    }
-    __syncthreads();
-    if (!active) continue;
-    const int cnt = min(BLOCK, s1 - base);
-    for (int q = 0; q < cnt; ++q) {
-      const int jj = base + q;
-      const bool src_is_seg = jj < a.num_segs;
-      const float dxf = xif - sxf[q][0], dyf = yif - sxf[q][1], dzf = zif - sxf[q][2];
-      const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
-      if (d2f >= (src_is_seg ? thr2_seg : thr2_blob)) continue;
-      const double asum = src_is_seg ? asum_seg : asum_blob;
-      // exclusions, :1319 and :1410
-      if (a.target_blobs) {
-        if (i + a.num_segs == jj) continue;
-      } else if (src_is_seg) {
-        const int fil_j = jj / a.nseg;
-        if (fil_i == fil_j && (i - jj <= 1 && jj - i <= 1)) continue;
-      }
-      const double dx = xi - sxd[q][0], dy = yi - sxd[q][1], dz = zi - sxd[q][2];
-      const double dist = sqrt(dx * dx + dy * dy + dz * dz);
-      if (dist < 1.1 * asum) {
-        const double chi = 10.0 / asum;
-        double fac = fmin(1.0, 1.0 - chi * (dist - asum));
-        fac *= emag * fac * fac * fac;
-        const double dm1 = 1.0 / dist;
-        fx += fac * dx * dm1;
-        fy += fac * dy * dm1;
-        fz += fac * dz * dm1;
-      }
+  int cand[kBarCand];
+  int n = 0;
+  bool over = false;
+#pragma unroll
+  for (int k = 0; k < 27; ++k) {
+    const int ex = cx + k % 3 - 1, ey = cy + (k / 3) % 3 - 1, ez = cz + k / 9 - 1;
+    for (int s = 0; s < cnt[k]; ++s) {
+      const float4 e = __ldg(g.entry + (size_t)bk[k] * kBarSlots + s);
+      // another cell sharing the bucket
+      if ((int)floorf(e.x / h) != ex || (int)floorf(e.y / h) != ey || (int)floorf(e.z / h) != ez)
+        continue;
+      const int j = __float_as_int(e.w);
+      const float ddx = px - e.x, ddy = py - e.y, ddz = pz - e.z;
+      const float d2f = ddx * ddx + ddy * ddy + ddz * ddz;
+      if (d2f >= (j < a.num_segs ? c.thr2_seg : c.thr2_blob)) continue;
+      if (n < kBarCand) cand[n++] = j;
+      else over = true;
     }
   }
-  if (!active) return;
-  if (a.splits > 1) {
-    double *o = a.scratch + ((size_t)blockIdx.y * n_tgt + i) * 3;
-    o[0] = fx;
-    o[1] = fy;
-    o[2] = fz;
-    return;
+  if (over) atomicExch(g.overflow, 1u);
+  // the reference's order: increasing source index (insertion sort)
+  for (int p = 1; p < n; ++p) {
+    const int v = cand[p];
+    int q = p - 1;
+    while (q >= 0 && cand[q] > v) {
+      cand[q + 1] = cand[q];
+      --q;
+    }
+    cand[q + 1] = v;
   }
-  if (a.target_blobs) {
-    a.f_blobs_repulsion[3 * (size_t)i] = fx;
-    a.f_blobs_repulsion[3 * (size_t)i + 1] = fy;
-    a.f_blobs_repulsion[3 * (size_t)i + 2] = fz;
+  double f[3] = {0.0, 0.0, 0.0};
+  const int fil_i = tb ? -1 : i / a.nseg;
+  for (int p = 0; p < n; ++p) bar_pair(a, c, tb, i, fil_i, xi, cand[p], f);
+  g.sum[3 * (size_t)t] = f[0];
+  g.sum[3 * (size_t)t + 1] = f[1];
+  g.sum[3 * (size_t)t + 2] = f[2];
+}
+
+// Applies the binned sums, or -- after an overflow -- recomputes each
+// target by the sequential loop over every source (the FP32 candidate test,
+// then the reference's pair), which gives the same sums.
+__global__ void bar_apply_kernel(const BarrierArgs a, BarGrid g) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n_tgt = a.num_segs + (a.free_body ? a.num_blobs : 0);
+  if (t >= n_tgt) return;
+  const bool tb = t >= a.num_segs;
+  const int i = tb ? t - a.num_segs : t;
+  double f[3];
+  if (*(volatile const unsigned *)g.overflow == 0u) {
+    f[0] = g.sum[3 * (size_t)t];
+    f[1] = g.sum[3 * (size_t)t + 1];
+    f[2] = g.sum[3 * (size_t)t + 2];
   } else {
-    a.f_segs[6 * (size_t)i] += fx;
-    a.f_segs[6 * (size_t)i + 1] += fy;
-    a.f_segs[6 * (size_t)i + 2] += fz;
+    const double *xp = tb ? a.x_blobs + 3 * (size_t)i : a.x_segs + 3 * (size_t)i;
+    const double xi[3] = {xp[0], xp[1], xp[2]};
+    const float px = float(xi[0] - a.origin[0]), py = float(xi[1] - a.origin[1]),
+                pz = float(xi[2] - a.origin[2]);
+    const BarPairConst c = bar_pair_const(a, tb);
+    const int fil_i = tb ? -1 : i / a.nseg;
+    f[0] = f[1] = f[2] = 0.0;
+    for (int j = 0; j < a.num_segs + a.num_blobs; ++j) {
+      const double *xj = bar_pos(a, j);
+      const float ddx = px - float(xj[0] - a.origin[0]), ddy = py - float(xj[1] - a.origin[1]),
+                  ddz = pz - float(xj[2] - a.origin[2]);
+      if (ddx * ddx + ddy * ddy + ddz * ddz >= (j < a.num_segs ? c.thr2_seg : c.thr2_blob))
+        continue;
+      bar_pair(a, c, tb, i, fil_i, xi, j, f);
+    }
+  }
+  if (tb) {
+    a.f_blobs_repulsion[3 * (size_t)i] = f[0];
+    a.f_blobs_repulsion[3 * (size_t)i + 1] = f[1];
+    a.f_blobs_repulsion[3 * (size_t)i + 2] = f[2];
+  } else {
+    a.f_segs[6 * (size_t)i] += f[0];
+    a.f_segs[6 * (size_t)i + 1] += f[1];
+    a.f_segs[6 * (size_t)i + 2] += f[2];
   }
 }
 
@@ -485,59 +521,45 @@ cudaError_t launch_tile(const TileArgs &a_in, int vd, int fda, int fdb, TileTuni
   return cudaGetLastError();
 }
 
-// Split barrier forces: out[stride * i + k] (+= or =) sum over splits s in
-// order of partial[s][i][k], k < 3.
-__global__ void barrier_reduce_kernel(double *__restrict__ out, int stride, int accumulate,
-                                      const double *__restrict__ partial, int n_tgt,
-                                      int splits) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= 3 * n_tgt) return;
-  const int i = e / 3, k = e - 3 * i;
-  double s = 0.0;
-  for (int p = 0; p < splits; ++p) s += partial[(size_t)p * 3 * n_tgt + e];
-  double *o = out + (size_t)stride * i + k;
-  *o = accumulate ? *o + s : s;
+// The hashed grid of barrier_grid_bytes(): bucket counters (a power of two
+// at least twice the sources), the overflow word, the buckets, the sums.
+static BarGrid bar_grid(void *base, int n_src) {
+  unsigned T = 64;
+  while (T < 2u * (unsigned)n_src) T <<= 1;
+  BarGrid g;
+  char *p = static_cast<char *>(base);
+  g.T = T;
+  g.count = reinterpret_cast<unsigned *>(p);
+  g.overflow = g.count + T;
+  const size_t off_e = ((4 * (size_t)T + 4) + 15) / 16 * 16;
+  g.entry = reinterpret_cast<float4 *>(p + off_e);
+  g.sum = reinterpret_cast<double *>(p + off_e + 16 * (size_t)T * kBarSlots);
+  return g;
 }
 
-// One target kind: grid = target CTAs x source splits, the split count chosen
-// for about eight CTAs per SM; partial forces summed in split order.
-static cudaError_t barrier_launch(BarrierArgs a, int target_blobs, cudaStream_t st) {
-  constexpr int B = 128;
-  a.target_blobs = target_blobs;
-  const int n_tgt = target_blobs ? a.num_blobs : a.num_segs;
-  const int n_src = a.num_segs + a.num_blobs;
-  const int ctas = (n_tgt + B - 1) / B;
-  int splits = std::max(1, (8 * num_sms() + ctas - 1) / ctas);
-  splits = std::min(splits, kMaxSplits);
-  splits = std::min(splits, std::max(1, n_src / (2 * B)));
-  if (a.scratch == nullptr || (size_t)splits * 3 * n_tgt > a.scratch_elems) splits = 1;
-  int chunk = (n_src + splits - 1) / splits;
-  chunk = std::max(B, ((chunk + B - 1) / B) * B);
-  splits = std::max(1, (n_src + chunk - 1) / chunk);
-  a.chunk = chunk;
-  a.splits = splits;
-  barrier_kernel<B><<<dim3(ctas, splits), B, 0, st>>>(a);
-  count_launch();
-  if (splits > 1) {
-    barrier_reduce_kernel<<<(3 * n_tgt + 255) / 256, 256, 0, st>>>(
-        target_blobs ? a.f_blobs_repulsion : a.f_segs, target_blobs ? 3 : 6,
-        target_blobs ? 0 : 1, a.scratch, n_tgt, splits);
-    count_launch();
-  }
-  return cudaGetLastError();
+size_t barrier_grid_bytes(int num_segs, int num_blobs) {
+  const int n_src = num_segs + num_blobs;
+  unsigned T = 64;
+  while (T < 2u * (unsigned)n_src) T <<= 1;
+  const size_t off_e = ((4 * (size_t)T + 4) + 15) / 16 * 16;
+  return off_e + 16 * (size_t)T * kBarSlots + 24 * (size_t)std::max(n_src, 1);
 }
 
 cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st) {
-  cudaError_t e = cudaSuccess;
   const int n_src = a.num_segs + a.num_blobs;
-  if (a.boxes != nullptr && n_src > 0) {
-    tile_box_kernel<128><<<(n_src + 127) / 128, 128, 0, st>>>(a, n_src);
-    count_launch();
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-  if (a.num_segs > 0 && (e = barrier_launch(a, 0, st)) != cudaSuccess) return e;
-  if (a.free_body && a.num_blobs > 0) e = barrier_launch(a, 1, st);
-  return e;
+  const int n_tgt = a.num_segs + (a.free_body ? a.num_blobs : 0);
+  if (n_src <= 0 || n_tgt <= 0) return cudaSuccess;
+  if (a.grid == nullptr) return cudaErrorInvalidValue;
+  const BarGrid g = bar_grid(a.grid, n_src);
+  cudaError_t e = cudaMemsetAsync(g.count, 0, 4 * ((size_t)g.T + 1), st);
+  if (e != cudaSuccess) return e;
+  bar_bin_kernel<<<(n_src + 255) / 256, 256, 0, st>>>(a, g);
+  count_launch();
+  bar_pair_kernel<<<(n_tgt + 127) / 128, 128, 0, st>>>(a, g);
+  count_launch();
+  bar_apply_kernel<<<(n_tgt + 255) / 256, 256, 0, st>>>(a, g);
+  count_launch();
+  return cudaGetLastError();
 }
 
 }  // namespace tfs

@@ -106,7 +106,7 @@ static void free_all(tfs_solver *s) {
   cudaFree(s->rec_segs_x2);
   cudaFree(s->rec_blobs_x2);
   cudaFree(s->rec_ff);
-  cudaFree(s->tile_boxes);
+  cudaFree(s->bar_grid);
   cudaFree(s->wc_z);
   cudaFree(s->wc_f);
   cudaFree(s->scratch);
@@ -356,7 +356,7 @@ int tfs_solver_create(const tfs_config *cfg, tfs_solver **out) {
       (rc = alloc_dev(&s->rec_segs_x2, 80 * (size_t)ns)) ||
       (rc = alloc_dev(&s->rec_blobs_x2, 48 * (size_t)nb)) ||
       (rc = alloc_dev(&s->rec_ff, ff_record_bytes() * nb)) ||
-      (rc = alloc_dev((void **)&s->tile_boxes, sizeof(float) * 6 * ((ns + nb + 127) / 128 + 1))) ||
+      (rc = alloc_dev(&s->bar_grid, barrier_grid_bytes(ns, nb))) ||
       (rc = alloc_dev((void **)&s->scratch, dsz * s->scratch_elems)) ||
       (rc = alloc_dev((void **)&s->qjobs_dev, sizeof s->qjobs)) ||
       (rc = alloc_dev((void **)&s->qcount, sizeof(unsigned) * qcount_elems)) ||
@@ -581,9 +581,7 @@ int tfs_apply_interparticle_forces(tfs_solver *s) {
   a.end_force_magnitude = s->cfg.end_force_magnitude;
   a.repulsive_force_factor = s->cfg.repulsive_force_factor;
   a.free_body = s->cfg.free_body;
-  a.scratch = s->scratch;
-  a.scratch_elems = s->scratch_elems;
-  a.boxes = s->tile_boxes;
+  a.grid = s->bar_grid;
   cudaError_t e = launch_barrier(a, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "barrier kernel");
   return TFS_OK;

@@ -47,12 +47,17 @@ struct BarrierArgs {
   int end_force_magnitude;
   double repulsive_force_factor;
   int free_body;
-  double *scratch;            // split partial forces (kMaxSplits * 6 * max(Ns, Nb) doubles)
-  float *boxes;               // 6 per 128-source tile (segments then blobs): FP32 bounds of the
-                              // origin-relative positions, for culling whole tiles (null: none)
-  size_t scratch_elems;
-  int target_blobs;           // set by the launcher
-  int chunk, splits;          // set by the launcher
+  void *grid;                 // barrier_grid_bytes(): the hashed grid of the sources
+};
+
+// The barrier forces' hashed grid (rpy_kernels.cu): T bucket counters, the
+// overflow word, T buckets of source entries {x, y, z, index}, 3 sums per
+// target.
+struct BarGrid {
+  unsigned *count, *overflow;
+  float4 *entry;
+  double *sum;
+  unsigned T;
 };
 
 // Launch variants of the tile kernel and their dispatch tables
@@ -179,6 +184,8 @@ cudaError_t launch_tile(const TileArgs &a, int vd, int fda, int fdb, TileTuning 
                         double *scratch, size_t scratch_elems, int mode, cudaStream_t st,
                         cudaEvent_t *ev = nullptr);
 cudaError_t launch_barrier(const BarrierArgs &a, cudaStream_t st);
+// Bytes of BarrierArgs::grid for these sizes.
+size_t barrier_grid_bytes(int num_segs, int num_blobs);
 // The weakly coupled filaments' segment product (weak.cu): filament means
 // Z and total forces Ft (3 nfil each, written), then v_segs (6 Ns).
 cudaError_t launch_msf(const double *x_segs, const double *f_segs, int nfil, int nseg,

@@ -33,7 +33,7 @@ struct tfs_solver {
   void *rec_segs = nullptr, *rec_blobs = nullptr;
   void *rec_segs_x2 = nullptr, *rec_blobs_x2 = nullptr;  // FP32x2 records
   void *rec_ff = nullptr;  // float-float blob records (the refinement residual)
-  float *tile_boxes = nullptr;  // barrier forces: bounds of each 128-source tile
+  void *bar_grid = nullptr;     // barrier forces: hashed grid of the sources
   double *wc_z = nullptr, *wc_f = nullptr;  // weakly coupled filaments: means, total forces
   double *scratch = nullptr;
   size_t scratch_elems = 0;
