@@ -97,6 +97,10 @@ def test_tiny_and_ragged_fp64(tag):
 
 @pytest.mark.parametrize("case", ["small_matvec", "overlap_a16"])
 def test_barrier_forces_match_reference(case):
+    """Barrier forces against the reference's own kernels. small_matvec runs
+    the hashed-grid path (at most 2 particles per cell); overlap_a16 puts 17
+    particles in one cell, overflows its bucket and runs the sequential
+    fallback."""
     import torch
 
     d = load(case)
