@@ -83,6 +83,18 @@ __device__ void block_sum_vec(double (&v)[L], double *red, double *sh) {
   for (int k = 0; k < L; ++k) v[k] = sh[k];
 }
 
+// Sum of n strided per-CTA partials p[c * stride], c < n, by one warp: lanes
+// take c = lane (mod 32), then a fixed shuffle tree, so every lane gets the
+// same bits. (GB300 issues an FP64 warp instruction in ~19 SM cycles: a
+// single thread adding G partials in sequence costs microseconds.)
+__device__ __forceinline__ double warp_sum_strided(const double *p, int n, size_t stride) {
+  double t = 0.0;
+  for (int c = threadIdx.x & 31; c < n; c += 32) t += __ldcg(p + (size_t)c * stride);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  return t;
+}
+
 // The rows of a slice: its blobs' rows, then (last CTA) the six body rows.
 __device__ __forceinline__ int slice_rows(const Slice &sl) {
   return 3 * (sl.m1 - sl.m0) + (sl.body ? 6 : 0);
@@ -189,10 +201,10 @@ __device__ void kt_partial(const GmresArgs &a, const Slice &sl, const double *l,
 
 // sum over CTAs (in order) of part6, by the last CTA; result in sh[0..6)
 __device__ void sum_part6(const double *part6, int G, double *sh) {
-  if (threadIdx.x < 6) {
-    double t = 0.0;
-    for (int c = 0; c < G; ++c) t += __ldcg(part6 + 6 * c + threadIdx.x);
-    sh[threadIdx.x] = t;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = wid; k < 6; k += nw) {
+    const double t = warp_sum_strided(part6 + k, G, 6);
+    if (lane == 0) sh[k] = t;
   }
   __syncthreads();
 }
@@ -274,9 +286,9 @@ __global__ void __launch_bounds__(kGT) gmres_start_kernel(GmresArgs a) {
   block_sum_vec<1>(ss, red, sh);
   if (threadIdx.x == 0) a.part[blockIdx.x] = ss[0];
   if (!last_cta(a.counters + 1)) return;
+  const double tsum = threadIdx.x < 32 ? warp_sum_strided(a.part, gridDim.x, 1) : 0.0;
   if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + c);
+    const double t = tsum;
     st->norm_rhs = sqrt(t);
     st->iter = 0;
     st->done = 0;
@@ -319,9 +331,9 @@ __global__ void __launch_bounds__(kGT) gmres_residual_kernel(GmresArgs a) {
   if (threadIdx.x == 0) a.part[blockIdx.x] = ss[0];
   if (!last_cta(a.counters + 2)) return;
   sum_part6(a.part6, gridDim.x, sh);
+  const double tsum = threadIdx.x < 32 ? warp_sum_strided(a.part, gridDim.x, 1) : 0.0;
   if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + c);
+    double t = tsum;
     for (int k = 0; k < 6; ++k) {
       const double r = a.rhs[vel + k] - (-sh[k]);
       q0[vel + k] = r;
@@ -400,12 +412,13 @@ __global__ void __launch_bounds__(kGT) arnoldi_dot1_kernel(GmresArgs a) {
   sum_part6(a.part6, gridDim.x, sh);
   if (threadIdx.x < 6) w[vel + threadIdx.x] = -sh[threadIdx.x];
   __syncthreads();
-  for (int i = threadIdx.x; i < k; i += blockDim.x) {
-    double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + (size_t)c * a.part_stride + i);
-    const double *qi = a.Q + (size_t)i * n;
-    for (int j = 0; j < 6; ++j) t += w[vel + j] * qi[vel + j];
-    a.h1[i] = t;
+  for (int i = threadIdx.x >> 5; i < k; i += blockDim.x >> 5) {
+    double t = warp_sum_strided(a.part + i, gridDim.x, a.part_stride);
+    if ((threadIdx.x & 31) == 0) {
+      const double *qi = a.Q + (size_t)i * n;
+      for (int j = 0; j < 6; ++j) t += w[vel + j] * qi[vel + j];
+      a.h1[i] = t;
+    }
   }
   if (threadIdx.x == 0) a.counters[3] = 0;
 }
@@ -430,11 +443,12 @@ __global__ void __launch_bounds__(kGT) arnoldi_dot2_kernel(GmresArgs a) {
   block_dots(a, sl, true, w, k, a.part, a.part_stride, red);
   if (!last_cta(a.counters + 4)) return;
   const int ld = a.max_iter + 1;
-  for (int i = threadIdx.x; i < k; i += blockDim.x) {
-    double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + (size_t)c * a.part_stride + i);
-    a.h2[i] = t;
-    a.H[i + (size_t)(k - 1) * ld] = a.h1[i] + t;
+  for (int i = threadIdx.x >> 5; i < k; i += blockDim.x >> 5) {
+    const double t = warp_sum_strided(a.part + i, gridDim.x, a.part_stride);
+    if ((threadIdx.x & 31) == 0) {
+      a.h2[i] = t;
+      a.H[i + (size_t)(k - 1) * ld] = a.h1[i] + t;
+    }
   }
   if (threadIdx.x == 0) a.counters[4] = 0;
 }
@@ -461,9 +475,9 @@ __global__ void __launch_bounds__(kGT) arnoldi_norm_kernel(GmresArgs a) {
   block_sum_vec<1>(ss, red, sh);
   if (threadIdx.x == 0) a.part[blockIdx.x] = ss[0];
   if (!last_cta(a.counters + 5)) return;
+  const double tsum = threadIdx.x < 32 ? warp_sum_strided(a.part, gridDim.x, 1) : 0.0;
   if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) t += __ldcg(a.part + c);
+    const double t = tsum;
     const double qn = sqrt(t);
     st->qnorm = qn;
     const int ld = a.max_iter + 1;
@@ -601,12 +615,14 @@ __global__ void __launch_bounds__(kGT) refine_residual_kernel(GmresArgs a, const
   }
   if (!last_cta(a.counters + 6)) return;
   sum_part6(a.part6, gridDim.x, sh);
+  // warp 0: sum of r^2, warp 1: sum of b^2 over the CTAs' partials
+  if (threadIdx.x < 64) {
+    const double t = warp_sum_strided(a.part + (threadIdx.x >> 5), gridDim.x, 2);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    double rr = 0.0, bb = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) {
-      rr += __ldcg(a.part + 2 * c);
-      bb += __ldcg(a.part + 2 * c + 1);
-    }
+    double rr = red[0], bb = red[1];
     for (int k = 0; k < 6; ++k) {
       const double b = a.rhs[vel + k];
       const double t = b - (-sh[k]);

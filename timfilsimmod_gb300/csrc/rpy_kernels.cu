@@ -40,63 +40,81 @@ namespace tfs {
 // ---------------------------------------------------------------------------
 constexpr int kOriginCTAs = 64;
 
-// Two passes over all particles, kOriginCTAs CTAs each: pass 0 sums the
-// positions (the mean goes to out[0..2]), pass 1 takes the largest
-// |x_k - o_k| (out[3]). Per-CTA partials live in out[4..], the last CTA to
-// finish combines them in CTA order (deterministic).
+// One pass over all particles, kOriginCTAs CTAs: the FP32 bounds of the
+// positions (min and max are exact in any order); the last CTA to finish
+// combines the CTAs' bounds and writes the origin, the centre of the bounds
+// (out[0..2]), and out[3], an upper bound of every |x_k - o_k|: the largest
+// half-width plus the FP32 rounding of the coordinates (2^-23 of the largest
+// magnitude). The FP32 products and the barrier's candidate test measure
+// positions from this origin. Per-CTA bounds live in out[4..] (as floats).
 __global__ void __launch_bounds__(256) origin_kernel(const double *__restrict__ xa, int na,
                                                      const double *__restrict__ xb, int nb,
                                                      double *__restrict__ out /* [4 + 4 kOriginCTAs] */,
-                                                     unsigned *__restrict__ counter, int pass) {
-  __shared__ double red[256][3];
+                                                     unsigned *__restrict__ counter) {
+  __shared__ float red[8][6];
   __shared__ bool last;
-  const int tid = threadIdx.x, n = na + nb;
-  double *part = out + 4;
-  double s[3] = {0, 0, 0};
-  double o[3] = {0, 0, 0};
-  if (pass == 1)
-    for (int k = 0; k < 3; ++k) o[k] = out[k];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, n = na + nb;
+  float *part = reinterpret_cast<float *>(out + 4);
+  float v[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
   for (int i = blockIdx.x * blockDim.x + tid; i < n; i += gridDim.x * blockDim.x) {
     const double *x = i < na ? xa + 3 * (size_t)i : xb + 3 * (size_t)(i - na);
-    if (pass == 0) {
-      for (int k = 0; k < 3; ++k) s[k] += x[k];
-    } else {
-      for (int k = 0; k < 3; ++k) s[0] = fmax(s[0], fabs(x[k] - o[k]));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float c = float(x[k]);
+      v[k] = fminf(v[k], c);
+      v[k + 3] = fmaxf(v[k + 3], c);
     }
   }
-  for (int k = 0; k < 3; ++k) red[tid][k] = s[k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float w = __shfl_xor_sync(0xffffffffu, v[k], o);
+      v[k] = k < 3 ? fminf(v[k], w) : fmaxf(v[k], w);
+    }
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) red[wid][k] = v[k];
   __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (tid < w) {
-      if (pass == 0)
-        for (int k = 0; k < 3; ++k) red[tid][k] += red[tid + w][k];
-      else
-        red[tid][0] = fmax(red[tid][0], red[tid + w][0]);
-    }
-    __syncthreads();
+  if (tid < 6) {
+    float b = red[0][tid];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      b = tid < 3 ? fminf(b, red[w][tid]) : fmaxf(b, red[w][tid]);
+    part[6 * blockIdx.x + tid] = b;
   }
+  __syncthreads();
   if (tid == 0) {
-    if (pass == 0)
-      for (int k = 0; k < 3; ++k) part[3 * blockIdx.x + k] = red[0][k];
-    else
-      part[3 * kOriginCTAs + blockIdx.x] = red[0][0];
     __threadfence();
-    last = atomicAdd(counter + pass, 1u) == gridDim.x - 1;
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || tid != 0) return;
+  if (!last || wid != 0) return;
   __threadfence();
-  if (pass == 0) {
-    double t[3] = {0, 0, 0};
-    for (int c = 0; c < (int)gridDim.x; ++c)
-      for (int k = 0; k < 3; ++k) t[k] += __ldcg(part + 3 * c + k);
-    for (int k = 0; k < 3; ++k) out[k] = n > 0 ? t[k] / n : 0.0;
-  } else {
-    double m = 0.0;
-    for (int c = 0; c < (int)gridDim.x; ++c) m = fmax(m, __ldcg(part + 3 * kOriginCTAs + c));
-    out[3] = m;
+  float u[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int c = lane; c < (int)gridDim.x; c += 32)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float w = __ldcg(part + 6 * c + k);
+      u[k] = k < 3 ? fminf(u[k], w) : fmaxf(u[k], w);
+    }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      const float w = __shfl_xor_sync(0xffffffffu, u[k], o);
+      u[k] = k < 3 ? fminf(u[k], w) : fmaxf(u[k], w);
+    }
+  if (lane == 0) {
+    double ext = 0.0, mag = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double lo = n > 0 ? (double)u[k] : 0.0, hi = n > 0 ? (double)u[k + 3] : 0.0;
+      out[k] = 0.5 * (lo + hi);
+      ext = fmax(ext, 0.5 * (hi - lo));
+      mag = fmax(mag, fmax(fabs(lo), fabs(hi)));
+    }
+    out[3] = ext + mag * 1.1920928955078125e-07;
+    counter[0] = 0;
   }
-  counter[pass] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -371,10 +389,8 @@ cudaError_t launch_reduce_partials(double *out, const double *partial, int n_ele
 cudaError_t launch_origin(const double *xa, int na, const double *xb, int nb, double *out,
                           unsigned *counter, cudaStream_t st) {
   const int ctas = std::max(1, std::min(kOriginCTAs, (na + nb + 255) / 256));
-  for (int pass = 0; pass < 2; ++pass) {
-    origin_kernel<<<ctas, 256, 0, st>>>(xa, na, xb, nb, out, counter, pass);
-    count_launch();
-  }
+  origin_kernel<<<ctas, 256, 0, st>>>(xa, na, xb, nb, out, counter);
+  count_launch();
   return cudaGetLastError();
 }
 
