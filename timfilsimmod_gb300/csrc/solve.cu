@@ -602,9 +602,29 @@ int refine_cycles(tfs_solver *s, const GmresArgs &g64, int vec64, int *total, in
   return TFS_OK;
 }
 
-// xr = the caller's warm start (f_blobs, v_bodies)
+// x = 2 a - b (the linear extrapolation of two steps' solutions)
+__global__ void extrapolate_kernel(double *__restrict__ x, const double *__restrict__ a,
+                                   const double *__restrict__ b, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = 2.0 * a[i] - b[i];
+}
+
+// xr = the caller's warm start (f_blobs, v_bodies), or, for the first solve
+// of a time step after two earlier steps, 2 x_{n-1} - x_{n-2} of their final
+// solutions: the blob forces and body velocity change smoothly with time, so
+// the extrapolation starts the refinement several digits closer and its
+// inner solve asks for less (the refined result meets the same residual)
 int refine_start(tfs_solver *s) {
   const int vel = 3 * s->nb;
+  if (s->extrap_next) {
+    s->extrap_next = false;
+    const double *h1 = s->whist + (size_t)s->whist_head * s->n;
+    const double *h2 = s->whist + (size_t)(s->whist_head ^ 1) * s->n;
+    extrapolate_kernel<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->xr, h1, h2, s->n);
+    TFS_CUDA(cudaGetLastError(), "extrapolated warm start");
+    count_launch();
+    return TFS_OK;
+  }
   TFS_CUDA(cudaMemcpyAsync(s->xr, s->f_blobs, sizeof(double) * vel, cudaMemcpyDeviceToDevice,
                            s->stream),
            "refinement start");
@@ -666,6 +686,7 @@ int linear_solve(tfs_solver *s, int *iters) {
   *iters = total;
   s->last_outer = cycles;
   s->last_rel = h.rel;
+  s->solved = true;
   return TFS_OK;
 }
 
@@ -691,6 +712,7 @@ int solve_alloc(tfs_solver *s) {
       (rc = alloc_dev((void **)&s->v_bodies, 8 * 6)) ||
       (rc = alloc_dev((void **)&s->swimmer_f, 8 * 6)) ||
       (rc = alloc_dev((void **)&s->xr, 8 * n)) || (rc = alloc_dev((void **)&s->r, 8 * n)) ||
+      (rc = alloc_dev((void **)&s->whist, 8 * 2 * n)) ||
       (rc = alloc_dev((void **)&s->dx, 8 * n)) ||
       (rc = alloc_dev((void **)&s->gst, 2 * sizeof(GmresScalars))))
     return rc;
@@ -760,7 +782,7 @@ void solve_free(tfs_solver *s) {
   s->chunk_graphs.clear();
   double *bufs[] = {s->refs, s->diff, s->mats, s->Q, s->H, s->beta, s->cs, s->sn, s->y, s->z,
                     s->tmp, s->soln, s->rhs, s->vtmp, s->v_bodies, s->swimmer_f, s->xr, s->r,
-                    s->dx, s->gpart, s->gpart6, s->gh1, s->gh2};
+                    s->dx, s->gpart, s->gpart6, s->gh1, s->gh2, s->whist};
   for (double *b : bufs) cudaFree(b);
   cudaFree(s->gcounters);
   cudaFree(s->pg_x32);
@@ -939,6 +961,32 @@ int compute_velocities_dev(tfs_solver *s, int *gmres_iters) {
   s->last_iters = iters;
   if (gmres_iters) *gmres_iters = iters;
   return TFS_OK;
+}
+
+int solver_new_step(tfs_solver *s) {
+  if (s->cfg.precision != TFS_FP32C || s->whist == nullptr) return TFS_OK;
+  if (s->solved) {
+    const int slot = s->whist_head ^ 1;  // the older entry
+    double *h = s->whist + (size_t)slot * s->n;
+    const int vel = 3 * s->nb;
+    TFS_CUDA(cudaMemcpyAsync(h, s->f_blobs, sizeof(double) * vel, cudaMemcpyDeviceToDevice,
+                             s->stream),
+             "solution history");
+    TFS_CUDA(cudaMemcpyAsync(h + vel, s->v_bodies, sizeof(double) * 6, cudaMemcpyDeviceToDevice,
+                             s->stream),
+             "solution history");
+    s->whist_head = slot;
+    s->whist_n = std::min(2, s->whist_n + 1);
+    s->solved = false;
+  }
+  s->extrap_next = s->whist_n == 2;
+  return TFS_OK;
+}
+
+void solver_reset_history(tfs_solver *s) {
+  s->whist_n = 0;
+  s->solved = false;
+  s->extrap_next = false;
 }
 
 }  // namespace tfs

@@ -1532,6 +1532,8 @@ int tfs_stepper_create(tfs_solver *s, const tfs_step_config *cfg, const double *
 
 int tfs_stepper_initial_guess(tfs_stepper *st, int nt) {
   TFS_CHECK_STEPPER(st);
+  const int hrc = tfs::solver_new_step(st->s);
+  if (hrc != TFS_OK) return hrc;
   // rigid_body::initial_guess (rigid_body.cpp:395-480)
   double gx[3], gu[3];
   for (int k = 0; k < 3; ++k) {
@@ -1826,6 +1828,7 @@ int tfs_stepper_state(tfs_stepper *st, double *x, double *q, double *u, double *
 }
 
 int tfs_stepper_reset(tfs_stepper *st, const double *seg_rotation) {
+  if (st != nullptr) tfs::solver_reset_history(st->s);
   TFS_CHECK_STEPPER(st);
   int rc = load_start(st, seg_rotation);
   if (rc != TFS_OK) return rc;
@@ -1917,6 +1920,7 @@ int stepper_backup(tfs_stepper *st, std::vector<double> &out) {
 // rigid_body.cpp:16-60: q^{n-1} = q); Broyden's memory is cleared and the
 // solver's warm start is the one it had when the stepper was created.
 int stepper_load(tfs_stepper *st, const double *v) {
+  solver_reset_history(st->s);
   const StepDev &d = st->d;
   const size_t ns = d.ns, nf = d.nfil, nl = 3 * (size_t)(d.nseg - 1) * nf;
   std::vector<double> q(4 * ns), x(3 * ns), xm1(3 * ns), xm2(3 * ns), u(3 * ns), um1(3 * ns),

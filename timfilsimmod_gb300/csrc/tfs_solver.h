@@ -46,6 +46,12 @@ struct tfs_solver {
   double tol = 1e-4;         // LINEAR_SYSTEM_TOL
   double inner_tol = 1e-4;   // FP32C: inner GMRES tolerance of each refinement cycle
   bool bootstrap = false;    // the solves of make_body_reference_matrices are running
+  // FP32C: the final solutions of the last two time steps (2 x n, ring of two
+  // with the newest at whist_head), for the first solve of the next step to
+  // start from their linear extrapolation
+  double *whist = nullptr;
+  int whist_n = 0, whist_head = 0;
+  bool solved = false, extrap_next = false;
   long long vec64_retries = 0;  // FP32C refinements rerun with FP64 Arnoldi vectors
   int max_outer = 12;        // FP32C: refinement cycles
   int chunk = 8;             // Arnoldi steps launched between polls of the done flag
@@ -162,4 +168,10 @@ void product_service_stats(ProductService *sv, long long *launches, long long *p
 // compute_velocities on the swimmer force already in s->swimmer_f, queued on
 // s->stream without a host wait at the end (solve.cu).
 int compute_velocities_dev(tfs_solver *s, int *gmres_iters);
+// A new time step begins (the stepper's initial guess): FP32C solvers keep
+// the last step's final solution for the extrapolated warm start of the next
+// step's first solve (solve.cu).
+int solver_new_step(tfs_solver *s);
+// Forget the solutions of earlier steps (the stepper restarted or reloaded).
+void solver_reset_history(tfs_solver *s);
 }  // namespace tfs
