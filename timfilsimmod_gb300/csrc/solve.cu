@@ -534,8 +534,8 @@ namespace {
 // solve with FP64 Arnoldi vectors (on the solver's own launch) instead of
 // FP32 ones. *stalled: a cycle did not reduce the residual (the inner solves
 // cannot make progress on this system).
-int refine_cycles(tfs_solver *s, const GmresArgs &g64, int vec64, int *total, int *cycles,
-                  GmresScalars *h, bool *stalled) {
+int refine_cycles(tfs_solver *s, const GmresArgs &g64, int vec64, bool first_ready, int *total,
+                  int *cycles, GmresScalars *h, bool *stalled) {
   const int vel = 3 * s->nb;
   // the solver's own cooperative launch: when enabled, and for FP64 vectors
   // of a swimmer whose FP32 solves go to a shared launch
@@ -548,11 +548,15 @@ int refine_cycles(tfs_solver *s, const GmresArgs &g64, int vec64, int *total, in
   *stalled = false;
   for (int it = 0; it <= s->max_outer; ++it) {
     // the residual's M_bb product in float-float arithmetic (FP64-grade
-    // accuracy at FP32 instruction rates)
-    cudaError_t e = launch_bb_ff(s->x_blobs, s->xr, s->nb, s->origin, s->cfg.a_blob,
-                                 1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu), s->rec_ff, s->vtmp, s->scratch,
-                                 s->scratch_elems, s->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "refinement residual product");
+    // accuracy at FP32 instruction rates); the first one may have run
+    // already, beside the segment products
+    cudaError_t e = cudaSuccess;
+    if (!(it == 0 && first_ready) &&
+        (e = launch_bb_ff(s->x_blobs, s->xr, s->nb, s->origin, s->cfg.a_blob,
+                          1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu),
+                          s->rec_ff, s->vtmp, s->scratch, s->scratch_elems, s->stream)) !=
+            cudaSuccess)
+      return cuda_fail(e, "refinement residual product");
     if ((e = launch_refine_residual(g64, s->xr, s->r, s->dx, it, s->stream)) != cudaSuccess)
       return cuda_fail(e, "refinement residual");
     if (pending) {
@@ -609,28 +613,53 @@ __global__ void extrapolate_kernel(double *__restrict__ x, const double *__restr
   if (i < n) x[i] = 2.0 * a[i] - b[i];
 }
 
-// xr = the caller's warm start (f_blobs, v_bodies), or, for the first solve
+// xr (on stream st) = the caller's warm start (f_blobs, v_bodies), or, for the first solve
 // of a time step after two earlier steps, 2 x_{n-1} - x_{n-2} of their final
 // solutions: the blob forces and body velocity change smoothly with time, so
 // the extrapolation starts the refinement several digits closer and its
 // inner solve asks for less (the refined result meets the same residual)
-int refine_start(tfs_solver *s) {
+int refine_start(tfs_solver *s, cudaStream_t st) {
   const int vel = 3 * s->nb;
   if (s->extrap_next) {
     s->extrap_next = false;
     const double *h1 = s->whist + (size_t)s->whist_head * s->n;
     const double *h2 = s->whist + (size_t)(s->whist_head ^ 1) * s->n;
-    extrapolate_kernel<<<(s->n + 255) / 256, 256, 0, s->stream>>>(s->xr, h1, h2, s->n);
+    extrapolate_kernel<<<(s->n + 255) / 256, 256, 0, st>>>(s->xr, h1, h2, s->n);
     TFS_CUDA(cudaGetLastError(), "extrapolated warm start");
     count_launch();
     return TFS_OK;
   }
-  TFS_CUDA(cudaMemcpyAsync(s->xr, s->f_blobs, sizeof(double) * vel, cudaMemcpyDeviceToDevice,
-                           s->stream),
+  TFS_CUDA(cudaMemcpyAsync(s->xr, s->f_blobs, sizeof(double) * vel, cudaMemcpyDeviceToDevice, st),
            "refinement start");
-  TFS_CUDA(cudaMemcpyAsync(s->xr + vel, s->v_bodies, sizeof(double) * 6,
-                           cudaMemcpyDeviceToDevice, s->stream),
+  TFS_CUDA(cudaMemcpyAsync(s->xr + vel, s->v_bodies, sizeof(double) * 6, cudaMemcpyDeviceToDevice,
+                           st),
            "refinement start");
+  return TFS_OK;
+}
+
+// compute_velocities' first refinement residual product, on the solver's
+// second stream beside the segment products (which it does not touch): the
+// warm start into xr and M_bb xr (float-float) into vtmp, with partial sums
+// in a buffer of its own. The main stream waits for it before the solve.
+int early_residual_product(tfs_solver *s) {
+  if (s->aux_stream == nullptr) {
+    if (cudaStreamCreateWithFlags(&s->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->aux_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->aux_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(TFS_ECUDA, "second stream creation failed");
+    }
+  }
+  int rc;
+  TFS_CUDA(cudaEventRecord(s->aux_fork, s->stream), "second stream fork");
+  TFS_CUDA(cudaStreamWaitEvent(s->aux_stream, s->aux_fork, 0), "second stream fork");
+  if ((rc = refine_start(s, s->aux_stream)) != TFS_OK) return rc;
+  cudaError_t e = launch_bb_ff(s->x_blobs, s->xr, s->nb, s->origin, s->cfg.a_blob,
+                               1.0 / (8.0 * 3.14159265358979323846264338327950288 * s->cfg.mu),
+                               s->rec_ff, s->vtmp, s->ff_scratch, s->ff_scratch_elems,
+                               s->aux_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "refinement residual product");
+  TFS_CUDA(cudaEventRecord(s->aux_join, s->aux_stream), "second stream join");
   return TFS_OK;
 }
 
@@ -641,8 +670,9 @@ int refine_start(tfs_solver *s) {
 // body rows unscaled against the blob rows, beyond what an FP32 basis
 // resolves, so those solves take FP64 vectors. A refinement that stalls
 // with FP32 vectors is run again from the warm start with FP64 ones, and
-// one that stalls with those finishes in plain FP64 GMRES.
-int linear_solve(tfs_solver *s, int *iters) {
+// one that stalls with those finishes in plain FP64 GMRES. first_ready: xr
+// and its M_bb product are already there (early_residual_product).
+int linear_solve(tfs_solver *s, int *iters, bool first_ready = false) {
   const int fp32 = s->cfg.precision == TFS_FP32C;
   int rc;
   if (!fp32) {
@@ -658,14 +688,14 @@ int linear_solve(tfs_solver *s, int *iters) {
   GmresScalars h{};
   bool stalled = false;
   int vec64 = s->bootstrap ? 1 : 0;
-  if ((rc = refine_start(s)) != TFS_OK ||
-      (rc = refine_cycles(s, g64, vec64, &total, &cycles, &h, &stalled)) != TFS_OK)
+  if ((!first_ready && (rc = refine_start(s, s->stream)) != TFS_OK) ||
+      (rc = refine_cycles(s, g64, vec64, first_ready, &total, &cycles, &h, &stalled)) != TFS_OK)
     return rc;
   if (stalled && !vec64 && s->pg_ok && (s->pg_enabled || s->service)) {
     vec64 = 1;
     ++s->vec64_retries;
-    if ((rc = refine_start(s)) != TFS_OK ||
-        (rc = refine_cycles(s, g64, vec64, &total, &cycles, &h, &stalled)) != TFS_OK)
+    if ((rc = refine_start(s, s->stream)) != TFS_OK ||
+        (rc = refine_cycles(s, g64, vec64, false, &total, &cycles, &h, &stalled)) != TFS_OK)
       return rc;
   }
   if (stalled) {
@@ -699,6 +729,7 @@ int solve_alloc(tfs_solver *s) {
   s->max_iter = std::min(350, s->n);
   const size_t n = s->n, m = s->max_iter, nb3 = 3 * (size_t)s->nb;
   int rc;
+  s->ff_scratch_elems = (size_t)kMaxSplits * 3 * (size_t)s->nb;
   if ((rc = alloc_dev((void **)&s->refs, 8 * nb3)) || (rc = alloc_dev((void **)&s->diff, 8 * nb3)) ||
       (rc = alloc_dev((void **)&s->mats, 8 * 72)) ||
       (rc = alloc_dev((void **)&s->Q, 8 * n * (m + 1))) ||
@@ -713,6 +744,7 @@ int solve_alloc(tfs_solver *s) {
       (rc = alloc_dev((void **)&s->swimmer_f, 8 * 6)) ||
       (rc = alloc_dev((void **)&s->xr, 8 * n)) || (rc = alloc_dev((void **)&s->r, 8 * n)) ||
       (rc = alloc_dev((void **)&s->whist, 8 * 2 * n)) ||
+      (rc = alloc_dev((void **)&s->ff_scratch, 8 * s->ff_scratch_elems)) ||
       (rc = alloc_dev((void **)&s->dx, 8 * n)) ||
       (rc = alloc_dev((void **)&s->gst, 2 * sizeof(GmresScalars))))
     return rc;
@@ -775,6 +807,12 @@ int solve_alloc(tfs_solver *s) {
 }
 
 void solve_free(tfs_solver *s) {
+  if (s->aux_stream) cudaStreamSynchronize(s->aux_stream);
+  if (s->aux_fork) cudaEventDestroy(s->aux_fork);
+  if (s->aux_join) cudaEventDestroy(s->aux_join);
+  if (s->aux_stream) cudaStreamDestroy(s->aux_stream);
+  s->aux_stream = nullptr;
+  s->aux_fork = s->aux_join = nullptr;
   if (s->ready_ev) cudaEventDestroy(s->ready_ev);
   if (s->done_ev) cudaEventDestroy(s->done_ev);
   s->ready_ev = s->done_ev = nullptr;
@@ -782,7 +820,7 @@ void solve_free(tfs_solver *s) {
   s->chunk_graphs.clear();
   double *bufs[] = {s->refs, s->diff, s->mats, s->Q, s->H, s->beta, s->cs, s->sn, s->y, s->z,
                     s->tmp, s->soln, s->rhs, s->vtmp, s->v_bodies, s->swimmer_f, s->xr, s->r,
-                    s->dx, s->gpart, s->gpart6, s->gh1, s->gh2, s->whist};
+                    s->dx, s->gpart, s->gpart6, s->gh1, s->gh2, s->whist, s->ff_scratch};
   for (double *b : bufs) cudaFree(b);
   cudaFree(s->gcounters);
   cudaFree(s->pg_x32);
@@ -943,6 +981,12 @@ int compute_velocities_dev(tfs_solver *s, int *gmres_iters) {
   int rc;
   // read_positions_and_forces: barrier forces (device f_segs, blob repulsion)
   if ((rc = tfs_apply_interparticle_forces(s)) != TFS_OK) return rc;
+  // FP32C: the refinement's first residual product runs beside the segment
+  // products, on the second stream (a solver alone; in a batch or server the
+  // other swimmers' work already fills the GPU)
+  const bool early = s->cfg.precision == TFS_FP32C && s->nb > 0 && s->ff_scratch != nullptr &&
+                     s->service == nullptr && s->product_service == nullptr;
+  if (early && (rc = early_residual_product(s)) != TFS_OK) return rc;
   // v_segs = Mss f_segs, v_blobs = Mbs f_segs (one work-queue launch when
   // both target sets exist)
   if (s->ns > 0 && s->nb > 0) {
@@ -954,8 +998,9 @@ int compute_velocities_dev(tfs_solver *s, int *gmres_iters) {
   const GmresArgs ga = gmres_args(s, s->rhs, s->f_blobs, s->v_bodies, s->gst, s->tol, 0);
   cudaError_t e = launch_rhs(ga, s->f_rep, s->v_blobs, s->swimmer_f, s->rhs, s->stream);
   if (e != cudaSuccess) return cuda_fail(e, "right-hand side");
+  if (early) TFS_CUDA(cudaStreamWaitEvent(s->stream, s->aux_join, 0), "second stream join");
   int iters = 0;
-  if ((rc = linear_solve(s, &iters)) != TFS_OK) return rc;
+  if ((rc = linear_solve(s, &iters, early)) != TFS_OK) return rc;
   // v_segs += Msb f_blobs (the solved blob forces)
   if ((rc = tfs_evaluate_segment_blob_mobility(s)) != TFS_OK) return rc;
   s->last_iters = iters;

@@ -52,6 +52,12 @@ struct tfs_solver {
   double *whist = nullptr;
   int whist_n = 0, whist_head = 0;
   bool solved = false, extrap_next = false;
+  // FP32C: the first refinement residual's M_bb product runs on a second
+  // stream beside the segment products (its own partial sums buffer)
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
+  double *ff_scratch = nullptr;
+  size_t ff_scratch_elems = 0;
   long long vec64_retries = 0;  // FP32C refinements rerun with FP64 Arnoldi vectors
   int max_outer = 12;        // FP32C: refinement cycles
   int chunk = 8;             // Arnoldi steps launched between polls of the done flag
