@@ -115,3 +115,37 @@ def test_medium_default_time_step_fp64_match_reference():
 def test_medium_default_time_step_fp32c_within_1e6():
     broy, ref, _, _ = run_and_compare("step_medium_default_dt", "fp32c", 1e-6)
     assert broy == ref, (broy, ref)
+
+
+def test_fp32c_extrapolated_warm_start():
+    """FP32C: from the third step on, the first solve of a step starts from
+    the linear extrapolation of the last two steps' solutions. Every solve
+    still meets the linear tolerance; the inner GMRES needs far fewer Arnoldi
+    steps than at step 1 (which starts from the last solution); and a reset
+    forgets the history, so the same steps run again give the same states,
+    bit for bit."""
+    d = np.load(os.path.join(GOLD, "step_medium.npz"))
+    s, st = make(d, "fp32c")
+    tol = float(d["linear_tol"])
+    try:
+        runs = []
+        for _ in range(2):
+            gm, states = [], []
+            for nt in range(8):
+                _, g = st.step(nt)
+                info = s.solve_info()
+                assert info["rel_residual"] <= tol, (nt, info)
+                gm.append(g)
+                states.append(st.state())
+            runs.append((gm, states))
+            st.reset()
+        gm, states = runs[0]
+        print("GMRES iterations per step", gm)
+        assert sum(gm[3:]) <= 0.5 * len(gm[3:]) * gm[1], gm
+        assert runs[1][0] == gm
+        for a, b in zip(states, runs[1][1]):
+            for k in a:
+                assert np.array_equal(a[k], b[k]), k
+    finally:
+        st.close()
+        s.finalise()

@@ -716,7 +716,8 @@ int linear_solve(tfs_solver *s, int *iters, bool first_ready = false) {
   *iters = total;
   s->last_outer = cycles;
   s->last_rel = h.rel;
-  s->solved = true;
+  // a solution of a time step (not one of the body-reference solves)
+  if (!s->bootstrap) s->solved = true;
   return TFS_OK;
 }
 

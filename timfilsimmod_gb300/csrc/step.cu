@@ -1503,6 +1503,7 @@ int tfs_stepper_create(tfs_solver *s, const tfs_step_config *cfg, const double *
     tfs_stepper_destroy(st);
     return rc;
   }
+  tfs::solver_reset_history(s);
   // the warm start of the first solve, restored by tfs_stepper_reset
   const size_t nw = 3 * (size_t)s->nb + 6;
   if (cudaMalloc(&st->warm, sizeof(double) * nw) != cudaSuccess) {
