@@ -703,23 +703,25 @@ __device__ void gj_invert_lo(typename Ops::E *J, int n6, typename Ops::E *col, i
       J[(size_t)k * n6 + j] = j == k ? rp : Ops::mul(J[(size_t)k * n6 + j], rp);
     __syncthreads();
     if (jcol < n6) {
-      // four rows at a time, their loads issued together (the shared-memory
-      // latency would otherwise be paid row by row)
-      const E rk = J[(size_t)k * n6 + jcol];
-      for (int i0 = g; i0 < n6; i0 += 4 * ng) {
-        E c[4], x[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int i = i0 + u * ng;
-          c[u] = i < n6 ? col[i] : Ops::zero();
-          x[u] = i < n6 ? J[(size_t)i * n6 + jcol] : Ops::zero();
+      const E rk = J[k * n6 + jcol];
+      E *q = J + g * n6 + jcol;  // rows g, g + ng, ... of column jcol
+      const int st = ng * n6;
+      if (jcol != k) {
+        // col[k] = 0 leaves the pivot row as it is; four rows at a time,
+        // their loads issued together
+        int i = g;
+        for (; i + 3 * ng < n6; i += 4 * ng, q += 4 * st) {
+          const E c0 = col[i], c1 = col[i + ng], c2 = col[i + 2 * ng], c3 = col[i + 3 * ng];
+          const E x0 = q[0], x1 = q[st], x2 = q[2 * st], x3 = q[3 * st];
+          q[0] = Ops::sub_mul(x0, c0, rk);
+          q[st] = Ops::sub_mul(x1, c1, rk);
+          q[2 * st] = Ops::sub_mul(x2, c2, rk);
+          q[3 * st] = Ops::sub_mul(x3, c3, rk);
         }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int i = i0 + u * ng;
-          if (i < n6 && i != k)
-            J[(size_t)i * n6 + jcol] = jcol == k ? Ops::neg_mul(c[u], rk) : Ops::sub_mul(x[u], c[u], rk);
-        }
+        for (; i < n6; i += ng, q += st) q[0] = Ops::sub_mul(q[0], col[i], rk);
+      } else {
+        for (int i = g; i < n6; i += ng, q += st)
+          if (i != k) q[0] = Ops::neg_mul(col[i], rk);
       }
     }
     __syncthreads();
@@ -740,15 +742,16 @@ __device__ void gj_invert_lo(typename Ops::E *J, int n6, typename Ops::E *col, i
 // invert it in place (Gauss-Jordan, partial pivoting), store the inverse,
 // the product JB = B J^-1 and this filament's share of the Schur complement
 // (JB A) and of the body's Lie-algebra self-dependence. With kFF (FP32C
-// solvers) the assembled J and B go to global memory instead and
-// k_jacobian_lo inverts.
+// solvers) J and B are assembled in their global slots instead (no shared
+// memory: launched with few threads, several CTAs share an SM and overlap
+// the FP64 chains of the assembly) and k_jacobian_lo inverts.
 template <bool kFF>
 __global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt) {
   extern __shared__ double sm[];
   const int n = d.nseg, n6 = 6 * n, fil = blockIdx.x, tid = threadIdx.x, nth = blockDim.x;
-  double *J = sm;                          // n6 * n6
-  double *Bm = J + (size_t)n6 * n6;        // 6 * n6
-  double *col = Bm + 6 * n6;               // n6
+  double *J = kFF ? d.jinv + (size_t)n6 * n6 * fil : sm;          // n6 * n6
+  double *Bm = kFF ? d.jb + (size_t)6 * n6 * fil : J + (size_t)n6 * n6;  // 6 * n6
+  double *col = kFF ? sm : Bm + 6 * n6;  // n6 (the inversion's; unused with kFF)
   double *red = col + n6;                  // 32 (pivot search) + 8
   int *perm = reinterpret_cast<int *>(red + 40);
   const int s0 = fil * n;
@@ -821,12 +824,7 @@ __global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt)
     put_block(J, n6, 3 * n + 3, 3 * n, m3_zero());
   }
   __syncthreads();
-  if constexpr (kFF) {  // J and B to global memory; k_jacobian_lo inverts
-    double *jg = d.jinv + (size_t)n6 * n6 * fil, *bg = d.jb + (size_t)6 * n6 * fil;
-    for (int i = tid; i < n6 * n6; i += nth) jg[i] = J[i];
-    for (int i = tid; i < 6 * n6; i += nth) bg[i] = Bm[i];
-    return;
-  }
+  if constexpr (kFF) return;  // J and B are in global memory; k_jacobian_lo inverts
   // Gauss-Jordan inversion in place
   const int warp = tid >> 5, lane = tid & 31;
   const int ng = nth / n6 > 0 ? nth / n6 : 1;  // row groups
@@ -913,6 +911,7 @@ __global__ void __launch_bounds__(256) k_jacobian(StepDev d, BodyArgs b, int nt)
 // keep the reference's Broyden iteration counts (tested at DT 1e-3 and at
 // the reference's default DT) at a third of the float-float form's time.
 constexpr int kJacLoThreads = 512;
+constexpr int kJacAsmThreads = 64;  // k_jacobian<true>: assembly only
 template <class Ops>
 __global__ void __launch_bounds__(kJacLoThreads) k_jacobian_lo(StepDev d, BodyArgs b) {
   using E = typename Ops::E;
@@ -1640,7 +1639,7 @@ int tfs_stepper_prepare_jacobian_inv(tfs_stepper *st, int nt, double *schur_inv)
   // this GPU's slowest pipe)
   st->jinv_f32 = st->s->cfg.precision == TFS_FP32C;
   if (st->jinv_f32) {
-    k_jacobian<true><<<d.nfil, 256, st->jac_smem, str>>>(d, b, nt);
+    k_jacobian<true><<<d.nfil, kJacAsmThreads, 0, str>>>(d, b, nt);
     ST_LAUNCH("approximate Jacobian");
     k_jacobian_lo<JacLoOps><<<d.nfil, kJacLoThreads, st->jac_ff_smem, str>>>(d, b);
   } else {
