@@ -469,3 +469,24 @@ def test_float_host_arrays_match_float64_path():
     s.finalise()
     for g, w in zip(got, want):
         assert np.array_equal(g, w.astype(np.float32))
+
+
+def test_host_arrays_are_page_locked():
+    """The solver's and the flow evaluator's host arrays are page-locked, so
+    the copy hooks run at DMA speed without staging through pageable memory."""
+    from timfilsimmod_gb300.flow_field import FlowFieldEvaluator
+    from timfilsimmod_gb300.mobility import RpyMobilitySolver, host_array_pinned
+
+    s = RpyMobilitySolver(1, 4, 5, 12, precision="fp64")
+    try:
+        for name in ("x_segs_host", "f_segs_host", "v_segs_host", "x_blobs_host",
+                     "f_blobs_host", "v_blobs_host", "f_blobs_repulsion_host"):
+            assert host_array_pinned(getattr(s, name)), name
+    finally:
+        s.finalise()
+    ev = FlowFieldEvaluator(1, 4, 5, 12, 64, precision="fp64")
+    try:
+        for name in ("x_flow_host", "v_flow_host", "x_segs_host", "f_segs_host"):
+            assert host_array_pinned(getattr(ev, name)), name
+    finally:
+        ev.close()

@@ -41,13 +41,15 @@ class FlowFieldEvaluator:
                                          ctypes.byref(h)))
         self._h = h
         ns, nb = nbod * nfil * nseg, nbod * nblob
-        self.x_flow_host = _host_array(3 * nflow, pinned)
-        self.v_flow_host = _host_array(3 * nflow, pinned)
-        self.x_segs_host = _host_array(3 * ns, pinned)
-        self.f_segs_host = _host_array(6 * ns, pinned)
-        self.x_blobs_host = _host_array(3 * nb, pinned)
-        self.f_blobs_host = _host_array(3 * nb, pinned)
-        self.x_bods_host = _host_array(3 * nbod, pinned)
+        self._host_tensors: list = []
+        keep = self._host_tensors
+        self.x_flow_host = _host_array(3 * nflow, pinned, keep)
+        self.v_flow_host = _host_array(3 * nflow, pinned, keep)
+        self.x_segs_host = _host_array(3 * ns, pinned, keep)
+        self.f_segs_host = _host_array(6 * ns, pinned, keep)
+        self.x_blobs_host = _host_array(3 * nb, pinned, keep)
+        self.f_blobs_host = _host_array(3 * nb, pinned, keep)
+        self.x_bods_host = _host_array(3 * nbod, pinned, keep)
 
     def close(self) -> None:
         if self._h is not None:

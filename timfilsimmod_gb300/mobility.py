@@ -28,18 +28,29 @@ class _DeviceArray:
                                          "strides": None}
 
 
-def _host_array(n: int, pinned: bool) -> np.ndarray:
+def _host_array(n: int, pinned: bool, keep: list) -> np.ndarray:
+    """A float64 host array, page-locked when PyTorch can pin it (copies to
+    and from the device then run at DMA speed without staging); the owning
+    tensor is kept in `keep` for the array's lifetime."""
     if pinned:
         try:
             import torch
             if torch.cuda.is_available():
                 t = torch.zeros(n, dtype=torch.float64, pin_memory=True)
-                arr = t.numpy()
-                arr._tfs_keepalive = t  # type: ignore[attr-defined]
-                return arr
+                keep.append(t)
+                return t.numpy()
         except Exception:  # pragma: no cover - pinned memory is an optimisation only
             pass
     return np.zeros(n, dtype=np.float64)
+
+
+def host_array_pinned(a: np.ndarray) -> bool:
+    """Whether a host array is page-locked (False without a GPU)."""
+    try:
+        import torch
+        return torch.cuda.is_available() and bool(torch.from_numpy(a).is_pinned())
+    except Exception:
+        return False
 
 
 def _ptr(a: np.ndarray) -> int:
@@ -87,13 +98,15 @@ class RpyMobilitySolver:
         N.check(self.lib.tfs_solver_create(ctypes.byref(self.cfg), ctypes.byref(h)))
         self._h = h
         ns, nb, pin = self.num_segs, self.num_blobs, self._pinned
-        self.x_segs_host = _host_array(3 * ns, pin)
-        self.f_segs_host = _host_array(6 * ns, pin)
-        self.v_segs_host = _host_array(6 * ns, pin)
-        self.x_blobs_host = _host_array(3 * nb, pin)
-        self.f_blobs_host = _host_array(3 * nb, pin)
-        self.v_blobs_host = _host_array(3 * nb, pin)
-        self.f_blobs_repulsion_host = _host_array(3 * nb, pin)
+        self._host_tensors: list = []
+        keep = self._host_tensors
+        self.x_segs_host = _host_array(3 * ns, pin, keep)
+        self.f_segs_host = _host_array(6 * ns, pin, keep)
+        self.v_segs_host = _host_array(6 * ns, pin, keep)
+        self.x_blobs_host = _host_array(3 * nb, pin, keep)
+        self.f_blobs_host = _host_array(3 * nb, pin, keep)
+        self.v_blobs_host = _host_array(3 * nb, pin, keep)
+        self.f_blobs_repulsion_host = _host_array(3 * nb, pin, keep)
 
     # -- free_host_memory / free_device_memory
     def finalise(self) -> None:
