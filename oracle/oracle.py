@@ -448,3 +448,70 @@ class ReferenceStep:
         self.lib.ref_step_state(*[_ptr(out[k]) for k in ("x", "q", "u", "lam", "tether", "clamp",
                                                          "body_x", "body_q", "body_u")])
         return out
+
+
+class ReferencePrescribed:
+    """The reference's prescribed-cilia mobility solve (mobility_solver.cpp
+    compute_velocities, assemble_rhs, solve_linear_system,
+    apply_preconditioner_new and system_matrix_mult_new under PRESCRIBED_CILIA,
+    with swimmer::make_precon_mat) compiled for the CPU by `make -C oracle ref`
+    in one of the configurations p1, p2, p3 (oracle/Makefile); FP64, GMRES
+    tolerance 1e-10; single instance per process."""
+
+    FLAG_NAMES = {1: "prescribed_body", 2: "dynamic_phase", 4: "dynamic_angle", 8: "weakly_coupled"}
+
+    def __init__(self, config, nfil, nseg, blob_refs, seg_sep, body_x, body_q, phase_refs=(),
+                 angle_refs=()):
+        path = os.path.join(REF_DIR, f"libref_pres_{config}.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = ctypes.CDLL(path)
+        self.nfil, self.nseg = nfil, nseg
+        self.ns = nfil * nseg
+        self.refs = _c(blob_refs)
+        self.nblob = self.refs.size // 3
+        pr, ar = _c(phase_refs if len(phase_refs) else [0.0]), _c(angle_refs if len(angle_refs) else [0.0])
+        bx, bq = _c(body_x), _c(body_q)
+        rc = self.lib.ref_pres_setup(nfil, nseg, self.nblob, ctypes.c_double(seg_sep),
+                                     _ptr(self.refs), _ptr(bx), _ptr(bq), _ptr(pr), len(phase_refs),
+                                     _ptr(ar), len(angle_refs))
+        if rc != 0:
+            raise RuntimeError("ref_pres_setup failed")
+        self.flags = self.lib.ref_pres_flags()
+        self.n = self.lib.ref_pres_system_size()
+
+    @staticmethod
+    def available(config="p1") -> bool:
+        return os.path.exists(os.path.join(REF_DIR, f"libref_pres_{config}.so"))
+
+    def set_kinematics(self, x_segs, vel_dir_phase, vel_dir_angle, phase, omega0, angle, phase_dot):
+        arrs = [_c(a) for a in (x_segs, vel_dir_phase, vel_dir_angle, phase, omega0, angle,
+                                phase_dot)]
+        self.lib.ref_pres_set_kinematics(*[_ptr(a) for a in arrs])
+
+    def set_rates(self, phase_dot, angle_dot):
+        p, a = _c(phase_dot), _c(angle_dot)
+        self.lib.ref_pres_set_rates(_ptr(p), _ptr(a))
+
+    def ktminvk(self):
+        out = np.zeros(36)
+        self.lib.ref_pres_ktminvk(_ptr(out))
+        return out
+
+    def rhs(self, nt=0):
+        out = np.zeros(self.n)
+        self.lib.ref_pres_rhs(int(nt), _ptr(out))
+        return out
+
+    def apply(self, which, v):
+        v = _c(v)
+        out = np.zeros(self.n)
+        self.lib.ref_pres_apply(int(which), _ptr(v), _ptr(out))
+        return out
+
+    def compute_velocities(self, nt=0):
+        fs, fb = np.zeros(3 * self.ns), np.zeros(3 * self.nblob)
+        vb, pd, ad = np.zeros(6), np.zeros(self.nfil), np.zeros(self.nfil)
+        it = self.lib.ref_pres_compute_velocities(int(nt), _ptr(fs), _ptr(fb), _ptr(vb), _ptr(pd),
+                                                  _ptr(ad))
+        return dict(iters=it, f_segs=fs, f_blobs=fb, v_body=vb, phase_dot=pd, angle_dot=ad)

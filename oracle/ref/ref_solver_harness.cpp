@@ -119,6 +119,7 @@ void ref_mss(double *, const double *, const double *, int);
 void ref_msb(double *, const double *, const double *, const double *, int);
 void ref_mbb(double *, const double *, const double *, int);
 void ref_mbs(double *, const double *, const double *, const double *, int);
+void ref_msf(double *, const double *, const double *, int, int);
 void ref_barrier_forces(double *, double *, const double *, const double *, int, int);
 }
 
@@ -171,16 +172,24 @@ class emu_rpy_mobility_solver : public mobility_solver {
   void copy_blob_velocities_to_host() override { std::memcpy(v_blobs_host, vb_d.data(), 8 * vb_d.size()); }
   void copy_segment_velocities_to_host() override { std::memcpy(v_segs_host, vs_d.data(), 8 * vs_d.size()); }
   void apply_interparticle_forces() override {
+#if !PRESCRIBED_CILIA  // the prescribed-cilia configurations never call it
     if (g_use_port)
       orc_barrier_forces(&g_port_params, fs_d.data(), frep_d.data(), xs_d.data(), xb_d.data(), ns(),
                          nb(), NSEG, (int)END_FORCE_MAGNITUDE, REPULSIVE_FORCE_FACTOR, 1);
     else
       ref_barrier_forces(fs_d.data(), frep_d.data(), xs_d.data(), xb_d.data(), ns(), nb());
+#endif
   }
   void wait_for_device() override {}
   void evaluate_segment_segment_mobility() override {
+#if WEAKLY_COUPLED_FILAMENTS_RPY_MOBILITY
+    // weakly_coupled_filaments_rpy_mobility_solver.cu:50-107: filament means
+    // and total forces, then Msf_mult (all by the reference's kernels)
+    ref_msf(vs_d.data(), fs_d.data(), xs_d.data(), ns(), NSWIM * NFIL);
+#else
     if (g_use_port) orc_mss(&g_port_params, vs_d.data(), fs_d.data(), xs_d.data(), ns());
     else ref_mss(vs_d.data(), fs_d.data(), xs_d.data(), ns());
+#endif
   }
   void evaluate_segment_blob_mobility() override {
     if (g_use_port) orc_msb(&g_port_params, vs_d.data(), fb_d.data(), xs_d.data(), xb_d.data(), ns(), nb());
@@ -285,6 +294,7 @@ int ref_max_linear_system_iter(void) { return MAX_LINEAR_SYSTEM_ITER; }
 
 }  // extern "C"
 
+#if INSTABILITY_CILIA
 // ---------------------------------------------------------------------------
 // Implicit time steps (src/cilia/cilia_sim_main.cu:355-527) of one free
 // swimmer with elastic filaments, driven stage by stage so that tests can
@@ -508,3 +518,186 @@ void ref_step_write_files(const char *prefix, int nt) {
 }
 
 }  // extern "C"
+#endif  // INSTABILITY_CILIA
+
+#if PRESCRIBED_CILIA
+// ---------------------------------------------------------------------------
+// Prescribed-cilia mobility solve of one swimmer: compute_velocities under
+// PRESCRIBED_CILIA (mobility_solver.cpp:2574-2596) with assemble_rhs
+// (:282-437), solve_linear_system (:2092-2570), apply_preconditioner_new
+// (:1040-1436) and system_matrix_mult_new (:1806-2026). The filaments'
+// kinematics (segment positions, d x / d phase, d x / d angle, phases,
+// natural frequencies, shape-rotation angles, prescribed phase rates) are
+// set directly instead of by the shape-sequence code, and
+// swimmer::make_precon_mat (swimmer.cpp:1154-1322) runs after them, as
+// swimmer::initial_guess runs it.
+#include <sys/stat.h>
+#include <unistd.h>
+
+// Under PRESCRIBED_CILIA the time step is a run-time global (globals.cu:21);
+// it only scales the prescribed body velocities' time argument, which are
+// zero (rigid_body.cpp:584-598). The solver's DISPLAYTIME blocks
+// (config.hpp:531) synchronise the device before each timer read.
+Real DT = 1.0;
+cudaError_t cudaDeviceSynchronize(void) { return cudaSuccess; }
+
+extern "C" {
+
+// Which prescribed-cilia branches this build compiled: 1 prescribed body
+// velocities, 2 dynamic phase evolution, 4 dynamic shape rotation, 8 weakly
+// coupled filaments' mobility.
+int ref_pres_flags(void) {
+  return (PRESCRIBED_BODY_VELOCITIES ? 1 : 0) | (DYNAMIC_PHASE_EVOLUTION ? 2 : 0) |
+         (DYNAMIC_SHAPE_ROTATION ? 4 : 0) | (WEAKLY_COUPLED_FILAMENTS_RPY_MOBILITY ? 8 : 0);
+}
+
+static void write_force_refs(const std::string &name, const double *v, int n) {
+  std::ofstream f(name);
+  f << n << std::scientific << std::setprecision(17);
+  for (int i = 0; i < n; ++i) f << " " << v[i];
+  f << std::endl;
+}
+
+// One swimmer of nfil x nseg prescribed filaments and nblob blobs. The
+// generalised-force tables (dynamic phase / shape rotation) are written
+// where mobility_solver::initialise reads them (filament.cpp:2036-2083: a
+// path relative to the working directory, here a fresh temporary one).
+int ref_pres_setup(int nfil, int nseg, int nblob, double seg_sep, const double *blob_refs,
+                   const double *body_x, const double *body_q, const double *phase_refs,
+                   int n_phase_refs, const double *angle_refs, int n_angle_refs) {
+  NSWIM = 1; NFIL = nfil; NSEG = nseg; NBLOB = nblob;
+  SEG_SEP = seg_sep; DL = seg_sep;
+  NTOTAL = NSWIM * (NFIL * NSEG + NBLOB);
+  ref_sync_var(NSWIM, NSEG, NFIL, NBLOB, 0, SEG_SEP);
+  delete g_swimmers;
+  g_swimmers = nullptr;
+  if (g_solver) { g_solver->finalise(); delete g_solver; g_solver = nullptr; }
+  char dir[] = "/tmp/tfs_pres_XXXXXX";
+  char cwd[4096];
+  if (mkdtemp(dir) == nullptr || getcwd(cwd, sizeof cwd) == nullptr || chdir(dir) != 0) return -1;
+  mkdir("data", 0755);
+  mkdir("data/forcing", 0755);
+#if DYNAMIC_PHASE_EVOLUTION
+  write_force_refs(reference_phase_generalised_force_file_name(), phase_refs, n_phase_refs);
+#endif
+#if DYNAMIC_SHAPE_ROTATION
+  write_force_refs(reference_angle_generalised_force_file_name(), angle_refs, n_angle_refs);
+#endif
+  g_solver = new emu_rpy_mobility_solver();
+  g_solver->initialise();
+  if (chdir(cwd) != 0) return -1;
+  g_swimmers = new std::vector<swimmer>(1);
+  swimmer &s = (*g_swimmers)[0];
+  s.f = matrix(6, 1);
+  s.f.zero();
+  s.KTMinvK_inv = matrix(6, 6);
+  s.KTMinvK_inv.zero();
+  rigid_body &b = s.body;
+  b.blob_references.assign(blob_refs, blob_refs + 3 * nblob);
+  for (int k = 0; k < 3; ++k) b.x[k] = body_x[k];
+  b.q = quaternion(body_q[0], body_q[1], body_q[2], body_q[3]);
+  b.qm1 = b.q;
+  s.filaments = std::vector<filament>(NFIL);
+  for (int i = 0; i < NFIL; ++i) {
+    filament &fl = s.filaments[i];
+    fl.segments = std::vector<segment>(NSEG);
+    for (int j = 0; j < NSEG; ++j) fl.segments[j].x = &g_solver->x_segs_host[3 * (i * NSEG + j)];
+    fl.vel_dir_phase.assign(3 * NSEG, 0.0);
+    fl.phase = fl.phase_dot = fl.omega0 = 0.0;
+#if DYNAMIC_SHAPE_ROTATION
+    fl.vel_dir_angle.assign(3 * NSEG, 0.0);
+    fl.shape_rotation_angle = fl.shape_rotation_angle_dot = 0.0;
+#endif
+  }
+  return 0;
+}
+
+int ref_pres_system_size(void) { return g_solver->rhs.num_rows; }
+
+// The kinematics of the current step (NULL for the arrays a build does not
+// use), then read_positions_and_forces and make_precon_mat.
+void ref_pres_set_kinematics(const double *x_segs, const double *vel_dir_phase,
+                             const double *vel_dir_angle, const double *phase,
+                             const double *omega0, const double *angle,
+                             const double *phase_dot_prescribed) {
+  swimmer &s = (*g_swimmers)[0];
+  std::memcpy(g_solver->x_segs_host, x_segs, 8 * 3 * g_solver->ns());
+  for (int i = 0; i < NFIL; ++i) {
+    filament &fl = s.filaments[i];
+    for (int k = 0; k < 3 * NSEG; ++k) fl.vel_dir_phase[k] = vel_dir_phase[3 * i * NSEG + k];
+    fl.phase = phase[i];
+    fl.omega0 = omega0[i];
+#if DYNAMIC_SHAPE_ROTATION
+    for (int k = 0; k < 3 * NSEG; ++k) fl.vel_dir_angle[k] = vel_dir_angle[3 * i * NSEG + k];
+    fl.shape_rotation_angle = angle[i];
+#endif
+#if !DYNAMIC_PHASE_EVOLUTION
+    fl.phase_dot = phase_dot_prescribed[i];
+#endif
+  }
+  s.body.qm1 = s.body.q;
+  s.make_precon_mat();
+  g_solver->read_positions_and_forces(*g_swimmers);
+}
+
+// The unknown rates' current values (the warm start of the next solve).
+void ref_pres_set_rates(const double *phase_dot, const double *angle_dot) {
+  swimmer &s = (*g_swimmers)[0];
+  for (int i = 0; i < NFIL; ++i) {
+#if DYNAMIC_PHASE_EVOLUTION
+    s.filaments[i].phase_dot = phase_dot[i];
+#endif
+#if DYNAMIC_SHAPE_ROTATION
+    s.filaments[i].shape_rotation_angle_dot = angle_dot[i];
+#endif
+  }
+}
+
+// swimmer::KTMinvK_inv after make_precon_mat (6x6, column-major).
+void ref_pres_ktminvk(double *out) {
+  const matrix &M = (*g_swimmers)[0].KTMinvK_inv;
+  for (int k = 0; k < 36; ++k) out[k] = M.data[k];
+}
+
+void ref_pres_rhs(int nt, double *rhs) {
+  g_solver->assemble_rhs(*g_swimmers, nt);
+  std::memcpy(rhs, g_solver->rhs.data.data(), 8 * g_solver->rhs.num_rows);
+}
+
+// which = 0: system_matrix_mult_new(in); 1: apply_preconditioner_new(in).
+// (The product writes its input into the solver's force arrays, the warm
+// start of the next solve, as it does in the reference.)
+void ref_pres_apply(int which, const double *in, double *out) {
+  const int n = g_solver->rhs.num_rows;
+  matrix v(n, 1);
+  std::memcpy(v.data.data(), in, 8 * n);
+  const matrix r = which == 0 ? g_solver->system_matrix_mult_new(v, *g_swimmers)
+                              : g_solver->apply_preconditioner_new(v, *g_swimmers);
+  std::memcpy(out, r.data.data(), 8 * n);
+}
+
+// compute_velocities on the kinematics set last; the solution: segment
+// forces (3 per segment), blob forces, body velocities, phase and angle
+// rates. Returns the GMRES iterations.
+int ref_pres_compute_velocities(int nt, double *f_segs, double *f_blobs, double *v_body,
+                                double *phase_dot, double *angle_dot) {
+  swimmer &s = (*g_swimmers)[0];
+  int iters = 0;
+  g_solver->compute_velocities(*g_swimmers, iters, nt);
+  for (int n = 0; n < g_solver->ns(); ++n)
+    for (int k = 0; k < 3; ++k) f_segs[3 * n + k] = g_solver->f_segs_host[6 * n + k];
+  std::memcpy(f_blobs, g_solver->f_blobs_host, 8 * 3 * g_solver->nb());
+  for (int k = 0; k < 6; ++k) v_body[k] = g_solver->v_bodies(k);
+  for (int i = 0; i < NFIL; ++i) {
+    phase_dot[i] = s.filaments[i].phase_dot;
+#if DYNAMIC_SHAPE_ROTATION
+    angle_dot[i] = s.filaments[i].shape_rotation_angle_dot;
+#else
+    angle_dot[i] = 0.0;
+#endif
+  }
+  return iters;
+}
+
+}  // extern "C"
+#endif  // PRESCRIBED_CILIA

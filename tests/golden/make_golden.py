@@ -20,9 +20,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-from oracle import ReferenceFlow, ReferenceKernels, ReferenceSolver, ReferenceStep  # noqa: E402
+from oracle import (ReferenceFlow, ReferenceKernels, ReferencePrescribed, ReferenceSolver,  # noqa: E402
+                    ReferenceStep)
 
-from timfilsimmod_gb300.geometry import fibonacci_sphere, make_config  # noqa: E402
+from timfilsimmod_gb300.geometry import fibonacci_sphere, make_config, prescribed_swimmer  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 END_FORCE = 100      # integer device copy of END_FORCE_MAGNITUDE (globals.hpp:14)
@@ -388,11 +389,67 @@ def case_step_medium_default_dt():
     return _medium_trajectory("s2", 36.3833 / 300.0, 4, (0, 1, 2, 3))
 
 
+def prescribed_inputs(nsteps=3, seed=7):
+    """Kinematics of 8 prescribed filaments x 10 segments on a 162-blob sphere
+    (R = 10) in a rotated, shifted body pose, over nsteps steps, plus
+    generalised-force tables of 40 points."""
+    g = prescribed_swimmer(8, 10, radius=10.0, subdivisions=2, seg_sep=2.6)
+    rng = np.random.default_rng(seed)
+    q = np.array([0.95, 0.1, -0.2, 0.15])
+    q /= np.linalg.norm(q)
+    bx = np.array([0.5, -1.0, 2.0])
+    t = 2.0 * np.pi * np.arange(40) / 40
+    phase_refs = 1.0 + 0.5 * np.sin(t) + 0.2 * np.cos(2.0 * t)
+    angle_refs = 0.1 + 0.3 * np.sin(t) - 0.05 * np.cos(3.0 * t)
+    phase0 = rng.uniform(0.0, 2.0 * np.pi, g.nfil)
+    omega0 = 2.0 * np.pi * (1.0 + 0.2 * rng.uniform(-1.0, 1.0, g.nfil))
+    angle0 = rng.uniform(-0.3, 0.3, g.nfil)
+    phase = np.stack([phase0 + 0.05 * omega0 * nt for nt in range(nsteps)])
+    angle = np.stack([angle0 * np.cos(nt) for nt in range(nsteps)])
+    kin = [g.kinematics(phase[nt], angle[nt], bx, q) for nt in range(nsteps)]
+    return dict(nfil=g.nfil, nseg=g.nseg, seg_sep=g.seg_sep, blob_refs=g.blob_references,
+                body_x=bx, body_q=q, phase_refs=phase_refs, angle_refs=angle_refs, omega0=omega0,
+                phase=phase, angle=angle, x_segs=np.stack([k[0] for k in kin]),
+                vel_dir_phase=np.stack([k[1] for k in kin]),
+                vel_dir_angle=np.stack([k[2] for k in kin]),
+                phase_dot0=omega0.copy(), angle_dot0=np.zeros(g.nfil),
+                gen_force_magnitude_factor=1.0, torsional_spring_magnitude_factor=2.0)
+
+
+def case_prescribed(config):
+    """The reference's prescribed-cilia solve (configuration p1, p2 or p3 of
+    oracle/Makefile): three consecutive solves (warm started from the last),
+    then, on the first step's kinematics, the right-hand side, swimmer
+    KTMinvK_inv, and the operator and preconditioner applied to a seeded
+    vector."""
+    d = prescribed_inputs()
+    ref = ReferencePrescribed(config, d["nfil"], d["nseg"], d["blob_refs"], d["seg_sep"],
+                              d["body_x"], d["body_q"], d["phase_refs"], d["angle_refs"])
+    ref.set_rates(d["phase_dot0"], d["angle_dot0"])
+    outs = []
+    for nt in range(d["phase"].shape[0]):
+        ref.set_kinematics(d["x_segs"][nt], d["vel_dir_phase"][nt], d["vel_dir_angle"][nt],
+                           d["phase"][nt], d["omega0"], d["angle"][nt], d["omega0"])
+        outs.append(ref.compute_velocities(nt))
+    ref.set_kinematics(d["x_segs"][0], d["vel_dir_phase"][0], d["vel_dir_angle"][0],
+                       d["phase"][0], d["omega0"], d["angle"][0], d["omega0"])
+    v_in = np.random.default_rng(11).normal(size=ref.n)
+    d.update(flags=ref.flags, n=ref.n, ktminvk=ref.ktminvk(), rhs0=ref.rhs(0), v_in=v_in,
+             a_v=ref.apply(0, v_in), pinv_v=ref.apply(1, v_in),
+             iters=np.array([o["iters"] for o in outs]))
+    for key in ("f_segs", "f_blobs", "v_body", "phase_dot", "angle_dot"):
+        d[key] = np.stack([o[key] for o in outs])
+    return d
+
+
 CASES = {"small_matvec": case_small, "overlap_a16": case_overlap, "tiny": case_tiny,
          "flow_small": case_flow, "solve_small": case_solve, "step_small": case_step,
          "step_io": case_step_io, "step_default_dt": case_step_default_dt,
          "weak_coupled": case_weak, "step_medium": case_step_medium,
-         "step_medium_default_dt": case_step_medium_default_dt}
+         "step_medium_default_dt": case_step_medium_default_dt,
+         "prescribed_p1": lambda: case_prescribed("p1"),
+         "prescribed_p2": lambda: case_prescribed("p2"),
+         "prescribed_p3": lambda: case_prescribed("p3")}
 
 
 def main():

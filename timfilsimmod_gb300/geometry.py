@@ -168,3 +168,71 @@ def elastic_swimmer(nfil: int, nseg: int = 20, seg_sep: float = 2.2, a_blob: flo
     normals = fibonacci_sphere(nfil)
     fil_refs = (radius + a_blob + 0.5 * seg_sep) * normals
     return blob_refs, fil_refs, normals, radius
+
+
+def quat_rot(q) -> np.ndarray:
+    """Rotation matrix of the unit quaternion q = (q0, q1, q2, q3), scalar
+    first (quaternion.cpp rot_mat)."""
+    q0, q1, q2, q3 = (float(v) for v in q)
+    return np.array([
+        [1 - 2 * (q2 * q2 + q3 * q3), 2 * (q1 * q2 - q0 * q3), 2 * (q1 * q3 + q0 * q2)],
+        [2 * (q1 * q2 + q0 * q3), 1 - 2 * (q1 * q1 + q3 * q3), 2 * (q2 * q3 - q0 * q1)],
+        [2 * (q1 * q3 - q0 * q2), 2 * (q2 * q3 + q0 * q1), 1 - 2 * (q1 * q1 + q2 * q2)]])
+
+
+@dataclass
+class PrescribedSwimmer:
+    """A sphere of blobs carrying filaments whose shapes follow a prescribed
+    beat: link j of a filament at phase phi makes the angle
+    theta_j = A sin(phi - k s_j) s_j (s_j = (j + 1/2) / nseg) with the surface
+    normal n, in the plane of n and a tangent t1, and the whole shape is
+    tilted by the shape-rotation angle psi about t2 = n x t1 (the axis the
+    reference's DYNAMIC_SHAPE_ROTATION turns the beat plane's vertical about).
+    Synthetic kinematics of the reference's prescribed-cilia solve, whose
+    shape sequences (filament.cpp:680-860) need its fitted s-value files."""
+    blob_references: np.ndarray  # (Nb, 3) body frame
+    normals: np.ndarray          # (nfil, 3) body frame
+    t1: np.ndarray
+    t2: np.ndarray
+    base: np.ndarray             # (nfil, 3) body frame: filament roots
+    nfil: int
+    nseg: int
+    seg_sep: float
+    amplitude: float = 0.9
+    wavenumber: float = 2.0
+
+    def kinematics(self, phase, angle, body_x=(0.0, 0.0, 0.0), body_q=(1.0, 0.0, 0.0, 0.0)):
+        """Segment positions x (Ns, 3) and the velocity directions d x / d phase
+        and d x / d psi (Ns, 3 each) at the filaments' phases and shape-rotation
+        angles, in the lab frame of the body pose (body_x, body_q)."""
+        phase = np.asarray(phase, dtype=np.float64)[:, None]
+        psi = np.asarray(angle, dtype=np.float64)[:, None, None]
+        s = (np.arange(self.nseg, dtype=np.float64) + 0.5) / self.nseg
+        th = self.amplitude * np.sin(phase - self.wavenumber * s[None, :]) * s[None, :]
+        dth = self.amplitude * np.cos(phase - self.wavenumber * s[None, :]) * s[None, :]
+        n, t1, t2 = self.normals[:, None, :], self.t1[:, None, :], self.t2[:, None, :]
+        # the beat in the (n, t1) plane tilted by psi about t2: n -> n cos psi - t1 sin psi
+        nt = n * np.cos(psi) - t1 * np.sin(psi)
+        tt = t1 * np.cos(psi) + n * np.sin(psi)
+        tang = np.cos(th)[..., None] * nt + np.sin(th)[..., None] * tt
+        dtang = (-np.sin(th) * dth)[..., None] * nt + (np.cos(th) * dth)[..., None] * tt
+        zero = np.zeros((self.nfil, 1, 3))
+        rel = np.cumsum(np.concatenate([zero, self.seg_sep * tang[:, :-1, :]], axis=1), axis=1)
+        vphi = np.cumsum(np.concatenate([zero, self.seg_sep * dtang[:, :-1, :]], axis=1), axis=1)
+        vpsi = np.cross(rel, np.broadcast_to(t2, rel.shape))  # d rel / d psi
+        R = quat_rot(body_q)
+        bx = np.asarray(body_x, dtype=np.float64)
+        x = bx + (self.base[:, None, :] + rel).reshape(-1, 3) @ R.T
+        return (np.ascontiguousarray(x), np.ascontiguousarray(vphi.reshape(-1, 3) @ R.T),
+                np.ascontiguousarray(vpsi.reshape(-1, 3) @ R.T))
+
+
+def prescribed_swimmer(nfil: int, nseg: int = 10, radius: float = 10.0, subdivisions: int = 2,
+                       seg_sep: float = 2.6, a_blob: float = 1.0) -> PrescribedSwimmer:
+    """Blobs on an icosphere of the given radius, filaments rooted on a
+    Fibonacci lattice one blob radius plus half a segment gap above it."""
+    normals = fibonacci_sphere(nfil)
+    t1, t2 = _tangent_frames(normals)
+    return PrescribedSwimmer(blob_references=radius * icosphere(subdivisions), normals=normals,
+                             t1=t1, t2=t2, base=(radius + a_blob + 0.5 * seg_sep) * normals,
+                             nfil=nfil, nseg=nseg, seg_sep=seg_sep)
