@@ -223,6 +223,80 @@ int tfs_solve_info(tfs_solver *s, int *iters, int *cycles, double *rel_residual)
  * stall (a count over the solver's life). */
 int tfs_refinement_retries(tfs_solver *s, long long *retries);
 
+/* --- prescribed-cilia solve ---------------------------------------------- */
+/* The reference's mobility solve for filaments that follow a prescribed
+ * sequence of shapes (CILIA_TYPE 3): compute_velocities under
+ * PRESCRIBED_CILIA (mobility_solver.cpp:2574-2596) with assemble_rhs
+ * (:282-437), solve_linear_system (:2092-2570), apply_preconditioner_new
+ * (:1040-1436), system_matrix_mult_new (:1806-2026) and
+ * swimmer::make_precon_mat (swimmer.cpp:1154-1322), for one swimmer, FP64.
+ * Unknowns (reference order): segment forces (3 Ns), blob forces (3 Nb), body
+ * velocity and angular velocity (6, free body), phase rates (nfil, dynamic
+ * phase), shape-rotation rates (nfil, dynamic shape rotation). Segment
+ * positions come through tfs_copy_segment_positions_to_device, the body
+ * through tfs_set_blob_references and tfs_set_body_pose; the GMRES tolerance
+ * through tfs_set_linear_solver (the iteration cap is the reference's
+ * MAX_LINEAR_SYSTEM_ITER, min(350, unknowns)). */
+#define TFS_PRESCRIBED_BODY 1 /* PRESCRIBED_BODY_VELOCITIES: the body moves as given */
+#define TFS_DYNAMIC_PHASE 2   /* DYNAMIC_PHASE_EVOLUTION: phase rates are unknowns */
+#define TFS_DYNAMIC_ANGLE 4   /* DYNAMIC_SHAPE_ROTATION: shape-rotation rates are unknowns */
+#define TFS_WEAKLY_COUPLED 8  /* WEAKLY_COUPLED_FILAMENTS_RPY_MOBILITY: Msf_mult for the
+                                 segment block (cuda_functions.cu:1129-1229) */
+typedef struct tfs_prescribed_config {
+  int flags;                                /* TFS_PRESCRIBED_BODY | ... */
+  double gen_force_magnitude_factor;        /* GEN_FORCE_MAGNITUDE_FACTOR (globals) */
+  double torsional_spring_magnitude_factor; /* TORSIONAL_SPRING_MAGNITUDE_FACTOR */
+  double fil_length;                        /* FIL_LENGTH = DL (NSEG - 1), config.hpp:515-521 */
+} tfs_prescribed_config;
+/* Defaults: factors 1 and 2 (globals.ini), fil_length = dl (nseg - 1). */
+int tfs_prescribed_config_default(tfs_prescribed_config *pc, int flags, int nseg, double dl);
+/* Allocates the solve for the solver's sizes (nswim = 1; the blob references
+ * must be set). The generalised-force tables over one period (the reference
+ * reads them in mobility_solver::initialise, :28-116) are needed with the
+ * dynamic phase / shape rotation flags. A free body takes both dynamic flags
+ * or neither: the reference's free-body preconditioner indexes both. The
+ * solution (warm start) starts at zero. */
+int tfs_prescribed_setup(tfs_solver *s, const tfs_prescribed_config *pc,
+                         const double *phase_force_refs, int n_phase_refs,
+                         const double *angle_force_refs, int n_angle_refs);
+/* The filaments' state for one solve (the fields of filament.hpp the solve
+ * reads); arrays a configuration does not use may be NULL. */
+typedef struct tfs_prescribed_kinematics {
+  const double *vel_dir_phase;        /* 3 Ns: d x / d phase of every segment */
+  const double *vel_dir_angle;        /* 3 Ns: d x / d angle (dynamic shape rotation) */
+  const double *phase;                /* nfil (dynamic phase or shape rotation) */
+  const double *omega0;               /* nfil natural frequencies (idem) */
+  const double *shape_rotation_angle; /* nfil (dynamic shape rotation) */
+  const double *phase_dot;            /* nfil prescribed rates (without dynamic phase) */
+  const double *v_body;               /* 6: prescribed body velocities; NULL = zero, as
+                                         rigid_body.cpp:584-598 */
+} tfs_prescribed_kinematics;
+/* Uploads the kinematics and computes the per-filament constants and (free
+ * body) the inverse body block, swimmer.KTMinvK_inv, on the current segment
+ * positions and body pose. Synchronises the solver's stream. */
+int tfs_prescribed_set_kinematics(tfs_solver *s, const tfs_prescribed_kinematics *k);
+/* assemble_rhs and the GMRES solve on the kinematics set last, warm started
+ * from the previous solution. Synchronises the solver's stream. */
+int tfs_prescribed_solve(tfs_solver *s, int *gmres_iters);
+/* tfs_prescribed_set_kinematics, then tfs_prescribed_solve. */
+int tfs_prescribed_compute_velocities(tfs_solver *s, const tfs_prescribed_kinematics *k,
+                                      int *gmres_iters);
+/* One piece on host vectors of tfs_prescribed_size entries: which = 0 the
+ * operator A in, 1 the preconditioner P^-1 in, 2 the right-hand side (in
+ * unused). */
+int tfs_prescribed_apply(tfs_solver *s, int which, const double *in, double *out);
+int tfs_prescribed_size(tfs_solver *s, int *n);
+/* The inverse body block (6 x 6, column-major) of the kinematics set last. */
+int tfs_prescribed_precon_matrix(tfs_solver *s, double *m36);
+/* The solution of the last solve, which is also the next solve's warm start:
+ * segment forces (3 Ns), blob forces (3 Nb), body velocities (6), phase and
+ * angle rates (nfil each); NULL skips a part, absent parts read as zero. */
+int tfs_prescribed_solution(tfs_solver *s, double *f_segs, double *f_blobs, double *v_body,
+                            double *phase_dot, double *angle_dot);
+int tfs_prescribed_set_solution(tfs_solver *s, const double *f_segs, const double *f_blobs,
+                                const double *v_body, const double *phase_dot,
+                                const double *angle_dot);
+
 /* --- autotuning ---------------------------------------------------------- */
 /* Products run as work-queue launches: one persistent grid whose CTAs take
  * (target block, source chunk) units of every product of the launch from a

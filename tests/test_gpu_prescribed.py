@@ -1,0 +1,155 @@
+"""GPU parity of the prescribed-cilia solve (tfs_prescribed_*) against the
+reference's own solver in three prescribed-cilia configurations
+(tests/golden/prescribed_p*.npz: mobility_solver.cpp under PRESCRIBED_CILIA,
+LINEAR_SYSTEM_TOL = 1e-10) and against the CPU restatement
+(oracle/prescribed.py) on a larger swimmer.
+
+Tolerances, FP64 throughout:
+  pieces (right-hand side, operator, preconditioner, KTMinvK_inv): relative
+  max-abs error <= 1e-12 (the pair sums differ from the reference's
+  sequential order only by rounding);
+  solves: <= 1e-8 relative max-abs error (two GMRES runs stopped at a 1e-10
+  relative residual agree to about cond(A) x 1e-10), GMRES iteration counts
+  within one of the reference's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+CONFIGS = ("p1", "p2", "p3")
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def load(cfg):
+    return dict(np.load(os.path.join(GOLD, f"prescribed_{cfg}.npz")))
+
+
+def make(d, tol=1e-10):
+    from timfilsimmod_gb300.prescribed import PrescribedCiliaSolver
+    return PrescribedCiliaSolver(int(d["flags"]), int(d["nfil"]), int(d["nseg"]), d["blob_refs"],
+                                 float(d["seg_sep"]), d["phase_refs"], d["angle_refs"],
+                                 body_x=d["body_x"], body_q=d["body_q"], tol=tol,
+                                 gen_force_magnitude_factor=float(d["gen_force_magnitude_factor"]),
+                                 torsional_spring_magnitude_factor=float(
+                                     d["torsional_spring_magnitude_factor"]))
+
+
+def kin(d, nt):
+    return dict(x_segs=d["x_segs"][nt], vel_dir_phase=d["vel_dir_phase"][nt],
+                vel_dir_angle=d["vel_dir_angle"][nt], phase=d["phase"][nt], omega0=d["omega0"],
+                shape_rotation_angle=d["angle"][nt], phase_dot=d["omega0"])
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_pieces_match_reference(cfg):
+    d = load(cfg)
+    ps = make(d)
+    assert ps.n == int(d["n"])
+    ps.set_kinematics(**kin(d, 0))
+    assert rel(ps.apply("rhs"), d["rhs0"]) <= 1e-12
+    assert rel(ps.apply("operator", d["v_in"]), d["a_v"]) <= 1e-12
+    assert rel(ps.apply("preconditioner", d["v_in"]), d["pinv_v"]) <= 1e-12
+    if not int(d["flags"]) & 1:  # free body: swimmer.KTMinvK_inv
+        assert rel(ps.precon_matrix(), d["ktminvk"]) <= 1e-12
+    ps.finalise()
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_warm_started_solves_match_reference(cfg):
+    """Three consecutive solves, each warm started from the last (the first
+    from phase rates omega0 and zero angle rates, as the golden's)."""
+    d = load(cfg)
+    ps = make(d)
+    ps.set_solution(phase_dot=d["phase_dot0"], angle_dot=d["angle_dot0"])
+    flags = int(d["flags"])
+    for nt in range(d["phase"].shape[0]):
+        iters = ps.compute_velocities(**kin(d, nt))
+        assert abs(iters - int(d["iters"][nt])) <= 1, (nt, iters, int(d["iters"][nt]))
+        sol = ps.solution()
+        assert rel(sol["f_segs"], d["f_segs"][nt]) <= 1e-8
+        assert rel(sol["f_blobs"], d["f_blobs"][nt]) <= 1e-8
+        if not flags & 1:
+            assert rel(sol["v_body"], d["v_body"][nt]) <= 1e-8
+        if flags & 2:
+            assert rel(sol["phase_dot"], d["phase_dot"][nt]) <= 1e-8
+        if flags & 4:
+            assert rel(sol["angle_dot"], d["angle_dot"][nt]) <= 1e-8
+    ps.finalise()
+
+
+def test_zero_rhs_gives_zero_solution():
+    """A zero right-hand side (no prescribed rates, no generalised forces)
+    zeroes the whole solution and takes no GMRES step
+    (mobility_solver.cpp:2121-2200)."""
+    d = load("p3")
+    ps = make(d)
+    ps.set_solution(f_segs=np.ones(3 * int(d["nfil"]) * int(d["nseg"])))
+    k = kin(d, 0)
+    k["phase_dot"] = np.zeros_like(d["omega0"])
+    assert ps.compute_velocities(**k) == 0
+    sol = ps.solution()
+    assert np.all(sol["f_segs"] == 0.0) and np.all(sol["f_blobs"] == 0.0)
+    assert np.all(sol["v_body"] == 0.0)
+    ps.finalise()
+
+
+@pytest.mark.parametrize("flags", [0, 6, 15])
+def test_larger_swimmer_vs_oracle(flags):
+    """160 filaments x 20 segments on a 642-blob sphere (3 842 particles):
+    the operator and preconditioner against the CPU restatement, and the
+    solve's residual ||b - A x|| <= 1e-10 ||b|| through the GPU operator."""
+    from prescribed import PrescribedSystem
+    from timfilsimmod_gb300.geometry import prescribed_swimmer
+    from timfilsimmod_gb300.prescribed import PrescribedCiliaSolver
+    g = prescribed_swimmer(160, 20, radius=20.0, subdivisions=3, seg_sep=2.2)
+    rng = np.random.default_rng(3)
+    q = np.array([0.9, -0.1, 0.3, 0.2])
+    q /= np.linalg.norm(q)
+    bx = np.array([1.0, 2.0, -0.5])
+    phase = rng.uniform(0, 2 * np.pi, g.nfil)
+    angle = rng.uniform(-0.2, 0.2, g.nfil)
+    omega0 = 2 * np.pi * (1 + 0.1 * rng.uniform(-1, 1, g.nfil))
+    x, vp, va = g.kinematics(phase, angle, bx, q)
+    t = 2 * np.pi * np.arange(64) / 64
+    tp, ta = 1 + 0.4 * np.sin(t), 0.2 * np.cos(t)
+    ps = PrescribedCiliaSolver(flags, g.nfil, g.nseg, g.blob_references, g.seg_sep, tp, ta,
+                               body_x=bx, body_q=q, tol=1e-10)
+    k = dict(x_segs=x, vel_dir_phase=vp, vel_dir_angle=va, phase=phase, omega0=omega0,
+             shape_rotation_angle=angle, phase_dot=omega0)
+    ps.set_kinematics(**k)
+    S = PrescribedSystem(flags, g.nfil, g.nseg, x, g.blob_references, bx, q, vp, va)
+    S.orc.set_threads(os.cpu_count() or 1)
+    v = rng.normal(size=ps.n)
+    assert rel(ps.apply("operator", v), S.apply_a(v)) <= 1e-12
+    assert rel(ps.apply("preconditioner", v), S.apply_pinv(v)) <= 1e-12
+    b = ps.apply("rhs")
+    assert rel(b, S.rhs(phase, omega0, angle, omega0, tp, ta,
+                        fil_length=g.seg_sep * (g.nseg - 1))) <= 1e-13
+    iters = ps.solve()
+    assert 0 < iters < 350
+    sol = ps.solution()
+    xs = np.concatenate([sol["f_segs"].ravel(), sol["f_blobs"].ravel()]
+                        + ([sol["v_body"]] if not flags & 1 else [])
+                        + ([sol["phase_dot"]] if flags & 2 else [])
+                        + ([sol["angle_dot"]] if flags & 4 else []))
+    assert np.linalg.norm(b - ps.apply("operator", xs)) <= 1.5e-10 * np.linalg.norm(b)
+    ps.finalise()
+
+
+def test_flag_validation():
+    """Free body with only one of the dynamic flags is rejected (the
+    reference's free-body preconditioner indexes both)."""
+    from timfilsimmod_gb300 import _native as N
+    d = load("p1")
+    with pytest.raises(N.TfsError):
+        from timfilsimmod_gb300.prescribed import PrescribedCiliaSolver
+        PrescribedCiliaSolver(2, int(d["nfil"]), int(d["nseg"]), d["blob_refs"],
+                              float(d["seg_sep"]), d["phase_refs"], d["angle_refs"])

@@ -57,6 +57,24 @@ class StepConfig(ctypes.Structure):
                 ("body_q", ctypes.c_double * 4)]
 
 
+class PrescribedConfig(ctypes.Structure):
+    _fields_ = [("flags", ctypes.c_int), ("gen_force_magnitude_factor", ctypes.c_double),
+                ("torsional_spring_magnitude_factor", ctypes.c_double),
+                ("fil_length", ctypes.c_double)]
+
+
+class PrescribedKinematics(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("vel_dir_phase", "vel_dir_angle", "phase",
+                                                "omega0", "shape_rotation_angle", "phase_dot",
+                                                "v_body")]
+
+
+TFS_PRESCRIBED_BODY = 1
+TFS_DYNAMIC_PHASE = 2
+TFS_DYNAMIC_ANGLE = 4
+TFS_WEAKLY_COUPLED = 8
+
+
 class Request(ctypes.Structure):
     _fields_ = [("nfil", ctypes.c_int), ("nseg", ctypes.c_int), ("nblob", ctypes.c_int),
                 ("blob_refs", ctypes.c_void_p), ("fil_refs", ctypes.c_void_p),
@@ -125,6 +143,18 @@ _SIGNATURES = {
     "tfs_set_body_velocities": [_H, _P],
     "tfs_copy_blob_forces_to_host": [_H, _P],
     "tfs_refinement_retries": [_H, ctypes.POINTER(ctypes.c_longlong)],
+    "tfs_prescribed_config_default": [ctypes.POINTER(PrescribedConfig), ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_double],
+    "tfs_prescribed_setup": [_H, ctypes.POINTER(PrescribedConfig), _P, ctypes.c_int, _P,
+                             ctypes.c_int],
+    "tfs_prescribed_set_kinematics": [_H, ctypes.POINTER(PrescribedKinematics)],
+    "tfs_prescribed_solve": [_H, _IP],
+    "tfs_prescribed_compute_velocities": [_H, ctypes.POINTER(PrescribedKinematics), _IP],
+    "tfs_prescribed_apply": [_H, ctypes.c_int, _P, _P],
+    "tfs_prescribed_size": [_H, _IP],
+    "tfs_prescribed_precon_matrix": [_H, _P],
+    "tfs_prescribed_solution": [_H, _P, _P, _P, _P, _P],
+    "tfs_prescribed_set_solution": [_H, _P, _P, _P, _P, _P],
     "tfs_solve_info": [_H, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                        ctypes.POINTER(ctypes.c_double)],
     "tfs_solver_enable_kernel_timing": [_H, ctypes.c_int],

@@ -91,6 +91,7 @@ static void free_all(tfs_solver *s) {
   s->events.clear();
   if (s->pready_ev) cudaEventDestroy(s->pready_ev);
   if (s->pdone_ev) cudaEventDestroy(s->pdone_ev);
+  pres_free(s);
   solve_free(s);
   cudaFree(s->x_segs);
   cudaFree(s->f_segs);

@@ -15,6 +15,7 @@
 namespace tfs {
 struct GmresService;
 struct ProductService;
+struct PresState;
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 long long launch_count();
@@ -126,6 +127,8 @@ struct tfs_solver {
   };
   std::vector<ChunkGraph> chunk_graphs;
   bool graphs_enabled = true;
+  // the prescribed-cilia solve (prescribed.cu), made by tfs_prescribed_setup
+  tfs::PresState *pres = nullptr;
   // dominant-kernel timing (tfs_solver_enable_kernel_timing)
   bool timing = false;
   std::vector<cudaEvent_t> events;  // pairs, in launch order
@@ -180,4 +183,6 @@ int compute_velocities_dev(tfs_solver *s, int *gmres_iters);
 int solver_new_step(tfs_solver *s);
 // Forget the solutions of earlier steps (the stepper restarted or reloaded).
 void solver_reset_history(tfs_solver *s);
+// Free the prescribed-cilia solve's buffers (prescribed.cu).
+void pres_free(tfs_solver *s);
 }  // namespace tfs
