@@ -306,6 +306,8 @@ def bench_ours(args):
     large = None if args.no_large else large_bench(stream, flush, args, peak32, peak64)
     # --- the flow-field evaluator on a 128^3 grid around the large swimmer -----
     flow = None if args.no_flow else flow_bench(stream, flush, args, peak32, peak64, rank)
+    # --- the prescribed-cilia solve on the medium swimmer's sizes ---------------
+    prescribed = None if args.no_prescribed else prescribed_bench(args)
     clocks = sampler.stop()
 
     # max over ranks
@@ -387,12 +389,72 @@ def bench_ours(args):
             result["flow"] = flow
         if large is not None:
             result["large"] = large
+        if prescribed is not None:
+            result["prescribed"] = prescribed
     for sv in (s32, s64):
         sv.finalise()
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
     return result
+
+
+def prescribed_bench(args, timed=4):
+    """The prescribed-cilia solve (compute_velocities under PRESCRIBED_CILIA,
+    tfs_prescribed_*) at the medium swimmer's sizes: 640 beating filaments x
+    20 segments on the 2562-blob sphere (R = 60), 47 366 unknowns; the
+    shipped branches (zero prescribed body velocities, dynamic phase and
+    shape rotation) and the free body with the same dynamic unknowns, RPY
+    mobility, LINEAR_SYSTEM_TOL 1e-8. One warm-up solve, then `timed`
+    consecutive warm-started solves with the phases advanced by omega0 dt
+    (dt = 1e-2); wall clock per compute_velocities (it ends with a stream
+    synchronisation), FP64 and FP32C."""
+    from timfilsimmod_gb300.geometry import prescribed_swimmer
+    from timfilsimmod_gb300.prescribed import PrescribedCiliaSolver
+    g = prescribed_swimmer(640, 20, radius=60.0, subdivisions=4, seg_sep=2.6)
+    rng = np.random.default_rng(5)
+    phase0 = rng.uniform(0.0, 2.0 * np.pi, g.nfil)
+    omega0 = 2.0 * np.pi * (1.0 + 0.05 * rng.uniform(-1.0, 1.0, g.nfil))
+    angle0 = rng.uniform(-0.1, 0.1, g.nfil)
+    t = 2.0 * np.pi * np.arange(100) / 100
+    tab_p, tab_a = 1.0 + 0.5 * np.sin(t), 0.2 * np.cos(t)
+    out = {"workload": (f"{g.nfil} prescribed filaments x {g.nseg} segments, "
+                        f"{g.blob_references.shape[0]} blobs; RPY mobility, dynamic phase and "
+                        "shape rotation, linear residual 1e-8; solves warm started from the "
+                        "previous step's solution")}
+    for name, flags in (("prescribed_body", 7), ("free_body", 6)):
+        leg, sols = {}, {}
+        for prec in ("fp64", "fp32c"):
+            ps = PrescribedCiliaSolver(flags, g.nfil, g.nseg, g.blob_references, g.seg_sep, tab_p,
+                                       tab_a, tol=1e-8, precision=prec)
+            ps.set_solution(phase_dot=omega0)
+            ms, its, cyc, rels = [], [], [], []
+            for nt in range(timed + 1):
+                ph = phase0 + omega0 * 1e-2 * nt
+                x, vp, va = g.kinematics(ph, angle0, (0.0, 0.0, 0.0), (1.0, 0.0, 0.0, 0.0))
+                t0 = time.perf_counter()
+                it = ps.compute_velocities(x, vp, va, ph, omega0, angle0, omega0)
+                t1 = time.perf_counter()
+                if nt == 0:
+                    continue
+                info = ps.solve_info()
+                ms.append((t1 - t0) * 1e3)
+                its.append(it)
+                cyc.append(info["cycles"])
+                rels.append(info["rel_residual"])
+            sols[prec] = ps.solution()
+            leg[prec] = {"ms_per_solve": float(np.mean(ms)), "solves_per_s": 1e3 / float(np.mean(ms)),
+                         "gmres_iters_mean": float(np.mean(its)), "cycles_last": int(cyc[-1]),
+                         "rel_residual_max": float(np.max(rels)), "unknowns": ps.n,
+                         "timed_solves": timed}
+            ps.finalise()
+        ref = sols["fp64"]
+        dev = max(float(np.abs(sols["fp32c"][k] - ref[k]).max() / max(np.abs(ref[k]).max(), 1e-300))
+                  for k in ("f_segs", "f_blobs", "phase_dot", "angle_dot"))
+        leg["speedup_fp32c_vs_fp64"] = leg["fp64"]["ms_per_solve"] / leg["fp32c"]["ms_per_solve"]
+        leg["fp32c_rel_dev_vs_fp64"] = dev
+        out[name] = leg
+    return out
 
 
 def solve_bench(sw, stream, args, RpyMobilitySolver, steps=None):
@@ -1108,6 +1170,8 @@ def main():
     p.add_argument("--no-batch", action="store_true", help="skip the batched-swimmers timing")
     p.add_argument("--no-serve", action="store_true", help="skip the request-stream timing")
     p.add_argument("--no-large", action="store_true", help="skip the large-swimmer timing")
+    p.add_argument("--no-prescribed", action="store_true",
+                   help="skip the prescribed-cilia solve timing")
     p.add_argument("--batch-size", type=int, default=64, help="swimmers in the batch leg")
     p.add_argument("--batch-workers", type=int, default=32, help="host workers of the batch")
     p.add_argument("--serve-bases", type=int, default=12, help="base swimmers of the stream")

@@ -4,13 +4,18 @@ reference's own solver in three prescribed-cilia configurations
 LINEAR_SYSTEM_TOL = 1e-10) and against the CPU restatement
 (oracle/prescribed.py) on a larger swimmer.
 
-Tolerances, FP64 throughout:
-  pieces (right-hand side, operator, preconditioner, KTMinvK_inv): relative
-  max-abs error <= 1e-12 (the pair sums differ from the reference's
+Tolerances:
+  pieces (right-hand side, operator, preconditioner, KTMinvK_inv), FP64:
+  relative max-abs error <= 1e-12 (the pair sums differ from the reference's
   sequential order only by rounding);
   solves: <= 1e-8 relative max-abs error (two GMRES runs stopped at a 1e-10
-  relative residual agree to about cond(A) x 1e-10), GMRES iteration counts
-  within one of the reference's.
+  relative residual agree to about cond(A) x 1e-10); FP64 GMRES iteration
+  counts within one of the reference's. FP32C (inner solves with FP32 pair
+  sums, refined on FP64 residuals): FP64 residual <= 1e-10 as the
+  reference's, solutions within 5e-6 (two solutions with residuals below
+  1e-10 ||b|| differ by at most cond(A) x 2e-10 ~ 5e-6 for these systems,
+  whose condition number is ~2.6e4 (tests/test_prescribed_oracle.py);
+  measured 2e-8 to 4e-7).
 """
 import os
 
@@ -32,11 +37,12 @@ def load(cfg):
     return dict(np.load(os.path.join(GOLD, f"prescribed_{cfg}.npz")))
 
 
-def make(d, tol=1e-10):
+def make(d, tol=1e-10, precision="fp64"):
     from timfilsimmod_gb300.prescribed import PrescribedCiliaSolver
     return PrescribedCiliaSolver(int(d["flags"]), int(d["nfil"]), int(d["nseg"]), d["blob_refs"],
                                  float(d["seg_sep"]), d["phase_refs"], d["angle_refs"],
                                  body_x=d["body_x"], body_q=d["body_q"], tol=tol,
+                                 precision=precision,
                                  gen_force_magnitude_factor=float(d["gen_force_magnitude_factor"]),
                                  torsional_spring_magnitude_factor=float(
                                      d["torsional_spring_magnitude_factor"]))
@@ -62,26 +68,33 @@ def test_pieces_match_reference(cfg):
     ps.finalise()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
 @pytest.mark.parametrize("cfg", CONFIGS)
-def test_warm_started_solves_match_reference(cfg):
+def test_warm_started_solves_match_reference(cfg, precision):
     """Three consecutive solves, each warm started from the last (the first
-    from phase rates omega0 and zero angle rates, as the golden's)."""
+    from phase rates omega0 and zero angle rates, as the golden's). FP32C:
+    the refinement drives the FP64 residual to the same tolerance, so the
+    same bar holds; its iteration count is the inner steps' sum."""
     d = load(cfg)
-    ps = make(d)
+    ps = make(d, precision=precision)
     ps.set_solution(phase_dot=d["phase_dot0"], angle_dot=d["angle_dot0"])
     flags = int(d["flags"])
     for nt in range(d["phase"].shape[0]):
         iters = ps.compute_velocities(**kin(d, nt))
-        assert abs(iters - int(d["iters"][nt])) <= 1, (nt, iters, int(d["iters"][nt]))
+        if precision == "fp64":
+            assert abs(iters - int(d["iters"][nt])) <= 1, (nt, iters, int(d["iters"][nt]))
+        else:
+            assert ps.solve_info()["rel_residual"] <= 1e-10
         sol = ps.solution()
-        assert rel(sol["f_segs"], d["f_segs"][nt]) <= 1e-8
-        assert rel(sol["f_blobs"], d["f_blobs"][nt]) <= 1e-8
+        bar = 1e-8 if precision == "fp64" else 5e-6
+        assert rel(sol["f_segs"], d["f_segs"][nt]) <= bar
+        assert rel(sol["f_blobs"], d["f_blobs"][nt]) <= bar
         if not flags & 1:
-            assert rel(sol["v_body"], d["v_body"][nt]) <= 1e-8
+            assert rel(sol["v_body"], d["v_body"][nt]) <= bar
         if flags & 2:
-            assert rel(sol["phase_dot"], d["phase_dot"][nt]) <= 1e-8
+            assert rel(sol["phase_dot"], d["phase_dot"][nt]) <= bar
         if flags & 4:
-            assert rel(sol["angle_dot"], d["angle_dot"][nt]) <= 1e-8
+            assert rel(sol["angle_dot"], d["angle_dot"][nt]) <= bar
     ps.finalise()
 
 

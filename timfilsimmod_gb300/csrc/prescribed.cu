@@ -102,6 +102,18 @@ struct PresState {
   QueueJob jobs[4];
   int n_jobs = 0;
   QueueJob *jobs_dev = nullptr;
+  // FP32C: FP32 3-force records (origin-relative positions) and their jobs
+  float *rec_s32 = nullptr, *rec_b32 = nullptr;
+  QueueJob jobs32[4];
+  QueueJob *jobs32_dev = nullptr;
+  long long fallbacks = 0;  // FP32C refinements that stalled and finished in FP64
+  // FP32C residuals in float-float arithmetic (rpy_ff.cu) when every
+  // particle has the same radius and no block is the weakly coupled one: the
+  // translational mobility of all particles is then one equal-radius
+  // product over the concatenated positions (segments, then blobs)
+  bool use_ff = false;
+  double *x_all = nullptr, *v_all = nullptr;  // 3 (Ns + Nb)
+  void *rec_ff = nullptr;
 };
 
 namespace {
@@ -447,6 +459,35 @@ __global__ void pres_pack_kernel(PA a, const double *z, const double *x_blobs, d
   }
 }
 
+// FP32 3-force records {x - o, y - o, z - o, f0, f1, f2, 0, 0}: the
+// positions relative to the solver's origin, as the FP32 work-queue kernel
+// reads them.
+__global__ void pres_pack32_kernel(PA a, const double *z, const double *x_blobs,
+                                   const double *origin, float *rec_s, float *rec_b) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const double *x;
+  float *r;
+  const double *f;
+  if (p < a.ns) {
+    x = a.x_segs + 3 * (size_t)p;
+    f = z + 3 * (size_t)p;
+    r = rec_s + 8 * (size_t)p;
+  } else if (p < a.ns + a.nb) {
+    const int j = p - a.ns;
+    x = x_blobs + 3 * (size_t)j;
+    f = z + 3 * ((size_t)a.ns + j);
+    r = rec_b + 8 * (size_t)j;
+  } else {
+    return;
+  }
+  for (int c = 0; c < 3; ++c) {
+    r[c] = float(x[c] - origin[c]);
+    r[3 + c] = float(f[c]);
+  }
+  r[6] = 0.f;
+  r[7] = 0.f;
+}
+
 // out = A z from the products: segments v_ss (or the 6-stride v6 of the
 // weakly coupled product) + v_sb, blobs v_bb + v_bs, minus K [U; Omega;
 // phase rates; angle rates]; phase and angle rows -K^T; body rows -K^T (the
@@ -476,7 +517,7 @@ __global__ void __launch_bounds__(kPT) pres_combine_kernel(PA a, const double *z
         if (a.free_body) o[c] -= U[c];
         if (a.phase) o[c] -= pd * a.kphi[3 * (size_t)i + c];
         if (a.angle) o[c] -= ad * a.kth[3 * (size_t)i + c];
-        o[c] += vs + v_sb[3 * (size_t)i + c];
+        o[c] += vs + (v_sb != nullptr ? v_sb[3 * (size_t)i + c] : 0.0);
         if (a.phase) dp += a.kphi[3 * (size_t)i + c] * f[c];
         if (a.angle) da += a.kth[3 * (size_t)i + c] * f[c];
       }
@@ -521,7 +562,7 @@ __global__ void __launch_bounds__(kPT) pres_combine_kernel(PA a, const double *z
       }
       for (int c = 0; c < 3; ++c) {
         const size_t row = 3 * ((size_t)a.ns + j) + c;
-        o[c] += v_bb[3 * (size_t)j + c] + v_bs[3 * (size_t)j + c];
+        o[c] += v_bb[3 * (size_t)j + c] + (v_bs != nullptr ? v_bs[3 * (size_t)j + c] : 0.0);
         out[row] = resid != nullptr ? resid[row] - o[c] : o[c];
       }
     }
@@ -945,6 +986,12 @@ void pres_free(tfs_solver *s) {
   cudaFree(p->st);
   cudaFree(p->qcnt);
   cudaFree(p->jobs_dev);
+  cudaFree(p->rec_s32);
+  cudaFree(p->rec_b32);
+  cudaFree(p->x_all);
+  cudaFree(p->v_all);
+  cudaFree(p->rec_ff);
+  cudaFree(p->jobs32_dev);
   if (p->st_host) cudaFreeHost(p->st_host);
   delete p;
   s->pres = nullptr;
@@ -987,7 +1034,7 @@ PA pres_pa(tfs_solver *s) {
 
 int pa_ctas(const PA &a) { return std::max(1, (a.fil_warps + a.blob_warps + kPW - 1) / kPW); }
 
-GA pres_ga(tfs_solver *s) {
+GA pres_ga(tfs_solver *s, double tol) {
   PresState *p = s->pres;
   GA g{};
   g.n = p->n;
@@ -996,7 +1043,7 @@ GA pres_ga(tfs_solver *s) {
   g.ld = kPresMaxIter + 1;
   g.pstride = p->pstride;
   g.max_iter = p->max_iter;
-  g.tol = s->tol;
+  g.tol = tol;
   g.Q = p->Q;
   g.H = p->H;
   g.beta = p->beta;
@@ -1102,6 +1149,27 @@ int pres_alloc(tfs_solver *s) {
   });
   TFS_CUDA(cudaMemcpy(p->jobs_dev, p->jobs, sizeof(QueueJob) * p->n_jobs, cudaMemcpyHostToDevice),
            "copy queue jobs");
+  // the same jobs on FP32 records (FP32C inner solves): same partials and
+  // arrival counters (launches never overlap), float2 partial sums
+  if ((rc = alloc_dev((void **)&p->rec_s32, sizeof(float) * 8 * std::max<size_t>(1, ns))) != TFS_OK ||
+      (rc = alloc_dev((void **)&p->rec_b32, sizeof(float) * 8 * std::max<size_t>(1, nb))) != TFS_OK ||
+      (rc = alloc_dev((void **)&p->jobs32_dev, sizeof(QueueJob) * 4)) != TFS_OK)
+    return rc;
+  for (int j = 0; j < p->n_jobs; ++j) {
+    QueueJob q = p->jobs[j];
+    q.tgt_rec = q.tgt_rec == p->rec_s ? (const void *)p->rec_s32 : (const void *)p->rec_b32;
+    q.src_a = q.src_a == p->rec_s ? (const void *)p->rec_s32 : (const void *)p->rec_b32;
+    p->jobs32[j] = q;
+  }
+  TFS_CUDA(cudaMemcpy(p->jobs32_dev, p->jobs32, sizeof(QueueJob) * p->n_jobs,
+                      cudaMemcpyHostToDevice),
+           "copy queue jobs");
+  p->use_ff = !p->weak && s->cfg.a_seg == s->cfg.a_blob && ns + nb > 0;
+  if (p->use_ff &&
+      ((rc = alloc_dev((void **)&p->x_all, sizeof(double) * 3 * (ns + nb))) != TFS_OK ||
+       (rc = alloc_dev((void **)&p->v_all, sizeof(double) * 3 * (ns + nb))) != TFS_OK ||
+       (rc = alloc_dev(&p->rec_ff, ff_record_bytes() * (ns + nb))) != TFS_OK))
+    return rc;
   // outputs of absent blocks stay zero
   for (double *v : {p->v_ss, p->v_sb})
     TFS_CUDA(cudaMemset(v, 0, sizeof(double) * std::max<size_t>(1, 3 * ns)), "cudaMemset");
@@ -1110,15 +1178,26 @@ int pres_alloc(tfs_solver *s) {
   return TFS_OK;
 }
 
-// out = A z (resid == nullptr) or resid - A z.
-int pres_operator(tfs_solver *s, const double *z, const double *resid, double *out) {
+// out = A z (resid == nullptr) or resid - A z; fp32: the pair sums of the
+// work-queue kernel in FP32 with compensated accumulation.
+int pres_operator(tfs_solver *s, int fp32, const double *z, const double *resid, double *out) {
   PresState *p = s->pres;
   const PA a = pres_pa(s);
   const int np = p->ns + p->nb;
   if (np > 0) {
-    pres_pack_kernel<<<(np + 255) / 256, 256, 0, s->stream>>>(a, z, s->x_blobs, p->rec_s, p->rec_b,
-                                                              p->weak ? p->f6 : nullptr);
-    count_launch();
+    if (fp32) {
+      int rc;
+      if ((rc = ensure_origin(s)) != TFS_OK) return rc;
+      pres_pack32_kernel<<<(np + 255) / 256, 256, 0, s->stream>>>(a, z, s->x_blobs, s->origin,
+                                                                  p->rec_s32, p->rec_b32);
+      if (p->weak)  // the weakly coupled segment block stays FP64
+        pres_pack_kernel<<<(np + 255) / 256, 256, 0, s->stream>>>(a, z, s->x_blobs, p->rec_s,
+                                                                  p->rec_b, p->f6);
+    } else {
+      pres_pack_kernel<<<(np + 255) / 256, 256, 0, s->stream>>>(a, z, s->x_blobs, p->rec_s,
+                                                                p->rec_b, p->weak ? p->f6 : nullptr);
+    }
+    count_launch_n(fp32 && p->weak ? 2 : 1);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "prescribed pack kernel");
@@ -1133,8 +1212,10 @@ int pres_operator(tfs_solver *s, const double *z, const double *resid, double *o
     if (e != cudaSuccess) return cuda_fail(e, "weakly coupled segment product");
   }
   if (p->n_jobs > 0) {
-    e = launch_queue(0, s->qtune[0][QK_MBB], Q_BLOB, p->jobs_dev, p->jobs, p->n_jobs, p->qcnt,
-                     s->stream);
+    e = fp32 ? launch_queue(1, s->qtune[1][QK_MBB], Q_BLOB, p->jobs32_dev, p->jobs32, p->n_jobs,
+                            p->qcnt, s->stream)
+             : launch_queue(0, s->qtune[0][QK_MBB], Q_BLOB, p->jobs_dev, p->jobs, p->n_jobs,
+                            p->qcnt, s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "RPY work-queue kernel (prescribed)");
   }
   pres_combine_kernel<<<pa_ctas(a), kPT, 0, s->stream>>>(a, z, p->v_ss, p->v6, p->v_sb, p->v_bb,
@@ -1194,60 +1275,175 @@ int upload(tfs_solver *s, double *dst, const double *src, size_t n, const char *
   return TFS_OK;
 }
 
+// Host read of the device scalars (synchronises the stream).
+int pres_read_scalars(tfs_solver *s, const char *what) {
+  PresState *p = s->pres;
+  TFS_CUDA(cudaMemcpyAsync(p->st_host, p->st, sizeof(PresScalars), cudaMemcpyDeviceToHost,
+                           s->stream),
+           "read solve scalars");
+  TFS_CUDA(cudaStreamSynchronize(s->stream), what);
+  return TFS_OK;
+}
+
+// Arnoldi steps from the normalised Q_0 (beta[0] and st->norm_rhs set) until
+// |beta_k| <= tol st->norm_rhs or the cap, then x += P^-1 (Q y). fp32: FP32
+// pair sums in the operator. Returns the steps in *iters.
+int pres_arnoldi(tfs_solver *s, int fp32, double tol, int *iters) {
+  PresState *p = s->pres;
+  const GA g = pres_ga(s, tol);
+  int rc;
+  *iters = 0;
+  for (int k = 1; k <= p->max_iter; ++k) {
+    double *qprev = p->Q + (size_t)(k - 1) * p->n, *w = p->Q + (size_t)k * p->n;
+    if ((rc = pres_precond(s, qprev, p->z)) != TFS_OK) return rc;
+    if ((rc = pres_operator(s, fp32, p->z, nullptr, w)) != TFS_OK) return rc;
+    pres_dots1_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
+    pres_dots2_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
+    pres_norm_givens_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
+    pres_scale_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
+    count_launch_n(4);
+    TFS_CUDA(cudaGetLastError(), "prescribed Arnoldi step");
+    if ((rc = pres_read_scalars(s, "prescribed Arnoldi step")) != TFS_OK) return rc;
+    if (p->st_host->status != 0) return fail(TFS_ENAN, "non-finite GMRES residual");
+    if (p->st_host->done) {
+      *iters = k;
+      break;
+    }
+  }
+  pres_qy_kernel<<<g.G, kPT, 0, s->stream>>>(g, *iters, p->tmp);
+  count_launch();
+  if ((rc = pres_precond(s, p->tmp, p->z)) != TFS_OK) return rc;
+  pres_axpy_kernel<<<g.G, kPT, 0, s->stream>>>(p->x, p->z, p->n);
+  count_launch();
+  TFS_CUDA(cudaGetLastError(), "prescribed GMRES finish");
+  return TFS_OK;
+}
+
+// out = resid - A z with the pair sums in float-float arithmetic (use_ff):
+// v = M z over the concatenated particles, then the couplings.
+int pres_operator_ff(tfs_solver *s, const double *z, const double *resid, double *out) {
+  PresState *p = s->pres;
+  int rc;
+  if ((rc = ensure_origin(s)) != TFS_OK) return rc;
+  const int np = p->ns + p->nb;
+  TFS_CUDA(cudaMemcpyAsync(p->x_all, s->x_segs, sizeof(double) * 3 * p->ns,
+                           cudaMemcpyDeviceToDevice, s->stream),
+           "gather positions");
+  TFS_CUDA(cudaMemcpyAsync(p->x_all + 3 * (size_t)p->ns, s->x_blobs, sizeof(double) * 3 * p->nb,
+                           cudaMemcpyDeviceToDevice, s->stream),
+           "gather positions");
+  const size_t scratch = (size_t)kMaxSplits * 3 * (2 * (size_t)p->ns + 2 * (size_t)p->nb);
+  cudaError_t e = launch_bb_ff(p->x_all, z, np, s->origin, s->cfg.a_seg,
+                               1.0 / (8.0 * kPiP * s->cfg.mu), p->rec_ff, p->v_all, p->qpart,
+                               scratch, s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "float-float product (prescribed)");
+  const PA a = pres_pa(s);
+  pres_combine_kernel<<<pa_ctas(a), kPT, 0, s->stream>>>(a, z, p->v_all, nullptr, nullptr,
+                                                         p->v_all + 3 * (size_t)p->ns, nullptr,
+                                                         resid, out);
+  count_launch();
+  TFS_CUDA(cudaGetLastError(), "prescribed combine kernel");
+  return TFS_OK;
+}
+
+// Q_0 = b - A x (FP64, or float-float pair sums under FP32C when every
+// particle has the same radius) and its norm into st->beta0 (returned).
+int pres_residual(tfs_solver *s, double *norm) {
+  PresState *p = s->pres;
+  const GA g = pres_ga(s, s->tol);
+  int rc;
+  const bool ff = p->use_ff && s->cfg.precision == TFS_FP32C;
+  if ((rc = ff ? pres_operator_ff(s, p->x, p->b, p->Q) : pres_operator(s, 0, p->x, p->b, p->Q)) !=
+      TFS_OK)
+    return rc;
+  pres_norm_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->Q, &p->st->beta0);
+  count_launch();
+  TFS_CUDA(cudaGetLastError(), "prescribed residual");
+  if ((rc = pres_read_scalars(s, "prescribed residual")) != TFS_OK) return rc;
+  *norm = p->st_host->beta0;
+  return TFS_OK;
+}
+
+// Start an inner solve on Q_0 = r (unnormalised, ||r|| = nr): Q_0 /= nr,
+// beta[0] = nr, and the stopping test relative to nr.
+__global__ void pres_inner_start_kernel(GA g, double nr) {
+  PresScalars *st = g.st;
+  st->norm_rhs = nr;
+  st->flag = 0;
+  st->done = 0;
+  st->status = 0;
+  g.beta[0] = nr;
+}
+
 int pres_solve(tfs_solver *s, int *iters_out) {
   PresState *p = s->pres;
   if (!p->have_kin) return fail(TFS_ESTATE, "set the kinematics first");
-  const GA g = pres_ga(s);
+  const bool fp32 = s->cfg.precision == TFS_FP32C;
+  const GA g = pres_ga(s, s->tol);
   int rc;
   if ((rc = pres_rhs(s)) != TFS_OK) return rc;
-  // ||rhs||; r0 = rhs - A x0 into Q_0; beta0 = ||r0||; the warm-start tests
+  // ||rhs||; r0 = rhs - A x0 into Q_0 (FP64); beta0 = ||r0||; the warm-start
+  // tests (mobility_solver.cpp:2121-2320)
   pres_norm_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->b, &p->st->norm_rhs);
   count_launch();
-  if ((rc = pres_operator(s, p->x, p->b, p->Q)) != TFS_OK) return rc;
+  rc = fp32 && p->use_ff ? pres_operator_ff(s, p->x, p->b, p->Q)
+                         : pres_operator(s, 0, p->x, p->b, p->Q);
+  if (rc != TFS_OK) return rc;
   pres_norm_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->Q, &p->st->beta0);
   pres_start_kernel<<<1, 1, 0, s->stream>>>(g);
   pres_q0_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->b, p->x);
   count_launch_n(3);
   TFS_CUDA(cudaGetLastError(), "prescribed GMRES start");
-  TFS_CUDA(cudaMemcpyAsync(p->st_host, p->st, sizeof(PresScalars), cudaMemcpyDeviceToHost, s->stream),
-           "read solve scalars");
-  TFS_CUDA(cudaStreamSynchronize(s->stream), "prescribed GMRES start");
+  if ((rc = pres_read_scalars(s, "prescribed GMRES start")) != TFS_OK) return rc;
   if (p->st_host->status == 1) return fail(TFS_ENAN, "non-finite residual at the start");
-  int iters = 0;
+  const double nb = p->st_host->norm_rhs;
+  int iters = 0, cycles = 0;
+  double rel = nb > 0.0 ? p->st_host->beta0 / nb : 0.0;
   if (!p->st_host->done) {
-    for (int k = 1; k <= p->max_iter; ++k) {
-      double *qprev = p->Q + (size_t)(k - 1) * p->n, *w = p->Q + (size_t)k * p->n;
-      if ((rc = pres_precond(s, qprev, p->z)) != TFS_OK) return rc;
-      if ((rc = pres_operator(s, p->z, nullptr, w)) != TFS_OK) return rc;
-      pres_dots1_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
-      pres_dots2_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
-      pres_norm_givens_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
-      pres_scale_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
-      count_launch_n(4);
-      TFS_CUDA(cudaGetLastError(), "prescribed Arnoldi step");
-      TFS_CUDA(cudaMemcpyAsync(p->st_host, p->st, sizeof(PresScalars), cudaMemcpyDeviceToHost,
-                               s->stream),
-               "read solve scalars");
-      TFS_CUDA(cudaStreamSynchronize(s->stream), "prescribed Arnoldi step");
-      if (p->st_host->status != 0) return fail(TFS_ENAN, "non-finite GMRES residual");
-      if (p->st_host->done) {
-        iters = k;
-        break;
+    if (!fp32) {
+      if ((rc = pres_arnoldi(s, 0, s->tol, &iters)) != TFS_OK) return rc;
+      rel = p->st_host->rel;
+      cycles = 1;
+    } else {
+      // iterative refinement: inner GMRES with FP32 pair sums on the FP64
+      // residual r, each to max(inner_tol, tol ||b|| / (2 ||r||)), until
+      // ||b - A x|| <= tol ||b|| in FP64; a cycle that does not reduce the
+      // residual hands over to FP64 GMRES from the current x
+      double cur = p->st_host->flag == 2 ? nb : p->st_host->beta0;
+      bool fp64_finish = false;
+      pres_inner_start_kernel<<<1, 1, 0, s->stream>>>(g, cur);  // Q_0 is normalised already
+      count_launch();
+      for (;;) {
+        const double tin = std::max(s->inner_tol, 0.5 * s->tol * nb / cur);
+        int it = 0;
+        if ((rc = pres_arnoldi(s, fp64_finish ? 0 : 1, fp64_finish ? s->tol * nb / cur : tin,
+                               &it)) != TFS_OK)
+          return rc;
+        iters += it;
+        ++cycles;
+        double nr;
+        if ((rc = pres_residual(s, &nr)) != TFS_OK) return rc;
+        if (!(nr == nr)) return fail(TFS_ENAN, "non-finite residual in the refinement");
+        rel = nr / nb;
+        if (rel <= s->tol || fp64_finish || cycles >= s->max_outer + 1) break;
+        if (nr >= cur) {  // stalled: finish in FP64
+          fp64_finish = true;
+          ++p->fallbacks;
+        }
+        cur = nr;
+        pres_inner_start_kernel<<<1, 1, 0, s->stream>>>(g, cur);
+        pres_q0_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->b, p->x);
+        count_launch_n(2);
+        TFS_CUDA(cudaGetLastError(), "prescribed refinement restart");
       }
     }
-    // x += P^-1 (Q y)
-    pres_qy_kernel<<<g.G, kPT, 0, s->stream>>>(g, iters, p->tmp);
-    count_launch();
-    if ((rc = pres_precond(s, p->tmp, p->z)) != TFS_OK) return rc;
-    pres_axpy_kernel<<<g.G, kPT, 0, s->stream>>>(p->x, p->z, p->n);
-    count_launch();
-    TFS_CUDA(cudaGetLastError(), "prescribed GMRES finish");
   }
   TFS_CUDA(cudaStreamSynchronize(s->stream), "prescribed solve");
   s->last_iters = iters;
-  s->last_outer = 1;
-  s->last_rel = p->st_host->rel;
+  s->last_outer = cycles;
+  s->last_rel = rel;
   if (iters_out) *iters_out = iters;
+  if (fp32 && rel > s->tol) return fail(TFS_ENOTCONV, "refinement stopped at %.3e", rel);
   return TFS_OK;
 }
 
@@ -1410,7 +1606,8 @@ int tfs_prescribed_apply(tfs_solver *s, int which, const double *in, double *out
   if (out == nullptr || (which != 2 && in == nullptr)) return fail(TFS_EINVAL, "null vector");
   if (which == 0 || which == 1) {
     if ((rc = upload(s, p->tmp, in, p->n, "copy vector")) != TFS_OK) return rc;
-    rc = which == 0 ? pres_operator(s, p->tmp, nullptr, p->z) : pres_precond(s, p->tmp, p->z);
+    rc = which == 0 ? pres_operator(s, s->cfg.precision == TFS_FP32C, p->tmp, nullptr, p->z)
+                    : pres_precond(s, p->tmp, p->z);
     if (rc != TFS_OK) return rc;
     TFS_CUDA(cudaMemcpyAsync(out, p->z, sizeof(double) * p->n, cudaMemcpyDeviceToHost, s->stream),
              "copy result");

@@ -46,7 +46,10 @@ class PrescribedCiliaSolver:
     WEAKLY_COUPLED (the weakly coupled filaments' mobility). seg_sep: DL, for
     FIL_LENGTH = DL (NSEG - 1). phase_force_refs / angle_force_refs: the
     generalised-force tables over one period (the reference's
-    data/forcing/*_reference_*_generalised_forces files).
+    data/forcing/*_reference_*_generalised_forces files). precision "fp64"
+    (the reference's FP64 build) or "fp32c": inner GMRES solves with FP32 pair
+    sums (compensated accumulation), refined on FP64 residuals to the same
+    tolerance.
     """
 
     def __init__(self, flags: int, nfil: int, nseg: int, blob_refs, seg_sep: float,
@@ -54,11 +57,11 @@ class PrescribedCiliaSolver:
                  body_q=(1.0, 0.0, 0.0, 0.0), mu: float = 1.0, a_seg: float = 1.0,
                  a_blob: float = 1.0, tol: float = 1e-4,
                  gen_force_magnitude_factor: float = 1.0,
-                 torsional_spring_magnitude_factor: float = 2.0):
+                 torsional_spring_magnitude_factor: float = 2.0, precision: str = "fp64"):
         refs = _arr(blob_refs)
         self.flags, self.nfil, self.nseg = int(flags), int(nfil), int(nseg)
         self.nblob = refs.size // 3
-        self.solver = RpyMobilitySolver(1, nfil, nseg, self.nblob, "fp64", mu=mu, a_seg=a_seg,
+        self.solver = RpyMobilitySolver(1, nfil, nseg, self.nblob, precision, mu=mu, a_seg=a_seg,
                                         a_blob=a_blob)
         self.lib = self.solver.lib
         s = self.solver
