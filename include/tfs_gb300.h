@@ -236,7 +236,11 @@ int tfs_refinement_retries(tfs_solver *s, long long *retries);
  * positions come through tfs_copy_segment_positions_to_device, the body
  * through tfs_set_blob_references and tfs_set_body_pose; the GMRES tolerance
  * through tfs_set_linear_solver (the iteration cap is the reference's
- * MAX_LINEAR_SYSTEM_ITER, min(350, unknowns)). */
+ * MAX_LINEAR_SYSTEM_ITER, min(350, unknowns)). After tfs_prescribed_setup the
+ * four block hooks (tfs_evaluate_*_mobility) take the form of the reference's
+ * kernels under PRESCRIBED_CILIA (cuda_functions.cu:362-757): 3x3 pairs on
+ * the forces only (segment torques are not read), zero rotational segment
+ * velocities, and blob <- segment adding to blob <- blob. */
 #define TFS_PRESCRIBED_BODY 1 /* PRESCRIBED_BODY_VELOCITIES: the body moves as given */
 #define TFS_DYNAMIC_PHASE 2   /* DYNAMIC_PHASE_EVOLUTION: phase rates are unknowns */
 #define TFS_DYNAMIC_ANGLE 4   /* DYNAMIC_SHAPE_ROTATION: shape-rotation rates are unknowns */

@@ -166,3 +166,39 @@ def test_flag_validation():
         from timfilsimmod_gb300.prescribed import PrescribedCiliaSolver
         PrescribedCiliaSolver(2, int(d["nfil"]), int(d["nseg"]), d["blob_refs"],
                               float(d["seg_sep"]), d["phase_refs"], d["angle_refs"])
+
+
+@pytest.mark.parametrize("cfg", ["p1", "p2"])
+def test_block_hooks_take_the_prescribed_form(cfg):
+    """After the prescribed setup the four block hooks are the reference's
+    PRESCRIBED_CILIA kernels (cuda_functions.cu:362-757): 3x3 pairs on the
+    forces only (the torque slots of f_segs, here random, are not read), zero
+    rotational segment velocities, Mbs adding to Mbb's result. Checked
+    through evaluate_full_mobility against the CPU restatement's blocks."""
+    from prescribed import PrescribedSystem
+    d = load(cfg)
+    ps = make(d)
+    ps.set_kinematics(**kin(d, 0))
+    s = ps.solver
+    nfil, nseg = int(d["nfil"]), int(d["nseg"])
+    ns, nb = nfil * nseg, d["blob_refs"].size // 3
+    rng = np.random.default_rng(9)
+    s.f_segs_host[:] = rng.normal(size=6 * ns)
+    s.f_blobs_host[:] = rng.normal(size=3 * nb)
+    s.copy_segment_forces_to_device()
+    s.copy_blob_forces_to_device()
+    s.evaluate_full_mobility()
+    S = PrescribedSystem(int(d["flags"]), nfil, nseg, d["x_segs"][0], d["blob_refs"], d["body_x"],
+                         d["body_q"], d["vel_dir_phase"][0], d["vel_dir_angle"][0])
+    o = S.orc
+    fs3 = s.f_segs_host.reshape(-1, 6)[:, :3].copy()
+    fb = s.f_blobs_host.copy()
+    vs = o.block(3, 3, S.x_segs, 1.0, S.x_segs, fs3, 1.0)
+    vs = o.block(3, 3, S.x_segs, 1.0, S.x_blobs, fb, 1.0, v=vs)
+    vb = o.block(3, 3, S.x_blobs, 1.0, S.x_blobs, fb, 1.0)
+    vb = o.block(3, 3, S.x_blobs, 1.0, S.x_segs, fs3, 1.0, v=vb)
+    v6 = s.v_segs_host.reshape(-1, 6)
+    assert rel(v6[:, :3], vs) <= 1e-12
+    assert np.all(v6[:, 3:] == 0.0)
+    assert rel(s.v_blobs_host, vb) <= 1e-12
+    ps.finalise()

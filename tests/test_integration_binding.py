@@ -1,7 +1,9 @@
 """The binding a maintainer of the reference adds (timfilsimmod_gb300/integration:
 a replacement rpy_mobility_solver.cu for the 17 hooks, the device-resident
 compute_velocities and make_body_reference_matrices of mobility_solver, and
-flow_field_evaluator::velocities) compiles against the reference's unchanged
+flow_field_evaluator::velocities; for the prescribed-cilia configuration, the
+weakly coupled solver class and the prescribed-cilia compute_velocities)
+compiles against the reference's unchanged
 headers (rpy_mobility_solver.hpp, mobility_solver.hpp, swimmer.hpp,
 flow_field_evaluator.hpp) with Real = double and with the shipped
 Real = float, and links against libtfs_gb300.so: every library symbol the
@@ -45,7 +47,8 @@ def bindings():
     res = subprocess.run(["make", "-C", INTEG, "check", f"REF={ref}"], capture_output=True,
                          text=True)
     assert res.returncode == 0, res.stdout[-3000:] + res.stderr[-3000:]
-    return {c: os.path.join(INTEG, "_build", f"binding_{c}.so") for c in ("fp64", "fp32")}
+    return {c: os.path.join(INTEG, "_build", f"binding_{c}.so")
+            for c in ("fp64", "fp32", "pres_fp64", "pres_fp32")}
 
 
 def test_binding_compiles_and_links_in_both_precisions(bindings):
@@ -66,3 +69,15 @@ def test_float_build_uses_the_float_entry_points(bindings):
     for h in hooks:
         assert h in f64 and h + "_f32" not in f64, h
         assert h + "_f32" in f32 and h not in f32, h
+
+
+def test_prescribed_binding_calls_the_prescribed_solve(bindings):
+    """The prescribed-cilia build (the shipped CILIA_TYPE 3 branches with the
+    weakly coupled mobility) binds compute_velocities to tfs_prescribed_* and
+    the weakly coupled class's segment product to its library call."""
+    for cfg in ("pres_fp64", "pres_fp32"):
+        need = symbols(bindings[cfg], defined=False)
+        for name in ("tfs_prescribed_setup", "tfs_prescribed_compute_velocities",
+                     "tfs_prescribed_solution", "tfs_evaluate_weakly_coupled_segment_mobility"):
+            assert name in need, (cfg, name)
+    assert "tfs_copy_segment_positions_to_device_f32" in symbols(bindings["pres_fp32"], False)

@@ -101,7 +101,8 @@ struct PresState {
   unsigned *qcnt = nullptr;                        // [2] launch counters, arrival counters
   QueueJob jobs[4];
   int n_jobs = 0;
-  QueueJob *jobs_dev = nullptr;
+  QueueJob *jobs_dev = nullptr;  // four slots; weakly coupled: the fourth holds hook_ss
+  QueueJob hook_ss{};            // weakly coupled: the seg <- seg job of the block hook
   // FP32C: FP32 3-force records (origin-relative positions) and their jobs
   float *rec_s32 = nullptr, *rec_b32 = nullptr;
   QueueJob jobs32[4];
@@ -750,6 +751,47 @@ __global__ void __launch_bounds__(kPT) pres_precond_b_kernel(PA a, double *out) 
 }
 
 // ---------------------------------------------------------------------------
+// The four block hooks in the prescribed-cilia form of the reference's
+// kernels (cuda_functions.cu:362-757 under PRESCRIBED_CILIA): forces only
+// (the torque slots of f_segs are not read), rpy_interaction<3,3>, zero
+// rotational segment velocities, Mbs_mult adding to Mbb_mult's result.
+// ---------------------------------------------------------------------------
+// Records of the solver's own force arrays: segments from f_segs (6 per
+// segment, the first three), blobs from f_blobs.
+__global__ void pres_hook_pack_kernel(PA a, const double *f_segs, const double *f_blobs,
+                                      const double *x_blobs, double *rec_s, double *rec_b) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < a.ns) {
+    double *r = rec_s + 6 * (size_t)p;
+    for (int c = 0; c < 3; ++c) {
+      r[c] = a.x_segs[3 * (size_t)p + c];
+      r[3 + c] = f_segs[6 * (size_t)p + c];
+    }
+  } else if (p < a.ns + a.nb) {
+    const int j = p - a.ns;
+    double *r = rec_b + 6 * (size_t)j;
+    for (int c = 0; c < 3; ++c) {
+      r[c] = x_blobs[3 * (size_t)j + c];
+      r[3 + c] = f_blobs[3 * (size_t)j + c];
+    }
+  }
+}
+
+// out (stride `stride`) = or += v (3 per target); stride 6 zeroes the
+// rotational slots on assignment.
+__global__ void pres_hook_out_kernel(const double *v, double *out, int n, int stride, int add) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int c = 0; c < 3; ++c) {
+    const double t = v[3 * (size_t)i + c];
+    double *o = out + (size_t)stride * i + c;
+    *o = add ? *o + t : t;
+  }
+  if (stride == 6 && !add)
+    for (int c = 3; c < 6; ++c) out[6 * (size_t)i + c] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
 // GMRES over flat vectors of n rows: G CTAs, `rows` consecutive rows each
 // ---------------------------------------------------------------------------
 struct GA {
@@ -821,17 +863,38 @@ __global__ void pres_q0_kernel(GA g, const double *rhs, double *x) {
   }
 }
 
-// Dots <w, Q_i>, i < k, over this CTA's rows (warps take i mod 4), into
-// part[cta][i]; the last CTA sums them in CTA order into h.
+// Dots <w, Q_i>, i < k, over this CTA's rows into part[cta][i]: columns in
+// blocks of 8, every thread accumulating its rows' products for the 8 at once
+// (coalesced row loads, eight in flight per row), block sums per column; the
+// last CTA sums the partials in CTA order into h.
 __device__ void pres_dots(const GA &g, const double *w, int k, double *h) {
+  __shared__ double red[kPW][8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int r0 = blockIdx.x * g.rows, r1 = min(g.n, r0 + g.rows);
-  for (int i = wid; i < k; i += kPW) {
-    const double *qi = g.Q + (size_t)i * g.n;
-    double t = 0.0;
-    for (int r = r0 + lane; r < r1; r += 32) t += w[r] * qi[r];
-    t = pw_sum(t);
-    if (lane == 0) g.part[(size_t)blockIdx.x * g.pstride + i] = t;
+  for (int i0 = 0; i0 < k; i0 += 8) {
+    const int nc = min(8, k - i0);
+    double acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = 0.0;
+    for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+      const double wr = w[r];
+      const double *q = g.Q + (size_t)i0 * g.n + r;
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (j < nc) acc[j] += q[(size_t)j * g.n] * wr;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = pw_sum(acc[j]);
+    if (lane == 0)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) red[wid][j] = acc[j];
+    __syncthreads();
+    if ((int)threadIdx.x < nc) {
+      double t = 0.0;
+      for (int q = 0; q < kPW; ++q) t += red[q][threadIdx.x];
+      g.part[(size_t)blockIdx.x * g.pstride + i0 + threadIdx.x] = t;
+    }
+    __syncthreads();
   }
   if (!pres_last_cta(g.cnt)) return;
   for (int i = wid; i < k; i += kPW) {
@@ -842,12 +905,27 @@ __device__ void pres_dots(const GA &g, const double *w, int k, double *h) {
   if (threadIdx.x == 0) *g.cnt = 0u;
 }
 
-// w -= sum_i h_i Q_i over this CTA's rows.
+// w -= sum_i h_i Q_i over this CTA's rows (h staged in shared memory; the
+// columns of a row subtracted in order, four loads in flight).
 __device__ void pres_orth(const GA &g, double *w, int k, const double *h) {
+  __shared__ double hs[kPresMaxIter];
+  for (int i = threadIdx.x; i < k; i += blockDim.x) hs[i] = h[i];
+  __syncthreads();
   const int r0 = blockIdx.x * g.rows, r1 = min(g.n, r0 + g.rows);
+  const size_t n = g.n;
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     double t = w[r];
-    for (int i = 0; i < k; ++i) t -= h[i] * g.Q[(size_t)i * g.n + r];
+    const double *q = g.Q + r;
+    int i = 0;
+    for (; i + 4 <= k; i += 4) {
+      const double a0 = q[(size_t)i * n], a1 = q[(size_t)(i + 1) * n];
+      const double a2 = q[(size_t)(i + 2) * n], a3 = q[(size_t)(i + 3) * n];
+      t -= hs[i] * a0;
+      t -= hs[i + 1] * a1;
+      t -= hs[i + 2] * a2;
+      t -= hs[i + 3] * a3;
+    }
+    for (; i < k; ++i) t -= hs[i] * q[(size_t)i * n];
     w[r] = t;
   }
   __syncthreads();
@@ -1089,7 +1167,9 @@ int pres_alloc(tfs_solver *s) {
   PresState *p = s->pres;
   const size_t n = p->n, ns = p->ns, nb = p->nb, nf = p->nfil;
   const int ld = kPresMaxIter + 1;
-  p->G = (int)std::max<size_t>(1, std::min<size_t>((size_t)num_sms(), (n + 511) / 512));
+  // GMRES vector kernels: CTAs of 256 consecutive rows (two per thread), at
+  // most eight per SM
+  p->G = (int)std::max<size_t>(1, std::min<size_t>((size_t)8 * num_sms(), (n + 255) / 256));
   p->rows = (int)((n + p->G - 1) / p->G);
   p->pstride = kPresMaxIter + 2;
   const size_t warps = nf + (nb + 31) / 32;
@@ -1149,6 +1229,11 @@ int pres_alloc(tfs_solver *s) {
   });
   TFS_CUDA(cudaMemcpy(p->jobs_dev, p->jobs, sizeof(QueueJob) * p->n_jobs, cudaMemcpyHostToDevice),
            "copy queue jobs");
+  if (p->weak && ns > 0) {  // partials and counters of the absent seg <- seg job
+    p->hook_ss = pres_job(s, p->rec_s, (int)ns, as, p->rec_s, (int)ns, as, p->v_ss, part, blk);
+    TFS_CUDA(cudaMemcpy(p->jobs_dev + 3, &p->hook_ss, sizeof(QueueJob), cudaMemcpyHostToDevice),
+             "copy queue jobs");
+  }
   // the same jobs on FP32 records (FP32C inner solves): same partials and
   // arrival counters (launches never overlap), float2 partial sums
   if ((rc = alloc_dev((void **)&p->rec_s32, sizeof(float) * 8 * std::max<size_t>(1, ns))) != TFS_OK ||
@@ -1448,6 +1533,50 @@ int pres_solve(tfs_solver *s, int *iters_out) {
 }
 
 }  // namespace
+
+// One block hook in the prescribed-cilia form: tgt_segs / src_segs pick the
+// block (seg <- seg assigns, seg <- blob adds, blob <- blob assigns, blob <-
+// seg adds).
+int pres_hook(tfs_solver *s, bool tgt_segs, bool src_segs) {
+  PresState *p = s->pres;
+  const int n_tgt = tgt_segs ? p->ns : p->nb;
+  const bool add = tgt_segs != src_segs;
+  if (n_tgt == 0) return TFS_OK;
+  double *out = tgt_segs ? s->v_segs : s->v_blobs;
+  const int stride = tgt_segs ? 6 : 3;
+  if ((src_segs ? p->ns : p->nb) == 0) {  // no sources: assign zero, or leave the sum alone
+    if (!add)
+      TFS_CUDA(cudaMemsetAsync(out, 0, sizeof(double) * stride * n_tgt, s->stream), "cudaMemsetAsync");
+    return TFS_OK;
+  }
+  const PA a = pres_pa(s);
+  const int np = p->ns + p->nb;
+  pres_hook_pack_kernel<<<(np + 255) / 256, 256, 0, s->stream>>>(a, s->f_segs, s->f_blobs,
+                                                                  s->x_blobs, p->rec_s, p->rec_b);
+  count_launch();
+  const void *tgt = tgt_segs ? (const void *)p->rec_s : (const void *)p->rec_b;
+  const void *src = src_segs ? (const void *)p->rec_s : (const void *)p->rec_b;
+  int j = -1;
+  for (int q = 0; q < p->n_jobs; ++q)
+    if (p->jobs[q].tgt_rec == tgt && p->jobs[q].src_a == src) j = q;
+  double *v = nullptr;
+  if (j >= 0) {
+    cudaError_t e = launch_queue(0, s->qtune[0][QK_MBB], Q_BLOB, p->jobs_dev + j, &p->jobs[j], 1,
+                                 p->qcnt, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "RPY work-queue kernel (prescribed hook)");
+    v = p->jobs[j].out;
+  } else {  // weakly coupled: the solve has no seg <- seg job; the hook's own
+    cudaError_t e = launch_queue(0, s->qtune[0][QK_MBB], Q_BLOB, p->jobs_dev + 3, &p->hook_ss, 1,
+                                 p->qcnt, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "RPY work-queue kernel (prescribed hook)");
+    v = p->v_ss;
+  }
+  pres_hook_out_kernel<<<(n_tgt + 255) / 256, 256, 0, s->stream>>>(v, out, n_tgt, stride, add);
+  count_launch();
+  TFS_CUDA(cudaGetLastError(), "prescribed hook");
+  return TFS_OK;
+}
+
 }  // namespace tfs
 
 using namespace tfs;

@@ -597,14 +597,17 @@ int tfs_wait_for_device(tfs_solver *s) {
 
 int tfs_evaluate_segment_segment_mobility(tfs_solver *s) {
   TFS_CHECK_SOLVER(s);
+  if (s->pres != nullptr) return pres_hook(s, true, true);
   return product(s, true, true, false, OUT_ASSIGN);
 }
 int tfs_evaluate_segment_blob_mobility(tfs_solver *s) {
   TFS_CHECK_SOLVER(s);
+  if (s->pres != nullptr) return pres_hook(s, true, false);
   return product(s, true, false, true, OUT_ACCUMULATE);
 }
 int tfs_evaluate_blob_blob_mobility(tfs_solver *s) {
   TFS_CHECK_SOLVER(s);
+  if (s->pres != nullptr) return pres_hook(s, false, false);
   return product(s, false, false, true, OUT_ASSIGN);
 }
 int tfs_evaluate_weakly_coupled_segment_mobility(tfs_solver *s) {
@@ -636,6 +639,7 @@ int tfs_evaluate_blob_blob_mobility_ff(tfs_solver *s) {
 }
 int tfs_evaluate_blob_segment_mobility(tfs_solver *s) {
   TFS_CHECK_SOLVER(s);
+  if (s->pres != nullptr) return pres_hook(s, false, true);
   return product(s, false, true, false, OUT_ASSIGN);
 }
 

@@ -185,4 +185,8 @@ int solver_new_step(tfs_solver *s);
 void solver_reset_history(tfs_solver *s);
 // Free the prescribed-cilia solve's buffers (prescribed.cu).
 void pres_free(tfs_solver *s);
+// A block hook in the reference's PRESCRIBED_CILIA form (after
+// tfs_prescribed_setup): forces only, 3x3 pairs, zero rotational segment
+// velocities, blob <- seg adding (prescribed.cu).
+int pres_hook(tfs_solver *s, bool tgt_segs, bool src_segs);
 }  // namespace tfs

@@ -41,7 +41,11 @@ void rpy_mobility_solver::allocate_device_memory() {
   cfg.a_seg = RSEG;
   cfg.a_blob = RBLOB;
   cfg.end_force_magnitude = (int)END_FORCE_MAGNITUDE;  // the device's int copy (sync_var)
+#if PRESCRIBED_CILIA  // prescribed filaments have no barrier forces (cuda_functions.cu:1242)
+  cfg.repulsive_force_factor = 0.0;
+#else
   cfg.repulsive_force_factor = REPULSIVE_FORCE_FACTOR;
+#endif
   cfg.free_body = PRESCRIBED_BODY_VELOCITIES ? 0 : 1;
   cfg.precision = TFS_FP64;  // TFS_FP32C: FP32 pair sums, FP64-refined solves
   tfs_check(tfs_solver_create(&cfg, &g_tfs_solver));

@@ -73,6 +73,39 @@ def run_steps(sw, args):
     s.finalise()
 
 
+def run_prescribed(args):
+    """Prescribed-cilia solves (tfs_prescribed_*) of 640 beating filaments x
+    20 segments on the 2562-blob sphere (dynamic phase and shape rotation,
+    zero prescribed body velocities, RPY mobility, linear residual 1e-8):
+    one warm-up solve, then --reps warm-started solves."""
+    import numpy as np
+
+    from .geometry import prescribed_swimmer
+    from .prescribed import PrescribedCiliaSolver
+
+    g = prescribed_swimmer(640, 20, radius=60.0, subdivisions=4, seg_sep=2.6)
+    rng = np.random.default_rng(5)
+    phase0 = rng.uniform(0.0, 2.0 * np.pi, g.nfil)
+    omega0 = 2.0 * np.pi * (1.0 + 0.05 * rng.uniform(-1.0, 1.0, g.nfil))
+    angle0 = rng.uniform(-0.1, 0.1, g.nfil)
+    t = 2.0 * np.pi * np.arange(100) / 100
+    ps = PrescribedCiliaSolver(7, g.nfil, g.nseg, g.blob_references, g.seg_sep,
+                               1.0 + 0.5 * np.sin(t), 0.2 * np.cos(t), tol=1e-8,
+                               precision=args.precision)
+    ps.set_solution(phase_dot=omega0)
+    dts = []
+    for nt in range(args.reps + 1):
+        ph = phase0 + omega0 * 1e-2 * nt
+        x, vp, va = g.kinematics(ph, angle0)
+        t0 = time.perf_counter()
+        it = ps.compute_velocities(x, vp, va, ph, omega0, angle0, omega0)
+        dts.append(time.perf_counter() - t0)
+        info = ps.solve_info()
+        print(f"solve {nt}: {it} GMRES steps, {info['cycles']} cycles, residual "
+              f"{info['rel_residual']:.2e}, {dts[-1] * 1e3:.1f} ms")
+    ps.finalise()
+
+
 def print_pg_trace():
     """Median duration (us) of each phase of an Arnoldi step of the last
     cooperative GMRES solve, as CTA 0 (which also runs the Givens step) and
@@ -98,7 +131,8 @@ def main():
     p.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"])
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--dt", type=float, default=1e-3, help="time step (op step)")
-    p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier", "solve", "flow", "step"])
+    p.add_argument("--op", default="grand", choices=["grand", "mss", "mbb", "barrier", "solve", "flow", "step",
+                            "prescribed"])
     p.add_argument("--flow-grid", type=int, default=64, help="flow points per axis (op flow)")
     p.add_argument("--variant", type=int, default=None,
                    help="pin every combination to this tile-kernel variant")
@@ -111,6 +145,9 @@ def main():
                         "step; needs a library built with -DTFS_PG_TRACE)")
     args = p.parse_args()
     sw = make_config(args.config, seed=1)
+    if args.op == "prescribed":
+        run_prescribed(args)
+        return
     if args.op == "flow":
         return run_flow(sw, args)
     if args.op == "step":
