@@ -454,7 +454,37 @@ def prescribed_bench(args, timed=4):
         leg["speedup_fp32c_vs_fp64"] = leg["fp64"]["ms_per_solve"] / leg["fp32c"]["ms_per_solve"]
         leg["fp32c_rel_dev_vs_fp64"] = dev
         out[name] = leg
+    if not args.no_cpu:
+        out["cpu_baseline"] = prescribed_cpu_baseline(
+            g, phase0, omega0, angle0, out["prescribed_body"]["fp64"]["gmres_iters_mean"])
     return out
+
+
+def prescribed_cpu_baseline(g, phase, omega0, angle, gmres_steps):
+    """The prescribed-cilia solve's cost on the host cores: one application
+    of the operator by the CPU restatement of the reference's solve
+    (oracle/prescribed.py, pair sums in the C oracle on all threads), after one
+    warm-up, times (the FP64 solve's GMRES steps + 1): one operator
+    application per Arnoldi step and one for the start's residual."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from prescribed import PrescribedSystem
+
+    x, vp, va = g.kinematics(phase, angle)
+    S = PrescribedSystem(7, g.nfil, g.nseg, x, g.blob_references, (0.0, 0.0, 0.0),
+                         (1.0, 0.0, 0.0, 0.0), vp, va)
+    threads = os.cpu_count() or 1
+    S.orc.set_threads(threads)
+    v = np.random.default_rng(0).normal(size=S.n)
+    S.apply_a(v)  # warm-up
+    t0 = time.perf_counter()
+    S.apply_a(v)
+    op = time.perf_counter() - t0
+    ms = op * (gmres_steps + 1) * 1e3
+    return {"value": 1e3 / ms, "unit": "solves/s", "ms_per_solve": ms, "cores": threads,
+            "kind": "port",
+            "sample": (f"one operator application of the CPU restatement ({op:.2f} s, "
+                       f"{S.n} unknowns) x (the FP64 solve's {gmres_steps:.1f} GMRES steps + 1 "
+                       "residual), extrapolated")}
 
 
 def solve_bench(sw, stream, args, RpyMobilitySolver, steps=None):
