@@ -27,8 +27,11 @@
 // Gram-Schmidt applied twice (two reductions per step; the reference uses
 // modified Gram-Schmidt, equal in exact arithmetic), with the reference's
 // Givens sign convention and stopping test; its vectors and Hessenberg
-// matrix live on the device and the host polls one flag per step. FP64, as
-// the reference's FIL_USE_DOUBLE_PRECISION build.
+// matrix live on the device. The step kernels read the step index from the
+// device scalars and skip once the solve is finished, so the Arnoldi steps
+// run in chunks replayed as a CUDA graph, the host polling one flag per
+// chunk. FP64, as the reference's FIL_USE_DOUBLE_PRECISION build, or FP32C
+// (inner solves on FP32 pair sums refined on float-float or FP64 residuals).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -49,6 +52,7 @@ constexpr int kPT = 128;         // threads per CTA of the O(N) kernels
 constexpr int kPW = kPT / 32;    // warps per CTA
 constexpr int kFilC = 16;        // per-filament constants (below)
 constexpr int kPresMaxIter = 350;  // MAX_LINEAR_SYSTEM_ITER (config.hpp:312)
+constexpr int kPresChunk = 4;      // Arnoldi steps launched between polls of the done flag
 
 // Per filament m (swimmer.cpp:1255-1287, mobility_solver.cpp:1060-1100):
 // [0] c11 = K_phi.K_phi, [1] c22 = K_th.K_th, [2] c12 = K_phi.K_th,
@@ -58,6 +62,8 @@ enum { FC11 = 0, FC22 = 1, FC12 = 2, FVPHI = 3, FVTH = 6, FUPHI = 9, FUTH = 12 }
 
 struct PresScalars {
   double norm_rhs, beta0, qnorm, rel;
+  double tol;  // stopping test of the running GMRES: |beta_k| <= tol norm_rhs
+  int iter;    // the Arnoldi step being built (k, from 1)
   int flag;    // warm-start test: 1 accepted, 2 discarded, 3 zero right-hand side
   int done;    // 1: converged or out of steps
   int iters;   // Arnoldi steps taken
@@ -115,6 +121,16 @@ struct PresState {
   bool use_ff = false;
   double *x_all = nullptr, *v_all = nullptr;  // 3 (Ns + Nb)
   void *rec_ff = nullptr;
+  double *body_dev = nullptr;  // [3] body position of the kinematics set last
+  // Arnoldi steps run in chunks of kPresChunk, device-driven: the step
+  // kernels read the step from the scalars and skip once finished, and the
+  // products' jobs skip through *skip = st->done (jobs_it, jobs32_it); each
+  // chunk replays a CUDA graph captured once per precision
+  QueueJob *jobs_it_dev = nullptr, *jobs32_it_dev = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  long long graph_kernels[2] = {0, 0};
+  int graph_variant[2] = {-1, -1};
+  bool graphs_ok = true;
 };
 
 namespace {
@@ -176,7 +192,7 @@ struct PA {
   int ns, nb, nfil, nseg, n, o_body, o_phase, o_angle;
   int free_body, phase, angle, weak;
   double c, cb;
-  double bx, by, bz;
+  const double *body;  // device [3]: the body position
   const double *x_segs, *d_blobs, *kphi, *kth, *fil, *m6inv;
   double *part6;
   unsigned *cnt;
@@ -188,9 +204,9 @@ __device__ __forceinline__ int pa_warp() {
 }
 
 __device__ __forceinline__ void seg_d(const PA &a, int i, double *d) {
-  d[0] = a.x_segs[3 * (size_t)i] - a.bx;
-  d[1] = a.x_segs[3 * (size_t)i + 1] - a.by;
-  d[2] = a.x_segs[3 * (size_t)i + 2] - a.bz;
+  d[0] = a.x_segs[3 * (size_t)i] - a.body[0];
+  d[1] = a.x_segs[3 * (size_t)i + 1] - a.body[1];
+  d[2] = a.x_segs[3 * (size_t)i + 2] - a.body[2];
 }
 
 // Sum of the warps' partial 6-vectors (warp order), by the last CTA: result
@@ -437,7 +453,8 @@ __global__ void __launch_bounds__(kPT) pres_rhs_kernel(PA a, RhsArgs r, double *
 // FP64 3-force records {x, y, z, f0, f1, f2} of every segment and blob with
 // the forces of z; the 6-stride segment forces of the weakly coupled product.
 __global__ void pres_pack_kernel(PA a, const double *z, const double *x_blobs, double *rec_s,
-                                 double *rec_b, double *f6) {
+                                 double *rec_b, double *f6, const PresScalars *it) {
+  if (it != nullptr && it->done) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p < a.ns) {
     double *r = rec_s + 6 * (size_t)p;
@@ -464,7 +481,9 @@ __global__ void pres_pack_kernel(PA a, const double *z, const double *x_blobs, d
 // positions relative to the solver's origin, as the FP32 work-queue kernel
 // reads them.
 __global__ void pres_pack32_kernel(PA a, const double *z, const double *x_blobs,
-                                   const double *origin, float *rec_s, float *rec_b) {
+                                   const double *origin, float *rec_s, float *rec_b,
+                                   const PresScalars *it) {
+  if (it != nullptr && it->done) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   const double *x;
   float *r;
@@ -492,12 +511,18 @@ __global__ void pres_pack32_kernel(PA a, const double *z, const double *x_blobs,
 // out = A z from the products: segments v_ss (or the 6-stride v6 of the
 // weakly coupled product) + v_sb, blobs v_bb + v_bs, minus K [U; Omega;
 // phase rates; angle rates]; phase and angle rows -K^T; body rows -K^T (the
-// last CTA). resid != nullptr: out = resid - A z instead.
+// last CTA). resid != nullptr: out = resid - A z instead. it != nullptr (an
+// Arnoldi step): out is column it->iter of out, and a finished solve skips.
 __global__ void __launch_bounds__(kPT) pres_combine_kernel(PA a, const double *z, const double *v_ss,
                                                            const double *v6, const double *v_sb,
                                                            const double *v_bb, const double *v_bs,
-                                                           const double *resid, double *out) {
+                                                           const double *resid, double *out,
+                                                           const PresScalars *it) {
   __shared__ double sh[8];
+  if (it != nullptr) {
+    if (it->done) return;
+    out += (size_t)it->iter * a.n;
+  }
   const int w = pa_warp(), lane = threadIdx.x & 31;
   double U[6] = {0, 0, 0, 0, 0, 0};
   if (a.free_body)
@@ -599,8 +624,13 @@ __device__ __forceinline__ void pres_cinv(const double *F, double &i11, double &
 // phase/angle rows after their 2x2 solve are stored, the body block's
 // right-hand side t = -in_body - sum (s; d x s) - sum (p v + a v'; p u + a u')
 // is summed over the warps, and the last CTA writes B = M^-1 t.
-__global__ void __launch_bounds__(kPT) pres_precond_a_kernel(PA a, const double *in, double *out) {
+__global__ void __launch_bounds__(kPT) pres_precond_a_kernel(PA a, const double *in, double *out,
+                                                             const PresScalars *it) {
   __shared__ double sh[8];
+  if (it != nullptr) {  // an Arnoldi step: in is column it->iter - 1 of in
+    if (it->done) return;
+    in += (size_t)(it->iter - 1) * a.n;
+  }
   const int w = pa_warp(), lane = threadIdx.x & 31;
   double p6[6] = {0, 0, 0, 0, 0, 0};
   if (w < a.fil_warps) {
@@ -702,7 +732,9 @@ __global__ void __launch_bounds__(kPT) pres_precond_a_kernel(PA a, const double 
 
 // Pass B (free body): the phase/angle rows' correction by the body block B
 // and s += c (B0 + B1 x d + p K_phi + a K_th), blobs += cb (B0 + B1 x d).
-__global__ void __launch_bounds__(kPT) pres_precond_b_kernel(PA a, double *out) {
+__global__ void __launch_bounds__(kPT) pres_precond_b_kernel(PA a, double *out,
+                                                             const PresScalars *it) {
+  if (it != nullptr && it->done) return;
   const int w = pa_warp(), lane = threadIdx.x & 31;
   double B[6];
   for (int k = 0; k < 6; ++k) B[k] = out[a.o_body + k];
@@ -796,7 +828,6 @@ __global__ void pres_hook_out_kernel(const double *v, double *out, int n, int st
 // ---------------------------------------------------------------------------
 struct GA {
   int n, G, rows, ld, pstride, max_iter;
-  double tol;
   double *Q, *H, *beta, *cs, *sn, *y, *h1, *h2, *part;
   unsigned *cnt;
   PresScalars *st;
@@ -830,12 +861,14 @@ __global__ void __launch_bounds__(kPT) pres_norm_kernel(GA g, const double *v, d
 // The warm-start tests of solve_linear_system (mobility_solver.cpp:2121-2320)
 // on beta0 = ||rhs - A x0|| and ||rhs||: flag 3 zero right-hand side, 1 the
 // warm start already solves the system, 2 discard it (beta0 > ||rhs||).
-__global__ void pres_start_kernel(GA g) {
+__global__ void pres_start_kernel(GA g, double tol) {
   PresScalars *st = g.st;
   const double nr = st->norm_rhs, b0 = st->beta0;
+  st->tol = tol;
+  st->iter = 1;
   int flag = 0;
   if (nr == 0.0) flag = 3;
-  else if (fabs(b0) <= g.tol * nr) flag = 1;
+  else if (fabs(b0) <= tol * nr) flag = 1;
   else if (fabs(b0) > nr) flag = 2;
   st->flag = flag;
   st->done = (flag == 1 || flag == 3) ? 1 : 0;
@@ -931,13 +964,19 @@ __device__ void pres_orth(const GA &g, double *w, int k, const double *h) {
   __syncthreads();
 }
 
-// Step k, pass 1: h1 = Q^T w.
-__global__ void __launch_bounds__(kPT) pres_dots1_kernel(GA g, int k) {
+// Step k = st->iter, pass 1: h1 = Q^T w. (The step kernels read k from the
+// device scalars and skip once the solve is finished, so a chunk of steps
+// is the same launch sequence every time.)
+__global__ void __launch_bounds__(kPT) pres_dots1_kernel(GA g) {
+  if (g.st->done) return;
+  const int k = g.st->iter;
   pres_dots(g, g.Q + (size_t)k * g.n, k, g.h1);
 }
 
-// Step k, pass 2: w -= Q h1, h2 = Q^T w; the last CTA sets H(:, k-1) = h1 + h2.
-__global__ void __launch_bounds__(kPT) pres_dots2_kernel(GA g, int k) {
+// Step k, pass 2: w -= Q h1, h2 = Q^T w.
+__global__ void __launch_bounds__(kPT) pres_dots2_kernel(GA g) {
+  if (g.st->done) return;
+  const int k = g.st->iter;
   double *w = g.Q + (size_t)k * g.n;
   pres_orth(g, w, k, g.h1);
   pres_dots(g, w, k, g.h2);
@@ -947,9 +986,11 @@ __global__ void __launch_bounds__(kPT) pres_dots2_kernel(GA g, int k) {
 // earlier Givens rotations and the new one (mobility_solver.cpp:2370-2404),
 // tests convergence (:2409-2413) and, when finishing, back-solves y (:2419-
 // 2438) with warp-parallel inner sums.
-__global__ void __launch_bounds__(kPT) pres_norm_givens_kernel(GA g, int k) {
+__global__ void __launch_bounds__(kPT) pres_norm_givens_kernel(GA g) {
   __shared__ double red[kPW];
   __shared__ int fin;
+  if (g.st->done) return;
+  const int k = g.st->iter;
   double *w = g.Q + (size_t)k * g.n;
   pres_orth(g, w, k, g.h2);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1003,10 +1044,11 @@ __global__ void __launch_bounds__(kPT) pres_norm_givens_kernel(GA g, int k) {
     g.beta[c] = cs * g.beta[c];
     const double rel = fabs(g.beta[k]) / st->norm_rhs;
     st->rel = rel;
-    const int finished = (rel <= g.tol) || (k == g.max_iter) || !(rel == rel);
+    const int finished = (rel <= st->tol) || (k == g.max_iter) || !(rel == rel);
     if (!(rel == rel)) st->status = 1;
     st->iters = k;
     st->done = finished;
+    if (!finished) st->iter = k + 1;
     fin = finished;
     *g.cnt = 0u;
   }
@@ -1024,9 +1066,10 @@ __global__ void __launch_bounds__(kPT) pres_norm_givens_kernel(GA g, int k) {
   }
 }
 
-// Q_k = w / ||w|| (unless finished).
-__global__ void pres_scale_kernel(GA g, int k) {
+// Q_k = w / ||w|| for the step just built (k = st->iter - 1; unless finished).
+__global__ void pres_scale_kernel(GA g) {
   if (g.st->done) return;
+  const int k = g.st->iter - 1;
   const double inv = 1.0 / g.st->qnorm;
   double *w = g.Q + (size_t)k * g.n;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < g.n; r += gridDim.x * blockDim.x)
@@ -1069,6 +1112,11 @@ void pres_free(tfs_solver *s) {
   cudaFree(p->x_all);
   cudaFree(p->v_all);
   cudaFree(p->rec_ff);
+  cudaFree(p->body_dev);
+  cudaFree(p->jobs_it_dev);
+  cudaFree(p->jobs32_it_dev);
+  for (cudaGraphExec_t g : p->graph)
+    if (g) cudaGraphExecDestroy(g);
   cudaFree(p->jobs32_dev);
   if (p->st_host) cudaFreeHost(p->st_host);
   delete p;
@@ -1094,9 +1142,7 @@ PA pres_pa(tfs_solver *s) {
   a.weak = p->weak;
   a.c = 6.0 * kPiP * s->cfg.mu * s->cfg.a_seg;
   a.cb = 6.0 * kPiP * s->cfg.mu * s->cfg.a_blob;
-  a.bx = s->pose.x[0];
-  a.by = s->pose.x[1];
-  a.bz = s->pose.x[2];
+  a.body = p->body_dev;
   a.x_segs = s->x_segs;
   a.d_blobs = s->diff;
   a.kphi = p->kphi;
@@ -1112,7 +1158,7 @@ PA pres_pa(tfs_solver *s) {
 
 int pa_ctas(const PA &a) { return std::max(1, (a.fil_warps + a.blob_warps + kPW - 1) / kPW); }
 
-GA pres_ga(tfs_solver *s, double tol) {
+GA pres_ga(tfs_solver *s) {
   PresState *p = s->pres;
   GA g{};
   g.n = p->n;
@@ -1121,7 +1167,6 @@ GA pres_ga(tfs_solver *s, double tol) {
   g.ld = kPresMaxIter + 1;
   g.pstride = p->pstride;
   g.max_iter = p->max_iter;
-  g.tol = tol;
   g.Q = p->Q;
   g.H = p->H;
   g.beta = p->beta;
@@ -1249,6 +1294,29 @@ int pres_alloc(tfs_solver *s) {
   TFS_CUDA(cudaMemcpy(p->jobs32_dev, p->jobs32, sizeof(QueueJob) * p->n_jobs,
                       cudaMemcpyHostToDevice),
            "copy queue jobs");
+  // the step jobs: the same, skipping once the solve is finished
+  if ((rc = alloc_dev((void **)&p->jobs_it_dev, sizeof(QueueJob) * 4)) != TFS_OK ||
+      (rc = alloc_dev((void **)&p->jobs32_it_dev, sizeof(QueueJob) * 4)) != TFS_OK ||
+      (rc = alloc_dev((void **)&p->body_dev, sizeof(double) * 3)) != TFS_OK)
+    return rc;
+  {
+    QueueJob it64[4], it32[4];
+    for (int j = 0; j < p->n_jobs; ++j) {
+      it64[j] = p->jobs[j];
+      it32[j] = p->jobs32[j];
+      it64[j].skip = &p->st->done;
+      it32[j].skip = &p->st->done;
+    }
+    TFS_CUDA(cudaMemcpy(p->jobs_it_dev, it64, sizeof(QueueJob) * p->n_jobs, cudaMemcpyHostToDevice),
+             "copy queue jobs");
+    TFS_CUDA(cudaMemcpy(p->jobs32_it_dev, it32, sizeof(QueueJob) * p->n_jobs,
+                        cudaMemcpyHostToDevice),
+             "copy queue jobs");
+  }
+  if (p->weak && ns > 0 && s->wc_z == nullptr &&  // the weakly coupled product's means, totals
+      ((rc = alloc_dev((void **)&s->wc_z, sizeof(double) * 3 * p->nfil)) != TFS_OK ||
+       (rc = alloc_dev((void **)&s->wc_f, sizeof(double) * 3 * p->nfil)) != TFS_OK))
+    return rc;
   p->use_ff = !p->weak && s->cfg.a_seg == s->cfg.a_blob && ns + nb > 0;
   if (p->use_ff &&
       ((rc = alloc_dev((void **)&p->x_all, sizeof(double) * 3 * (ns + nb))) != TFS_OK ||
@@ -1264,60 +1332,59 @@ int pres_alloc(tfs_solver *s) {
 }
 
 // out = A z (resid == nullptr) or resid - A z; fp32: the pair sums of the
-// work-queue kernel in FP32 with compensated accumulation.
-int pres_operator(tfs_solver *s, int fp32, const double *z, const double *resid, double *out) {
+// work-queue kernel in FP32 with compensated accumulation (the origin must be
+// current: ensure_origin before). it != nullptr: an Arnoldi step (out is
+// column it->iter of out; everything skips once the solve is finished).
+int pres_operator(tfs_solver *s, int fp32, const double *z, const double *resid, double *out,
+                  const PresScalars *it = nullptr) {
   PresState *p = s->pres;
   const PA a = pres_pa(s);
   const int np = p->ns + p->nb;
   if (np > 0) {
     if (fp32) {
-      int rc;
-      if ((rc = ensure_origin(s)) != TFS_OK) return rc;
       pres_pack32_kernel<<<(np + 255) / 256, 256, 0, s->stream>>>(a, z, s->x_blobs, s->origin,
-                                                                  p->rec_s32, p->rec_b32);
+                                                                  p->rec_s32, p->rec_b32, it);
       if (p->weak)  // the weakly coupled segment block stays FP64
         pres_pack_kernel<<<(np + 255) / 256, 256, 0, s->stream>>>(a, z, s->x_blobs, p->rec_s,
-                                                                  p->rec_b, p->f6);
+                                                                  p->rec_b, p->f6, it);
     } else {
-      pres_pack_kernel<<<(np + 255) / 256, 256, 0, s->stream>>>(a, z, s->x_blobs, p->rec_s,
-                                                                p->rec_b, p->weak ? p->f6 : nullptr);
+      pres_pack_kernel<<<(np + 255) / 256, 256, 0, s->stream>>>(
+          a, z, s->x_blobs, p->rec_s, p->rec_b, p->weak ? p->f6 : nullptr, it);
     }
     count_launch_n(fp32 && p->weak ? 2 : 1);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "prescribed pack kernel");
-  if (p->weak && p->ns > 0) {
-    int rc;
-    if (s->wc_z == nullptr &&
-        ((rc = alloc_dev((void **)&s->wc_z, sizeof(double) * 3 * p->nfil)) != TFS_OK ||
-         (rc = alloc_dev((void **)&s->wc_f, sizeof(double) * 3 * p->nfil)) != TFS_OK))
-      return rc;
+  if (p->weak && p->ns > 0) {  // (buffers allocated by the setup)
     e = launch_msf(s->x_segs, p->f6, p->nfil, p->nseg, s->cfg.a_seg, s->cfg.mu, s->wc_z, s->wc_f,
                    p->v6, s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "weakly coupled segment product");
   }
   if (p->n_jobs > 0) {
-    e = fp32 ? launch_queue(1, s->qtune[1][QK_MBB], Q_BLOB, p->jobs32_dev, p->jobs32, p->n_jobs,
-                            p->qcnt, s->stream)
-             : launch_queue(0, s->qtune[0][QK_MBB], Q_BLOB, p->jobs_dev, p->jobs, p->n_jobs,
-                            p->qcnt, s->stream);
+    const QueueJob *d64 = it ? p->jobs_it_dev : p->jobs_dev;
+    const QueueJob *d32 = it ? p->jobs32_it_dev : p->jobs32_dev;
+    e = fp32 ? launch_queue(1, s->qtune[1][QK_MBB], Q_BLOB, d32, p->jobs32, p->n_jobs, p->qcnt,
+                            s->stream)
+             : launch_queue(0, s->qtune[0][QK_MBB], Q_BLOB, d64, p->jobs, p->n_jobs, p->qcnt,
+                            s->stream);
     if (e != cudaSuccess) return cuda_fail(e, "RPY work-queue kernel (prescribed)");
   }
   pres_combine_kernel<<<pa_ctas(a), kPT, 0, s->stream>>>(a, z, p->v_ss, p->v6, p->v_sb, p->v_bb,
-                                                         p->v_bs, resid, out);
+                                                         p->v_bs, resid, out, it);
   count_launch();
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "prescribed combine kernel");
   return TFS_OK;
 }
 
-// out = P^-1 in (in != out).
-int pres_precond(tfs_solver *s, const double *in, double *out) {
+// out = P^-1 in (in != out); it: as for pres_operator (in is column
+// it->iter - 1 of in).
+int pres_precond(tfs_solver *s, const double *in, double *out, const PresScalars *it = nullptr) {
   const PA a = pres_pa(s);
-  pres_precond_a_kernel<<<pa_ctas(a), kPT, 0, s->stream>>>(a, in, out);
+  pres_precond_a_kernel<<<pa_ctas(a), kPT, 0, s->stream>>>(a, in, out, it);
   count_launch();
   if (a.free_body) {
-    pres_precond_b_kernel<<<pa_ctas(a), kPT, 0, s->stream>>>(a, out);
+    pres_precond_b_kernel<<<pa_ctas(a), kPT, 0, s->stream>>>(a, out, it);
     count_launch();
   }
   cudaError_t e = cudaGetLastError();
@@ -1370,31 +1437,96 @@ int pres_read_scalars(tfs_solver *s, const char *what) {
   return TFS_OK;
 }
 
-// Arnoldi steps from the normalised Q_0 (beta[0] and st->norm_rhs set) until
-// |beta_k| <= tol st->norm_rhs or the cap, then x += P^-1 (Q y). fp32: FP32
-// pair sums in the operator. Returns the steps in *iters.
-int pres_arnoldi(tfs_solver *s, int fp32, double tol, int *iters) {
+// kPresChunk Arnoldi steps: preconditioner, operator, CGS2, norm and Givens,
+// every kernel reading the step from the device scalars and skipping once the
+// solve is finished (the same launch sequence every time).
+int pres_chunk(tfs_solver *s, int fp32) {
   PresState *p = s->pres;
-  const GA g = pres_ga(s, tol);
+  const GA g = pres_ga(s);
   int rc;
-  *iters = 0;
-  for (int k = 1; k <= p->max_iter; ++k) {
-    double *qprev = p->Q + (size_t)(k - 1) * p->n, *w = p->Q + (size_t)k * p->n;
-    if ((rc = pres_precond(s, qprev, p->z)) != TFS_OK) return rc;
-    if ((rc = pres_operator(s, fp32, p->z, nullptr, w)) != TFS_OK) return rc;
-    pres_dots1_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
-    pres_dots2_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
-    pres_norm_givens_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
-    pres_scale_kernel<<<g.G, kPT, 0, s->stream>>>(g, k);
+  for (int c = 0; c < kPresChunk; ++c) {
+    if ((rc = pres_precond(s, p->Q, p->z, p->st)) != TFS_OK) return rc;
+    if ((rc = pres_operator(s, fp32, p->z, nullptr, p->Q, p->st)) != TFS_OK) return rc;
+    pres_dots1_kernel<<<g.G, kPT, 0, s->stream>>>(g);
+    pres_dots2_kernel<<<g.G, kPT, 0, s->stream>>>(g);
+    pres_norm_givens_kernel<<<g.G, kPT, 0, s->stream>>>(g);
+    pres_scale_kernel<<<g.G, kPT, 0, s->stream>>>(g);
     count_launch_n(4);
     TFS_CUDA(cudaGetLastError(), "prescribed Arnoldi step");
-    if ((rc = pres_read_scalars(s, "prescribed Arnoldi step")) != TFS_OK) return rc;
-    if (p->st_host->status != 0) return fail(TFS_ENAN, "non-finite GMRES residual");
-    if (p->st_host->done) {
-      *iters = k;
-      break;
-    }
   }
+  return TFS_OK;
+}
+
+// The chunk as a CUDA graph, captured once per precision (and work-queue
+// variant); nullptr: launch it directly (capture unavailable, or kernel
+// timing on).
+cudaGraphExec_t pres_graph(tfs_solver *s, int fp32, long long *kernels) {
+  PresState *p = s->pres;
+  const int var = s->qtune[fp32][QK_MBB];
+  if (!p->graphs_ok || s->timing) return nullptr;
+  if (p->graph[fp32] != nullptr && p->graph_variant[fp32] == var) {
+    *kernels = p->graph_kernels[fp32];
+    return p->graph[fp32];
+  }
+  if (p->graph[fp32] != nullptr) {
+    cudaGraphExecDestroy(p->graph[fp32]);
+    p->graph[fp32] = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const long long before = launch_count();
+  if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    p->graphs_ok = false;
+    return nullptr;
+  }
+  const int rc = pres_chunk(s, fp32);
+  const cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+  const long long recorded = launch_count() - before;
+  count_launch_n(-recorded);  // recorded, not launched
+  if (rc != TFS_OK || e != cudaSuccess || graph == nullptr ||
+      cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+    cudaGetLastError();
+    if (graph) cudaGraphDestroy(graph);
+    p->graphs_ok = false;
+    return nullptr;
+  }
+  cudaGraphDestroy(graph);
+  p->graph[fp32] = exec;
+  p->graph_kernels[fp32] = recorded;
+  p->graph_variant[fp32] = var;
+  *kernels = recorded;
+  return exec;
+}
+
+// Arnoldi steps from the normalised Q_0 (beta[0], st->norm_rhs, st->tol and
+// st->iter = 1 set) in chunks, one poll of the scalars per chunk, until
+// |beta_k| <= tol norm_rhs or the cap; then x += P^-1 (Q y). fp32: FP32 pair
+// sums in the operator. The first chunk of each precision runs eagerly (it
+// initialises the launch paths), later ones replay the captured graph.
+int pres_arnoldi(tfs_solver *s, int fp32, int *iters) {
+  PresState *p = s->pres;
+  const GA g = pres_ga(s);
+  int rc;
+  *iters = 0;
+  const int max_chunks = p->max_iter / kPresChunk + 2;
+  bool eager = p->graph[fp32] == nullptr;
+  for (int c = 0; c < max_chunks; ++c) {
+    long long kernels = 0;
+    cudaGraphExec_t exec = eager ? nullptr : pres_graph(s, fp32, &kernels);
+    if (exec != nullptr) {
+      TFS_CUDA(cudaGraphLaunch(exec, s->stream), "prescribed Arnoldi chunk");
+      count_launch_n(kernels);
+    } else if ((rc = pres_chunk(s, fp32)) != TFS_OK) {
+      return rc;
+    }
+    eager = false;
+    if ((rc = pres_read_scalars(s, "prescribed Arnoldi chunk")) != TFS_OK) return rc;
+    if (p->st_host->status != 0) return fail(TFS_ENAN, "non-finite GMRES residual");
+    if (p->st_host->done) break;
+  }
+  if (!p->st_host->done) return fail(TFS_ENOTCONV, "GMRES did not finish within %d steps", p->max_iter);
+  *iters = p->st_host->iters;
   pres_qy_kernel<<<g.G, kPT, 0, s->stream>>>(g, *iters, p->tmp);
   count_launch();
   if ((rc = pres_precond(s, p->tmp, p->z)) != TFS_OK) return rc;
@@ -1425,7 +1557,7 @@ int pres_operator_ff(tfs_solver *s, const double *z, const double *resid, double
   const PA a = pres_pa(s);
   pres_combine_kernel<<<pa_ctas(a), kPT, 0, s->stream>>>(a, z, p->v_all, nullptr, nullptr,
                                                          p->v_all + 3 * (size_t)p->ns, nullptr,
-                                                         resid, out);
+                                                         resid, out, nullptr);
   count_launch();
   TFS_CUDA(cudaGetLastError(), "prescribed combine kernel");
   return TFS_OK;
@@ -1435,7 +1567,7 @@ int pres_operator_ff(tfs_solver *s, const double *z, const double *resid, double
 // particle has the same radius) and its norm into st->beta0 (returned).
 int pres_residual(tfs_solver *s, double *norm) {
   PresState *p = s->pres;
-  const GA g = pres_ga(s, s->tol);
+  const GA g = pres_ga(s);
   int rc;
   const bool ff = p->use_ff && s->cfg.precision == TFS_FP32C;
   if ((rc = ff ? pres_operator_ff(s, p->x, p->b, p->Q) : pres_operator(s, 0, p->x, p->b, p->Q)) !=
@@ -1449,11 +1581,14 @@ int pres_residual(tfs_solver *s, double *norm) {
   return TFS_OK;
 }
 
-// Start an inner solve on Q_0 = r (unnormalised, ||r|| = nr): Q_0 /= nr,
-// beta[0] = nr, and the stopping test relative to nr.
-__global__ void pres_inner_start_kernel(GA g, double nr) {
+// Start an inner solve on Q_0 = r (unnormalised, ||r|| = nr; pres_q0_kernel
+// then divides it by beta[0] = nr): the stopping test |beta_k| <= tol nr,
+// from step 1.
+__global__ void pres_inner_start_kernel(GA g, double nr, double tol) {
   PresScalars *st = g.st;
   st->norm_rhs = nr;
+  st->tol = tol;
+  st->iter = 1;
   st->flag = 0;
   st->done = 0;
   st->status = 0;
@@ -1464,8 +1599,9 @@ int pres_solve(tfs_solver *s, int *iters_out) {
   PresState *p = s->pres;
   if (!p->have_kin) return fail(TFS_ESTATE, "set the kinematics first");
   const bool fp32 = s->cfg.precision == TFS_FP32C;
-  const GA g = pres_ga(s, s->tol);
+  const GA g = pres_ga(s);
   int rc;
+  if (fp32 && (rc = ensure_origin(s)) != TFS_OK) return rc;  // the FP32 records' origin
   if ((rc = pres_rhs(s)) != TFS_OK) return rc;
   // ||rhs||; r0 = rhs - A x0 into Q_0 (FP64); beta0 = ||r0||; the warm-start
   // tests (mobility_solver.cpp:2121-2320)
@@ -1475,7 +1611,7 @@ int pres_solve(tfs_solver *s, int *iters_out) {
                          : pres_operator(s, 0, p->x, p->b, p->Q);
   if (rc != TFS_OK) return rc;
   pres_norm_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->Q, &p->st->beta0);
-  pres_start_kernel<<<1, 1, 0, s->stream>>>(g);
+  pres_start_kernel<<<1, 1, 0, s->stream>>>(g, s->tol);
   pres_q0_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->b, p->x);
   count_launch_n(3);
   TFS_CUDA(cudaGetLastError(), "prescribed GMRES start");
@@ -1486,7 +1622,7 @@ int pres_solve(tfs_solver *s, int *iters_out) {
   double rel = nb > 0.0 ? p->st_host->beta0 / nb : 0.0;
   if (!p->st_host->done) {
     if (!fp32) {
-      if ((rc = pres_arnoldi(s, 0, s->tol, &iters)) != TFS_OK) return rc;
+      if ((rc = pres_arnoldi(s, 0, &iters)) != TFS_OK) return rc;
       rel = p->st_host->rel;
       cycles = 1;
     } else {
@@ -1496,14 +1632,14 @@ int pres_solve(tfs_solver *s, int *iters_out) {
       // residual hands over to FP64 GMRES from the current x
       double cur = p->st_host->flag == 2 ? nb : p->st_host->beta0;
       bool fp64_finish = false;
-      pres_inner_start_kernel<<<1, 1, 0, s->stream>>>(g, cur);  // Q_0 is normalised already
+      auto inner_tol = [&]() {
+        return fp64_finish ? s->tol * nb / cur : std::max(s->inner_tol, 0.5 * s->tol * nb / cur);
+      };
+      pres_inner_start_kernel<<<1, 1, 0, s->stream>>>(g, cur, inner_tol());  // Q_0 normalised
       count_launch();
       for (;;) {
-        const double tin = std::max(s->inner_tol, 0.5 * s->tol * nb / cur);
         int it = 0;
-        if ((rc = pres_arnoldi(s, fp64_finish ? 0 : 1, fp64_finish ? s->tol * nb / cur : tin,
-                               &it)) != TFS_OK)
-          return rc;
+        if ((rc = pres_arnoldi(s, fp64_finish ? 0 : 1, &it)) != TFS_OK) return rc;
         iters += it;
         ++cycles;
         double nr;
@@ -1516,7 +1652,7 @@ int pres_solve(tfs_solver *s, int *iters_out) {
           ++p->fallbacks;
         }
         cur = nr;
-        pres_inner_start_kernel<<<1, 1, 0, s->stream>>>(g, cur);
+        pres_inner_start_kernel<<<1, 1, 0, s->stream>>>(g, cur, inner_tol());
         pres_q0_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->b, p->x);
         count_launch_n(2);
         TFS_CUDA(cudaGetLastError(), "prescribed refinement restart");
@@ -1694,7 +1830,9 @@ int tfs_prescribed_set_kinematics(tfs_solver *s, const tfs_prescribed_kinematics
   }
   // per-filament constants and (free body) the body block's inverse, on the
   // current segment positions and body pose (swimmer::make_precon_mat runs
-  // after the filaments' kinematics, swimmer.cpp:433-466)
+  // after the filaments' kinematics, swimmer.cpp:433-466); the body position
+  // the solve's kernels read
+  if ((rc = upload(s, p->body_dev, s->pose.x, 3, "copy body position")) != TFS_OK) return rc;
   const PA a = pres_pa(s);
   if (p->nfil > 0) {
     pres_fil_kernel<<<(p->nfil + kPW - 1) / kPW, kPT, 0, s->stream>>>(a, p->fil);
