@@ -202,3 +202,40 @@ def test_block_hooks_take_the_prescribed_form(cfg):
     assert np.all(v6[:, 3:] == 0.0)
     assert rel(s.v_blobs_host, vb) <= 1e-12
     ps.finalise()
+
+
+@pytest.mark.parametrize("flags", [0, 7])
+def test_filaments_without_blobs(flags):
+    """A body without blobs (NBLOB = 0): the operator, preconditioner and
+    right-hand side against the CPU restatement, and a solve to its
+    residual; the blob parts of the solution are empty."""
+    from prescribed import PrescribedSystem
+    from timfilsimmod_gb300.geometry import prescribed_swimmer
+    from timfilsimmod_gb300.prescribed import PrescribedCiliaSolver
+    g = prescribed_swimmer(6, 8, radius=8.0, subdivisions=1, seg_sep=2.6)
+    refs = np.zeros((0, 3))
+    rng = np.random.default_rng(4)
+    phase = rng.uniform(0, 2 * np.pi, g.nfil)
+    angle = rng.uniform(-0.2, 0.2, g.nfil)
+    omega0 = 2 * np.pi * np.ones(g.nfil)
+    x, vp, va = g.kinematics(phase, angle)
+    t = 2 * np.pi * np.arange(32) / 32
+    tp, ta = 1 + 0.3 * np.sin(t), 0.1 * np.cos(t)
+    ps = PrescribedCiliaSolver(flags, g.nfil, g.nseg, refs, g.seg_sep, tp, ta, tol=1e-10)
+    k = dict(x_segs=x, vel_dir_phase=vp, vel_dir_angle=va, phase=phase, omega0=omega0,
+             shape_rotation_angle=angle, phase_dot=omega0)
+    ps.set_kinematics(**k)
+    S = PrescribedSystem(flags, g.nfil, g.nseg, x, refs, (0, 0, 0), (1, 0, 0, 0), vp, va)
+    assert ps.n == S.n
+    v = rng.normal(size=ps.n)
+    assert rel(ps.apply("operator", v), S.apply_a(v)) <= 1e-12
+    assert rel(ps.apply("preconditioner", v), S.apply_pinv(v)) <= 1e-12
+    b = ps.apply("rhs")
+    assert rel(b, S.rhs(phase, omega0, angle, omega0, tp, ta,
+                        fil_length=g.seg_sep * (g.nseg - 1))) <= 1e-13
+    ps.solve()
+    sol = ps.solution()
+    assert sol["f_blobs"].size == 0
+    x_sol, _ = S.solve(b, np.zeros(S.n), tol=1e-10)
+    assert rel(sol["f_segs"], x_sol[:3 * g.nfil * g.nseg]) <= 1e-6
+    ps.finalise()
