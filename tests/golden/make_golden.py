@@ -417,7 +417,7 @@ def prescribed_inputs(nsteps=3, seed=7):
 
 
 def case_prescribed(config):
-    """The reference's prescribed-cilia solve (configuration p1, p2 or p3 of
+    """The reference's prescribed-cilia solve (configuration p1 ... p6 of
     oracle/Makefile): three consecutive solves (warm started from the last),
     then, on the first step's kinematics, the right-hand side, swimmer
     KTMinvK_inv, and the operator and preconditioner applied to a seeded
@@ -449,7 +449,10 @@ CASES = {"small_matvec": case_small, "overlap_a16": case_overlap, "tiny": case_t
          "step_medium_default_dt": case_step_medium_default_dt,
          "prescribed_p1": lambda: case_prescribed("p1"),
          "prescribed_p2": lambda: case_prescribed("p2"),
-         "prescribed_p3": lambda: case_prescribed("p3")}
+         "prescribed_p3": lambda: case_prescribed("p3"),
+         "prescribed_p4": lambda: case_prescribed("p4"),
+         "prescribed_p5": lambda: case_prescribed("p5"),
+         "prescribed_p6": lambda: case_prescribed("p6")}
 
 
 def main():

@@ -23,7 +23,7 @@ import numpy as np
 import pytest
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
-CONFIGS = ("p1", "p2", "p3")
+CONFIGS = ("p1", "p2", "p3", "p4", "p5", "p6")
 
 pytestmark = pytest.mark.gpu
 

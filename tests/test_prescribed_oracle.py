@@ -14,7 +14,7 @@ import pytest
 from prescribed import PrescribedSystem, spline
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
-CONFIGS = ("p1", "p2", "p3")
+CONFIGS = ("p1", "p2", "p3", "p4", "p5", "p6")
 
 
 def load(cfg):
