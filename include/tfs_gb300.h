@@ -280,7 +280,11 @@ typedef struct tfs_prescribed_kinematics {
  * positions and body pose. Synchronises the solver's stream. */
 int tfs_prescribed_set_kinematics(tfs_solver *s, const tfs_prescribed_kinematics *k);
 /* assemble_rhs and the GMRES solve on the kinematics set last, warm started
- * from the previous solution. Synchronises the solver's stream. */
+ * from the previous solution. FP32C: inner solves on FP32 pair sums (FP64
+ * Krylov vectors), each to max(1e-7, tol ||b|| / (2 ||r||)), refined on
+ * float-float (equal radii, RPY) or FP64 residuals until the FP64 relative
+ * residual meets the tolerance; tfs_solve_info reports the inner steps and
+ * cycles. Synchronises the solver's stream. */
 int tfs_prescribed_solve(tfs_solver *s, int *gmres_iters);
 /* tfs_prescribed_set_kinematics, then tfs_prescribed_solve. */
 int tfs_prescribed_compute_velocities(tfs_solver *s, const tfs_prescribed_kinematics *k,

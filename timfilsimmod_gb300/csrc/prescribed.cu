@@ -53,6 +53,10 @@ constexpr int kPW = kPT / 32;    // warps per CTA
 constexpr int kFilC = 16;        // per-filament constants (below)
 constexpr int kPresMaxIter = 350;  // MAX_LINEAR_SYSTEM_ITER (config.hpp:312)
 constexpr int kPresChunk = 4;      // Arnoldi steps launched between polls of the done flag
+// FP32C: the deepest relative reduction an inner solve is asked for. Its
+// Krylov vectors are FP64 and only the pair sums are FP32 (compensated,
+// ~1e-7 relative), so below this the correction's own error dominates.
+constexpr double kPresInnerFloor = 1e-7;
 
 // Per filament m (swimmer.cpp:1255-1287, mobility_solver.cpp:1060-1100):
 // [0] c11 = K_phi.K_phi, [1] c22 = K_th.K_th, [2] c12 = K_phi.K_th,
@@ -1627,13 +1631,14 @@ int pres_solve(tfs_solver *s, int *iters_out) {
       cycles = 1;
     } else {
       // iterative refinement: inner GMRES with FP32 pair sums on the FP64
-      // residual r, each to max(inner_tol, tol ||b|| / (2 ||r||)), until
-      // ||b - A x|| <= tol ||b|| in FP64; a cycle that does not reduce the
-      // residual hands over to FP64 GMRES from the current x
+      // residual r, each to max(1e-7, tol ||b|| / (2 ||r||)), until
+      // ||b - A x|| <= tol ||b|| in FP64 (a warm start within ~20x of the
+      // tolerance needs one cycle); a cycle that does not reduce the residual
+      // hands over to FP64 GMRES from the current x
       double cur = p->st_host->flag == 2 ? nb : p->st_host->beta0;
       bool fp64_finish = false;
       auto inner_tol = [&]() {
-        return fp64_finish ? s->tol * nb / cur : std::max(s->inner_tol, 0.5 * s->tol * nb / cur);
+        return fp64_finish ? s->tol * nb / cur : std::max(kPresInnerFloor, 0.5 * s->tol * nb / cur);
       };
       pres_inner_start_kernel<<<1, 1, 0, s->stream>>>(g, cur, inner_tol());  // Q_0 normalised
       count_launch();
