@@ -472,9 +472,11 @@ class ReferencePrescribed:
         self.nblob = self.refs.size // 3
         pr, ar = _c(phase_refs if len(phase_refs) else [0.0]), _c(angle_refs if len(angle_refs) else [0.0])
         bx, bq = _c(body_x), _c(body_q)
+        scratch = os.path.join(REF_DIR, "scratch")  # the tables' temporary directory
+        os.makedirs(scratch, exist_ok=True)
         rc = self.lib.ref_pres_setup(nfil, nseg, self.nblob, ctypes.c_double(seg_sep),
                                      _ptr(self.refs), _ptr(bx), _ptr(bq), _ptr(pr), len(phase_refs),
-                                     _ptr(ar), len(angle_refs))
+                                     _ptr(ar), len(angle_refs), scratch.encode())
         if rc != 0:
             raise RuntimeError("ref_pres_setup failed")
         self.flags = self.lib.ref_pres_flags()

@@ -561,10 +561,12 @@ static void write_force_refs(const std::string &name, const double *v, int n) {
 // One swimmer of nfil x nseg prescribed filaments and nblob blobs. The
 // generalised-force tables (dynamic phase / shape rotation) are written
 // where mobility_solver::initialise reads them (filament.cpp:2036-2083: a
-// path relative to the working directory, here a fresh temporary one).
+// path relative to the working directory, here a fresh directory made under
+// scratch_dir and removed once they are read).
 int ref_pres_setup(int nfil, int nseg, int nblob, double seg_sep, const double *blob_refs,
                    const double *body_x, const double *body_q, const double *phase_refs,
-                   int n_phase_refs, const double *angle_refs, int n_angle_refs) {
+                   int n_phase_refs, const double *angle_refs, int n_angle_refs,
+                   const char *scratch_dir) {
   NSWIM = 1; NFIL = nfil; NSEG = nseg; NBLOB = nblob;
   SEG_SEP = seg_sep; DL = seg_sep;
   NTOTAL = NSWIM * (NFIL * NSEG + NBLOB);
@@ -572,9 +574,13 @@ int ref_pres_setup(int nfil, int nseg, int nblob, double seg_sep, const double *
   delete g_swimmers;
   g_swimmers = nullptr;
   if (g_solver) { g_solver->finalise(); delete g_solver; g_solver = nullptr; }
-  char dir[] = "/tmp/tfs_pres_XXXXXX";
+  std::string tmpl = std::string(scratch_dir) + "/tfs_pres_XXXXXX";
+  std::vector<char> dir(tmpl.begin(), tmpl.end());
+  dir.push_back('\0');
   char cwd[4096];
-  if (mkdtemp(dir) == nullptr || getcwd(cwd, sizeof cwd) == nullptr || chdir(dir) != 0) return -1;
+  if (mkdtemp(dir.data()) == nullptr || getcwd(cwd, sizeof cwd) == nullptr ||
+      chdir(dir.data()) != 0)
+    return -1;
   mkdir("data", 0755);
   mkdir("data/forcing", 0755);
 #if DYNAMIC_PHASE_EVOLUTION
@@ -585,7 +591,17 @@ int ref_pres_setup(int nfil, int nseg, int nblob, double seg_sep, const double *
 #endif
   g_solver = new emu_rpy_mobility_solver();
   g_solver->initialise();
+  // the tables are read; remove them and the directory
+#if DYNAMIC_PHASE_EVOLUTION
+  unlink(reference_phase_generalised_force_file_name().c_str());
+#endif
+#if DYNAMIC_SHAPE_ROTATION
+  unlink(reference_angle_generalised_force_file_name().c_str());
+#endif
+  rmdir("data/forcing");
+  rmdir("data");
   if (chdir(cwd) != 0) return -1;
+  rmdir(dir.data());
   g_swimmers = new std::vector<swimmer>(1);
   swimmer &s = (*g_swimmers)[0];
   s.f = matrix(6, 1);
