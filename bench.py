@@ -1129,6 +1129,66 @@ def reference_gpu_leg(sw, reps64=3, reps32=10):
     return out
 
 
+def reference_gpu_prescribed_leg(reps64=2, reps32=5):
+    """The reference's own kernels of its prescribed-cilia build on this GPU
+    (oracle/ref_gpu.py, configuration p1: forces only, rpy_interaction<3,3>,
+    Mbs_mult adding): the four products of one application of the
+    prescribed-cilia operator (system_matrix_mult_new's evaluate_full_mobility,
+    mobility_solver.cpp:1829-1840) at the sizes of our arm's prescribed leg
+    (640 beating filaments x 20 segments, 2 562 blobs), launched as its
+    rpy_mobility_solver launches them, CUDA events around each kernel. Only
+    the pair products: the reference's GMRES and its host-device copies per
+    step come on top. None when the cubins were not built here."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_gpu
+    from timfilsimmod_gb300.geometry import prescribed_swimmer
+
+    if not torch.cuda.is_available() or not (ref_gpu.available("fp64", "prescribed")
+                                             and ref_gpu.available("fp32", "prescribed")):
+        return None
+    g = prescribed_swimmer(640, 20, radius=60.0, subdivisions=4, seg_sep=2.6)
+    rng = np.random.default_rng(5)
+    x, _, _ = g.kinematics(rng.uniform(0.0, 2.0 * np.pi, g.nfil), np.zeros(g.nfil))
+    ns, nb = g.nfil * g.nseg, g.blob_references.shape[0]
+    fs = np.zeros((ns, 6))
+    fs[:, :3] = rng.normal(size=(ns, 3))  # the prescribed build reads forces only
+    fb = rng.normal(size=(nb, 3))
+    out = {"kernels": "cuda_functions.cu Mss/Msb/Mbb/Mbs_mult of the prescribed-cilia build "
+                      "(configuration p1), 64 threads per CTA (the reference's launches)",
+           "pairs_per_application": (ns + nb) ** 2}
+    for precision, reps in (("fp64", reps64), ("fp32", reps32)):
+        k = ref_gpu.RefGpuKernels(precision, "prescribed")
+        dt = k.dtype
+        t = {n: torch.tensor(np.asarray(a).ravel(), dtype=dt, device="cuda")
+             for n, a in (("xs", x), ("fs", fs), ("xb", g.blob_references), ("fb", fb))}
+        vs = torch.zeros(6 * ns, dtype=dt, device="cuda")
+        vb = torch.zeros(3 * nb, dtype=dt, device="cuda")
+        k.sync(1, g.nseg, g.nfil, nb)
+        calls = [("Mss", lambda: k.mss(vs, t["fs"], t["xs"])),
+                 ("Msb", lambda: k.msb(vs, t["fb"], t["xs"], t["xb"])),
+                 ("Mbb", lambda: k.mbb(vb, t["fb"], t["xb"])),
+                 ("Mbs", lambda: k.mbs(vb, t["fs"], t["xb"], t["xs"]))]
+        for _, c in calls:  # warm-up
+            c()
+        torch.cuda.synchronize()
+        ms = 0.0
+        for _ in range(reps):
+            for _, c in calls:
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                c()
+                b.record()
+                torch.cuda.synchronize()
+                ms += a.elapsed_time(b)
+        ms /= reps
+        out[precision] = {"ms_per_application": ms, "reps": reps,
+                          "achieved_tflops": 40.0 * (ns + nb) ** 2 / (ms * 1e-3) / 1e12}
+        k.close()
+    return out
+
+
 def bench_reference(args):
     """Reference arm: the reference's RPY sums on the host cores."""
     world, rank, _ = dist_setup()
@@ -1180,6 +1240,9 @@ def bench_reference(args):
     gpu = reference_gpu_leg(sw)
     if gpu is not None:
         line["reference_gpu"] = gpu
+    pres = None if args.no_prescribed else reference_gpu_prescribed_leg()
+    if pres is not None:
+        line["reference_gpu_prescribed"] = pres
     return line
 
 

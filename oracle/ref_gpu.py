@@ -3,7 +3,10 @@
 `make -C oracle ref REF=<reference checkout>` compiles the reference's
 src/cilia/cuda_functions.cu, unchanged, for sm_103a as device code only
 (_ref/ref_kernels_fp64.cubin with Real = double, _ref/ref_kernels_fp32.cubin
-with the shipped Real = float; RPY mobility, elastic filaments, free body).
+with the shipped Real = float; RPY mobility, elastic filaments, free body;
+and _ref/ref_kernels_pres_fp{64,32}.cubin in the prescribed-cilia
+configuration p1, whose kernels take forces only and pair particles with
+rpy_interaction<3,3>).
 This module loads such a cubin through the CUDA driver API (ctypes on
 libcuda; no host code of the reference runs) in the current context, sets
 the kernels' sizes with the reference's own sync_var kernel
@@ -37,18 +40,20 @@ _NAMES = {
 }
 
 
-def cubin_path(precision: str) -> str:
-    return os.path.join(REF_DIR, f"ref_kernels_{precision}.cubin")
+def cubin_path(precision: str, model: str = "elastic") -> str:
+    tag = "pres_" if model == "prescribed" else ""
+    return os.path.join(REF_DIR, f"ref_kernels_{tag}{precision}.cubin")
 
 
-def available(precision: str = "fp64") -> bool:
-    return os.path.exists(cubin_path(precision))
+def available(precision: str = "fp64", model: str = "elastic") -> bool:
+    return os.path.exists(cubin_path(precision, model))
 
 
 class RefGpuKernels:
-    """The reference's four RPY kernels of one precision ("fp64" or "fp32")."""
+    """The reference's four RPY kernels of one precision ("fp64" or "fp32")
+    in the elastic-filament or the prescribed-cilia build."""
 
-    def __init__(self, precision: str = "fp64"):
+    def __init__(self, precision: str = "fp64", model: str = "elastic"):
         import torch
 
         self.precision = precision
@@ -58,7 +63,7 @@ class RefGpuKernels:
         self._chk(self.cu.cuInit(0), "cuInit")
         self.mod = ctypes.c_void_p()
         self._chk(self.cu.cuModuleLoad(ctypes.byref(self.mod),
-                                       cubin_path(precision).encode()), "cuModuleLoad")
+                                       cubin_path(precision, model).encode()), "cuModuleLoad")
         self.fn = {}
         for key, name in _NAMES[precision].items():
             f = ctypes.c_void_p()
