@@ -250,7 +250,7 @@ typedef struct tfs_prescribed_config {
   int flags;                                /* TFS_PRESCRIBED_BODY | ... */
   double gen_force_magnitude_factor;        /* GEN_FORCE_MAGNITUDE_FACTOR (globals) */
   double torsional_spring_magnitude_factor; /* TORSIONAL_SPRING_MAGNITUDE_FACTOR */
-  double fil_length;                        /* FIL_LENGTH = DL (NSEG - 1), config.hpp:515-521 */
+  double fil_length;                        /* FIL_LENGTH = DL (NSEG - 1), config.hpp:515-517 */
 } tfs_prescribed_config;
 /* Defaults: factors 1 and 2 (globals.ini), fil_length = dl (nseg - 1). */
 int tfs_prescribed_config_default(tfs_prescribed_config *pc, int flags, int nseg, double dl);
