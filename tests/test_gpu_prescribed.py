@@ -239,3 +239,29 @@ def test_filaments_without_blobs(flags):
     x_sol, _ = S.solve(b, np.zeros(S.n), tol=1e-10)
     assert rel(sol["f_segs"], x_sol[:3 * g.nfil * g.nseg]) <= 1e-6
     ps.finalise()
+
+
+def test_error_paths():
+    """Calls out of order and missing kinematics fail with the library's
+    status and leave the solver usable: a solve before any kinematics
+    (ESTATE), dynamic shape rotation without d x / d angle (EINVAL), dynamic
+    phase without its table (EINVAL)."""
+    from timfilsimmod_gb300 import _native as N
+    from timfilsimmod_gb300.prescribed import PrescribedCiliaSolver
+    d = load("p1")
+    ps = make(d)
+    with pytest.raises(N.TfsError) as e:
+        ps.solve()
+    assert e.value.code == N.TFS_ESTATE
+    k = kin(d, 0)
+    k["vel_dir_angle"] = None
+    with pytest.raises(N.TfsError) as e:
+        ps.set_kinematics(**k)
+    assert e.value.code == N.TFS_EINVAL
+    ps.set_kinematics(**kin(d, 0))  # still usable
+    assert ps.solve() > 0
+    ps.finalise()
+    with pytest.raises(N.TfsError) as e:
+        PrescribedCiliaSolver(7, int(d["nfil"]), int(d["nseg"]), d["blob_refs"],
+                              float(d["seg_sep"]), None, d["angle_refs"])
+    assert e.value.code == N.TFS_EINVAL
