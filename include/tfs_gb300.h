@@ -167,6 +167,16 @@ int tfs_set_linear_solver(tfs_solver *s, double tol, int max_iter);
  * r = rhs - A x around inner GMRES solves with FP32 blob-blob products, each
  * to inner_tol relative to |r|, at most max_cycles cycles. */
 int tfs_set_refinement(tfs_solver *s, double inner_tol, int max_cycles);
+/* TFS_FP32C only: the Arnoldi vectors of the cooperative inner solves.
+ * TFS_VECTORS_FP32 (the default): FP32 vectors; a refinement that stalls is
+ * run again from the warm start with FP64 ones. TFS_VECTORS_FP64: FP64
+ * vectors for every solve (a few percent fewer Arnoldi steps, each slower:
+ * medium swimmer's implicit steps at DT 0.121, 15.5 against 14.1 ms). The
+ * inner solves of tfs_make_body_reference_matrices take FP64 vectors in
+ * either mode. */
+#define TFS_VECTORS_FP32 0
+#define TFS_VECTORS_FP64 1
+int tfs_set_refinement_vectors(tfs_solver *s, int mode);
 /* FP32C only: run each inner GMRES solve of the refinement as one
  * cooperative kernel (enable = 1, the default where the device supports
  * cooperative launch and the system has at most 64 blobs per SM pair of
@@ -213,7 +223,7 @@ int tfs_copy_blob_forces_to_host_f32(tfs_solver *s, float *f_blobs_host);
 /* Iterations (summed over refinement cycles), refinement cycles and final
  * relative residual of the last solve. FP32C: the cooperative inner solves
  * keep their Arnoldi vectors in FP32 (FP64 during
- * tfs_make_body_reference_matrices). A refinement cycle that does not reduce
+ * tfs_make_body_reference_matrices, or under TFS_VECTORS_FP64). A refinement cycle that does not reduce
  * the FP64 residual ends the refinement; it is run again from the caller's
  * warm start with FP64 Arnoldi vectors, and if that stalls too the solve
  * finishes as plain FP64 GMRES from the warm start; cycles is then negative

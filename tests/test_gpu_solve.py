@@ -198,6 +198,43 @@ def test_persistent_and_kernel_sequence_agree():
         assert rel_max(x, y) < 2e-5
 
 
+def test_refinement_vector_modes_agree():
+    """FP32C Arnoldi vectors in FP32 (the default) and FP64: each mode
+    refines the medium swimmer's solve to the FP64 residual target, and their
+    solutions agree to the FP32 product error. An unknown mode is refused
+    with TFS_EINVAL."""
+    from timfilsimmod_gb300._native import TFS_EINVAL, TfsError
+    from timfilsimmod_gb300.geometry import make_config
+
+    sw = make_config("medium", seed=11)
+    F = sw.f_segs[:, :3].sum(0)
+    T = (np.cross(sw.x_segs, sw.f_segs[:, :3]) + sw.f_segs[:, 3:]).sum(0)
+    out = {}
+    for mode in ("fp32", "fp64"):
+        s = new_solver(sw.nfil, sw.nseg, sw.num_blobs, "fp32c")
+        s.set_refinement_vectors(mode)
+        s.set_blob_references(sw.blob_references)
+        s.set_body_pose([0.0, 0.0, 0.0], [1.0, 0.0, 0.0, 0.0])
+        s.set_linear_solver(1e-8)
+        set_segments(s, sw.x_segs, sw.f_segs)
+        s.make_body_reference_matrices()
+        it, _ = s.compute_velocities(np.concatenate([F, T]))
+        s.copy_segment_velocities_to_host()
+        s.wait_for_device()
+        out[mode] = (it, s.v_segs_host.copy(), s.blob_forces(), s.body_velocities(),
+                     s.solve_info())
+        if mode == "fp32":
+            with pytest.raises(TfsError) as e:
+                s._call("tfs_set_refinement_vectors", 2)
+            assert e.value.code == TFS_EINVAL
+        s.finalise()
+    print({m: (v[0], v[4]) for m, v in out.items()})
+    for mode, v in out.items():
+        assert v[4]["rel_residual"] <= 1e-8 and v[4]["cycles"] > 0, mode
+        for x, y in zip(v[1:4], out["fp32"][1:4]):
+            assert rel_max(x, y) < 2e-5, mode
+
+
 def test_persistent_large_slices_agree():
     """10 242 blobs (the large swimmer's body, R = 150) with 64 filaments: 68
     blobs per cooperative CTA on 152 SMs, beyond the 64 of the smaller

@@ -132,6 +132,7 @@ _SIGNATURES = {
     "tfs_set_body_pose": [_H, _P, _P],
     "tfs_set_linear_solver": [_H, ctypes.c_double, ctypes.c_int],
     "tfs_set_refinement": [_H, ctypes.c_double, ctypes.c_int],
+    "tfs_set_refinement_vectors": [_H, ctypes.c_int],
     "tfs_set_persistent_gmres": [_H, ctypes.c_int],
     "tfs_inject_barrier_stall": [_H, ctypes.c_int],
     "tfs_make_body_reference_matrices": [_H],

@@ -687,7 +687,7 @@ int linear_solve(tfs_solver *s, int *iters, bool first_ready = false) {
   int total = 0, cycles = 0;
   GmresScalars h{};
   bool stalled = false;
-  int vec64 = s->bootstrap ? 1 : 0;
+  int vec64 = (s->bootstrap || s->vec_mode == TFS_VECTORS_FP64) ? 1 : 0;
   if ((!first_ready && (rc = refine_start(s, s->stream)) != TFS_OK) ||
       (rc = refine_cycles(s, g64, vec64, first_ready, &total, &cycles, &h, &stalled)) != TFS_OK)
     return rc;
@@ -889,6 +889,14 @@ int tfs_set_refinement(tfs_solver *s, double inner_tol, int max_cycles) {
     return fail(TFS_EINVAL, "inner_tol in (0, 1), max_cycles >= 1");
   s->inner_tol = inner_tol;
   s->max_outer = max_cycles;
+  return TFS_OK;
+}
+
+int tfs_set_refinement_vectors(tfs_solver *s, int mode) {
+  TFS_CHECK_SOLVER(s);
+  if (mode != TFS_VECTORS_FP32 && mode != TFS_VECTORS_FP64)
+    return fail(TFS_EINVAL, "mode is TFS_VECTORS_FP32 or TFS_VECTORS_FP64");
+  s->vec_mode = mode;
   return TFS_OK;
 }
 

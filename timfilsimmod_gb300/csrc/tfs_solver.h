@@ -60,6 +60,8 @@ struct tfs_solver {
   double *ff_scratch = nullptr;
   size_t ff_scratch_elems = 0;
   long long vec64_retries = 0;  // FP32C refinements rerun with FP64 Arnoldi vectors
+  // FP32C: Arnoldi vectors of the cooperative inner solves (TFS_VECTORS_*)
+  int vec_mode = 0;
   int max_outer = 12;        // FP32C: refinement cycles
   int chunk = 8;             // Arnoldi steps launched between polls of the done flag
   bool have_refs = false;

@@ -276,6 +276,15 @@ class RpyMobilitySolver:
     def set_refinement(self, inner_tol: float = 1e-4, max_cycles: int = 12) -> None:
         self._call("tfs_set_refinement", float(inner_tol), int(max_cycles))
 
+    def set_refinement_vectors(self, mode: str = "fp32") -> None:
+        """FP32C: Arnoldi vectors of the cooperative inner solves. "fp32"
+        (default; a refinement that stalls is rerun with FP64 vectors) or
+        "fp64" (every solve)."""
+        modes = {"fp32": 0, "fp64": 1}
+        if mode not in modes:
+            raise ValueError(f"mode is one of {sorted(modes)}")
+        self._call("tfs_set_refinement_vectors", modes[mode])
+
     def set_persistent_gmres(self, enable: bool = True) -> None:
         """FP32C inner GMRES as one cooperative kernel (default) or as a
         sequence of kernels per Arnoldi step."""

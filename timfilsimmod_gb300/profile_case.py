@@ -54,19 +54,34 @@ def run_steps(sw, args):
                           end_force_magnitude=int(efm))
     s.set_blob_references(sw.blob_references)
     s.set_linear_solver(1e-8)
+    if args.precision == "fp32c":
+        s.set_refinement_vectors(args.vectors)
     st = ImplicitStepper(s, sw.nfil, sw.nseg, fil_refs, normals, seg_sep=sw.seg_sep, dt=args.dt,
                          tol=1e-4, end_force_magnitude=efm, body_radius=sw.radius)
     t0 = time.perf_counter()
     from .mobility import kernel_launch_count
 
+    ms, gm = [], []
     for nt in range(args.reps):
         # the launch index where step nt begins (ncu -s skips the ones before)
         print(f"kernel launches before step {nt}: {kernel_launch_count()}")
+        r0 = s.refinement_retries() if args.precision == "fp32c" else 0
+        t1 = time.perf_counter()
         b, g = st.step(nt, allow_unconverged=True)
-        print(f"step {nt}: {b} Broyden iterations, {g} GMRES iterations")
+        s.wait_for_device()
+        ms.append((time.perf_counter() - t1) * 1e3)
+        gm.append(g)
+        r = (s.refinement_retries() - r0) if args.precision == "fp32c" else 0
+        print(f"step {nt}: {b} Broyden iterations, {g} GMRES iterations, "
+              f"{r} FP64-vector retries, {ms[-1]:.2f} ms")
     s.wait_for_device()
     dt = time.perf_counter() - t0
     print(f"{args.reps} steps ({args.precision}, {args.config}): {dt * 1e3:.2f} ms")
+    if args.reps > 4:
+        import numpy as np
+
+        print(f"steps 4..{args.reps - 1} ({args.vectors} vectors): median {np.median(ms[4:]):.2f} ms, "
+              f"mean {np.mean(ms[4:]):.2f} ms, {np.mean(gm[4:]):.1f} GMRES iterations per step")
     if args.pg_trace:
         print_pg_trace()
     st.close()
@@ -139,6 +154,8 @@ def main():
     p.add_argument("--waves", type=int, default=1)
     p.add_argument("--queue-variant", type=int, default=None,
                    help="pin every work-queue product kind to this variant")
+    p.add_argument("--vectors", default="fp32", choices=["fp32", "fp64"],
+                   help="Arnoldi vectors of the FP32C inner solves (op step)")
     p.add_argument("--autotune", action="store_true", help="print the autotuner's table")
     p.add_argument("--pg-trace", action="store_true",
                    help="print the phase table of the last cooperative GMRES solve (ops solve, "
