@@ -50,6 +50,10 @@ namespace {
 constexpr double kPiP = 3.14159265358979323846264338327950288;
 constexpr int kPT = 128;         // threads per CTA of the O(N) kernels
 constexpr int kPW = kPT / 32;    // warps per CTA
+// threads per CTA of the GMRES vector kernels (one CTA per SM at the medium
+// swimmer's sizes: eight warps to cover the L2 latency of their row loads)
+constexpr int kGT = 256;
+constexpr int kGW = kGT / 32;
 constexpr int kFilC = 16;        // per-filament constants (below)
 constexpr int kPresMaxIter = 350;  // MAX_LINEAR_SYSTEM_ITER (config.hpp:312)
 constexpr int kPresChunk = 4;      // Arnoldi steps launched between polls of the done flag
@@ -148,12 +152,93 @@ __device__ __forceinline__ double pw_sum(double v) {
   return v;
 }
 
-// Sum over c < n of p[c * stride] by one warp (lanes stride the terms, then
-// a fixed shuffle tree): every lane gets the same bits.
+// Sum over c < n of p[c * stride] by one warp: lane l adds the terms c = l,
+// l + 32, l + 64, ... in that order, then a fixed shuffle tree, so every lane
+// gets the same bits. The terms are loaded eight per lane at a time: one L2
+// round trip covers 256 of them.
 __device__ __forceinline__ double pw_sum_strided(const double *p, int n, size_t stride) {
+  const int lane = threadIdx.x & 31;
   double t = 0.0;
-  for (int c = threadIdx.x & 31; c < n; c += 32) t += __ldcg(p + (size_t)c * stride);
+  for (int c0 = 0; c0 < n; c0 += 256) {
+    double v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int c = c0 + lane + 32 * j;
+      v[j] = c < n ? __ldcg(p + (size_t)c * stride) : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (c0 + lane + 32 * j < n) t += v[j];
+  }
   return pw_sum(t);
+}
+
+// Warp sums of eight values a lane by a reduce-scatter butterfly: at each of
+// the first three levels a lane keeps half of its columns and adds its
+// partner's half of them, then two plain levels; 9 FP64 adds a lane instead
+// of the 40 of eight shuffle trees (the FP64 pipe bounds these kernels on
+// this part). Lanes 4c .. 4c+3 return the same bits: column c's sum.
+__device__ __forceinline__ double pw_sum8(const double v[8]) {
+  const int lane = threadIdx.x & 31;
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  double w[4], x[2];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const double keep = b4 ? v[4 + j] : v[j], send = b4 ? v[j] : v[4 + j];
+    w[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const double keep = b3 ? w[2 + j] : w[j], send = b3 ? w[j] : w[2 + j];
+    x[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+  double y = (b2 ? x[1] : x[0]) + __shfl_xor_sync(0xffffffffu, b2 ? x[0] : x[1], 4);
+  y += __shfl_xor_sync(0xffffffffu, y, 2);
+  y += __shfl_xor_sync(0xffffffffu, y, 1);
+  return y;
+}
+
+// The same for four values a lane (6 adds instead of 20): lanes 8c .. 8c+7
+// return column c's sum.
+__device__ __forceinline__ double pw_sum4(const double v[4]) {
+  const int lane = threadIdx.x & 31;
+  const bool b4 = lane & 16, b3 = lane & 8;
+  double w[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const double keep = b4 ? v[2 + j] : v[j], send = b4 ? v[j] : v[2 + j];
+    w[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+  double y = (b3 ? w[1] : w[0]) + __shfl_xor_sync(0xffffffffu, b3 ? w[0] : w[1], 8);
+  y += __shfl_xor_sync(0xffffffffu, y, 4);
+  y += __shfl_xor_sync(0xffffffffu, y, 2);
+  y += __shfl_xor_sync(0xffffffffu, y, 1);
+  return y;
+}
+
+// Four adjacent columns at once: the sum over c < n of p[c * stride + j] for
+// j < m (m <= 4), lane l adding the terms c = l, l + 32, ... in that order,
+// then pw_sum4 (lanes 8j .. 8j+7 return column j's sum), with the loads of
+// all four columns for 128 terms in flight together.
+__device__ __forceinline__ double pw_sum_strided4(const double *p, int n, size_t stride, int m) {
+  const int lane = threadIdx.x & 31;
+  double t[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int c0 = 0; c0 < n; c0 += 128) {
+    double v[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int c = c0 + lane + 32 * a;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        v[a][j] = (c < n && j < m) ? __ldcg(p + (size_t)c * stride + j) : 0.0;
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+      if (c0 + lane + 32 * a < n)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) t[j] += v[a][j];
+  }
+  return pw_sum4(t);
 }
 
 // True in exactly one CTA, the last to arrive after writing its partials
@@ -838,18 +923,18 @@ struct GA {
 };
 
 // ||v|| into *out (the last CTA), v of n rows.
-__global__ void __launch_bounds__(kPT) pres_norm_kernel(GA g, const double *v, double *out) {
+__global__ void __launch_bounds__(kGT) pres_norm_kernel(GA g, const double *v, double *out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int r0 = blockIdx.x * g.rows, r1 = min(g.n, r0 + g.rows);
   double t = 0.0;
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) t += v[r] * v[r];
-  __shared__ double red[kPW];
+  __shared__ double red[kGW];
   t = pw_sum(t);
   if (lane == 0) red[wid] = t;
   __syncthreads();
   if (threadIdx.x == 0) {
     double u = 0.0;
-    for (int w = 0; w < kPW; ++w) u += red[w];
+    for (int w = 0; w < kGW; ++w) u += red[w];
     g.part[(size_t)blockIdx.x * g.pstride] = u;
   }
   if (!pres_last_cta(g.cnt)) return;
@@ -902,68 +987,90 @@ __global__ void pres_q0_kernel(GA g, const double *rhs, double *x) {
 
 // Dots <w, Q_i>, i < k, over this CTA's rows into part[cta][i]: columns in
 // blocks of 8, every thread accumulating its rows' products for the 8 at once
-// (coalesced row loads, eight in flight per row), block sums per column; the
-// last CTA sums the partials in CTA order into h.
+// (coalesced row loads; two rows a thread at a time, sixteen loads in
+// flight, each row's products added in row order), block sums per column;
+// the last CTA sums the partials in CTA order into h, four columns a warp at
+// a time.
 __device__ void pres_dots(const GA &g, const double *w, int k, double *h) {
-  __shared__ double red[kPW][8];
+  __shared__ double red[kGW][8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int r0 = blockIdx.x * g.rows, r1 = min(g.n, r0 + g.rows);
+  const int bd = blockDim.x;
   for (int i0 = 0; i0 < k; i0 += 8) {
     const int nc = min(8, k - i0);
     double acc[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[j] = 0.0;
-    for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-      const double wr = w[r];
+    for (int r = r0 + threadIdx.x; r < r1; r += 2 * bd) {
+      const bool two = r + bd < r1;
+      const double wr = w[r], wr2 = two ? w[r + bd] : 0.0;
       const double *q = g.Q + (size_t)i0 * g.n + r;
+      double a[8], b[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        a[j] = j < nc ? q[(size_t)j * g.n] : 0.0;
+        b[j] = (j < nc && two) ? q[(size_t)j * g.n + bd] : 0.0;
+      }
 #pragma unroll
       for (int j = 0; j < 8; ++j)
-        if (j < nc) acc[j] += q[(size_t)j * g.n] * wr;
+        if (j < nc) acc[j] += a[j] * wr;
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (j < nc && two) acc[j] += b[j] * wr2;
     }
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc[j] = pw_sum(acc[j]);
-    if (lane == 0)
-#pragma unroll
-      for (int j = 0; j < 8; ++j) red[wid][j] = acc[j];
+    const double sc = pw_sum8(acc);
+    if ((lane & 3) == 0) red[wid][lane >> 2] = sc;
     __syncthreads();
     if ((int)threadIdx.x < nc) {
       double t = 0.0;
-      for (int q = 0; q < kPW; ++q) t += red[q][threadIdx.x];
+      for (int q = 0; q < kGW; ++q) t += red[q][threadIdx.x];
       g.part[(size_t)blockIdx.x * g.pstride + i0 + threadIdx.x] = t;
     }
     __syncthreads();
   }
   if (!pres_last_cta(g.cnt)) return;
-  for (int i = wid; i < k; i += kPW) {
-    const double t = pw_sum_strided(g.part + i, g.G, g.pstride);
-    if (lane == 0) h[i] = t;
+  for (int i0 = 4 * wid; i0 < k; i0 += 4 * kGW) {
+    const int m = min(4, k - i0);
+    const double t = pw_sum_strided4(g.part + i0, g.G, g.pstride, m);
+    if ((lane & 7) == 0 && (lane >> 3) < m) h[i0 + (lane >> 3)] = t;
   }
   __syncthreads();
   if (threadIdx.x == 0) *g.cnt = 0u;
 }
 
 // w -= sum_i h_i Q_i over this CTA's rows (h staged in shared memory; the
-// columns of a row subtracted in order, four loads in flight).
+// columns of a row subtracted in order; two rows a thread at a time, sixteen
+// loads in flight).
 __device__ void pres_orth(const GA &g, double *w, int k, const double *h) {
   __shared__ double hs[kPresMaxIter];
   for (int i = threadIdx.x; i < k; i += blockDim.x) hs[i] = h[i];
   __syncthreads();
   const int r0 = blockIdx.x * g.rows, r1 = min(g.n, r0 + g.rows);
+  const int bd = blockDim.x;
   const size_t n = g.n;
-  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-    double t = w[r];
+  for (int r = r0 + threadIdx.x; r < r1; r += 2 * bd) {
+    const bool two = r + bd < r1;
+    double t = w[r], u = two ? w[r + bd] : 0.0;
     const double *q = g.Q + r;
     int i = 0;
-    for (; i + 4 <= k; i += 4) {
-      const double a0 = q[(size_t)i * n], a1 = q[(size_t)(i + 1) * n];
-      const double a2 = q[(size_t)(i + 2) * n], a3 = q[(size_t)(i + 3) * n];
-      t -= hs[i] * a0;
-      t -= hs[i + 1] * a1;
-      t -= hs[i + 2] * a2;
-      t -= hs[i + 3] * a3;
+    for (; i + 8 <= k; i += 8) {
+      double a[8], b[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        a[j] = q[(size_t)(i + j) * n];
+        b[j] = two ? q[(size_t)(i + j) * n + bd] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) t -= hs[i + j] * a[j];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) u -= hs[i + j] * b[j];
     }
-    for (; i < k; ++i) t -= hs[i] * q[(size_t)i * n];
+    for (; i < k; ++i) {
+      t -= hs[i] * q[(size_t)i * n];
+      if (two) u -= hs[i] * q[(size_t)i * n + bd];
+    }
     w[r] = t;
+    if (two) w[r + bd] = u;
   }
   __syncthreads();
 }
@@ -971,14 +1078,14 @@ __device__ void pres_orth(const GA &g, double *w, int k, const double *h) {
 // Step k = st->iter, pass 1: h1 = Q^T w. (The step kernels read k from the
 // device scalars and skip once the solve is finished, so a chunk of steps
 // is the same launch sequence every time.)
-__global__ void __launch_bounds__(kPT) pres_dots1_kernel(GA g) {
+__global__ void __launch_bounds__(kGT) pres_dots1_kernel(GA g) {
   if (g.st->done) return;
   const int k = g.st->iter;
   pres_dots(g, g.Q + (size_t)k * g.n, k, g.h1);
 }
 
 // Step k, pass 2: w -= Q h1, h2 = Q^T w.
-__global__ void __launch_bounds__(kPT) pres_dots2_kernel(GA g) {
+__global__ void __launch_bounds__(kGT) pres_dots2_kernel(GA g) {
   if (g.st->done) return;
   const int k = g.st->iter;
   double *w = g.Q + (size_t)k * g.n;
@@ -989,9 +1096,11 @@ __global__ void __launch_bounds__(kPT) pres_dots2_kernel(GA g) {
 // Step k: w -= Q h2, ||w||; the last CTA writes H(:, k-1), applies the
 // earlier Givens rotations and the new one (mobility_solver.cpp:2370-2404),
 // tests convergence (:2409-2413) and, when finishing, back-solves y (:2419-
-// 2438) with warp-parallel inner sums.
-__global__ void __launch_bounds__(kPT) pres_norm_givens_kernel(GA g) {
-  __shared__ double red[kPW];
+// 2438) with warp-parallel inner sums. The column and the rotations are
+// staged in shared memory for the serial rotation chain.
+__global__ void __launch_bounds__(kGT) pres_norm_givens_kernel(GA g) {
+  __shared__ double red[kGW];
+  __shared__ double hc[kPresMaxIter + 1], css[kPresMaxIter], sns[kPresMaxIter];
   __shared__ int fin;
   if (g.st->done) return;
   const int k = g.st->iter;
@@ -1006,27 +1115,34 @@ __global__ void __launch_bounds__(kPT) pres_norm_givens_kernel(GA g) {
   __syncthreads();
   if (threadIdx.x == 0) {
     double u = 0.0;
-    for (int q = 0; q < kPW; ++q) u += red[q];
+    for (int q = 0; q < kGW; ++q) u += red[q];
     g.part[(size_t)blockIdx.x * g.pstride] = u;
   }
   if (!pres_last_cta(g.cnt)) return;
+  const int ld = g.ld, c = k - 1;
+  double *H = g.H;
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    hc[i] = g.h1[i] + g.h2[i];
+    if (i < c) {
+      css[i] = g.cs[i];
+      sns[i] = g.sn[i];
+    }
+  }
   double ss = 0.0;
   if (wid == 0) ss = pw_sum_strided(g.part, g.G, g.pstride);
+  __syncthreads();
   PresScalars *st = g.st;
   if (threadIdx.x == 0) {
-    const int ld = g.ld, c = k - 1;
-    double *H = g.H;
-    for (int i = 0; i < k; ++i) H[i + (size_t)c * ld] = g.h1[i] + g.h2[i];
     const double qn = sqrt(ss);
     st->qnorm = qn;
-    H[k + (size_t)c * ld] = qn;
+    hc[k] = qn;
     for (int i = 1; i < k; ++i) {
-      const double a0 = H[i - 1 + (size_t)c * ld], a1 = H[i + (size_t)c * ld];
-      const double tt = g.cs[i - 1] * a0 + g.sn[i - 1] * a1;
-      H[i + (size_t)c * ld] = g.cs[i - 1] * a1 - g.sn[i - 1] * a0;
-      H[i - 1 + (size_t)c * ld] = tt;
+      const double a0 = hc[i - 1], a1 = hc[i];
+      const double tt = css[i - 1] * a0 + sns[i - 1] * a1;
+      hc[i] = css[i - 1] * a1 - sns[i - 1] * a0;
+      hc[i - 1] = tt;
     }
-    const double hk = H[k + (size_t)c * ld], hd = H[c + (size_t)c * ld];
+    const double hk = hc[k], hd = hc[c];
     double cs, sn;
     if (hk == 0.0) {
       cs = 1.0;
@@ -1042,8 +1158,8 @@ __global__ void __launch_bounds__(kPT) pres_norm_givens_kernel(GA g) {
     }
     g.cs[c] = cs;
     g.sn[c] = sn;
-    H[c + (size_t)c * ld] = cs * hd + sn * hk;
-    H[k + (size_t)c * ld] = 0.0;
+    hc[c] = cs * hd + sn * hk;
+    hc[k] = 0.0;
     g.beta[k] = -sn * g.beta[c];
     g.beta[c] = cs * g.beta[c];
     const double rel = fabs(g.beta[k]) / st->norm_rhs;
@@ -1057,9 +1173,10 @@ __global__ void __launch_bounds__(kPT) pres_norm_givens_kernel(GA g) {
     *g.cnt = 0u;
   }
   __syncthreads();
+  for (int i = threadIdx.x; i <= k; i += blockDim.x) H[i + (size_t)c * ld] = hc[i];
+  __syncthreads();
   if (!fin || wid != 0) return;
   // y(k-1) = beta / H, then upward: y(i) = (beta(i) - sum_{j>i} H(i,j) y(j)) / H(i,i)
-  const int ld = g.ld;
   for (int i = k - 1; i >= 0; --i) {
     double sacc = 0.0;
     for (int j = i + 1 + lane; j < k; j += 32) sacc += g.H[i + (size_t)j * ld] * g.y[j];
@@ -1216,9 +1333,12 @@ int pres_alloc(tfs_solver *s) {
   PresState *p = s->pres;
   const size_t n = p->n, ns = p->ns, nb = p->nb, nf = p->nfil;
   const int ld = kPresMaxIter + 1;
-  // GMRES vector kernels: CTAs of 256 consecutive rows (two per thread), at
-  // most eight per SM
-  p->G = (int)std::max<size_t>(1, std::min<size_t>((size_t)8 * num_sms(), (n + 255) / 256));
+  // GMRES vector kernels: CTAs of at least 256 consecutive rows; up to one
+  // per SM as the rows allow, beyond that a multiple of the SM count (at most
+  // eight per SM). Each SM's FP64 pipe bounds these kernels on this part, so
+  // every SM gets the same share of the rows.
+  const size_t sms = (size_t)num_sms(), g0 = (n + 255) / 256;
+  p->G = (int)std::max<size_t>(1, g0 <= sms ? g0 : std::min<size_t>(8 * sms, g0 / sms * sms));
   p->rows = (int)((n + p->G - 1) / p->G);
   p->pstride = kPresMaxIter + 2;
   const size_t warps = nf + (nb + 31) / 32;
@@ -1451,10 +1571,10 @@ int pres_chunk(tfs_solver *s, int fp32) {
   for (int c = 0; c < kPresChunk; ++c) {
     if ((rc = pres_precond(s, p->Q, p->z, p->st)) != TFS_OK) return rc;
     if ((rc = pres_operator(s, fp32, p->z, nullptr, p->Q, p->st)) != TFS_OK) return rc;
-    pres_dots1_kernel<<<g.G, kPT, 0, s->stream>>>(g);
-    pres_dots2_kernel<<<g.G, kPT, 0, s->stream>>>(g);
-    pres_norm_givens_kernel<<<g.G, kPT, 0, s->stream>>>(g);
-    pres_scale_kernel<<<g.G, kPT, 0, s->stream>>>(g);
+    pres_dots1_kernel<<<g.G, kGT, 0, s->stream>>>(g);
+    pres_dots2_kernel<<<g.G, kGT, 0, s->stream>>>(g);
+    pres_norm_givens_kernel<<<g.G, kGT, 0, s->stream>>>(g);
+    pres_scale_kernel<<<g.G, kGT, 0, s->stream>>>(g);
     count_launch_n(4);
     TFS_CUDA(cudaGetLastError(), "prescribed Arnoldi step");
   }
@@ -1531,10 +1651,10 @@ int pres_arnoldi(tfs_solver *s, int fp32, int *iters) {
   }
   if (!p->st_host->done) return fail(TFS_ENOTCONV, "GMRES did not finish within %d steps", p->max_iter);
   *iters = p->st_host->iters;
-  pres_qy_kernel<<<g.G, kPT, 0, s->stream>>>(g, *iters, p->tmp);
+  pres_qy_kernel<<<g.G, kGT, 0, s->stream>>>(g, *iters, p->tmp);
   count_launch();
   if ((rc = pres_precond(s, p->tmp, p->z)) != TFS_OK) return rc;
-  pres_axpy_kernel<<<g.G, kPT, 0, s->stream>>>(p->x, p->z, p->n);
+  pres_axpy_kernel<<<g.G, kGT, 0, s->stream>>>(p->x, p->z, p->n);
   count_launch();
   TFS_CUDA(cudaGetLastError(), "prescribed GMRES finish");
   return TFS_OK;
@@ -1577,7 +1697,7 @@ int pres_residual(tfs_solver *s, double *norm) {
   if ((rc = ff ? pres_operator_ff(s, p->x, p->b, p->Q) : pres_operator(s, 0, p->x, p->b, p->Q)) !=
       TFS_OK)
     return rc;
-  pres_norm_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->Q, &p->st->beta0);
+  pres_norm_kernel<<<g.G, kGT, 0, s->stream>>>(g, p->Q, &p->st->beta0);
   count_launch();
   TFS_CUDA(cudaGetLastError(), "prescribed residual");
   if ((rc = pres_read_scalars(s, "prescribed residual")) != TFS_OK) return rc;
@@ -1609,14 +1729,14 @@ int pres_solve(tfs_solver *s, int *iters_out) {
   if ((rc = pres_rhs(s)) != TFS_OK) return rc;
   // ||rhs||; r0 = rhs - A x0 into Q_0 (FP64); beta0 = ||r0||; the warm-start
   // tests (mobility_solver.cpp:2121-2320)
-  pres_norm_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->b, &p->st->norm_rhs);
+  pres_norm_kernel<<<g.G, kGT, 0, s->stream>>>(g, p->b, &p->st->norm_rhs);
   count_launch();
   rc = fp32 && p->use_ff ? pres_operator_ff(s, p->x, p->b, p->Q)
                          : pres_operator(s, 0, p->x, p->b, p->Q);
   if (rc != TFS_OK) return rc;
-  pres_norm_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->Q, &p->st->beta0);
+  pres_norm_kernel<<<g.G, kGT, 0, s->stream>>>(g, p->Q, &p->st->beta0);
   pres_start_kernel<<<1, 1, 0, s->stream>>>(g, s->tol);
-  pres_q0_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->b, p->x);
+  pres_q0_kernel<<<g.G, kGT, 0, s->stream>>>(g, p->b, p->x);
   count_launch_n(3);
   TFS_CUDA(cudaGetLastError(), "prescribed GMRES start");
   if ((rc = pres_read_scalars(s, "prescribed GMRES start")) != TFS_OK) return rc;
@@ -1658,7 +1778,7 @@ int pres_solve(tfs_solver *s, int *iters_out) {
         }
         cur = nr;
         pres_inner_start_kernel<<<1, 1, 0, s->stream>>>(g, cur, inner_tol());
-        pres_q0_kernel<<<g.G, kPT, 0, s->stream>>>(g, p->b, p->x);
+        pres_q0_kernel<<<g.G, kGT, 0, s->stream>>>(g, p->b, p->x);
         count_launch_n(2);
         TFS_CUDA(cudaGetLastError(), "prescribed refinement restart");
       }

@@ -93,6 +93,8 @@ def run_prescribed(args):
     20 segments on the 2562-blob sphere (dynamic phase and shape rotation,
     zero prescribed body velocities, RPY mobility, linear residual 1e-8):
     one warm-up solve, then --reps warm-started solves."""
+    import hashlib
+
     import numpy as np
 
     from .geometry import prescribed_swimmer
@@ -118,6 +120,11 @@ def run_prescribed(args):
         info = ps.solve_info()
         print(f"solve {nt}: {it} GMRES steps, {info['cycles']} cycles, residual "
               f"{info['rel_residual']:.2e}, {dts[-1] * 1e3:.1f} ms")
+    # the bits of the last solution, for comparing two builds
+    sol = ps.solution()
+    digest = hashlib.sha256(b"".join(np.ascontiguousarray(sol[k]).tobytes()
+                                     for k in sorted(sol))).hexdigest()[:16]
+    print(f"solution digest: {digest}")
     ps.finalise()
 
 
