@@ -989,8 +989,8 @@ __global__ void pres_q0_kernel(GA g, const double *rhs, double *x) {
 // blocks of 8, every thread accumulating its rows' products for the 8 at once
 // (coalesced row loads; two rows a thread at a time, sixteen loads in
 // flight, each row's products added in row order), block sums per column;
-// the last CTA sums the partials in CTA order into h, four columns a warp at
-// a time.
+// the last CTA sums the partials in a fixed order into h, four columns a warp
+// at a time.
 __device__ void pres_dots(const GA &g, const double *w, int k, double *h) {
   __shared__ double red[kGW][8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
