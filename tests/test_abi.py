@@ -65,6 +65,7 @@ def test_last_error_and_argument_checks_without_gpu():
     assert lib.tfs_solver_create(ctypes.byref(bad), ctypes.byref(h)) == N.TFS_EINVAL
     assert lib.tfs_evaluate_segment_segment_mobility(None) == N.TFS_EINVAL
     assert lib.tfs_wait_for_device(None) == N.TFS_EINVAL
+    assert lib.tfs_set_refinement_vectors(None, 0) == N.TFS_EINVAL
 
 
 def test_stepper_argument_checks_without_gpu():
